@@ -1,0 +1,392 @@
+"""Headline benchmark: 257^3 Poisson solves/s of the matrix-diagonalisation
+solver, split-BF16 tensor-core transforms + FP64 iterative refinement to
+<= 1e-10 relative error, next to the plain FP64 GPU path.
+
+Workload (one step = one solve): 257 x 257 x 257 nodes on [0,1]^3, uniform
+in x and z, tanh(2.0)-stretched in y, 6th-order compact scheme, Dirichlet
+(zero) boundaries, sigma = 0.  The right-hand side is a seeded (seed 5)
+zero-mean Gaussian random field with a k^(-5/3) spectrum (FFT filter).
+Inputs are synthetic: the reference publishes no dataset.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Under torchrun (N > 1) every rank solves its own copy (the path has no data
+exchange; replicas only) and value = total solves/s over all ranks.
+``--impl reference`` times the CPU restatement of the reference algorithm
+(oracle/, NumPy + OpenBLAS on all host cores): the Fortran reference needs a
+Fortran compiler, MPI and PETSc, none of which exist on this system.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "mflops3d-md_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "257^3 Poisson solves/s: split-precision+refinement vs FP64 plain @1e-10 rel err"
+UNIT = "solves/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--nodes", type=int, default=257)
+    ap.add_argument("--cpu-sample", type=int, default=2, help="oracle solves timed for cpu_baseline")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+# workload
+# ---------------------------------------------------------------------------
+
+def workload(nodes):
+    from oracle import mesh
+    gx = mesh.uniform_grid(nodes)
+    gy = mesh.tanh_grid(nodes, 2.0)
+    gz = mesh.uniform_grid(nodes)
+    n = nodes - 2
+    rng = np.random.default_rng(5)
+    white = rng.standard_normal((n, n, n))
+    spec = np.fft.rfftn(white)
+    kx = np.fft.fftfreq(n)[:, None, None]
+    ky = np.fft.fftfreq(n)[None, :, None]
+    kz = np.fft.rfftfreq(n)[None, None, :]
+    k = np.sqrt(kx ** 2 + ky ** 2 + kz ** 2)
+    k[0, 0, 0] = 1.0
+    spec *= k ** (-5.0 / 6.0)  # amplitude ~ k^(-5/6) -> energy spectrum ~ k^(-5/3)
+    spec[0, 0, 0] = 0.0
+    rhs = np.fft.irfftn(spec, s=(n, n, n), axes=(0, 1, 2))
+    rhs = np.asfortranarray(rhs / np.std(rhs))
+    bcx = np.zeros((n, n, 2), order="F")
+    return (gx, gy, gz), rhs, (bcx, bcx.copy(), bcx.copy())
+
+
+def cpu_oracle_solve(grids, rhs, bcs):
+    from oracle import solver as S
+    sc = S.Solver3D(*grids, (1,) * 6, 6)
+    n1, n2, n3 = rhs.shape
+    solf = np.zeros((n1 + 2, n2 + 2, n3 + 2))
+    t0 = time.perf_counter()
+    out = S.solve_3d(sc, rhs, 0.0, solf, *bcs)
+    return out, time.perf_counter() - t0, sc
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            p = json.load(f)
+        return p["hbm_gbs"], p["bf16_tflops"], "measured"
+    except Exception:
+        return 6800.0, 1900.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(index), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.file,
+                stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.file.flush()
+        self.file.seek(0)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.file.read().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.file.name)
+        busy = [s for s in sm if smax and s > 0.5 * smax] or sm
+        return {"sm_mhz": statistics.median(busy) if busy else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# reference arm: CPU restatement of the reference algorithm
+# ---------------------------------------------------------------------------
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    grids, rhs, bcs = workload(args.nodes)
+    from oracle import solver as S
+    sc = S.Solver3D(*grids, (1,) * 6, 6)
+    n1, n2, n3 = rhs.shape
+    solf = np.zeros((n1 + 2, n2 + 2, n3 + 2))
+    for _ in range(args.warmup):
+        S.solve_3d(sc, rhs, 0.0, solf, *bcs)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        S.solve_3d(sc, rhs, 0.0, solf, *bcs)
+    dt = time.perf_counter() - t0
+    v = args.steps / dt
+    cores = os.cpu_count()
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": "poisson_257cube_tanh2y_dirichlet_so6", "nodes": args.nodes,
+                       "path": "plain FP64 matrix diagonalisation (oracle restatement, NumPy/OpenBLAS)"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": "%d full 257^3 solves" % args.steps},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "Fortran reference unbuildable here (no Fortran compiler/MPI/PETSc): timed the "
+                    "oracle restatement of class_solver_3d.f90:83-299 on %d host threads" % cores}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GB300 arm
+# ---------------------------------------------------------------------------
+
+def run_gb300(args, rank, world, dist):
+    import torch
+    import mflops_gb300 as mf
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev_stream = torch.cuda.current_stream()
+    grids, rhs, bcs = workload(args.nodes)
+    n = args.nodes - 2
+    sc = mf.SolverCoeffs3D(*grids, (1,) * 6, 6)
+    d_rhs = mf.to_device(rhs)
+    d_bc = [mf.to_device(b) for b in bcs]
+    d_solf = mf.empty_device((n + 2, n + 2, n + 2))
+    d_ref = mf.empty_device((n + 2, n + 2, n + 2))
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    # plain FP64 GPU reference solve (drop-in path) and its rate
+    sc.solve_3d(d_rhs, 0.0, d_ref, *d_bc)
+    torch.cuda.synchronize()
+    plain_ms = []
+    for _ in range(2):
+        flush.fill_(1.0)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        sc.solve_3d(d_rhs, 0.0, d_ref, *d_bc)
+        b.record()
+        torch.cuda.synchronize()
+        plain_ms.append(a.elapsed_time(b))
+    ref_interior = d_ref[1:-1, 1:-1, 1:-1]
+    ref_norm = torch.linalg.vector_norm(ref_interior).item()
+
+    def mixed(refine):
+        sc.solve_3d(d_rhs, 0.0, d_solf, *d_bc, precision=mf.MF_PREC_SPLIT_BF16, refine=refine)
+
+    def err_vs_plain():
+        return (torch.linalg.vector_norm(d_solf[1:-1, 1:-1, 1:-1] - ref_interior) / ref_norm).item()
+
+    # smallest refinement count that reaches 1e-10 against the FP64 solution
+    errs = {}
+    refine = None
+    for r in (0, 1, 2, 3, 4):
+        mixed(r)
+        torch.cuda.synchronize()
+        errs[r] = err_vs_plain()
+        if errs[r] <= 1e-10 and refine is None:
+            refine = r
+            break
+    if refine is None:
+        refine = 4
+
+    for _ in range(max(args.warmup, 3)):
+        mixed(refine)
+    torch.cuda.synchronize()
+
+    # timed region: K solves, per-step CUDA events on the launching stream,
+    # L2 flushed (256 MiB write) between steps outside the event pairs
+    clocks = ClockSampler(local)
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    wall0 = time.perf_counter()
+    for i in range(args.steps):
+        flush.fill_(float(i))
+        ev[i][0].record(dev_stream)
+        mixed(refine)
+        ev[i][1].record(dev_stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    if dist is not None:
+        dist.barrier()
+    clk = clocks.stop()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    total_ms = sum(step_ms)
+    if dist is not None:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = t.item()
+    final_err = err_vs_plain()
+
+    # per-kernel timing of one solve (separate pass, profiling on)
+    sc.profile(True)
+    flush.fill_(0.0)
+    mixed(refine)
+    torch.cuda.synchronize()
+    prof = sc.profile_read()
+    sc.profile(False)
+    launches = sum(v[1] for v in prof.values())
+
+    # end to end through the C ABI with pinned host buffers (copies timed)
+    pin_rhs = torch.empty(n * n * n, dtype=torch.float64, pin_memory=True).numpy().reshape(
+        (n, n, n), order="F")
+    pin_rhs[...] = rhs
+    pin_solf = torch.zeros((n + 2) ** 3, dtype=torch.float64, pin_memory=True).numpy().reshape(
+        (n + 2, n + 2, n + 2), order="F")
+    pin_bc = []
+    for b in bcs:
+        p = torch.empty(b.size, dtype=torch.float64, pin_memory=True).numpy().reshape(b.shape, order="F")
+        p[...] = b
+        pin_bc.append(p)
+    for _ in range(2):
+        sc.solve_3d(pin_rhs, 0.0, pin_solf, *pin_bc, precision=mf.MF_PREC_SPLIT_BF16, refine=refine)
+    e2e_steps = max(3, min(args.steps, 10))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        sc.solve_3d(pin_rhs, 0.0, pin_solf, *pin_bc, precision=mf.MF_PREC_SPLIT_BF16, refine=refine)
+    e2e_dt = (time.perf_counter() - t0) / e2e_steps
+    h2d = pin_rhs.nbytes + pin_solf.nbytes + sum(b.nbytes for b in pin_bc)
+    d2h = pin_solf.nbytes
+
+    if rank != 0:
+        return
+
+    # CPU baseline: the oracle restatement on the host cores, bounded sample
+    cpu = None
+    oracle_err = None
+    if not args.no_cpu:
+        times = []
+        out = None
+        for _ in range(max(1, args.cpu_sample)):
+            out, dt, _ = cpu_oracle_solve(grids, rhs, bcs)
+            times.append(dt)
+        cpu = {"value": 1.0 / statistics.median(times), "unit": UNIT, "cores": os.cpu_count(),
+               "kind": "port",
+               "sample": "%d full 257^3 plain-FP64 solves of the oracle restatement (NumPy/OpenBLAS)"
+                         % len(times)}
+        got = mf.to_host(d_solf)
+        oracle_err = float(np.linalg.norm(got[1:-1, 1:-1, 1:-1] - out[1:-1, 1:-1, 1:-1]) /
+                           np.linalg.norm(out[1:-1, 1:-1, 1:-1]))
+        plain_vs_oracle = float(np.linalg.norm(mf.to_host(d_ref)[1:-1, 1:-1, 1:-1] - out[1:-1, 1:-1, 1:-1]) /
+                                np.linalg.norm(out[1:-1, 1:-1, 1:-1]))
+    else:
+        plain_vs_oracle = None
+
+    hbm, bf16, src = peaks()
+    tc_ms, tc_n = prof["tc_transform"]
+    algo_flops = 2.0 * n * n * n * n  # one dense transform: 2 * n_axis * (n_b*n_c) * n_axis
+    shares = {k: v[0] for k, v in prof.items()}
+    solve_ms = sum(shares.values())
+    dominant = max(shares, key=shares.get)
+    if dominant == "tc_transform":
+        achieved = algo_flops / (tc_ms / tc_n * 1e-3) / 1e12
+        roof = {"kernel": "k_tc_transform", "bound": "tensor", "achieved": achieved, "peak": bf16,
+                "unit": "TFLOP/s", "frac": achieved / bf16, "traffic": None,
+                "peak_source": src + " bf16 burst", "algorithmic_per_launch": algo_flops}
+    else:
+        ms, cnt = prof[dominant]
+        per_pt = 24.0  # read u, read rhs/partial residual, write result (FP64)
+        algo_bytes = per_pt * n ** 3
+        achieved = algo_bytes / (ms / cnt * 1e-3) / 1e9
+        roof = {"kernel": dominant, "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": achieved / hbm, "traffic": None, "peak_source": src + " copy",
+                "algorithmic_per_launch": algo_bytes}
+    value = world * args.steps / (total_ms * 1e-3)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "bf16x3+f64", "data": "synthetic",
+        "config": {"workload": "poisson_257cube_tanh2y_dirichlet_so6", "nodes": args.nodes,
+                   "precision": "split-BF16 three-product (tcgen05, FP32 accum) + FP64 residual refinement",
+                   "refine_steps": refine, "l2": "256 MiB flush between steps, per-step CUDA events",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "accuracy": {"rel_l2_vs_fp64_gpu": final_err, "rel_l2_vs_cpu_oracle": oracle_err,
+                     "fp64_gpu_vs_cpu_oracle": plain_vs_oracle,
+                     "rel_l2_by_refine_steps": {str(k): v for k, v in errs.items()}},
+        "fp64_plain": {"solves_per_s": 1e3 / statistics.median(plain_ms),
+                       "ms_per_solve": statistics.median(plain_ms)},
+        "speedup_vs_fp64_plain": (1e3 / statistics.median(plain_ms)) and
+                                 value / world / (1e3 / statistics.median(plain_ms)),
+        "kernel_ms_per_solve": {k: v[0] for k, v in prof.items() if v[1]},
+        "kernel_launches_per_solve": {k: v[1] for k, v in prof.items() if v[1]},
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "e2e": {"value": world / e2e_dt, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "api": "mf_solve_3d_mixed with pinned host pointers"},
+        "gpu_launches": launches * args.steps,
+        "gpu_launches_per_step": launches,
+        "clocks": clk,
+        "wall_s_timed": wall,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as tdist
+        backend = "nccl" if args.impl == "gb300" else "gloo"
+        if args.impl == "gb300":
+            torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        tdist.init_process_group(backend=backend)
+        dist = tdist
+    try:
+        if args.impl == "reference":
+            run_reference(args, rank)
+        else:
+            run_gb300(args, rank, world, dist)
+    finally:
+        if dist is not None:
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

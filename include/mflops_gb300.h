@@ -1,0 +1,182 @@
+/*
+ * mflops_gb300.h -- C ABI of the GB300 (sm_103a) implementation of the
+ * MFLOPS3D-MD hot path: compact finite-difference derivatives, the
+ * matrix-diagonalisation Poisson/Helmholtz solver, the spline filter and
+ * the influence-matrix multidomain coupling.
+ *
+ * Conventions
+ *  - Every function returns an int status (MF_OK = 0); mf_last_error()
+ *    returns a thread-local description of the last failure.  No function
+ *    calls exit() and no device code traps.
+ *  - 3D arrays are FP64, Fortran (column-major) order: f(i,j,k) lives at
+ *    f[i + nx*(j + ny*k)], x fastest, exactly the memory of the reference's
+ *    real(rk) :: f(nx,ny,nz).  Coefficient tables exported by the set-up
+ *    functions are Fortran-ordered too (dl(n,5) -> dl[i + n*m]).
+ *  - Field pointers may be HOST or DEVICE memory; the library inspects each
+ *    pointer.  Host pointers are staged through device buffers owned by the
+ *    handle and the call returns after the result is back in host memory.
+ *    Device-pointer calls are asynchronous on `stream` (a cudaStream_t, NULL
+ *    for the legacy default stream).
+ *  - A handle may be used by one host thread at a time; distinct handles
+ *    are independent.
+ */
+#ifndef MFLOPS_GB300_H
+#define MFLOPS_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MF_OK 0
+#define MF_ERR_ARG 1           /* bad argument, shape or size              */
+#define MF_ERR_COMPLEX_EIG 2   /* 1D operator has complex eigenvalues       */
+#define MF_ERR_SINGULAR 3      /* singular small/dense system in set-up     */
+#define MF_ERR_CUDA 4          /* CUDA runtime error                        */
+#define MF_ERR_TIMEOUT 5       /* a bounded device wait expired             */
+#define MF_ERR_NOT_CONVERGED 6 /* iteration limit reached                   */
+#define MF_ERR_ALLOC 7         /* device allocation failed                  */
+#define MF_ERR_UNSUPPORTED 8   /* size/mode outside what the kernels support */
+
+/* Precision modes of the solver transforms. */
+#define MF_PREC_FP64 0        /* plain FP64 (drop-in, matches the reference)       */
+#define MF_PREC_SPLIT_BF16 1  /* split-BF16 three-product on tcgen05, FP32 accum.  */
+#define MF_PREC_3XTF32 2      /* 3xTF32 on tcgen05, FP32 accumulation              */
+
+const char* mf_last_error(void);
+int mf_version(void);
+/* 1 when a CUDA device is usable from this process, else 0. */
+int mf_device_available(void);
+
+/* ------------------------------------------------------------------------
+ * Host-only set-up routines (no GPU needed).
+ * ---------------------------------------------------------------------- */
+
+/* One row of the compact scheme; replaces der_coeffs_generic of
+ * src/class_derivatives/class_derivatives_coefficient.f90:31-191. */
+int mf_der_coeffs_generic(const double h0[7], int cl, int der, int so,
+                          double coef_imp[5], double coef_exp[7]);
+
+/* dl(n,5) and dr(n,7) of a whole line, NOT factored; replaces
+ * der_coeffs_generic_gobal, src/class_derivatives/class_derivatives.f90:330-377. */
+int mf_der_line_coeffs(const double* grid, int n, int der, int so, double* dl, double* dr);
+
+/* In-place quasi-pentadiagonal LU of dl(n,5); replaces pentalu,
+ * src/class_derivatives/class_derivatives.f90:379-423. */
+int mf_pentalu(int n, double* dl);
+
+/* One axis of the solver set-up; replaces solver_coeffs_init,
+ * src/class_solver/class_solver_3d.f90:413-466.  grid has nall nodes,
+ * n = nall-2.  Outputs (any may be NULL): ddl(n,5), ddr(n,8),
+ * inv_lhs(n,n), eigen(n), vect(n,n), inv_vect(n,n), neum(2,7); all
+ * Fortran-ordered, vect untransposed (eigenvectors in columns). */
+int mf_solver_axis_setup(const double* grid, int nall, const int bct[2], int so,
+                         double* ddl, double* ddr, double* inv_lhs, double* eigen,
+                         double* vect, double* inv_vect, double* neum);
+
+/* ------------------------------------------------------------------------
+ * Compact derivatives: type(derivatives_coefficients)
+ * ---------------------------------------------------------------------- */
+typedef struct mf_der mf_der_t;
+
+/* der_coeffs_init(grid,dc,n,solve,so), src/class_derivatives/class_derivatives.f90:111-184.
+ * solver_type != 0 also builds the n-2 "solver type" coefficient set. */
+int mf_der_coeffs_init(const double* grid, int n, int solver_type, int so, mf_der_t** dc);
+int mf_der_destroy(mf_der_t* dc);
+/* dertype(dc), class_derivatives.f90:96-109 */
+int mf_dertype(const mf_der_t* dc, int* solver_type);
+
+/* Field-level pencil drivers derx, dery, derz, dderx, ddery, dderz of
+ * src/class_field/class_field.f90:629-978: df = d/dx_axis^order of f along
+ * `axis` (0=x,1=y,2=z), order 1 or 2.  f, df are (nx,ny,nz).  With a
+ * solver-type dc, the pencils on the two boundary faces normal to the other
+ * axes use der_s/dder_s (interior n-2 points, end values 0) and the four
+ * edge lines are 0. */
+int mf_der_apply(const mf_der_t* dc, int axis, int order, const double* f, double* df,
+                 int nx, int ny, int nz, void* stream);
+int mf_derx(const mf_der_t* dc, const double* f, double* df, int nx, int ny, int nz, void* stream);
+int mf_dery(const mf_der_t* dc, const double* f, double* df, int nx, int ny, int nz, void* stream);
+int mf_derz(const mf_der_t* dc, const double* f, double* df, int nx, int ny, int nz, void* stream);
+int mf_dderx(const mf_der_t* dc, const double* f, double* df, int nx, int ny, int nz, void* stream);
+int mf_ddery(const mf_der_t* dc, const double* f, double* df, int nx, int ny, int nz, void* stream);
+int mf_dderz(const mf_der_t* dc, const double* f, double* df, int nx, int ny, int nz, void* stream);
+
+/* Single-pencil forms der/dder/der_s/dder_s (class_derivatives.f90:186-260)
+ * on `count` contiguous pencils of length n (x[p*n + i]). */
+int mf_der_lines(const mf_der_t* dc, int order, int solver_variant, const double* x, double* dx,
+                 int count, void* stream);
+
+/* ------------------------------------------------------------------------
+ * Matrix-diagonalisation solver: type(solver_coeffs_3d)
+ * ---------------------------------------------------------------------- */
+typedef struct mf_solver3d mf_solver3d_t;
+
+/* solver_coeffs_init_3d(grid1,grid2,grid3,sc,n1,n2,n3,bct,so),
+ * src/class_solver/class_solver_3d.f90:380-411.  n1,n2,n3 are the node
+ * counts INCLUDING the two boundary nodes (grid1(n1) ...).
+ * bct = (x1,x2,y1,y2,z1,z2), 1 Dirichlet / 2 Neumann / 3 second derivative. */
+int mf_solver_coeffs_init_3d(const double* grid1, const double* grid2, const double* grid3,
+                             int n1, int n2, int n3, const int bct[6], int so,
+                             mf_solver3d_t** sc);
+int mf_solver3d_destroy(mf_solver3d_t* sc);
+
+/* solve_3d(sc,rhs,sigma,solf,bcx,bcy,bcz,n1,n2,n3),
+ * src/class_solver/class_solver_3d.f90:83-299, plain FP64.
+ * Here n1,n2,n3 are INTERIOR counts: rhs(n1,n2,n3), solf(0:n1+1,0:n2+1,0:n3+1),
+ * bcx(n2,n3,2), bcy(n1,n3,2), bcz(n1,n2,2).  Solves
+ * (Lx+Ly+Lz+sigma) u = rhs; writes the interior and the six faces of solf
+ * (edges/corners untouched).  Unlike the reference, rhs is not modified. */
+int mf_solve_3d(mf_solver3d_t* sc, const double* rhs, double sigma, double* solf,
+                const double* bcx, const double* bcy, const double* bcz,
+                int n1, int n2, int n3, void* stream);
+
+/* Same problem with the eigenvector transforms on the tensor cores
+ * (precision = MF_PREC_SPLIT_BF16 or MF_PREC_3XTF32) and `refine`
+ * iterative-refinement steps whose residual is computed in FP64 with the
+ * solver's own compact operator.  refine < 0 selects the default count. */
+int mf_solve_3d_mixed(mf_solver3d_t* sc, const double* rhs, double sigma, double* solf,
+                      const double* bcx, const double* bcy, const double* bcz,
+                      int n1, int n2, int n3, int precision, int refine, void* stream);
+
+/* class_field::solver_3d(sc,g,u,bc,sigma), src/class_field/class_field.f90:1072-1109:
+ * g,u are (nx,ny,nz) fields (nx = n1+2 ...); the interior of g is the
+ * right-hand side and the result is written into u. */
+int mf_solver_3d(mf_solver3d_t* sc, const double* g, double* u,
+                 const double* bcx, const double* bcy, const double* bcz,
+                 int nx, int ny, int nz, double sigma, int precision, void* stream);
+
+/* Replaces the eigen-decomposition of one axis (0=x,1=y,2=z) with
+ * caller-supplied tables: eigen(n), vect(n,n) (eigenvectors in columns) and
+ * inv_vect(n,n), Fortran-ordered and untransposed -- e.g. the LAPACK dgeev
+ * output that solver_matrix_init computes (class_solver_3d.f90:535-564).
+ * The solve is invariant to the choice of eigenvector basis, but operators
+ * with a null eigenvalue (bct = 3 next to Dirichlet, all-Neumann) amplify the
+ * basis' rounding; loading the caller's tables makes the results follow the
+ * caller's decomposition.  Synchronous; device or host pointers. */
+int mf_solver3d_set_eigen(mf_solver3d_t* sc, int axis, const double* eigen, const double* vect,
+                          const double* inv_vect);
+
+/* Reads and clears the device-side error flag of the tensor-core pipeline
+ * (MF_ERR_TIMEOUT if a bounded wait expired since the last call). Syncs. */
+int mf_solver3d_device_status(mf_solver3d_t* sc);
+
+/* Per-kernel CUDA-event timers of a solver handle (stage timers in the
+ * spirit of the reference's cpu_time/MPI_WTIME stage prints,
+ * class_solver_3d.f90:106-259, class_field.f90:1317-1386).  profile(sc,1)
+ * resets and enables, profile(sc,0) disables.  profile_read syncs and
+ * returns the accumulated time and launch count of one kernel kind:
+ * 0 tensor-core transform, 1 residual x pass, 2 residual y/z passes,
+ * 3 FP64->split-BF16 conversion, 4 boundary fold, 5 boundary faces,
+ * 6 FP64 transform, 7 interior copy. */
+int mf_solver3d_profile(mf_solver3d_t* sc, int enable);
+int mf_solver3d_profile_read(mf_solver3d_t* sc, int kind, double* total_ms, long long* launches);
+
+/* FP64 residual r = g - (Lx+Ly+Lz+sigma) u on the interior (u with its
+ * boundary data bcx/bcy/bcz), all interior-sized (n1,n2,n3).  Device memory. */
+int mf_solver_residual(mf_solver3d_t* sc, const double* g, const double* u, double sigma,
+                       const double* bcx, const double* bcy, const double* bcz,
+                       double* r, int n1, int n2, int n3, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MFLOPS_GB300_H */

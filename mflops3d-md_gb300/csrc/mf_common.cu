@@ -1,0 +1,183 @@
+// Error reporting, pointer classification and device buffers.
+#include <cstdio>
+#include <cstring>
+
+#include "mf_internal.h"
+#include "mf_setup.h"
+
+namespace mf {
+
+static thread_local std::string g_last_error;
+
+int set_error(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+int cuda_error(cudaError_t e, const char* what) {
+  return set_error(e == cudaErrorMemoryAllocation ? MF_ERR_ALLOC : MF_ERR_CUDA,
+                   "CUDA error in %s: %s", what, cudaGetErrorString(e));
+}
+
+bool is_device_ptr(const void* p) {
+  if (p == nullptr) return false;
+  cudaPointerAttributes attr;
+  cudaError_t e = cudaPointerGetAttributes(&attr, p);
+  if (e != cudaSuccess) {
+    cudaGetLastError();  // clear the sticky-free error of an unknown pointer
+    return false;
+  }
+  return attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged;
+}
+
+int DevBuf::ensure(size_t nbytes) {
+  if (nbytes <= bytes) return MF_OK;
+  release();
+  cudaError_t e = cudaMalloc(&ptr, nbytes);
+  if (e != cudaSuccess) {
+    ptr = nullptr;
+    bytes = 0;
+    return cuda_error(e, "cudaMalloc");
+  }
+  bytes = nbytes;
+  return MF_OK;
+}
+
+void DevBuf::release() {
+  if (ptr) cudaFree(ptr);
+  ptr = nullptr;
+  bytes = 0;
+}
+
+int stage_in(DevBuf& buf, const void* host, size_t bytes, cudaStream_t s) {
+  int rc = buf.ensure(bytes);
+  if (rc) return rc;
+  MF_CUDA(cudaMemcpyAsync(buf.ptr, host, bytes, cudaMemcpyHostToDevice, s));
+  return MF_OK;
+}
+
+void StageProfiler::begin(int kind, cudaStream_t st) {
+  if (!on) return;
+  Rec r{kind, nullptr, nullptr};
+  cudaEventCreate(&r.a);
+  cudaEventCreate(&r.b);
+  cudaEventRecord(r.a, st);
+  pending.push_back(r);
+}
+
+void StageProfiler::end(cudaStream_t st) {
+  if (!on || pending.empty()) return;
+  cudaEventRecord(pending.back().b, st);
+}
+
+void StageProfiler::collect() {
+  for (Rec& r : pending) {
+    float ms = 0.f;
+    if (cudaEventSynchronize(r.b) == cudaSuccess && cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) {
+      total_ms[r.kind] += ms;
+      launches[r.kind] += 1;
+    }
+    cudaEventDestroy(r.a);
+    cudaEventDestroy(r.b);
+  }
+  pending.clear();
+  cudaGetLastError();
+}
+
+void StageProfiler::reset() {
+  collect();
+  for (int k = 0; k < kKinds; ++k) {
+    total_ms[k] = 0.0;
+    launches[k] = 0;
+  }
+}
+
+}  // namespace mf
+
+using namespace mf;
+
+extern "C" {
+
+const char* mf_last_error(void) { return g_last_error.c_str(); }
+
+int mf_version(void) { return 1; }
+
+int mf_device_available(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n > 0 ? 1 : 0;
+}
+
+int mf_der_coeffs_generic(const double h0[7], int cl, int der, int so, double coef_imp[5],
+                          double coef_exp[7]) {
+  if (cl < 1 || cl > 3 || (der != 1 && der != 2) || (so != 2 && so != 4 && so != 6 && so != 8))
+    return set_error(MF_ERR_ARG, "mf_der_coeffs_generic: bad cl/der/so (%d,%d,%d)", cl, der, so);
+  if (!der_coeffs_generic(h0, cl, der, so, coef_imp, coef_exp))
+    return set_error(MF_ERR_SINGULAR, "mf_der_coeffs_generic: singular Taylor system");
+  return MF_OK;
+}
+
+int mf_der_line_coeffs(const double* grid, int n, int der, int so, double* dl, double* dr) {
+  if (n < 7 || !grid || !dl || !dr || (der != 1 && der != 2) ||
+      (so != 2 && so != 4 && so != 6 && so != 8))
+    return set_error(MF_ERR_ARG, "mf_der_line_coeffs: bad arguments (n=%d der=%d so=%d)", n, der, so);
+  std::vector<double> l(5 * n), r(7 * n);
+  if (!der_line_coeffs(grid, n, der, so, l.data(), r.data()))
+    return set_error(MF_ERR_SINGULAR, "mf_der_line_coeffs: singular Taylor system");
+  for (int i = 0; i < n; ++i) {
+    for (int m = 0; m < 5; ++m) dl[i + n * m] = l[5 * i + m];
+    for (int m = 0; m < 7; ++m) dr[i + n * m] = r[7 * i + m];
+  }
+  return MF_OK;
+}
+
+int mf_pentalu(int n, double* dl) {
+  if (n < 7 || !dl) return set_error(MF_ERR_ARG, "mf_pentalu: n must be >= 7");
+  std::vector<double> l(5 * n);
+  for (int i = 0; i < n; ++i)
+    for (int m = 0; m < 5; ++m) l[5 * i + m] = dl[i + n * m];
+  pentalu(n, l.data());
+  for (int i = 0; i < n; ++i)
+    for (int m = 0; m < 5; ++m) dl[i + n * m] = l[5 * i + m];
+  return MF_OK;
+}
+
+int mf_solver_axis_setup(const double* grid, int nall, const int bct[2], int so, double* ddl,
+                         double* ddr, double* inv_lhs, double* eigen, double* vect,
+                         double* inv_vect, double* neum) {
+  if (!grid || !bct) return set_error(MF_ERR_ARG, "mf_solver_axis_setup: null grid/bct");
+  SolverAxisHost ax;
+  std::string msg;
+  int rc = solver_axis_setup(grid, nall, bct, so, ax, msg);
+  if (rc) return set_error(rc, "mf_solver_axis_setup: %s", msg.c_str());
+  const int n = ax.n;
+  if (ddl)
+    for (int i = 0; i < n; ++i)
+      for (int m = 0; m < 5; ++m) ddl[i + n * m] = ax.ddl[5 * i + m];
+  if (ddr)
+    for (int i = 0; i < n; ++i)
+      for (int m = 0; m < 8; ++m) ddr[i + n * m] = ax.ddr[8 * i + m];
+  auto colmajor = [&](const std::vector<double>& src, double* dst) {
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j) dst[i + (size_t)n * j] = src[(size_t)i * n + j];
+  };
+  if (inv_lhs) colmajor(ax.inv_lhs, inv_lhs);
+  if (eigen)
+    for (int i = 0; i < n; ++i) eigen[i] = ax.eigen[i];
+  if (vect) colmajor(ax.vect, vect);
+  if (inv_vect) colmajor(ax.inv_vect, inv_vect);
+  if (neum)
+    for (int s = 0; s < 2; ++s)
+      for (int m = 0; m < 7; ++m) neum[s + 2 * m] = ax.neum[7 * s + m];
+  return MF_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,896 @@
+// Matrix-diagonalisation Poisson/Helmholtz solver on GB300.
+//
+// Reference path: solver_3d (class_field.f90:1072-1109) -> solve_3d
+// (class_solver_3d.f90:83-299): boundary fold, three forward eigenvector
+// transforms (dgx/dgy/dgz with V^-1), eigenvalue divide, three inverse
+// transforms (with V), interior copy and boundary insertion / Neumann
+// extrapolation.
+//
+// Layout.  Each transform contracts the axis that is contiguous in memory
+// and writes its output with the axes rotated, Y[n][m] with m contiguous,
+// so that the next axis to contract is contiguous again:
+//   (i,j,k) -x-> (j,k,i') -y-> (k,i',j') -z-> (i',j',k')
+// After three transforms the array is back in the reference's x-fastest
+// order, every transform is a plain "X[m][k] times B^T" product with both
+// operands K-major, and every store is coalesced along m.
+//
+// Plain path (MF_PREC_FP64): FP64 DFMA tiles; GB300's FP64 pipe bounds it.
+// Mixed path: the six transforms run on tcgen05 (mf_tc.cu) as split-BF16
+// three-product GEMMs into FP32 TMEM accumulators, with the eigenvalue
+// divide fused into the third transform's epilogue and the solution update
+// into the sixth's; iterative refinement recomputes the residual in FP64
+// with the solver's own compact operator (pentalu factors of ddl and the
+// 8-wide ddr), so the refined result converges to the FP64 solution.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "mf_line.cuh"
+#include "mf_setup.h"
+#include "mf_solver.h"
+
+namespace mf {
+
+// Null-mode threshold of the eigen divide: the reference compares with the
+// default-kind literal 1e-11 (class_solver_3d.f90:207-208).
+static const double kNullThresh = (double)1e-11f;
+
+struct AxisDev {
+  int n = 0, P = 0;
+  int bc[2] = {1, 1};
+  double bcc[4] = {0, 0, 0, 0};  // ddr(1,1), ddr(2,1), ddr(n-1,8), ddr(n,7)
+  double neum[14] = {0};
+  DevBuf V, Vinv, eig, invl4, rows;           // FP64
+  DevBuf Vh, Vl, Vih, Vil, eigf, nullf;       // mixed path (padded P x P)
+};
+
+}  // namespace mf
+
+using namespace mf;
+
+struct mf_solver3d {
+  AxisDev ax[3];
+  int n[3] = {0, 0, 0};
+  int P[3] = {0, 0, 0};
+  DevBuf w0, w1;                               // FP64 work arrays (plain path)
+  DevBuf st_rhs, st_solf, st_bc[3];            // host staging
+  DevBuf U, R, R2;                             // mixed path FP64 arrays
+  DevBuf Xa_hi, Xa_lo, Xb_hi, Xb_lo;           // mixed path split planes
+  DevBuf err;                                  // device error flag (int)
+  TcPlan* plan[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  bool mixed_ready = false;
+  StageProfiler prof;
+};
+
+namespace mf {
+
+// ---------------------------------------------------------------------------
+// Kernels
+// ---------------------------------------------------------------------------
+
+// rhs minus the boundary folds inv_lhs(:,{1,2,n-1,n}) * (ddr_bc * bc)
+// (class_solver_3d.f90:104-175), x then y then z like the reference.
+struct FoldArgs {
+  const double* ix[4];
+  const double* iy[4];
+  const double* iz[4];
+  double cx[4], cy[4], cz[4];
+};
+
+__global__ void k_fold(const double* __restrict__ rhs, double* __restrict__ out,
+                       const double* __restrict__ bcx, const double* __restrict__ bcy,
+                       const double* __restrict__ bcz, FoldArgs a, int n1, int n2, int n3) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long tot = (long long)n1 * n2 * n3;
+  if (idx >= tot) return;
+  const int i = (int)(idx % n1);
+  const long long jk = idx / n1;
+  const int j = (int)(jk % n2), k = (int)(jk / n2);
+  double r = rhs[idx];
+  {
+    const double bl = bcx[j + (long long)n2 * k], bh = bcx[j + (long long)n2 * k + (long long)n2 * n3];
+    r = r - a.ix[0][i] * (a.cx[0] * bl) - a.ix[1][i] * (a.cx[1] * bl) - a.ix[2][i] * (a.cx[2] * bh) -
+        a.ix[3][i] * (a.cx[3] * bh);
+  }
+  {
+    const double bl = bcy[i + (long long)n1 * k], bh = bcy[i + (long long)n1 * k + (long long)n1 * n3];
+    r = r - a.iy[0][j] * (a.cy[0] * bl) - a.iy[1][j] * (a.cy[1] * bl) - a.iy[2][j] * (a.cy[2] * bh) -
+        a.iy[3][j] * (a.cy[3] * bh);
+  }
+  {
+    const double bl = bcz[i + (long long)n1 * j], bh = bcz[i + (long long)n1 * j + (long long)n1 * n2];
+    r = r - a.iz[0][k] * (a.cz[0] * bl) - a.iz[1][k] * (a.cz[1] * bl) - a.iz[2][k] * (a.cz[2] * bh) -
+        a.iz[3][k] * (a.cz[3] * bh);
+  }
+  out[idx] = r;
+}
+
+// FP64 transform Y[n][m] = sum_k A[n][k] X[m][k]  (A row-major N x K).
+// Epilogues: 0 plain store; 1 eigenvalue divide (m = i + n1*j, n = k);
+// 2 store into the interior of solf(0:n1+1,0:n2+1,0:n3+1).
+struct GemmEpi {
+  int kind = 0;
+  const double* lx = nullptr;
+  const double* ly = nullptr;
+  const double* lz = nullptr;
+  double sigma = 0.0, thresh = 0.0;
+  int n1 = 0, n2 = 0;
+};
+
+constexpr int GBM = 64, GBN = 64, GBK = 16;
+
+__global__ void __launch_bounds__(256) k_gemm_f64(const double* __restrict__ X, int M, int K,
+                                                  const double* __restrict__ A, int N,
+                                                  double* __restrict__ Y, GemmEpi e) {
+  __shared__ double Xs[GBK][GBM + 1];
+  __shared__ double As[GBK][GBN + 1];
+  const int t = threadIdx.x, tx = t % 16, ty = t / 16;
+  const long long m0 = (long long)blockIdx.x * GBM;
+  const int n0 = blockIdx.y * GBN;
+  double acc[4][4];
+#pragma unroll
+  for (int b = 0; b < 4; ++b)
+#pragma unroll
+    for (int a = 0; a < 4; ++a) acc[b][a] = 0.0;
+  for (int k0 = 0; k0 < K; k0 += GBK) {
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int id = t + 256 * r;
+      const int row = id / GBK, kk = id % GBK;
+      const long long m = m0 + row;
+      const int k = k0 + kk;
+      Xs[kk][row] = (m < M && k < K) ? X[m * K + k] : 0.0;
+      const int nn = n0 + row;
+      As[kk][row] = (nn < N && k < K) ? A[(long long)nn * K + k] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < GBK; ++kk) {
+      double xa[4], ab[4];
+#pragma unroll
+      for (int a = 0; a < 4; ++a) xa[a] = Xs[kk][tx + 16 * a];
+#pragma unroll
+      for (int b = 0; b < 4; ++b) ab[b] = As[kk][ty + 16 * b];
+#pragma unroll
+      for (int b = 0; b < 4; ++b)
+#pragma unroll
+        for (int a = 0; a < 4; ++a) acc[b][a] = fma(ab[b], xa[a], acc[b][a]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int b = 0; b < 4; ++b) {
+    const int n = n0 + ty + 16 * b;
+    if (n >= N) continue;
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+      const long long m = m0 + tx + 16 * a;
+      if (m >= M) continue;
+      double v = acc[b][a];
+      if (e.kind == 0) {
+        Y[(long long)n * M + m] = v;
+      } else {
+        const int i = (int)(m % e.n1), j = (int)(m / e.n1);
+        if (e.kind == 1) {
+          const double lx = e.lx[i], ly = e.ly[j], lz = e.lz[n];
+          const double big = fmax(fmax(fmax(fabs(e.sigma), fabs(lx)), fabs(ly)), fabs(lz));
+          Y[(long long)n * M + m] = (big < e.thresh) ? 0.0 : v / (((lx + ly) + lz) + e.sigma);
+        } else {
+          const long long p1 = e.n1 + 2, p2 = e.n2 + 2;
+          Y[(i + 1) + p1 * ((j + 1) + p2 * (long long)(n + 1))] = v;
+        }
+      }
+    }
+  }
+}
+
+// Boundary faces of solf: Dirichlet copy or 7-point Neumann extrapolation
+// (class_solver_3d.f90:263-297, extrapolation_neum_{x,y,z} :658-776).
+struct FaceArgs {
+  long long sA, sa, sb;  // strides along the axis and the two face directions
+  int n, na, nb;         // interior count along the axis, face extents
+  int bc0, bc1;
+  double nl[7], nr[7];
+};
+
+__global__ void k_faces(double* solf, const double* __restrict__ bc, FaceArgs f) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)f.na * f.nb) return;
+  const int a = (int)(t % f.na), b = (int)(t / f.na);
+  double* p = solf + (a + 1) * f.sa + (b + 1) * f.sb;  // ghost-left node of this line
+  const double blo = bc[t], bhi = bc[t + (long long)f.na * f.nb];
+  if (f.bc0 == 1) {
+    p[0] = blo;
+  } else {
+    double acc = blo;
+    for (int m = 1; m < 7; ++m) acc = acc - f.nl[m] * p[m * f.sA];
+    p[0] = acc * (1.0 / f.nl[0]);
+  }
+  const long long last = (long long)(f.n + 1) * f.sA;
+  if (f.bc1 == 1) {
+    p[last] = bhi;
+  } else {
+    double acc = bhi;
+    for (int m = 5; m >= 0; --m) acc = acc - f.nr[m] * p[(long long)(f.n - 5 + m) * f.sA];
+    p[last] = acc * (1.0 / f.nr[6]);
+  }
+}
+
+// ---- FP64 residual r = g - sigma*u - (Lx + Ly + Lz) u, boundary data included
+
+struct StoreSub {
+  const double* rin;
+  __device__ __forceinline__ void operator()(double* out, long long idx, double y) const {
+    out[idx] = rin[idx] - y;
+  }
+};
+
+constexpr int kResLines = 32;
+
+// x pass: r = g - sigma*u - Lx u (x lines staged in shared memory).
+__global__ void __launch_bounds__(32) k_resid_x(const double* __restrict__ rows, const double* u,
+                                                const double* __restrict__ g, double sigma,
+                                                const double* __restrict__ bcx, double4 bcc,
+                                                double* __restrict__ r, int n1, int n2, int n3,
+                                                int pitch) {
+  extern __shared__ double tile[];
+  const int lane = threadIdx.x;
+  const long long nlines = (long long)n2 * n3;
+  const long long l0 = (long long)blockIdx.x * kResLines;
+  const int nl = (int)min((long long)kResLines, nlines - l0);
+  for (int l = 0; l < nl; ++l) {
+    const double* src = u + (l0 + l) * n1;
+    for (int i = lane; i < n1; i += 32) tile[l * pitch + i] = src[i];
+  }
+  __syncwarp();
+  if (lane < nl) {
+    const long long line = l0 + lane;
+    LineBC bc;
+    bc.lo = bcx[line];
+    bc.hi = bcx[line + nlines];
+    bc.c0 = bcc.x; bc.c1 = bcc.y; bc.c2 = bcc.z; bc.c3 = bcc.w;
+    double* row = tile + lane * pitch;
+    solve_line(rows, n1, row, row, 1, bc, StorePlain());
+  }
+  __syncwarp();
+  for (int l = 0; l < nl; ++l) {
+    const long long base = (l0 + l) * n1;
+    for (int i = lane; i < n1; i += 32)
+      r[base + i] = g[base + i] - sigma * u[base + i] - tile[l * pitch + i];
+  }
+}
+
+// y or z pass: rout = rin - L u, one thread per line, coalesced along x.
+__global__ void k_resid_strided(const double* __restrict__ rows, int n, const double* u,
+                                const double* rin, double* rout, const double* __restrict__ bc,
+                                double4 bcc, int na, int nb, long long sa, long long sb,
+                                long long s) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)na * nb) return;
+  const int a = (int)(t % na), b = (int)(t / na);
+  const long long base = a * sa + b * sb;
+  LineBC lb;
+  lb.lo = bc[t];
+  lb.hi = bc[t + (long long)na * nb];
+  lb.c0 = bcc.x; lb.c1 = bcc.y; lb.c2 = bcc.z; lb.c3 = bcc.w;
+  solve_line(rows, n, u + base, rout + base, s, lb, StoreSub{rin + base});
+}
+
+// FP64 interior array -> split-BF16 planes in the padded (P1,P2,P3) layout.
+__global__ void k_split_in(const double* __restrict__ r, __nv_bfloat16* __restrict__ hi,
+                           __nv_bfloat16* __restrict__ lo, int n1, int n2, int n3, int P1, int P2,
+                           int P3) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long tot = (long long)P1 * P2 * P3;
+  if (idx >= tot) return;
+  const int i = (int)(idx % P1);
+  const long long jk = idx / P1;
+  const int j = (int)(jk % P2), k = (int)(jk / P2);
+  float v = 0.f;
+  if (i < n1 && j < n2 && k < n3) v = (float)r[i + (long long)n1 * (j + (long long)n2 * k)];
+  const __nv_bfloat16 h = __float2bfloat16_rn(v);
+  hi[idx] = h;
+  lo[idx] = __float2bfloat16_rn(v - __bfloat162float(h));
+}
+
+// Copies the FP64 interior u (n1,n2,n3) into solf(1:n1,1:n2,1:n3).
+__global__ void k_copy_interior(const double* __restrict__ u, double* __restrict__ solf, int n1,
+                                int n2, int n3) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long tot = (long long)n1 * n2 * n3;
+  if (idx >= tot) return;
+  const int i = (int)(idx % n1);
+  const long long jk = idx / n1;
+  const int j = (int)(jk % n2), k = (int)(jk / n2);
+  solf[(i + 1) + (long long)(n1 + 2) * ((j + 1) + (long long)(n2 + 2) * (k + 1))] = u[idx];
+}
+
+// Extracts the interior of a (nx,ny,nz) field into an (nx-2,ny-2,nz-2) array.
+__global__ void k_extract_interior(const double* __restrict__ g, double* __restrict__ out, int n1,
+                                   int n2, int n3) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long tot = (long long)n1 * n2 * n3;
+  if (idx >= tot) return;
+  const int i = (int)(idx % n1);
+  const long long jk = idx / n1;
+  const int j = (int)(jk % n2), k = (int)(jk / n2);
+  out[idx] = g[(i + 1) + (long long)(n1 + 2) * ((j + 1) + (long long)(n2 + 2) * (k + 1))];
+}
+
+static inline unsigned blocks_for(long long n, int t) { return (unsigned)((n + t - 1) / t); }
+
+// Profiler kinds (see mf_solver3d_profile_read in the C ABI).
+enum ProfKind { kProfTc = 0, kProfResidX = 1, kProfResidYZ = 2, kProfSplit = 3, kProfFold = 4,
+                kProfFaces = 5, kProfGemm64 = 6, kProfCopy = 7 };
+
+// ---------------------------------------------------------------------------
+// Host orchestration
+// ---------------------------------------------------------------------------
+
+template <class T>
+static int upload(DevBuf& b, const std::vector<T>& v) {
+  int rc = b.ensure(v.size() * sizeof(T));
+  if (rc) return rc;
+  MF_CUDA(cudaMemcpy(b.ptr, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+  return MF_OK;
+}
+
+static void split_bf16(const std::vector<double>& m, int n, int P, std::vector<__nv_bfloat16>& hi,
+                       std::vector<__nv_bfloat16>& lo) {
+  hi.assign((size_t)P * P, __float2bfloat16_rn(0.f));
+  lo.assign((size_t)P * P, __float2bfloat16_rn(0.f));
+  for (int r = 0; r < n; ++r)
+    for (int c = 0; c < n; ++c) {
+      const float v = (float)m[(size_t)r * n + c];
+      const __nv_bfloat16 h = __float2bfloat16_rn(v);
+      hi[(size_t)r * P + c] = h;
+      lo[(size_t)r * P + c] = __float2bfloat16_rn(v - __bfloat162float(h));
+    }
+}
+
+// Uploads eigen tables (row-major V, V^-1) and their split-BF16 copies.
+static int axis_set_eigen(AxisDev& d, const std::vector<double>& eig, const std::vector<double>& V,
+                          const std::vector<double>& Vinv) {
+  int rc;
+  if ((rc = upload(d.V, V)) || (rc = upload(d.Vinv, Vinv)) || (rc = upload(d.eig, eig))) return rc;
+  std::vector<__nv_bfloat16> hi, lo;
+  split_bf16(Vinv, d.n, d.P, hi, lo);
+  if ((rc = upload(d.Vih, hi)) || (rc = upload(d.Vil, lo))) return rc;
+  split_bf16(V, d.n, d.P, hi, lo);
+  if ((rc = upload(d.Vh, hi)) || (rc = upload(d.Vl, lo))) return rc;
+  std::vector<float> ef(d.P, 0.f);
+  std::vector<uint8_t> nf(d.P, 0);
+  for (int i = 0; i < d.n; ++i) {
+    ef[i] = (float)eig[i];
+    nf[i] = std::fabs(eig[i]) < kNullThresh ? 1 : 0;
+  }
+  if ((rc = upload(d.eigf, ef)) || (rc = upload(d.nullf, nf))) return rc;
+  return MF_OK;
+}
+
+static int axis_upload(AxisDev& d, const SolverAxisHost& h) {
+  const int n = h.n;
+  d.n = n;
+  d.P = (n + 63) / 64 * 64;
+  d.bc[0] = h.bc[0];
+  d.bc[1] = h.bc[1];
+  d.bcc[0] = h.ddr[0];
+  d.bcc[1] = h.ddr[8];
+  d.bcc[2] = h.ddr[8 * (n - 2) + 7];
+  d.bcc[3] = h.ddr[8 * (n - 1) + 6];
+  for (int m = 0; m < 14; ++m) d.neum[m] = h.neum[m];
+  int rc;
+  std::vector<double> l4((size_t)4 * n);
+  const int cols[4] = {0, 1, n - 2, n - 1};
+  for (int c = 0; c < 4; ++c)
+    for (int i = 0; i < n; ++i) l4[(size_t)c * n + i] = h.inv_lhs[(size_t)i * n + cols[c]];
+  if ((rc = upload(d.invl4, l4))) return rc;
+  // residual operator rows: factored lhs + 7-wide explicit stencil (see mf_line.cuh)
+  std::vector<double> rows((size_t)kRow * n, 0.0);
+  for (int i = 0; i < n; ++i) {
+    double* r = &rows[(size_t)kRow * i];
+    r[0] = h.ddl_lu[5 * i + 0];
+    r[1] = h.ddl_lu[5 * i + 1];
+    r[2] = 1.0 / h.ddl_lu[5 * i + 2];
+    r[3] = h.ddl_lu[5 * i + 3];
+    r[4] = h.ddl_lu[5 * i + 4];
+    const double* dr = &h.ddr[8 * i];
+    if (i == 0) {
+      for (int m = 0; m < 6; ++m) r[5 + m] = dr[1 + m];
+    } else if (i == 1) {
+      for (int m = 0; m < 7; ++m) r[5 + m] = dr[1 + m];
+    } else if (i == n - 2) {
+      for (int m = 0; m < 7; ++m) r[5 + m] = dr[m];
+    } else if (i == n - 1) {
+      for (int m = 0; m < 6; ++m) r[6 + m] = dr[m];
+    } else {
+      for (int m = 0; m < 5; ++m) r[5 + m] = dr[m];
+    }
+  }
+  if ((rc = upload(d.rows, rows))) return rc;
+  return axis_set_eigen(d, h.eigen, h.vect, h.inv_vect);
+}
+
+static int gemm_f64(StageProfiler& prof, const double* X, int M, int K, const double* A, int N,
+                    double* Y, const GemmEpi& e, cudaStream_t st) {
+  dim3 grid(blocks_for(M, GBM), blocks_for(N, GBN));
+  prof.begin(kProfGemm64, st);
+  k_gemm_f64<<<grid, 256, 0, st>>>(X, M, K, A, N, Y, e);
+  prof.end(st);
+  MF_CUDA(cudaGetLastError());
+  return MF_OK;
+}
+
+static int faces(mf_solver3d* sc, double* solf, const double* bcs[3], cudaStream_t st) {
+  const int n1 = sc->n[0], n2 = sc->n[1], n3 = sc->n[2];
+  const long long p1 = n1 + 2, p2 = n2 + 2;
+  for (int axis = 0; axis < 3; ++axis) {
+    const AxisDev& d = sc->ax[axis];
+    FaceArgs f;
+    if (axis == 0) { f.sA = 1; f.sa = p1; f.sb = p1 * p2; f.n = n1; f.na = n2; f.nb = n3; }
+    if (axis == 1) { f.sA = p1; f.sa = 1; f.sb = p1 * p2; f.n = n2; f.na = n1; f.nb = n3; }
+    if (axis == 2) { f.sA = p1 * p2; f.sa = 1; f.sb = p1; f.n = n3; f.na = n1; f.nb = n2; }
+    f.bc0 = d.bc[0];
+    f.bc1 = d.bc[1];
+    for (int m = 0; m < 7; ++m) { f.nl[m] = d.neum[m]; f.nr[m] = d.neum[7 + m]; }
+    sc->prof.begin(kProfFaces, st);
+    k_faces<<<blocks_for((long long)f.na * f.nb, 128), 128, 0, st>>>(solf, bcs[axis], f);
+    sc->prof.end(st);
+    MF_CUDA(cudaGetLastError());
+  }
+  return MF_OK;
+}
+
+static FoldArgs fold_args(mf_solver3d* sc) {
+  FoldArgs a;
+  for (int c = 0; c < 4; ++c) {
+    a.ix[c] = sc->ax[0].invl4.as<double>() + (size_t)c * sc->n[0];
+    a.iy[c] = sc->ax[1].invl4.as<double>() + (size_t)c * sc->n[1];
+    a.iz[c] = sc->ax[2].invl4.as<double>() + (size_t)c * sc->n[2];
+    a.cx[c] = sc->ax[0].bcc[c];
+    a.cy[c] = sc->ax[1].bcc[c];
+    a.cz[c] = sc->ax[2].bcc[c];
+  }
+  return a;
+}
+
+// Plain FP64 solve on device pointers.
+static int solve_plain_dev(mf_solver3d* sc, const double* rhs, double sigma, double* solf,
+                           const double* bcs[3], cudaStream_t st) {
+  const int n1 = sc->n[0], n2 = sc->n[1], n3 = sc->n[2];
+  const long long tot = (long long)n1 * n2 * n3;
+  int rc;
+  if ((rc = sc->w0.ensure(tot * sizeof(double))) || (rc = sc->w1.ensure(tot * sizeof(double))))
+    return rc;
+  double* w0 = sc->w0.as<double>();
+  double* w1 = sc->w1.as<double>();
+  sc->prof.begin(kProfFold, st);
+  k_fold<<<blocks_for(tot, 256), 256, 0, st>>>(rhs, w0, bcs[0], bcs[1], bcs[2], fold_args(sc), n1,
+                                               n2, n3);
+  sc->prof.end(st);
+  MF_CUDA(cudaGetLastError());
+  GemmEpi plain;
+  const double* Vi[3] = {sc->ax[0].Vinv.as<double>(), sc->ax[1].Vinv.as<double>(),
+                         sc->ax[2].Vinv.as<double>()};
+  const double* Vf[3] = {sc->ax[0].V.as<double>(), sc->ax[1].V.as<double>(),
+                         sc->ax[2].V.as<double>()};
+  // forward transforms with V^-1: x, y, z (+ divide)
+  if ((rc = gemm_f64(sc->prof, w0, n2 * n3, n1, Vi[0], n1, w1, plain, st))) return rc;
+  if ((rc = gemm_f64(sc->prof, w1, n3 * n1, n2, Vi[1], n2, w0, plain, st))) return rc;
+  GemmEpi div;
+  div.kind = 1;
+  div.lx = sc->ax[0].eig.as<double>();
+  div.ly = sc->ax[1].eig.as<double>();
+  div.lz = sc->ax[2].eig.as<double>();
+  div.sigma = sigma;
+  div.thresh = kNullThresh;
+  div.n1 = n1;
+  div.n2 = n2;
+  if ((rc = gemm_f64(sc->prof, w0, n1 * n2, n3, Vi[2], n3, w1, div, st))) return rc;
+  // inverse transforms with V, the last one written into solf's interior
+  if ((rc = gemm_f64(sc->prof, w1, n2 * n3, n1, Vf[0], n1, w0, plain, st))) return rc;
+  if ((rc = gemm_f64(sc->prof, w0, n3 * n1, n2, Vf[1], n2, w1, plain, st))) return rc;
+  GemmEpi out;
+  out.kind = 2;
+  out.n1 = n1;
+  out.n2 = n2;
+  if ((rc = gemm_f64(sc->prof, w1, n1 * n2, n3, Vf[2], n3, solf, out, st))) return rc;
+  return faces(sc, solf, bcs, st);
+}
+
+// FP64 residual on device pointers: r = g - sigma*u - sum_a L_a u.
+static int residual_dev(mf_solver3d* sc, const double* g, const double* u, double sigma,
+                        const double* bcs[3], double* r, double* tmp, cudaStream_t st) {
+  const int n1 = sc->n[0], n2 = sc->n[1], n3 = sc->n[2];
+  auto bcc = [&](int a) {
+    return make_double4(sc->ax[a].bcc[0], sc->ax[a].bcc[1], sc->ax[a].bcc[2], sc->ax[a].bcc[3]);
+  };
+  const int pitch = n1 | 1;
+  const size_t smem = (size_t)kResLines * pitch * sizeof(double);
+  if (smem > 200 * 1024) return set_error(MF_ERR_UNSUPPORTED, "residual: n1=%d too large", n1);
+  static bool attr = false;
+  if (!attr) {
+    MF_CUDA(cudaFuncSetAttribute(k_resid_x, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    attr = true;
+  }
+  const long long xl = (long long)n2 * n3;
+  // x pass -> r; y pass r -> tmp; z pass tmp -> r
+  sc->prof.begin(kProfResidX, st);
+  k_resid_x<<<blocks_for(xl, kResLines), 32, smem, st>>>(sc->ax[0].rows.as<double>(), u, g, sigma,
+                                                         bcs[0], bcc(0), r, n1, n2, n3, pitch);
+  sc->prof.end(st);
+  MF_CUDA(cudaGetLastError());
+  // y lines (i,k): stride n1
+  sc->prof.begin(kProfResidYZ, st);
+  k_resid_strided<<<blocks_for((long long)n1 * n3, 128), 128, 0, st>>>(
+      sc->ax[1].rows.as<double>(), n2, u, r, tmp, bcs[1], bcc(1), n1, n3, 1, (long long)n1 * n2, n1);
+  sc->prof.end(st);
+  MF_CUDA(cudaGetLastError());
+  // z lines (i,j): stride n1*n2
+  sc->prof.begin(kProfResidYZ, st);
+  k_resid_strided<<<blocks_for((long long)n1 * n2, 128), 128, 0, st>>>(
+      sc->ax[2].rows.as<double>(), n3, u, tmp, r, bcs[2], bcc(2), n1, n2, 1, n1,
+      (long long)n1 * n2);
+  sc->prof.end(st);
+  MF_CUDA(cudaGetLastError());
+  return MF_OK;
+}
+
+static int mixed_prepare(mf_solver3d* sc) {
+  if (sc->mixed_ready) return MF_OK;
+  for (int a = 0; a < 3; ++a)
+    if (sc->P[a] > 256)
+      return set_error(MF_ERR_UNSUPPORTED,
+                       "mixed-precision transforms support up to 256 interior points per axis "
+                       "(axis %d has %d)", a, sc->n[a]);
+  const long long tot = (long long)sc->n[0] * sc->n[1] * sc->n[2];
+  const long long ptot = (long long)sc->P[0] * sc->P[1] * sc->P[2];
+  int rc;
+  if ((rc = sc->U.ensure(tot * 8)) || (rc = sc->R.ensure(tot * 8)) || (rc = sc->R2.ensure(tot * 8)))
+    return rc;
+  if ((rc = sc->Xa_hi.ensure(ptot * 2)) || (rc = sc->Xa_lo.ensure(ptot * 2)) ||
+      (rc = sc->Xb_hi.ensure(ptot * 2)) || (rc = sc->Xb_lo.ensure(ptot * 2)))
+    return rc;
+  MF_CUDA(cudaMemset(sc->Xa_hi.ptr, 0, ptot * 2));
+  MF_CUDA(cudaMemset(sc->Xa_lo.ptr, 0, ptot * 2));
+  MF_CUDA(cudaMemset(sc->Xb_hi.ptr, 0, ptot * 2));
+  MF_CUDA(cudaMemset(sc->Xb_lo.ptr, 0, ptot * 2));
+  if ((rc = sc->err.ensure(sizeof(int)))) return rc;
+  MF_CUDA(cudaMemset(sc->err.ptr, 0, sizeof(int)));
+  const int P1 = sc->P[0], P2 = sc->P[1], P3 = sc->P[2];
+  auto bf = [](DevBuf& b) { return b.as<__nv_bfloat16>(); };
+  struct Spec { DevBuf *xh, *xl; int axis; bool inv; int M; };
+  Spec specs[6] = {{&sc->Xa_hi, &sc->Xa_lo, 0, true, P2 * P3}, {&sc->Xb_hi, &sc->Xb_lo, 1, true, P3 * P1},
+                   {&sc->Xa_hi, &sc->Xa_lo, 2, true, P1 * P2}, {&sc->Xb_hi, &sc->Xb_lo, 0, false, P2 * P3},
+                   {&sc->Xa_hi, &sc->Xa_lo, 1, false, P3 * P1}, {&sc->Xb_hi, &sc->Xb_lo, 2, false, P1 * P2}};
+  for (int t = 0; t < 6; ++t) {
+    AxisDev& d = sc->ax[specs[t].axis];
+    DevBuf& bh = specs[t].inv ? d.Vih : d.Vh;
+    DevBuf& bl = specs[t].inv ? d.Vil : d.Vl;
+    if ((rc = tc_plan_create(&sc->plan[t], bf(*specs[t].xh), bf(*specs[t].xl), bf(bh), bf(bl),
+                             specs[t].M, d.P, d.P)))
+      return rc;
+  }
+  sc->mixed_ready = true;
+  return MF_OK;
+}
+
+static int tc_run(mf_solver3d* sc, int t, const TcEpilogue& e, cudaStream_t st) {
+  sc->prof.begin(kProfTc, st);
+  int rc = tc_transform(sc->plan[t], e, sc->err.as<int>(), st);
+  sc->prof.end(st);
+  return rc;
+}
+
+// One approximate solve of the folded right-hand side already split into Xa.
+static int approx_solve(mf_solver3d* sc, double sigma, bool accumulate, cudaStream_t st) {
+  int* err = sc->err.as<int>();
+  auto bf = [](DevBuf& b) { return b.as<__nv_bfloat16>(); };
+  TcEpilogue e;
+  int rc;
+  e.kind = 0;
+  e.y_hi = bf(sc->Xb_hi); e.y_lo = bf(sc->Xb_lo);
+  if ((rc = tc_run(sc, 0, e, st))) return rc;
+  e.y_hi = bf(sc->Xa_hi); e.y_lo = bf(sc->Xa_lo);
+  if ((rc = tc_run(sc, 1, e, st))) return rc;
+  TcEpilogue d = e;
+  d.kind = 1;
+  d.y_hi = bf(sc->Xb_hi); d.y_lo = bf(sc->Xb_lo);
+  d.lam_x = sc->ax[0].eigf.as<float>();
+  d.lam_y = sc->ax[1].eigf.as<float>();
+  d.lam_z = sc->ax[2].eigf.as<float>();
+  d.null_x = sc->ax[0].nullf.as<uint8_t>();
+  d.null_y = sc->ax[1].nullf.as<uint8_t>();
+  d.null_z = sc->ax[2].nullf.as<uint8_t>();
+  d.sigma = (float)sigma;
+  d.sigma_null = std::fabs(sigma) < kNullThresh ? 1 : 0;
+  d.n1 = sc->n[0]; d.n2 = sc->n[1]; d.n3 = sc->n[2];
+  d.P1 = sc->P[0]; d.P2 = sc->P[1];
+  if ((rc = tc_run(sc, 2, d, st))) return rc;
+  e.y_hi = bf(sc->Xa_hi); e.y_lo = bf(sc->Xa_lo);
+  if ((rc = tc_run(sc, 3, e, st))) return rc;
+  e.y_hi = bf(sc->Xb_hi); e.y_lo = bf(sc->Xb_lo);
+  if ((rc = tc_run(sc, 4, e, st))) return rc;
+  TcEpilogue u;
+  u.kind = 2;
+  u.u = sc->U.as<double>();
+  u.accumulate = accumulate ? 1 : 0;
+  u.n1 = sc->n[0]; u.n2 = sc->n[1]; u.n3 = sc->n[2];
+  u.P1 = sc->P[0]; u.P2 = sc->P[1];
+  return tc_run(sc, 5, u, st);
+}
+
+static int split_r(mf_solver3d* sc, const double* r, cudaStream_t st) {
+  const long long ptot = (long long)sc->P[0] * sc->P[1] * sc->P[2];
+  sc->prof.begin(kProfSplit, st);
+  k_split_in<<<blocks_for(ptot, 256), 256, 0, st>>>(r, sc->Xa_hi.as<__nv_bfloat16>(),
+                                                    sc->Xa_lo.as<__nv_bfloat16>(), sc->n[0],
+                                                    sc->n[1], sc->n[2], sc->P[0], sc->P[1], sc->P[2]);
+  sc->prof.end(st);
+  MF_CUDA(cudaGetLastError());
+  return MF_OK;
+}
+
+static int solve_mixed_dev(mf_solver3d* sc, const double* rhs, double sigma, double* solf,
+                           const double* bcs[3], int prec, int refine, cudaStream_t st) {
+  if (prec != MF_PREC_SPLIT_BF16)
+    return set_error(MF_ERR_UNSUPPORTED, "precision mode %d is not available", prec);
+  int rc;
+  if ((rc = mixed_prepare(sc))) return rc;
+  const int n1 = sc->n[0], n2 = sc->n[1], n3 = sc->n[2];
+  const long long tot = (long long)n1 * n2 * n3;
+  double* R = sc->R.as<double>();
+  sc->prof.begin(kProfFold, st);
+  k_fold<<<blocks_for(tot, 256), 256, 0, st>>>(rhs, R, bcs[0], bcs[1], bcs[2], fold_args(sc), n1,
+                                               n2, n3);
+  sc->prof.end(st);
+  MF_CUDA(cudaGetLastError());
+  if ((rc = split_r(sc, R, st))) return rc;
+  if ((rc = approx_solve(sc, sigma, false, st))) return rc;
+  for (int it = 0; it < refine; ++it) {
+    if ((rc = residual_dev(sc, rhs, sc->U.as<double>(), sigma, bcs, R, sc->R2.as<double>(), st)))
+      return rc;
+    if ((rc = split_r(sc, R, st))) return rc;
+    if ((rc = approx_solve(sc, sigma, true, st))) return rc;
+  }
+  sc->prof.begin(kProfCopy, st);
+  k_copy_interior<<<blocks_for(tot, 256), 256, 0, st>>>(sc->U.as<double>(), solf, n1, n2, n3);
+  sc->prof.end(st);
+  MF_CUDA(cudaGetLastError());
+  return faces(sc, solf, bcs, st);
+}
+
+}  // namespace mf
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+int mf_solver_coeffs_init_3d(const double* g1, const double* g2, const double* g3, int n1, int n2,
+                             int n3, const int bct[6], int so, mf_solver3d_t** out) {
+  if (!g1 || !g2 || !g3 || !bct || !out)
+    return set_error(MF_ERR_ARG, "mf_solver_coeffs_init_3d: null argument");
+  *out = nullptr;
+  const double* grids[3] = {g1, g2, g3};
+  const int nall[3] = {n1, n2, n3};
+  SolverAxisHost host[3];
+  for (int a = 0; a < 3; ++a) {
+    std::string msg;
+    int rc = solver_axis_setup(grids[a], nall[a], bct + 2 * a, so, host[a], msg);
+    if (rc) return set_error(rc, "mf_solver_coeffs_init_3d: axis %d: %s", a, msg.c_str());
+  }
+  mf_solver3d* sc = new mf_solver3d();
+  for (int a = 0; a < 3; ++a) {
+    int rc = axis_upload(sc->ax[a], host[a]);
+    if (rc) {
+      mf_solver3d_destroy(sc);
+      return rc;
+    }
+    sc->n[a] = host[a].n;
+    sc->P[a] = sc->ax[a].P;
+  }
+  *out = sc;
+  return MF_OK;
+}
+
+int mf_solver3d_destroy(mf_solver3d_t* sc) {
+  if (!sc) return MF_OK;
+  for (int t = 0; t < 6; ++t) tc_plan_destroy(sc->plan[t]);
+  for (auto& d : sc->ax) {
+    for (DevBuf* b : {&d.V, &d.Vinv, &d.eig, &d.invl4, &d.rows, &d.Vh, &d.Vl, &d.Vih, &d.Vil,
+                      &d.eigf, &d.nullf})
+      b->release();
+  }
+  for (DevBuf* b : {&sc->w0, &sc->w1, &sc->st_rhs, &sc->st_solf, &sc->st_bc[0], &sc->st_bc[1],
+                    &sc->st_bc[2], &sc->U, &sc->R, &sc->R2, &sc->Xa_hi, &sc->Xa_lo, &sc->Xb_hi,
+                    &sc->Xb_lo, &sc->err})
+    b->release();
+  delete sc;
+  return MF_OK;
+}
+
+}  // extern "C"
+
+// Shared front end of the solve entry points: validates, stages host
+// pointers, runs `body` on device pointers, copies solf back.
+template <class Body>
+static int solve_front(mf_solver3d_t* sc, const double* rhs, double* solf, const double* bcx,
+                       const double* bcy, const double* bcz, int n1, int n2, int n3, void* stream,
+                       Body body) {
+  if (!sc || !rhs || !solf || !bcx || !bcy || !bcz)
+    return set_error(MF_ERR_ARG, "solve_3d: null argument");
+  if (n1 != sc->n[0] || n2 != sc->n[1] || n3 != sc->n[2])
+    return set_error(MF_ERR_ARG, "solve_3d: shape (%d,%d,%d) differs from the set-up (%d,%d,%d)",
+                     n1, n2, n3, sc->n[0], sc->n[1], sc->n[2]);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const size_t rb = (size_t)n1 * n2 * n3 * 8, sb = (size_t)(n1 + 2) * (n2 + 2) * (n3 + 2) * 8;
+  const size_t bb[3] = {(size_t)n2 * n3 * 2 * 8, (size_t)n1 * n3 * 2 * 8, (size_t)n1 * n2 * 2 * 8};
+  const double* bcs_in[3] = {bcx, bcy, bcz};
+  const double* bcs[3];
+  int rc;
+  bool any_host = false;
+  for (int a = 0; a < 3; ++a) {
+    if (is_device_ptr(bcs_in[a])) {
+      bcs[a] = bcs_in[a];
+    } else {
+      if ((rc = stage_in(sc->st_bc[a], bcs_in[a], bb[a], st))) return rc;
+      bcs[a] = sc->st_bc[a].as<double>();
+      any_host = true;
+    }
+  }
+  const double* r = rhs;
+  if (!is_device_ptr(rhs)) {
+    if ((rc = stage_in(sc->st_rhs, rhs, rb, st))) return rc;
+    r = sc->st_rhs.as<double>();
+    any_host = true;
+  }
+  double* s = solf;
+  const bool host_solf = !is_device_ptr(solf);
+  if (host_solf) {
+    if ((rc = stage_in(sc->st_solf, solf, sb, st))) return rc;
+    s = sc->st_solf.as<double>();
+    any_host = true;
+  }
+  if ((rc = body(r, s, bcs, st))) return rc;
+  if (host_solf) MF_CUDA(cudaMemcpyAsync(solf, s, sb, cudaMemcpyDeviceToHost, st));
+  if (any_host) {
+    MF_CUDA(cudaStreamSynchronize(st));
+    if (sc->err.ptr) {
+      int herr = 0;
+      MF_CUDA(cudaMemcpy(&herr, sc->err.ptr, sizeof(int), cudaMemcpyDeviceToHost));
+      if (herr) return set_error(MF_ERR_TIMEOUT, "solve_3d: a tensor-core pipeline wait expired");
+    }
+  }
+  return MF_OK;
+}
+
+extern "C" {
+
+int mf_solve_3d(mf_solver3d_t* sc, const double* rhs, double sigma, double* solf,
+                const double* bcx, const double* bcy, const double* bcz, int n1, int n2, int n3,
+                void* stream) {
+  return solve_front(sc, rhs, solf, bcx, bcy, bcz, n1, n2, n3, stream,
+                     [&](const double* r, double* s, const double** bcs, cudaStream_t st) {
+                       return solve_plain_dev(sc, r, sigma, s, bcs, st);
+                     });
+}
+
+int mf_solve_3d_mixed(mf_solver3d_t* sc, const double* rhs, double sigma, double* solf,
+                      const double* bcx, const double* bcy, const double* bcz, int n1, int n2,
+                      int n3, int precision, int refine, void* stream) {
+  if (precision == MF_PREC_FP64)
+    return mf_solve_3d(sc, rhs, sigma, solf, bcx, bcy, bcz, n1, n2, n3, stream);
+  if (refine < 0) refine = 2;
+  return solve_front(sc, rhs, solf, bcx, bcy, bcz, n1, n2, n3, stream,
+                     [&](const double* r, double* s, const double** bcs, cudaStream_t st) {
+                       return solve_mixed_dev(sc, r, sigma, s, bcs, precision, refine, st);
+                     });
+}
+
+int mf_solver_3d(mf_solver3d_t* sc, const double* g, double* u, const double* bcx,
+                 const double* bcy, const double* bcz, int nx, int ny, int nz, double sigma,
+                 int precision, void* stream) {
+  if (!sc || !g || !u) return set_error(MF_ERR_ARG, "mf_solver_3d: null argument");
+  const int n1 = nx - 2, n2 = ny - 2, n3 = nz - 2;
+  if (n1 != sc->n[0] || n2 != sc->n[1] || n3 != sc->n[2])
+    return set_error(MF_ERR_ARG, "mf_solver_3d: field (%d,%d,%d) does not match the set-up", nx, ny, nz);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const long long tot = (long long)n1 * n2 * n3;
+  int rc;
+  // interior of g -> contiguous rhs (class_field.f90:1092-1098)
+  DevBuf& gr = sc->st_rhs;
+  const double* gd = g;
+  DevBuf gstage;
+  if (!is_device_ptr(g)) {
+    if ((rc = stage_in(gstage, g, (size_t)nx * ny * nz * 8, st))) return rc;
+    gd = gstage.as<double>();
+  }
+  if ((rc = gr.ensure(tot * 8))) { gstage.release(); return rc; }
+  k_extract_interior<<<blocks_for(tot, 256), 256, 0, st>>>(gd, gr.as<double>(), n1, n2, n3);
+  if (cudaGetLastError() != cudaSuccess) { gstage.release(); return set_error(MF_ERR_CUDA, "extract"); }
+  rc = (precision == MF_PREC_FP64)
+           ? mf_solve_3d(sc, gr.as<double>(), sigma, u, bcx, bcy, bcz, n1, n2, n3, stream)
+           : mf_solve_3d_mixed(sc, gr.as<double>(), sigma, u, bcx, bcy, bcz, n1, n2, n3, precision,
+                               -1, stream);
+  if (gstage.ptr) {
+    cudaStreamSynchronize(st);
+    gstage.release();
+  }
+  return rc;
+}
+
+int mf_solver3d_set_eigen(mf_solver3d_t* sc, int axis, const double* eigen, const double* vect,
+                          const double* inv_vect) {
+  if (!sc || !eigen || !vect || !inv_vect || axis < 0 || axis > 2)
+    return set_error(MF_ERR_ARG, "mf_solver3d_set_eigen: bad arguments");
+  AxisDev& d = sc->ax[axis];
+  const int n = d.n;
+  std::vector<double> e(n), vc((size_t)n * n), ic((size_t)n * n);
+  auto fetch = [&](const double* src, double* dst, size_t count) -> int {
+    if (is_device_ptr(src)) {
+      MF_CUDA(cudaMemcpy(dst, src, count * sizeof(double), cudaMemcpyDeviceToHost));
+    } else {
+      std::memcpy(dst, src, count * sizeof(double));
+    }
+    return MF_OK;
+  };
+  int rc;
+  if ((rc = fetch(eigen, e.data(), n)) || (rc = fetch(vect, vc.data(), (size_t)n * n)) ||
+      (rc = fetch(inv_vect, ic.data(), (size_t)n * n)))
+    return rc;
+  std::vector<double> V((size_t)n * n), Vi((size_t)n * n);
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) {
+      V[(size_t)i * n + j] = vc[i + (size_t)n * j];
+      Vi[(size_t)i * n + j] = ic[i + (size_t)n * j];
+    }
+  MF_CUDA(cudaDeviceSynchronize());
+  return axis_set_eigen(d, e, V, Vi);
+}
+
+int mf_solver3d_device_status(mf_solver3d_t* sc) {
+  if (!sc) return set_error(MF_ERR_ARG, "mf_solver3d_device_status: null handle");
+  if (!sc->err.ptr) return MF_OK;
+  MF_CUDA(cudaDeviceSynchronize());
+  int herr = 0;
+  MF_CUDA(cudaMemcpy(&herr, sc->err.ptr, sizeof(int), cudaMemcpyDeviceToHost));
+  MF_CUDA(cudaMemset(sc->err.ptr, 0, sizeof(int)));
+  if (herr) return set_error(MF_ERR_TIMEOUT, "tensor-core pipeline wait expired");
+  return MF_OK;
+}
+
+int mf_solver3d_profile(mf_solver3d_t* sc, int enable) {
+  if (!sc) return set_error(MF_ERR_ARG, "mf_solver3d_profile: null handle");
+  sc->prof.reset();
+  sc->prof.on = enable != 0;
+  return MF_OK;
+}
+
+int mf_solver3d_profile_read(mf_solver3d_t* sc, int kind, double* total_ms, long long* launches) {
+  if (!sc || !total_ms || !launches || kind < 0 || kind >= StageProfiler::kKinds)
+    return set_error(MF_ERR_ARG, "mf_solver3d_profile_read: bad arguments");
+  sc->prof.collect();
+  *total_ms = sc->prof.total_ms[kind];
+  *launches = sc->prof.launches[kind];
+  return MF_OK;
+}
+
+int mf_solver_residual(mf_solver3d_t* sc, const double* g, const double* u, double sigma,
+                       const double* bcx, const double* bcy, const double* bcz, double* r, int n1,
+                       int n2, int n3, void* stream) {
+  if (!sc || !g || !u || !bcx || !bcy || !bcz || !r)
+    return set_error(MF_ERR_ARG, "mf_solver_residual: null argument");
+  if (n1 != sc->n[0] || n2 != sc->n[1] || n3 != sc->n[2])
+    return set_error(MF_ERR_ARG, "mf_solver_residual: shape mismatch");
+  for (const void* p : {(const void*)g, (const void*)u, (const void*)bcx, (const void*)bcy,
+                        (const void*)bcz, (const void*)r})
+    if (!is_device_ptr(p)) return set_error(MF_ERR_ARG, "mf_solver_residual: device pointers only");
+  int rc;
+  if ((rc = sc->R2.ensure((size_t)n1 * n2 * n3 * 8))) return rc;
+  const double* bcs[3] = {bcx, bcy, bcz};
+  return residual_dev(sc, g, u, sigma, bcs, r, sc->R2.as<double>(),
+                      static_cast<cudaStream_t>(stream));
+}
+
+}  // extern "C"

@@ -1,0 +1,42 @@
+// Internal interface between the solver orchestration (mf_solver.cu) and
+// the tcgen05 split-precision transform (mf_tc.cu).
+#pragma once
+#include <cuda_bf16.h>
+#include <cstdint>
+
+#include "mf_internal.h"
+
+namespace mf {
+
+// One axis transform  Y[n][m] = sum_k B[n][k] * X[m][k]  on the tensor cores,
+// with X and B given as split-BF16 (hi, lo) planes and three products
+// hi*hi + hi*lo + lo*hi accumulated in FP32.  X rows have pitch K, Y rows
+// pitch M.  M is a multiple of 128, K = N is a multiple of 16 and <= 256.
+struct TcEpilogue {
+  int kind = 0;                  // 0 split store, 1 eigen divide + split store, 2 FP64 update
+  __nv_bfloat16* y_hi = nullptr; // kinds 0,1: [N][M]
+  __nv_bfloat16* y_lo = nullptr;
+  // kind 1: m = i + P1*j, n = k
+  const float* lam_x = nullptr;  // [P1], [P2], [P3] eigenvalues, 0 past n
+  const float* lam_y = nullptr;
+  const float* lam_z = nullptr;
+  const uint8_t* null_x = nullptr;  // 1 where |lambda| < 1e-11 (FP64 test at set-up)
+  const uint8_t* null_y = nullptr;
+  const uint8_t* null_z = nullptr;
+  float sigma = 0.f;
+  int sigma_null = 0;            // |sigma| < 1e-11
+  // kind 2: u[i + n1*(j + n2*k)] (+)= y
+  double* u = nullptr;
+  int accumulate = 0;
+  int n1 = 0, n2 = 0, n3 = 0, P1 = 0, P2 = 0;
+};
+
+struct TcPlan;  // opaque: tensor maps for one transform
+
+// Creates tensor maps for X (rows=M, cols=K) and the matrix planes (N x K).
+int tc_plan_create(TcPlan** plan, const __nv_bfloat16* x_hi, const __nv_bfloat16* x_lo,
+                   const __nv_bfloat16* b_hi, const __nv_bfloat16* b_lo, int M, int N, int K);
+void tc_plan_destroy(TcPlan* plan);
+int tc_transform(const TcPlan* plan, const TcEpilogue& epi, int* dev_err, cudaStream_t st);
+
+}  // namespace mf

@@ -1,0 +1,395 @@
+"""Python host mirror of the MFLOPS3D-MD hot-path interfaces over the C ABI
+of ``libmflops_gb300.so`` (declared in ``include/mflops_gb300.h``).
+
+The names, argument orders and meanings follow the reference's Fortran
+module procedures:
+
+=============================  ==============================================
+here                           reference
+=============================  ==============================================
+``der_coeffs_init``            class_derivatives.f90:111 ``der_coeffs_init``
+``derx .. dderz``              class_field.f90:629-978
+``der/dder/der_s/dder_s``      class_derivatives.f90:186-260 (on pencils)
+``solver_coeffs_init_3d``      class_solver_3d.f90:380 ``solver_coeffs_init_3d``
+``solve_3d``                   class_solver_3d.f90:83 ``solve_3d``
+``solver_3d``                  class_field.f90:1072 ``solver_3d``
+=============================  ==============================================
+
+Field arrays are FP64 in the reference's memory order (x fastest).  Device
+data is passed as torch CUDA tensors of shape (nx, ny, nz) with strides
+(1, nx, nx*ny) -- see :func:`to_device` -- and host data as NumPy arrays in
+Fortran order.  Errors raise :class:`MflopsError` with the library's message.
+The CUDA library is required: importing this module without it raises.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(os.path.dirname(_HERE), "lib", "libmflops_gb300.so")
+
+MF_OK = 0
+MF_ERR_ARG = 1
+MF_ERR_COMPLEX_EIG = 2
+MF_ERR_SINGULAR = 3
+MF_ERR_CUDA = 4
+MF_ERR_TIMEOUT = 5
+MF_ERR_NOT_CONVERGED = 6
+MF_ERR_ALLOC = 7
+MF_ERR_UNSUPPORTED = 8
+
+MF_PREC_FP64 = 0
+MF_PREC_SPLIT_BF16 = 1
+MF_PREC_3XTF32 = 2
+
+
+class MflopsError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("[mflops_gb300 error %d] %s" % (code, msg))
+        self.code = code
+
+
+def lib_path():
+    return _LIB_PATH
+
+
+def _load():
+    if not os.path.exists(_LIB_PATH):
+        raise ImportError("libmflops_gb300.so is not built (%s); run __graft_entry__.build()" % _LIB_PATH)
+    return ctypes.CDLL(_LIB_PATH)
+
+
+_lib = _load()
+
+_P = ctypes.c_void_p
+_I = ctypes.c_int
+_D = ctypes.c_double
+_DP = ctypes.POINTER(ctypes.c_double)
+_IP = ctypes.POINTER(ctypes.c_int)
+
+# name -> argtypes (all return int)
+_PROTOS = {
+    "mf_version": [],
+    "mf_device_available": [],
+    "mf_der_coeffs_generic": [_DP, _I, _I, _I, _DP, _DP],
+    "mf_der_line_coeffs": [_DP, _I, _I, _I, _DP, _DP],
+    "mf_pentalu": [_I, _DP],
+    "mf_solver_axis_setup": [_DP, _I, _IP, _I, _DP, _DP, _DP, _DP, _DP, _DP, _DP],
+    "mf_der_coeffs_init": [_DP, _I, _I, _I, ctypes.POINTER(_P)],
+    "mf_der_destroy": [_P],
+    "mf_dertype": [_P, _IP],
+    "mf_der_apply": [_P, _I, _I, _P, _P, _I, _I, _I, _P],
+    "mf_derx": [_P, _P, _P, _I, _I, _I, _P],
+    "mf_dery": [_P, _P, _P, _I, _I, _I, _P],
+    "mf_derz": [_P, _P, _P, _I, _I, _I, _P],
+    "mf_dderx": [_P, _P, _P, _I, _I, _I, _P],
+    "mf_ddery": [_P, _P, _P, _I, _I, _I, _P],
+    "mf_dderz": [_P, _P, _P, _I, _I, _I, _P],
+    "mf_der_lines": [_P, _I, _I, _P, _P, _I, _P],
+    "mf_solver_coeffs_init_3d": [_DP, _DP, _DP, _I, _I, _I, _IP, _I, ctypes.POINTER(_P)],
+    "mf_solver3d_destroy": [_P],
+    "mf_solve_3d": [_P, _P, _D, _P, _P, _P, _P, _I, _I, _I, _P],
+    "mf_solve_3d_mixed": [_P, _P, _D, _P, _P, _P, _P, _I, _I, _I, _I, _I, _P],
+    "mf_solver_3d": [_P, _P, _P, _P, _P, _P, _I, _I, _I, _D, _I, _P],
+    "mf_solver_residual": [_P, _P, _P, _D, _P, _P, _P, _P, _I, _I, _I, _P],
+    "mf_solver3d_set_eigen": [_P, _I, _DP, _DP, _DP],
+    "mf_solver3d_device_status": [_P],
+    "mf_solver3d_profile": [_P, _I],
+    "mf_solver3d_profile_read": [_P, _I, _DP, ctypes.POINTER(ctypes.c_longlong)],
+}
+
+for _name, _args in _PROTOS.items():
+    _fn = getattr(_lib, _name)
+    _fn.argtypes = _args
+    _fn.restype = ctypes.c_int
+_lib.mf_last_error.restype = ctypes.c_char_p
+_lib.mf_last_error.argtypes = []
+
+
+def exported_symbols():
+    """Names declared in include/mflops_gb300.h that this module binds."""
+    return sorted(list(_PROTOS) + ["mf_last_error"])
+
+
+def _check(rc):
+    if rc != MF_OK:
+        raise MflopsError(rc, _lib.mf_last_error().decode())
+
+
+def device_available():
+    return bool(_lib.mf_device_available())
+
+
+def _dptr(a):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    return a, a.ctypes.data_as(_DP)
+
+
+# ---------------------------------------------------------------------------
+# host-only set-up routines (no GPU needed)
+# ---------------------------------------------------------------------------
+
+def der_coeffs_generic(h0, cl, der, so):
+    h0, hp = _dptr(h0)
+    ci = np.zeros(5)
+    ce = np.zeros(7)
+    _check(_lib.mf_der_coeffs_generic(hp, cl, der, so, ci.ctypes.data_as(_DP), ce.ctypes.data_as(_DP)))
+    return ci, ce
+
+
+def der_line_coeffs(grid, der, so):
+    """(dl[n,5], dr[n,7]) unfactored, like der_coeffs_generic_gobal."""
+    g, gp = _dptr(grid)
+    n = g.size
+    dl = np.zeros((n, 5), order="F")
+    dr = np.zeros((n, 7), order="F")
+    _check(_lib.mf_der_line_coeffs(gp, n, der, so, dl.ctypes.data_as(_DP), dr.ctypes.data_as(_DP)))
+    return dl, dr
+
+
+def pentalu(dl):
+    a = np.asfortranarray(np.array(dl, dtype=np.float64))
+    _check(_lib.mf_pentalu(a.shape[0], a.ctypes.data_as(_DP)))
+    return a
+
+
+def solver_axis_setup(grid, bct, so=6):
+    """Per-axis solver set-up; returns a dict of Fortran-ordered arrays."""
+    g, gp = _dptr(grid)
+    n = g.size - 2
+    b = (ctypes.c_int * 2)(int(bct[0]), int(bct[1]))
+    out = {"ddl": np.zeros((n, 5), order="F"), "ddr": np.zeros((n, 8), order="F"),
+           "inv_lhs": np.zeros((n, n), order="F"), "eigen": np.zeros(n),
+           "vect": np.zeros((n, n), order="F"), "inv_vect": np.zeros((n, n), order="F"),
+           "neum": np.zeros((2, 7), order="F")}
+    _check(_lib.mf_solver_axis_setup(gp, g.size, b, so, *[out[k].ctypes.data_as(_DP) for k in
+                                                          ("ddl", "ddr", "inv_lhs", "eigen", "vect",
+                                                           "inv_vect", "neum")]))
+    return out
+
+
+# ---------------------------------------------------------------------------
+# array plumbing
+# ---------------------------------------------------------------------------
+
+def to_device(a):
+    """NumPy (nx,ny,nz) array -> torch CUDA tensor with the same memory order."""
+    import torch
+    a = np.asfortranarray(np.asarray(a, dtype=np.float64))
+    t = torch.from_numpy(np.ascontiguousarray(a.T)).cuda()
+    return t.permute(*reversed(range(a.ndim)))
+
+
+def to_host(t):
+    """Inverse of :func:`to_device`."""
+    rev = list(reversed(range(t.dim())))
+    return np.asfortranarray(t.permute(*rev).contiguous().cpu().numpy().T)
+
+
+def empty_device(shape):
+    import torch
+    return torch.zeros(tuple(reversed(shape)), dtype=torch.float64, device="cuda").permute(
+        *reversed(range(len(shape))))
+
+
+def _is_fortran_tensor(t):
+    n = t.dim()
+    return t.permute(*reversed(range(n))).is_contiguous()
+
+
+def _arg(a):
+    """Pointer of a torch CUDA tensor (Fortran layout) or NumPy host array."""
+    if hasattr(a, "data_ptr"):
+        if a.dtype.__repr__() != "torch.float64":
+            raise TypeError("expected a float64 tensor")
+        if not _is_fortran_tensor(a):
+            raise ValueError("tensor must have x-fastest (Fortran) layout; use to_device()")
+        return ctypes.c_void_p(a.data_ptr())
+    if not isinstance(a, np.ndarray) or a.dtype != np.float64 or not a.flags.f_contiguous:
+        raise TypeError("expected a Fortran-ordered float64 NumPy array")
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+def _stream(stream):
+    if stream is not None:
+        return ctypes.c_void_p(stream)
+    try:
+        import torch
+        if torch.cuda.is_available():
+            return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    except ImportError:
+        pass
+    return ctypes.c_void_p(0)
+
+
+# ---------------------------------------------------------------------------
+# derivatives
+# ---------------------------------------------------------------------------
+
+class DerivativesCoefficients:
+    """type(derivatives_coefficients) handle (device-resident coefficients)."""
+
+    def __init__(self, grid, n=None, solve=False, so=6):
+        g, gp = _dptr(grid)
+        self.n = g.size if n is None else int(n)
+        self.so = so
+        self._h = ctypes.c_void_p()
+        _check(_lib.mf_der_coeffs_init(gp, self.n, 1 if solve else 0, so, ctypes.byref(self._h)))
+
+    def dertype(self):
+        v = ctypes.c_int()
+        _check(_lib.mf_dertype(self._h, ctypes.byref(v)))
+        return bool(v.value)
+
+    def apply(self, axis, order, f, out=None, stream=None):
+        shape = tuple(f.shape)
+        if out is None:
+            out = empty_device(shape) if hasattr(f, "data_ptr") else np.zeros(shape, order="F")
+        _check(_lib.mf_der_apply(self._h, axis, order, _arg(f), _arg(out), shape[0], shape[1],
+                                 shape[2], _stream(stream)))
+        return out
+
+    def lines(self, order, x, solver_variant=False, out=None, stream=None):
+        """der/dder (or der_s/dder_s) on pencils: x has shape (n, count)."""
+        if out is None:
+            out = empty_device(tuple(x.shape)) if hasattr(x, "data_ptr") else np.zeros(x.shape, order="F")
+        _check(_lib.mf_der_lines(self._h, order, 1 if solver_variant else 0, _arg(x), _arg(out),
+                                 x.shape[1], _stream(stream)))
+        return out
+
+    def close(self):
+        if self._h:
+            _lib.mf_der_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def der_coeffs_init(grid, n, solve, so):
+    """der_coeffs_init(grid,dc,n,solve,so) -> dc"""
+    return DerivativesCoefficients(grid, n, solve, so)
+
+
+def derx(dc, x, out=None, stream=None):
+    return dc.apply(0, 1, x, out, stream)
+
+
+def dery(dc, x, out=None, stream=None):
+    return dc.apply(1, 1, x, out, stream)
+
+
+def derz(dc, x, out=None, stream=None):
+    return dc.apply(2, 1, x, out, stream)
+
+
+def dderx(dc, x, out=None, stream=None):
+    return dc.apply(0, 2, x, out, stream)
+
+
+def ddery(dc, x, out=None, stream=None):
+    return dc.apply(1, 2, x, out, stream)
+
+
+def dderz(dc, x, out=None, stream=None):
+    return dc.apply(2, 2, x, out, stream)
+
+
+# ---------------------------------------------------------------------------
+# solver
+# ---------------------------------------------------------------------------
+
+class SolverCoeffs3D:
+    """type(solver_coeffs_3d) handle.  n1,n2,n3 = node counts incl. boundaries."""
+
+    def __init__(self, grid1, grid2, grid3, bct, so=6):
+        g1, p1 = _dptr(grid1)
+        g2, p2 = _dptr(grid2)
+        g3, p3 = _dptr(grid3)
+        b = (ctypes.c_int * 6)(*[int(v) for v in bct])
+        self.nall = (g1.size, g2.size, g3.size)
+        self.n = tuple(v - 2 for v in self.nall)
+        self._h = ctypes.c_void_p()
+        _check(_lib.mf_solver_coeffs_init_3d(p1, p2, p3, g1.size, g2.size, g3.size, b, so,
+                                             ctypes.byref(self._h)))
+
+    def solve_3d(self, rhs, sigma, solf, bcx, bcy, bcz, precision=MF_PREC_FP64, refine=-1,
+                 stream=None):
+        n1, n2, n3 = (int(v) for v in rhs.shape)
+        if precision == MF_PREC_FP64:
+            _check(_lib.mf_solve_3d(self._h, _arg(rhs), float(sigma), _arg(solf), _arg(bcx),
+                                    _arg(bcy), _arg(bcz), n1, n2, n3, _stream(stream)))
+        else:
+            _check(_lib.mf_solve_3d_mixed(self._h, _arg(rhs), float(sigma), _arg(solf), _arg(bcx),
+                                          _arg(bcy), _arg(bcz), n1, n2, n3, precision, refine,
+                                          _stream(stream)))
+        return solf
+
+    def solver_3d(self, g, u, bcx, bcy, bcz, sigma, precision=MF_PREC_FP64, stream=None):
+        nx, ny, nz = (int(v) for v in g.shape)
+        _check(_lib.mf_solver_3d(self._h, _arg(g), _arg(u), _arg(bcx), _arg(bcy), _arg(bcz), nx, ny,
+                                 nz, float(sigma), precision, _stream(stream)))
+        return u
+
+    def set_eigen(self, axis, eigen, vect, inv_vect):
+        """Load an externally computed eigen-decomposition for one axis
+        (e.g. LAPACK dgeev, as solver_matrix_init does)."""
+        e, ep = _dptr(eigen)
+        v = np.asfortranarray(np.asarray(vect, dtype=np.float64))
+        vi = np.asfortranarray(np.asarray(inv_vect, dtype=np.float64))
+        _check(_lib.mf_solver3d_set_eigen(self._h, axis, ep, v.ctypes.data_as(_DP),
+                                          vi.ctypes.data_as(_DP)))
+
+    PROFILE_KINDS = ("tc_transform", "residual_x", "residual_yz", "split_bf16", "bc_fold",
+                     "bc_faces", "fp64_transform", "interior_copy")
+
+    def profile(self, enable=True):
+        _check(_lib.mf_solver3d_profile(self._h, 1 if enable else 0))
+
+    def profile_read(self):
+        """{kind: (total_ms, launches)} accumulated since profile(True)."""
+        out = {}
+        for k, name in enumerate(self.PROFILE_KINDS):
+            ms = ctypes.c_double()
+            n = ctypes.c_longlong()
+            _check(_lib.mf_solver3d_profile_read(self._h, k, ctypes.byref(ms), ctypes.byref(n)))
+            out[name] = (ms.value, n.value)
+        return out
+
+    def device_status(self):
+        _check(_lib.mf_solver3d_device_status(self._h))
+
+    def residual(self, g, u, sigma, bcx, bcy, bcz, r, stream=None):
+        n1, n2, n3 = (int(v) for v in g.shape)
+        _check(_lib.mf_solver_residual(self._h, _arg(g), _arg(u), float(sigma), _arg(bcx), _arg(bcy),
+                                       _arg(bcz), _arg(r), n1, n2, n3, _stream(stream)))
+        return r
+
+    def close(self):
+        if self._h:
+            _lib.mf_solver3d_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def solver_coeffs_init_3d(grid1, grid2, grid3, n1, n2, n3, bct, so):
+    """solver_coeffs_init_3d(grid1,grid2,grid3,sc,n1,n2,n3,bct,so) -> sc"""
+    assert (len(grid1), len(grid2), len(grid3)) == (n1, n2, n3)
+    return SolverCoeffs3D(grid1, grid2, grid3, bct, so)
+
+
+def solve_3d(sc, rhs, sigma, solf, bcx, bcy, bcz, n1=None, n2=None, n3=None, **kw):
+    return sc.solve_3d(rhs, sigma, solf, bcx, bcy, bcz, **kw)
+
+
+def solver_3d(sc, g, u, bcx, bcy, bcz, sigma, **kw):
+    return sc.solver_3d(g, u, bcx, bcy, bcz, sigma, **kw)

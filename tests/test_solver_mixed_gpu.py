@@ -1,0 +1,46 @@
+"""Split-BF16 tensor-core transforms + FP64 iterative refinement against the
+FP64 oracle.  Tolerance (north-star): relative L2 error <= 1e-10 after
+refinement; the unrefined split-precision error is reported alongside."""
+import numpy as np
+import pytest
+
+from oracle import solver as S
+from oracle import mesh
+
+from helpers import bc_arrays, field, grids, rel_l2, solf_mask
+
+pytestmark = pytest.mark.gpu
+
+
+def mixed_case(mf, nall, bct, sigma, refine, kind="tanh", seed=5):
+    gx, gy, gz = grids(*nall, kind=kind)
+    n1, n2, n3 = (v - 2 for v in nall)
+    sc_ref = S.Solver3D(gx, gy, gz, bct, 6)
+    sc = mf.SolverCoeffs3D(gx, gy, gz, bct, 6)
+    rhs = field((n1, n2, n3), seed)
+    bcx, bcy, bcz = bc_arrays(n1, n2, n3, seed + 1)
+    solf0 = np.zeros((n1 + 2, n2 + 2, n3 + 2), order="F")
+    ref = S.solve_3d(sc_ref, rhs, sigma, solf0, bcx, bcy, bcz)
+    got = sc.solve_3d(mf.to_device(rhs), sigma, mf.to_device(solf0), mf.to_device(bcx),
+                      mf.to_device(bcy), mf.to_device(bcz), precision=mf.MF_PREC_SPLIT_BF16,
+                      refine=refine)
+    m = solf_mask(n1, n2, n3)
+    return rel_l2(mf.to_host(got)[m], ref[m])
+
+
+def test_mixed_unrefined_is_split_precision_accurate(mf, gpu):
+    err = mixed_case(mf, (66, 66, 66), (1,) * 6, -1e3, refine=0)
+    print("split-bf16 unrefined rel L2 error: %.3e" % err)
+    assert err < 1e-3
+
+
+@pytest.mark.parametrize("sigma", [0.0, -1e3])
+def test_mixed_refined_reaches_1e10(mf, gpu, sigma):
+    err = mixed_case(mf, (66, 66, 66), (1,) * 6, sigma, refine=3)
+    print("split-bf16 + 3 refinements rel L2 error: %.3e" % err)
+    assert err < 1e-10
+
+
+def test_mixed_uneven_and_neumann(mf, gpu):
+    err = mixed_case(mf, (50, 66, 98), (1, 2, 1, 1, 2, 1), -1e6 * 1e-3, refine=3)
+    assert err < 1e-10
