@@ -164,9 +164,11 @@ int mf_solver3d_device_status(mf_solver3d_t* sc);
  * class_solver_3d.f90:106-259, class_field.f90:1317-1386).  profile(sc,1)
  * resets and enables, profile(sc,0) disables.  profile_read syncs and
  * returns the accumulated time and launch count of one kernel kind:
- * 0 tensor-core transform, 1 residual x pass, 2 residual y/z passes,
+ * 0 tensor-core transform (split store), 1 residual x pass, 2 residual y/z passes,
  * 3 FP64->split-BF16 conversion, 4 boundary fold, 5 boundary faces,
- * 6 FP64 transform, 7 interior copy. */
+ * 6 FP64 transform, 7 interior copy, 8 tensor-core transform with the
+ * eigenvalue divide, 9 tensor-core transform updating the FP64 solution,
+ * 10 FP32 correction residual. */
 int mf_solver3d_profile(mf_solver3d_t* sc, int enable);
 int mf_solver3d_profile_read(mf_solver3d_t* sc, int kind, double* total_ms, long long* launches);
 

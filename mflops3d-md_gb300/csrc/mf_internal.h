@@ -41,7 +41,7 @@ int stage_in(DevBuf& buf, const void* host, size_t bytes, cudaStream_t s);
 // launch of the handle is bracketed by an event pair on its stream; read()
 // synchronises on the recorded events and accumulates per-kind totals.
 struct StageProfiler {
-  static constexpr int kKinds = 8;
+  static constexpr int kKinds = 12;
   bool on = false;
   struct Rec {
     int kind;

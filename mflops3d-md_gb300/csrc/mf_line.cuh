@@ -1,93 +1,250 @@
-// Device routine shared by the derivative kernels and the FP64 residual of
-// the solver: one quasi-pentadiagonal compact-scheme line solve,
+// Device routine shared by the derivative kernels and the residuals of the
+// solver's iterative refinement: one quasi-pentadiagonal compact-scheme line
+// solve,
 //   y = L^-1 (R x + boundary terms),
 // with L given by its pentalu factors and R by a 7-wide explicit stencil
 // (rows 1,2 on x(1..7), rows n-1,n on x(n-6..n), 5 points in between).
 // Restates derx_rhs + pentares (class_derivatives.f90:262-295,425-466).
+//
+// T is the arithmetic type (double for the FP64 paths, float for the
+// correction residual); In is the storage type of the line being
+// differentiated (a float input is widened exactly to double).
 #pragma once
+#include <cstdint>
 
 namespace mf {
 
 // Packed per-row coefficients: p, f, 1/c, d, e, r[0..6].
 constexpr int kRow = 12;
 
-struct LineSet {
-  const double* __restrict__ c;  // n rows of kRow doubles
+template <class T>
+struct LineSetT {
+  const T* __restrict__ c;  // n rows of kRow values
   int n;
 };
+using LineSet = LineSetT<double>;
 
 // Boundary contributions folded into rows 1, 2, n-1, n of the right-hand side.
-struct LineBC {
-  double lo = 0.0, hi = 0.0;      // boundary values at both ends
-  double c0 = 0.0, c1 = 0.0;      // coefficients of `lo` in rows 1, 2
-  double c2 = 0.0, c3 = 0.0;      // coefficients of `hi` in rows n-1, n
+template <class T>
+struct LineBCT {
+  T lo = 0, hi = 0;  // boundary values at both ends
+  T c0 = 0, c1 = 0;  // coefficients of `lo` in rows 1, 2
+  T c2 = 0, c3 = 0;  // coefficients of `hi` in rows n-1, n
 };
+using LineBC = LineBCT<double>;
 
-// Default final store: out(i) = y.
+// Exact float -> double widening built from the bit fields (integer pipe;
+// GB300's conversion unit shares the narrow FP64 rate).  Subnormal floats
+// flush to signed zero, infinities and NaN keep their class.
+__device__ __forceinline__ double widen(float f) {
+  const uint32_t u = __float_as_uint(f);
+  const uint32_t e = (u >> 23) & 0xFFu;
+  const uint64_t sgn = (uint64_t)(u & 0x80000000u) << 32;
+  if (e == 0) return __longlong_as_double((long long)sgn);
+  const uint64_t exp = (e == 0xFFu) ? 0x7FFull : (uint64_t)(e + 896u);
+  return __longlong_as_double((long long)(sgn | (exp << 52) | ((uint64_t)(u & 0x7FFFFFu) << 29)));
+}
+
+template <class T, class In>
+__device__ __forceinline__ T load_as(const In* p, long long i);
+template <>
+__device__ __forceinline__ double load_as<double, double>(const double* p, long long i) { return p[i]; }
+template <>
+__device__ __forceinline__ double load_as<double, float>(const float* p, long long i) { return widen(p[i]); }
+template <>
+__device__ __forceinline__ float load_as<float, float>(const float* p, long long i) { return p[i]; }
+
+// Default final store: out(i) = y.  Final-store functors receive the row
+// index i, the element offset idx = i*s of the row in the line, and y.
 struct StorePlain {
-  __device__ __forceinline__ void operator()(double* out, long long idx, double y) const {
+  template <class T>
+  __device__ __forceinline__ void operator()(T* out, int, long long idx, T y) const {
     out[idx] = y;
   }
 };
 
-// Solves one pencil.  `in` and `out` may alias: every input value is read
-// before the store that could overwrite it.  The forward-elimination values
-// are parked in `out` and read back by the back substitution, whose result
-// goes through `fin(out, index, y)`.
-template <class Fin>
-__device__ __forceinline__ void solve_line(const double* __restrict__ C, int n, const double* in,
-                                           double* out, long long s, const LineBC& bc,
-                                           const Fin& fin) {
-  const double f0 = in[0], f1 = in[s], f2 = in[2 * s], f3 = in[3 * s], f4 = in[4 * s],
-               f5 = in[5 * s], f6 = in[6 * s];
-  const double g0 = in[(long long)(n - 7) * s], g1 = in[(long long)(n - 6) * s],
-               g2 = in[(long long)(n - 5) * s], g3 = in[(long long)(n - 4) * s],
-               g4 = in[(long long)(n - 3) * s], g5 = in[(long long)(n - 2) * s],
-               g6 = in[(long long)(n - 1) * s];
-  const double* c0 = C;
-  const double* c1 = C + kRow;
-  const double x0 = c0[5] * f0 + c0[6] * f1 + c0[7] * f2 + c0[8] * f3 + c0[9] * f4 +
-                    c0[10] * f5 + c0[11] * f6 + bc.c0 * bc.lo;
-  const double b1 = c1[5] * f0 + c1[6] * f1 + c1[7] * f2 + c1[8] * f3 + c1[9] * f4 +
-                    c1[10] * f5 + c1[11] * f6 + bc.c1 * bc.lo;
-  const double x1 = b1 - x0 * c1[1];
+// Right-hand-side evaluators of one row: plain products, or the compensated
+// form (see CompSum below) for the FP32 correction residual.
+template <class T>
+struct PlainStencil {
+  __device__ __forceinline__ T row5(const T* c, T w0, T w1, T w2, T w3, T w4) const {
+    return c[5] * w0 + c[6] * w1 + c[7] * w2 + c[8] * w3 + c[9] * w4;
+  }
+  __device__ __forceinline__ T row7(const T* c, T a0, T a1, T a2, T a3, T a4, T a5, T a6) const {
+    return c[5] * a0 + c[6] * a1 + c[7] * a2 + c[8] * a3 + c[9] * a4 + c[10] * a5 + c[11] * a6;
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Compensated FP32 stencil.
+//
+// On smooth data a second-difference stencil with coefficients ~1/h^2
+// cancels by 1e4-1e5 on a stretched 257-node line, so plain FP32 (and the
+// FP32 rounding of the coefficients) loses most digits.  Here each product
+// c*x is formed exactly (hi part by the FMA two-product, plus the lo part of
+// the coefficient) and summed with TwoSum compensation; only the result of
+// the cancellation is rounded to FP32.  The triangular sweeps that follow are
+// well conditioned and run in plain FP32.
+// Row layout: p, f, 1/c, d, e, r_hi[0..6], r_lo[0..6].
+constexpr int kRowF = 19;
+
+struct CompSum {
+  float s = 0.f, e = 0.f;
+  __device__ __forceinline__ void add(float chi, float clo, float x) {
+    const float p = chi * x;
+    const float pe = fmaf(chi, x, -p);
+    const float t = s + p;
+    const float bb = t - s;
+    const float te = (s - (t - bb)) + (p - bb);
+    s = t;
+    e += te + pe + clo * x;
+  }
+  __device__ __forceinline__ float value() const { return s + e; }
+};
+
+struct CompStencil {
+  __device__ __forceinline__ float row5(const float* c, float w0, float w1, float w2, float w3,
+                                        float w4) const {
+    CompSum cs;
+    cs.add(c[5], c[12], w0);
+    cs.add(c[6], c[13], w1);
+    cs.add(c[7], c[14], w2);
+    cs.add(c[8], c[15], w3);
+    cs.add(c[9], c[16], w4);
+    return cs.value();
+  }
+  __device__ __forceinline__ float row7(const float* c, float a0, float a1, float a2, float a3,
+                                        float a4, float a5, float a6) const {
+    CompSum cs;
+    cs.add(c[5], c[12], a0);
+    cs.add(c[6], c[13], a1);
+    cs.add(c[7], c[14], a2);
+    cs.add(c[8], c[15], a3);
+    cs.add(c[9], c[16], a4);
+    cs.add(c[10], c[17], a5);
+    cs.add(c[11], c[18], a6);
+    return cs.value();
+  }
+};
+
+// Loads issued this many steps ahead of their use in both sweeps (register
+// ring), so that one thread's walk along its line is not serialised on the
+// memory latency of every step.
+constexpr int kAhead = 8;
+
+// Solves one pencil.  `in` and `out` may alias (same type): every input
+// value is read before the store that could overwrite it.  The
+// forward-elimination values are parked in `out` and read back by the back
+// substitution, whose result goes through `fin(out, i, index, y)`.
+// R is the row stride of the packed coefficients C.
+template <int R, class T, class In, class Fin, class St>
+__device__ __forceinline__ void solve_line_impl(const T* __restrict__ C, int n, const In* in, T* out,
+                                                long long s, const LineBCT<T>& bc, const Fin& fin,
+                                                const St& st) {
+  const T f0 = load_as<T, In>(in, 0), f1 = load_as<T, In>(in, s), f2 = load_as<T, In>(in, 2 * s),
+          f3 = load_as<T, In>(in, 3 * s), f4 = load_as<T, In>(in, 4 * s),
+          f5 = load_as<T, In>(in, 5 * s), f6 = load_as<T, In>(in, 6 * s);
+  const T g0 = load_as<T, In>(in, (long long)(n - 7) * s), g1 = load_as<T, In>(in, (long long)(n - 6) * s),
+          g2 = load_as<T, In>(in, (long long)(n - 5) * s), g3 = load_as<T, In>(in, (long long)(n - 4) * s),
+          g4 = load_as<T, In>(in, (long long)(n - 3) * s), g5 = load_as<T, In>(in, (long long)(n - 2) * s),
+          g6 = load_as<T, In>(in, (long long)(n - 1) * s);
+  const T* c0 = C;
+  const T* c1 = C + R;
+  const T x0 = st.row7(c0, f0, f1, f2, f3, f4, f5, f6) + bc.c0 * bc.lo;
+  const T x1 = st.row7(c1, f0, f1, f2, f3, f4, f5, f6) + bc.c1 * bc.lo - x0 * c1[1];
   out[0] = x0;
   out[s] = x1;
-  double xm2 = x0, xm1 = x1;
-  double w0 = f0, w1 = f1, w2 = f2, w3 = f3, w4 = f4;
-  for (int i = 2; i < n - 2; ++i) {
-    const double* c = C + kRow * i;
-    const double b = c[5] * w0 + c[6] * w1 + c[7] * w2 + c[8] * w3 + c[9] * w4;
-    const double x = b - c[0] * xm2 - c[1] * xm1;
+  T xm2 = x0, xm1 = x1;
+  T w0 = f0, w1 = f1, w2 = f2, w3 = f3, w4 = f4;
+  // forward sweep, rows 2 .. n-3; pf[u] = in(i + 3 + u)
+  T pf[kAhead];
+#pragma unroll
+  for (int u = 0; u < kAhead; ++u) pf[u] = (5 + u < n) ? load_as<T, In>(in, (long long)(5 + u) * s) : T(0);
+  int i = 2;
+  for (; i + kAhead <= n - 2; i += kAhead) {
+    T nb[kAhead];
+#pragma unroll
+    for (int u = 0; u < kAhead; ++u) {
+      const int j = i + 3 + kAhead + u;
+      nb[u] = (j < n) ? load_as<T, In>(in, (long long)j * s) : T(0);
+    }
+#pragma unroll
+    for (int u = 0; u < kAhead; ++u) {
+      const T* c = C + R * (i + u);
+      const T x = st.row5(c, w0, w1, w2, w3, w4) - c[0] * xm2 - c[1] * xm1;
+      w0 = w1; w1 = w2; w2 = w3; w3 = w4; w4 = pf[u];
+      out[(long long)(i + u) * s] = x;
+      xm2 = xm1;
+      xm1 = x;
+    }
+#pragma unroll
+    for (int u = 0; u < kAhead; ++u) pf[u] = nb[u];
+  }
+  for (; i < n - 2; ++i) {
+    const T* c = C + R * i;
+    const T x = st.row5(c, w0, w1, w2, w3, w4) - c[0] * xm2 - c[1] * xm1;
     w0 = w1; w1 = w2; w2 = w3; w3 = w4;
-    if (i + 3 < n) w4 = in[(long long)(i + 3) * s];
+    if (i + 3 < n) w4 = load_as<T, In>(in, (long long)(i + 3) * s);
     out[(long long)i * s] = x;
     xm2 = xm1;
     xm1 = x;
   }
-  const double* cA = C + kRow * (n - 2);
-  const double* cB = C + kRow * (n - 1);
-  const double bA = cA[5] * g0 + cA[6] * g1 + cA[7] * g2 + cA[8] * g3 + cA[9] * g4 +
-                    cA[10] * g5 + cA[11] * g6 + bc.c2 * bc.hi;
-  const double xA = bA - cA[0] * xm2 - cA[1] * xm1;
-  const double bB = cB[5] * g0 + cB[6] * g1 + cB[7] * g2 + cB[8] * g3 + cB[9] * g4 +
-                    cB[10] * g5 + cB[11] * g6 + bc.c3 * bc.hi;
-  const double xB = bB - cB[0] * xm1 - cB[1] * xA - cB[4] * xm2;  // e(n) holds beta
-  const double yB = xB * cB[2];
-  const double yA = (xA - cA[3] * yB) * cA[2];
-  fin(out, (long long)(n - 1) * s, yB);
-  fin(out, (long long)(n - 2) * s, yA);
-  double y2 = yB, y1 = yA, y3 = 0.0;
-  for (int i = n - 3; i >= 1; --i) {
-    const double* c = C + kRow * i;
-    const double y = (out[(long long)i * s] - c[4] * y2 - c[3] * y1) * c[2];
-    fin(out, (long long)i * s, y);
+  const T* cA = C + R * (n - 2);
+  const T* cB = C + R * (n - 1);
+  const T xA = st.row7(cA, g0, g1, g2, g3, g4, g5, g6) + bc.c2 * bc.hi - cA[0] * xm2 - cA[1] * xm1;
+  const T xB = st.row7(cB, g0, g1, g2, g3, g4, g5, g6) + bc.c3 * bc.hi - cB[0] * xm1 - cB[1] * xA -
+               cB[4] * xm2;  // e(n) holds beta
+  // back substitution; rb[u] = forward value of row i - u
+  const T yB = xB * cB[2];
+  const T yA = (xA - cA[3] * yB) * cA[2];
+  fin(out, n - 1, (long long)(n - 1) * s, yB);
+  fin(out, n - 2, (long long)(n - 2) * s, yA);
+  T y2 = yB, y1 = yA, y3 = 0;
+  i = n - 3;
+  T rb[kAhead];
+#pragma unroll
+  for (int u = 0; u < kAhead; ++u) rb[u] = (i - u >= 1) ? out[(long long)(i - u) * s] : T(0);
+  for (; i - (kAhead - 1) >= 1; i -= kAhead) {
+    T nb[kAhead];
+#pragma unroll
+    for (int u = 0; u < kAhead; ++u) {
+      const int j = i - kAhead - u;
+      nb[u] = (j >= 1) ? out[(long long)j * s] : T(0);
+    }
+#pragma unroll
+    for (int u = 0; u < kAhead; ++u) {
+      const T* c = C + R * (i - u);
+      const T y = (rb[u] - c[4] * y2 - c[3] * y1) * c[2];
+      fin(out, i - u, (long long)(i - u) * s, y);
+      y3 = y2;
+      y2 = y1;
+      y1 = y;
+    }
+#pragma unroll
+    for (int u = 0; u < kAhead; ++u) rb[u] = nb[u];
+  }
+  for (; i >= 1; --i) {
+    const T* c = C + R * i;
+    const T y = (out[(long long)i * s] - c[4] * y2 - c[3] * y1) * c[2];
+    fin(out, i, (long long)i * s, y);
     y3 = y2;
     y2 = y1;
     y1 = y;
   }
-  const double y0 = (out[0] - c0[4] * y2 - c0[3] * y1 - c0[0] * y3) * c0[2];
-  fin(out, 0, y0);
+  const T y0 = (out[0] - c0[4] * y2 - c0[3] * y1 - c0[0] * y3) * c0[2];
+  fin(out, 0, 0, y0);
+}
+
+template <class T, class In, class Fin>
+__device__ __forceinline__ void solve_line(const T* __restrict__ C, int n, const In* in, T* out,
+                                           long long s, const LineBCT<T>& bc, const Fin& fin) {
+  solve_line_impl<kRow>(C, n, in, out, s, bc, fin, PlainStencil<T>());
+}
+
+template <class Fin>
+__device__ __forceinline__ void solve_line_comp(const float* __restrict__ C, int n, const float* in,
+                                                float* out, long long s, const Fin& fin) {
+  solve_line_impl<kRowF>(C, n, in, out, s, LineBCT<float>(), fin, CompStencil());
 }
 
 }  // namespace mf

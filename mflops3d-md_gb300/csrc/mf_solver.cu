@@ -42,6 +42,8 @@ struct AxisDev {
   double neum[14] = {0};
   DevBuf V, Vinv, eig, invl4, rows;           // FP64
   DevBuf Vh, Vl, Vih, Vil, eigf, nullf;       // mixed path (padded P x P)
+  DevBuf invl4f;                               // FP32 copy of invl4
+  DevBuf rowsf;                                // FP32 copy of rows
 };
 
 }  // namespace mf
@@ -54,9 +56,11 @@ struct mf_solver3d {
   int P[3] = {0, 0, 0};
   DevBuf w0, w1;                               // FP64 work arrays (plain path)
   DevBuf st_rhs, st_solf, st_bc[3];            // host staging
-  DevBuf U, R, R2;                             // mixed path FP64 arrays
+  DevBuf R, R2;                                // FP64 scratch of the residual
+  DevBuf U32, C32, R1f;                        // mixed path: u1, correction, r1 (FP32)
   DevBuf Xa_hi, Xa_lo, Xb_hi, Xb_lo;           // mixed path split planes
   DevBuf err;                                  // device error flag (int)
+  DevBuf foldf;                                // FP32 c*bc face products (mixed path)
   TcPlan* plan[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   bool mixed_ready = false;
   StageProfiler prof;
@@ -216,70 +220,121 @@ __global__ void k_faces(double* solf, const double* __restrict__ bc, FaceArgs f)
   }
 }
 
-// ---- FP64 residual r = g - sigma*u - (Lx + Ly + Lz) u, boundary data included
-
-struct StoreSub {
-  const double* rin;
-  __device__ __forceinline__ void operator()(double* out, long long idx, double y) const {
-    out[idx] = rin[idx] - y;
+// ---- residuals of the iterative refinement
+//
+// r = rin - sigma*u - (Lx + Ly + Lz) u, boundary data included, in three
+// passes with one thread per line; lines are numbered so that a warp covers
+// 32 neighbouring lines.  For y and z every step of the recurrence is then a
+// coalesced access; for x the 32 lines are 4-8*n1 bytes apart and each
+// thread walks its own cache lines, which stay in L1 while it consumes them.
+// Many resident warps hide the latency of the dependent chains.
+// T is the arithmetic type (double: the residual of the first approximate
+// solution u1; float: the residual update r1 - A*C of the accumulated
+// correction C), In the storage type of the differentiated array.
+// The forward-elimination values go to a scratch array; the final store:
+//   mode 0 (first pass):  out = rin - sigma*u - L u
+//   mode 1 (middle pass): out = rin - L u
+//   mode 2 (last pass):   split-BF16 planes of rin - L u in the padded
+//                         (P1,P2,P3) layout of the tensor-core transforms
+//   mode 3 (last pass):   mode 2, and rin - L u also stored as FP32 (r32).
+template <class T, class In>
+struct ResidFin {
+  int mode;
+  const T* rin;          // offset to the line
+  const In* u;           // mode 0, offset to the line
+  T sigma;
+  T* out;                // modes 0,1: result array, offset to the line
+  __nv_bfloat16* hi;     // modes 2,3: planes, offset to the line's padded base
+  __nv_bfloat16* lo;
+  long long pstride;     // modes 2,3: padded stride along the line
+  float* r32;            // mode 3: offset to the line
+  __device__ __forceinline__ void operator()(T*, int i, long long idx, T y) const {
+    if (mode == 0) {
+      out[idx] = rin[idx] - sigma * load_as<T, In>(u, idx) - y;
+    } else if (mode == 1) {
+      out[idx] = rin[idx] - y;
+    } else {
+      const float v = (float)(rin[idx] - y);
+      const __nv_bfloat16 h = __float2bfloat16_rn(v);
+      hi[i * pstride] = h;
+      lo[i * pstride] = __float2bfloat16_rn(v - __bfloat162float(h));
+      if (mode == 3) r32[idx] = v;
+    }
   }
 };
 
-constexpr int kResLines = 32;
+template <class T>
+struct ResidPass {
+  const T* rows;       // packed operator rows of this axis
+  int n;               // line length
+  int na, nb;          // line grid
+  long long sa, sb, s; // strides of the line grid and along the line
+  const double* bc;    // bc(na, nb, 2), or null for homogeneous data
+  double4 bcc;
+  int mode;
+  T sigma;
+  long long pa, pb, pstride;  // modes 2,3: padded strides of (a, b) and along the line
+};
 
-// x pass: r = g - sigma*u - Lx u (x lines staged in shared memory).
-__global__ void __launch_bounds__(32) k_resid_x(const double* __restrict__ rows, const double* u,
-                                                const double* __restrict__ g, double sigma,
-                                                const double* __restrict__ bcx, double4 bcc,
-                                                double* __restrict__ r, int n1, int n2, int n3,
-                                                int pitch) {
-  extern __shared__ double tile[];
-  const int lane = threadIdx.x;
-  const long long nlines = (long long)n2 * n3;
-  const long long l0 = (long long)blockIdx.x * kResLines;
-  const int nl = (int)min((long long)kResLines, nlines - l0);
-  for (int l = 0; l < nl; ++l) {
-    const double* src = u + (l0 + l) * n1;
-    for (int i = lane; i < n1; i += 32) tile[l * pitch + i] = src[i];
-  }
-  __syncwarp();
-  if (lane < nl) {
-    const long long line = l0 + lane;
-    LineBC bc;
-    bc.lo = bcx[line];
-    bc.hi = bcx[line + nlines];
-    bc.c0 = bcc.x; bc.c1 = bcc.y; bc.c2 = bcc.z; bc.c3 = bcc.w;
-    double* row = tile + lane * pitch;
-    solve_line(rows, n1, row, row, 1, bc, StorePlain());
-  }
-  __syncwarp();
-  for (int l = 0; l < nl; ++l) {
-    const long long base = (l0 + l) * n1;
-    for (int i = lane; i < n1; i += 32)
-      r[base + i] = g[base + i] - sigma * u[base + i] - tile[l * pitch + i];
-  }
-}
-
-// y or z pass: rout = rin - L u, one thread per line, coalesced along x.
-__global__ void k_resid_strided(const double* __restrict__ rows, int n, const double* u,
-                                const double* rin, double* rout, const double* __restrict__ bc,
-                                double4 bcc, int na, int nb, long long sa, long long sb,
-                                long long s) {
+template <class T, class In>
+__global__ void __launch_bounds__(128) k_resid_lines(ResidPass<T> p, const In* u, const T* rin,
+                                                     T* scratch, T* rout, __nv_bfloat16* hi,
+                                                     __nv_bfloat16* lo, float* r32) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (long long)na * nb) return;
-  const int a = (int)(t % na), b = (int)(t / na);
-  const long long base = a * sa + b * sb;
-  LineBC lb;
-  lb.lo = bc[t];
-  lb.hi = bc[t + (long long)na * nb];
-  lb.c0 = bcc.x; lb.c1 = bcc.y; lb.c2 = bcc.z; lb.c3 = bcc.w;
-  solve_line(rows, n, u + base, rout + base, s, lb, StoreSub{rin + base});
+  if (t >= (long long)p.na * p.nb) return;
+  const int a = (int)(t % p.na), b = (int)(t / p.na);
+  const long long base = a * p.sa + b * p.sb;
+  LineBCT<T> lb;
+  if (p.bc) {
+    lb.lo = (T)p.bc[t];
+    lb.hi = (T)p.bc[t + (long long)p.na * p.nb];
+    lb.c0 = (T)p.bcc.x; lb.c1 = (T)p.bcc.y; lb.c2 = (T)p.bcc.z; lb.c3 = (T)p.bcc.w;
+  }
+  ResidFin<T, In> fin;
+  fin.mode = p.mode;
+  fin.rin = rin + base;
+  fin.u = u + base;
+  fin.sigma = p.sigma;
+  fin.out = rout ? rout + base : nullptr;
+  const long long pbase = a * p.pa + b * p.pb;
+  fin.hi = hi ? hi + pbase : nullptr;
+  fin.lo = lo ? lo + pbase : nullptr;
+  fin.pstride = p.pstride;
+  fin.r32 = r32 ? r32 + base : nullptr;
+  if constexpr (sizeof(T) == 4)
+    solve_line_comp(p.rows, p.n, u + base, scratch + base, p.s, fin);
+  else
+    solve_line(p.rows, p.n, u + base, scratch + base, p.s, lb, fin);
 }
 
-// FP64 interior array -> split-BF16 planes in the padded (P1,P2,P3) layout.
-__global__ void k_split_in(const double* __restrict__ r, __nv_bfloat16* __restrict__ hi,
-                           __nv_bfloat16* __restrict__ lo, int n1, int n2, int n3, int P1, int P2,
-                           int P3) {
+// solf(1:n1,1:n2,1:n3) = u1 + C, widened exactly and summed in FP64.
+__global__ void k_finalize(const float* __restrict__ u1, const float* __restrict__ c,
+                           double* __restrict__ solf, int n1, int n2, int n3) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long tot = (long long)n1 * n2 * n3;
+  if (idx >= tot) return;
+  const int i = (int)(idx % n1);
+  const long long jk = idx / n1;
+  const int j = (int)(jk % n2), k = (int)(jk / n2);
+  double v = widen(u1[idx]);
+  if (c) v += widen(c[idx]);
+  solf[(i + 1) + (long long)(n1 + 2) * ((j + 1) + (long long)(n2 + 2) * (k + 1))] = v;
+}
+
+// rhs minus the boundary folds, in FP32, split straight into BF16 planes
+// (padded layout).  Only feeds the first approximate solve of the mixed
+// path: the FP64 residual that follows carries the boundary data exactly.
+struct FoldArgsF {
+  const float* ix[4];
+  const float* iy[4];
+  const float* iz[4];
+  const float* bx;  // c * bc products, [4][n2*n3] etc.
+  const float* by;
+  const float* bz;
+};
+
+__global__ void k_fold_split(const double* __restrict__ rhs, FoldArgsF a, __nv_bfloat16* hi,
+                             __nv_bfloat16* lo, int n1, int n2, int n3, int P1, int P2, int P3) {
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long tot = (long long)P1 * P2 * P3;
   if (idx >= tot) return;
@@ -287,23 +342,33 @@ __global__ void k_split_in(const double* __restrict__ r, __nv_bfloat16* __restri
   const long long jk = idx / P1;
   const int j = (int)(jk % P2), k = (int)(jk / P2);
   float v = 0.f;
-  if (i < n1 && j < n2 && k < n3) v = (float)r[i + (long long)n1 * (j + (long long)n2 * k)];
+  if (i < n1 && j < n2 && k < n3) {
+    v = (float)rhs[i + (long long)n1 * (j + (long long)n2 * k)];
+    const long long fx = j + (long long)n2 * k, fy = i + (long long)n1 * k, fz = i + (long long)n1 * j;
+    const long long sx = (long long)n2 * n3, sy = (long long)n1 * n3, sz = (long long)n1 * n2;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      v -= a.ix[c][i] * a.bx[c * sx + fx];
+      v -= a.iy[c][j] * a.by[c * sy + fy];
+      v -= a.iz[c][k] * a.bz[c * sz + fz];
+    }
+  }
   const __nv_bfloat16 h = __float2bfloat16_rn(v);
   hi[idx] = h;
   lo[idx] = __float2bfloat16_rn(v - __bfloat162float(h));
 }
 
-// Copies the FP64 interior u (n1,n2,n3) into solf(1:n1,1:n2,1:n3).
-__global__ void k_copy_interior(const double* __restrict__ u, double* __restrict__ solf, int n1,
-                                int n2, int n3) {
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const long long tot = (long long)n1 * n2 * n3;
-  if (idx >= tot) return;
-  const int i = (int)(idx % n1);
-  const long long jk = idx / n1;
-  const int j = (int)(jk % n2), k = (int)(jk / n2);
-  solf[(i + 1) + (long long)(n1 + 2) * ((j + 1) + (long long)(n2 + 2) * (k + 1))] = u[idx];
+// c * bc face products of the fold, in FP32: out[c][face point].
+__global__ void k_fold_faces(const double* __restrict__ bc, double4 cc, float* out, long long nf) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nf) return;
+  const double lo = bc[t], hi = bc[t + nf];
+  out[t] = (float)(cc.x * lo);
+  out[t + nf] = (float)(cc.y * lo);
+  out[t + 2 * nf] = (float)(cc.z * hi);
+  out[t + 3 * nf] = (float)(cc.w * hi);
 }
+
 
 // Extracts the interior of a (nx,ny,nz) field into an (nx-2,ny-2,nz-2) array.
 __global__ void k_extract_interior(const double* __restrict__ g, double* __restrict__ out, int n1,
@@ -321,7 +386,8 @@ static inline unsigned blocks_for(long long n, int t) { return (unsigned)((n + t
 
 // Profiler kinds (see mf_solver3d_profile_read in the C ABI).
 enum ProfKind { kProfTc = 0, kProfResidX = 1, kProfResidYZ = 2, kProfSplit = 3, kProfFold = 4,
-                kProfFaces = 5, kProfGemm64 = 6, kProfCopy = 7 };
+                kProfFaces = 5, kProfGemm64 = 6, kProfCopy = 7, kProfTcDivide = 8,
+                kProfTcUpdate = 9, kProfResid32 = 10 };
 
 // ---------------------------------------------------------------------------
 // Host orchestration
@@ -385,6 +451,8 @@ static int axis_upload(AxisDev& d, const SolverAxisHost& h) {
   for (int c = 0; c < 4; ++c)
     for (int i = 0; i < n; ++i) l4[(size_t)c * n + i] = h.inv_lhs[(size_t)i * n + cols[c]];
   if ((rc = upload(d.invl4, l4))) return rc;
+  std::vector<float> l4f(l4.begin(), l4.end());
+  if ((rc = upload(d.invl4f, l4f))) return rc;
   // residual operator rows: factored lhs + 7-wide explicit stencil (see mf_line.cuh)
   std::vector<double> rows((size_t)kRow * n, 0.0);
   for (int i = 0; i < n; ++i) {
@@ -408,6 +476,20 @@ static int axis_upload(AxisDev& d, const SolverAxisHost& h) {
     }
   }
   if ((rc = upload(d.rows, rows))) return rc;
+  // FP32 rows for the correction residual: factored lhs rounded, explicit
+  // stencil as hi + lo pairs (see solve_line_comp)
+  std::vector<float> rowsf((size_t)kRowF * n, 0.f);
+  for (int i = 0; i < n; ++i) {
+    const double* r = &rows[(size_t)kRow * i];
+    float* o = &rowsf[(size_t)kRowF * i];
+    for (int m = 0; m < 5; ++m) o[m] = (float)r[m];
+    for (int m = 0; m < 7; ++m) {
+      const float hi = (float)r[5 + m];
+      o[5 + m] = hi;
+      o[12 + m] = (float)(r[5 + m] - (double)hi);
+    }
+  }
+  if ((rc = upload(d.rowsf, rowsf))) return rc;
   return axis_set_eigen(d, h.eigen, h.vect, h.inv_vect);
 }
 
@@ -498,42 +580,57 @@ static int solve_plain_dev(mf_solver3d* sc, const double* rhs, double sigma, dou
   return faces(sc, solf, bcs, st);
 }
 
-// FP64 residual on device pointers: r = g - sigma*u - sum_a L_a u.
-static int residual_dev(mf_solver3d* sc, const double* g, const double* u, double sigma,
-                        const double* bcs[3], double* r, double* tmp, cudaStream_t st) {
-  const int n1 = sc->n[0], n2 = sc->n[1], n3 = sc->n[2];
-  auto bcc = [&](int a) {
-    return make_double4(sc->ax[a].bcc[0], sc->ax[a].bcc[1], sc->ax[a].bcc[2], sc->ax[a].bcc[3]);
+// Residual on device pointers, three passes (x, y, z):
+//   r = rin - sigma*u - sum_a L_a u.
+// rin/u/bcs describe the problem (bcs may be null: homogeneous data).  The
+// last pass writes the FP64/FP32 array `r` (when planes are null) or the
+// split-BF16 planes (and, with r32, an FP32 copy of r).
+template <class T, class In>
+static int residual_passes(mf_solver3d* sc, const T* rin, const In* u, double sigma,
+                           const double* bcs[3], T* s0, T* s1, T* r, __nv_bfloat16* hi,
+                           __nv_bfloat16* lo, float* r32, int prof_kind_x, int prof_kind_yz,
+                           cudaStream_t st) {
+  const long long n1 = sc->n[0], n2 = sc->n[1], n3 = sc->n[2];
+  auto pass = [&](int axis) {
+    ResidPass<T> p;
+    const AxisDev& d = sc->ax[axis];
+    p.rows = sizeof(T) == 8 ? reinterpret_cast<const T*>(d.rows.ptr) : reinterpret_cast<const T*>(d.rowsf.ptr);
+    p.n = d.n;
+    p.bc = bcs ? bcs[axis] : nullptr;
+    p.bcc = make_double4(d.bcc[0], d.bcc[1], d.bcc[2], d.bcc[3]);
+    p.sigma = (T)sigma;
+    p.pa = p.pb = p.pstride = 0;
+    if (axis == 0) { p.na = (int)n2; p.nb = (int)n3; p.sa = n1; p.sb = n1 * n2; p.s = 1; }
+    if (axis == 1) { p.na = (int)n1; p.nb = (int)n3; p.sa = 1; p.sb = n1 * n2; p.s = n1; }
+    if (axis == 2) { p.na = (int)n1; p.nb = (int)n2; p.sa = 1; p.sb = n1; p.s = n1 * n2; }
+    return p;
   };
-  const int pitch = n1 | 1;
-  const size_t smem = (size_t)kResLines * pitch * sizeof(double);
-  if (smem > 200 * 1024) return set_error(MF_ERR_UNSUPPORTED, "residual: n1=%d too large", n1);
-  static bool attr = false;
-  if (!attr) {
-    MF_CUDA(cudaFuncSetAttribute(k_resid_x, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-    attr = true;
+  auto launch = [&](const ResidPass<T>& p, int kind, const T* in_r, T* scratch, T* rout,
+                    __nv_bfloat16* h, __nv_bfloat16* l, float* r32p) -> int {
+    sc->prof.begin(kind, st);
+    k_resid_lines<T, In><<<blocks_for((long long)p.na * p.nb, 128), 128, 0, st>>>(
+        p, u, in_r, scratch, rout, h, l, r32p);
+    sc->prof.end(st);
+    MF_CUDA(cudaGetLastError());
+    return MF_OK;
+  };
+  int rc;
+  ResidPass<T> px = pass(0);
+  px.mode = 0;
+  if ((rc = launch(px, prof_kind_x, rin, s0, s0, nullptr, nullptr, nullptr))) return rc;
+  ResidPass<T> py = pass(1);
+  py.mode = 1;
+  if ((rc = launch(py, prof_kind_yz, s0, s1, s1, nullptr, nullptr, nullptr))) return rc;
+  ResidPass<T> pz = pass(2);
+  if (hi) {
+    pz.mode = r32 ? 3 : 2;
+    pz.pa = 1;
+    pz.pb = sc->P[0];
+    pz.pstride = (long long)sc->P[0] * sc->P[1];
+    return launch(pz, prof_kind_yz, s1, s0, nullptr, hi, lo, r32);
   }
-  const long long xl = (long long)n2 * n3;
-  // x pass -> r; y pass r -> tmp; z pass tmp -> r
-  sc->prof.begin(kProfResidX, st);
-  k_resid_x<<<blocks_for(xl, kResLines), 32, smem, st>>>(sc->ax[0].rows.as<double>(), u, g, sigma,
-                                                         bcs[0], bcc(0), r, n1, n2, n3, pitch);
-  sc->prof.end(st);
-  MF_CUDA(cudaGetLastError());
-  // y lines (i,k): stride n1
-  sc->prof.begin(kProfResidYZ, st);
-  k_resid_strided<<<blocks_for((long long)n1 * n3, 128), 128, 0, st>>>(
-      sc->ax[1].rows.as<double>(), n2, u, r, tmp, bcs[1], bcc(1), n1, n3, 1, (long long)n1 * n2, n1);
-  sc->prof.end(st);
-  MF_CUDA(cudaGetLastError());
-  // z lines (i,j): stride n1*n2
-  sc->prof.begin(kProfResidYZ, st);
-  k_resid_strided<<<blocks_for((long long)n1 * n2, 128), 128, 0, st>>>(
-      sc->ax[2].rows.as<double>(), n3, u, tmp, r, bcs[2], bcc(2), n1, n2, 1, n1,
-      (long long)n1 * n2);
-  sc->prof.end(st);
-  MF_CUDA(cudaGetLastError());
-  return MF_OK;
+  pz.mode = 1;
+  return launch(pz, prof_kind_yz, s1, r, r, nullptr, nullptr, nullptr);
 }
 
 static int mixed_prepare(mf_solver3d* sc) {
@@ -546,7 +643,8 @@ static int mixed_prepare(mf_solver3d* sc) {
   const long long tot = (long long)sc->n[0] * sc->n[1] * sc->n[2];
   const long long ptot = (long long)sc->P[0] * sc->P[1] * sc->P[2];
   int rc;
-  if ((rc = sc->U.ensure(tot * 8)) || (rc = sc->R.ensure(tot * 8)) || (rc = sc->R2.ensure(tot * 8)))
+  if ((rc = sc->R.ensure(tot * 8)) || (rc = sc->R2.ensure(tot * 8)) || (rc = sc->U32.ensure(tot * 4)) ||
+      (rc = sc->C32.ensure(tot * 4)) || (rc = sc->R1f.ensure(tot * 4)))
     return rc;
   if ((rc = sc->Xa_hi.ensure(ptot * 2)) || (rc = sc->Xa_lo.ensure(ptot * 2)) ||
       (rc = sc->Xb_hi.ensure(ptot * 2)) || (rc = sc->Xb_lo.ensure(ptot * 2)))
@@ -576,15 +674,14 @@ static int mixed_prepare(mf_solver3d* sc) {
 }
 
 static int tc_run(mf_solver3d* sc, int t, const TcEpilogue& e, cudaStream_t st) {
-  sc->prof.begin(kProfTc, st);
+  sc->prof.begin(e.kind == 0 ? kProfTc : e.kind == 1 ? kProfTcDivide : kProfTcUpdate, st);
   int rc = tc_transform(sc->plan[t], e, sc->err.as<int>(), st);
   sc->prof.end(st);
   return rc;
 }
 
 // One approximate solve of the folded right-hand side already split into Xa.
-static int approx_solve(mf_solver3d* sc, double sigma, bool accumulate, cudaStream_t st) {
-  int* err = sc->err.as<int>();
+static int approx_solve(mf_solver3d* sc, double sigma, float* dest, bool accumulate, cudaStream_t st) {
   auto bf = [](DevBuf& b) { return b.as<__nv_bfloat16>(); };
   TcEpilogue e;
   int rc;
@@ -613,24 +710,54 @@ static int approx_solve(mf_solver3d* sc, double sigma, bool accumulate, cudaStre
   if ((rc = tc_run(sc, 4, e, st))) return rc;
   TcEpilogue u;
   u.kind = 2;
-  u.u = sc->U.as<double>();
+  u.out = dest;
   u.accumulate = accumulate ? 1 : 0;
   u.n1 = sc->n[0]; u.n2 = sc->n[1]; u.n3 = sc->n[2];
   u.P1 = sc->P[0]; u.P2 = sc->P[1];
   return tc_run(sc, 5, u, st);
 }
 
-static int split_r(mf_solver3d* sc, const double* r, cudaStream_t st) {
+// First right-hand side of the mixed path: FP32 fold + split into Xa.
+static int fold_split(mf_solver3d* sc, const double* rhs, const double* bcs[3], cudaStream_t st) {
+  const long long n1 = sc->n[0], n2 = sc->n[1], n3 = sc->n[2];
+  const long long nf[3] = {n2 * n3, n1 * n3, n1 * n2};
+  int rc;
+  if ((rc = sc->foldf.ensure(sizeof(float) * 4 * (nf[0] + nf[1] + nf[2])))) return rc;
+  float* f = sc->foldf.as<float>();
+  float* fa[3] = {f, f + 4 * nf[0], f + 4 * (nf[0] + nf[1])};
+  sc->prof.begin(kProfFold, st);
+  for (int a = 0; a < 3; ++a) {
+    const AxisDev& d = sc->ax[a];
+    k_fold_faces<<<blocks_for(nf[a], 256), 256, 0, st>>>(
+        bcs[a], make_double4(d.bcc[0], d.bcc[1], d.bcc[2], d.bcc[3]), fa[a], nf[a]);
+  }
+  FoldArgsF args;
+  for (int c = 0; c < 4; ++c) {
+    args.ix[c] = sc->ax[0].invl4f.as<float>() + (size_t)c * n1;
+    args.iy[c] = sc->ax[1].invl4f.as<float>() + (size_t)c * n2;
+    args.iz[c] = sc->ax[2].invl4f.as<float>() + (size_t)c * n3;
+  }
+  args.bx = fa[0];
+  args.by = fa[1];
+  args.bz = fa[2];
   const long long ptot = (long long)sc->P[0] * sc->P[1] * sc->P[2];
-  sc->prof.begin(kProfSplit, st);
-  k_split_in<<<blocks_for(ptot, 256), 256, 0, st>>>(r, sc->Xa_hi.as<__nv_bfloat16>(),
-                                                    sc->Xa_lo.as<__nv_bfloat16>(), sc->n[0],
-                                                    sc->n[1], sc->n[2], sc->P[0], sc->P[1], sc->P[2]);
+  k_fold_split<<<blocks_for(ptot, 256), 256, 0, st>>>(rhs, args, sc->Xa_hi.as<__nv_bfloat16>(),
+                                                      sc->Xa_lo.as<__nv_bfloat16>(), (int)n1, (int)n2,
+                                                      (int)n3, sc->P[0], sc->P[1], sc->P[2]);
   sc->prof.end(st);
   MF_CUDA(cudaGetLastError());
   return MF_OK;
 }
 
+// Mixed-precision solve:
+//   u1 = S~ (rhs - fold)                        (FP32 fold, tensor-core solve)
+//   r1 = rhs - A u1                             (FP64 residual, boundary data)
+//   C  = S~ r1;  for k >= 2: r_k = r1 - A C     (FP32 residual update)
+//                            C += S~ r_k
+//   solf = u1 + C                               (widened, summed in FP64)
+// S~ is the split-BF16 approximate inverse (six tensor-core transforms).  The
+// cancellation in r_k = r1 - A C is relative to |r1| (~1e-5 |rhs|), so FP32
+// keeps it to ~1e-12 |rhs|; the FP64 residual of u1 carries the accuracy.
 static int solve_mixed_dev(mf_solver3d* sc, const double* rhs, double sigma, double* solf,
                            const double* bcs[3], int prec, int refine, cudaStream_t st) {
   if (prec != MF_PREC_SPLIT_BF16)
@@ -639,22 +766,30 @@ static int solve_mixed_dev(mf_solver3d* sc, const double* rhs, double sigma, dou
   if ((rc = mixed_prepare(sc))) return rc;
   const int n1 = sc->n[0], n2 = sc->n[1], n3 = sc->n[2];
   const long long tot = (long long)n1 * n2 * n3;
-  double* R = sc->R.as<double>();
-  sc->prof.begin(kProfFold, st);
-  k_fold<<<blocks_for(tot, 256), 256, 0, st>>>(rhs, R, bcs[0], bcs[1], bcs[2], fold_args(sc), n1,
-                                               n2, n3);
-  sc->prof.end(st);
-  MF_CUDA(cudaGetLastError());
-  if ((rc = split_r(sc, R, st))) return rc;
-  if ((rc = approx_solve(sc, sigma, false, st))) return rc;
+  __nv_bfloat16* xh = sc->Xa_hi.as<__nv_bfloat16>();
+  __nv_bfloat16* xl = sc->Xa_lo.as<__nv_bfloat16>();
+  float* u1 = sc->U32.as<float>();
+  float* C = sc->C32.as<float>();
+  if ((rc = fold_split(sc, rhs, bcs, st))) return rc;
+  if ((rc = approx_solve(sc, sigma, u1, false, st))) return rc;
   for (int it = 0; it < refine; ++it) {
-    if ((rc = residual_dev(sc, rhs, sc->U.as<double>(), sigma, bcs, R, sc->R2.as<double>(), st)))
-      return rc;
-    if ((rc = split_r(sc, R, st))) return rc;
-    if ((rc = approx_solve(sc, sigma, true, st))) return rc;
+    if (it == 0) {
+      if ((rc = residual_passes<double, float>(sc, rhs, u1, sigma, bcs, sc->R.as<double>(),
+                                               sc->R2.as<double>(), (double*)nullptr, xh, xl,
+                                               sc->R1f.as<float>(), kProfResidX, kProfResidYZ, st)))
+        return rc;
+    } else {
+      float* f0 = reinterpret_cast<float*>(sc->R.ptr);
+      float* f1 = reinterpret_cast<float*>(sc->R2.ptr);
+      if ((rc = residual_passes<float, float>(sc, sc->R1f.as<float>(), C, sigma, nullptr, f0, f1,
+                                              (float*)nullptr, xh, xl, nullptr, kProfResid32,
+                                              kProfResid32, st)))
+        return rc;
+    }
+    if ((rc = approx_solve(sc, sigma, C, it > 0, st))) return rc;
   }
   sc->prof.begin(kProfCopy, st);
-  k_copy_interior<<<blocks_for(tot, 256), 256, 0, st>>>(sc->U.as<double>(), solf, n1, n2, n3);
+  k_finalize<<<blocks_for(tot, 256), 256, 0, st>>>(u1, refine > 0 ? C : nullptr, solf, n1, n2, n3);
   sc->prof.end(st);
   MF_CUDA(cudaGetLastError());
   return faces(sc, solf, bcs, st);
@@ -699,12 +834,12 @@ int mf_solver3d_destroy(mf_solver3d_t* sc) {
   for (int t = 0; t < 6; ++t) tc_plan_destroy(sc->plan[t]);
   for (auto& d : sc->ax) {
     for (DevBuf* b : {&d.V, &d.Vinv, &d.eig, &d.invl4, &d.rows, &d.Vh, &d.Vl, &d.Vih, &d.Vil,
-                      &d.eigf, &d.nullf})
+                      &d.eigf, &d.nullf, &d.invl4f, &d.rowsf})
       b->release();
   }
   for (DevBuf* b : {&sc->w0, &sc->w1, &sc->st_rhs, &sc->st_solf, &sc->st_bc[0], &sc->st_bc[1],
-                    &sc->st_bc[2], &sc->U, &sc->R, &sc->R2, &sc->Xa_hi, &sc->Xa_lo, &sc->Xb_hi,
-                    &sc->Xb_lo, &sc->err})
+                    &sc->st_bc[2], &sc->R, &sc->R2, &sc->Xa_hi, &sc->Xa_lo, &sc->Xb_hi,
+                    &sc->Xb_lo, &sc->err, &sc->foldf, &sc->U32, &sc->C32, &sc->R1f})
     b->release();
   delete sc;
   return MF_OK;
@@ -887,10 +1022,12 @@ int mf_solver_residual(mf_solver3d_t* sc, const double* g, const double* u, doub
                         (const void*)bcz, (const void*)r})
     if (!is_device_ptr(p)) return set_error(MF_ERR_ARG, "mf_solver_residual: device pointers only");
   int rc;
-  if ((rc = sc->R2.ensure((size_t)n1 * n2 * n3 * 8))) return rc;
+  const size_t tb = (size_t)n1 * n2 * n3 * 8;
+  if ((rc = sc->R.ensure(tb)) || (rc = sc->R2.ensure(tb))) return rc;
   const double* bcs[3] = {bcx, bcy, bcz};
-  return residual_dev(sc, g, u, sigma, bcs, r, sc->R2.as<double>(),
-                      static_cast<cudaStream_t>(stream));
+  return residual_passes<double, double>(sc, g, u, sigma, bcs, sc->R.as<double>(),
+                                        sc->R2.as<double>(), r, nullptr, nullptr, nullptr,
+                                        kProfResidX, kProfResidYZ, static_cast<cudaStream_t>(stream));
 }
 
 }  // extern "C"

@@ -13,7 +13,7 @@ namespace mf {
 // hi*hi + hi*lo + lo*hi accumulated in FP32.  X rows have pitch K, Y rows
 // pitch M.  M is a multiple of 128, K = N is a multiple of 16 and <= 256.
 struct TcEpilogue {
-  int kind = 0;                  // 0 split store, 1 eigen divide + split store, 2 FP64 update
+  int kind = 0;                  // 0 split store, 1 eigen divide + split store, 2 FP32 store/add
   __nv_bfloat16* y_hi = nullptr; // kinds 0,1: [N][M]
   __nv_bfloat16* y_lo = nullptr;
   // kind 1: m = i + P1*j, n = k
@@ -25,8 +25,8 @@ struct TcEpilogue {
   const uint8_t* null_z = nullptr;
   float sigma = 0.f;
   int sigma_null = 0;            // |sigma| < 1e-11
-  // kind 2: u[i + n1*(j + n2*k)] (+)= y
-  double* u = nullptr;
+  // kind 2: out[i + n1*(j + n2*k)] (+)= y  (interior layout, FP32)
+  float* out = nullptr;
   int accumulate = 0;
   int n1 = 0, n2 = 0, n3 = 0, P1 = 0, P2 = 0;
 };

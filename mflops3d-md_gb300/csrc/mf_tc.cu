@@ -3,20 +3,28 @@
 //   Y[n][m] = sum_k B[n][k] X[m][k],   X = Xh + Xl,  B = Bh + Bl  (BF16 pairs)
 //   D = Xh*Bh + Xh*Bl + Xl*Bh           (three tcgen05.mma, FP32 in TMEM)
 //
-// One CTA owns a 128-row tile of X and the whole N (<= 256) extent of B, so
-// the accumulator is a 128-lane x N-column block of tensor memory.  Warp 0
-// (one elected thread) streams 64-wide K chunks of Xh, Xl, Bh, Bl with TMA
-// into 128-byte-swizzled shared memory (two stages); warp 1 allocates TMEM
-// and one of its threads issues the MMAs and commits each stage back to the
-// producer.  After the last commit all four warps drain TMEM with
-// tcgen05.ld (warp w owns lanes 32w..32w+31) and run the fused epilogue:
-//   kind 0: split the FP32 result into BF16 planes Y[n][m] (coalesced in m);
-//   kind 1: same, after the eigenvalue divide 1/(lx_i+ly_j+lz_k+sigma);
-//   kind 2: add (or store) the result into the FP64 solution u.
+// Persistent, warp-specialised kernel (one CTA per SM):
+//  * the N extent is cut into NS slices of NW = N/NS columns; a CTA owns one
+//    slice and keeps both BF16 planes of that slice of B resident in shared
+//    memory (K x NW x 2 planes, <= 128 KB), loaded once by TMA;
+//  * warp 0 (one lane) streams 128 x 64 chunks of Xh and Xl through a ring
+//    of TMA stages (128-byte swizzle);
+//  * warp 1 allocates TMEM and one lane issues the three tcgen05.mma per
+//    16-deep K step into one of two FP32 accumulators (2 x NW columns), so
+//    the MMAs of tile t+1 overlap the epilogue of tile t;
+//  * warps 2-5 drain the accumulator with tcgen05.ld (warp w owns TMEM lanes
+//    32*(w%4)..+31) and run the fused epilogue:
+//      kind 0: split the FP32 result into BF16 planes Y[n][m] (coalesced in m);
+//      kind 1: same, after the eigenvalue divide 1/(lx_i+ly_j+lz_k+sigma);
+//      kind 2: add (or store) the result into the FP64 solution u.
+// The two CTAs that own the two slices of the same M tile run in step, so
+// the second read of each X tile is served by L2.
 // Every mbarrier wait is bounded (about two seconds of clock); on expiry the
 // kernel raises *err, skips the remaining work and still releases TMEM.
 #include <cuda.h>
 #include <cudaTypedefs.h>
+
+#include <algorithm>
 
 #include "mf_solver.h"
 
@@ -31,8 +39,9 @@ namespace {
 
 constexpr int kBlockM = 128;
 constexpr int kChunkK = 64;  // bf16 elements per 128-byte swizzle row
-constexpr int kStages = 2;
 constexpr long long kWaitCycles = 4000000000LL;
+constexpr int kEpiWarps = 8;      // two per TMEM lane quarter, each on half the columns
+constexpr int kEpiThreads = 32 * kEpiWarps;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -139,39 +148,110 @@ __device__ __forceinline__ void tmem_load32(uint32_t taddr, float* v) {
   for (int q = 0; q < 32; ++q) v[q] = __uint_as_float(r[q]);
 }
 
-__device__ __forceinline__ void store_split(__nv_bfloat16* hi, __nv_bfloat16* lo, long long idx,
+__device__ __forceinline__ void store_split(__nv_bfloat16* hi, __nv_bfloat16* lo, int idx,
                                             float v) {
   const __nv_bfloat16 h = __float2bfloat16_rn(v);
   hi[idx] = h;
   lo[idx] = __float2bfloat16_rn(v - __bfloat162float(h));
 }
 
-__global__ void __launch_bounds__(128, 1)
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+constexpr int kMaxStages = 4;
+constexpr int kThreads = 64 + kEpiThreads;  // warp 0 TMA, warp 1 MMA, warps 2-9 epilogue
+
+// Shared-memory plan of one launch (host and device agree on it).
+struct TcShape {
+  int NS, NW, nk, stages;
+  __host__ __device__ uint32_t b_chunk() const { return (uint32_t)NW * 128; }
+  __host__ __device__ uint32_t b_bytes() const { return 2u * nk * b_chunk(); }
+  __host__ __device__ uint32_t a_stage() const { return 2u * kBlockM * 128; }
+  __host__ __device__ uint32_t smem() const { return b_bytes() + stages * a_stage() + 1024; }
+};
+
+// Epilogue of 32 accumulator columns n0..n0+31 of row m (all indices fit in
+// 32 bits: M*N and n1*n2*n3 are below 2^31 for every supported shape).
+// (i, j) = (m % P1, m / P1) for kinds 1 and 2, computed once per tile.
+__device__ __forceinline__ void epilogue_cols(const TcEpilogue& e, const float* v, int M, int m,
+                                              int n0, int i, int j, bool valid, float lxy, bool nxy,
+                                              const float* s_lz, const uint8_t* s_nz) {
+  if (e.kind == 0) {
+    int idx = n0 * M + m;
+#pragma unroll
+    for (int q = 0; q < 32; ++q, idx += M) store_split(e.y_hi, e.y_lo, idx, v[q]);
+  } else if (e.kind == 1) {
+    // s_lz holds lam_z(k) + sigma
+    int idx = n0 * M + m;
+    if (valid && !nxy && n0 + 32 <= e.n3) {
+#pragma unroll
+      for (int q = 0; q < 32; ++q, idx += M)
+        store_split(e.y_hi, e.y_lo, idx, __fdividef(v[q], lxy + s_lz[n0 + q]));
+    } else {
+#pragma unroll
+      for (int q = 0; q < 32; ++q, idx += M) {
+        const int k = n0 + q;
+        float r = 0.f;
+        if (valid && k < e.n3 && !(nxy && s_nz[k])) r = __fdividef(v[q], lxy + s_lz[k]);
+        store_split(e.y_hi, e.y_lo, idx, r);
+      }
+    }
+  } else {
+    if (!valid) return;
+    const int plane = e.n1 * e.n2;
+    const int base = i + e.n1 * j + n0 * plane;
+    const int cols = min(32, e.n3 - n0);
+    float old[32];
+    // all loads first: the stores below may alias them as far as the
+    // compiler knows, which would otherwise serialise load -> add -> store
+#pragma unroll
+    for (int q = 0; q < 32; ++q) old[q] = (e.accumulate && q < cols) ? e.out[base + q * plane] : 0.f;
+#pragma unroll
+    for (int q = 0; q < 32; ++q)
+      if (q < cols) e.out[base + q * plane] = old[q] + v[q];
+  }
+}
+
+__global__ void __launch_bounds__(kThreads, 1)
     k_tc_transform(const __grid_constant__ CUtensorMap tx_hi, const __grid_constant__ CUtensorMap tx_lo,
                    const __grid_constant__ CUtensorMap tb_hi, const __grid_constant__ CUtensorMap tb_lo,
-                   int M, int N, int K, TcEpilogue e, int* err) {
+                   int M, TcShape sh, TcEpilogue e, int* err) {
   extern __shared__ uint8_t smem_raw[];
-  __shared__ uint64_t full_bar[kStages], empty_bar[kStages], done_bar;
+  __shared__ uint64_t bar_b, full_bar[kMaxStages], empty_bar[kMaxStages], acc_full[2], acc_empty[2];
   __shared__ uint32_t tmem_slot;
+  __shared__ float s_lz[256];     // z eigenvalues (divide epilogue)
+  __shared__ uint8_t s_nz[256];   // z null-mode flags
   uint8_t* smem = reinterpret_cast<uint8_t*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
-  const uint32_t a_bytes = kBlockM * 128;        // one 128 x 64 BF16 tile
-  const uint32_t b_bytes = (uint32_t)N * 128;    // one N x 64 BF16 tile
-  const uint32_t stage_bytes = 2 * a_bytes + 2 * b_bytes;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = blockIdx.x * kBlockM;
-  const int nk = K / kChunkK;
+  if (e.kind == 1)
+    for (int k = threadIdx.x; k < 256; k += blockDim.x) {
+      s_lz[k] = k < e.n3 ? e.lam_z[k] + e.sigma : 0.f;
+      s_nz[k] = k < e.n3 ? e.null_z[k] : 0;
+    }
+  const int NW = sh.NW, nk = sh.nk, S = sh.stages;
+  const int slice = blockIdx.x % sh.NS;
+  const int cta_rank = blockIdx.x / sh.NS, cta_count = gridDim.x / sh.NS;
+  const int mtiles = M / kBlockM;
+  const uint32_t bchunk = sh.b_chunk();
+  uint8_t* b_hi = smem;
+  uint8_t* b_lo = smem + (size_t)nk * bchunk;
+  uint8_t* a_base = smem + sh.b_bytes();
 
   if (threadIdx.x == 0) {
-    for (int s = 0; s < kStages; ++s) {
+    mbar_init(&bar_b, 1);
+    for (int s = 0; s < S; ++s) {
       mbar_init(&full_bar[s], 1);
       mbar_init(&empty_bar[s], 1);
     }
-    mbar_init(&done_bar, 1);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&acc_full[b], 1);
+      mbar_init(&acc_empty[b], kEpiThreads);
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  // TMEM columns: power of two >= 32 covering N
-  const uint32_t ncols = N <= 32 ? 32 : N <= 64 ? 64 : N <= 128 ? 128 : 256;
+  const uint32_t ncols = 2 * NW <= 32 ? 32 : 2 * NW <= 64 ? 64 : 2 * NW <= 128 ? 128 : 256;
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(&tmem_slot)),
@@ -183,88 +263,94 @@ __global__ void __launch_bounds__(128, 1)
   fence_after();
   const uint32_t tmem = tmem_slot;
 
-  if (threadIdx.x == 0) {
-    // producer
-    for (int c = 0; c < nk; ++c) {
-      const int s = c % kStages;
-      if (c >= kStages && !mbar_wait(&empty_bar[s], ((c / kStages) - 1) & 1, err)) break;
-      uint8_t* st = smem + s * stage_bytes;
-      mbar_expect_tx(&full_bar[s], stage_bytes);
-      tma_load_2d(st, &tx_hi, &full_bar[s], c * kChunkK, m0);
-      tma_load_2d(st + a_bytes, &tx_lo, &full_bar[s], c * kChunkK, m0);
-      tma_load_2d(st + 2 * a_bytes, &tb_hi, &full_bar[s], c * kChunkK, 0);
-      tma_load_2d(st + 2 * a_bytes + b_bytes, &tb_lo, &full_bar[s], c * kChunkK, 0);
-    }
-  } else if (threadIdx.x == 32) {
-    // MMA issuer
-    const uint32_t idesc = instr_desc_bf16(kBlockM, N);
-    bool ok = true;
-    for (int c = 0; c < nk && ok; ++c) {
-      const int s = c % kStages;
-      ok = mbar_wait(&full_bar[s], (c / kStages) & 1, err);
-      if (!ok) break;
-      fence_after();
-      const uint32_t base = smem_u32(smem + s * stage_bytes);
-#pragma unroll
-      for (int kk = 0; kk < kChunkK / 16; ++kk) {
-        const uint64_t ah = smem_desc(base + kk * 32);
-        const uint64_t al = smem_desc(base + a_bytes + kk * 32);
-        const uint64_t bh = smem_desc(base + 2 * a_bytes + kk * 32);
-        const uint64_t bl = smem_desc(base + 2 * a_bytes + b_bytes + kk * 32);
-        mma_bf16(tmem, al, bh, idesc, (c | kk) != 0 ? 1u : 0u);
-        mma_bf16(tmem, ah, bl, idesc, 1u);
-        mma_bf16(tmem, ah, bh, idesc, 1u);
+  if (warp == 0) {
+    if (lane == 0) {
+      // resident slice of B
+      mbar_expect_tx(&bar_b, sh.b_bytes());
+      for (int c = 0; c < nk; ++c) {
+        tma_load_2d(b_hi + (size_t)c * bchunk, &tb_hi, &bar_b, c * kChunkK, slice * NW);
+        tma_load_2d(b_lo + (size_t)c * bchunk, &tb_lo, &bar_b, c * kChunkK, slice * NW);
       }
-      mma_commit(&empty_bar[s]);
+      int it = 0;
+      bool ok = true;
+      for (int t = cta_rank; t < mtiles && ok; t += cta_count) {
+        for (int c = 0; c < nk; ++c, ++it) {
+          const int s = it % S, u = it / S;
+          if (u > 0 && !(ok = mbar_wait(&empty_bar[s], (u - 1) & 1, err))) break;
+          uint8_t* st = a_base + (size_t)s * sh.a_stage();
+          mbar_expect_tx(&full_bar[s], sh.a_stage());
+          tma_load_2d(st, &tx_hi, &full_bar[s], c * kChunkK, t * kBlockM);
+          tma_load_2d(st + kBlockM * 128, &tx_lo, &full_bar[s], c * kChunkK, t * kBlockM);
+        }
+      }
     }
-    if (ok) mma_commit(&done_bar);
+  } else if (warp == 1) {
+    if (lane == 0) {
+      const uint32_t idesc = instr_desc_bf16(kBlockM, NW);
+      bool ok = mbar_wait(&bar_b, 0, err);
+      int it = 0, tc = 0;
+      const uint32_t bh0 = smem_u32(b_hi), bl0 = smem_u32(b_lo);
+      for (int t = cta_rank; t < mtiles && ok; t += cta_count, ++tc) {
+        const int b = tc & 1, u = tc >> 1;
+        if (u > 0 && !(ok = mbar_wait(&acc_empty[b], (u - 1) & 1, err))) break;
+        fence_after();
+        const uint32_t d = tmem + (uint32_t)(b * NW);
+        for (int c = 0; c < nk; ++c, ++it) {
+          const int s = it % S;
+          if (!(ok = mbar_wait(&full_bar[s], (it / S) & 1, err))) break;
+          fence_after();
+          const uint32_t ab = smem_u32(a_base + (size_t)s * sh.a_stage());
+#pragma unroll
+          for (int kk = 0; kk < kChunkK / 16; ++kk) {
+            const uint64_t ah = smem_desc(ab + kk * 32);
+            const uint64_t al = smem_desc(ab + kBlockM * 128 + kk * 32);
+            const uint64_t bh = smem_desc(bh0 + c * bchunk + kk * 32);
+            const uint64_t bl = smem_desc(bl0 + c * bchunk + kk * 32);
+            mma_bf16(d, al, bh, idesc, (c | kk) != 0 ? 1u : 0u);
+            mma_bf16(d, ah, bl, idesc, 1u);
+            mma_bf16(d, ah, bh, idesc, 1u);
+          }
+          mma_commit(&empty_bar[s]);
+        }
+        if (ok) mma_commit(&acc_full[b]);
+      }
+    }
+  } else {
+    const int q = warp & 3;                 // TMEM lane quarter this warp may access
+    const int half = (warp - 2) >> 2;       // which half of the NW columns
+    const int row = q * 32 + lane;
+    int tc = 0;
+    for (int t = cta_rank; t < mtiles; t += cta_count, ++tc) {
+      const int b = tc & 1;
+      if (!mbar_wait(&acc_full[b], (tc >> 1) & 1, err)) break;
+      __syncwarp();
+      fence_after();
+      const int m = t * kBlockM + row;
+      int i = 0, j = 0;
+      bool valid = false, nxy = false;
+      float lxy = 0.f;
+      if (e.kind != 0) {
+        i = m % e.P1;
+        j = m / e.P1;
+        valid = (i < e.n1) && (j < e.n2);
+        if (e.kind == 1 && valid) {
+          lxy = e.lam_x[i] + e.lam_y[j];
+          nxy = e.sigma_null && e.null_x[i] && e.null_y[j];
+        }
+      }
+      const uint32_t trow = tmem + (static_cast<uint32_t>(q * 32) << 16) + (uint32_t)(b * NW);
+      float v[32];
+      const int chunks = NW / 32, first = (chunks + 1) / 2;  // split on 32-column chunks
+      const int c_lo = half ? first * 32 : 0, c_hi = half ? NW : first * 32;
+      for (int cc = c_lo; cc < c_hi; cc += 32) {
+        tmem_load32(trow + cc, v);
+        epilogue_cols(e, v, M, m, slice * NW + cc, i, j, valid, lxy, nxy, s_lz, s_nz);
+      }
+      fence_before();
+      mbar_arrive(&acc_empty[b]);
+    }
   }
   __syncwarp();
-
-  // epilogue: all 128 threads, lane row = warp*32 + lane
-  const bool ready = mbar_wait(&done_bar, 0, err);
-  fence_after();
-  if (ready) {
-    const long long m = m0 + warp * 32 + lane;
-    const uint32_t trow = tmem + (static_cast<uint32_t>(warp * 32) << 16);
-    float v[32];
-    if (e.kind == 0) {
-      for (int cc = 0; cc < N / 32; ++cc) {
-        tmem_load32(trow + cc * 32, v);
-#pragma unroll
-        for (int q = 0; q < 32; ++q) store_split(e.y_hi, e.y_lo, (long long)(cc * 32 + q) * M + m, v[q]);
-      }
-    } else if (e.kind == 1) {
-      const int i = (int)(m % e.P1), j = (int)(m / e.P1);
-      const bool valid = (i < e.n1) && (j < e.n2);
-      const float lxy = valid ? e.lam_x[i] + e.lam_y[j] : 0.f;
-      const bool nxy = valid && e.sigma_null && e.null_x[i] && e.null_y[j];
-      for (int cc = 0; cc < N / 32; ++cc) {
-        tmem_load32(trow + cc * 32, v);
-#pragma unroll
-        for (int q = 0; q < 32; ++q) {
-          const int k = cc * 32 + q;
-          float r = 0.f;
-          if (valid && k < e.n3 && !(nxy && e.null_z[k])) r = v[q] / ((lxy + e.lam_z[k]) + e.sigma);
-          store_split(e.y_hi, e.y_lo, (long long)k * M + m, r);
-        }
-      }
-    } else {
-      const int i = (int)(m % e.P1), j = (int)(m / e.P1);
-      const bool valid = (i < e.n1) && (j < e.n2);
-      for (int cc = 0; cc < N / 32; ++cc) {
-        tmem_load32(trow + cc * 32, v);
-        if (!valid) continue;
-#pragma unroll
-        for (int q = 0; q < 32; ++q) {
-          const int k = cc * 32 + q;
-          if (k >= e.n3) continue;
-          const long long idx = i + (long long)e.n1 * (j + (long long)e.n2 * k);
-          e.u[idx] = e.accumulate ? e.u[idx] + (double)v[q] : (double)v[q];
-        }
-      }
-    }
-  }
   fence_before();
   __syncthreads();
   if (warp == 1) {
@@ -302,10 +388,22 @@ int make_map(CUtensorMap* map, const __nv_bfloat16* ptr, int rows, int cols, int
 
 }  // namespace
 
+static TcShape shape_for(int N, int K) {
+  TcShape sh;
+  sh.NS = N >= 128 ? 2 : 1;
+  sh.NW = N / sh.NS;
+  sh.nk = K / kChunkK;
+  const uint32_t budget = 224 * 1024;
+  const uint32_t left = budget - sh.b_bytes();
+  sh.stages = (int)std::min<uint32_t>(kMaxStages, left / sh.a_stage());
+  return sh;
+}
+
 int tc_plan_create(TcPlan** out, const __nv_bfloat16* x_hi, const __nv_bfloat16* x_lo,
                    const __nv_bfloat16* b_hi, const __nv_bfloat16* b_lo, int M, int N, int K) {
   *out = nullptr;
-  if (M % kBlockM || K % kChunkK || N != K || N < 64 || N > 256 || N % 32)
+  if (M % kBlockM || K % kChunkK || N != K || N < 64 || N > 256 || N % 32 ||
+      (long long)M * N >= (1LL << 31))
     return set_error(MF_ERR_UNSUPPORTED, "tensor-core transform: unsupported shape M=%d N=%d K=%d", M,
                      N, K);
   for (const void* p : {(const void*)x_hi, (const void*)x_lo, (const void*)b_hi, (const void*)b_lo})
@@ -313,12 +411,15 @@ int tc_plan_create(TcPlan** out, const __nv_bfloat16* x_hi, const __nv_bfloat16*
       return set_error(MF_ERR_ARG, "tensor-core transform: operands must be 16-byte aligned");
   int rc = get_encode();
   if (rc) return rc;
+  const TcShape sh = shape_for(N, K);
+  if (sh.stages < 2 || sh.NW % 32)
+    return set_error(MF_ERR_UNSUPPORTED, "tensor-core transform: no shared-memory plan for N=%d", N);
   TcPlan* p = new TcPlan();
   p->M = M;
   p->N = N;
   p->K = K;
   if ((rc = make_map(&p->x_hi, x_hi, M, K, kBlockM)) || (rc = make_map(&p->x_lo, x_lo, M, K, kBlockM)) ||
-      (rc = make_map(&p->b_hi, b_hi, N, K, N)) || (rc = make_map(&p->b_lo, b_lo, N, K, N))) {
+      (rc = make_map(&p->b_hi, b_hi, N, K, sh.NW)) || (rc = make_map(&p->b_lo, b_lo, N, K, sh.NW))) {
     delete p;
     return rc;
   }
@@ -329,16 +430,19 @@ int tc_plan_create(TcPlan** out, const __nv_bfloat16* x_hi, const __nv_bfloat16*
 void tc_plan_destroy(TcPlan* p) { delete p; }
 
 int tc_transform(const TcPlan* p, const TcEpilogue& e, int* dev_err, cudaStream_t st) {
-  const size_t stage = 2 * (size_t)kBlockM * 128 + 2 * (size_t)p->N * 128;
-  const size_t smem = kStages * stage + 1024;
-  static bool attr = false;
-  if (!attr) {
+  const TcShape sh = shape_for(p->N, p->K);
+  static int num_sms = 0;
+  if (!num_sms) {
+    int dev = 0;
+    MF_CUDA(cudaGetDevice(&dev));
+    MF_CUDA(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev));
     MF_CUDA(cudaFuncSetAttribute(k_tc_transform, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)(kStages * (2 * kBlockM * 128 + 2 * 256 * 128) + 1024)));
-    attr = true;
+                                 224 * 1024 + 1024));
   }
-  k_tc_transform<<<p->M / kBlockM, 128, smem, st>>>(p->x_hi, p->x_lo, p->b_hi, p->b_lo, p->M, p->N,
-                                                    p->K, e, dev_err);
+  const int mtiles = p->M / kBlockM;
+  int grid = std::min(num_sms / sh.NS, mtiles) * sh.NS;
+  k_tc_transform<<<grid, kThreads, sh.smem(), st>>>(p->x_hi, p->x_lo, p->b_hi, p->b_lo, p->M, sh, e,
+                                                    dev_err);
   MF_CUDA(cudaGetLastError());
   return MF_OK;
 }

@@ -345,7 +345,8 @@ class SolverCoeffs3D:
                                           vi.ctypes.data_as(_DP)))
 
     PROFILE_KINDS = ("tc_transform", "residual_x", "residual_yz", "split_bf16", "bc_fold",
-                     "bc_faces", "fp64_transform", "interior_copy")
+                     "bc_faces", "fp64_transform", "interior_copy", "tc_transform_divide",
+                     "tc_transform_update", "residual_fp32")
 
     def profile(self, enable=True):
         _check(_lib.mf_solver3d_profile(self._h, 1 if enable else 0))

@@ -44,3 +44,29 @@ def test_mixed_refined_reaches_1e10(mf, gpu, sigma):
 def test_mixed_uneven_and_neumann(mf, gpu):
     err = mixed_case(mf, (50, 66, 98), (1, 2, 1, 1, 2, 1), -1e6 * 1e-3, refine=3)
     assert err < 1e-10
+
+
+def test_mixed_slice_shapes(mf, gpu):
+    # padded sizes 192 (two 96-column slices), 64 and 128 on the three axes
+    err = mixed_case(mf, (150, 34, 98), (1,) * 6, -1e6, refine=3)
+    assert err < 1e-10
+
+
+def test_mixed_matches_fp64_gpu_at_257(mf, gpu):
+    """Headline shape: 257^3 Poisson, tanh(2.0) in y; refined split-BF16
+    solution vs the plain FP64 GPU solution."""
+    import torch
+    from oracle import mesh
+    n = 255
+    gx, gy = mesh.uniform_grid(257), mesh.tanh_grid(257, 2.0)
+    sc = mf.SolverCoeffs3D(gx, gy, gx, (1,) * 6, 6)
+    rhs = torch.randn((n, n, n), dtype=torch.float64, device="cuda", generator=torch.Generator("cuda").manual_seed(5)).permute(2, 1, 0)
+    bc = [mf.empty_device((n, n, 2)) for _ in range(3)]
+    plain = mf.empty_device((257, 257, 257))
+    mixed = mf.empty_device((257, 257, 257))
+    sc.solve_3d(rhs, 0.0, plain, *bc)
+    sc.solve_3d(rhs, 0.0, mixed, *bc, precision=mf.MF_PREC_SPLIT_BF16, refine=2)
+    sc.device_status()
+    err = (torch.linalg.vector_norm(mixed - plain) / torch.linalg.vector_norm(plain)).item()
+    print("257^3 split-bf16 + 2 refinements vs FP64 GPU: %.3e" % err)
+    assert err < 1e-10
