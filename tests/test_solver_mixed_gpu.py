@@ -1,5 +1,5 @@
 """Split-BF16 tensor-core transforms + FP64 iterative refinement against the
-FP64 oracle.  Tolerance (north-star): relative L2 error <= 1e-10 after
+FP64 oracle.  Tolerance: relative L2 error <= 1e-10 after
 refinement; the unrefined split-precision error is reported alongside."""
 import numpy as np
 import pytest
