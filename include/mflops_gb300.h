@@ -129,6 +129,23 @@ int mf_solve_3d(mf_solver3d_t* sc, const double* rhs, double sigma, double* solf
                 const double* bcx, const double* bcy, const double* bcz,
                 int n1, int n2, int n3, void* stream);
 
+/* Allocation-free variant of mf_solve_3d (plain FP64), with no counterpart
+ * in the reference.  It is for callers that cannot allocate device memory
+ * while they run: code captured into a CUDA graph (cudaMalloc is not
+ * permitted during stream capture) and hosts whose device memory belongs to
+ * another allocator that forbids the library from calling cudaMalloc.  Its
+ * two work arrays live in a fixed 4 MiB file-scope device array, so the
+ * interior n1*n2*n3 is limited to 262144 points (64^3); larger sizes return
+ * MF_ERR_UNSUPPORTED.  All pointers must be device memory (MF_ERR_ARG
+ * otherwise).  The first call on each device looks up that array's address
+ * (no allocation) and should come before any stream capture.  Every call
+ * shares the array, so calls that overlap on the GPU (different streams or
+ * handles) race; each call overwrites the work arrays before reading them.
+ * It calls no cudaMalloc, cudaFree or allocating library routine. */
+int mf_solve_3d_noalloc(mf_solver3d_t* sc, const double* rhs, double sigma, double* solf,
+                        const double* bcx, const double* bcy, const double* bcz,
+                        int n1, int n2, int n3, void* stream);
+
 /* Same problem with the eigenvector transforms on the tensor cores
  * (precision = MF_PREC_SPLIT_BF16 or MF_PREC_3XTF32) and `refine`
  * iterative-refinement steps whose residual is computed in FP64 with the

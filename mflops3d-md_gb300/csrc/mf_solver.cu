@@ -24,6 +24,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 
 #include "mf_line.cuh"
 #include "mf_setup.h"
@@ -795,6 +796,38 @@ static int solve_mixed_dev(mf_solver3d* sc, const double* rhs, double sigma, dou
   return faces(sc, solf, bcs, st);
 }
 
+// ---------------------------------------------------------------------------
+// Allocation-free plain solve (mf_solve_3d_noalloc).
+//
+// For callers that must not allocate device memory while they run: code
+// being captured into a CUDA graph (cudaMalloc is not permitted during
+// stream capture) and hosts whose memory is owned by another allocator that
+// forbids the library from calling cudaMalloc.  The two FP64 work arrays of
+// the plain path live in this fixed file-scope array instead of the handle's
+// buffers.  Every GPU that loads the library holds it until exit.
+constexpr long long kNoAllocMaxPoints = 1LL << 18;  // interior points n1*n2*n3 (64^3)
+static __device__ __align__(256) double g_noalloc_scratch[2 * kNoAllocMaxPoints];  // 4 MiB
+
+// Device address of g_noalloc_scratch for the current device, looked up
+// once per device (the first call on a device does this; it allocates
+// nothing and should happen before any stream capture).
+static int noalloc_scratch(double** out) {
+  static std::mutex mu;
+  static double* addr[64] = {nullptr};
+  int dev = 0;
+  MF_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return set_error(MF_ERR_UNSUPPORTED, "device ordinal %d out of range", dev);
+  std::lock_guard<std::mutex> lock(mu);
+  if (!addr[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_error(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+    addr[dev] = static_cast<double*>(p);
+  }
+  *out = addr[dev];
+  return MF_OK;
+}
+
 }  // namespace mf
 
 // ---------------------------------------------------------------------------
@@ -953,6 +986,75 @@ int mf_solver_3d(mf_solver3d_t* sc, const double* g, double* u, const double* bc
     gstage.release();
   }
   return rc;
+}
+
+int mf_solve_3d_noalloc(mf_solver3d_t* sc, const double* rhs, double sigma, double* solf,
+                        const double* bcx, const double* bcy, const double* bcz, int n1, int n2,
+                        int n3, void* stream) {
+  if (!sc || !rhs || !solf || !bcx || !bcy || !bcz)
+    return set_error(MF_ERR_ARG, "mf_solve_3d_noalloc: null argument");
+  if (n1 != sc->n[0] || n2 != sc->n[1] || n3 != sc->n[2])
+    return set_error(MF_ERR_ARG, "mf_solve_3d_noalloc: shape (%d,%d,%d) differs from the set-up (%d,%d,%d)",
+                     n1, n2, n3, sc->n[0], sc->n[1], sc->n[2]);
+  const long long tot = (long long)n1 * n2 * n3;
+  if (tot > kNoAllocMaxPoints)
+    return set_error(MF_ERR_UNSUPPORTED,
+                     "mf_solve_3d_noalloc: %lld interior points exceed the fixed scratch of %lld "
+                     "points (use mf_solve_3d)", tot, kNoAllocMaxPoints);
+  for (const void* p : {(const void*)rhs, (const void*)solf, (const void*)bcx, (const void*)bcy,
+                        (const void*)bcz})
+    if (!is_device_ptr(p))
+      return set_error(MF_ERR_ARG, "mf_solve_3d_noalloc: device pointers only (host data needs staging buffers)");
+  double* scratch = nullptr;
+  int rc = noalloc_scratch(&scratch);
+  if (rc) return rc;
+  // every entry of both work arrays is written before it is read, so the
+  // previous call's contents need no clearing
+  double* w0 = scratch;
+  double* w1 = scratch + kNoAllocMaxPoints;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const double* bcs[3] = {bcx, bcy, bcz};
+  k_fold<<<blocks_for(tot, 256), 256, 0, st>>>(rhs, w0, bcx, bcy, bcz, fold_args(sc), n1, n2, n3);
+  MF_CUDA(cudaGetLastError());
+  StageProfiler off;  // no event timers on this path
+  GemmEpi plain;
+  const double* Vi[3] = {sc->ax[0].Vinv.as<double>(), sc->ax[1].Vinv.as<double>(),
+                         sc->ax[2].Vinv.as<double>()};
+  const double* Vf[3] = {sc->ax[0].V.as<double>(), sc->ax[1].V.as<double>(),
+                         sc->ax[2].V.as<double>()};
+  if ((rc = gemm_f64(off, w0, n2 * n3, n1, Vi[0], n1, w1, plain, st))) return rc;
+  if ((rc = gemm_f64(off, w1, n3 * n1, n2, Vi[1], n2, w0, plain, st))) return rc;
+  GemmEpi div;
+  div.kind = 1;
+  div.lx = sc->ax[0].eig.as<double>();
+  div.ly = sc->ax[1].eig.as<double>();
+  div.lz = sc->ax[2].eig.as<double>();
+  div.sigma = sigma;
+  div.thresh = kNullThresh;
+  div.n1 = n1;
+  div.n2 = n2;
+  if ((rc = gemm_f64(off, w0, n1 * n2, n3, Vi[2], n3, w1, div, st))) return rc;
+  if ((rc = gemm_f64(off, w1, n2 * n3, n1, Vf[0], n1, w0, plain, st))) return rc;
+  if ((rc = gemm_f64(off, w0, n3 * n1, n2, Vf[1], n2, w1, plain, st))) return rc;
+  GemmEpi out;
+  out.kind = 2;
+  out.n1 = n1;
+  out.n2 = n2;
+  if ((rc = gemm_f64(off, w1, n1 * n2, n3, Vf[2], n3, solf, out, st))) return rc;
+  const long long p1 = n1 + 2, p2 = n2 + 2;
+  for (int axis = 0; axis < 3; ++axis) {
+    const AxisDev& d = sc->ax[axis];
+    FaceArgs f;
+    if (axis == 0) { f.sA = 1; f.sa = p1; f.sb = p1 * p2; f.n = n1; f.na = n2; f.nb = n3; }
+    if (axis == 1) { f.sA = p1; f.sa = 1; f.sb = p1 * p2; f.n = n2; f.na = n1; f.nb = n3; }
+    if (axis == 2) { f.sA = p1 * p2; f.sa = 1; f.sb = p1; f.n = n3; f.na = n1; f.nb = n2; }
+    f.bc0 = d.bc[0];
+    f.bc1 = d.bc[1];
+    for (int m = 0; m < 7; ++m) { f.nl[m] = d.neum[m]; f.nr[m] = d.neum[7 + m]; }
+    k_faces<<<blocks_for((long long)f.na * f.nb, 128), 128, 0, st>>>(solf, bcs[axis], f);
+    MF_CUDA(cudaGetLastError());
+  }
+  return MF_OK;
 }
 
 int mf_solver3d_set_eigen(mf_solver3d_t* sc, int axis, const double* eigen, const double* vect,

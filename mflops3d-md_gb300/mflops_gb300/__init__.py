@@ -90,6 +90,7 @@ _PROTOS = {
     "mf_solver_coeffs_init_3d": [_DP, _DP, _DP, _I, _I, _I, _IP, _I, ctypes.POINTER(_P)],
     "mf_solver3d_destroy": [_P],
     "mf_solve_3d": [_P, _P, _D, _P, _P, _P, _P, _I, _I, _I, _P],
+    "mf_solve_3d_noalloc": [_P, _P, _D, _P, _P, _P, _P, _I, _I, _I, _P],
     "mf_solve_3d_mixed": [_P, _P, _D, _P, _P, _P, _P, _I, _I, _I, _I, _I, _P],
     "mf_solver_3d": [_P, _P, _P, _P, _P, _P, _I, _I, _I, _D, _I, _P],
     "mf_solver_residual": [_P, _P, _P, _D, _P, _P, _P, _P, _I, _I, _I, _P],
@@ -327,6 +328,14 @@ class SolverCoeffs3D:
             _check(_lib.mf_solve_3d_mixed(self._h, _arg(rhs), float(sigma), _arg(solf), _arg(bcx),
                                           _arg(bcy), _arg(bcz), n1, n2, n3, precision, refine,
                                           _stream(stream)))
+        return solf
+
+    def solve_3d_noalloc(self, rhs, sigma, solf, bcx, bcy, bcz, stream=None):
+        """Plain FP64 solve that allocates no device memory (device tensors
+        only; interior limited to 2**18 points)."""
+        n1, n2, n3 = (int(v) for v in rhs.shape)
+        _check(_lib.mf_solve_3d_noalloc(self._h, _arg(rhs), float(sigma), _arg(solf), _arg(bcx),
+                                        _arg(bcy), _arg(bcz), n1, n2, n3, _stream(stream)))
         return solf
 
     def solver_3d(self, g, u, bcx, bcy, bcz, sigma, precision=MF_PREC_FP64, stream=None):
