@@ -195,6 +195,54 @@ int mf_solver_residual(mf_solver3d_t* sc, const double* g, const double* u, doub
                        const double* bcx, const double* bcy, const double* bcz,
                        double* r, int n1, int n2, int n3, void* stream);
 
+/* ------------------------------------------------------------------------
+ * Influence-matrix multidomain coupling (class_md + class_field MD driver),
+ * every subdomain resident on one GPU.
+ * Subdomain (i,j,k) of an nd = (nd1,nd2,nd3) decomposition has index
+ * s = i + nd1*(j + nd2*k) and owns the x-grid of slab i, the y-grid of slab j
+ * and the z-grid of slab k (conforming faces; neighbours share their
+ * interface nodes).  Interface faces are Dirichlet; physical faces use bct.
+ * ---------------------------------------------------------------------- */
+typedef struct mf_md mf_md_t;
+
+/* Interface numbering of md_influence_matrix_param,
+ * src/class_md/class_md.f90:1450-1680 (host only).  nint_x[i] = interior
+ * points of x-slab i, etc.  Outputs (any may be NULL): dm_int(nd1,nd2,nd3,3,2)
+ * Fortran-ordered (1-based ids, -1 none; side 1 left, 2 right), and per
+ * interface its axis (0..2), size (points) and offset (first row); it =
+ * number of interfaces, ninf = number of interface unknowns. */
+int mf_md_topology(const int nd[3], const int periods[3], const int* nint_x, const int* nint_y,
+                   const int* nint_z, int* dm_int, int* kind, int* size, int* offset, int* it,
+                   long long* ninf);
+
+/* Creates the subdomain solvers (solver_coeffs_init_3d) and solver-type
+ * derivative coefficients (der_coeffs_init) of every subdomain:
+ * gridx[i] has nx[i] nodes (i < nd1), gridy[j] ny[j], gridz[k] nz[k];
+ * md_bc_init (class_md.f90:275-293) turns interface faces into Dirichlet. */
+int mf_md_create(const int nd[3], const int periods[3], const double* const* gridx, const int* nx,
+                 const double* const* gridy, const int* ny, const double* const* gridz, const int* nz,
+                 const int bct[6], int so, mf_md_t** md);
+int mf_md_destroy(mf_md_t* md);
+int mf_md_ninf(const mf_md_t* md, long long* ninf, int* it);
+
+/* Builds and factorises the influence matrix for one sigma
+ * (influence_matrix_init_end + md_influence_matrix_set,
+ * class_field.f90:1216-1287,1396-1510): one Dirac column per interface point,
+ * FP64, then an FP64 LU.  null_mode: 0 none, 1 constant null space (rhs and
+ * solution made mean-free, as a KSP with a null space), 2 row 0 pinned
+ * (md_add_pert / md_vector_zero_lastpoint, class_md.f90:223-268). */
+int mf_md_influence_matrix_set(mf_md_t* md, double sigma, int null_mode, void* stream);
+
+/* multidomain_solve(mpid,inf,sc,bc,u,g,du,sigma,dcx,dcy,dcz,null),
+ * class_field.f90:1295-1388: per subdomain s, g[s] and u[s] are (nx,ny,nz)
+ * fields and bcx[s](ny-2,nz-2,2), bcy[s], bcz[s] the physical boundary data
+ * (interface faces ignored).  Device pointers. */
+int mf_md_solve(mf_md_t* md, const double* const* g, double* const* u, const double* const* bcx,
+                const double* const* bcy, const double* const* bcz, void* stream);
+
+/* Copies the last interface solution (ninf values) to host memory. */
+int mf_md_interface(const mf_md_t* md, double* lambda);
+
 #ifdef __cplusplus
 }
 #endif

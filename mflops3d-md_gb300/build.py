@@ -69,7 +69,10 @@ def build(verbose=False):
         objs = list(ex.map(lambda s: _compile(s, verbose), srcs))
     out = lib_path()
     if not os.path.exists(out) or os.path.getmtime(out) < max(os.path.getmtime(o) for o in objs):
-        cmd = [_nvcc()] + ARCH + ["-shared", "-o", out] + objs + ["-cudart", "static"]
+        cuda_lib = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "lib64")
+        cmd = ([_nvcc()] + ARCH + ["-shared", "-o", out] + objs +
+               ["-cudart", "static", "-L" + cuda_lib, "-lcusolver",
+                "-Xlinker", "-rpath", "-Xlinker", cuda_lib])
         if verbose:
             print(" ".join(cmd), flush=True)
         res = subprocess.run(cmd, capture_output=True, text=True)

@@ -1,0 +1,579 @@
+// Influence-matrix multidomain coupling, every subdomain resident on one GPU.
+//
+// Reference path: multidomain_solve (class_field.f90:1295-1388) with the
+// interface topology of md_influence_matrix_param (class_md.f90:1450-1680),
+// the Dirac-column assembly of md_influence_matrix_set (class_field.f90:
+// 1396-1510, class_md.f90:1049-1095), the rhs gather / solution scatter of
+// md_vector_setvalues / md_vector_getvalues (class_md.f90:663-708,445-550)
+// and the interface solve of md_solve (class_md.f90:379-438).
+//
+// GB300 form: the MPI ranks of the reference become subdomain handles on one
+// device; the neighbour exchange becomes a gather of signed face derivatives
+// into the interface vector and a scatter of the interface solution into the
+// subdomains' boundary arrays (device kernels).  The PETSc KSP is replaced by
+// a dense FP64 LU factorised once (cuSOLVER getrf at set-up) and two blocked
+// triangular solves per call (own kernels, HBM-bound on the factor).
+#include <cusolverDn.h>
+
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "mf_internal.h"
+
+namespace mf {
+
+// Host restatement of the interface numbering (class_md.f90:1450-1680).
+// dm[((((i*nd2)+j)*nd3+k)*3+l)*2+m]: interface id (1-based, -1 none) of face
+// l side m of subdomain (i,j,k); kind/size/offset per interface.
+struct MdTopology {
+  int nd[3] = {1, 1, 1};
+  int periods[3] = {0, 0, 0};
+  std::vector<int> dm, kind, size, offset;
+  int it = 0;
+  long long ninf = 0;
+  int& at(int i, int j, int k, int l, int m) {
+    return dm[((((size_t)i * nd[1] + j) * nd[2] + k) * 3 + l) * 2 + m];
+  }
+  int get(int i, int j, int k, int l, int m) const {
+    return dm[((((size_t)i * nd[1] + j) * nd[2] + k) * 3 + l) * 2 + m];
+  }
+};
+
+static int topology_build(const int nd[3], const int periods[3], const int* const nint[3],
+                          MdTopology& t) {
+  for (int l = 0; l < 3; ++l) {
+    if (nd[l] < 1) return set_error(MF_ERR_ARG, "md topology: nd must be >= 1");
+    t.nd[l] = nd[l];
+    t.periods[l] = periods[l] ? 1 : 0;
+  }
+  t.dm.assign((size_t)nd[0] * nd[1] * nd[2] * 6, -1);
+  t.kind.clear();
+  int count = 0;
+  for (int i = 0; i < nd[0]; ++i)
+    for (int j = 0; j < nd[1]; ++j)
+      for (int k = 0; k < nd[2]; ++k) {
+        const int idx[3] = {i, j, k};
+        for (int l = 0; l < 3; ++l)
+          if (idx[l] < nd[l] - 1 || t.periods[l]) {
+            t.at(i, j, k, l, 1) = ++count;
+            t.kind.push_back(l);
+          }
+      }
+  // left face = right face of the left neighbour (periodic wrap)
+  for (int i = 0; i < nd[0]; ++i)
+    for (int j = 0; j < nd[1]; ++j)
+      for (int k = 0; k < nd[2]; ++k) {
+        const int idx[3] = {i, j, k};
+        for (int l = 0; l < 3; ++l) {
+          int nb[3] = {i, j, k};
+          if (idx[l] > 0) {
+            nb[l] = idx[l] - 1;
+          } else if (t.periods[l]) {
+            nb[l] = nd[l] - 1;
+          } else {
+            continue;
+          }
+          t.at(i, j, k, l, 0) = t.get(nb[0], nb[1], nb[2], l, 1);
+        }
+      }
+  t.it = count;
+  t.size.assign(count, 0);
+  for (int i = 0; i < nd[0]; ++i)
+    for (int j = 0; j < nd[1]; ++j)
+      for (int k = 0; k < nd[2]; ++k)
+        for (int l = 0; l < 3; ++l) {
+          const int p = t.get(i, j, k, l, 1);
+          if (p <= 0) continue;
+          const int n[3] = {nint[0][i], nint[1][j], nint[2][k]};
+          const int a = l == 0 ? 1 : 0, b = l == 2 ? 1 : 2;
+          t.size[p - 1] = n[a] * n[b];
+        }
+  t.offset.assign(count, 0);
+  long long acc = 0;
+  for (int p = 0; p < count; ++p) {
+    t.offset[p] = (int)acc;
+    acc += t.size[p];
+  }
+  t.ninf = acc;
+  if (acc >= (1LL << 31)) return set_error(MF_ERR_UNSUPPORTED, "md topology: interface too large");
+  return MF_OK;
+}
+
+// ---------------------------------------------------------------------------
+// kernels
+// ---------------------------------------------------------------------------
+
+// Signed normal derivatives of one face into a target vector:
+//   out[row0 + q] += scale * (m == 0 ? -1 : +1) * du(face node q)
+// q runs over the face interior points in Fortran order of the face array.
+struct FaceGather {
+  int l, m;             // face axis and side
+  int nx, ny, nz;       // subdomain nodes
+  long long row0;       // first row of the interface
+  double scale;
+};
+
+__global__ void k_face_gather(const double* __restrict__ du, double* out, FaceGather f) {
+  const int na = (f.l == 0 ? f.ny : f.nx) - 2;
+  const int nb = (f.l == 2 ? f.ny : f.nz) - 2;
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= na * nb) return;
+  const int a = q % na + 1, b = q / na + 1;
+  int i, j, k;
+  if (f.l == 0) { i = f.m ? f.nx - 1 : 0; j = a; k = b; }
+  else if (f.l == 1) { i = a; j = f.m ? f.ny - 1 : 0; k = b; }
+  else { i = a; j = b; k = f.m ? f.nz - 1 : 0; }
+  const double v = du[i + (long long)f.nx * (j + (long long)f.ny * k)];
+  out[f.row0 + q] += f.scale * (f.m ? v : -v);
+}
+
+// bc face (l, m) of a subdomain: copy from the caller's array, then the
+// interface faces get either 0 or the interface solution.
+__global__ void k_face_set(double* bc, long long nf, int m, const double* __restrict__ src,
+                           long long row0, int mode, double dirac_q) {
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nf) return;
+  double v = 0.0;
+  if (mode == 1) v = src[row0 + q];          // interface value
+  if (mode == 2) v = (q == (long long)dirac_q) ? 1.0 : 0.0;  // Dirac column
+  bc[q + nf * m] = v;
+}
+
+// Pivot application, then blocked triangular solves with the LU factor
+// (column-major n x n, unit lower L, upper U) on one right-hand side.
+__global__ void k_apply_pivots(double* x, const int* __restrict__ ipiv, int n) {
+  if (blockIdx.x == 0 && threadIdx.x == 0)
+    for (int k = 0; k < n; ++k) {
+      const int p = ipiv[k] - 1;
+      if (p != k) {
+        const double t = x[k];
+        x[k] = x[p];
+        x[p] = t;
+      }
+    }
+}
+
+constexpr int kTriBlock = 128;
+
+// Solves the diagonal block [k0, k0+nb) in place (one CTA).
+__global__ void k_tri_diag(const double* __restrict__ A, double* x, int n, int k0, int nb, int upper) {
+  __shared__ double xs[kTriBlock];
+  for (int t = threadIdx.x; t < nb; t += blockDim.x) xs[t] = x[k0 + t];
+  __syncthreads();
+  if (!upper) {
+    for (int c = 0; c < nb; ++c) {
+      const double xc = xs[c];
+      for (int r = c + 1 + threadIdx.x; r < nb; r += blockDim.x)
+        xs[r] -= A[(k0 + r) + (long long)n * (k0 + c)] * xc;
+      __syncthreads();
+    }
+  } else {
+    for (int c = nb - 1; c >= 0; --c) {
+      if (threadIdx.x == 0) xs[c] /= A[(k0 + c) + (long long)n * (k0 + c)];
+      __syncthreads();
+      const double xc = xs[c];
+      for (int r = threadIdx.x; r < c; r += blockDim.x)
+        xs[r] -= A[(k0 + r) + (long long)n * (k0 + c)] * xc;
+      __syncthreads();
+    }
+  }
+  for (int t = threadIdx.x; t < nb; t += blockDim.x) x[k0 + t] = xs[t];
+}
+
+// x[r] -= sum_{c in block} A[r, c] x[c] for rows r in [r0, r1).
+__global__ void k_tri_update(const double* __restrict__ A, double* x, int n, int k0, int nb, int r0,
+                             int r1) {
+  const int r = r0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= r1) return;
+  double acc = 0.0;
+  for (int c = 0; c < nb; ++c) acc += A[r + (long long)n * (k0 + c)] * x[k0 + c];
+  x[r] -= acc;
+}
+
+// Mean removal (single CTA reduction; interface vectors are small).
+__global__ void k_remove_mean(double* x, int n) {
+  __shared__ double part[256];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s += x[i];
+  part[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w /= 2) {
+    if (threadIdx.x < w) part[threadIdx.x] += part[threadIdx.x + w];
+    __syncthreads();
+  }
+  const double mean = part[0] / n;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] -= mean;
+}
+
+__global__ void k_set_scalar(double* x, long long i, double v) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) x[i] = v;
+}
+
+__global__ void k_pin_row0(double* M, int n) {
+  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < n) M[(long long)n * c] = (c == 0) ? 5.0 : 0.0;
+}
+
+__global__ void k_extract_int(const double* __restrict__ g, double* __restrict__ out, int n1, int n2,
+                              int n3) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long tot = (long long)n1 * n2 * n3;
+  if (idx >= tot) return;
+  const int i = (int)(idx % n1);
+  const long long jk = idx / n1;
+  const int j = (int)(jk % n2), k = (int)(jk / n2);
+  out[idx] = g[(i + 1) + (long long)(n1 + 2) * ((j + 1) + (long long)(n2 + 2) * (k + 1))];
+}
+
+static inline unsigned nblk(long long n, int t) { return (unsigned)((n + t - 1) / t); }
+
+int der_launch(const mf_der_t* dc, int axis, int order, int mode, const double* f, double* df,
+               int nx, int ny, int nz, cudaStream_t st);
+
+}  // namespace mf
+
+using namespace mf;
+
+struct mf_md {
+  MdTopology topo;
+  struct Sub {
+    int n[3];          // nodes
+    int bct[6];        // effective boundary types
+    mf_solver3d_t* sc = nullptr;
+    mf_der_t* dc[3] = {nullptr, nullptr, nullptr};
+    DevBuf bc[3];      // face arrays (2 sides each)
+  };
+  std::vector<Sub> sub;  // index i + nd1*(j + nd2*k)
+  DevBuf M, ipiv, vec, info, work, zero_int, du[3], rint, ufield;
+  cusolverDnHandle_t cs = nullptr;
+  int null_mode = 0;
+  double sigma = 0.0;
+  bool factored = false;
+};
+
+namespace mf {
+
+static int md_sub_index(const mf_md* md, int i, int j, int k) {
+  return i + md->topo.nd[0] * (j + md->topo.nd[1] * k);
+}
+
+// Solves subdomain s with interior rhs `rint` and its internal bc arrays,
+// writing the full field u (interior + faces).
+static int md_sub_solve(mf_md* md, int s, const double* rint, double* u, cudaStream_t st) {
+  mf_md::Sub& sd = md->sub[s];
+  return mf_solve_3d(sd.sc, rint, md->sigma, u, sd.bc[0].as<double>(), sd.bc[1].as<double>(),
+                     sd.bc[2].as<double>(), sd.n[0] - 2, sd.n[1] - 2, sd.n[2] - 2, st);
+}
+
+// Normal derivatives of u on every interface face of subdomain (i,j,k),
+// added (times scale, signed like the reference) into out[rows].
+static int md_gather(mf_md* md, int i, int j, int k, const double* u, double* out, double scale,
+                     cudaStream_t st) {
+  const int s = md_sub_index(md, i, j, k);
+  mf_md::Sub& sd = md->sub[s];
+  bool need[3] = {false, false, false};
+  for (int l = 0; l < 3; ++l)
+    for (int m = 0; m < 2; ++m)
+      if (md->topo.get(i, j, k, l, m) > 0) need[l] = true;
+  int rc;
+  for (int l = 0; l < 3; ++l) {
+    if (!need[l]) continue;
+    if ((rc = der_launch(sd.dc[l], l, 1, 3, u, md->du[l].as<double>(), sd.n[0], sd.n[1], sd.n[2], st)))
+      return rc;
+  }
+  for (int l = 0; l < 3; ++l)
+    for (int m = 0; m < 2; ++m) {
+      const int p = md->topo.get(i, j, k, l, m);
+      if (p <= 0) continue;
+      FaceGather f{l, m, sd.n[0], sd.n[1], sd.n[2], (long long)md->topo.offset[p - 1], scale};
+      k_face_gather<<<nblk(md->topo.size[p - 1], 128), 128, 0, st>>>(md->du[l].as<double>(), out, f);
+      MF_CUDA(cudaGetLastError());
+    }
+  return MF_OK;
+}
+
+// Face sizes of subdomain s along axis l.
+static long long face_points(const mf_md::Sub& sd, int l) {
+  const int a = l == 0 ? 1 : 0, b = l == 2 ? 1 : 2;
+  return (long long)(sd.n[a] - 2) * (sd.n[b] - 2);
+}
+
+// Blocked triangular solves with the LU factor in md->M.
+static int md_lu_solve(mf_md* md, double* x, cudaStream_t st) {
+  const int n = (int)md->topo.ninf;
+  const double* A = md->M.as<double>();
+  k_apply_pivots<<<1, 1, 0, st>>>(x, md->ipiv.as<int>(), n);
+  for (int k0 = 0; k0 < n; k0 += kTriBlock) {
+    const int nb = std::min(kTriBlock, n - k0);
+    k_tri_diag<<<1, 128, 0, st>>>(A, x, n, k0, nb, 0);
+    if (k0 + nb < n) k_tri_update<<<nblk(n - k0 - nb, 256), 256, 0, st>>>(A, x, n, k0, nb, k0 + nb, n);
+  }
+  for (int k0 = ((n - 1) / kTriBlock) * kTriBlock; k0 >= 0; k0 -= kTriBlock) {
+    const int nb = std::min(kTriBlock, n - k0);
+    k_tri_diag<<<1, 128, 0, st>>>(A, x, n, k0, nb, 1);
+    if (k0 > 0) k_tri_update<<<nblk(k0, 256), 256, 0, st>>>(A, x, n, k0, nb, 0, k0);
+  }
+  MF_CUDA(cudaGetLastError());
+  return MF_OK;
+}
+
+}  // namespace mf
+
+extern "C" {
+
+int mf_md_topology(const int nd[3], const int periods[3], const int* nint_x, const int* nint_y,
+                   const int* nint_z, int* dm_int, int* kind, int* size, int* offset, int* it,
+                   long long* ninf) {
+  if (!nd || !periods || !nint_x || !nint_y || !nint_z)
+    return set_error(MF_ERR_ARG, "mf_md_topology: null argument");
+  const int* nint[3] = {nint_x, nint_y, nint_z};
+  MdTopology t;
+  int rc = topology_build(nd, periods, nint, t);
+  if (rc) return rc;
+  if (dm_int) {
+    // Fortran order dm_int(nd1,nd2,nd3,3,2)
+    for (int i = 0; i < nd[0]; ++i)
+      for (int j = 0; j < nd[1]; ++j)
+        for (int k = 0; k < nd[2]; ++k)
+          for (int l = 0; l < 3; ++l)
+            for (int m = 0; m < 2; ++m)
+              dm_int[i + nd[0] * (j + nd[1] * (k + nd[2] * (l + 3 * m)))] = t.get(i, j, k, l, m);
+  }
+  for (int p = 0; p < t.it; ++p) {
+    if (kind) kind[p] = t.kind[p];
+    if (size) size[p] = t.size[p];
+    if (offset) offset[p] = t.offset[p];
+  }
+  if (it) *it = t.it;
+  if (ninf) *ninf = t.ninf;
+  return MF_OK;
+}
+
+int mf_md_create(const int nd[3], const int periods[3], const double* const* gridx, const int* nx,
+                 const double* const* gridy, const int* ny, const double* const* gridz, const int* nz,
+                 const int bct[6], int so, mf_md_t** out) {
+  if (!nd || !periods || !gridx || !gridy || !gridz || !nx || !ny || !nz || !bct || !out)
+    return set_error(MF_ERR_ARG, "mf_md_create: null argument");
+  *out = nullptr;
+  std::vector<int> nint[3];
+  const int* sizes[3] = {nx, ny, nz};
+  for (int l = 0; l < 3; ++l)
+    for (int s = 0; s < nd[l]; ++s) nint[l].push_back(sizes[l][s] - 2);
+  const int* np[3] = {nint[0].data(), nint[1].data(), nint[2].data()};
+  mf_md* md = new mf_md();
+  int rc = topology_build(nd, periods, np, md->topo);
+  if (rc) {
+    delete md;
+    return rc;
+  }
+  const int ns = nd[0] * nd[1] * nd[2];
+  md->sub.resize(ns);
+  size_t max_field = 0;
+  for (int k = 0; k < nd[2]; ++k)
+    for (int j = 0; j < nd[1]; ++j)
+      for (int i = 0; i < nd[0]; ++i) {
+        mf_md::Sub& sd = md->sub[md_sub_index(md, i, j, k)];
+        sd.n[0] = nx[i];
+        sd.n[1] = ny[j];
+        sd.n[2] = nz[k];
+        for (int f = 0; f < 6; ++f) sd.bct[f] = bct[f];
+        for (int l = 0; l < 3; ++l)
+          for (int m = 0; m < 2; ++m)
+            if (md->topo.get(i, j, k, l, m) > 0) sd.bct[2 * l + m] = 1;  // md_bc_init
+        const double* g[3] = {gridx[i], gridy[j], gridz[k]};
+        if ((rc = mf_solver_coeffs_init_3d(g[0], g[1], g[2], sd.n[0], sd.n[1], sd.n[2], sd.bct, so,
+                                           &sd.sc)))
+          break;
+        for (int l = 0; l < 3 && !rc; ++l) rc = mf_der_coeffs_init(g[l], sd.n[l], 1, so, &sd.dc[l]);
+        if (rc) break;
+        for (int l = 0; l < 3 && !rc; ++l) rc = sd.bc[l].ensure(sizeof(double) * 2 * face_points(sd, l));
+        if (rc) break;
+        max_field = std::max(max_field, (size_t)sd.n[0] * sd.n[1] * sd.n[2]);
+      }
+  if (!rc)
+    for (int l = 0; l < 3 && !rc; ++l) rc = md->du[l].ensure(max_field * 8);
+  if (!rc) rc = md->rint.ensure(max_field * 8);
+  if (!rc) rc = md->zero_int.ensure(max_field * 8);
+  if (!rc) rc = md->ufield.ensure(max_field * 8);
+  if (!rc) rc = md->vec.ensure(sizeof(double) * std::max<long long>(1, md->topo.ninf));
+  if (!rc && cudaMemset(md->zero_int.ptr, 0, max_field * 8) != cudaSuccess)
+    rc = set_error(MF_ERR_CUDA, "mf_md_create: memset failed");
+  if (rc) {
+    mf_md_destroy(md);
+    return rc;
+  }
+  *out = md;
+  return MF_OK;
+}
+
+int mf_md_destroy(mf_md_t* md) {
+  if (!md) return MF_OK;
+  for (auto& sd : md->sub) {
+    mf_solver3d_destroy(sd.sc);
+    for (int l = 0; l < 3; ++l) {
+      mf_der_destroy(sd.dc[l]);
+      sd.bc[l].release();
+    }
+  }
+  for (DevBuf* b : {&md->M, &md->ipiv, &md->vec, &md->info, &md->work, &md->zero_int, &md->du[0],
+                    &md->du[1], &md->du[2], &md->rint, &md->ufield})
+    b->release();
+  if (md->cs) cusolverDnDestroy(md->cs);
+  delete md;
+  return MF_OK;
+}
+
+int mf_md_ninf(const mf_md_t* md, long long* ninf, int* it) {
+  if (!md) return set_error(MF_ERR_ARG, "mf_md_ninf: null handle");
+  if (ninf) *ninf = md->topo.ninf;
+  if (it) *it = md->topo.it;
+  return MF_OK;
+}
+
+int mf_md_influence_matrix_set(mf_md_t* md, double sigma, int null_mode, void* stream) {
+  if (!md || null_mode < 0 || null_mode > 2)
+    return set_error(MF_ERR_ARG, "mf_md_influence_matrix_set: bad arguments");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const long long n = md->topo.ninf;
+  if (n == 0) return set_error(MF_ERR_ARG, "mf_md_influence_matrix_set: no interface");
+  md->sigma = sigma;
+  md->null_mode = null_mode;
+  int rc;
+  if ((rc = md->M.ensure(sizeof(double) * n * n)) || (rc = md->ipiv.ensure(sizeof(int) * n)) ||
+      (rc = md->info.ensure(sizeof(int))))
+    return rc;
+  MF_CUDA(cudaMemsetAsync(md->M.ptr, 0, sizeof(double) * n * n, st));
+  double* M = md->M.as<double>();
+  double* u = md->ufield.as<double>();
+  const MdTopology& t = md->topo;
+  // md_influence_matrix_set: a Dirac on every interface point of every
+  // subdomain, solved with g = 0; the signed normal derivatives on the
+  // subdomain's interface faces, negated, form that point's column.
+  for (int k = 0; k < t.nd[2]; ++k)
+    for (int j = 0; j < t.nd[1]; ++j)
+      for (int i = 0; i < t.nd[0]; ++i) {
+        const int s = md_sub_index(md, i, j, k);
+        mf_md::Sub& sd = md->sub[s];
+        const size_t nfull = (size_t)sd.n[0] * sd.n[1] * sd.n[2];
+        MF_CUDA(cudaMemsetAsync(u, 0, nfull * 8, st));
+        for (int m = 0; m < 2; ++m)
+          for (int l = 0; l < 3; ++l) {
+            const int p = t.get(i, j, k, l, m);
+            if (p <= 0) continue;
+            for (int q = 0; q < t.size[p - 1]; ++q) {
+              for (int l2 = 0; l2 < 3; ++l2)
+                MF_CUDA(cudaMemsetAsync(sd.bc[l2].ptr, 0, sizeof(double) * 2 * face_points(sd, l2), st));
+              const long long nf = face_points(sd, l);
+              k_face_set<<<nblk(nf, 128), 128, 0, st>>>(sd.bc[l].as<double>(), nf, m, nullptr, 0, 2,
+                                                        (double)q);
+              MF_CUDA(cudaGetLastError());
+              if ((rc = md_sub_solve(md, s, md->zero_int.as<double>(), u, st))) return rc;
+              double* col = M + (long long)n * (t.offset[p - 1] + q);
+              if ((rc = md_gather(md, i, j, k, u, col, -1.0, st))) return rc;
+            }
+          }
+      }
+  if (null_mode >= 1) {
+    k_pin_row0<<<nblk(n, 256), 256, 0, st>>>(M, (int)n);
+    MF_CUDA(cudaGetLastError());
+  }
+  // LU factorisation (set-up): cuSOLVER getrf, FP64
+  if (!md->cs && cusolverDnCreate(&md->cs) != CUSOLVER_STATUS_SUCCESS)
+    return set_error(MF_ERR_CUDA, "cusolverDnCreate failed");
+  cusolverDnSetStream(md->cs, st);
+  int lwork = 0;
+  if (cusolverDnDgetrf_bufferSize(md->cs, (int)n, (int)n, M, (int)n, &lwork) != CUSOLVER_STATUS_SUCCESS)
+    return set_error(MF_ERR_CUDA, "getrf buffer query failed");
+  if ((rc = md->work.ensure(sizeof(double) * std::max(1, lwork)))) return rc;
+  if (cusolverDnDgetrf(md->cs, (int)n, (int)n, M, (int)n, md->work.as<double>(), md->ipiv.as<int>(),
+                       md->info.as<int>()) != CUSOLVER_STATUS_SUCCESS)
+    return set_error(MF_ERR_CUDA, "getrf failed");
+  int hinfo = 0;
+  MF_CUDA(cudaMemcpyAsync(&hinfo, md->info.ptr, sizeof(int), cudaMemcpyDeviceToHost, st));
+  MF_CUDA(cudaStreamSynchronize(st));
+  if (hinfo != 0)
+    return set_error(MF_ERR_SINGULAR, "influence matrix is singular (getrf info %d)%s", hinfo,
+                     null_mode ? "" : "; an all-Neumann problem needs a null-space mode");
+  md->factored = true;
+  return MF_OK;
+}
+
+int mf_md_solve(mf_md_t* md, const double* const* g, double* const* u, const double* const* bcx,
+                const double* const* bcy, const double* const* bcz, void* stream) {
+  if (!md || !g || !u || !bcx || !bcy || !bcz) return set_error(MF_ERR_ARG, "mf_md_solve: null argument");
+  if (!md->factored) return set_error(MF_ERR_ARG, "mf_md_solve: influence matrix not set");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const MdTopology& t = md->topo;
+  const long long n = t.ninf;
+  double* vec = md->vec.as<double>();
+  const int ns = (int)md->sub.size();
+  for (int s = 0; s < ns; ++s)
+    for (const void* p : {(const void*)g[s], (const void*)u[s], (const void*)bcx[s],
+                          (const void*)bcy[s], (const void*)bcz[s]})
+      if (!is_device_ptr(p)) return set_error(MF_ERR_ARG, "mf_md_solve: device pointers only");
+  MF_CUDA(cudaMemsetAsync(vec, 0, sizeof(double) * n, st));
+  int rc;
+  auto load_bc = [&](int s, int i, int j, int k, int mode) -> int {
+    mf_md::Sub& sd = md->sub[s];
+    const double* src[3] = {bcx[s], bcy[s], bcz[s]};
+    for (int l = 0; l < 3; ++l) {
+      const long long nf = face_points(sd, l);
+      MF_CUDA(cudaMemcpyAsync(sd.bc[l].ptr, src[l], sizeof(double) * 2 * nf, cudaMemcpyDeviceToDevice, st));
+      for (int m = 0; m < 2; ++m) {
+        const int p = t.get(i, j, k, l, m);
+        if (p <= 0) continue;
+        k_face_set<<<nblk(nf, 128), 128, 0, st>>>(sd.bc[l].as<double>(), nf, m, vec, t.offset[p - 1],
+                                                  mode, 0.0);
+        MF_CUDA(cudaGetLastError());
+      }
+    }
+    return MF_OK;
+  };
+  // 1. homogeneous-interface solves and the signed derivative jumps
+  for (int k = 0; k < t.nd[2]; ++k)
+    for (int j = 0; j < t.nd[1]; ++j)
+      for (int i = 0; i < t.nd[0]; ++i) {
+        const int s = md_sub_index(md, i, j, k);
+        mf_md::Sub& sd = md->sub[s];
+        if ((rc = load_bc(s, i, j, k, 0))) return rc;
+        const long long tot = (long long)(sd.n[0] - 2) * (sd.n[1] - 2) * (sd.n[2] - 2);
+        k_extract_int<<<nblk(tot, 256), 256, 0, st>>>(g[s], md->rint.as<double>(), sd.n[0] - 2,
+                                                       sd.n[1] - 2, sd.n[2] - 2);
+        MF_CUDA(cudaGetLastError());
+        if ((rc = md_sub_solve(md, s, md->rint.as<double>(), u[s], st))) return rc;
+        if ((rc = md_gather(md, i, j, k, u[s], vec, 1.0, st))) return rc;
+      }
+  // 2. interface system (null-space handling as md_rhs_nullspace / md_vector_zero_lastpoint)
+  if (md->null_mode == 1) {
+    k_remove_mean<<<1, 256, 0, st>>>(vec, (int)n);
+  }
+  if (md->null_mode >= 1) k_set_scalar<<<1, 1, 0, st>>>(vec, 0, 0.0);
+  if ((rc = md_lu_solve(md, vec, st))) return rc;
+  if (md->null_mode == 1) k_remove_mean<<<1, 256, 0, st>>>(vec, (int)n);
+  MF_CUDA(cudaGetLastError());
+  // 3. final solves with the interface values
+  for (int k = 0; k < t.nd[2]; ++k)
+    for (int j = 0; j < t.nd[1]; ++j)
+      for (int i = 0; i < t.nd[0]; ++i) {
+        const int s = md_sub_index(md, i, j, k);
+        mf_md::Sub& sd = md->sub[s];
+        if ((rc = load_bc(s, i, j, k, 1))) return rc;
+        const long long tot = (long long)(sd.n[0] - 2) * (sd.n[1] - 2) * (sd.n[2] - 2);
+        k_extract_int<<<nblk(tot, 256), 256, 0, st>>>(g[s], md->rint.as<double>(), sd.n[0] - 2,
+                                                       sd.n[1] - 2, sd.n[2] - 2);
+        MF_CUDA(cudaGetLastError());
+        if ((rc = md_sub_solve(md, s, md->rint.as<double>(), u[s], st))) return rc;
+      }
+  return MF_OK;
+}
+
+int mf_md_interface(const mf_md_t* md, double* lambda) {
+  if (!md || !lambda) return set_error(MF_ERR_ARG, "mf_md_interface: null argument");
+  MF_CUDA(cudaDeviceSynchronize());
+  MF_CUDA(cudaMemcpy(lambda, md->vec.ptr, sizeof(double) * md->topo.ninf, cudaMemcpyDeviceToHost));
+  return MF_OK;
+}
+
+}  // extern "C"

@@ -96,6 +96,16 @@ _PROTOS = {
     "mf_solver_residual": [_P, _P, _P, _D, _P, _P, _P, _P, _I, _I, _I, _P],
     "mf_solver3d_set_eigen": [_P, _I, _DP, _DP, _DP],
     "mf_solver3d_device_status": [_P],
+    "mf_md_topology": [_IP, _IP, _IP, _IP, _IP, _IP, _IP, _IP, _IP, _IP,
+                       ctypes.POINTER(ctypes.c_longlong)],
+    "mf_md_create": [_IP, _IP, ctypes.POINTER(_DP), _IP, ctypes.POINTER(_DP), _IP,
+                     ctypes.POINTER(_DP), _IP, _IP, _I, ctypes.POINTER(_P)],
+    "mf_md_destroy": [_P],
+    "mf_md_ninf": [_P, ctypes.POINTER(ctypes.c_longlong), _IP],
+    "mf_md_influence_matrix_set": [_P, _D, _I, _P],
+    "mf_md_solve": [_P, ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.POINTER(_P),
+                    ctypes.POINTER(_P), ctypes.POINTER(_P), _P],
+    "mf_md_interface": [_P, _DP],
     "mf_solver3d_profile": [_P, _I],
     "mf_solver3d_profile_read": [_P, _I, _DP, ctypes.POINTER(ctypes.c_longlong)],
 }
@@ -403,3 +413,94 @@ def solve_3d(sc, rhs, sigma, solf, bcx, bcy, bcz, n1=None, n2=None, n3=None, **k
 
 def solver_3d(sc, g, u, bcx, bcy, bcz, sigma, **kw):
     return sc.solver_3d(g, u, bcx, bcy, bcz, sigma, **kw)
+
+
+# ---------------------------------------------------------------------------
+# multidomain
+# ---------------------------------------------------------------------------
+
+def _ivec(v):
+    return (ctypes.c_int * len(v))(*[int(x) for x in v])
+
+
+def md_topology(nd, periods, nint):
+    """Interface numbering (md_influence_matrix_param): returns dict with
+    dm_int (nd1,nd2,nd3,3,2) 1-based ids, kind, size, offset, it, ninf."""
+    nd1, nd2, nd3 = (int(v) for v in nd)
+    dm = np.zeros(nd1 * nd2 * nd3 * 6, dtype=np.int32)
+    maxit = 3 * nd1 * nd2 * nd3
+    kind = np.zeros(maxit, dtype=np.int32)
+    size = np.zeros(maxit, dtype=np.int32)
+    off = np.zeros(maxit, dtype=np.int32)
+    it = ctypes.c_int()
+    ninf = ctypes.c_longlong()
+    ip = lambda a: a.ctypes.data_as(_IP)
+    _check(_lib.mf_md_topology(_ivec(nd), _ivec(periods), _ivec(nint[0]), _ivec(nint[1]),
+                               _ivec(nint[2]), ip(dm), ip(kind), ip(size), ip(off),
+                               ctypes.byref(it), ctypes.byref(ninf)))
+    n = it.value
+    return {"dm_int": dm.reshape((nd1, nd2, nd3, 3, 2), order="F"), "kind": kind[:n],
+            "size": size[:n], "offset": off[:n], "it": n, "ninf": ninf.value}
+
+
+class MultiDomain:
+    """All subdomains on the GPU, coupled by the influence matrix."""
+
+    def __init__(self, nd, periods, gx, gy, gz, bct, so=6):
+        self.nd = tuple(int(v) for v in nd)
+        self._keep = [np.ascontiguousarray(g, dtype=np.float64) for g in list(gx) + list(gy) + list(gz)]
+        k = 0
+        arrs = []
+        for lst in (gx, gy, gz):
+            ptrs = (_DP * len(lst))()
+            for s in range(len(lst)):
+                ptrs[s] = self._keep[k].ctypes.data_as(_DP)
+                k += 1
+            arrs.append(ptrs)
+        self.sizes = ([len(g) for g in gx], [len(g) for g in gy], [len(g) for g in gz])
+        self._h = ctypes.c_void_p()
+        _check(_lib.mf_md_create(_ivec(nd), _ivec(periods), arrs[0], _ivec(self.sizes[0]), arrs[1],
+                                 _ivec(self.sizes[1]), arrs[2], _ivec(self.sizes[2]), _ivec(bct), so,
+                                 ctypes.byref(self._h)))
+
+    def shape(self, i, j, k):
+        return (self.sizes[0][i], self.sizes[1][j], self.sizes[2][k])
+
+    def subdomains(self):
+        nd1, nd2, nd3 = self.nd
+        return [(i, j, k) for k in range(nd3) for j in range(nd2) for i in range(nd1)]
+
+    def ninf(self):
+        n = ctypes.c_longlong()
+        it = ctypes.c_int()
+        _check(_lib.mf_md_ninf(self._h, ctypes.byref(n), ctypes.byref(it)))
+        return n.value
+
+    def influence_matrix_set(self, sigma, null=0, stream=None):
+        _check(_lib.mf_md_influence_matrix_set(self._h, float(sigma), int(null), _stream(stream)))
+
+    def solve(self, g, u, bc, stream=None):
+        """g, u: {(i,j,k): device field}; bc: {(i,j,k): (bcx, bcy, bcz)}."""
+        subs = self.subdomains()
+        n = len(subs)
+        mk = lambda seq: (_P * n)(*[_arg(a) for a in seq])
+        _check(_lib.mf_md_solve(self._h, mk([g[c] for c in subs]), mk([u[c] for c in subs]),
+                                mk([bc[c][0] for c in subs]), mk([bc[c][1] for c in subs]),
+                                mk([bc[c][2] for c in subs]), _stream(stream)))
+        return u
+
+    def interface(self):
+        lam = np.zeros(self.ninf())
+        _check(_lib.mf_md_interface(self._h, lam.ctypes.data_as(_DP)))
+        return lam
+
+    def close(self):
+        if self._h:
+            _lib.mf_md_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
