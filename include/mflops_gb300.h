@@ -243,6 +243,66 @@ int mf_md_solve(mf_md_t* md, const double* const* g, double* const* u, const dou
 /* Copies the last interface solution (ninf values) to host memory. */
 int mf_md_interface(const mf_md_t* md, double* lambda);
 
+/* ------------------------------------------------------------------------
+ * Least-squares B-spline filter (class_filter).  For fixed data sites,
+ * weights and knots the fit is a linear operator P (no x ni) shared by every
+ * pencil of an axis; P' gives the first derivative.
+ * ---------------------------------------------------------------------- */
+typedef struct mf_filter mf_filter_t;
+
+/* Operators of LSQUnivariateSpline(ni,xi,yi,wi,nn,xn,no,xo,yo,ypo,k),
+ * src/class_filter/class_filter.f90:104-174 (fixed-knot weighted least
+ * squares of degree k, knots (k+1)*xi(1), xn(2:nn-1), (k+1)*xi(ni); values
+ * and first derivatives at xo).  Host only; P, Pd are (no,ni) Fortran-ordered,
+ * either may be NULL; wi may be NULL (unit weights). */
+int mf_filter_lsq_matrix(const double* xi, int ni, const double* wi, const double* xn, int nn,
+                         const double* xo, int no, int k, double* P, double* Pd);
+/* Operators of interp_period(ni,xi,yi,nos,xos,yos), class_filter.f90:267-347
+ * (periodic quintic least squares on nn = ni-6 equispaced nodes, evaluated at
+ * xos; the last data point only fixes the period).  Host only. */
+int mf_filter_period_matrix(const double* xi, int ni, const double* xos, int nos, double* P,
+                            double* Pd);
+/* Handles holding the operators on the device (filter type + flt_init,
+ * class_filter.f90:9-73). */
+int mf_filter_lsq_init(const double* xi, int ni, const double* wi, const double* xn, int nn,
+                       const double* xo, int no, int k, mf_filter_t** f);
+int mf_filter_period_init(const double* xi, int ni, const double* xos, int nos, mf_filter_t** f);
+int mf_filter_destroy(mf_filter_t* f);
+int mf_filter_matrix(const mf_filter_t* f, int deriv, double* P);
+/* Applies the filter (deriv = 0) or its derivative (deriv = 1) along `axis`
+ * of an (nx,ny,nz) field whose length along that axis is ni; out has no
+ * points along it.  Host or device pointers. */
+int mf_filter_apply(const mf_filter_t* f, int axis, int deriv, const double* in, int nx, int ny,
+                    int nz, double* out, void* stream);
+/* Pencil forms with the reference's signatures (one pencil; GPU apply). */
+int mf_lsq_univariate_spline(int ni, const double* xi, const double* yi, const double* wi, int nn,
+                             const double* xn, int no, const double* xo, double* yo, double* ypo,
+                             int k);
+int mf_interp_period(int ni, const double* xi, const double* yi, int nos, const double* xos,
+                     double* yos);
+
+/* ------------------------------------------------------------------------
+ * LES eddy viscosity: navier_LES, src/class_navier/class_navier_3D.f90:1225-1455
+ * (with les_sigma, :1458-1502).  les_type 0 none, 1 Smagorinsky, 2 WALE,
+ * 3 sigma model; nu is multiplied by (dx^2+dy^2+dz^2)/3 (one-sided spacing
+ * at the ends) and is zero on the twelve edge lines.
+ * ---------------------------------------------------------------------- */
+typedef struct mf_les mf_les_t;
+
+/* Grids of the three axes (host), as in navier%gridx/gridy/gridz. */
+int mf_les_create(const double* gx, int nx, const double* gy, int ny, const double* gz, int nz,
+                  mf_les_t** les);
+int mf_les_destroy(mf_les_t* les);
+/* nu from the nine gradient fields du[3*i+j] = d u_i / d x_j (device, (nx,ny,nz)). */
+int mf_les_nu(const mf_les_t* les, int les_type, double c, const double* const* du, double* nu,
+              void* stream);
+/* Whole navier_LES step from the velocity: the nine first derivatives of
+ * u, v, w with the derivative handles of x, y and z (derx/dery/derz), then
+ * nu.  Device pointers; the gradients live in scratch owned by `les`. */
+int mf_les_nu_velocity(mf_les_t* les, const mf_der_t* dcx, const mf_der_t* dcy,
+                       const mf_der_t* dcz, int les_type, double c, const double* u,
+                       const double* v, const double* w, double* nu, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

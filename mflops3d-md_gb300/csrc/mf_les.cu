@@ -1,0 +1,193 @@
+// LES eddy viscosity on GB300: one fused pointwise kernel over the nine
+// velocity-gradient fields (navier_LES, class_navier_3D.f90:1225-1455, and
+// les_sigma, :1458-1502): Smagorinsky, WALE or sigma model, times
+// Delta^2 = (dx^2 + dy^2 + dz^2)/3, zero on the edge lines (field_zero_edges,
+// class_field.f90:366-391; gradients on edges count as zero as well).
+// 72 bytes read + 8 written per point: HBM-bound except the sigma model's
+// FP64 acos/cos, which the narrow FP64 pipe of GB300 makes compute-heavy.
+#include <cmath>
+#include <vector>
+
+#include "mf_internal.h"
+
+namespace mf {
+
+// The reference compares with default-kind (single precision) 1e-10.
+static __device__ __constant__ double kLesThresh = (double)1e-10f;
+
+struct LesGrad {
+  const double* g[9];  // g[3*i + j] = d u_i / d x_j
+};
+
+__device__ __forceinline__ bool on_edge(int i, int j, int k, int nx, int ny, int nz) {
+  const int e = (i == 0 || i == nx - 1) + (j == 0 || j == ny - 1) + (k == 0 || k == nz - 1);
+  return e >= 2;
+}
+
+__global__ void k_les_nu(LesGrad d, const double* __restrict__ dx2, const double* __restrict__ dy2,
+                         const double* __restrict__ dz2, int nx, int ny, int nz, int type, double c,
+                         double* __restrict__ nu) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)nx * ny * nz) return;
+  const int i = (int)(idx % nx);
+  const long long jk = idx / nx;
+  const int j = (int)(jk % ny), k = (int)(jk / ny);
+  if (type == 0 || on_edge(i, j, k, nx, ny, nz)) {
+    nu[idx] = 0.0;
+    return;
+  }
+  double g[3][3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b) g[a][b] = d.g[3 * a + b][idx];
+  double v = 0.0;
+  if (type == 1 || type == 2) {
+    double ss = 0.0;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      ss += g[a][a] * g[a][a];
+#pragma unroll
+      for (int b = a + 1; b < 3; ++b) ss += 0.5 * (g[a][b] + g[b][a]) * (g[a][b] + g[b][a]);
+    }
+    if (type == 1) {
+      v = c * sqrt(2.0 * ss);
+    } else {
+      double g2[3][3];
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) g2[a][b] = g[a][0] * g[0][b] + g[a][1] * g[1][b] + g[a][2] * g[2][b];
+      const double tr = g2[0][0] + g2[1][1] + g2[2][2];
+      double sd = 0.0;
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+          double s = 0.5 * (g2[a][b] + g2[b][a]);
+          if (a == b) s -= tr / 3.0;
+          sd += s * s;
+        }
+      v = (sd < kLesThresh) ? 0.0 : c * pow(sd, 1.5) / (pow(ss, 2.5) + pow(sd, 1.25));
+    }
+  } else {
+    // sigma model: singular values of g from the invariants of g g^T
+    double G[3][3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int b = 0; b < 3; ++b) G[a][b] = g[a][0] * g[b][0] + g[a][1] * g[b][1] + g[a][2] * g[b][2];
+    const double i1 = G[0][0] + G[1][1] + G[2][2];
+    const double i2 = G[0][0] * G[1][1] + G[0][0] * G[2][2] + G[1][1] * G[2][2] - G[0][1] * G[1][0] -
+                      G[0][2] * G[2][0] - G[1][2] * G[2][1];
+    const double i3 = G[0][0] * G[1][1] * G[2][2] + G[1][0] * G[2][1] * G[0][2] +
+                      G[2][0] * G[0][1] * G[1][2] - G[0][2] * G[1][1] * G[2][0] -
+                      G[1][2] * G[2][1] * G[0][0] - G[2][2] * G[0][1] * G[1][0];
+    const double a1 = i1 * i1 / 9.0 - i2 / 3.0;
+    const double a2 = i1 * i1 * i1 / 27.0 - i1 * i2 / 6.0 + i3 / 2.0;
+    const double a3 = (a1 < kLesThresh) ? 0.0 : acos(a2 / pow(a1, 1.5)) / 3.0;
+    const double pi = 3.14159265358979323846;
+    const double sq = sqrt(fmax(a1, 0.0));
+    double s1 = i1 / 3.0 + 2.0 * sq * cos(a3);
+    double s2 = i1 / 3.0 - 2.0 * sq * cos(a3 + pi / 3.0);
+    double s3 = i1 - s1 - s2;
+    s1 = sqrt(fmax(s1, 0.0));
+    s2 = sqrt(fmax(s2, 0.0));
+    s3 = sqrt(fmax(s3, 0.0));
+    v = (s1 < kLesThresh) ? 0.0 : c * s3 * (s1 - s2) * (s2 - s3) / (s1 * s1);
+  }
+  nu[idx] = v * ((dx2[i] + dy2[j] + dz2[k]) / 3.0);
+}
+
+}  // namespace mf
+
+using namespace mf;
+
+struct mf_les {
+  int n[3] = {0, 0, 0};
+  DevBuf d2[3];  // squared spacings per axis
+  DevBuf grad;   // nine gradient fields for mf_les_nu_velocity
+};
+
+extern "C" {
+
+int mf_les_create(const double* gx, int nx, const double* gy, int ny, const double* gz, int nz,
+                  mf_les_t** out) {
+  if (!gx || !gy || !gz || !out || nx < 2 || ny < 2 || nz < 2)
+    return set_error(MF_ERR_ARG, "mf_les_create: bad arguments");
+  *out = nullptr;
+  mf_les* les = new mf_les();
+  const double* g[3] = {gx, gy, gz};
+  const int n[3] = {nx, ny, nz};
+  for (int a = 0; a < 3; ++a) {
+    les->n[a] = n[a];
+    std::vector<double> d2(n[a]);
+    for (int i = 0; i < n[a]; ++i) {
+      double d;
+      if (i == 0) d = g[a][1] - g[a][0];
+      else if (i == n[a] - 1) d = g[a][i] - g[a][i - 1];
+      else d = (g[a][i + 1] - g[a][i - 1]) * 0.5;
+      d2[i] = d * d;
+    }
+    int rc = les->d2[a].ensure(n[a] * 8);
+    if (!rc && cudaMemcpy(les->d2[a].ptr, d2.data(), n[a] * 8, cudaMemcpyHostToDevice) != cudaSuccess)
+      rc = set_error(MF_ERR_CUDA, "mf_les_create: upload failed");
+    if (rc) {
+      mf_les_destroy(les);
+      return rc;
+    }
+  }
+  *out = les;
+  return MF_OK;
+}
+
+int mf_les_destroy(mf_les_t* les) {
+  if (!les) return MF_OK;
+  for (auto& b : les->d2) b.release();
+  les->grad.release();
+  delete les;
+  return MF_OK;
+}
+
+int mf_les_nu(const mf_les_t* les, int les_type, double c, const double* const* du, double* nu,
+              void* stream) {
+  if (!les || !du || !nu || les_type < 0 || les_type > 3)
+    return set_error(MF_ERR_ARG, "mf_les_nu: bad arguments");
+  LesGrad d;
+  for (int q = 0; q < 9; ++q) {
+    if (!du[q] || !is_device_ptr(du[q])) return set_error(MF_ERR_ARG, "mf_les_nu: device gradients required");
+    d.g[q] = du[q];
+  }
+  if (!is_device_ptr(nu)) return set_error(MF_ERR_ARG, "mf_les_nu: device output required");
+  const long long tot = (long long)les->n[0] * les->n[1] * les->n[2];
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  k_les_nu<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(
+      d, les->d2[0].as<double>(), les->d2[1].as<double>(), les->d2[2].as<double>(), les->n[0],
+      les->n[1], les->n[2], les_type, c, nu);
+  MF_CUDA(cudaGetLastError());
+  return MF_OK;
+}
+
+int mf_les_nu_velocity(mf_les_t* les, const mf_der_t* dcx, const mf_der_t* dcy,
+                       const mf_der_t* dcz, int les_type, double c, const double* u,
+                       const double* v, const double* w, double* nu, void* stream) {
+  if (!les || !dcx || !dcy || !dcz || !u || !v || !w || !nu)
+    return set_error(MF_ERR_ARG, "mf_les_nu_velocity: bad arguments");
+  const int nx = les->n[0], ny = les->n[1], nz = les->n[2];
+  const size_t tot = (size_t)nx * ny * nz;
+  int rc = les->grad.ensure(9 * tot * sizeof(double));
+  if (rc) return rc;
+  const double* vel[3] = {u, v, w};
+  const mf_der_t* dc[3] = {dcx, dcy, dcz};
+  const double* du[9];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      double* g = les->grad.as<double>() + (3 * i + j) * tot;
+      rc = mf_der_apply(dc[j], j, 1, vel[i], g, nx, ny, nz, stream);
+      if (rc) return rc;
+      du[3 * i + j] = g;
+    }
+  return mf_les_nu(les, les_type, c, du, nu, stream);
+}
+
+}  // extern "C"

@@ -106,6 +106,19 @@ _PROTOS = {
     "mf_md_solve": [_P, ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.POINTER(_P),
                     ctypes.POINTER(_P), ctypes.POINTER(_P), _P],
     "mf_md_interface": [_P, _DP],
+    "mf_filter_lsq_matrix": [_DP, _I, _DP, _DP, _I, _DP, _I, _I, _DP, _DP],
+    "mf_filter_period_matrix": [_DP, _I, _DP, _I, _DP, _DP],
+    "mf_filter_lsq_init": [_DP, _I, _DP, _DP, _I, _DP, _I, _I, ctypes.POINTER(_P)],
+    "mf_filter_period_init": [_DP, _I, _DP, _I, ctypes.POINTER(_P)],
+    "mf_filter_destroy": [_P],
+    "mf_filter_matrix": [_P, _I, _DP],
+    "mf_filter_apply": [_P, _I, _I, _P, _I, _I, _I, _P, _P],
+    "mf_lsq_univariate_spline": [_I, _DP, _DP, _DP, _I, _DP, _I, _DP, _DP, _DP, _I],
+    "mf_interp_period": [_I, _DP, _DP, _I, _DP, _DP],
+    "mf_les_create": [_DP, _I, _DP, _I, _DP, _I, ctypes.POINTER(_P)],
+    "mf_les_destroy": [_P],
+    "mf_les_nu": [_P, _I, _D, ctypes.POINTER(_P), _P, _P],
+    "mf_les_nu_velocity": [_P, _P, _P, _P, _I, _D, _P, _P, _P, _P, _P],
     "mf_solver3d_profile": [_P, _I],
     "mf_solver3d_profile_read": [_P, _I, _DP, ctypes.POINTER(ctypes.c_longlong)],
 }
@@ -497,6 +510,147 @@ class MultiDomain:
     def close(self):
         if self._h:
             _lib.mf_md_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ---------------------------------------------------------------------------
+# spline filter
+# ---------------------------------------------------------------------------
+
+def filter_lsq_matrix(xi, wi, xn, xo, k):
+    """(P, P') of LSQUnivariateSpline as (no, ni) arrays (host only)."""
+    xi, xp = _dptr(xi)
+    xn, np_ = _dptr(xn)
+    xo, op = _dptr(xo)
+    wp = None
+    if wi is not None:
+        wi, wp = _dptr(wi)
+    P = np.zeros((xo.size, xi.size), order="F")
+    Pd = np.zeros((xo.size, xi.size), order="F")
+    _check(_lib.mf_filter_lsq_matrix(xp, xi.size, wp, np_, xn.size, op, xo.size, k,
+                                     P.ctypes.data_as(_DP), Pd.ctypes.data_as(_DP)))
+    return P, Pd
+
+
+def filter_period_matrix(xi, xos):
+    xi, xp = _dptr(xi)
+    xos, op = _dptr(xos)
+    P = np.zeros((xos.size, xi.size), order="F")
+    Pd = np.zeros((xos.size, xi.size), order="F")
+    _check(_lib.mf_filter_period_matrix(xp, xi.size, op, xos.size, P.ctypes.data_as(_DP),
+                                        Pd.ctypes.data_as(_DP)))
+    return P, Pd
+
+
+class SplineFilter:
+    """Filter handle: LSQ (xn, k given) or periodic (xn None, k = 5)."""
+
+    def __init__(self, xi, xo, xn=None, wi=None, k=5):
+        self._keep = []
+        xi, xp = _dptr(xi)
+        xo, op = _dptr(xo)
+        self.ni, self.no = xi.size, xo.size
+        self._h = ctypes.c_void_p()
+        if xn is None:
+            _check(_lib.mf_filter_period_init(xp, xi.size, op, xo.size, ctypes.byref(self._h)))
+        else:
+            xn, np_ = _dptr(xn)
+            wp = None
+            if wi is not None:
+                wi, wp = _dptr(wi)
+            self._keep = [xi, xo, xn, wi]
+            _check(_lib.mf_filter_lsq_init(xp, xi.size, wp, np_, xn.size, op, xo.size, k,
+                                           ctypes.byref(self._h)))
+
+    def apply(self, f, axis, deriv=False, out=None, stream=None):
+        shape = list(f.shape)
+        shape[axis] = self.no
+        if out is None:
+            out = empty_device(tuple(shape)) if hasattr(f, "data_ptr") else np.zeros(shape, order="F")
+        _check(_lib.mf_filter_apply(self._h, axis, 1 if deriv else 0, _arg(f), f.shape[0], f.shape[1],
+                                    f.shape[2], _arg(out), _stream(stream)))
+        return out
+
+    def close(self):
+        if self._h:
+            _lib.mf_filter_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def lsq_univariate_spline(xi, yi, wi, xn, xo, k):
+    """LSQUnivariateSpline(ni,xi,yi,wi,nn,xn,no,xo,yo,ypo,k) -> (yo, ypo)."""
+    xi, xp = _dptr(xi)
+    yi, yp = _dptr(yi)
+    wi, wp = _dptr(wi)
+    xn, np_ = _dptr(xn)
+    xo, op = _dptr(xo)
+    yo = np.zeros(xo.size)
+    ypo = np.zeros(xo.size)
+    _check(_lib.mf_lsq_univariate_spline(xi.size, xp, yp, wp, xn.size, np_, xo.size, op,
+                                         yo.ctypes.data_as(_DP), ypo.ctypes.data_as(_DP), k))
+    return yo, ypo
+
+
+def interp_period(xi, yi, xos):
+    """interp_period(ni,xi,yi,nos,xos,yos) -> yos."""
+    xi, xp = _dptr(xi)
+    yi, yp = _dptr(yi)
+    xos, op = _dptr(xos)
+    yos = np.zeros(xos.size)
+    _check(_lib.mf_interp_period(xi.size, xp, yp, xos.size, op, yos.ctypes.data_as(_DP)))
+    return yos
+
+
+LES_TYPES = {"none": 0, "smagorinsky": 1, "wale": 2, "sigma": 3}
+
+
+class LesModel:
+    """navier_LES eddy viscosity on the grids (gx, gy, gz) (device fields)."""
+
+    def __init__(self, gx, gy, gz):
+        gx, xp = _dptr(gx)
+        gy, yp = _dptr(gy)
+        gz, zp = _dptr(gz)
+        self.shape = (gx.size, gy.size, gz.size)
+        self._h = ctypes.c_void_p()
+        _check(_lib.mf_les_create(xp, gx.size, yp, gy.size, zp, gz.size, ctypes.byref(self._h)))
+
+    @staticmethod
+    def _type(les_type):
+        return LES_TYPES[les_type] if isinstance(les_type, str) else int(les_type)
+
+    def nu(self, du, les_type, c, out=None, stream=None):
+        """du: 3x3 nested sequence of device fields, du[i][j] = d u_i / d x_j."""
+        if out is None:
+            out = empty_device(self.shape)
+        ptrs = (_P * 9)(*[_arg(du[i][j]) for i in range(3) for j in range(3)])
+        _check(_lib.mf_les_nu(self._h, self._type(les_type), float(c), ptrs, _arg(out),
+                              _stream(stream)))
+        return out
+
+    def nu_velocity(self, dcx, dcy, dcz, u, v, w, les_type, c, out=None, stream=None):
+        if out is None:
+            out = empty_device(self.shape)
+        _check(_lib.mf_les_nu_velocity(self._h, dcx._h, dcy._h, dcz._h, self._type(les_type),
+                                       float(c), _arg(u), _arg(v), _arg(w), _arg(out),
+                                       _stream(stream)))
+        return out
+
+    def close(self):
+        if self._h:
+            _lib.mf_les_destroy(self._h)
             self._h = ctypes.c_void_p()
 
     def __del__(self):
