@@ -43,8 +43,11 @@ struct AxisDev {
   double neum[14] = {0};
   DevBuf V, Vinv, eig, invl4, rows;           // FP64
   DevBuf Vh, Vl, Vih, Vil, eigf, nullf;       // mixed path (padded P x P)
+  DevBuf Vh32, Vl32, Vih32, Vil32;             // 3xTF32 planes (FP32, padded P x P)
   DevBuf invl4f;                               // FP32 copy of invl4
   DevBuf rowsf;                                // FP32 copy of rows
+  DevBuf tri;                                  // TriRow[n] when the lhs is tridiagonal
+  bool tri_ok = false;
 };
 
 }  // namespace mf
@@ -59,11 +62,13 @@ struct mf_solver3d {
   DevBuf st_rhs, st_solf, st_bc[3];            // host staging
   DevBuf R, R2;                                // FP64 scratch of the residual
   DevBuf U32, C32, R1f;                        // mixed path: u1, correction, r1 (FP32)
-  DevBuf Xa_hi, Xa_lo, Xb_hi, Xb_lo;           // mixed path split planes
+  DevBuf Xa_hi, Xa_lo, Xb_hi, Xb_lo;           // split-BF16 planes
+  DevBuf Xa32, Xb32;                           // 3xTF32 operands (FP32)
   DevBuf err;                                  // device error flag (int)
   DevBuf foldf;                                // FP32 c*bc face products (mixed path)
   TcPlan* plan[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
-  bool mixed_ready = false;
+  TcPlan* plan32[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  bool mixed_ready = false, mixed32_ready = false;
   StageProfiler prof;
 };
 
@@ -235,8 +240,9 @@ __global__ void k_faces(double* solf, const double* __restrict__ bc, FaceArgs f)
 // The forward-elimination values go to a scratch array; the final store:
 //   mode 0 (first pass):  out = rin - sigma*u - L u
 //   mode 1 (middle pass): out = rin - L u
-//   mode 2 (last pass):   split-BF16 planes of rin - L u in the padded
-//                         (P1,P2,P3) layout of the tensor-core transforms
+//   mode 2 (last pass):   rin - L u in the padded (P1,P2,P3) layout of the
+//                         tensor-core transforms: split-BF16 planes, or FP32
+//                         (x32) for the 3xTF32 transforms
 //   mode 3 (last pass):   mode 2, and rin - L u also stored as FP32 (r32).
 template <class T, class In>
 struct ResidFin {
@@ -247,6 +253,7 @@ struct ResidFin {
   T* out;                // modes 0,1: result array, offset to the line
   __nv_bfloat16* hi;     // modes 2,3: planes, offset to the line's padded base
   __nv_bfloat16* lo;
+  float* x32;            // modes 2,3 (3xTF32): FP32 operand, same offsets
   long long pstride;     // modes 2,3: padded stride along the line
   float* r32;            // mode 3: offset to the line
   __device__ __forceinline__ void operator()(T*, int i, long long idx, T y) const {
@@ -256,9 +263,13 @@ struct ResidFin {
       out[idx] = rin[idx] - y;
     } else {
       const float v = (float)(rin[idx] - y);
-      const __nv_bfloat16 h = __float2bfloat16_rn(v);
-      hi[i * pstride] = h;
-      lo[i * pstride] = __float2bfloat16_rn(v - __bfloat162float(h));
+      if (x32) {
+        x32[i * pstride] = v;
+      } else {
+        const __nv_bfloat16 h = __float2bfloat16_rn(v);
+        hi[i * pstride] = h;
+        lo[i * pstride] = __float2bfloat16_rn(v - __bfloat162float(h));
+      }
       if (mode == 3) r32[idx] = v;
     }
   }
@@ -280,7 +291,7 @@ struct ResidPass {
 template <class T, class In>
 __global__ void __launch_bounds__(128) k_resid_lines(ResidPass<T> p, const In* u, const T* rin,
                                                      T* scratch, T* rout, __nv_bfloat16* hi,
-                                                     __nv_bfloat16* lo, float* r32) {
+                                                     __nv_bfloat16* lo, float* x32, float* r32) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (long long)p.na * p.nb) return;
   const int a = (int)(t % p.na), b = (int)(t / p.na);
@@ -300,12 +311,187 @@ __global__ void __launch_bounds__(128) k_resid_lines(ResidPass<T> p, const In* u
   const long long pbase = a * p.pa + b * p.pb;
   fin.hi = hi ? hi + pbase : nullptr;
   fin.lo = lo ? lo + pbase : nullptr;
+  fin.x32 = x32 ? x32 + pbase : nullptr;
   fin.pstride = p.pstride;
   fin.r32 = r32 ? r32 + base : nullptr;
   if constexpr (sizeof(T) == 4)
     solve_line_comp(p.rows, p.n, u + base, scratch + base, p.s, fin);
   else
     solve_line(p.rows, p.n, u + base, scratch + base, p.s, lb, fin);
+}
+
+// ---- residual of an FP32 iterate with a tridiagonal operator (moment form)
+//
+// The solver's second-derivative operator has a tridiagonal implicit part
+// (p = e = alpha = beta = 0 in its factors) and a 5-point explicit stencil
+// inside the line.  With 1/c_i folded into the rows,
+//   x~_i = S_i - ft_i x~_{i-1},   y_i = x~_i - dt_i y_{i+1},
+//   S_i  = sum_m (r_m/c_i) u_{j_m} + (cbc/c_i) bc,
+// which costs one FP64 FMA per sweep.  S_i is where FP64 loses its digits:
+// on smooth data its terms are ~1e5 times the result.  For an FP32 iterate
+// u it is evaluated in the moment form
+//   S_i = sum_m r~_m (u_{j_m} - u_i) + cbc~ (bc - u_i) + rho_i u_i,
+//   rho_i = sum_m r~_m + cbc~   (exact sum of the FP64 coefficients),
+// an identity of exact arithmetic.  The differences of FP32 values are
+// exact as two floats, their products with the coefficients (hi + lo
+// floats) are formed with FMA error terms and summed with TwoSum, so the
+// remaining cancellation (~1e2) meets ~2^-48 relative rounding: the result
+// is more accurate than the FP64 evaluation of the same sum, and only the
+// two sweeps and the final combination use the FP64 pipe.
+struct TriRow {
+  float wh[7], wl[7];  // r_m / c_i as hi + lo floats, stencil order of the packed rows
+  float rh, rl;        // rho_i as hi + lo floats
+  double ft, dt;       // f_i c_{i-1} / c_i,  d_i / c_i
+  double cbc;          // boundary coefficient / c_i (rows 0, 1, n-2, n-1)
+  double pad;
+};
+static_assert(sizeof(TriRow) == 96, "TriRow layout");
+
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+// sum_{m < W, m != skip} (wh + wl)_m (v_m - ref) + rho ref, as FP64.
+template <int W>
+__device__ __forceinline__ double moment_sum(const TriRow& r, const float (&v)[W], float ref,
+                                             int skip) {
+  float h = 0.f, l = 0.f;
+#pragma unroll
+  for (int m = 0; m < W; ++m) {
+    if (m == skip) continue;
+    float dh, dl;
+    two_sum(v[m], -ref, dh, dl);
+    const float ph = r.wh[m] * dh;
+    float pl = fmaf(r.wh[m], dh, -ph);
+    pl = fmaf(r.wh[m], dl, pl);
+    pl = fmaf(r.wl[m], dh, pl);
+    float sh, se;
+    two_sum(h, ph, sh, se);
+    h = sh;
+    l += se + pl;
+  }
+  const float ph = r.rh * ref;
+  float pl = fmaf(r.rh, ref, -ph);
+  pl = fmaf(r.rl, ref, pl);
+  float sh, se;
+  two_sum(h, ph, sh, se);
+  return widen(sh) + widen(l + se + pl);
+}
+
+template <class Fin>
+__device__ __forceinline__ void solve_line_tri(const TriRow* __restrict__ R, int n, const float* u,
+                                               double* xs, long long s, double lo, double hi,
+                                               const Fin& fin) {
+  float f[7], g[7];
+#pragma unroll
+  for (int m = 0; m < 7; ++m) {
+    f[m] = u[(long long)m * s];
+    g[m] = u[(long long)(n - 7 + m) * s];
+  }
+  // rows 0 and 1: 7-wide stencils on u_0..u_6, boundary value lo
+  double x0 = moment_sum<7>(R[0], f, f[0], 0) + R[0].cbc * (lo - widen(f[0]));
+  double x1 = moment_sum<7>(R[1], f, f[1], 1) + R[1].cbc * (lo - widen(f[1])) - R[1].ft * x0;
+  xs[0] = x0;
+  xs[s] = x1;
+  double xm = x1;
+  float w[5] = {f[0], f[1], f[2], f[3], f[4]};
+  // interior rows 2..n-3; pf[k] = u(i + 3 + k)
+  float pf[kAhead];
+#pragma unroll
+  for (int k = 0; k < kAhead; ++k) pf[k] = (5 + k < n) ? u[(long long)(5 + k) * s] : 0.f;
+  int i = 2;
+  for (; i + kAhead <= n - 2; i += kAhead) {
+    float nb[kAhead];
+#pragma unroll
+    for (int k = 0; k < kAhead; ++k) {
+      const int j = i + 3 + kAhead + k;
+      nb[k] = (j < n) ? u[(long long)j * s] : 0.f;
+    }
+#pragma unroll
+    for (int k = 0; k < kAhead; ++k) {
+      const TriRow& r = R[i + k];
+      const double x = moment_sum<5>(r, w, w[2], 2) - r.ft * xm;
+      xs[(long long)(i + k) * s] = x;
+      xm = x;
+      w[0] = w[1]; w[1] = w[2]; w[2] = w[3]; w[3] = w[4]; w[4] = pf[k];
+    }
+#pragma unroll
+    for (int k = 0; k < kAhead; ++k) pf[k] = nb[k];
+  }
+  for (; i < n - 2; ++i) {
+    const TriRow& r = R[i];
+    const double x = moment_sum<5>(r, w, w[2], 2) - r.ft * xm;
+    xs[(long long)i * s] = x;
+    xm = x;
+    w[0] = w[1]; w[1] = w[2]; w[2] = w[3]; w[3] = w[4];
+    if (i + 3 < n) w[4] = u[(long long)(i + 3) * s];
+  }
+  // rows n-2 and n-1: 7-wide stencils on u_{n-7}..u_{n-1}, boundary value hi
+  const TriRow& rA = R[n - 2];
+  const TriRow& rB = R[n - 1];
+  const double xA = moment_sum<7>(rA, g, g[5], 5) + rA.cbc * (hi - widen(g[5])) - rA.ft * xm;
+  const double xB = moment_sum<7>(rB, g, g[6], 6) + rB.cbc * (hi - widen(g[6])) - rB.ft * xA;
+  // back substitution; rb[k] = forward value of row i - k
+  double y1 = xB;
+  fin(xs, n - 1, (long long)(n - 1) * s, xB);
+  double y = xA - rA.dt * y1;
+  fin(xs, n - 2, (long long)(n - 2) * s, y);
+  y1 = y;
+  i = n - 3;
+  double rb[kAhead];
+#pragma unroll
+  for (int k = 0; k < kAhead; ++k) rb[k] = (i - k >= 0) ? xs[(long long)(i - k) * s] : 0.0;
+  for (; i - (kAhead - 1) >= 0; i -= kAhead) {
+    double nb[kAhead];
+#pragma unroll
+    for (int k = 0; k < kAhead; ++k) {
+      const int j = i - kAhead - k;
+      nb[k] = (j >= 0) ? xs[(long long)j * s] : 0.0;
+    }
+#pragma unroll
+    for (int k = 0; k < kAhead; ++k) {
+      const double yy = rb[k] - R[i - k].dt * y1;
+      fin(xs, i - k, (long long)(i - k) * s, yy);
+      y1 = yy;
+    }
+#pragma unroll
+    for (int k = 0; k < kAhead; ++k) rb[k] = nb[k];
+  }
+  for (; i >= 0; --i) {
+    const double yy = xs[(long long)i * s] - R[i].dt * y1;
+    fin(xs, i, (long long)i * s, yy);
+    y1 = yy;
+  }
+}
+
+__global__ void __launch_bounds__(128) k_resid_tri(ResidPass<double> p, const TriRow* __restrict__ R,
+                                                   const float* u, const double* rin, double* scratch,
+                                                   double* rout, __nv_bfloat16* hi,
+                                                   __nv_bfloat16* lo, float* x32, float* r32) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)p.na * p.nb) return;
+  const int a = (int)(t % p.na), b = (int)(t / p.na);
+  const long long base = a * p.sa + b * p.sb;
+  double blo = 0.0, bhi = 0.0;
+  if (p.bc) {
+    blo = p.bc[t];
+    bhi = p.bc[t + (long long)p.na * p.nb];
+  }
+  ResidFin<double, float> fin;
+  fin.mode = p.mode;
+  fin.rin = rin + base;
+  fin.u = u + base;
+  fin.sigma = p.sigma;
+  fin.out = rout ? rout + base : nullptr;
+  const long long pbase = a * p.pa + b * p.pb;
+  fin.hi = hi ? hi + pbase : nullptr;
+  fin.lo = lo ? lo + pbase : nullptr;
+  fin.x32 = x32 ? x32 + pbase : nullptr;
+  fin.pstride = p.pstride;
+  fin.r32 = r32 ? r32 + base : nullptr;
+  solve_line_tri(R, p.n, u + base, scratch + base, p.s, blo, bhi, fin);
 }
 
 // solf(1:n1,1:n2,1:n3) = u1 + C, widened exactly and summed in FP64.
@@ -335,7 +521,8 @@ struct FoldArgsF {
 };
 
 __global__ void k_fold_split(const double* __restrict__ rhs, FoldArgsF a, __nv_bfloat16* hi,
-                             __nv_bfloat16* lo, int n1, int n2, int n3, int P1, int P2, int P3) {
+                             __nv_bfloat16* lo, float* x32, int n1, int n2, int n3, int P1, int P2,
+                             int P3) {
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long tot = (long long)P1 * P2 * P3;
   if (idx >= tot) return;
@@ -353,6 +540,10 @@ __global__ void k_fold_split(const double* __restrict__ rhs, FoldArgsF a, __nv_b
       v -= a.iy[c][j] * a.by[c * sy + fy];
       v -= a.iz[c][k] * a.bz[c * sz + fz];
     }
+  }
+  if (x32) {
+    x32[idx] = v;
+    return;
   }
   const __nv_bfloat16 h = __float2bfloat16_rn(v);
   hi[idx] = h;
@@ -415,7 +606,33 @@ static void split_bf16(const std::vector<double>& m, int n, int P, std::vector<_
     }
 }
 
-// Uploads eigen tables (row-major V, V^-1) and their split-BF16 copies.
+// Nearest TF32 value of x (ties away from zero), kept as an FP32 number:
+// the 13 low mantissa bits are rounded off on the bit pattern.
+static float tf32_round(float x) {
+  uint32_t u;
+  std::memcpy(&u, &x, 4);
+  if ((u & 0x7F800000u) != 0x7F800000u) u = (u + 0x1000u) & 0xFFFFE000u;
+  float r;
+  std::memcpy(&r, &u, 4);
+  return r;
+}
+
+// hi = tf32(m), lo = tf32(m - hi), zero-padded to P x P.
+static void split_tf32(const std::vector<double>& m, int n, int P, std::vector<float>& hi,
+                       std::vector<float>& lo) {
+  hi.assign((size_t)P * P, 0.f);
+  lo.assign((size_t)P * P, 0.f);
+  for (int r = 0; r < n; ++r)
+    for (int c = 0; c < n; ++c) {
+      const double v = m[(size_t)r * n + c];
+      const float h = tf32_round((float)v);
+      hi[(size_t)r * P + c] = h;
+      lo[(size_t)r * P + c] = tf32_round((float)(v - (double)h));
+    }
+}
+
+// Uploads eigen tables (row-major V, V^-1), their split-BF16 copies and
+// their 3xTF32 planes.
 static int axis_set_eigen(AxisDev& d, const std::vector<double>& eig, const std::vector<double>& V,
                           const std::vector<double>& Vinv) {
   int rc;
@@ -425,6 +642,11 @@ static int axis_set_eigen(AxisDev& d, const std::vector<double>& eig, const std:
   if ((rc = upload(d.Vih, hi)) || (rc = upload(d.Vil, lo))) return rc;
   split_bf16(V, d.n, d.P, hi, lo);
   if ((rc = upload(d.Vh, hi)) || (rc = upload(d.Vl, lo))) return rc;
+  std::vector<float> h32, l32;
+  split_tf32(Vinv, d.n, d.P, h32, l32);
+  if ((rc = upload(d.Vih32, h32)) || (rc = upload(d.Vil32, l32))) return rc;
+  split_tf32(V, d.n, d.P, h32, l32);
+  if ((rc = upload(d.Vh32, h32)) || (rc = upload(d.Vl32, l32))) return rc;
   std::vector<float> ef(d.P, 0.f);
   std::vector<uint8_t> nf(d.P, 0);
   for (int i = 0; i < d.n; ++i) {
@@ -432,6 +654,41 @@ static int axis_set_eigen(AxisDev& d, const std::vector<double>& eig, const std:
     nf[i] = std::fabs(eig[i]) < kNullThresh ? 1 : 0;
   }
   if ((rc = upload(d.eigf, ef)) || (rc = upload(d.nullf, nf))) return rc;
+  return MF_OK;
+}
+
+// TriRow table of an axis whose factored lhs is tridiagonal (p, e, alpha
+// and beta all zero), from the packed rows p, f, 1/c, d, e, r0..r6.
+static int build_tri_rows(AxisDev& d, const std::vector<double>& rows) {
+  const int n = d.n;
+  d.tri_ok = n >= 8;
+  for (int i = 0; i < n && d.tri_ok; ++i)
+    if (rows[(size_t)kRow * i + 0] != 0.0 || rows[(size_t)kRow * i + 4] != 0.0) d.tri_ok = false;
+  if (!d.tri_ok) return MF_OK;
+  std::vector<TriRow> tr(n);
+  for (int i = 0; i < n; ++i) {
+    const double* r = &rows[(size_t)kRow * i];
+    const double inv_c = r[2];
+    TriRow& t = tr[i];
+    std::memset(&t, 0, sizeof(t));
+    const int bcrow = i == 0 ? 0 : i == 1 ? 1 : i == n - 2 ? 2 : i == n - 1 ? 3 : -1;
+    t.cbc = bcrow >= 0 ? d.bcc[bcrow] * inv_c : 0.0;
+    long double rho = (long double)t.cbc;
+    for (int m = 0; m < 7; ++m) {
+      const double w = r[5 + m] * inv_c;
+      rho += (long double)w;
+      t.wh[m] = (float)w;
+      t.wl[m] = (float)(w - (double)t.wh[m]);
+    }
+    const double rd = (double)rho;
+    t.rh = (float)rd;
+    t.rl = (float)(rd - (double)t.rh);
+    t.ft = i > 0 ? r[1] * inv_c / rows[(size_t)kRow * (i - 1) + 2] : 0.0;
+    t.dt = i < n - 1 ? r[3] * inv_c : 0.0;
+  }
+  int rc = d.tri.ensure(sizeof(TriRow) * n);
+  if (rc) return rc;
+  MF_CUDA(cudaMemcpy(d.tri.ptr, tr.data(), sizeof(TriRow) * n, cudaMemcpyHostToDevice));
   return MF_OK;
 }
 
@@ -491,6 +748,7 @@ static int axis_upload(AxisDev& d, const SolverAxisHost& h) {
     }
   }
   if ((rc = upload(d.rowsf, rowsf))) return rc;
+  if ((rc = build_tri_rows(d, rows))) return rc;
   return axis_set_eigen(d, h.eigen, h.vect, h.inv_vect);
 }
 
@@ -584,13 +842,14 @@ static int solve_plain_dev(mf_solver3d* sc, const double* rhs, double sigma, dou
 // Residual on device pointers, three passes (x, y, z):
 //   r = rin - sigma*u - sum_a L_a u.
 // rin/u/bcs describe the problem (bcs may be null: homogeneous data).  The
-// last pass writes the FP64/FP32 array `r` (when planes are null) or the
-// split-BF16 planes (and, with r32, an FP32 copy of r).
+// last pass writes the FP64/FP32 array `r` (when planes and x32 are null),
+// the split-BF16 planes or the FP32 operand x32 of the 3xTF32 transforms
+// (and, with r32, an FP32 copy of r).
 template <class T, class In>
 static int residual_passes(mf_solver3d* sc, const T* rin, const In* u, double sigma,
                            const double* bcs[3], T* s0, T* s1, T* r, __nv_bfloat16* hi,
-                           __nv_bfloat16* lo, float* r32, int prof_kind_x, int prof_kind_yz,
-                           cudaStream_t st) {
+                           __nv_bfloat16* lo, float* x32, float* r32, int prof_kind_x,
+                           int prof_kind_yz, cudaStream_t st) {
   const long long n1 = sc->n[0], n2 = sc->n[1], n3 = sc->n[2];
   auto pass = [&](int axis) {
     ResidPass<T> p;
@@ -606,11 +865,25 @@ static int residual_passes(mf_solver3d* sc, const T* rin, const In* u, double si
     if (axis == 2) { p.na = (int)n1; p.nb = (int)n2; p.sa = 1; p.sb = n1; p.s = n1 * n2; }
     return p;
   };
+  // FP32 iterate, FP64 residual, tridiagonal operators: moment form
+  bool tri = false;
+  if constexpr (sizeof(T) == 8 && sizeof(In) == 4)
+    tri = sc->ax[0].tri_ok && sc->ax[1].tri_ok && sc->ax[2].tri_ok;
+  int axis_of_pass = 0;
   auto launch = [&](const ResidPass<T>& p, int kind, const T* in_r, T* scratch, T* rout,
-                    __nv_bfloat16* h, __nv_bfloat16* l, float* r32p) -> int {
+                    __nv_bfloat16* h, __nv_bfloat16* l, float* x, float* r32p) -> int {
     sc->prof.begin(kind, st);
+    if constexpr (sizeof(T) == 8 && sizeof(In) == 4) {
+      if (tri) {
+        k_resid_tri<<<blocks_for((long long)p.na * p.nb, 128), 128, 0, st>>>(
+            p, sc->ax[axis_of_pass].tri.template as<TriRow>(), u, in_r, scratch, rout, h, l, x, r32p);
+        sc->prof.end(st);
+        MF_CUDA(cudaGetLastError());
+        return MF_OK;
+      }
+    }
     k_resid_lines<T, In><<<blocks_for((long long)p.na * p.nb, 128), 128, 0, st>>>(
-        p, u, in_r, scratch, rout, h, l, r32p);
+        p, u, in_r, scratch, rout, h, l, x, r32p);
     sc->prof.end(st);
     MF_CUDA(cudaGetLastError());
     return MF_OK;
@@ -618,24 +891,29 @@ static int residual_passes(mf_solver3d* sc, const T* rin, const In* u, double si
   int rc;
   ResidPass<T> px = pass(0);
   px.mode = 0;
-  if ((rc = launch(px, prof_kind_x, rin, s0, s0, nullptr, nullptr, nullptr))) return rc;
+  axis_of_pass = 0;
+  if ((rc = launch(px, prof_kind_x, rin, s0, s0, nullptr, nullptr, nullptr, nullptr))) return rc;
   ResidPass<T> py = pass(1);
   py.mode = 1;
-  if ((rc = launch(py, prof_kind_yz, s0, s1, s1, nullptr, nullptr, nullptr))) return rc;
+  axis_of_pass = 1;
+  if ((rc = launch(py, prof_kind_yz, s0, s1, s1, nullptr, nullptr, nullptr, nullptr))) return rc;
   ResidPass<T> pz = pass(2);
-  if (hi) {
+  axis_of_pass = 2;
+  if (hi || x32) {
     pz.mode = r32 ? 3 : 2;
     pz.pa = 1;
     pz.pb = sc->P[0];
     pz.pstride = (long long)sc->P[0] * sc->P[1];
-    return launch(pz, prof_kind_yz, s1, s0, nullptr, hi, lo, r32);
+    return launch(pz, prof_kind_yz, s1, s0, nullptr, hi, lo, x32, r32);
   }
   pz.mode = 1;
-  return launch(pz, prof_kind_yz, s1, r, r, nullptr, nullptr, nullptr);
+  return launch(pz, prof_kind_yz, s1, r, r, nullptr, nullptr, nullptr, nullptr);
 }
 
-static int mixed_prepare(mf_solver3d* sc) {
-  if (sc->mixed_ready) return MF_OK;
+// Operand buffers and tensor-core plans of one mixed format (split-BF16 or
+// 3xTF32), created on first use.
+static int mixed_prepare(mf_solver3d* sc, bool tf32) {
+  if (tf32 ? sc->mixed32_ready : sc->mixed_ready) return MF_OK;
   for (int a = 0; a < 3; ++a)
     if (sc->P[a] > 256)
       return set_error(MF_ERR_UNSUPPORTED,
@@ -647,53 +925,67 @@ static int mixed_prepare(mf_solver3d* sc) {
   if ((rc = sc->R.ensure(tot * 8)) || (rc = sc->R2.ensure(tot * 8)) || (rc = sc->U32.ensure(tot * 4)) ||
       (rc = sc->C32.ensure(tot * 4)) || (rc = sc->R1f.ensure(tot * 4)))
     return rc;
-  if ((rc = sc->Xa_hi.ensure(ptot * 2)) || (rc = sc->Xa_lo.ensure(ptot * 2)) ||
-      (rc = sc->Xb_hi.ensure(ptot * 2)) || (rc = sc->Xb_lo.ensure(ptot * 2)))
-    return rc;
-  MF_CUDA(cudaMemset(sc->Xa_hi.ptr, 0, ptot * 2));
-  MF_CUDA(cudaMemset(sc->Xa_lo.ptr, 0, ptot * 2));
-  MF_CUDA(cudaMemset(sc->Xb_hi.ptr, 0, ptot * 2));
-  MF_CUDA(cudaMemset(sc->Xb_lo.ptr, 0, ptot * 2));
+  // operands are zero-padded to P per axis; the padding stays zero because
+  // the padded rows and columns of every matrix are zero
+  DevBuf* xa[2] = {tf32 ? &sc->Xa32 : &sc->Xa_hi, tf32 ? nullptr : &sc->Xa_lo};
+  DevBuf* xb[2] = {tf32 ? &sc->Xb32 : &sc->Xb_hi, tf32 ? nullptr : &sc->Xb_lo};
+  const size_t bytes = (size_t)ptot * (tf32 ? 4 : 2);
+  for (DevBuf* x : {xa[0], xa[1], xb[0], xb[1]}) {
+    if (!x) continue;
+    if ((rc = x->ensure(bytes))) return rc;
+    MF_CUDA(cudaMemset(x->ptr, 0, bytes));
+  }
   if ((rc = sc->err.ensure(sizeof(int)))) return rc;
   MF_CUDA(cudaMemset(sc->err.ptr, 0, sizeof(int)));
   const int P1 = sc->P[0], P2 = sc->P[1], P3 = sc->P[2];
-  auto bf = [](DevBuf& b) { return b.as<__nv_bfloat16>(); };
-  struct Spec { DevBuf *xh, *xl; int axis; bool inv; int M; };
-  Spec specs[6] = {{&sc->Xa_hi, &sc->Xa_lo, 0, true, P2 * P3}, {&sc->Xb_hi, &sc->Xb_lo, 1, true, P3 * P1},
-                   {&sc->Xa_hi, &sc->Xa_lo, 2, true, P1 * P2}, {&sc->Xb_hi, &sc->Xb_lo, 0, false, P2 * P3},
-                   {&sc->Xa_hi, &sc->Xa_lo, 1, false, P3 * P1}, {&sc->Xb_hi, &sc->Xb_lo, 2, false, P1 * P2}};
+  struct Spec { DevBuf** x; int axis; bool inv; int M; };
+  const Spec specs[6] = {{xa, 0, true, P2 * P3}, {xb, 1, true, P3 * P1}, {xa, 2, true, P1 * P2},
+                         {xb, 0, false, P2 * P3}, {xa, 1, false, P3 * P1}, {xb, 2, false, P1 * P2}};
+  TcPlan** plans = tf32 ? sc->plan32 : sc->plan;
   for (int t = 0; t < 6; ++t) {
     AxisDev& d = sc->ax[specs[t].axis];
-    DevBuf& bh = specs[t].inv ? d.Vih : d.Vh;
-    DevBuf& bl = specs[t].inv ? d.Vil : d.Vl;
-    if ((rc = tc_plan_create(&sc->plan[t], bf(*specs[t].xh), bf(*specs[t].xl), bf(bh), bf(bl),
-                             specs[t].M, d.P, d.P)))
+    DevBuf& bh = tf32 ? (specs[t].inv ? d.Vih32 : d.Vh32) : (specs[t].inv ? d.Vih : d.Vh);
+    DevBuf& bl = tf32 ? (specs[t].inv ? d.Vil32 : d.Vl32) : (specs[t].inv ? d.Vil : d.Vl);
+    const void* xlo = specs[t].x[1] ? specs[t].x[1]->ptr : nullptr;
+    if ((rc = tc_plan_create(&plans[t], tf32, specs[t].x[0]->ptr, xlo, bh.ptr, bl.ptr, specs[t].M,
+                             d.P, d.P)))
       return rc;
   }
-  sc->mixed_ready = true;
+  (tf32 ? sc->mixed32_ready : sc->mixed_ready) = true;
   return MF_OK;
 }
 
-static int tc_run(mf_solver3d* sc, int t, const TcEpilogue& e, cudaStream_t st) {
+static int tc_run(mf_solver3d* sc, bool tf32, int t, const TcEpilogue& e, cudaStream_t st) {
   sc->prof.begin(e.kind == 0 ? kProfTc : e.kind == 1 ? kProfTcDivide : kProfTcUpdate, st);
-  int rc = tc_transform(sc->plan[t], e, sc->err.as<int>(), st);
+  int rc = tc_transform((tf32 ? sc->plan32 : sc->plan)[t], e, sc->err.as<int>(), st);
   sc->prof.end(st);
   return rc;
 }
 
-// One approximate solve of the folded right-hand side already split into Xa.
-static int approx_solve(mf_solver3d* sc, double sigma, float* dest, bool accumulate, cudaStream_t st) {
-  auto bf = [](DevBuf& b) { return b.as<__nv_bfloat16>(); };
+// Points the store epilogue at operand buffer A (second = false) or B.
+static void set_target(TcEpilogue& e, mf_solver3d* sc, bool tf32, bool to_b) {
+  if (tf32) {
+    e.y32 = (to_b ? sc->Xb32 : sc->Xa32).as<float>();
+  } else {
+    e.y_hi = (to_b ? sc->Xb_hi : sc->Xa_hi).as<__nv_bfloat16>();
+    e.y_lo = (to_b ? sc->Xb_lo : sc->Xa_lo).as<__nv_bfloat16>();
+  }
+}
+
+// One approximate solve of the folded right-hand side already stored in
+// operand buffer A; the six transforms ping-pong between A and B.
+static int approx_solve(mf_solver3d* sc, bool tf32, double sigma, float* dest, bool accumulate,
+                        cudaStream_t st) {
   TcEpilogue e;
   int rc;
   e.kind = 0;
-  e.y_hi = bf(sc->Xb_hi); e.y_lo = bf(sc->Xb_lo);
-  if ((rc = tc_run(sc, 0, e, st))) return rc;
-  e.y_hi = bf(sc->Xa_hi); e.y_lo = bf(sc->Xa_lo);
-  if ((rc = tc_run(sc, 1, e, st))) return rc;
-  TcEpilogue d = e;
+  set_target(e, sc, tf32, true);
+  if ((rc = tc_run(sc, tf32, 0, e, st))) return rc;
+  set_target(e, sc, tf32, false);
+  if ((rc = tc_run(sc, tf32, 1, e, st))) return rc;
+  TcEpilogue d;
   d.kind = 1;
-  d.y_hi = bf(sc->Xb_hi); d.y_lo = bf(sc->Xb_lo);
+  set_target(d, sc, tf32, true);
   d.lam_x = sc->ax[0].eigf.as<float>();
   d.lam_y = sc->ax[1].eigf.as<float>();
   d.lam_z = sc->ax[2].eigf.as<float>();
@@ -704,22 +996,24 @@ static int approx_solve(mf_solver3d* sc, double sigma, float* dest, bool accumul
   d.sigma_null = std::fabs(sigma) < kNullThresh ? 1 : 0;
   d.n1 = sc->n[0]; d.n2 = sc->n[1]; d.n3 = sc->n[2];
   d.P1 = sc->P[0]; d.P2 = sc->P[1];
-  if ((rc = tc_run(sc, 2, d, st))) return rc;
-  e.y_hi = bf(sc->Xa_hi); e.y_lo = bf(sc->Xa_lo);
-  if ((rc = tc_run(sc, 3, e, st))) return rc;
-  e.y_hi = bf(sc->Xb_hi); e.y_lo = bf(sc->Xb_lo);
-  if ((rc = tc_run(sc, 4, e, st))) return rc;
+  if ((rc = tc_run(sc, tf32, 2, d, st))) return rc;
+  set_target(e, sc, tf32, false);
+  if ((rc = tc_run(sc, tf32, 3, e, st))) return rc;
+  set_target(e, sc, tf32, true);
+  if ((rc = tc_run(sc, tf32, 4, e, st))) return rc;
   TcEpilogue u;
   u.kind = 2;
   u.out = dest;
   u.accumulate = accumulate ? 1 : 0;
   u.n1 = sc->n[0]; u.n2 = sc->n[1]; u.n3 = sc->n[2];
   u.P1 = sc->P[0]; u.P2 = sc->P[1];
-  return tc_run(sc, 5, u, st);
+  return tc_run(sc, tf32, 5, u, st);
 }
 
-// First right-hand side of the mixed path: FP32 fold + split into Xa.
-static int fold_split(mf_solver3d* sc, const double* rhs, const double* bcs[3], cudaStream_t st) {
+// First right-hand side of the mixed path: FP32 fold, stored into operand
+// buffer A (split into BF16 planes, or as FP32).
+static int fold_split(mf_solver3d* sc, bool tf32, const double* rhs, const double* bcs[3],
+                      cudaStream_t st) {
   const long long n1 = sc->n[0], n2 = sc->n[1], n3 = sc->n[2];
   const long long nf[3] = {n2 * n3, n1 * n3, n1 * n2};
   int rc;
@@ -742,9 +1036,10 @@ static int fold_split(mf_solver3d* sc, const double* rhs, const double* bcs[3], 
   args.by = fa[1];
   args.bz = fa[2];
   const long long ptot = (long long)sc->P[0] * sc->P[1] * sc->P[2];
-  k_fold_split<<<blocks_for(ptot, 256), 256, 0, st>>>(rhs, args, sc->Xa_hi.as<__nv_bfloat16>(),
-                                                      sc->Xa_lo.as<__nv_bfloat16>(), (int)n1, (int)n2,
-                                                      (int)n3, sc->P[0], sc->P[1], sc->P[2]);
+  k_fold_split<<<blocks_for(ptot, 256), 256, 0, st>>>(
+      rhs, args, tf32 ? nullptr : sc->Xa_hi.as<__nv_bfloat16>(),
+      tf32 ? nullptr : sc->Xa_lo.as<__nv_bfloat16>(), tf32 ? sc->Xa32.as<float>() : nullptr,
+      (int)n1, (int)n2, (int)n3, sc->P[0], sc->P[1], sc->P[2]);
   sc->prof.end(st);
   MF_CUDA(cudaGetLastError());
   return MF_OK;
@@ -756,38 +1051,43 @@ static int fold_split(mf_solver3d* sc, const double* rhs, const double* bcs[3], 
 //   C  = S~ r1;  for k >= 2: r_k = r1 - A C     (FP32 residual update)
 //                            C += S~ r_k
 //   solf = u1 + C                               (widened, summed in FP64)
-// S~ is the split-BF16 approximate inverse (six tensor-core transforms).  The
-// cancellation in r_k = r1 - A C is relative to |r1| (~1e-5 |rhs|), so FP32
-// keeps it to ~1e-12 |rhs|; the FP64 residual of u1 carries the accuracy.
+// S~ is the approximate inverse by six tensor-core transforms (split-BF16
+// or 3xTF32).  The cancellation in r_k = r1 - A C is relative to |r1|
+// (~1e-5 |rhs|), so FP32 keeps it to ~1e-12 |rhs|; the FP64 residual of u1
+// carries the accuracy.
 static int solve_mixed_dev(mf_solver3d* sc, const double* rhs, double sigma, double* solf,
                            const double* bcs[3], int prec, int refine, cudaStream_t st) {
-  if (prec != MF_PREC_SPLIT_BF16)
+  if (prec != MF_PREC_SPLIT_BF16 && prec != MF_PREC_3XTF32)
     return set_error(MF_ERR_UNSUPPORTED, "precision mode %d is not available", prec);
+  const bool tf32 = prec == MF_PREC_3XTF32;
   int rc;
-  if ((rc = mixed_prepare(sc))) return rc;
+  if ((rc = mixed_prepare(sc, tf32))) return rc;
   const int n1 = sc->n[0], n2 = sc->n[1], n3 = sc->n[2];
   const long long tot = (long long)n1 * n2 * n3;
-  __nv_bfloat16* xh = sc->Xa_hi.as<__nv_bfloat16>();
-  __nv_bfloat16* xl = sc->Xa_lo.as<__nv_bfloat16>();
+  __nv_bfloat16* xh = tf32 ? nullptr : sc->Xa_hi.as<__nv_bfloat16>();
+  __nv_bfloat16* xl = tf32 ? nullptr : sc->Xa_lo.as<__nv_bfloat16>();
+  float* x32 = tf32 ? sc->Xa32.as<float>() : nullptr;
   float* u1 = sc->U32.as<float>();
   float* C = sc->C32.as<float>();
-  if ((rc = fold_split(sc, rhs, bcs, st))) return rc;
-  if ((rc = approx_solve(sc, sigma, u1, false, st))) return rc;
+  if ((rc = fold_split(sc, tf32, rhs, bcs, st))) return rc;
+  if ((rc = approx_solve(sc, tf32, sigma, u1, false, st))) return rc;
   for (int it = 0; it < refine; ++it) {
     if (it == 0) {
+      // the FP32 copy of r1 only feeds later refinement steps
       if ((rc = residual_passes<double, float>(sc, rhs, u1, sigma, bcs, sc->R.as<double>(),
-                                               sc->R2.as<double>(), (double*)nullptr, xh, xl,
-                                               sc->R1f.as<float>(), kProfResidX, kProfResidYZ, st)))
+                                               sc->R2.as<double>(), (double*)nullptr, xh, xl, x32,
+                                               refine > 1 ? sc->R1f.as<float>() : nullptr,
+                                               kProfResidX, kProfResidYZ, st)))
         return rc;
     } else {
       float* f0 = reinterpret_cast<float*>(sc->R.ptr);
       float* f1 = reinterpret_cast<float*>(sc->R2.ptr);
       if ((rc = residual_passes<float, float>(sc, sc->R1f.as<float>(), C, sigma, nullptr, f0, f1,
-                                              (float*)nullptr, xh, xl, nullptr, kProfResid32,
+                                              (float*)nullptr, xh, xl, x32, nullptr, kProfResid32,
                                               kProfResid32, st)))
         return rc;
     }
-    if ((rc = approx_solve(sc, sigma, C, it > 0, st))) return rc;
+    if ((rc = approx_solve(sc, tf32, sigma, C, it > 0, st))) return rc;
   }
   sc->prof.begin(kProfCopy, st);
   k_finalize<<<blocks_for(tot, 256), 256, 0, st>>>(u1, refine > 0 ? C : nullptr, solf, n1, n2, n3);
@@ -864,15 +1164,20 @@ int mf_solver_coeffs_init_3d(const double* g1, const double* g2, const double* g
 
 int mf_solver3d_destroy(mf_solver3d_t* sc) {
   if (!sc) return MF_OK;
-  for (int t = 0; t < 6; ++t) tc_plan_destroy(sc->plan[t]);
+  for (int t = 0; t < 6; ++t) {
+    tc_plan_destroy(sc->plan[t]);
+    tc_plan_destroy(sc->plan32[t]);
+  }
   for (auto& d : sc->ax) {
     for (DevBuf* b : {&d.V, &d.Vinv, &d.eig, &d.invl4, &d.rows, &d.Vh, &d.Vl, &d.Vih, &d.Vil,
-                      &d.eigf, &d.nullf, &d.invl4f, &d.rowsf})
+                      &d.Vh32, &d.Vl32, &d.Vih32, &d.Vil32, &d.eigf, &d.nullf, &d.invl4f,
+                      &d.rowsf, &d.tri})
       b->release();
   }
   for (DevBuf* b : {&sc->w0, &sc->w1, &sc->st_rhs, &sc->st_solf, &sc->st_bc[0], &sc->st_bc[1],
                     &sc->st_bc[2], &sc->R, &sc->R2, &sc->Xa_hi, &sc->Xa_lo, &sc->Xb_hi,
-                    &sc->Xb_lo, &sc->err, &sc->foldf, &sc->U32, &sc->C32, &sc->R1f})
+                    &sc->Xb_lo, &sc->Xa32, &sc->Xb32, &sc->err, &sc->foldf, &sc->U32, &sc->C32,
+                    &sc->R1f})
     b->release();
   delete sc;
   return MF_OK;
@@ -1128,7 +1433,7 @@ int mf_solver_residual(mf_solver3d_t* sc, const double* g, const double* u, doub
   if ((rc = sc->R.ensure(tb)) || (rc = sc->R2.ensure(tb))) return rc;
   const double* bcs[3] = {bcx, bcy, bcz};
   return residual_passes<double, double>(sc, g, u, sigma, bcs, sc->R.as<double>(),
-                                        sc->R2.as<double>(), r, nullptr, nullptr, nullptr,
+                                        sc->R2.as<double>(), r, nullptr, nullptr, nullptr, nullptr,
                                         kProfResidX, kProfResidYZ, static_cast<cudaStream_t>(stream));
 }
 

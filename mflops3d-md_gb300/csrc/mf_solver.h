@@ -9,13 +9,15 @@
 namespace mf {
 
 // One axis transform  Y[n][m] = sum_k B[n][k] * X[m][k]  on the tensor cores,
-// with X and B given as split-BF16 (hi, lo) planes and three products
-// hi*hi + hi*lo + lo*hi accumulated in FP32.  X rows have pitch K, Y rows
-// pitch M.  M is a multiple of 128, K = N is a multiple of 16 and <= 256.
+// with three products hi*hi + hi*lo + lo*hi accumulated in FP32, the
+// operands given either as split-BF16 (hi, lo) planes or (3xTF32) as FP32 X
+// and two TF32-rounded FP32 planes of B.  X rows have pitch K, Y rows pitch
+// M.  M is a multiple of 128, K = N is a multiple of 64 and <= 256.
 struct TcEpilogue {
-  int kind = 0;                  // 0 split store, 1 eigen divide + split store, 2 FP32 store/add
-  __nv_bfloat16* y_hi = nullptr; // kinds 0,1: [N][M]
+  int kind = 0;                  // 0 store, 1 eigen divide + store, 2 FP32 store/add
+  __nv_bfloat16* y_hi = nullptr; // kinds 0,1, BF16 format: [N][M]
   __nv_bfloat16* y_lo = nullptr;
+  float* y32 = nullptr;          // kinds 0,1, TF32 format: [N][M]
   // kind 1: m = i + P1*j, n = k
   const float* lam_x = nullptr;  // [P1], [P2], [P3] eigenvalues, 0 past n
   const float* lam_y = nullptr;
@@ -33,9 +35,10 @@ struct TcEpilogue {
 
 struct TcPlan;  // opaque: tensor maps for one transform
 
-// Creates tensor maps for X (rows=M, cols=K) and the matrix planes (N x K).
-int tc_plan_create(TcPlan** plan, const __nv_bfloat16* x_hi, const __nv_bfloat16* x_lo,
-                   const __nv_bfloat16* b_hi, const __nv_bfloat16* b_lo, int M, int N, int K);
+// Creates tensor maps for X (rows=M, cols=K) and the matrix planes (N x K):
+// BF16 planes, or with tf32 FP32 X (x_lo unused) and FP32 planes.
+int tc_plan_create(TcPlan** plan, bool tf32, const void* x_hi, const void* x_lo, const void* b_hi,
+                   const void* b_lo, int M, int N, int K);
 void tc_plan_destroy(TcPlan* plan);
 int tc_transform(const TcPlan* plan, const TcEpilogue& epi, int* dev_err, cudaStream_t st);
 

@@ -1,7 +1,17 @@
 // Split-precision eigenvector transform on the 5th-generation tensor cores.
 //
-//   Y[n][m] = sum_k B[n][k] X[m][k],   X = Xh + Xl,  B = Bh + Bl  (BF16 pairs)
+//   Y[n][m] = sum_k B[n][k] X[m][k],   X = Xh + Xl,  B = Bh + Bl
 //   D = Xh*Bh + Xh*Bl + Xl*Bh           (three tcgen05.mma, FP32 in TMEM)
+//
+// Two operand formats:
+//  * split-BF16 (kind::f16): X is stored as two BF16 planes, B likewise;
+//  * 3xTF32 (kind::tf32): X is stored as FP32.  The tensor core reads an FP32
+//    operand as TF32 by ignoring its 13 low mantissa bits, so the landed
+//    tile itself is the hi part, trunc(x); converter warps write the lo part
+//    rna_tf32(x - trunc(x)) beside it.  B is stored as two TF32-rounded FP32
+//    planes.  Each 128-byte swizzle row holds 32 K values instead of 64, and
+//    the split keeps ~21 bits of every operand instead of ~16, which lets
+//    one refinement step reach 1e-10.
 //
 // Persistent, warp-specialised kernel (one CTA per SM):
 //  * the N extent is cut into NS slices of NW = N/NS columns; a CTA owns one
@@ -10,13 +20,22 @@
 //  * warp 0 (one lane) streams 128 x 64 chunks of Xh and Xl through a ring
 //    of TMA stages (128-byte swizzle);
 //  * warp 1 allocates TMEM and one lane issues the three tcgen05.mma per
-//    16-deep K step into one of two FP32 accumulators (2 x NW columns), so
-//    the MMAs of tile t+1 overlap the epilogue of tile t;
-//  * warps 2-5 drain the accumulator with tcgen05.ld (warp w owns TMEM lanes
-//    32*(w%4)..+31) and run the fused epilogue:
-//      kind 0: split the FP32 result into BF16 planes Y[n][m] (coalesced in m);
+//    32-byte K step into one of two accumulator sets, so the MMAs of tile
+//    t+1 overlap the epilogue of tile t.  BF16: one FP32 accumulator per set
+//    (NW columns).  TF32: three per set, because every MMA rounds its
+//    running sum and the error grows with the number of MMAs accumulated
+//    into one sum: the small products hi*lo + lo*hi, and hi*hi over the
+//    first and over the second half of K, are summed by the epilogue;
+//  * (3xTF32 only) 4 converter warps write the lo part of each landed FP32
+//    stage; the MMA warp issues the two products with the hi part as soon
+//    as the stage lands and the lo product once the converters release it;
+//  * the epilogue warps (8 for BF16, 4 for TF32) drain the accumulator with
+//    tcgen05.ld (warp w owns TMEM lanes 32*(w%4)..+31) and run the fused
+//    epilogue:
+//      kind 0: store the result Y[n][m] (coalesced in m) in the operand format
+//              of the next transform (BF16 planes or FP32);
 //      kind 1: same, after the eigenvalue divide 1/(lx_i+ly_j+lz_k+sigma);
-//      kind 2: add (or store) the result into the FP64 solution u.
+//      kind 2: add (or store) the result into the FP32 solution array.
 // The two CTAs that own the two slices of the same M tile run in step, so
 // the second read of each X tile is served by L2.
 // Every mbarrier wait is bounded (about two seconds of clock); on expiry the
@@ -31,17 +50,27 @@
 namespace mf {
 
 struct TcPlan {
-  CUtensorMap x_hi, x_lo, b_hi, b_lo;
+  CUtensorMap x_hi, x_lo, b_hi, b_lo;  // x_lo unused for 3xTF32
   int M = 0, N = 0, K = 0;
+  bool tf32 = false;
 };
 
 namespace {
 
 constexpr int kBlockM = 128;
-constexpr int kChunkK = 64;  // bf16 elements per 128-byte swizzle row
 constexpr long long kWaitCycles = 4000000000LL;
-constexpr int kEpiWarps = 8;      // two per TMEM lane quarter, each on half the columns
-constexpr int kEpiThreads = 32 * kEpiWarps;
+
+// Per-format constants.  Warp roles: 0 TMA, 1 MMA, then the epilogue warps,
+// then (TF32) the converter warps.
+template <bool kTf32>
+struct Cfg {
+  static constexpr int kChunkK = kTf32 ? 32 : 64;  // K values per 128-byte swizzle row
+  static constexpr int kEpiWarps = kTf32 ? 4 : 8;  // one or two per TMEM lane quarter
+  static constexpr int kCvtWarps = kTf32 ? 4 : 0;
+  static constexpr int kEpiThreads = 32 * kEpiWarps;
+  static constexpr int kCvtThreads = 32 * kCvtWarps;
+  static constexpr int kThreads = 64 + kEpiThreads + kCvtThreads;
+};
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -90,6 +119,15 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, u
       : "memory");
 }
 
+// L2 prefetch of one box (no shared memory, no barrier): hides the DRAM part
+// of a later stage's load latency.
+__device__ __forceinline__ void tma_prefetch_2d(const CUtensorMap* map, int c0, int c1) {
+  asm volatile("cp.async.bulk.prefetch.tensor.2d.L2.global [%0, {%1, %2}];" ::"l"(
+                   reinterpret_cast<uint64_t>(map)),
+               "r"(c0), "r"(c1)
+               : "memory");
+}
+
 __device__ __forceinline__ void fence_before() {
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
 }
@@ -109,19 +147,40 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
   return d;
 }
 
-// Instruction descriptor: kind::f16 with BF16 A/B, FP32 D, both K-major.
-__host__ __device__ constexpr uint32_t instr_desc_bf16(int M, int N) {
-  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) |
-         ((uint32_t)(M >> 4) << 24);
+// Instruction descriptor, FP32 D, both operands K-major: kind::f16 with BF16
+// A/B (format 1) or kind::tf32 (format 2).
+__host__ __device__ constexpr uint32_t instr_desc(int M, int N, bool tf32) {
+  return (1u << 4) | ((tf32 ? 2u : 1u) << 7) | ((tf32 ? 2u : 1u) << 10) |
+         ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
-__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc,
-                                         uint32_t accumulate) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
-      "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+template <bool kTf32>
+__device__ __forceinline__ void mma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc,
+                                    uint32_t accumulate) {
+  if constexpr (kTf32)
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+  else
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+}
+
+// Nearest TF32 value (ties away from zero) kept as an FP32 number: the 13
+// low mantissa bits are rounded off on the bit pattern with two integer
+// operations (operands here are finite and far below FLT_MAX).
+__device__ __forceinline__ float tf32_rna(float x) {
+  return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
+}
+
+// lo part of x against its truncated TF32 value (x - trunc(x) is exact).
+__device__ __forceinline__ float tf32_lo(float x) {
+  return tf32_rna(x - __uint_as_float(__float_as_uint(x) & 0xFFFFE000u));
 }
 
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
@@ -160,9 +219,14 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
 }
 
 constexpr int kMaxStages = 4;
-constexpr int kThreads = 64 + kEpiThreads;  // warp 0 TMA, warp 1 MMA, warps 2-9 epilogue
+// Stages whose A boxes are prefetched into L2 ahead of their shared-memory
+// load.  A load that misses L2 takes ~2 us on a busy GB300, several times
+// the time the tensor cores need for the stages that fit in the ring.
+constexpr int kPrefetchAhead = 8;
 
-// Shared-memory plan of one launch (host and device agree on it).
+// Shared-memory plan of one launch (host and device agree on it).  A stage
+// holds two 128 x 128-byte tiles: the hi and lo BF16 planes, or the FP32
+// tile (hi after conversion) and its lo part.
 struct TcShape {
   int NS, NW, nk, stages;
   __host__ __device__ uint32_t b_chunk() const { return (uint32_t)NW * 128; }
@@ -174,27 +238,36 @@ struct TcShape {
 // Epilogue of 32 accumulator columns n0..n0+31 of row m (all indices fit in
 // 32 bits: M*N and n1*n2*n3 are below 2^31 for every supported shape).
 // (i, j) = (m % P1, m / P1) for kinds 1 and 2, computed once per tile.
+template <bool kTf32>
+__device__ __forceinline__ void store_y(const TcEpilogue& e, int idx, float v) {
+  if constexpr (kTf32)
+    e.y32[idx] = v;
+  else
+    store_split(e.y_hi, e.y_lo, idx, v);
+}
+
+template <bool kTf32>
 __device__ __forceinline__ void epilogue_cols(const TcEpilogue& e, const float* v, int M, int m,
                                               int n0, int i, int j, bool valid, float lxy, bool nxy,
                                               const float* s_lz, const uint8_t* s_nz) {
   if (e.kind == 0) {
     int idx = n0 * M + m;
 #pragma unroll
-    for (int q = 0; q < 32; ++q, idx += M) store_split(e.y_hi, e.y_lo, idx, v[q]);
+    for (int q = 0; q < 32; ++q, idx += M) store_y<kTf32>(e, idx, v[q]);
   } else if (e.kind == 1) {
     // s_lz holds lam_z(k) + sigma
     int idx = n0 * M + m;
     if (valid && !nxy && n0 + 32 <= e.n3) {
 #pragma unroll
       for (int q = 0; q < 32; ++q, idx += M)
-        store_split(e.y_hi, e.y_lo, idx, __fdividef(v[q], lxy + s_lz[n0 + q]));
+        store_y<kTf32>(e, idx, __fdividef(v[q], lxy + s_lz[n0 + q]));
     } else {
 #pragma unroll
       for (int q = 0; q < 32; ++q, idx += M) {
         const int k = n0 + q;
         float r = 0.f;
         if (valid && k < e.n3 && !(nxy && s_nz[k])) r = __fdividef(v[q], lxy + s_lz[k]);
-        store_split(e.y_hi, e.y_lo, idx, r);
+        store_y<kTf32>(e, idx, r);
       }
     }
   } else {
@@ -213,12 +286,15 @@ __device__ __forceinline__ void epilogue_cols(const TcEpilogue& e, const float* 
   }
 }
 
-__global__ void __launch_bounds__(kThreads, 1)
+template <bool kTf32>
+__global__ void __launch_bounds__(Cfg<kTf32>::kThreads, 1)
     k_tc_transform(const __grid_constant__ CUtensorMap tx_hi, const __grid_constant__ CUtensorMap tx_lo,
                    const __grid_constant__ CUtensorMap tb_hi, const __grid_constant__ CUtensorMap tb_lo,
                    int M, TcShape sh, TcEpilogue e, int* err) {
+  using C = Cfg<kTf32>;
   extern __shared__ uint8_t smem_raw[];
-  __shared__ uint64_t bar_b, full_bar[kMaxStages], empty_bar[kMaxStages], acc_full[2], acc_empty[2];
+  __shared__ uint64_t bar_b, full_bar[kMaxStages], cvt_bar[kMaxStages], empty_bar[kMaxStages],
+      acc_full[2], acc_empty[2];
   __shared__ uint32_t tmem_slot;
   __shared__ float s_lz[256];     // z eigenvalues (divide epilogue)
   __shared__ uint8_t s_nz[256];   // z null-mode flags
@@ -238,20 +314,27 @@ __global__ void __launch_bounds__(kThreads, 1)
   uint8_t* b_hi = smem;
   uint8_t* b_lo = smem + (size_t)nk * bchunk;
   uint8_t* a_base = smem + sh.b_bytes();
+  constexpr uint32_t kTile = kBlockM * 128;  // one 128-row x 128-byte tile
 
   if (threadIdx.x == 0) {
     mbar_init(&bar_b, 1);
     for (int s = 0; s < S; ++s) {
       mbar_init(&full_bar[s], 1);
+      mbar_init(&cvt_bar[s], kTf32 ? C::kCvtThreads : 1);
       mbar_init(&empty_bar[s], 1);
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&acc_full[b], 1);
-      mbar_init(&acc_empty[b], kEpiThreads);
+      mbar_init(&acc_empty[b], C::kEpiThreads);
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  const uint32_t ncols = 2 * NW <= 32 ? 32 : 2 * NW <= 64 ? 64 : 2 * NW <= 128 ? 128 : 256;
+  const int set_cols = kTf32 ? 3 * NW : NW;  // TMEM columns of one accumulator set
+  const uint32_t ncols = 2 * set_cols <= 32    ? 32
+                         : 2 * set_cols <= 64  ? 64
+                         : 2 * set_cols <= 128 ? 128
+                         : 2 * set_cols <= 256 ? 256
+                                               : 512;
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(&tmem_slot)),
@@ -268,25 +351,43 @@ __global__ void __launch_bounds__(kThreads, 1)
       // resident slice of B
       mbar_expect_tx(&bar_b, sh.b_bytes());
       for (int c = 0; c < nk; ++c) {
-        tma_load_2d(b_hi + (size_t)c * bchunk, &tb_hi, &bar_b, c * kChunkK, slice * NW);
-        tma_load_2d(b_lo + (size_t)c * bchunk, &tb_lo, &bar_b, c * kChunkK, slice * NW);
+        tma_load_2d(b_hi + (size_t)c * bchunk, &tb_hi, &bar_b, c * C::kChunkK, slice * NW);
+        tma_load_2d(b_lo + (size_t)c * bchunk, &tb_lo, &bar_b, c * C::kChunkK, slice * NW);
       }
       int it = 0;
       bool ok = true;
+      // prefetch cursor: (pt, pc) runs kPrefetchAhead stages ahead of (t, c)
+      int pt = cta_rank, pc = 0;
+      auto prefetch_next = [&]() {
+        if (pt >= mtiles) return;
+        tma_prefetch_2d(&tx_hi, pc * C::kChunkK, pt * kBlockM);
+        if constexpr (!kTf32) tma_prefetch_2d(&tx_lo, pc * C::kChunkK, pt * kBlockM);
+        if (++pc == nk) {
+          pc = 0;
+          pt += cta_count;
+        }
+      };
+      for (int q = 0; q < kPrefetchAhead; ++q) prefetch_next();
       for (int t = cta_rank; t < mtiles && ok; t += cta_count) {
         for (int c = 0; c < nk; ++c, ++it) {
           const int s = it % S, u = it / S;
+          prefetch_next();
           if (u > 0 && !(ok = mbar_wait(&empty_bar[s], (u - 1) & 1, err))) break;
           uint8_t* st = a_base + (size_t)s * sh.a_stage();
-          mbar_expect_tx(&full_bar[s], sh.a_stage());
-          tma_load_2d(st, &tx_hi, &full_bar[s], c * kChunkK, t * kBlockM);
-          tma_load_2d(st + kBlockM * 128, &tx_lo, &full_bar[s], c * kChunkK, t * kBlockM);
+          if constexpr (kTf32) {
+            mbar_expect_tx(&full_bar[s], kTile);
+            tma_load_2d(st, &tx_hi, &full_bar[s], c * C::kChunkK, t * kBlockM);
+          } else {
+            mbar_expect_tx(&full_bar[s], 2 * kTile);
+            tma_load_2d(st, &tx_hi, &full_bar[s], c * C::kChunkK, t * kBlockM);
+            tma_load_2d(st + kTile, &tx_lo, &full_bar[s], c * C::kChunkK, t * kBlockM);
+          }
         }
       }
     }
   } else if (warp == 1) {
     if (lane == 0) {
-      const uint32_t idesc = instr_desc_bf16(kBlockM, NW);
+      const uint32_t idesc = instr_desc(kBlockM, NW, kTf32);
       bool ok = mbar_wait(&bar_b, 0, err);
       int it = 0, tc = 0;
       const uint32_t bh0 = smem_u32(b_hi), bl0 = smem_u32(b_lo);
@@ -294,31 +395,59 @@ __global__ void __launch_bounds__(kThreads, 1)
         const int b = tc & 1, u = tc >> 1;
         if (u > 0 && !(ok = mbar_wait(&acc_empty[b], (u - 1) & 1, err))) break;
         fence_after();
-        const uint32_t d = tmem + (uint32_t)(b * NW);
+        const uint32_t d = tmem + (uint32_t)(b * set_cols);
         for (int c = 0; c < nk; ++c, ++it) {
           const int s = it % S;
           if (!(ok = mbar_wait(&full_bar[s], (it / S) & 1, err))) break;
           fence_after();
           const uint32_t ab = smem_u32(a_base + (size_t)s * sh.a_stage());
+          // four 32-byte K steps per 128-byte row (16 BF16 or 8 TF32 values)
+          if constexpr (kTf32) {
+            // hi products now: hi*hi of the first / second half of K into
+            // its own sum, hi*lo into the small-product sum
+            const int h = c < nk / 2 ? 1 : 2;
 #pragma unroll
-          for (int kk = 0; kk < kChunkK / 16; ++kk) {
-            const uint64_t ah = smem_desc(ab + kk * 32);
-            const uint64_t al = smem_desc(ab + kBlockM * 128 + kk * 32);
-            const uint64_t bh = smem_desc(bh0 + c * bchunk + kk * 32);
-            const uint64_t bl = smem_desc(bl0 + c * bchunk + kk * 32);
-            mma_bf16(d, al, bh, idesc, (c | kk) != 0 ? 1u : 0u);
-            mma_bf16(d, ah, bl, idesc, 1u);
-            mma_bf16(d, ah, bh, idesc, 1u);
+            for (int kk = 0; kk < 4; ++kk) {
+              const uint64_t ah = smem_desc(ab + kk * 32);
+              const uint64_t bh = smem_desc(bh0 + c * bchunk + kk * 32);
+              const uint64_t bl = smem_desc(bl0 + c * bchunk + kk * 32);
+              const bool first = (c == 0 || c == nk / 2) && kk == 0;
+              mma<true>(d + (uint32_t)(h * NW), ah, bh, idesc, first ? 0u : 1u);
+              mma<true>(d, ah, bl, idesc, (c | kk) != 0 ? 1u : 0u);
+            }
+            // lo*hi once the converters have written the lo tile
+            if (!(ok = mbar_wait(&cvt_bar[s], (it / S) & 1, err))) break;
+            fence_after();
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk) {
+              const uint64_t al = smem_desc(ab + kTile + kk * 32);
+              const uint64_t bh = smem_desc(bh0 + c * bchunk + kk * 32);
+              mma<true>(d, al, bh, idesc, 1u);
+            }
+          } else {
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk) {
+              const uint64_t ah = smem_desc(ab + kk * 32);
+              const uint64_t al = smem_desc(ab + kTile + kk * 32);
+              const uint64_t bh = smem_desc(bh0 + c * bchunk + kk * 32);
+              const uint64_t bl = smem_desc(bl0 + c * bchunk + kk * 32);
+              mma<false>(d, al, bh, idesc, (c | kk) != 0 ? 1u : 0u);
+              mma<false>(d, ah, bl, idesc, 1u);
+              mma<false>(d, ah, bh, idesc, 1u);
+            }
           }
           mma_commit(&empty_bar[s]);
         }
         if (ok) mma_commit(&acc_full[b]);
       }
     }
-  } else {
+  } else if (warp < 2 + C::kEpiWarps) {
     const int q = warp & 3;                 // TMEM lane quarter this warp may access
-    const int half = (warp - 2) >> 2;       // which half of the NW columns
+    const int part = (warp - 2) >> 2;       // which share of the NW columns
+    constexpr int parts = C::kEpiWarps / 4;
     const int row = q * 32 + lane;
+    const int chunks = NW / 32, per = (chunks + parts - 1) / parts;  // split on 32-column chunks
+    const int c_lo = part * per * 32, c_hi = min(NW, (part + 1) * per * 32);
     int tc = 0;
     for (int t = cta_rank; t < mtiles; t += cta_count, ++tc) {
       const int b = tc & 1;
@@ -338,16 +467,46 @@ __global__ void __launch_bounds__(kThreads, 1)
           nxy = e.sigma_null && e.null_x[i] && e.null_y[j];
         }
       }
-      const uint32_t trow = tmem + (static_cast<uint32_t>(q * 32) << 16) + (uint32_t)(b * NW);
+      const uint32_t trow = tmem + (static_cast<uint32_t>(q * 32) << 16) + (uint32_t)(b * set_cols);
       float v[32];
-      const int chunks = NW / 32, first = (chunks + 1) / 2;  // split on 32-column chunks
-      const int c_lo = half ? first * 32 : 0, c_hi = half ? NW : first * 32;
       for (int cc = c_lo; cc < c_hi; cc += 32) {
         tmem_load32(trow + cc, v);
-        epilogue_cols(e, v, M, m, slice * NW + cc, i, j, valid, lxy, nxy, s_lz, s_nz);
+        if constexpr (kTf32) {
+          float w[32];
+          tmem_load32(trow + 2 * NW + cc, w);
+#pragma unroll
+          for (int x = 0; x < 32; ++x) v[x] += w[x];
+          tmem_load32(trow + NW + cc, w);
+#pragma unroll
+          for (int x = 0; x < 32; ++x) v[x] += w[x];
+        }
+        epilogue_cols<kTf32>(e, v, M, m, slice * NW + cc, i, j, valid, lxy, nxy, s_lz, s_nz);
       }
       fence_before();
       mbar_arrive(&acc_empty[b]);
+    }
+  } else if constexpr (kTf32) {
+    // converter warps: lo part of every landed FP32 stage
+    const int ct = threadIdx.x - 32 * (2 + C::kEpiWarps);
+    int it = 0;
+    bool ok = true;
+    for (int t = cta_rank; t < mtiles && ok; t += cta_count) {
+      for (int c = 0; c < nk; ++c, ++it) {
+        const int s = it % S;
+        if (!(ok = mbar_wait(&full_bar[s], (it / S) & 1, err))) break;
+        const float4* hi = reinterpret_cast<const float4*>(a_base + (size_t)s * sh.a_stage());
+        float4* lo = reinterpret_cast<float4*>(a_base + (size_t)s * sh.a_stage() + kTile);
+        float4 x[kTile / 16 / C::kCvtThreads];
+#pragma unroll
+        for (int v = 0; v < (int)(kTile / 16 / C::kCvtThreads); ++v) x[v] = hi[ct + v * C::kCvtThreads];
+#pragma unroll
+        for (int v = 0; v < (int)(kTile / 16 / C::kCvtThreads); ++v)
+          lo[ct + v * C::kCvtThreads] =
+              make_float4(tf32_lo(x[v].x), tf32_lo(x[v].y), tf32_lo(x[v].z), tf32_lo(x[v].w));
+        // generic-proxy writes must be visible to the tensor core's reads
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_arrive(&cvt_bar[s]);
+      }
     }
   }
   __syncwarp();
@@ -373,13 +532,17 @@ int get_encode() {
   return MF_OK;
 }
 
-int make_map(CUtensorMap* map, const __nv_bfloat16* ptr, int rows, int cols, int box_rows) {
+// 2D map over a row-major rows x cols array of BF16 or FP32, box = one
+// 128-byte swizzle row of K values by box_rows rows.
+int make_map(CUtensorMap* map, const void* ptr, bool f32, int rows, int cols, int box_rows) {
+  const int esz = f32 ? 4 : 2;
   cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
-  cuuint64_t strides[1] = {(cuuint64_t)cols * 2};
-  cuuint32_t box[2] = {(cuuint32_t)kChunkK, (cuuint32_t)box_rows};
+  cuuint64_t strides[1] = {(cuuint64_t)cols * esz};
+  cuuint32_t box[2] = {(cuuint32_t)(128 / esz), (cuuint32_t)box_rows};
   cuuint32_t estr[2] = {1, 1};
-  CUresult r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<__nv_bfloat16*>(ptr),
-                        dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+  CUresult r = g_encode(map, f32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16,
+                        2, const_cast<void*>(ptr), dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE,
                         CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return set_error(MF_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
@@ -388,38 +551,49 @@ int make_map(CUtensorMap* map, const __nv_bfloat16* ptr, int rows, int cols, int
 
 }  // namespace
 
-static TcShape shape_for(int N, int K) {
+// BF16: NS = 2 slices from N = 128 (resident B <= 128 KB).  TF32 holds half
+// as many K values per byte and three accumulators per set, so it always
+// uses 64-column slices (2 x 3 x 64 TMEM columns).
+static TcShape shape_for(int N, int K, bool tf32) {
   TcShape sh;
-  sh.NS = N >= 128 ? 2 : 1;
+  if (tf32)
+    sh.NS = N / 64;
+  else
+    sh.NS = N >= 128 ? 2 : 1;
   sh.NW = N / sh.NS;
-  sh.nk = K / kChunkK;
+  sh.nk = K / (tf32 ? 32 : 64);
   const uint32_t budget = 224 * 1024;
-  const uint32_t left = budget - sh.b_bytes();
+  const uint32_t left = sh.b_bytes() < budget ? budget - sh.b_bytes() : 0;
   sh.stages = (int)std::min<uint32_t>(kMaxStages, left / sh.a_stage());
   return sh;
 }
 
-int tc_plan_create(TcPlan** out, const __nv_bfloat16* x_hi, const __nv_bfloat16* x_lo,
-                   const __nv_bfloat16* b_hi, const __nv_bfloat16* b_lo, int M, int N, int K) {
+int tc_plan_create(TcPlan** out, bool tf32, const void* x_hi, const void* x_lo, const void* b_hi,
+                   const void* b_lo, int M, int N, int K) {
   *out = nullptr;
-  if (M % kBlockM || K % kChunkK || N != K || N < 64 || N > 256 || N % 32 ||
+  const int chunk = tf32 ? 32 : 64;
+  if (M % kBlockM || K % chunk || N != K || N < 64 || N > 256 || N % 32 ||
       (long long)M * N >= (1LL << 31))
     return set_error(MF_ERR_UNSUPPORTED, "tensor-core transform: unsupported shape M=%d N=%d K=%d", M,
                      N, K);
-  for (const void* p : {(const void*)x_hi, (const void*)x_lo, (const void*)b_hi, (const void*)b_lo})
-    if (reinterpret_cast<uintptr_t>(p) % 16)
+  if (!tf32 && !x_lo) return set_error(MF_ERR_ARG, "tensor-core transform: missing lo plane");
+  for (const void* p : {x_hi, tf32 ? x_hi : x_lo, b_hi, b_lo})
+    if (!p || reinterpret_cast<uintptr_t>(p) % 16)
       return set_error(MF_ERR_ARG, "tensor-core transform: operands must be 16-byte aligned");
   int rc = get_encode();
   if (rc) return rc;
-  const TcShape sh = shape_for(N, K);
+  const TcShape sh = shape_for(N, K, tf32);
   if (sh.stages < 2 || sh.NW % 32)
     return set_error(MF_ERR_UNSUPPORTED, "tensor-core transform: no shared-memory plan for N=%d", N);
   TcPlan* p = new TcPlan();
   p->M = M;
   p->N = N;
   p->K = K;
-  if ((rc = make_map(&p->x_hi, x_hi, M, K, kBlockM)) || (rc = make_map(&p->x_lo, x_lo, M, K, kBlockM)) ||
-      (rc = make_map(&p->b_hi, b_hi, N, K, sh.NW)) || (rc = make_map(&p->b_lo, b_lo, N, K, sh.NW))) {
+  p->tf32 = tf32;
+  if ((rc = make_map(&p->x_hi, x_hi, tf32, M, K, kBlockM)) ||
+      (rc = make_map(&p->x_lo, tf32 ? x_hi : x_lo, tf32, M, K, kBlockM)) ||
+      (rc = make_map(&p->b_hi, b_hi, tf32, N, K, sh.NW)) ||
+      (rc = make_map(&p->b_lo, b_lo, tf32, N, K, sh.NW))) {
     delete p;
     return rc;
   }
@@ -429,22 +603,31 @@ int tc_plan_create(TcPlan** out, const __nv_bfloat16* x_hi, const __nv_bfloat16*
 
 void tc_plan_destroy(TcPlan* p) { delete p; }
 
-int tc_transform(const TcPlan* p, const TcEpilogue& e, int* dev_err, cudaStream_t st) {
-  const TcShape sh = shape_for(p->N, p->K);
+template <bool kTf32>
+static int launch(const TcPlan* p, const TcEpilogue& e, int* dev_err, cudaStream_t st) {
+  const TcShape sh = shape_for(p->N, p->K, kTf32);
   static int num_sms = 0;
   if (!num_sms) {
     int dev = 0;
     MF_CUDA(cudaGetDevice(&dev));
-    MF_CUDA(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev));
-    MF_CUDA(cudaFuncSetAttribute(k_tc_transform, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    MF_CUDA(cudaFuncSetAttribute(k_tc_transform<kTf32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  224 * 1024 + 1024));
+    int sms = 0;
+    MF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    num_sms = sms;
   }
   const int mtiles = p->M / kBlockM;
-  int grid = std::min(num_sms / sh.NS, mtiles) * sh.NS;
-  k_tc_transform<<<grid, kThreads, sh.smem(), st>>>(p->x_hi, p->x_lo, p->b_hi, p->b_lo, p->M, sh, e,
-                                                    dev_err);
+  const int grid = std::min(num_sms / sh.NS, mtiles) * sh.NS;
+  k_tc_transform<kTf32><<<grid, Cfg<kTf32>::kThreads, sh.smem(), st>>>(
+      p->x_hi, p->x_lo, p->b_hi, p->b_lo, p->M, sh, e, dev_err);
   MF_CUDA(cudaGetLastError());
   return MF_OK;
+}
+
+int tc_transform(const TcPlan* p, const TcEpilogue& e, int* dev_err, cudaStream_t st) {
+  if (p->tf32 ? !e.y32 && e.kind != 2 : (!e.y_hi || !e.y_lo) && e.kind != 2)
+    return set_error(MF_ERR_ARG, "tensor-core transform: output does not match the operand format");
+  return p->tf32 ? launch<true>(p, e, dev_err, st) : launch<false>(p, e, dev_err, st);
 }
 
 }  // namespace mf

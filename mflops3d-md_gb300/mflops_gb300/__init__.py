@@ -27,7 +27,9 @@ import os
 import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-_LIB_PATH = os.path.join(os.path.dirname(_HERE), "lib", "libmflops_gb300.so")
+# MFLOPS_GB300_LIB selects another build of the library (same C ABI).
+_LIB_PATH = os.environ.get("MFLOPS_GB300_LIB") or os.path.join(os.path.dirname(_HERE), "lib",
+                                                               "libmflops_gb300.so")
 
 MF_OK = 0
 MF_ERR_ARG = 1

@@ -1,5 +1,5 @@
-"""Split-BF16 tensor-core transforms + FP64 iterative refinement against the
-FP64 oracle.  Tolerance: relative L2 error <= 1e-10 after
+"""Split-BF16 and 3xTF32 tensor-core transforms + FP64 iterative refinement
+against the FP64 oracle.  Tolerance: relative L2 error <= 1e-10 after
 refinement; the unrefined split-precision error is reported alongside."""
 import numpy as np
 import pytest
@@ -12,7 +12,8 @@ from helpers import bc_arrays, field, grids, rel_l2, solf_mask
 pytestmark = pytest.mark.gpu
 
 
-def mixed_case(mf, nall, bct, sigma, refine, kind="tanh", seed=5):
+def mixed_case(mf, nall, bct, sigma, refine, kind="tanh", seed=5, prec=None):
+    prec = mf.MF_PREC_SPLIT_BF16 if prec is None else prec
     gx, gy, gz = grids(*nall, kind=kind)
     n1, n2, n3 = (v - 2 for v in nall)
     sc_ref = S.Solver3D(gx, gy, gz, bct, 6)
@@ -22,8 +23,7 @@ def mixed_case(mf, nall, bct, sigma, refine, kind="tanh", seed=5):
     solf0 = np.zeros((n1 + 2, n2 + 2, n3 + 2), order="F")
     ref = S.solve_3d(sc_ref, rhs, sigma, solf0, bcx, bcy, bcz)
     got = sc.solve_3d(mf.to_device(rhs), sigma, mf.to_device(solf0), mf.to_device(bcx),
-                      mf.to_device(bcy), mf.to_device(bcz), precision=mf.MF_PREC_SPLIT_BF16,
-                      refine=refine)
+                      mf.to_device(bcy), mf.to_device(bcz), precision=prec, refine=refine)
     m = solf_mask(n1, n2, n3)
     return rel_l2(mf.to_host(got)[m], ref[m])
 
@@ -70,3 +70,44 @@ def test_mixed_matches_fp64_gpu_at_257(mf, gpu):
     err = (torch.linalg.vector_norm(mixed - plain) / torch.linalg.vector_norm(plain)).item()
     print("257^3 split-bf16 + 2 refinements vs FP64 GPU: %.3e" % err)
     assert err < 1e-10
+
+
+def test_tf32_unrefined_is_more_accurate(mf, gpu):
+    err_bf = mixed_case(mf, (66, 66, 66), (1,) * 6, -1e3, refine=0)
+    err = mixed_case(mf, (66, 66, 66), (1,) * 6, -1e3, refine=0, prec=mf.MF_PREC_3XTF32)
+    print("3xtf32 unrefined rel L2 error: %.3e (split-bf16 %.3e)" % (err, err_bf))
+    assert err < 1e-5 and err < err_bf
+
+
+@pytest.mark.parametrize("sigma", [0.0, -1e3])
+def test_tf32_one_refinement_reaches_1e10(mf, gpu, sigma):
+    err = mixed_case(mf, (66, 66, 66), (1,) * 6, sigma, refine=1, prec=mf.MF_PREC_3XTF32)
+    print("3xtf32 + 1 refinement rel L2 error: %.3e" % err)
+    assert err < 1e-10
+
+
+def test_tf32_slice_shapes_and_neumann(mf, gpu):
+    # padded sizes 192 (three 64-column slices), 64 and 128 (one slice)
+    err = mixed_case(mf, (150, 34, 98), (1, 2, 1, 1, 2, 1), -1e6, refine=2,
+                     prec=mf.MF_PREC_3XTF32)
+    assert err < 1e-10
+
+
+def test_tf32_matches_fp64_gpu_at_257(mf, gpu):
+    import torch
+    from oracle import mesh
+    n = 255
+    gx, gy = mesh.uniform_grid(257), mesh.tanh_grid(257, 2.0)
+    sc = mf.SolverCoeffs3D(gx, gy, gx, (1,) * 6, 6)
+    rhs = torch.randn((n, n, n), dtype=torch.float64, device="cuda", generator=torch.Generator("cuda").manual_seed(5)).permute(2, 1, 0)
+    bc = [mf.empty_device((n, n, 2)) for _ in range(3)]
+    plain = mf.empty_device((257, 257, 257))
+    mixed = mf.empty_device((257, 257, 257))
+    sc.solve_3d(rhs, 0.0, plain, *bc)
+    errs = []
+    for refine in (0, 1, 2):
+        sc.solve_3d(rhs, 0.0, mixed, *bc, precision=mf.MF_PREC_3XTF32, refine=refine)
+        sc.device_status()
+        errs.append((torch.linalg.vector_norm(mixed - plain) / torch.linalg.vector_norm(plain)).item())
+    print("257^3 3xtf32 vs FP64 GPU, refine 0/1/2: %.3e %.3e %.3e" % tuple(errs))
+    assert errs[2] < 1e-10
