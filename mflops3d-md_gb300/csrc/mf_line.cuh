@@ -45,6 +45,24 @@ __device__ __forceinline__ double widen(float f) {
   return __longlong_as_double((long long)(sgn | (exp << 52) | ((uint64_t)(u & 0x7FFFFFu) << 29)));
 }
 
+// FP64 -> FP32 rounded to nearest even from the bit fields (integer pipe).
+// Results below the normal FP32 range flush to signed zero, overflow gives
+// infinity, NaN stays NaN.
+__device__ __forceinline__ float narrow(double d) {
+  const uint64_t u = (uint64_t)__double_as_longlong(d);
+  const uint32_t sgn = (uint32_t)(u >> 32) & 0x80000000u;
+  const int e = (int)((u >> 52) & 0x7FF);
+  const uint64_t m = u & 0xFFFFFFFFFFFFFull;
+  if (e == 0x7FF) return __uint_as_float(sgn | 0x7F800000u | (m ? 0x400000u : 0u));
+  const int ef = e - 1023 + 127;
+  if (ef <= 0) return __uint_as_float(sgn);
+  if (ef >= 255) return __uint_as_float(sgn | 0x7F800000u);
+  uint32_t r = ((uint32_t)ef << 23) | (uint32_t)(m >> 29);
+  const uint32_t rest = (uint32_t)(m & 0x1FFFFFFFu);
+  if (rest > 0x10000000u || (rest == 0x10000000u && (r & 1u))) ++r;  // may carry into the exponent
+  return __uint_as_float(sgn | r);
+}
+
 template <class T, class In>
 __device__ __forceinline__ T load_as(const In* p, long long i);
 template <>

@@ -257,12 +257,20 @@ struct ResidFin {
   long long pstride;     // modes 2,3: padded stride along the line
   float* r32;            // mode 3: offset to the line
   __device__ __forceinline__ void operator()(T*, int i, long long idx, T y) const {
+    put(i, idx, y, rin[idx], mode == 0 ? load_as<T, In>(u, idx) : T(0));
+  }
+  // Final store of row i with the row's rin (and, mode 0, u) value given.
+  __device__ __forceinline__ void put(int i, long long idx, T y, T r, T uv) const {
     if (mode == 0) {
-      out[idx] = rin[idx] - sigma * load_as<T, In>(u, idx) - y;
+      out[idx] = r - sigma * uv - y;
     } else if (mode == 1) {
-      out[idx] = rin[idx] - y;
+      out[idx] = r - y;
     } else {
-      const float v = (float)(rin[idx] - y);
+      float v;
+      if constexpr (sizeof(T) == 8)
+        v = narrow(r - y);
+      else
+        v = r - y;
       if (x32) {
         x32[i * pstride] = v;
       } else {
@@ -380,10 +388,9 @@ __device__ __forceinline__ double moment_sum(const TriRow& r, const float (&v)[W
   return widen(sh) + widen(l + se + pl);
 }
 
-template <class Fin>
 __device__ __forceinline__ void solve_line_tri(const TriRow* __restrict__ R, int n, const float* u,
                                                double* xs, long long s, double lo, double hi,
-                                               const Fin& fin) {
+                                               const ResidFin<double, float>& fin) {
   float f[7], g[7];
 #pragma unroll
   for (int m = 0; m < 7; ++m) {
@@ -433,35 +440,54 @@ __device__ __forceinline__ void solve_line_tri(const TriRow* __restrict__ R, int
   const TriRow& rB = R[n - 1];
   const double xA = moment_sum<7>(rA, g, g[5], 5) + rA.cbc * (hi - widen(g[5])) - rA.ft * xm;
   const double xB = moment_sum<7>(rB, g, g[6], 6) + rB.cbc * (hi - widen(g[6])) - rB.ft * xA;
-  // back substitution; rb[k] = forward value of row i - k
+  // back substitution with the final combination of each row; the forward
+  // value, rin and (first pass) u of row i - k are loaded kAhead rows ahead
+  const bool need_u = fin.mode == 0;
+  auto uval = [&](long long o) { return need_u ? widen(fin.u[o]) : 0.0; };
   double y1 = xB;
-  fin(xs, n - 1, (long long)(n - 1) * s, xB);
+  fin.put(n - 1, (long long)(n - 1) * s, xB, fin.rin[(long long)(n - 1) * s], uval((long long)(n - 1) * s));
   double y = xA - rA.dt * y1;
-  fin(xs, n - 2, (long long)(n - 2) * s, y);
+  fin.put(n - 2, (long long)(n - 2) * s, y, fin.rin[(long long)(n - 2) * s], uval((long long)(n - 2) * s));
   y1 = y;
   i = n - 3;
-  double rb[kAhead];
+  double rb[kAhead], rr[kAhead];
+  float ru[kAhead];
 #pragma unroll
-  for (int k = 0; k < kAhead; ++k) rb[k] = (i - k >= 0) ? xs[(long long)(i - k) * s] : 0.0;
+  for (int k = 0; k < kAhead; ++k) {
+    const bool in = i - k >= 0;
+    const long long o = (long long)(i - k) * s;
+    rb[k] = in ? xs[o] : 0.0;
+    rr[k] = in ? fin.rin[o] : 0.0;
+    ru[k] = (in && need_u) ? fin.u[o] : 0.f;
+  }
   for (; i - (kAhead - 1) >= 0; i -= kAhead) {
-    double nb[kAhead];
+    double nb[kAhead], nr[kAhead];
+    float nu[kAhead];
 #pragma unroll
     for (int k = 0; k < kAhead; ++k) {
       const int j = i - kAhead - k;
-      nb[k] = (j >= 0) ? xs[(long long)j * s] : 0.0;
+      const long long o = (long long)j * s;
+      nb[k] = (j >= 0) ? xs[o] : 0.0;
+      nr[k] = (j >= 0) ? fin.rin[o] : 0.0;
+      nu[k] = (j >= 0 && need_u) ? fin.u[o] : 0.f;
     }
 #pragma unroll
     for (int k = 0; k < kAhead; ++k) {
       const double yy = rb[k] - R[i - k].dt * y1;
-      fin(xs, i - k, (long long)(i - k) * s, yy);
+      fin.put(i - k, (long long)(i - k) * s, yy, rr[k], widen(ru[k]));
       y1 = yy;
     }
 #pragma unroll
-    for (int k = 0; k < kAhead; ++k) rb[k] = nb[k];
+    for (int k = 0; k < kAhead; ++k) {
+      rb[k] = nb[k];
+      rr[k] = nr[k];
+      ru[k] = nu[k];
+    }
   }
   for (; i >= 0; --i) {
-    const double yy = xs[(long long)i * s] - R[i].dt * y1;
-    fin(xs, i, (long long)i * s, yy);
+    const long long o = (long long)i * s;
+    const double yy = xs[o] - R[i].dt * y1;
+    fin.put(i, o, yy, fin.rin[o], uval(o));
     y1 = yy;
   }
 }
@@ -495,14 +521,12 @@ __global__ void __launch_bounds__(128) k_resid_tri(ResidPass<double> p, const Tr
 }
 
 // solf(1:n1,1:n2,1:n3) = u1 + C, widened exactly and summed in FP64.
+// Grid: x over i (blocks of 256), y = j, z = k.
 __global__ void k_finalize(const float* __restrict__ u1, const float* __restrict__ c,
                            double* __restrict__ solf, int n1, int n2, int n3) {
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const long long tot = (long long)n1 * n2 * n3;
-  if (idx >= tot) return;
-  const int i = (int)(idx % n1);
-  const long long jk = idx / n1;
-  const int j = (int)(jk % n2), k = (int)(jk / n2);
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+  if (i >= n1) return;
+  const long long idx = i + (long long)n1 * (j + (long long)n2 * k);
   double v = widen(u1[idx]);
   if (c) v += widen(c[idx]);
   solf[(i + 1) + (long long)(n1 + 2) * ((j + 1) + (long long)(n2 + 2) * (k + 1))] = v;
@@ -520,18 +544,17 @@ struct FoldArgsF {
   const float* bz;
 };
 
+// Grid: x over i (blocks of 256, P1 <= 256 is a multiple of 64), y = j < P2,
+// z = k < P3.
 __global__ void k_fold_split(const double* __restrict__ rhs, FoldArgsF a, __nv_bfloat16* hi,
                              __nv_bfloat16* lo, float* x32, int n1, int n2, int n3, int P1, int P2,
                              int P3) {
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const long long tot = (long long)P1 * P2 * P3;
-  if (idx >= tot) return;
-  const int i = (int)(idx % P1);
-  const long long jk = idx / P1;
-  const int j = (int)(jk % P2), k = (int)(jk / P2);
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+  if (i >= P1) return;
+  const long long idx = i + (long long)P1 * (j + (long long)P2 * k);
   float v = 0.f;
   if (i < n1 && j < n2 && k < n3) {
-    v = (float)rhs[i + (long long)n1 * (j + (long long)n2 * k)];
+    v = narrow(rhs[i + (long long)n1 * (j + (long long)n2 * k)]);
     const long long fx = j + (long long)n2 * k, fy = i + (long long)n1 * k, fz = i + (long long)n1 * j;
     const long long sx = (long long)n2 * n3, sy = (long long)n1 * n3, sz = (long long)n1 * n2;
 #pragma unroll
@@ -1035,8 +1058,7 @@ static int fold_split(mf_solver3d* sc, bool tf32, const double* rhs, const doubl
   args.bx = fa[0];
   args.by = fa[1];
   args.bz = fa[2];
-  const long long ptot = (long long)sc->P[0] * sc->P[1] * sc->P[2];
-  k_fold_split<<<blocks_for(ptot, 256), 256, 0, st>>>(
+  k_fold_split<<<dim3(blocks_for(sc->P[0], 256), sc->P[1], sc->P[2]), 256, 0, st>>>(
       rhs, args, tf32 ? nullptr : sc->Xa_hi.as<__nv_bfloat16>(),
       tf32 ? nullptr : sc->Xa_lo.as<__nv_bfloat16>(), tf32 ? sc->Xa32.as<float>() : nullptr,
       (int)n1, (int)n2, (int)n3, sc->P[0], sc->P[1], sc->P[2]);
@@ -1090,7 +1112,8 @@ static int solve_mixed_dev(mf_solver3d* sc, const double* rhs, double sigma, dou
     if ((rc = approx_solve(sc, tf32, sigma, C, it > 0, st))) return rc;
   }
   sc->prof.begin(kProfCopy, st);
-  k_finalize<<<blocks_for(tot, 256), 256, 0, st>>>(u1, refine > 0 ? C : nullptr, solf, n1, n2, n3);
+  k_finalize<<<dim3(blocks_for(n1, 256), n2, n3), 256, 0, st>>>(u1, refine > 0 ? C : nullptr, solf, n1,
+                                                                n2, n3);
   sc->prof.end(st);
   MF_CUDA(cudaGetLastError());
   return faces(sc, solf, bcs, st);

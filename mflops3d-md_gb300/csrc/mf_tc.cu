@@ -98,10 +98,29 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 
-// Bounded wait: false (and *err raised) once the clock budget is spent.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err) {
+// Non-blocking test of a phase.
+__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait: false (and *err raised) once the clock budget is spent.  A
+// completed phase returns after one test; threads that expect to wait long
+// (sleep_ns > 0) back off between polls so that the barrier unit stays free
+// for the latency-critical MMA thread.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err,
+                                          uint32_t sleep_ns = 0) {
+  if (mbar_test(bar, parity)) return true;
   const long long t0 = clock64();
   while (!mbar_try_wait(bar, parity)) {
+    if (sleep_ns) __nanosleep(sleep_ns);
     if (clock64() - t0 > kWaitCycles) {
       atomicExch(err, 1);
       return false;
@@ -354,7 +373,8 @@ __global__ void __launch_bounds__(Cfg<kTf32>::kThreads, 1)
         tma_load_2d(b_hi + (size_t)c * bchunk, &tb_hi, &bar_b, c * C::kChunkK, slice * NW);
         tma_load_2d(b_lo + (size_t)c * bchunk, &tb_lo, &bar_b, c * C::kChunkK, slice * NW);
       }
-      int it = 0;
+      int it = 0, s = 0;
+      uint32_t ph = 0;  // phase of the current use of stage s
       bool ok = true;
       // prefetch cursor: (pt, pc) runs kPrefetchAhead stages ahead of (t, c)
       int pt = cta_rank, pc = 0;
@@ -369,10 +389,9 @@ __global__ void __launch_bounds__(Cfg<kTf32>::kThreads, 1)
       };
       for (int q = 0; q < kPrefetchAhead; ++q) prefetch_next();
       for (int t = cta_rank; t < mtiles && ok; t += cta_count) {
-        for (int c = 0; c < nk; ++c, ++it) {
-          const int s = it % S, u = it / S;
+        for (int c = 0; c < nk; ++c) {
           prefetch_next();
-          if (u > 0 && !(ok = mbar_wait(&empty_bar[s], (u - 1) & 1, err))) break;
+          if (it >= S && !(ok = mbar_wait(&empty_bar[s], ph ^ 1u, err))) break;
           uint8_t* st = a_base + (size_t)s * sh.a_stage();
           if constexpr (kTf32) {
             mbar_expect_tx(&full_bar[s], kTile);
@@ -382,61 +401,68 @@ __global__ void __launch_bounds__(Cfg<kTf32>::kThreads, 1)
             tma_load_2d(st, &tx_hi, &full_bar[s], c * C::kChunkK, t * kBlockM);
             tma_load_2d(st + kTile, &tx_lo, &full_bar[s], c * C::kChunkK, t * kBlockM);
           }
+          ++it;
+          if (++s == S) {
+            s = 0;
+            ph ^= 1u;
+          }
         }
       }
     }
   } else if (warp == 1) {
     if (lane == 0) {
+      // This single thread paces the whole CTA, so its loop is kept short:
+      // descriptors are formed once and advanced by adding the byte offset
+      // / 16 to their start-address field, stage and phase are counters.
       const uint32_t idesc = instr_desc(kBlockM, NW, kTf32);
       bool ok = mbar_wait(&bar_b, 0, err);
-      int it = 0, tc = 0;
-      const uint32_t bh0 = smem_u32(b_hi), bl0 = smem_u32(b_lo);
+      const uint64_t a0 = smem_desc(smem_u32(a_base));
+      const uint64_t bh0 = smem_desc(smem_u32(b_hi)), bl0 = smem_desc(smem_u32(b_lo));
+      const uint32_t a_step = sh.a_stage() >> 4, b_step = bchunk >> 4, lo_off = kTile >> 4;
+      int s = 0, tc = 0;
+      uint32_t ph = 0;
       for (int t = cta_rank; t < mtiles && ok; t += cta_count, ++tc) {
         const int b = tc & 1, u = tc >> 1;
         if (u > 0 && !(ok = mbar_wait(&acc_empty[b], (u - 1) & 1, err))) break;
         fence_after();
         const uint32_t d = tmem + (uint32_t)(b * set_cols);
-        for (int c = 0; c < nk; ++c, ++it) {
-          const int s = it % S;
-          if (!(ok = mbar_wait(&full_bar[s], (it / S) & 1, err))) break;
+        uint64_t bh = bh0, bl = bl0;
+        for (int c = 0; c < nk; ++c) {
+          // TF32: the converters release a stage only after they saw it land
+          // (full_bar) and wrote its lo tile, so their barrier covers both:
+          // the tensor pipe idles during every test this thread makes
+          ok = mbar_wait(kTf32 ? &cvt_bar[s] : &full_bar[s], ph, err);
+          if (!ok) break;
           fence_after();
-          const uint32_t ab = smem_u32(a_base + (size_t)s * sh.a_stage());
+          const uint64_t ah = a0 + (uint64_t)(s * a_step), al = ah + lo_off;
           // four 32-byte K steps per 128-byte row (16 BF16 or 8 TF32 values)
           if constexpr (kTf32) {
-            // hi products now: hi*hi of the first / second half of K into
-            // its own sum, hi*lo into the small-product sum
-            const int h = c < nk / 2 ? 1 : 2;
+            // hi*hi of the first / second half of K into its own sum; hi*lo
+            // and lo*hi into the small-product sum
+            const uint32_t dh = d + (uint32_t)((c < nk / 2 ? 1 : 2) * NW);
+            const uint32_t acc_h = (c == 0 || c == nk / 2) ? 0u : 1u, acc_l = c == 0 ? 0u : 1u;
 #pragma unroll
             for (int kk = 0; kk < 4; ++kk) {
-              const uint64_t ah = smem_desc(ab + kk * 32);
-              const uint64_t bh = smem_desc(bh0 + c * bchunk + kk * 32);
-              const uint64_t bl = smem_desc(bl0 + c * bchunk + kk * 32);
-              const bool first = (c == 0 || c == nk / 2) && kk == 0;
-              mma<true>(d + (uint32_t)(h * NW), ah, bh, idesc, first ? 0u : 1u);
-              mma<true>(d, ah, bl, idesc, (c | kk) != 0 ? 1u : 0u);
-            }
-            // lo*hi once the converters have written the lo tile
-            if (!(ok = mbar_wait(&cvt_bar[s], (it / S) & 1, err))) break;
-            fence_after();
-#pragma unroll
-            for (int kk = 0; kk < 4; ++kk) {
-              const uint64_t al = smem_desc(ab + kTile + kk * 32);
-              const uint64_t bh = smem_desc(bh0 + c * bchunk + kk * 32);
-              mma<true>(d, al, bh, idesc, 1u);
+              mma<true>(dh, ah + 2 * kk, bh + 2 * kk, idesc, kk ? 1u : acc_h);
+              mma<true>(d, ah + 2 * kk, bl + 2 * kk, idesc, kk ? 1u : acc_l);
+              mma<true>(d, al + 2 * kk, bh + 2 * kk, idesc, 1u);
             }
           } else {
+            const uint32_t acc0 = c == 0 ? 0u : 1u;
 #pragma unroll
             for (int kk = 0; kk < 4; ++kk) {
-              const uint64_t ah = smem_desc(ab + kk * 32);
-              const uint64_t al = smem_desc(ab + kTile + kk * 32);
-              const uint64_t bh = smem_desc(bh0 + c * bchunk + kk * 32);
-              const uint64_t bl = smem_desc(bl0 + c * bchunk + kk * 32);
-              mma<false>(d, al, bh, idesc, (c | kk) != 0 ? 1u : 0u);
-              mma<false>(d, ah, bl, idesc, 1u);
-              mma<false>(d, ah, bh, idesc, 1u);
+              mma<false>(d, al + 2 * kk, bh + 2 * kk, idesc, kk ? 1u : acc0);
+              mma<false>(d, ah + 2 * kk, bl + 2 * kk, idesc, 1u);
+              mma<false>(d, ah + 2 * kk, bh + 2 * kk, idesc, 1u);
             }
           }
           mma_commit(&empty_bar[s]);
+          bh += b_step;
+          bl += b_step;
+          if (++s == S) {
+            s = 0;
+            ph ^= 1u;
+          }
         }
         if (ok) mma_commit(&acc_full[b]);
       }
@@ -451,7 +477,7 @@ __global__ void __launch_bounds__(Cfg<kTf32>::kThreads, 1)
     int tc = 0;
     for (int t = cta_rank; t < mtiles; t += cta_count, ++tc) {
       const int b = tc & 1;
-      if (!mbar_wait(&acc_full[b], (tc >> 1) & 1, err)) break;
+      if (!mbar_wait(&acc_full[b], (tc >> 1) & 1, err, 128)) break;
       __syncwarp();
       fence_after();
       const int m = t * kBlockM + row;
@@ -488,12 +514,12 @@ __global__ void __launch_bounds__(Cfg<kTf32>::kThreads, 1)
   } else if constexpr (kTf32) {
     // converter warps: lo part of every landed FP32 stage
     const int ct = threadIdx.x - 32 * (2 + C::kEpiWarps);
-    int it = 0;
+    int s = 0;
+    uint32_t ph = 0;
     bool ok = true;
     for (int t = cta_rank; t < mtiles && ok; t += cta_count) {
-      for (int c = 0; c < nk; ++c, ++it) {
-        const int s = it % S;
-        if (!(ok = mbar_wait(&full_bar[s], (it / S) & 1, err))) break;
+      for (int c = 0; c < nk; ++c) {
+        if (!(ok = mbar_wait(&full_bar[s], ph, err, 32))) break;
         const float4* hi = reinterpret_cast<const float4*>(a_base + (size_t)s * sh.a_stage());
         float4* lo = reinterpret_cast<float4*>(a_base + (size_t)s * sh.a_stage() + kTile);
         float4 x[kTile / 16 / C::kCvtThreads];
@@ -506,6 +532,10 @@ __global__ void __launch_bounds__(Cfg<kTf32>::kThreads, 1)
         // generic-proxy writes must be visible to the tensor core's reads
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         mbar_arrive(&cvt_bar[s]);
+        if (++s == S) {
+          s = 0;
+          ph ^= 1u;
+        }
       }
     }
   }
