@@ -521,15 +521,28 @@ __global__ void __launch_bounds__(128) k_resid_tri(ResidPass<double> p, const Tr
 }
 
 // solf(1:n1,1:n2,1:n3) = u1 + C, widened exactly and summed in FP64.
-// Grid: x over i (blocks of 256), y = j, z = k.
+// Grid: x over i (blocks of 256), y = j, z strides over k (kPlanes planes
+// per thread, loads issued together).
+constexpr int kPlanes = 8;
 __global__ void k_finalize(const float* __restrict__ u1, const float* __restrict__ c,
                            double* __restrict__ solf, int n1, int n2, int n3) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
   if (i >= n1) return;
-  const long long idx = i + (long long)n1 * (j + (long long)n2 * k);
-  double v = widen(u1[idx]);
-  if (c) v += widen(c[idx]);
-  solf[(i + 1) + (long long)(n1 + 2) * ((j + 1) + (long long)(n2 + 2) * (k + 1))] = v;
+  const long long plane = (long long)n1 * n2, oplane = (long long)(n1 + 2) * (n2 + 2);
+  const long long base = i + (long long)n1 * j;
+  const long long obase = (i + 1) + (long long)(n1 + 2) * (j + 1);
+  for (int k0 = blockIdx.z * kPlanes; k0 < n3; k0 += gridDim.z * kPlanes) {
+    float a[kPlanes], b[kPlanes];
+#pragma unroll
+    for (int q = 0; q < kPlanes; ++q) {
+      const int k = k0 + q;
+      a[q] = k < n3 ? u1[base + plane * k] : 0.f;
+      b[q] = (c && k < n3) ? c[base + plane * k] : 0.f;
+    }
+#pragma unroll
+    for (int q = 0; q < kPlanes; ++q)
+      if (k0 + q < n3) solf[obase + oplane * (k0 + q + 1)] = widen(a[q]) + widen(b[q]);
+  }
 }
 
 // rhs minus the boundary folds, in FP32, split straight into BF16 planes
@@ -545,32 +558,58 @@ struct FoldArgsF {
 };
 
 // Grid: x over i (blocks of 256, P1 <= 256 is a multiple of 64), y = j < P2,
-// z = k < P3.
+// z strides over k (kPlanes planes per thread).  The x- and z-face terms
+// that do not depend on k (inv_lhs_x(i), inv_lhs_y(j), bc_z(i, j)) are
+// loaded once per thread; per point only rhs, bc_x(j, k), bc_y(i, k) and
+// inv_lhs_z(k) are read.
 __global__ void k_fold_split(const double* __restrict__ rhs, FoldArgsF a, __nv_bfloat16* hi,
                              __nv_bfloat16* lo, float* x32, int n1, int n2, int n3, int P1, int P2,
                              int P3) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
   if (i >= P1) return;
-  const long long idx = i + (long long)P1 * (j + (long long)P2 * k);
-  float v = 0.f;
-  if (i < n1 && j < n2 && k < n3) {
-    v = narrow(rhs[i + (long long)n1 * (j + (long long)n2 * k)]);
-    const long long fx = j + (long long)n2 * k, fy = i + (long long)n1 * k, fz = i + (long long)n1 * j;
-    const long long sx = (long long)n2 * n3, sy = (long long)n1 * n3, sz = (long long)n1 * n2;
+  const bool in_ij = i < n1 && j < n2;
+  const long long sx = (long long)n2 * n3, sy = (long long)n1 * n3, sz = (long long)n1 * n2;
+  float cx[4] = {0.f, 0.f, 0.f, 0.f}, cy[4] = {0.f, 0.f, 0.f, 0.f}, fz[4] = {0.f, 0.f, 0.f, 0.f};
+  if (in_ij) {
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
-      v -= a.ix[c][i] * a.bx[c * sx + fx];
-      v -= a.iy[c][j] * a.by[c * sy + fy];
-      v -= a.iz[c][k] * a.bz[c * sz + fz];
+      cx[c] = a.ix[c][i];
+      cy[c] = a.iy[c][j];
+      fz[c] = a.bz[c * sz + i + (long long)n1 * j];
     }
   }
-  if (x32) {
-    x32[idx] = v;
-    return;
+  for (int k0 = blockIdx.z * kPlanes; k0 < P3; k0 += gridDim.z * kPlanes) {
+    double r[kPlanes];
+#pragma unroll
+    for (int q = 0; q < kPlanes; ++q) {
+      const int k = k0 + q;
+      r[q] = (in_ij && k < n3) ? rhs[i + (long long)n1 * (j + (long long)n2 * k)] : 0.0;
+    }
+#pragma unroll
+    for (int q = 0; q < kPlanes; ++q) {
+      const int k = k0 + q;
+      if (k >= P3) break;
+      float v = 0.f;
+      if (in_ij && k < n3) {
+        v = narrow(r[q]);
+        const long long fx = j + (long long)n2 * k, fy = i + (long long)n1 * k;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          v -= cx[c] * a.bx[c * sx + fx];
+          v -= cy[c] * a.by[c * sy + fy];
+          v -= a.iz[c][k] * fz[c];
+        }
+      }
+      const long long idx = i + (long long)P1 * (j + (long long)P2 * k);
+      if (x32) {
+        x32[idx] = v;
+      } else {
+        const __nv_bfloat16 h = __float2bfloat16_rn(v);
+        hi[idx] = h;
+        lo[idx] = __float2bfloat16_rn(v - __bfloat162float(h));
+      }
+    }
   }
-  const __nv_bfloat16 h = __float2bfloat16_rn(v);
-  hi[idx] = h;
-  lo[idx] = __float2bfloat16_rn(v - __bfloat162float(h));
 }
 
 // c * bc face products of the fold, in FP32: out[c][face point].
@@ -1058,7 +1097,7 @@ static int fold_split(mf_solver3d* sc, bool tf32, const double* rhs, const doubl
   args.bx = fa[0];
   args.by = fa[1];
   args.bz = fa[2];
-  k_fold_split<<<dim3(blocks_for(sc->P[0], 256), sc->P[1], sc->P[2]), 256, 0, st>>>(
+  k_fold_split<<<dim3(blocks_for(sc->P[0], 256), sc->P[1], 4), 256, 0, st>>>(
       rhs, args, tf32 ? nullptr : sc->Xa_hi.as<__nv_bfloat16>(),
       tf32 ? nullptr : sc->Xa_lo.as<__nv_bfloat16>(), tf32 ? sc->Xa32.as<float>() : nullptr,
       (int)n1, (int)n2, (int)n3, sc->P[0], sc->P[1], sc->P[2]);
@@ -1112,8 +1151,8 @@ static int solve_mixed_dev(mf_solver3d* sc, const double* rhs, double sigma, dou
     if ((rc = approx_solve(sc, tf32, sigma, C, it > 0, st))) return rc;
   }
   sc->prof.begin(kProfCopy, st);
-  k_finalize<<<dim3(blocks_for(n1, 256), n2, n3), 256, 0, st>>>(u1, refine > 0 ? C : nullptr, solf, n1,
-                                                                n2, n3);
+  k_finalize<<<dim3(blocks_for(n1, 256), n2, 4), 256, 0, st>>>(u1, refine > 0 ? C : nullptr, solf, n1,
+                                                               n2, n3);
   sc->prof.end(st);
   MF_CUDA(cudaGetLastError());
   return faces(sc, solf, bcs, st);

@@ -7,8 +7,11 @@
 //  * split-BF16 (kind::f16): X is stored as two BF16 planes, B likewise;
 //  * 3xTF32 (kind::tf32): X is stored as FP32.  The tensor core reads an FP32
 //    operand as TF32 by ignoring its 13 low mantissa bits, so the landed
-//    tile itself is the hi part, trunc(x); converter warps write the lo part
-//    rna_tf32(x - trunc(x)) beside it.  B is stored as two TF32-rounded FP32
+//    tile itself is the hi part, trunc(x); converter warps copy it and the
+//    lo part rna_tf32(x - trunc(x)) into TMEM, where all three MMAs read
+//    their A operand, so that shared memory serves only B and the landed
+//    tiles (an MMA reading both operands from shared memory is bound by
+//    its 128 bytes per cycle).  B is stored as two TF32-rounded FP32
 //    planes.  Each 128-byte swizzle row holds 32 K values instead of 64, and
 //    the split keeps ~21 bits of every operand instead of ~16, which lets
 //    one refinement step reach 1e-10.
@@ -26,9 +29,10 @@
 //    running sum and the error grows with the number of MMAs accumulated
 //    into one sum: the small products hi*lo + lo*hi, and hi*hi over the
 //    first and over the second half of K, are summed by the epilogue;
-//  * (3xTF32 only) 4 converter warps write the lo part of each landed FP32
-//    stage; the MMA warp issues the two products with the hi part as soon
-//    as the stage lands and the lo product once the converters release it;
+//  * (3xTF32 only) 4 converter warps copy each landed FP32 stage (hi and lo
+//    parts) into one of kOpSlots TMEM operand slots and release the ring
+//    stage; the MMA thread issues up to kOpSlots converted stages per
+//    barrier test;
 //  * the epilogue warps (8 for BF16, 4 for TF32) drain the accumulator with
 //    tcgen05.ld (warp w owns TMEM lanes 32*(w%4)..+31) and run the fused
 //    epilogue:
@@ -202,6 +206,39 @@ __device__ __forceinline__ float tf32_lo(float x) {
   return tf32_rna(x - __uint_as_float(__float_as_uint(x) & 0xFFFFE000u));
 }
 
+// kind::tf32 MMA with the A operand in TMEM (M = 128 lanes, one 32-bit
+// column per K value) and B from shared memory.
+__device__ __forceinline__ void mma_tf32_ta(uint32_t d_tmem, uint32_t a_tmem, uint64_t b,
+                                            uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+      "r"(a_tmem), "l"(b), "r"(idesc), "r"(accumulate));
+}
+
+// Stores 32 consecutive 32-bit TMEM columns of this thread's lane (warp
+// collective; a warp reaches the lane quarter 32*(warp%4)..+31 only).
+__device__ __forceinline__ void tmem_store32(uint32_t taddr, const float* v) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], "
+      "{%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,"
+      "%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32};" ::"r"(taddr),
+      "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
+      "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])),
+      "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7])), "r"(__float_as_uint(v[8])),
+      "r"(__float_as_uint(v[9])), "r"(__float_as_uint(v[10])), "r"(__float_as_uint(v[11])),
+      "r"(__float_as_uint(v[12])), "r"(__float_as_uint(v[13])), "r"(__float_as_uint(v[14])),
+      "r"(__float_as_uint(v[15])), "r"(__float_as_uint(v[16])), "r"(__float_as_uint(v[17])),
+      "r"(__float_as_uint(v[18])), "r"(__float_as_uint(v[19])), "r"(__float_as_uint(v[20])),
+      "r"(__float_as_uint(v[21])), "r"(__float_as_uint(v[22])), "r"(__float_as_uint(v[23])),
+      "r"(__float_as_uint(v[24])), "r"(__float_as_uint(v[25])), "r"(__float_as_uint(v[26])),
+      "r"(__float_as_uint(v[27])), "r"(__float_as_uint(v[28])), "r"(__float_as_uint(v[29])),
+      "r"(__float_as_uint(v[30])), "r"(__float_as_uint(v[31]))
+      : "memory");
+  asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+}
+
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
   asm volatile(
       "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
@@ -237,20 +274,28 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
-constexpr int kMaxStages = 4;
+constexpr int kMaxStages = 8;
+// 3xTF32: the A operand (hi and lo parts) lives in TMEM, where the tensor
+// core reads it without using shared-memory bandwidth; operand slots of
+// 64 columns (hi at +0, lo at +32) follow the two accumulator sets
+// (2 x 3 x 64 = 384 columns).  Shared memory then carries only the landed
+// tiles and B: an MMA that reads A and B from shared memory is bound by
+// its 128 bytes per cycle.
+constexpr int kOpSlots = 2;
+constexpr uint32_t kOpCol = 384;
 // Stages whose A boxes are prefetched into L2 ahead of their shared-memory
 // load.  A load that misses L2 takes ~2 us on a busy GB300, several times
 // the time the tensor cores need for the stages that fit in the ring.
 constexpr int kPrefetchAhead = 8;
 
-// Shared-memory plan of one launch (host and device agree on it).  A stage
-// holds two 128 x 128-byte tiles: the hi and lo BF16 planes, or the FP32
-// tile (hi after conversion) and its lo part.
+// Shared-memory plan of one launch (host and device agree on it).  A BF16
+// stage holds two 128 x 128-byte tiles (the hi and lo planes), a 3xTF32
+// stage one (the FP32 tile; its lo part goes to TMEM).
 struct TcShape {
-  int NS, NW, nk, stages;
+  int NS, NW, nk, stages, tiles;  // tiles: 128 x 128-byte tiles per stage
   __host__ __device__ uint32_t b_chunk() const { return (uint32_t)NW * 128; }
   __host__ __device__ uint32_t b_bytes() const { return 2u * nk * b_chunk(); }
-  __host__ __device__ uint32_t a_stage() const { return 2u * kBlockM * 128; }
+  __host__ __device__ uint32_t a_stage() const { return (uint32_t)tiles * kBlockM * 128; }
   __host__ __device__ uint32_t smem() const { return b_bytes() + stages * a_stage() + 1024; }
 };
 
@@ -312,8 +357,8 @@ __global__ void __launch_bounds__(Cfg<kTf32>::kThreads, 1)
                    int M, TcShape sh, TcEpilogue e, int* err) {
   using C = Cfg<kTf32>;
   extern __shared__ uint8_t smem_raw[];
-  __shared__ uint64_t bar_b, full_bar[kMaxStages], cvt_bar[kMaxStages], empty_bar[kMaxStages],
-      acc_full[2], acc_empty[2];
+  __shared__ uint64_t bar_b, full_bar[kMaxStages], empty_bar[kMaxStages], acc_full[2], acc_empty[2];
+  __shared__ uint64_t cvt_bar[kOpSlots], op_free[kOpSlots];  // 3xTF32 operand slots in TMEM
   __shared__ uint32_t tmem_slot;
   __shared__ float s_lz[256];     // z eigenvalues (divide epilogue)
   __shared__ uint8_t s_nz[256];   // z null-mode flags
@@ -339,8 +384,13 @@ __global__ void __launch_bounds__(Cfg<kTf32>::kThreads, 1)
     mbar_init(&bar_b, 1);
     for (int s = 0; s < S; ++s) {
       mbar_init(&full_bar[s], 1);
-      mbar_init(&cvt_bar[s], kTf32 ? C::kCvtThreads : 1);
-      mbar_init(&empty_bar[s], 1);
+      // released by the MMA commit (BF16) or by the converters once they
+      // have read the stage (3xTF32)
+      mbar_init(&empty_bar[s], kTf32 ? C::kCvtThreads : 1);
+    }
+    for (int o = 0; o < kOpSlots; ++o) {
+      mbar_init(&cvt_bar[o], C::kCvtThreads > 0 ? C::kCvtThreads : 1);
+      mbar_init(&op_free[o], 1);
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&acc_full[b], 1);
@@ -419,35 +469,50 @@ __global__ void __launch_bounds__(Cfg<kTf32>::kThreads, 1)
       const uint64_t a0 = smem_desc(smem_u32(a_base));
       const uint64_t bh0 = smem_desc(smem_u32(b_hi)), bl0 = smem_desc(smem_u32(b_lo));
       const uint32_t a_step = sh.a_stage() >> 4, b_step = bchunk >> 4, lo_off = kTile >> 4;
-      int s = 0, tc = 0;
-      uint32_t ph = 0;
+      int s = 0, o = 0, tc = 0;
+      uint32_t ph = 0, pho = 0;  // phases of ring stage s (BF16) and TMEM operand slot o (TF32)
       for (int t = cta_rank; t < mtiles && ok; t += cta_count, ++tc) {
         const int b = tc & 1, u = tc >> 1;
         if (u > 0 && !(ok = mbar_wait(&acc_empty[b], (u - 1) & 1, err))) break;
         fence_after();
         const uint32_t d = tmem + (uint32_t)(b * set_cols);
-        uint64_t bh = bh0, bl = bl0;
-        for (int c = 0; c < nk; ++c) {
-          // TF32: the converters release a stage only after they saw it land
-          // (full_bar) and wrote its lo tile, so their barrier covers both:
-          // the tensor pipe idles during every test this thread makes
-          ok = mbar_wait(kTf32 ? &cvt_bar[s] : &full_bar[s], ph, err);
-          if (!ok) break;
-          fence_after();
-          const uint64_t ah = a0 + (uint64_t)(s * a_step), al = ah + lo_off;
-          // four 32-byte K steps per 128-byte row (16 BF16 or 8 TF32 values)
-          if constexpr (kTf32) {
-            // hi*hi of the first / second half of K into its own sum; hi*lo
-            // and lo*hi into the small-product sum
-            const uint32_t dh = d + (uint32_t)((c < nk / 2 ? 1 : 2) * NW);
-            const uint32_t acc_h = (c == 0 || c == nk / 2) ? 0u : 1u, acc_l = c == 0 ? 0u : 1u;
+        if constexpr (kTf32) {
+          // Up to kOpSlots converted stages per barrier test: the converters
+          // finish stages in order, so a converted later stage implies the
+          // earlier one, and the tensor pipe (idle while this thread tests
+          // a barrier) gets the MMAs of both in a row.
+          for (int c = 0; c < nk && ok;) {
+            int m = min(kOpSlots, nk - c);
+            if (m == 2 && !mbar_test(&cvt_bar[o ^ 1], pho ^ (o == 1 ? 1u : 0u))) m = 1;
+            if (m == 1 && !(ok = mbar_wait(&cvt_bar[o], pho, err))) break;
+            fence_after();
+            for (int q = 0; q < m; ++q, ++c) {
+              const uint64_t bh = bh0 + (uint64_t)(c * b_step), bl = bl0 + (uint64_t)(c * b_step);
+              const uint32_t ahi = tmem + kOpCol + (uint32_t)(64 * o), alo = ahi + 32;
+              // hi*hi of the first / second half of K into its own sum; hi*lo
+              // and lo*hi into the small-product sum
+              const uint32_t dh = d + (uint32_t)((c < nk / 2 ? 1 : 2) * NW);
+              const uint32_t acc_h = (c == 0 || c == nk / 2) ? 0u : 1u, acc_l = c == 0 ? 0u : 1u;
 #pragma unroll
-            for (int kk = 0; kk < 4; ++kk) {
-              mma<true>(dh, ah + 2 * kk, bh + 2 * kk, idesc, kk ? 1u : acc_h);
-              mma<true>(d, ah + 2 * kk, bl + 2 * kk, idesc, kk ? 1u : acc_l);
-              mma<true>(d, al + 2 * kk, bh + 2 * kk, idesc, 1u);
+              for (int kk = 0; kk < 4; ++kk) {
+                mma_tf32_ta(dh, ahi + 8 * kk, bh + 2 * kk, idesc, kk ? 1u : acc_h);
+                mma_tf32_ta(d, ahi + 8 * kk, bl + 2 * kk, idesc, kk ? 1u : acc_l);
+                mma_tf32_ta(d, alo + 8 * kk, bh + 2 * kk, idesc, 1u);
+              }
+              mma_commit(&op_free[o]);
+              if (++o == kOpSlots) {
+                o = 0;
+                pho ^= 1u;
+              }
             }
-          } else {
+          }
+        } else {
+          uint64_t bh = bh0, bl = bl0;
+          for (int c = 0; c < nk; ++c) {
+            if (!(ok = mbar_wait(&full_bar[s], ph, err))) break;
+            fence_after();
+            const uint64_t ah = a0 + (uint64_t)(s * a_step), al = ah + lo_off;
+            // four 32-byte K steps (16 BF16 values) per 128-byte row
             const uint32_t acc0 = c == 0 ? 0u : 1u;
 #pragma unroll
             for (int kk = 0; kk < 4; ++kk) {
@@ -455,13 +520,13 @@ __global__ void __launch_bounds__(Cfg<kTf32>::kThreads, 1)
               mma<false>(d, ah + 2 * kk, bl + 2 * kk, idesc, 1u);
               mma<false>(d, ah + 2 * kk, bh + 2 * kk, idesc, 1u);
             }
-          }
-          mma_commit(&empty_bar[s]);
-          bh += b_step;
-          bl += b_step;
-          if (++s == S) {
-            s = 0;
-            ph ^= 1u;
+            mma_commit(&empty_bar[s]);
+            bh += b_step;
+            bl += b_step;
+            if (++s == S) {
+              s = 0;
+              ph ^= 1u;
+            }
           }
         }
         if (ok) mma_commit(&acc_full[b]);
@@ -512,29 +577,51 @@ __global__ void __launch_bounds__(Cfg<kTf32>::kThreads, 1)
       mbar_arrive(&acc_empty[b]);
     }
   } else if constexpr (kTf32) {
-    // converter warps: lo part of every landed FP32 stage
-    const int ct = threadIdx.x - 32 * (2 + C::kEpiWarps);
-    int s = 0;
-    uint32_t ph = 0;
+    // Converter warps: every landed FP32 stage goes to a TMEM operand slot,
+    // one tile row per thread: hi = the FP32 bits (read as TF32, i.e.
+    // truncated, by the tensor core) and lo = rna_tf32(x - trunc(x)).  A
+    // warp reaches only its TMEM lane quarter, so warp w converts rows
+    // 32*(w%4)..+31.  The tile has the 128-byte swizzle: 16-byte chunk j of
+    // row r sits at chunk position j ^ (r % 8).  The ring stage is released
+    // as soon as it has been read.
+    const int row = 32 * (warp & 3) + lane;
+    const uint32_t lane_base = static_cast<uint32_t>(32 * (warp & 3)) << 16;
+    int s = 0, o = 0, it = 0;
+    uint32_t ph = 0, pho = 0;
     bool ok = true;
     for (int t = cta_rank; t < mtiles && ok; t += cta_count) {
-      for (int c = 0; c < nk; ++c) {
+      for (int c = 0; c < nk; ++c, ++it) {
         if (!(ok = mbar_wait(&full_bar[s], ph, err, 32))) break;
-        const float4* hi = reinterpret_cast<const float4*>(a_base + (size_t)s * sh.a_stage());
-        float4* lo = reinterpret_cast<float4*>(a_base + (size_t)s * sh.a_stage() + kTile);
-        float4 x[kTile / 16 / C::kCvtThreads];
+        const float4* rowp =
+            reinterpret_cast<const float4*>(a_base + (size_t)s * sh.a_stage() + (size_t)row * 128);
+        float hi[32], lo[32];
 #pragma unroll
-        for (int v = 0; v < (int)(kTile / 16 / C::kCvtThreads); ++v) x[v] = hi[ct + v * C::kCvtThreads];
-#pragma unroll
-        for (int v = 0; v < (int)(kTile / 16 / C::kCvtThreads); ++v)
-          lo[ct + v * C::kCvtThreads] =
-              make_float4(tf32_lo(x[v].x), tf32_lo(x[v].y), tf32_lo(x[v].z), tf32_lo(x[v].w));
-        // generic-proxy writes must be visible to the tensor core's reads
+        for (int j = 0; j < 8; ++j) {
+          const float4 x = rowp[j ^ (row & 7)];
+          hi[4 * j + 0] = x.x;
+          hi[4 * j + 1] = x.y;
+          hi[4 * j + 2] = x.z;
+          hi[4 * j + 3] = x.w;
+        }
+        // reads done: the ring stage may be refilled by TMA
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        mbar_arrive(&cvt_bar[s]);
+        mbar_arrive(&empty_bar[s]);
+#pragma unroll
+        for (int q = 0; q < 32; ++q) lo[q] = tf32_lo(hi[q]);
+        // the operand slot is free once the MMAs of its previous stage completed
+        if (it >= kOpSlots && !(ok = mbar_wait(&op_free[o], pho ^ 1u, err, 32))) break;
+        const uint32_t slot = tmem + lane_base + kOpCol + (uint32_t)(64 * o);
+        tmem_store32(slot, hi);
+        tmem_store32(slot + 32, lo);
+        fence_before();
+        mbar_arrive(&cvt_bar[o]);
         if (++s == S) {
           s = 0;
           ph ^= 1u;
+        }
+        if (++o == kOpSlots) {
+          o = 0;
+          pho ^= 1u;
         }
       }
     }
@@ -592,6 +679,7 @@ static TcShape shape_for(int N, int K, bool tf32) {
     sh.NS = N >= 128 ? 2 : 1;
   sh.NW = N / sh.NS;
   sh.nk = K / (tf32 ? 32 : 64);
+  sh.tiles = tf32 ? 1 : 2;
   const uint32_t budget = 224 * 1024;
   const uint32_t left = sh.b_bytes() < budget ? budget - sh.b_bytes() : 0;
   sh.stages = (int)std::min<uint32_t>(kMaxStages, left / sh.a_stage());
