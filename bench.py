@@ -263,6 +263,14 @@ def run_gb300(args, rank, world, dist):
     def mixed(r=None):
         sc.solve_3d(d_rhs, 0.0, d_solf, *d_bc, precision=prec, refine=refine if r is None else r)
 
+    # the same solve with double-FP32 sweeps in the refinement residual, for reference
+    sc.set_residual(mf.MF_RESID_FF)
+    for _ in range(3):
+        mixed()
+    resid_ff = {"ms_per_solve": statistics.median(timed(mixed, 5))}
+    resid_ff["rel_l2_vs_fp64_gpu"] = err_vs_plain()
+    sc.set_residual(mf.MF_RESID_FP64)
+
     for _ in range(max(args.warmup, 3)):
         mixed()
     torch.cuda.synchronize()
@@ -379,6 +387,7 @@ def run_gb300(args, rank, world, dist):
         "accuracy": {"rel_l2_vs_fp64_gpu": final_err, "rel_l2_vs_cpu_oracle": oracle_err,
                      "fp64_gpu_vs_cpu_oracle": plain_vs_oracle,
                      "rel_l2_by_refine_steps": {str(k): v for k, v in errs.items()}},
+        "residual_double_fp32_sweeps": resid_ff,
         "formats": {k: {"precision": names[k], "refine_steps": c["refine"],
                         "ms_per_solve": c["ms"], "solves_per_s": 1e3 / c["ms"],
                         "rel_l2_by_refine_steps": {str(r): v for r, v in c["errs"].items()}}

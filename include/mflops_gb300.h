@@ -42,6 +42,13 @@ extern "C" {
 #define MF_PREC_SPLIT_BF16 1  /* split-BF16 three-product on tcgen05, FP32 accum.  */
 #define MF_PREC_3XTF32 2      /* 3xTF32 on tcgen05, FP32 accumulation              */
 
+/* Arithmetic of the FP64-accurate refinement residual of the mixed path
+ * (tridiagonal second-derivative operators): FP64 sweeps (default) or
+ * double-FP32 throughout (error-free products and sums on the FP32 pipe).
+ * Both evaluate the cancelling stencil sums in moment form. */
+#define MF_RESID_FF 0
+#define MF_RESID_FP64 1
+
 const char* mf_last_error(void);
 int mf_version(void);
 /* 1 when a CUDA device is usable from this process, else 0. */
@@ -174,6 +181,9 @@ int mf_solver3d_set_eigen(mf_solver3d_t* sc, int axis, const double* eigen, cons
 
 /* Reads and clears the device-side error flag of the tensor-core pipeline
  * (MF_ERR_TIMEOUT if a bounded wait expired since the last call). Syncs. */
+/* Selects the residual arithmetic (MF_RESID_FF or MF_RESID_FP64) used by the
+ * mixed solves of this handle; no counterpart in the reference. */
+int mf_solver3d_set_residual(mf_solver3d_t* sc, int mode);
 int mf_solver3d_device_status(mf_solver3d_t* sc);
 
 /* Per-kernel CUDA-event timers of a solver handle (stage timers in the

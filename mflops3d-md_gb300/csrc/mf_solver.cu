@@ -69,6 +69,7 @@ struct mf_solver3d {
   TcPlan* plan[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   TcPlan* plan32[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   bool mixed_ready = false, mixed32_ready = false;
+  int resid_mode = MF_RESID_FP64;             // residual arithmetic of the mixed path
   StageProfiler prof;
 };
 
@@ -352,14 +353,78 @@ struct TriRow {
   double ft, dt;       // f_i c_{i-1} / c_i,  d_i / c_i
   double cbc;          // boundary coefficient / c_i (rows 0, 1, n-2, n-1)
   double pad;
+  float fth, ftl, dth, dtl, cbh, cbl;  // ft, dt, cbc as hi + lo floats
+  float pad2[2];
 };
-static_assert(sizeof(TriRow) == 96, "TriRow layout");
+static_assert(sizeof(TriRow) == 128, "TriRow layout");
 
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
   s = a + b;
   const float bb = s - a;
   e = (a - (s - bb)) + (b - bb);
 }
+
+// ---- double-FP32 ("float-float") arithmetic: a value is h + l with
+// |l| <= ulp(h)/2; sums by TwoSum, products by the FMA error term
+// (Dekker, Knuth).  About 2^-48 relative rounding per operation.
+struct FF {
+  float h, l;
+};
+
+__device__ __forceinline__ FF ff_norm(float s, float e) {  // |s| >= |e|
+  const float h = s + e;
+  return {h, e - (h - s)};
+}
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+  float s, e;
+  two_sum(a.h, b.h, s, e);
+  return ff_norm(s, e + (a.l + b.l));
+}
+__device__ __forceinline__ FF ff_neg(FF a) { return {-a.h, -a.l}; }
+__device__ __forceinline__ FF ff_mul(FF a, FF b) {
+  const float p = a.h * b.h;
+  float e = fmaf(a.h, b.h, -p);
+  e = fmaf(a.h, b.l, e);
+  e = fmaf(a.l, b.h, e);
+  return ff_norm(p, e);
+}
+__device__ __forceinline__ FF ff_mul_f(FF a, float b) {
+  const float p = a.h * b;
+  float e = fmaf(a.h, b, -p);
+  e = fmaf(a.l, b, e);
+  return ff_norm(p, e);
+}
+__device__ __forceinline__ float ff_to_float(FF a) { return a.h + a.l; }
+
+// 2^k as a float for -126 <= k <= 127 (0 below, infinity above).
+__device__ __forceinline__ float pow2f(int k) {
+  if (k < -126) return 0.f;
+  if (k > 127) return __uint_as_float(0x7F800000u);
+  return __uint_as_float((uint32_t)(k + 127) << 23);
+}
+
+// Exact split of a double into h + l with integer operations: h holds the
+// leading 24 mantissa bits (rounded), l the signed remainder (rounded to
+// 24 bits, so the pair carries ~48 bits).  Values outside the normal FP32
+// range flush to zero.
+__device__ __forceinline__ FF ff_from_double(double d) {
+  const uint64_t b = (uint64_t)__double_as_longlong(d);
+  const int e = (int)((b >> 52) & 0x7FF);
+  if (e == 0) return {0.f, 0.f};
+  const uint64_t m = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+  const uint32_t hm = (uint32_t)((m + (1ull << 28)) >> 29);      // <= 2^24
+  const long long rem = (long long)m - ((long long)hm << 29);    // |rem| <= 2^28
+  const float sc = pow2f(e - 1075);                               // 2^(e - 1023 - 52)
+  float h = __uint2float_rn(hm) * (sc * 536870912.f);             // 2^29
+  float l = __int2float_rn((int)rem) * sc;
+  if (b >> 63) {
+    h = -h;
+    l = -l;
+  }
+  return {h, l};
+}
+
+
 
 // sum_{m < W, m != skip} (wh + wl)_m (v_m - ref) + rho ref, as FP64.
 template <int W>
@@ -518,6 +583,231 @@ __global__ void __launch_bounds__(128) k_resid_tri(ResidPass<double> p, const Tr
   fin.pstride = p.pstride;
   fin.r32 = r32 ? r32 + base : nullptr;
   solve_line_tri(R, p.n, u + base, scratch + base, p.s, blo, bhi, fin);
+}
+
+// ---- the same residual entirely on the FP32 pipe (double-float sweeps)
+//
+// The moment-form stencil sum is kept as a float pair, and the two sweeps
+// and the final combination run in double-float arithmetic; intermediate
+// arrays between the passes are float pairs (8 bytes, like FP64).  The
+// sweeps are well conditioned (|ft|, |dt| < 1), so ~2^-48 relative rounding
+// per operation gives a residual as accurate as the FP64 evaluation, which
+// on GB300 would be bound by the FP64 pipe (1/57 of FP32).
+
+template <int W>
+__device__ __forceinline__ FF moment_sum_ff(const TriRow& r, const float (&v)[W], float ref, int skip) {
+  float h = 0.f, l = 0.f;
+#pragma unroll
+  for (int m = 0; m < W; ++m) {
+    if (m == skip) continue;
+    float dh, dl;
+    two_sum(v[m], -ref, dh, dl);
+    const float ph = r.wh[m] * dh;
+    float pl = fmaf(r.wh[m], dh, -ph);
+    pl = fmaf(r.wh[m], dl, pl);
+    pl = fmaf(r.wl[m], dh, pl);
+    float sh, se;
+    two_sum(h, ph, sh, se);
+    h = sh;
+    l += se + pl;
+  }
+  const float ph = r.rh * ref;
+  float pl = fmaf(r.rh, ref, -ph);
+  pl = fmaf(r.rl, ref, pl);
+  float sh, se;
+  two_sum(h, ph, sh, se);
+  return ff_norm(sh, l + se + pl);
+}
+
+// cbc~ (bc - u_i) for a boundary row, bc an FP64 value.
+__device__ __forceinline__ FF bc_term_ff(const TriRow& r, double bc, float ui) {
+  return ff_mul({r.cbh, r.cbl}, ff_add(ff_from_double(bc), {-ui, 0.f}));
+}
+
+__device__ __forceinline__ FF ff_of(float2 v) { return {v.x, v.y}; }
+__device__ __forceinline__ float2 f2_of(FF v) { return make_float2(v.h, v.l); }
+
+// Final combination of one row (see ResidFin for the modes).
+struct FinFF {
+  int mode;
+  FF sigma;
+  float2* out;         // modes 0, 1: float-pair result, offset to the line
+  __nv_bfloat16* hi;   // modes 2, 3: operand planes / FP32 operand, padded offsets
+  __nv_bfloat16* lo;
+  float* x32;
+  long long pstride;
+  float* r32;          // mode 3
+  __device__ __forceinline__ void put(int i, long long idx, FF y, FF r, float u) const {
+    if (mode == 0) r = ff_add(r, ff_neg(ff_mul_f(sigma, u)));
+    const FF v = ff_add(r, ff_neg(y));
+    if (mode <= 1) {
+      out[idx] = f2_of(v);
+      return;
+    }
+    const float f = ff_to_float(v);
+    if (x32) {
+      x32[i * pstride] = f;
+    } else {
+      const __nv_bfloat16 h = __float2bfloat16_rn(f);
+      hi[i * pstride] = h;
+      lo[i * pstride] = __float2bfloat16_rn(f - __bfloat162float(h));
+    }
+    if (mode == 3) r32[idx] = f;
+  }
+};
+
+template <bool kRinDouble>
+__device__ __forceinline__ FF load_rin(const double* rd, const float2* rf, long long o) {
+  if constexpr (kRinDouble)
+    return ff_from_double(rd[o]);
+  else
+    return ff_of(rf[o]);
+}
+
+template <bool kRinDouble>
+__device__ __forceinline__ void solve_line_ff(const TriRow* __restrict__ R, int n, const float* u,
+                                              const double* rind, const float2* rinf, float2* xs,
+                                              long long s, double lo, double hi, const FinFF& fin) {
+  float f[7], g[7];
+#pragma unroll
+  for (int m = 0; m < 7; ++m) {
+    f[m] = u[(long long)m * s];
+    g[m] = u[(long long)(n - 7 + m) * s];
+  }
+  // rows 0 and 1: 7-wide stencils on u_0..u_6, boundary value lo
+  const FF x0 = ff_add(moment_sum_ff<7>(R[0], f, f[0], 0), bc_term_ff(R[0], lo, f[0]));
+  const FF x1 = ff_add(ff_add(moment_sum_ff<7>(R[1], f, f[1], 1), bc_term_ff(R[1], lo, f[1])),
+                       ff_neg(ff_mul({R[1].fth, R[1].ftl}, x0)));
+  xs[0] = f2_of(x0);
+  xs[s] = f2_of(x1);
+  FF xm = x1;
+  float w[5] = {f[0], f[1], f[2], f[3], f[4]};
+  float pf[kAhead];
+#pragma unroll
+  for (int k = 0; k < kAhead; ++k) pf[k] = (5 + k < n) ? u[(long long)(5 + k) * s] : 0.f;
+  int i = 2;
+  for (; i + kAhead <= n - 2; i += kAhead) {
+    float nb[kAhead];
+#pragma unroll
+    for (int k = 0; k < kAhead; ++k) {
+      const int j = i + 3 + kAhead + k;
+      nb[k] = (j < n) ? u[(long long)j * s] : 0.f;
+    }
+#pragma unroll
+    for (int k = 0; k < kAhead; ++k) {
+      const TriRow& r = R[i + k];
+      const FF x = ff_add(moment_sum_ff<5>(r, w, w[2], 2), ff_neg(ff_mul({r.fth, r.ftl}, xm)));
+      xs[(long long)(i + k) * s] = f2_of(x);
+      xm = x;
+      w[0] = w[1]; w[1] = w[2]; w[2] = w[3]; w[3] = w[4]; w[4] = pf[k];
+    }
+#pragma unroll
+    for (int k = 0; k < kAhead; ++k) pf[k] = nb[k];
+  }
+  for (; i < n - 2; ++i) {
+    const TriRow& r = R[i];
+    const FF x = ff_add(moment_sum_ff<5>(r, w, w[2], 2), ff_neg(ff_mul({r.fth, r.ftl}, xm)));
+    xs[(long long)i * s] = f2_of(x);
+    xm = x;
+    w[0] = w[1]; w[1] = w[2]; w[2] = w[3]; w[3] = w[4];
+    if (i + 3 < n) w[4] = u[(long long)(i + 3) * s];
+  }
+  // rows n-2 and n-1: 7-wide stencils on u_{n-7}..u_{n-1}, boundary value hi
+  const TriRow& rA = R[n - 2];
+  const TriRow& rB = R[n - 1];
+  const FF xA = ff_add(ff_add(moment_sum_ff<7>(rA, g, g[5], 5), bc_term_ff(rA, hi, g[5])),
+                       ff_neg(ff_mul({rA.fth, rA.ftl}, xm)));
+  const FF xB = ff_add(ff_add(moment_sum_ff<7>(rB, g, g[6], 6), bc_term_ff(rB, hi, g[6])),
+                       ff_neg(ff_mul({rB.fth, rB.ftl}, xA)));
+  // back substitution with the final combination of each row; the forward
+  // value, rin and (first pass) u of row i - k are loaded kAhead rows ahead
+  const bool need_u = fin.mode == 0;
+  auto uval = [&](long long o) { return need_u ? u[o] : 0.f; };
+  FF y1 = xB;
+  {
+    const long long o = (long long)(n - 1) * s;
+    fin.put(n - 1, o, xB, load_rin<kRinDouble>(rind, rinf, o), uval(o));
+  }
+  FF y = ff_add(xA, ff_neg(ff_mul({rA.dth, rA.dtl}, y1)));
+  {
+    const long long o = (long long)(n - 2) * s;
+    fin.put(n - 2, o, y, load_rin<kRinDouble>(rind, rinf, o), uval(o));
+  }
+  y1 = y;
+  i = n - 3;
+  float2 rb[kAhead];
+  FF rr[kAhead];
+  float ru[kAhead];
+#pragma unroll
+  for (int k = 0; k < kAhead; ++k) {
+    const bool in = i - k >= 0;
+    const long long o = (long long)(i - k) * s;
+    rb[k] = in ? xs[o] : make_float2(0.f, 0.f);
+    rr[k] = in ? load_rin<kRinDouble>(rind, rinf, o) : FF{0.f, 0.f};
+    ru[k] = (in && need_u) ? u[o] : 0.f;
+  }
+  for (; i - (kAhead - 1) >= 0; i -= kAhead) {
+    float2 nb[kAhead];
+    FF nr[kAhead];
+    float nu[kAhead];
+#pragma unroll
+    for (int k = 0; k < kAhead; ++k) {
+      const int j = i - kAhead - k;
+      const long long o = (long long)j * s;
+      nb[k] = (j >= 0) ? xs[o] : make_float2(0.f, 0.f);
+      nr[k] = (j >= 0) ? load_rin<kRinDouble>(rind, rinf, o) : FF{0.f, 0.f};
+      nu[k] = (j >= 0 && need_u) ? u[o] : 0.f;
+    }
+#pragma unroll
+    for (int k = 0; k < kAhead; ++k) {
+      const TriRow& r = R[i - k];
+      const FF yy = ff_add(ff_of(rb[k]), ff_neg(ff_mul({r.dth, r.dtl}, y1)));
+      fin.put(i - k, (long long)(i - k) * s, yy, rr[k], ru[k]);
+      y1 = yy;
+    }
+#pragma unroll
+    for (int k = 0; k < kAhead; ++k) {
+      rb[k] = nb[k];
+      rr[k] = nr[k];
+      ru[k] = nu[k];
+    }
+  }
+  for (; i >= 0; --i) {
+    const long long o = (long long)i * s;
+    const TriRow& r = R[i];
+    const FF yy = ff_add(ff_of(xs[o]), ff_neg(ff_mul({r.dth, r.dtl}, y1)));
+    fin.put(i, o, yy, load_rin<kRinDouble>(rind, rinf, o), uval(o));
+    y1 = yy;
+  }
+}
+
+template <bool kRinDouble>
+__global__ void __launch_bounds__(128) k_resid_ff(ResidPass<double> p, const TriRow* __restrict__ R,
+                                                  const float* u, const double* rind,
+                                                  const float2* rinf, float2* scratch, float2* rout,
+                                                  __nv_bfloat16* hi, __nv_bfloat16* lo, float* x32,
+                                                  float* r32, float sig_h, float sig_l) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)p.na * p.nb) return;
+  const int a = (int)(t % p.na), b = (int)(t / p.na);
+  const long long base = a * p.sa + b * p.sb;
+  double blo = 0.0, bhi = 0.0;
+  if (p.bc) {
+    blo = p.bc[t];
+    bhi = p.bc[t + (long long)p.na * p.nb];
+  }
+  FinFF fin;
+  fin.mode = p.mode;
+  fin.sigma = {sig_h, sig_l};
+  fin.out = rout ? rout + base : nullptr;
+  const long long pbase = a * p.pa + b * p.pb;
+  fin.hi = hi ? hi + pbase : nullptr;
+  fin.lo = lo ? lo + pbase : nullptr;
+  fin.x32 = x32 ? x32 + pbase : nullptr;
+  fin.pstride = p.pstride;
+  fin.r32 = r32 ? r32 + base : nullptr;
+  solve_line_ff<kRinDouble>(R, p.n, u + base, rind ? rind + base : nullptr, rinf ? rinf + base : nullptr,
+                            scratch + base, p.s, blo, bhi, fin);
 }
 
 // solf(1:n1,1:n2,1:n3) = u1 + C, widened exactly and summed in FP64.
@@ -747,6 +1037,13 @@ static int build_tri_rows(AxisDev& d, const std::vector<double>& rows) {
     t.rl = (float)(rd - (double)t.rh);
     t.ft = i > 0 ? r[1] * inv_c / rows[(size_t)kRow * (i - 1) + 2] : 0.0;
     t.dt = i < n - 1 ? r[3] * inv_c : 0.0;
+    auto split = [](double v, float& h, float& l) {
+      h = (float)v;
+      l = (float)(v - (double)h);
+    };
+    split(t.ft, t.fth, t.ftl);
+    split(t.dt, t.dth, t.dtl);
+    split(t.cbc, t.cbh, t.cbl);
   }
   int rc = d.tri.ensure(sizeof(TriRow) * n);
   if (rc) return rc;
@@ -907,6 +1204,55 @@ static int solve_plain_dev(mf_solver3d* sc, const double* rhs, double sigma, dou
 // last pass writes the FP64/FP32 array `r` (when planes and x32 are null),
 // the split-BF16 planes or the FP32 operand x32 of the 3xTF32 transforms
 // (and, with r32, an FP32 copy of r).
+// The three passes in double-float arithmetic (tridiagonal operators, FP32
+// iterate): x from the FP64 rin, y and z from float-pair intermediates.
+// Selected by mf_solver3d_set_residual(MF_RESID_FF).  Measured at 257^3 on
+// GB300 it is slower than the FP64 sweeps (1.02 vs 0.78 ms for the three
+// passes): without FP64 operations the passes become bound by the issue and
+// latency of the long dependent double-float chains of the sweeps.
+static int residual_ff(mf_solver3d* sc, const double* rin, const float* u, double sigma,
+                       const double* bcs[3], float2* s0, float2* s1, __nv_bfloat16* hi,
+                       __nv_bfloat16* lo, float* x32, float* r32, cudaStream_t st) {
+  const long long n1 = sc->n[0], n2 = sc->n[1], n3 = sc->n[2];
+  const float sh = (float)sigma, sl = (float)(sigma - (double)sh);
+  auto pass = [&](int axis, int mode) {
+    ResidPass<double> p;
+    const AxisDev& d = sc->ax[axis];
+    p.rows = nullptr;
+    p.n = d.n;
+    p.bc = bcs ? bcs[axis] : nullptr;
+    p.bcc = make_double4(0, 0, 0, 0);
+    p.sigma = sigma;
+    p.mode = mode;
+    p.pa = p.pb = p.pstride = 0;
+    if (axis == 0) { p.na = (int)n2; p.nb = (int)n3; p.sa = n1; p.sb = n1 * n2; p.s = 1; }
+    if (axis == 1) { p.na = (int)n1; p.nb = (int)n3; p.sa = 1; p.sb = n1 * n2; p.s = n1; }
+    if (axis == 2) {
+      p.na = (int)n1; p.nb = (int)n2; p.sa = 1; p.sb = n1; p.s = n1 * n2;
+      p.pa = 1; p.pb = sc->P[0]; p.pstride = (long long)sc->P[0] * sc->P[1];
+    }
+    return p;
+  };
+  auto blocks = [&](const ResidPass<double>& p) { return blocks_for((long long)p.na * p.nb, 128); };
+  ResidPass<double> px = pass(0, 0), py = pass(1, 1), pz = pass(2, r32 ? 3 : 2);
+  sc->prof.begin(kProfResidX, st);
+  k_resid_ff<true><<<blocks(px), 128, 0, st>>>(px, sc->ax[0].tri.as<TriRow>(), u, rin, nullptr, s0, s0,
+                                               nullptr, nullptr, nullptr, nullptr, sh, sl);
+  sc->prof.end(st);
+  MF_CUDA(cudaGetLastError());
+  sc->prof.begin(kProfResidYZ, st);
+  k_resid_ff<false><<<blocks(py), 128, 0, st>>>(py, sc->ax[1].tri.as<TriRow>(), u, nullptr, s0, s1, s1,
+                                                nullptr, nullptr, nullptr, nullptr, sh, sl);
+  sc->prof.end(st);
+  MF_CUDA(cudaGetLastError());
+  sc->prof.begin(kProfResidYZ, st);
+  k_resid_ff<false><<<blocks(pz), 128, 0, st>>>(pz, sc->ax[2].tri.as<TriRow>(), u, nullptr, s1, s0,
+                                                nullptr, hi, lo, x32, r32, sh, sl);
+  sc->prof.end(st);
+  MF_CUDA(cudaGetLastError());
+  return MF_OK;
+}
+
 template <class T, class In>
 static int residual_passes(mf_solver3d* sc, const T* rin, const In* u, double sigma,
                            const double* bcs[3], T* s0, T* s1, T* r, __nv_bfloat16* hi,
@@ -927,10 +1273,15 @@ static int residual_passes(mf_solver3d* sc, const T* rin, const In* u, double si
     if (axis == 2) { p.na = (int)n1; p.nb = (int)n2; p.sa = 1; p.sb = n1; p.s = n1 * n2; }
     return p;
   };
-  // FP32 iterate, FP64 residual, tridiagonal operators: moment form
+  // FP32 iterate, FP64-accurate residual, tridiagonal operators: moment
+  // form, with FP64 sweeps (default) or double-float sweeps
   bool tri = false;
-  if constexpr (sizeof(T) == 8 && sizeof(In) == 4)
+  if constexpr (sizeof(T) == 8 && sizeof(In) == 4) {
     tri = sc->ax[0].tri_ok && sc->ax[1].tri_ok && sc->ax[2].tri_ok;
+    if (tri && sc->resid_mode == MF_RESID_FF && (hi || x32))
+      return residual_ff(sc, rin, u, sigma, bcs, reinterpret_cast<float2*>(s0),
+                         reinterpret_cast<float2*>(s1), hi, lo, x32, r32, st);
+  }
   int axis_of_pass = 0;
   auto launch = [&](const ResidPass<T>& p, int kind, const T* in_r, T* scratch, T* rout,
                     __nv_bfloat16* h, __nv_bfloat16* l, float* x, float* r32p) -> int {
@@ -1451,6 +1802,13 @@ int mf_solver3d_set_eigen(mf_solver3d_t* sc, int axis, const double* eigen, cons
     }
   MF_CUDA(cudaDeviceSynchronize());
   return axis_set_eigen(d, e, V, Vi);
+}
+
+int mf_solver3d_set_residual(mf_solver3d_t* sc, int mode) {
+  if (!sc || (mode != MF_RESID_FF && mode != MF_RESID_FP64))
+    return set_error(MF_ERR_ARG, "mf_solver3d_set_residual: bad arguments");
+  sc->resid_mode = mode;
+  return MF_OK;
 }
 
 int mf_solver3d_device_status(mf_solver3d_t* sc) {

@@ -44,6 +44,8 @@ MF_ERR_UNSUPPORTED = 8
 MF_PREC_FP64 = 0
 MF_PREC_SPLIT_BF16 = 1
 MF_PREC_3XTF32 = 2
+MF_RESID_FF = 0
+MF_RESID_FP64 = 1
 
 
 class MflopsError(RuntimeError):
@@ -122,6 +124,7 @@ _PROTOS = {
     "mf_les_nu": [_P, _I, _D, ctypes.POINTER(_P), _P, _P],
     "mf_les_nu_velocity": [_P, _P, _P, _P, _I, _D, _P, _P, _P, _P, _P],
     "mf_solver3d_profile": [_P, _I],
+    "mf_solver3d_set_residual": [_P, _I],
     "mf_solver3d_profile_read": [_P, _I, _DP, ctypes.POINTER(ctypes.c_longlong)],
 }
 
@@ -397,6 +400,10 @@ class SolverCoeffs3D:
 
     def device_status(self):
         _check(_lib.mf_solver3d_device_status(self._h))
+
+    def set_residual(self, mode):
+        """Residual arithmetic of the mixed path: MF_RESID_FF or MF_RESID_FP64."""
+        _check(_lib.mf_solver3d_set_residual(self._h, int(mode)))
 
     def residual(self, g, u, sigma, bcx, bcy, bcz, r, stream=None):
         n1, n2, n3 = (int(v) for v in g.shape)

@@ -111,3 +111,29 @@ def test_tf32_matches_fp64_gpu_at_257(mf, gpu):
         errs.append((torch.linalg.vector_norm(mixed - plain) / torch.linalg.vector_norm(plain)).item())
     print("257^3 3xtf32 vs FP64 GPU, refine 0/1/2: %.3e %.3e %.3e" % tuple(errs))
     assert errs[2] < 1e-10
+
+
+@pytest.mark.parametrize("prec_name,refine", [("MF_PREC_3XTF32", 1), ("MF_PREC_SPLIT_BF16", 2)])
+def test_residual_arithmetic_modes_agree(mf, gpu, prec_name, refine):
+    """Double-FP32 and FP64 sweeps of the refinement residual give solutions
+    within 1e-10 of the FP64 oracle and within 1e-11 of each other."""
+    nall = (66, 50, 82)
+    gx, gy, gz = grids(*nall, kind="tanh")
+    n1, n2, n3 = (v - 2 for v in nall)
+    bct = (1, 2, 1, 1, 2, 1)
+    sc_ref = S.Solver3D(gx, gy, gz, bct, 6)
+    sc = mf.SolverCoeffs3D(gx, gy, gz, bct, 6)
+    rhs = field((n1, n2, n3), 9)
+    bcx, bcy, bcz = bc_arrays(n1, n2, n3, 10)
+    solf0 = np.zeros((n1 + 2, n2 + 2, n3 + 2), order="F")
+    ref = S.solve_3d(sc_ref, rhs, -30.0, solf0, bcx, bcy, bcz)
+    m = solf_mask(n1, n2, n3)
+    got = {}
+    for mode in (mf.MF_RESID_FF, mf.MF_RESID_FP64):
+        sc.set_residual(mode)
+        out = sc.solve_3d(mf.to_device(rhs), -30.0, mf.to_device(solf0), mf.to_device(bcx),
+                          mf.to_device(bcy), mf.to_device(bcz), precision=getattr(mf, prec_name),
+                          refine=refine)
+        got[mode] = mf.to_host(out)[m]
+        assert rel_l2(got[mode], ref[m]) < 1e-10
+    assert rel_l2(got[mf.MF_RESID_FF], got[mf.MF_RESID_FP64]) < 1e-11
