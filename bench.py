@@ -17,6 +17,7 @@ exchange; replicas only) and value = total solves/s over all ranks.
 Fortran compiler, MPI and PETSc, none of which exist on this system.
 """
 import argparse
+import datetime
 import json
 import os
 import statistics
@@ -40,14 +41,19 @@ UNIT = "solves/s"
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--nodes", type=int, default=257)
     ap.add_argument("--cpu-sample", type=int, default=2, help="oracle solves timed for cpu_baseline")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-rows", action="store_true", help="skip the measurements of the other rows")
     ap.add_argument("--precision", default="auto", choices=["auto", "bf16", "tf32"],
                     help="transform format; auto times both and reports the faster")
+    ap.add_argument("--probe", default=None, choices=["bf16", "tf32", "fp64"],
+                    help="profiling aid: run two untimed solves of the workload in this format "
+                         "(refinement steps from --refine) and exit")
+    ap.add_argument("--refine", type=int, default=1)
     return ap.parse_args()
 
 
@@ -98,22 +104,30 @@ def peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks/throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks and throttle reasons sampled every 50 ms; only the
+    samples taken inside the window given by mark_start/mark_end count."""
 
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, index):
         self.index = index
+        self.t0 = self.t1 = None
         self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(index), "--query-gpu=" + self.FIELDS,
-                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.file,
+                 "--format=csv,noheader,nounits", "-lms", "50"], stdout=self.file,
                 stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
+
+    def mark_start(self):
+        self.t0 = datetime.datetime.now()
+
+    def mark_end(self):
+        self.t1 = datetime.datetime.now()
 
     def stop(self):
         if self.proc is None:
@@ -125,24 +139,32 @@ class ClockSampler:
             self.proc.kill()
         self.file.flush()
         self.file.seek(0)
-        sm, smax, reasons = [], None, set()
+        sm, smax, reasons, power = [], None, set(), []
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for line in self.file.read().splitlines():
             parts = [p.strip() for p in line.split(",")]
-            if len(parts) < 9:
+            if len(parts) < 10:
                 continue
             try:
-                sm.append(float(parts[1]))
-                smax = float(parts[2])
+                ts = datetime.datetime.strptime(parts[0], "%Y/%m/%d %H:%M:%S.%f")
             except ValueError:
                 continue
-            for nm, v in zip(names, parts[5:9]):
+            if self.t0 is not None and not (self.t0 <= ts <= self.t1):
+                continue
+            try:
+                sm.append(float(parts[2]))
+                smax = float(parts[3])
+                power.append(float(parts[4]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[6:10]):
                 if v.lower() == "active":
                     reasons.add(nm)
         os.unlink(self.file.name)
         busy = [s for s in sm if smax and s > 0.5 * smax] or sm
         return {"sm_mhz": statistics.median(busy) if busy else None, "sm_max_mhz": smax,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm),
+                "power_w_median": statistics.median(power) if power else None}
 
 
 # ---------------------------------------------------------------------------
@@ -271,19 +293,28 @@ def run_gb300(args, rank, world, dist):
     resid_ff["rel_l2_vs_fp64_gpu"] = err_vs_plain()
     sc.set_residual(mf.MF_RESID_FP64)
 
-    for _ in range(max(args.warmup, 3)):
+    # clock sampler first, so that its samples cover the timed region; the
+    # warm-up runs at least W steps and at least 0.3 s
+    clocks = ClockSampler(local)
+    tw = time.perf_counter()
+    nw = 0
+    while nw < max(args.warmup, 3) or time.perf_counter() - tw < 0.3:
         mixed()
+        nw += 1
+        if nw % 10 == 0:
+            torch.cuda.synchronize()
     torch.cuda.synchronize()
 
     # timed region: K solves, per-step CUDA events on the launching stream,
     # L2 flushed (256 MiB write) between steps outside the event pairs
-    clocks = ClockSampler(local)
     if dist is not None:
         dist.barrier()
     torch.cuda.synchronize()
+    clocks.mark_start()
     wall0 = time.perf_counter()
     step_ms = timed(mixed, args.steps)
     wall = time.perf_counter() - wall0
+    clocks.mark_end()
     if dist is not None:
         dist.barrier()
     clk = clocks.stop()
@@ -349,6 +380,7 @@ def run_gb300(args, rank, world, dist):
         plain_vs_oracle = None
 
     hbm, bf16, src = peaks()
+    rows = None if args.no_rows else row_measurements(mf, torch, hbm)
     tc_ms = sum(prof[k][0] for k in ("tc_transform", "tc_transform_divide", "tc_transform_update"))
     tc_n = sum(prof[k][1] for k in ("tc_transform", "tc_transform_divide", "tc_transform_update"))
     algo_flops = 2.0 * n * n * n * n  # one dense transform: 2 * n_axis * (n_b*n_c) * n_axis
@@ -363,7 +395,9 @@ def run_gb300(args, rank, world, dist):
         # TF32 runs at half the BF16 tensor rate on this part (nominal ratio)
         peak = bf16 if best == "bf16" else bf16 / 2.0
         roof = {"kernel": "k_tc_transform", "bound": "tensor", "achieved": achieved, "peak": peak,
-                "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                "unit": "TFLOP/s", "frac": achieved / peak,
+                "traffic": profile_traffic("k_tc_transform_%s_257cube.md" % best),
+                "traffic_source": "ncu dram__bytes_read+write of one launch, profiles/",
                 "peak_source": src + (" bf16 burst" if best == "bf16" else " bf16 burst / 2 (tf32)"),
                 "algorithmic_per_launch": algo_flops}
     else:
@@ -372,7 +406,8 @@ def run_gb300(args, rank, world, dist):
         algo_bytes = per_pt * n ** 3
         achieved = algo_bytes / (ms / cnt * 1e-3) / 1e9
         roof = {"kernel": dominant, "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                "frac": achieved / hbm, "traffic": None, "peak_source": src + " copy",
+                "frac": achieved / hbm, "traffic": profile_traffic("k_resid_tri_257cube.md"),
+                "peak_source": src + " copy",
                 "algorithmic_per_launch": algo_bytes}
     value = world * args.steps / (total_ms * 1e-3)
     line = {
@@ -402,6 +437,7 @@ def run_gb300(args, rank, world, dist):
         "cpu_baseline": cpu,
         "e2e": {"value": world / e2e_dt, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "api": "mf_solve_3d_mixed with pinned host pointers"},
+        "rows": rows,
         "gpu_launches": launches * args.steps,
         "gpu_launches_per_step": launches,
         "clocks": clk,
@@ -410,8 +446,133 @@ def run_gb300(args, rank, world, dist):
     print(json.dumps(line), flush=True)
 
 
+def profile_traffic(name):
+    """DRAM bytes per launch (dram__bytes_read + dram__bytes_write of one ncu
+    capture) recorded in the kernel's summary under profiles/, or None."""
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles", name)
+    try:
+        with open(path) as fh:
+            for line in fh:
+                if line.startswith("traffic_bytes_per_launch:"):
+                    return float(line.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
+
+
+def row_measurements(mf, torch, hbm):
+    """Short event-timed measurements of the other rows of the path, each on
+    the shapes of the reference's configurations (synthetic data)."""
+    from oracle import mesh
+    out = {}
+
+    def time_fn(fn, reps=10):
+        fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(reps):
+            fn()
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps
+
+    def field(shape, seed):
+        gen = torch.Generator("cuda").manual_seed(seed)
+        return torch.rand(tuple(reversed(shape)), dtype=torch.float64, device="cuda",
+                          generator=gen).permute(*reversed(range(len(shape))))
+
+    # compact derivative sweeps, 257^3 FP64 field on a tanh(2.0) grid
+    # (16 algorithmic bytes per point: read f, write df; field > L2)
+    n = 257
+    g = mesh.tanh_grid(n, 2.0)
+    dc = mf.DerivativesCoefficients(g, so=6)
+    f = field((n, n, n), 11)
+    df = mf.empty_device((n, n, n))
+    for name, axis, order in (("derx", 0, 1), ("dery", 1, 1), ("derz", 2, 1), ("dderx", 0, 2)):
+        ms = time_fn(lambda: dc.apply(axis, order, f, out=df))
+        gbs = 16.0 * n ** 3 / (ms * 1e-3) / 1e9
+        out["derivative_%s_257cube" % name] = {"ms": ms, "GB_per_s": gbs, "frac_of_hbm": gbs / hbm}
+    del f, df
+    # configuration 1: 65^3, tanh(1.5) on all axes, Dirichlet, so = 6
+    n = 65
+    g = mesh.tanh_grid(n, 1.5)
+    sc = mf.SolverCoeffs3D(g, g, g, (1,) * 6, 6)
+    rhs = field((n - 2, n - 2, n - 2), 12)
+    bc = [mf.empty_device((n - 2, n - 2, 2)) for _ in range(3)]
+    solf = mf.empty_device((n, n, n))
+    for name, sigma in (("poisson", 0.0), ("helmholtz_1e3", -1e3)):
+        ms = time_fn(lambda: sc.solve_3d(rhs, sigma, solf, *bc), reps=20)
+        out["solve_fp64_%s_65cube" % name] = {"us": ms * 1e3}
+    dc = mf.DerivativesCoefficients(g, so=6)
+    f = field((n, n, n), 13)
+    df = mf.empty_device((n, n, n))
+    for name, axis, order in (("derx", 0, 1), ("dery", 1, 1), ("derz", 2, 1), ("dderx", 0, 2)):
+        ms = time_fn(lambda: dc.apply(axis, order, f, out=df), reps=50)
+        out["derivative_%s_65cube" % name] = {"us": ms * 1e3}
+    # multidomain: 2x2x2 subdomains of uneven 17/25-node slabs, Helmholtz
+    nodes = [17, 25]
+    slab = lambda lo, hi, m: mesh.tanh_grid(m, 1.0, lo, hi)
+    grids = [[slab(0.0, 0.5, nodes[0]), slab(0.5, 1.0, nodes[1])] for _ in range(3)]
+    md = mf.MultiDomain((2, 2, 2), (0, 0, 0), *grids, (1,) * 6)
+    t0 = time.perf_counter()
+    md.influence_matrix_set(-1e3)
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t0
+    subs = md.subdomains()
+    gd = {c: field(md.shape(*c), 20 + i) for i, c in enumerate(subs)}
+    ud = {c: mf.empty_device(md.shape(*c)) for c in subs}
+    bd = {c: [mf.empty_device((md.shape(*c)[1] - 2, md.shape(*c)[2] - 2, 2)),
+              mf.empty_device((md.shape(*c)[0] - 2, md.shape(*c)[2] - 2, 2)),
+              mf.empty_device((md.shape(*c)[0] - 2, md.shape(*c)[1] - 2, 2))] for c in subs}
+    ms = time_fn(lambda: md.solve(gd, ud, bd), reps=5)
+    out["multidomain_2x2x2_17_25"] = {"ninf": md.ninf(), "influence_setup_s": setup_s, "solve_ms": ms}
+    # spline filter: 384 -> 96 points along x of a 384 x 385 x 384 fine field
+    xi = mesh.uniform_grid(384)
+    xo = mesh.uniform_grid(96)
+    flt = mf.SplineFilter(xi, xo, xn=xo, k=3)
+    f = field((384, 385, 384), 30)
+    fo = mf.empty_device((96, 385, 384))
+    ms = time_fn(lambda: flt.apply(f, 0, out=fo), reps=5)
+    gbs = 8.0 * (384 + 96) * 385 * 384 / (ms * 1e-3) / 1e9
+    out["filter_x_384to96_fine_field"] = {"ms": ms, "GB_per_s": gbs}
+    del f
+    # LES eddy viscosity on the 96 x 97 x 96 LES grid from the velocity
+    shape = (96, 97, 96)
+    gx, gy, gz = mesh.uniform_grid(96), mesh.tanh_grid(97, 2.0), mesh.uniform_grid(96)
+    les = mf.LesModel(gx, gy, gz)
+    dcs = [mf.DerivativesCoefficients(gg, so=6) for gg in (gx, gy, gz)]
+    vel = [field(shape, 40 + q) for q in range(3)]
+    for name, t in (("smagorinsky", 1), ("wale", 2), ("sigma", 3)):
+        ms = time_fn(lambda: les.nu_velocity(*dcs, *vel, t, 0.18), reps=10)
+        out["les_%s_96x97x96" % name] = {"us": ms * 1e3}
+    return out
+
+
+def run_probe(args):
+    """Two untimed solves of the bench workload (for ncu launch lists and
+    captures of single kernels)."""
+    import torch
+    import mflops_gb300 as mf
+    grids, rhs, bcs = workload(args.nodes)
+    n = args.nodes - 2
+    sc = mf.SolverCoeffs3D(*grids, (1,) * 6, 6)
+    d_rhs = mf.to_device(rhs)
+    d_bc = [mf.to_device(b) for b in bcs]
+    d_solf = mf.empty_device((n + 2, n + 2, n + 2))
+    prec = {"bf16": mf.MF_PREC_SPLIT_BF16, "tf32": mf.MF_PREC_3XTF32, "fp64": mf.MF_PREC_FP64}[args.probe]
+    for _ in range(2):
+        sc.solve_3d(d_rhs, 0.0, d_solf, *d_bc, precision=prec, refine=args.refine)
+    torch.cuda.synchronize()
+    sc.device_status()
+    print("probe ok", args.probe, args.refine, flush=True)
+
+
 def main():
     args = parse()
+    if args.probe:
+        run_probe(args)
+        return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     dist = None
