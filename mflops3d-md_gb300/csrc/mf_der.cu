@@ -15,7 +15,8 @@
 //    pitch so the per-thread walks are bank-conflict free), and writes them
 //    back coalesced.
 // On GB300 the FP64 pipe (~1.2 TFLOP/s measured) rather than HBM bounds
-// these kernels: ~10 DFMA per point and pass against 16 bytes of traffic.
+// these kernels: ~10 DFMA per point and pass against 16 bytes of traffic,
+// ~7 with the tridiagonal row tables used for schemes of order <= 6.
 #include <algorithm>
 #include <cstring>
 
@@ -35,13 +36,26 @@ __device__ __forceinline__ int line_kind(int mode, int a, int na, int b, int nb)
   return (ea || eb) ? 1 : 0;
 }
 
-__device__ __forceinline__ void process_line(int kind, LineSet plain, LineSet sub, const double* in,
-                                             double* out, long long s) {
+// Row tables of the tridiagonal fast path (null when the scheme is not
+// tridiagonal): plain lines and der_s / dder_s lines.
+struct TriSets {
+  const DerTriRow* plain;
+  const DerTriRow* sub;
+};
+
+__device__ __forceinline__ void process_line(int kind, LineSet plain, LineSet sub, TriSets tri,
+                                             const double* in, double* out, long long s) {
   if (kind == 0) {
-    solve_line(plain.c, plain.n, in, out, s, LineBC(), StorePlain());
+    if (tri.plain)
+      solve_line_tri_d(tri.plain, plain.n, in, out, s);
+    else
+      solve_line(plain.c, plain.n, in, out, s, LineBC(), StorePlain());
   } else if (kind == 1) {
     const int n = plain.n;
-    solve_line(sub.c, sub.n, in + s, out + s, s, LineBC(), StorePlain());
+    if (tri.sub)
+      solve_line_tri_d(tri.sub, sub.n, in + s, out + s, s);
+    else
+      solve_line(sub.c, sub.n, in + s, out + s, s, LineBC(), StorePlain());
     out[0] = 0.0;
     out[(long long)(n - 1) * s] = 0.0;
   } else {
@@ -50,19 +64,19 @@ __device__ __forceinline__ void process_line(int kind, LineSet plain, LineSet su
 }
 
 // y (stride nx) or z (stride nx*ny) pencils; thread t -> (a = t % na, b = t / na).
-__global__ void der_lines_strided(LineSet plain, LineSet sub, int mode, const double* f,
+__global__ void der_lines_strided(LineSet plain, LineSet sub, TriSets tri, int mode, const double* f,
                                   double* df, int na, int nb, long long sa,
                                   long long sb, long long s) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (long long)na * nb) return;
   const int a = (int)(t % na), b = (int)(t / na);
   const long long base = a * sa + b * sb;
-  process_line(line_kind(mode, a, na, b, nb), plain, sub, f + base, df + base, s);
+  process_line(line_kind(mode, a, na, b, nb), plain, sub, tri, f + base, df + base, s);
 }
 
 // x pencils: 32 per warp, staged through shared memory.
 constexpr int kLinesPerBlock = 32;
-__global__ void __launch_bounds__(32) der_lines_contig(LineSet plain, LineSet sub, int mode,
+__global__ void __launch_bounds__(32) der_lines_contig(LineSet plain, LineSet sub, TriSets tri, int mode,
                                                        const double* __restrict__ f,
                                                        double* __restrict__ df, int n, int na,
                                                        int nb, int pitch) {
@@ -80,7 +94,7 @@ __global__ void __launch_bounds__(32) der_lines_contig(LineSet plain, LineSet su
     const long long line = l0 + lane;
     const int a = (int)(line % na), b = (int)(line / na);
     double* row = tile + lane * pitch;
-    process_line(line_kind(mode, a, na, b, nb), plain, sub, row, row, 1);
+    process_line(line_kind(mode, a, na, b, nb), plain, sub, tri, row, row, 1);
   }
   __syncwarp();
   for (int l = 0; l < nl; ++l) {
@@ -97,8 +111,28 @@ struct mf_der {
   int n = 0, so = 6, solver = 0;
   double* dev = nullptr;  // packed sets: der(n), dder(n), der_s(n-2), dder_s(n-2)
   size_t off[4] = {0, 0, 0, 0};
+  DevBuf tri;             // DerTriRow tables of the same sets (tridiagonal schemes)
+  size_t tri_off[4] = {0, 0, 0, 0};
+  bool tri_ok = false;
   DevBuf stage_in_buf, stage_out_buf;
 };
+
+// DerTriRow table of one set from its packed rows p, f, 1/c, d, e, r0..r6;
+// false when the factored implicit part is not tridiagonal.
+static bool tri_rows(const std::vector<double>& rows, int n, std::vector<DerTriRow>& out) {
+  for (int i = 0; i < n; ++i)
+    if (rows[(size_t)kRow * i + 0] != 0.0 || rows[(size_t)kRow * i + 4] != 0.0) return false;
+  out.resize(n);
+  for (int i = 0; i < n; ++i) {
+    const double* r = &rows[(size_t)kRow * i];
+    const double inv_c = r[2];
+    DerTriRow& t = out[i];
+    for (int m = 0; m < 7; ++m) t.w[m] = r[5 + m] * inv_c;
+    t.ft = i > 0 ? r[1] * inv_c / rows[(size_t)kRow * (i - 1) + 2] : 0.0;
+    t.dt = i < n - 1 ? r[3] * inv_c : 0.0;
+  }
+  return true;
+}
 
 static void pack_rows(const std::vector<double>& dl_lu, const std::vector<double>& dr, int n,
                       std::vector<double>& out) {
@@ -125,6 +159,9 @@ int mf_der_coeffs_init(const double* grid, int n, int solver_type, int so, mf_de
   const int nsets = solver_type ? 4 : 2;
   std::vector<double> packed;
   size_t off[4] = {0, 0, 0, 0};
+  std::vector<DerTriRow> tri_all;
+  size_t tri_off[4] = {0, 0, 0, 0};
+  bool tri_ok = true;
   for (int set = 0; set < nsets; ++set) {
     const int der = (set % 2) + 1;
     const bool sub = set >= 2;
@@ -138,12 +175,34 @@ int mf_der_coeffs_init(const double* grid, int n, int solver_type, int so, mf_de
     std::vector<double> rows((size_t)kRow * m);
     pack_rows(dl, dr, m, rows);
     std::copy(rows.begin(), rows.end(), packed.begin() + off[set]);
+    std::vector<DerTriRow> tr;
+    if (tri_ok && tri_rows(rows, m, tr)) {
+      tri_off[set] = tri_all.size();
+      tri_all.insert(tri_all.end(), tr.begin(), tr.end());
+    } else {
+      tri_ok = false;
+    }
   }
   mf_der* dc = new mf_der();
   dc->n = n;
   dc->so = so;
   dc->solver = solver_type ? 1 : 0;
-  for (int s = 0; s < 4; ++s) dc->off[s] = off[s];
+  for (int s = 0; s < 4; ++s) {
+    dc->off[s] = off[s];
+    dc->tri_off[s] = tri_off[s];
+  }
+  if (tri_ok) {
+    int rc = dc->tri.ensure(tri_all.size() * sizeof(DerTriRow));
+    if (!rc && cudaMemcpy(dc->tri.ptr, tri_all.data(), tri_all.size() * sizeof(DerTriRow),
+                          cudaMemcpyHostToDevice) != cudaSuccess)
+      rc = set_error(MF_ERR_CUDA, "mf_der_coeffs_init: upload of the row tables failed");
+    if (rc) {
+      dc->tri.release();
+      delete dc;
+      return rc;
+    }
+    dc->tri_ok = true;
+  }
   cudaError_t e = cudaMalloc(&dc->dev, packed.size() * sizeof(double));
   if (e != cudaSuccess) {
     delete dc;
@@ -164,6 +223,7 @@ int mf_der_destroy(mf_der_t* dc) {
   if (dc->dev) cudaFree(dc->dev);
   dc->stage_in_buf.release();
   dc->stage_out_buf.release();
+  dc->tri.release();
   delete dc;
   return MF_OK;
 }
@@ -184,12 +244,21 @@ int der_launch(const mf_der_t* dc, int axis, int order, int mode, const double* 
   const int set = order - 1;
   LineSet plain{dc->dev + dc->off[set], dc->n};
   LineSet sub{dc->solver ? dc->dev + dc->off[set + 2] : dc->dev + dc->off[set], dc->n - 2};
+  TriSets tri{nullptr, nullptr};
+  if (dc->tri_ok) {
+    const DerTriRow* t = dc->tri.as<DerTriRow>();
+    tri.plain = t + dc->tri_off[set];
+    tri.sub = dc->solver ? t + dc->tri_off[set + 2] : nullptr;
+  }
   if (axis == 0) {
     const int na = ny, nb = nz;
     const int pitch = nx | 1;
     const size_t smem = (size_t)kLinesPerBlock * pitch * sizeof(double);
     const long long nlines = (long long)na * nb;
-    if (smem <= 200 * 1024) {
+    // Staging 32 lines per one-warp block pays while the tile is small; for
+    // long lines it leaves too few warps per SM and the thread-per-line walk
+    // (lines cached in L1 as each thread consumes them) is faster.
+    if (smem <= 32 * 1024) {
       static bool attr_set = false;
       if (!attr_set) {
         MF_CUDA(cudaFuncSetAttribute(der_lines_contig, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -197,21 +266,21 @@ int der_launch(const mf_der_t* dc, int axis, int order, int mode, const double* 
         attr_set = true;
       }
       const unsigned grid = (unsigned)((nlines + kLinesPerBlock - 1) / kLinesPerBlock);
-      der_lines_contig<<<grid, 32, smem, st>>>(plain, sub, mode, f, df, nx, na, nb, pitch);
+      der_lines_contig<<<grid, 32, smem, st>>>(plain, sub, tri, mode, f, df, nx, na, nb, pitch);
     } else {
       const unsigned grid = (unsigned)((nlines + 127) / 128);
-      der_lines_strided<<<grid, 128, 0, st>>>(plain, sub, mode, f, df, na, nb, (long long)nx,
+      der_lines_strided<<<grid, 128, 0, st>>>(plain, sub, tri, mode, f, df, na, nb, (long long)nx,
                                               (long long)nx * ny, 1);
     }
   } else if (axis == 1) {
     const int na = nx, nb = nz;
     const unsigned grid = (unsigned)(((long long)na * nb + 127) / 128);
-    der_lines_strided<<<grid, 128, 0, st>>>(plain, sub, mode, f, df, na, nb, 1,
+    der_lines_strided<<<grid, 128, 0, st>>>(plain, sub, tri, mode, f, df, na, nb, 1,
                                             (long long)nx * ny, (long long)nx);
   } else {
     const int na = nx, nb = ny;
     const unsigned grid = (unsigned)(((long long)na * nb + 127) / 128);
-    der_lines_strided<<<grid, 128, 0, st>>>(plain, sub, mode, f, df, na, nb, 1, (long long)nx,
+    der_lines_strided<<<grid, 128, 0, st>>>(plain, sub, tri, mode, f, df, na, nb, 1, (long long)nx,
                                             (long long)nx * ny);
   }
   MF_CUDA(cudaGetLastError());
