@@ -19,6 +19,19 @@ int set_error(int code, const char* fmt, ...) {
   return code;
 }
 
+int num_sms() {
+  static int cached[64] = {0};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
+  if (!cached[dev]) {
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
+      sms = 152;
+    cached[dev] = sms;
+  }
+  return cached[dev];
+}
+
 int cuda_error(cudaError_t e, const char* what) {
   return set_error(e == cudaErrorMemoryAllocation ? MF_ERR_ALLOC : MF_ERR_CUDA,
                    "CUDA error in %s: %s", what, cudaGetErrorString(e));

@@ -25,6 +25,9 @@ int cuda_error(cudaError_t e, const char* what);
 // True when p points to device (or managed) memory.
 bool is_device_ptr(const void* p);
 
+// SM count of the current device (152 on GB300), cached per device.
+int num_sms();
+
 // Growable device buffer owned by a handle.
 struct DevBuf {
   void* ptr = nullptr;

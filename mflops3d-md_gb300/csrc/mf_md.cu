@@ -11,8 +11,12 @@
 // device; the neighbour exchange becomes a gather of signed face derivatives
 // into the interface vector and a scatter of the interface solution into the
 // subdomains' boundary arrays (device kernels).  The PETSc KSP is replaced by
-// a dense FP64 LU factorised once (cuSOLVER getrf at set-up) and two blocked
-// triangular solves per call (own kernels, HBM-bound on the factor).
+// a dense FP64 LU factorised once (cuSOLVER getrf at set-up), from which the
+// inverse is formed once as well (getrs against the identity); each call then
+// solves the interface system with one FP64 matrix-vector product, a read of
+// the n x n inverse at HBM rate, instead of two triangular solves whose rows
+// depend on one another.  The blocked triangular solves remain as the path
+// used when the inverse does not fit in device memory.
 #include <cusolverDn.h>
 
 #include <algorithm>
@@ -192,6 +196,34 @@ __global__ void k_tri_update(const double* __restrict__ A, double* x, int n, int
   x[r] -= acc;
 }
 
+// y = A x with A row-major n x n (the interface inverse): one warp per row,
+// lanes stride the contiguous row, shuffle reduction.
+__global__ void k_gemv_rows(const double* __restrict__ A, const double* __restrict__ x,
+                            double* __restrict__ y, int n) {
+  const int warp = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (warp >= n) return;
+  const double* row = A + (long long)warp * n;
+  double a0 = 0.0, a1 = 0.0;
+  int c = lane;
+  for (; c + 32 < n; c += 64) {
+    a0 = fma(row[c], x[c], a0);
+    a1 = fma(row[c + 32], x[c + 32], a1);
+  }
+  if (c < n) a0 = fma(row[c], x[c], a0);
+  double v = a0 + a1;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+  if (lane == 0) y[warp] = v;
+}
+
+// Identity matrix, n x n column-major.
+__global__ void k_identity(double* A, int n) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)n * n) return;
+  A[t] = (t % n == t / n) ? 1.0 : 0.0;
+}
+
 // Mean removal (single CTA reduction; interface vectors are small).
 __global__ void k_remove_mean(double* x, int n) {
   __shared__ double part[256];
@@ -247,6 +279,8 @@ struct mf_md {
   };
   std::vector<Sub> sub;  // index i + nd1*(j + nd2*k)
   DevBuf M, ipiv, vec, info, work, zero_int, du[3], rint, ufield;
+  DevBuf Minv, vec2;  // row-major inverse of the influence matrix, solve output
+  bool inv_ok = false;
   cusolverDnHandle_t cs = nullptr;
   int null_mode = 0;
   double sigma = 0.0;
@@ -417,6 +451,7 @@ int mf_md_destroy(mf_md_t* md) {
       sd.bc[l].release();
     }
   }
+  for (DevBuf* b : {&md->Minv, &md->vec2}) b->release();
   for (DevBuf* b : {&md->M, &md->ipiv, &md->vec, &md->info, &md->work, &md->zero_int, &md->du[0],
                     &md->du[1], &md->du[2], &md->rint, &md->ufield})
     b->release();
@@ -496,6 +531,29 @@ int mf_md_influence_matrix_set(mf_md_t* md, double sigma, int null_mode, void* s
   if (hinfo != 0)
     return set_error(MF_ERR_SINGULAR, "influence matrix is singular (getrf info %d)%s", hinfo,
                      null_mode ? "" : "; an all-Neumann problem needs a null-space mode");
+  // the inverse, row-major: A^T X = I gives X = A^-T column-major, i.e. A^-1
+  // stored by rows; skipped (triangular solves instead) when it does not fit
+  md->inv_ok = false;
+  {
+    const size_t bytes = sizeof(double) * (size_t)n * (size_t)n;
+    size_t freeb = 0, totalb = 0;
+    MF_CUDA(cudaMemGetInfo(&freeb, &totalb));
+    if (bytes < freeb / 2 && md->Minv.ensure(bytes) == MF_OK && md->vec2.ensure(sizeof(double) * n) == MF_OK) {
+      double* X = md->Minv.as<double>();
+      k_identity<<<nblk((long long)n * n, 256), 256, 0, st>>>(X, (int)n);
+      MF_CUDA(cudaGetLastError());
+      if (cusolverDnDgetrs(md->cs, CUBLAS_OP_T, (int)n, (int)n, M, (int)n, md->ipiv.as<int>(), X,
+                           (int)n, md->info.as<int>()) != CUSOLVER_STATUS_SUCCESS)
+        return set_error(MF_ERR_CUDA, "getrs (inverse of the influence matrix) failed");
+      MF_CUDA(cudaMemcpyAsync(&hinfo, md->info.ptr, sizeof(int), cudaMemcpyDeviceToHost, st));
+      MF_CUDA(cudaStreamSynchronize(st));
+      if (hinfo != 0) return set_error(MF_ERR_SINGULAR, "getrs info %d", hinfo);
+      md->inv_ok = true;
+    } else {
+      (void)cudaGetLastError();  // a refused allocation is not an error here
+      md->Minv.release();
+    }
+  }
   md->factored = true;
   return MF_OK;
 }
@@ -550,7 +608,14 @@ int mf_md_solve(mf_md_t* md, const double* const* g, double* const* u, const dou
     k_remove_mean<<<1, 256, 0, st>>>(vec, (int)n);
   }
   if (md->null_mode >= 1) k_set_scalar<<<1, 1, 0, st>>>(vec, 0, 0.0);
-  if ((rc = md_lu_solve(md, vec, st))) return rc;
+  if (md->inv_ok) {
+    k_gemv_rows<<<nblk(32LL * n, 256), 256, 0, st>>>(md->Minv.as<double>(), vec, md->vec2.as<double>(),
+                                                      (int)n);
+    MF_CUDA(cudaGetLastError());
+    MF_CUDA(cudaMemcpyAsync(vec, md->vec2.ptr, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+  } else if ((rc = md_lu_solve(md, vec, st))) {
+    return rc;
+  }
   if (md->null_mode == 1) k_remove_mean<<<1, 256, 0, st>>>(vec, (int)n);
   MF_CUDA(cudaGetLastError());
   // 3. final solves with the interface values

@@ -128,24 +128,30 @@ struct GemmEpi {
   int n1 = 0, n2 = 0;
 };
 
-constexpr int GBM = 64, GBN = 64, GBK = 16;
+constexpr int GBK = 16;
 
+// BT x BT output tile per 256-thread CTA, (BT/16)^2 outputs per thread.  The
+// FP64 pipe (about two DFMA per clock per SM) bounds this kernel at every
+// size, so the tile only decides how evenly the work spreads over the SMs:
+// 64 for large transforms, 32 when 64-wide tiles would leave SMs idle.
+template <int BT>
 __global__ void __launch_bounds__(256) k_gemm_f64(const double* __restrict__ X, int M, int K,
                                                   const double* __restrict__ A, int N,
                                                   double* __restrict__ Y, GemmEpi e) {
-  __shared__ double Xs[GBK][GBM + 1];
-  __shared__ double As[GBK][GBN + 1];
+  constexpr int R = BT / 16;
+  __shared__ double Xs[GBK][BT + 1];
+  __shared__ double As[GBK][BT + 1];
   const int t = threadIdx.x, tx = t % 16, ty = t / 16;
-  const long long m0 = (long long)blockIdx.x * GBM;
-  const int n0 = blockIdx.y * GBN;
-  double acc[4][4];
+  const long long m0 = (long long)blockIdx.x * BT;
+  const int n0 = blockIdx.y * BT;
+  double acc[R][R];
 #pragma unroll
-  for (int b = 0; b < 4; ++b)
+  for (int b = 0; b < R; ++b)
 #pragma unroll
-    for (int a = 0; a < 4; ++a) acc[b][a] = 0.0;
+    for (int a = 0; a < R; ++a) acc[b][a] = 0.0;
   for (int k0 = 0; k0 < K; k0 += GBK) {
 #pragma unroll
-    for (int r = 0; r < 4; ++r) {
+    for (int r = 0; r < (BT * GBK) / 256; ++r) {
       const int id = t + 256 * r;
       const int row = id / GBK, kk = id % GBK;
       const long long m = m0 + row;
@@ -157,24 +163,24 @@ __global__ void __launch_bounds__(256) k_gemm_f64(const double* __restrict__ X, 
     __syncthreads();
 #pragma unroll
     for (int kk = 0; kk < GBK; ++kk) {
-      double xa[4], ab[4];
+      double xa[R], ab[R];
 #pragma unroll
-      for (int a = 0; a < 4; ++a) xa[a] = Xs[kk][tx + 16 * a];
+      for (int a = 0; a < R; ++a) xa[a] = Xs[kk][tx + 16 * a];
 #pragma unroll
-      for (int b = 0; b < 4; ++b) ab[b] = As[kk][ty + 16 * b];
+      for (int b = 0; b < R; ++b) ab[b] = As[kk][ty + 16 * b];
 #pragma unroll
-      for (int b = 0; b < 4; ++b)
+      for (int b = 0; b < R; ++b)
 #pragma unroll
-        for (int a = 0; a < 4; ++a) acc[b][a] = fma(ab[b], xa[a], acc[b][a]);
+        for (int a = 0; a < R; ++a) acc[b][a] = fma(ab[b], xa[a], acc[b][a]);
     }
     __syncthreads();
   }
 #pragma unroll
-  for (int b = 0; b < 4; ++b) {
+  for (int b = 0; b < R; ++b) {
     const int n = n0 + ty + 16 * b;
     if (n >= N) continue;
 #pragma unroll
-    for (int a = 0; a < 4; ++a) {
+    for (int a = 0; a < R; ++a) {
       const long long m = m0 + tx + 16 * a;
       if (m >= M) continue;
       double v = acc[b][a];
@@ -1113,9 +1119,13 @@ static int axis_upload(AxisDev& d, const SolverAxisHost& h) {
 
 static int gemm_f64(StageProfiler& prof, const double* X, int M, int K, const double* A, int N,
                     double* Y, const GemmEpi& e, cudaStream_t st) {
-  dim3 grid(blocks_for(M, GBM), blocks_for(N, GBN));
+  const long long tiles64 = (long long)blocks_for(M, 64) * blocks_for(N, 64);
   prof.begin(kProfGemm64, st);
-  k_gemm_f64<<<grid, 256, 0, st>>>(X, M, K, A, N, Y, e);
+  if (tiles64 >= 2LL * num_sms()) {
+    k_gemm_f64<64><<<dim3(blocks_for(M, 64), blocks_for(N, 64)), 256, 0, st>>>(X, M, K, A, N, Y, e);
+  } else {
+    k_gemm_f64<32><<<dim3(blocks_for(M, 32), blocks_for(N, 32)), 256, 0, st>>>(X, M, K, A, N, Y, e);
+  }
   prof.end(st);
   MF_CUDA(cudaGetLastError());
   return MF_OK;
