@@ -250,6 +250,17 @@ int mf_md_influence_matrix_set(mf_md_t* md, double sigma, int null_mode, void* s
 int mf_md_solve(mf_md_t* md, const double* const* g, double* const* u, const double* const* bcx,
                 const double* const* bcy, const double* const* bcz, void* stream);
 
+/* Interface-system solve form (no reference counterpart: the reference solves
+ * it with a PETSc KSP, class_md.f90:379-438).  MF_MD_IFACE_AUTO (default):
+ * one FP64 matrix-vector product with the inverse formed at set-up when
+ * ninf <= 12,000 and it fits in device memory, else the triangular solves.
+ * MF_MD_IFACE_LU: always the two triangular solves on the getrf factors.
+ * Takes effect at the next mf_md_solve; the inverse, when wanted, is formed
+ * by mf_md_influence_matrix_set, so select MF_MD_IFACE_AUTO before it. */
+#define MF_MD_IFACE_AUTO 0
+#define MF_MD_IFACE_LU 1
+int mf_md_set_interface_solve(mf_md_t* md, int mode);
+
 /* Copies the last interface solution (ninf values) to host memory. */
 int mf_md_interface(const mf_md_t* md, double* lambda);
 

@@ -68,7 +68,14 @@ __global__ void k_les_nu(LesGrad d, const double* __restrict__ dx2, const double
           if (a == b) s -= tr / 3.0;
           sd += s * s;
         }
-      v = (sd < kLesThresh) ? 0.0 : c * pow(sd, 1.5) / (pow(ss, 2.5) + pow(sd, 1.25));
+      // x^1.5, x^2.5 and x^1.25 through square roots: FP64 pow costs tens of
+      // operations on the narrow FP64 pipe, a square root a handful
+      if (sd < kLesThresh) {
+        v = 0.0;
+      } else {
+        const double rsd = sqrt(sd), rss = sqrt(ss);
+        v = c * (sd * rsd) / (ss * ss * rss + rsd * sqrt(rsd));
+      }
     }
   } else {
     // sigma model: singular values of g from the invariants of g g^T
@@ -85,11 +92,14 @@ __global__ void k_les_nu(LesGrad d, const double* __restrict__ dx2, const double
                       G[1][2] * G[2][1] * G[0][0] - G[2][2] * G[0][1] * G[1][0];
     const double a1 = i1 * i1 / 9.0 - i2 / 3.0;
     const double a2 = i1 * i1 * i1 / 27.0 - i1 * i2 / 6.0 + i3 / 2.0;
-    const double a3 = (a1 < kLesThresh) ? 0.0 : acos(a2 / pow(a1, 1.5)) / 3.0;
-    const double pi = 3.14159265358979323846;
     const double sq = sqrt(fmax(a1, 0.0));
-    double s1 = i1 / 3.0 + 2.0 * sq * cos(a3);
-    double s2 = i1 / 3.0 - 2.0 * sq * cos(a3 + pi / 3.0);
+    const double a3 = (a1 < kLesThresh) ? 0.0 : acos(a2 / (a1 * sq)) / 3.0;
+    // cos(a3 + pi/3) = cos(a3)/2 - sin(a3) sqrt(3)/2: one sincos for both roots
+    double sn, cs;
+    sincos(a3, &sn, &cs);
+    const double h3 = 0.86602540378443864676;  // sqrt(3)/2
+    double s1 = i1 / 3.0 + 2.0 * sq * cs;
+    double s2 = i1 / 3.0 - 2.0 * sq * (0.5 * cs - h3 * sn);
     double s3 = i1 - s1 - s2;
     s1 = sqrt(fmax(s1, 0.0));
     s2 = sqrt(fmax(s2, 0.0));

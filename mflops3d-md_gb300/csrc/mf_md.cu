@@ -196,6 +196,9 @@ __global__ void k_tri_update(const double* __restrict__ A, double* x, int n, int
   x[r] -= acc;
 }
 
+// Largest interface system whose explicit inverse is formed at set-up.
+constexpr long long kMaxInverseRows = 12000;
+
 // y = A x with A row-major n x n (the interface inverse): one warp per row,
 // lanes stride the contiguous row, shuffle reduction.
 __global__ void k_gemv_rows(const double* __restrict__ A, const double* __restrict__ x,
@@ -281,6 +284,7 @@ struct mf_md {
   DevBuf M, ipiv, vec, info, work, zero_int, du[3], rint, ufield;
   DevBuf Minv, vec2;  // row-major inverse of the influence matrix, solve output
   bool inv_ok = false;
+  int iface_mode = MF_MD_IFACE_AUTO;
   cusolverDnHandle_t cs = nullptr;
   int null_mode = 0;
   double sigma = 0.0;
@@ -532,9 +536,12 @@ int mf_md_influence_matrix_set(mf_md_t* md, double sigma, int null_mode, void* s
     return set_error(MF_ERR_SINGULAR, "influence matrix is singular (getrf info %d)%s", hinfo,
                      null_mode ? "" : "; an all-Neumann problem needs a null-space mode");
   // the inverse, row-major: A^T X = I gives X = A^-T column-major, i.e. A^-1
-  // stored by rows; skipped (triangular solves instead) when it does not fit
+  // stored by rows.  Forming it costs 2 n^3 FP64 flops (three times the LU),
+  // a few seconds at n = 12,000 on the FP64 pipe; above that, when it does
+  // not fit, or when the triangular form is selected, the solves stay on the
+  // LU factors.
   md->inv_ok = false;
-  {
+  if (md->iface_mode == MF_MD_IFACE_AUTO && n <= kMaxInverseRows) {
     const size_t bytes = sizeof(double) * (size_t)n * (size_t)n;
     size_t freeb = 0, totalb = 0;
     MF_CUDA(cudaMemGetInfo(&freeb, &totalb));
@@ -608,7 +615,7 @@ int mf_md_solve(mf_md_t* md, const double* const* g, double* const* u, const dou
     k_remove_mean<<<1, 256, 0, st>>>(vec, (int)n);
   }
   if (md->null_mode >= 1) k_set_scalar<<<1, 1, 0, st>>>(vec, 0, 0.0);
-  if (md->inv_ok) {
+  if (md->inv_ok && md->iface_mode == MF_MD_IFACE_AUTO) {
     k_gemv_rows<<<nblk(32LL * n, 256), 256, 0, st>>>(md->Minv.as<double>(), vec, md->vec2.as<double>(),
                                                       (int)n);
     MF_CUDA(cudaGetLastError());
@@ -631,6 +638,13 @@ int mf_md_solve(mf_md_t* md, const double* const* g, double* const* u, const dou
         MF_CUDA(cudaGetLastError());
         if ((rc = md_sub_solve(md, s, md->rint.as<double>(), u[s], st))) return rc;
       }
+  return MF_OK;
+}
+
+int mf_md_set_interface_solve(mf_md_t* md, int mode) {
+  if (!md || (mode != MF_MD_IFACE_AUTO && mode != MF_MD_IFACE_LU))
+    return set_error(MF_ERR_ARG, "mf_md_set_interface_solve: bad arguments");
+  md->iface_mode = mode;
   return MF_OK;
 }
 

@@ -46,6 +46,8 @@ MF_PREC_SPLIT_BF16 = 1
 MF_PREC_3XTF32 = 2
 MF_RESID_FF = 0
 MF_RESID_FP64 = 1
+MD_IFACE_AUTO = 0
+MD_IFACE_LU = 1
 
 
 class MflopsError(RuntimeError):
@@ -110,6 +112,7 @@ _PROTOS = {
     "mf_md_solve": [_P, ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.POINTER(_P),
                     ctypes.POINTER(_P), ctypes.POINTER(_P), _P],
     "mf_md_interface": [_P, _DP],
+    "mf_md_set_interface_solve": [_P, ctypes.c_int],
     "mf_filter_lsq_matrix": [_DP, _I, _DP, _DP, _I, _DP, _I, _I, _DP, _DP],
     "mf_filter_period_matrix": [_DP, _I, _DP, _I, _DP, _DP],
     "mf_filter_lsq_init": [_DP, _I, _DP, _DP, _I, _DP, _I, _I, ctypes.POINTER(_P)],
@@ -510,6 +513,10 @@ class MultiDomain:
                                 mk([bc[c][0] for c in subs]), mk([bc[c][1] for c in subs]),
                                 mk([bc[c][2] for c in subs]), _stream(stream)))
         return u
+
+    def set_interface_solve(self, mode):
+        """MD_IFACE_AUTO (inverse when small enough) or MD_IFACE_LU."""
+        _check(_lib.mf_md_set_interface_solve(self._h, int(mode)))
 
     def interface(self):
         lam = np.zeros(self.ninf())

@@ -1,7 +1,9 @@
 """Influence-matrix multidomain solve on the GPU (multidomain_solve,
 class_field.f90:1295-1388) against the FP64 oracle, through the C ABI.
 Tolerance: max |gpu - oracle| <= 1e-11 * max |oracle| per subdomain field
-(the interface solve adds an LU on top of the 1e-12 subdomain solves)."""
+(the interface solve adds an LU on top of the 1e-12 subdomain solves).
+Both interface-solve forms are checked: the inverse formed at set-up (the
+default for small systems) and the triangular solves on the LU factors."""
 import numpy as np
 import pytest
 
@@ -49,11 +51,12 @@ def problem(grids, subs, sigma, bct):
     return g, bc, ex
 
 
-def run(mf, nd, periods, nodes, sigma, bct=(1,) * 6, null=0):
+def run(mf, nd, periods, nodes, sigma, bct=(1,) * 6, null=0, iface=0):
     grids = tuple(slabs(nd[l], nodes[l]) for l in range(3))
     ref = omd.MultiDomain(nd, periods, *grids, bct)
     ref.influence_matrix(sigma, null)
     dev = mf.MultiDomain(nd, periods, *grids, bct)
+    dev.set_interface_solve(iface)
     dev.influence_matrix_set(sigma, null)
     subs = dev.subdomains()
     g, bc, ex = problem(grids, subs, sigma, bct)
@@ -94,3 +97,25 @@ def test_md_pure_neumann_null_space(mf, gpu, null):
     # the reference pins row 0 (null=2) or works with a constant null space (null=1)
     err, lerr, _, _ = run(mf, (2, 1, 1), (0, 0, 0), (11, 11, 11), 0.0, bct=(2,) * 6, null=null)
     assert err < 1e-10 and lerr < 1e-10, (err, lerr)
+
+
+@pytest.mark.parametrize("nd,periods", [((2, 2, 2), (0, 0, 0)), ((2, 1, 1), (1, 0, 0))])
+def test_md_triangular_interface_solve(mf, gpu, nd, periods):
+    err, lerr, _, _ = run(mf, nd, periods, (11, 11, 11), -3.0, iface=mf.MD_IFACE_LU)
+    assert err < 1e-11 and lerr < 1e-11, (err, lerr)
+
+
+@pytest.mark.parametrize("null", [1, 2])
+def test_md_null_space_triangular_interface_solve(mf, gpu, null):
+    err, lerr, _, _ = run(mf, (2, 1, 1), (0, 0, 0), (11, 11, 11), 0.0, bct=(2,) * 6, null=null,
+                          iface=mf.MD_IFACE_LU)
+    assert err < 1e-10 and lerr < 1e-10, (err, lerr)
+
+
+def test_md_interface_forms_agree(mf, gpu):
+    # the same problem through both forms: both match the oracle, and the
+    # interface values agree to rounding
+    a = run(mf, (2, 2, 1), (0, 0, 0), ([11, 15], [13, 9], [11]), -1e3, iface=mf.MD_IFACE_AUTO)
+    b = run(mf, (2, 2, 1), (0, 0, 0), ([11, 15], [13, 9], [11]), -1e3, iface=mf.MD_IFACE_LU)
+    assert a[0] < 1e-11 and b[0] < 1e-11
+    assert a[1] < 1e-11 and b[1] < 1e-11
