@@ -324,6 +324,78 @@ int mf_les_nu_velocity(mf_les_t* les, const mf_der_t* dcx, const mf_der_t* dcy,
                        const mf_der_t* dcz, int les_type, double c, const double* u,
                        const double* v, const double* w, double* nu, void* stream);
 
+/* ------------------------------------------------------------------------
+ * Learned LES coefficient.  No reference counterpart: the reference has only
+ * the plain models above.  A 6-64-64-1 ReLU network (4,673 FP32 parameters)
+ * maps six invariants of the resolved velocity gradient,
+ *   S:S/G2, tr(S^3)/G2^1.5, tr(W^2 S)/G2^1.5, tr(W^2 S^2)/G2^2,
+ *   det(g)/G2^1.5, tr(g)/G2^0.5            (G2 = g:g),
+ * to C(x) in nu_t = C(x) Delta^2 sqrt(2 S:S).  Outside the training range of
+ * the features the plain Smagorinsky model is used per point.
+ * ---------------------------------------------------------------------- */
+typedef struct mf_mlp mf_mlp_t;
+
+/* New network: He-uniform weights from `seed`, zero biases, output bias 1. */
+int mf_mlp_create(unsigned long long seed, mf_mlp_t** mlp);
+int mf_mlp_destroy(mf_mlp_t* mlp);
+/* 4,673: W1[64][6], b1[64], W2[64][64], b2[64], w3[64], b3 (FP32). */
+int mf_mlp_num_params(void);
+int mf_mlp_get_params(const mf_mlp_t* mlp, float* host_params);
+/* Replaces the parameters and resets the Adam moments. */
+int mf_mlp_set_params(mf_mlp_t* mlp, const float* host_params);
+/* Input standardisation x = (f - mean) * istd, training range [lo, hi] per
+ * feature, output scale (C = cscale * network output) and loss scale. */
+int mf_mlp_set_scaling(mf_mlp_t* mlp, const float* mean, const float* istd, const float* lo,
+                       const float* hi, float cscale, float loss_scale);
+/* One training step on n points (device arrays: X (n_all, 6) raw features,
+ * base (n_all) = Delta^2 sqrt(2 S:S), target (n_all) eddy viscosity; idx
+ * (n, int32, each < n_all) selects the points, or NULL for the first n).
+ * Loss L = loss_scale / n * sum (C b - target)^2.  lr > 0 applies one Adam
+ * step (beta 0.9/0.999, eps 1e-8); lr = 0 only evaluates.  grad_host (4,673
+ * floats) and loss_host receive the gradient and loss before the update when
+ * not NULL (the call then synchronises the stream). */
+int mf_mlp_train_step(mf_mlp_t* mlp, const float* X, const float* base, const float* target,
+                      const int* idx, long long n, float lr, float* grad_host, float* loss_host,
+                      void* stream);
+/* C for n points of raw features X (device). */
+int mf_mlp_predict(const mf_mlp_t* mlp, const float* X, long long n, float* C, void* stream);
+
+/* Features and b for every point of the LES grid from the nine gradient
+ * fields (device; zero on the edge lines and where g = 0). */
+int mf_les_features(const mf_les_t* les, const double* const* du, float* X, float* base,
+                    void* stream);
+/* A-priori target from filtered fields: ubar[3] = F(u_i), uu[6] = F(u_i u_j)
+ * (00, 01, 02, 11, 12, 22), du = grad(ubar); nu = -tau^d:S / (2 S:S). */
+int mf_les_sgs_target(const mf_les_t* les, const double* const* ubar, const double* const* uu,
+                      const double* const* du, float* nu_true, void* stream);
+/* nu from the network where the features are inside its training range,
+ * else Smagorinsky with c_fallback (the value mf_les_nu type 1 gives).
+ * n_fallback (host, optional) receives the number of fallback points. */
+int mf_les_nu_mlp(mf_les_t* les, const mf_mlp_t* mlp, double c_fallback, const double* const* du,
+                  double* nu, long long* n_fallback, void* stream);
+
+/* ------------------------------------------------------------------------
+ * Fine-grid box flow that generates the training data (no reference
+ * counterpart): pointwise parts of an explicit RK2 + projection step of a
+ * decaying flow in a no-slip box; derivatives and the Neumann Poisson solve
+ * come from the entry points above.  Device fields (nx,ny,nz), FP64.
+ * ---------------------------------------------------------------------- */
+/* out_i = a w_i + b (u_i + dt (nu sum_j ddu[3i+j] - sum_j u_j du[3i+j])),
+ * zero on the walls; w may be NULL when a == 0. */
+int mf_flow_stage(int nx, int ny, int nz, double nu, double dt, double a, double b,
+                  const double* const* u, const double* const* w, const double* const* du,
+                  const double* const* ddu, double* const* out, void* stream);
+/* rhs (nx-2, ny-2, nz-2) = scale (dudx + dvdy + dwdz) at the interior points. */
+int mf_flow_divergence(int nx, int ny, int nz, double scale, const double* dudx, const double* dvdy,
+                       const double* dwdz, double* rhs, void* stream);
+/* u_i -= dt dphi_i in the interior, 0 on the walls. */
+int mf_flow_correct(int nx, int ny, int nz, double dt, double* const* u, const double* const* dphi,
+                    void* stream);
+/* uu = u_i u_j: 00, 01, 02, 11, 12, 22. */
+int mf_flow_products(int nx, int ny, int nz, const double* const* u, double* const* uu, void* stream);
+/* u = curl(psi) from dpsi[3i+j] = d psi_i / d x_j, 0 on the walls. */
+int mf_flow_curl(int nx, int ny, int nz, const double* const* dpsi, double* const* u, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "mf_internal.h"
+#include "mf_mlp.cuh"
 
 namespace mf {
 
@@ -109,6 +110,124 @@ __global__ void k_les_nu(LesGrad d, const double* __restrict__ dx2, const double
   nu[idx] = v * ((dx2[i] + dy2[j] + dz2[k]) / 3.0);
 }
 
+__device__ __forceinline__ void load_grad(const LesGrad& d, long long idx, double g[3][3]) {
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b) g[a][b] = d.g[3 * a + b][idx];
+}
+
+__device__ __forceinline__ double strain_ss(const double g[3][3]) {
+  double ss = 0.0;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    ss += g[a][a] * g[a][a];
+#pragma unroll
+    for (int b = a + 1; b < 3; ++b) ss += 0.5 * (g[a][b] + g[b][a]) * (g[a][b] + g[b][a]);
+  }
+  return ss;
+}
+
+// Training inputs of the learned coefficient: the six invariant features
+// (FP32) and b = Delta^2 sqrt(2 S:S), the factor multiplying C; zero on the
+// edge lines and where the gradient vanishes.
+__global__ void k_les_features(LesGrad d, const double* __restrict__ dx2, const double* __restrict__ dy2,
+                               const double* __restrict__ dz2, int nx, int ny, int nz,
+                               float* __restrict__ X, float* __restrict__ base) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)nx * ny * nz) return;
+  const int i = (int)(idx % nx);
+  const long long jk = idx / nx;
+  const int j = (int)(jk % ny), k = (int)(jk / ny);
+  double f[kMlpIn] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  double b = 0.0;
+  if (!on_edge(i, j, k, nx, ny, nz)) {
+    double g[3][3];
+    load_grad(d, idx, g);
+    if (grad_features(g, f)) b = sqrt(2.0 * strain_ss(g)) * ((dx2[i] + dy2[j] + dz2[k]) / 3.0);
+  }
+#pragma unroll
+  for (int q = 0; q < kMlpIn; ++q) X[idx * kMlpIn + q] = (float)f[q];
+  base[idx] = (float)b;
+}
+
+// A-priori target: the eddy viscosity that reproduces the local subgrid
+// dissipation of the filtered field, nu = -tau^d : S / (2 S:S), with
+// tau_ij = F(u_i u_j) - F(u_i) F(u_j) from filtered products.
+struct SgsFields {
+  const double* ub[3];
+  const double* uu[6];  // F(u_i u_j): 00, 01, 02, 11, 12, 22
+};
+
+__global__ void k_sgs_target(SgsFields s, LesGrad d, int nx, int ny, int nz, float* __restrict__ nu) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)nx * ny * nz) return;
+  const int i = (int)(idx % nx);
+  const long long jk = idx / nx;
+  const int j = (int)(jk % ny), k = (int)(jk / ny);
+  if (on_edge(i, j, k, nx, ny, nz)) {
+    nu[idx] = 0.f;
+    return;
+  }
+  double g[3][3];
+  load_grad(d, idx, g);
+  const double u0 = s.ub[0][idx], u1 = s.ub[1][idx], u2 = s.ub[2][idx];
+  double t[3][3];
+  t[0][0] = s.uu[0][idx] - u0 * u0;
+  t[0][1] = t[1][0] = s.uu[1][idx] - u0 * u1;
+  t[0][2] = t[2][0] = s.uu[2][idx] - u0 * u2;
+  t[1][1] = s.uu[3][idx] - u1 * u1;
+  t[1][2] = t[2][1] = s.uu[4][idx] - u1 * u2;
+  t[2][2] = s.uu[5][idx] - u2 * u2;
+  const double tr = (t[0][0] + t[1][1] + t[2][2]) / 3.0;
+  double ts = 0.0;
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b) ts += (t[a][b] - (a == b ? tr : 0.0)) * 0.5 * (g[a][b] + g[b][a]);
+  const double ss = strain_ss(g);
+  nu[idx] = ss > 1e-300 ? (float)(-ts / (2.0 * ss)) : 0.f;
+}
+
+// Learned-coefficient eddy viscosity with per-point fallback: where all six
+// features lie inside the training range nu = max(C(x), 0) Delta^2 sqrt(2 S:S)
+// with C from the network (FP32, parameters staged in shared memory), else the
+// plain Smagorinsky value with coefficient c_fallback, bit-identical to
+// k_les_nu type 1.  Edge lines are zero.
+__global__ void __launch_bounds__(128) k_les_nu_mlp(LesGrad d, const double* __restrict__ dx2,
+                                                    const double* __restrict__ dy2,
+                                                    const double* __restrict__ dz2, int nx, int ny, int nz,
+                                                    const float* __restrict__ params, MlpScaling s,
+                                                    double c_fallback, double* __restrict__ nu,
+                                                    unsigned long long* __restrict__ n_fallback) {
+  extern __shared__ __align__(16) float sp[];
+  for (int q = threadIdx.x; q < kMlpParams; q += blockDim.x) sp[q] = params[q];
+  __syncthreads();
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)nx * ny * nz) return;
+  const int i = (int)(idx % nx);
+  const long long jk = idx / nx;
+  const int j = (int)(jk % ny), k = (int)(jk / ny);
+  if (on_edge(i, j, k, nx, ny, nz)) {
+    nu[idx] = 0.0;
+    return;
+  }
+  double g[3][3];
+  load_grad(d, idx, g);
+  const double ss = strain_ss(g);
+  double f[kMlpIn];
+  float x[kMlpIn];
+  double c = c_fallback;
+  const bool in = grad_features(g, f) && mlp_input(s, f, x);
+  if (in) {
+    c = (double)fmaxf(s.cscale * mlp_forward(sp, x), 0.f);
+  } else if (n_fallback) {
+    atomicAdd(n_fallback, 1ull);
+  }
+  const double v = c * sqrt(2.0 * ss);
+  nu[idx] = v * ((dx2[i] + dy2[j] + dz2[k]) / 3.0);
+}
+
 }  // namespace mf
 
 using namespace mf;
@@ -117,6 +236,7 @@ struct mf_les {
   int n[3] = {0, 0, 0};
   DevBuf d2[3];  // squared spacings per axis
   DevBuf grad;   // nine gradient fields for mf_les_nu_velocity
+  DevBuf count;  // fallback counter of mf_les_nu_mlp
 };
 
 extern "C" {
@@ -155,6 +275,7 @@ int mf_les_destroy(mf_les_t* les) {
   if (!les) return MF_OK;
   for (auto& b : les->d2) b.release();
   les->grad.release();
+  les->count.release();
   delete les;
   return MF_OK;
 }
@@ -198,6 +319,79 @@ int mf_les_nu_velocity(mf_les_t* les, const mf_der_t* dcx, const mf_der_t* dcy,
       du[3 * i + j] = g;
     }
   return mf_les_nu(les, les_type, c, du, nu, stream);
+}
+
+static int les_grad_args(const mf_les_t* les, const double* const* du, LesGrad& d, const char* who) {
+  if (!les || !du) return set_error(MF_ERR_ARG, "%s: bad arguments", who);
+  for (int q = 0; q < 9; ++q) {
+    if (!du[q] || !is_device_ptr(du[q])) return set_error(MF_ERR_ARG, "%s: device gradients required", who);
+    d.g[q] = du[q];
+  }
+  return MF_OK;
+}
+
+int mf_les_features(const mf_les_t* les, const double* const* du, float* X, float* base, void* stream) {
+  LesGrad d;
+  int rc = les_grad_args(les, du, d, "mf_les_features");
+  if (rc) return rc;
+  if (!X || !base || !is_device_ptr(X) || !is_device_ptr(base))
+    return set_error(MF_ERR_ARG, "mf_les_features: device outputs required");
+  const long long tot = (long long)les->n[0] * les->n[1] * les->n[2];
+  k_les_features<<<(unsigned)((tot + 255) / 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+      d, les->d2[0].as<double>(), les->d2[1].as<double>(), les->d2[2].as<double>(), les->n[0], les->n[1],
+      les->n[2], X, base);
+  MF_CUDA(cudaGetLastError());
+  return MF_OK;
+}
+
+int mf_les_sgs_target(const mf_les_t* les, const double* const* ubar, const double* const* uu,
+                      const double* const* du, float* nu_true, void* stream) {
+  LesGrad d;
+  int rc = les_grad_args(les, du, d, "mf_les_sgs_target");
+  if (rc) return rc;
+  if (!ubar || !uu || !nu_true || !is_device_ptr(nu_true))
+    return set_error(MF_ERR_ARG, "mf_les_sgs_target: bad arguments");
+  SgsFields s;
+  for (int q = 0; q < 3; ++q) {
+    if (!ubar[q] || !is_device_ptr(ubar[q])) return set_error(MF_ERR_ARG, "mf_les_sgs_target: device fields required");
+    s.ub[q] = ubar[q];
+  }
+  for (int q = 0; q < 6; ++q) {
+    if (!uu[q] || !is_device_ptr(uu[q])) return set_error(MF_ERR_ARG, "mf_les_sgs_target: device fields required");
+    s.uu[q] = uu[q];
+  }
+  const long long tot = (long long)les->n[0] * les->n[1] * les->n[2];
+  k_sgs_target<<<(unsigned)((tot + 255) / 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+      s, d, les->n[0], les->n[1], les->n[2], nu_true);
+  MF_CUDA(cudaGetLastError());
+  return MF_OK;
+}
+
+int mf_les_nu_mlp(mf_les_t* les, const mf_mlp_t* mlp, double c_fallback, const double* const* du, double* nu,
+                  long long* n_fallback, void* stream) {
+  LesGrad d;
+  int rc = les_grad_args(les, du, d, "mf_les_nu_mlp");
+  if (rc) return rc;
+  if (!mlp || !nu || !is_device_ptr(nu)) return set_error(MF_ERR_ARG, "mf_les_nu_mlp: bad arguments");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  unsigned long long* cnt = nullptr;
+  if (n_fallback) {
+    if ((rc = les->count.ensure(sizeof(unsigned long long)))) return rc;
+    cnt = les->count.as<unsigned long long>();
+    MF_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), st));
+  }
+  const long long tot = (long long)les->n[0] * les->n[1] * les->n[2];
+  k_les_nu_mlp<<<(unsigned)((tot + 127) / 128), 128, sizeof(float) * kMlpParams, st>>>(
+      d, les->d2[0].as<double>(), les->d2[1].as<double>(), les->d2[2].as<double>(), les->n[0], les->n[1],
+      les->n[2], mlp_device_params(mlp), mlp_scaling(mlp), c_fallback, nu, cnt);
+  MF_CUDA(cudaGetLastError());
+  if (n_fallback) {
+    unsigned long long h = 0;
+    MF_CUDA(cudaMemcpyAsync(&h, cnt, sizeof(h), cudaMemcpyDeviceToHost, st));
+    MF_CUDA(cudaStreamSynchronize(st));
+    *n_fallback = (long long)h;
+  }
+  return MF_OK;
 }
 
 }  // extern "C"

@@ -1,0 +1,133 @@
+// Learned LES coefficient: shared device pieces.
+//
+// A 6-64-64-1 ReLU network maps six dimensionless invariants of the resolved
+// velocity gradient g = grad(u) to the coefficient C(x) of the Smagorinsky
+// form nu_t = C(x) Delta^2 sqrt(2 S:S) (the plain model is C = const,
+// navier_LES type 1, class_navier_3D.f90:1225-1455).  There is no reference
+// counterpart: the reference has only the plain models, which here act as
+// the per-point fallback outside the training range.
+//
+// Features (G2 = g:g, S and W the symmetric and antisymmetric parts of g):
+//   f0 = S:S / G2            f1 = tr(S^3) / G2^1.5    f2 = tr(W^2 S) / G2^1.5
+//   f3 = tr(W^2 S^2) / G2^2  f4 = det(g) / G2^1.5     f5 = tr(g) / G2^0.5
+// all invariant under rotations and under scaling of g, and bounded in
+// magnitude by 1 (f5 by sqrt(3)).  They are computed in FP64 and rounded to
+// FP32; the network runs in FP32.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "mflops_gb300.h"
+
+namespace mf {
+
+constexpr int kMlpIn = 6, kMlpH = 64;
+// parameter layout (FP32): W1[H][In], b1[H], W2[H][H] (row j = output j),
+// b2[H], w3[H], b3
+constexpr int kMlpW1 = 0;
+constexpr int kMlpB1 = kMlpW1 + kMlpH * kMlpIn;
+constexpr int kMlpW2 = kMlpB1 + kMlpH;
+constexpr int kMlpB2 = kMlpW2 + kMlpH * kMlpH;
+constexpr int kMlpW3 = kMlpB2 + kMlpH;
+constexpr int kMlpB3 = kMlpW3 + kMlpH;
+constexpr int kMlpParams = kMlpB3 + 1;  // 4673
+
+// Input standardisation and training range of a trained network.
+struct MlpScaling {
+  float mean[kMlpIn], istd[kMlpIn];  // x_net = (f - mean) * istd
+  float lo[kMlpIn], hi[kMlpIn];      // training range of the raw features
+  float cscale;                      // C = cscale * network output
+};
+
+// Invariant features of one gradient tensor; false when g vanishes.
+__device__ __forceinline__ bool grad_features(const double g[3][3], double f[kMlpIn]) {
+  double g2 = 0.0;
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b) g2 += g[a][b] * g[a][b];
+  if (!(g2 > 1e-300)) return false;
+  double S[3][3], W[3][3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+      S[a][b] = 0.5 * (g[a][b] + g[b][a]);
+      W[a][b] = 0.5 * (g[a][b] - g[b][a]);
+    }
+  double S2[3][3], W2[3][3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+      S2[a][b] = S[a][0] * S[0][b] + S[a][1] * S[1][b] + S[a][2] * S[2][b];
+      W2[a][b] = W[a][0] * W[0][b] + W[a][1] * W[1][b] + W[a][2] * W[2][b];
+    }
+  double ss = 0.0, s3 = 0.0, w2s = 0.0, w2s2 = 0.0;
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+      ss += S[a][b] * S[a][b];
+      s3 += S2[a][b] * S[b][a];
+      w2s += W2[a][b] * S[b][a];
+      w2s2 += W2[a][b] * S2[b][a];
+    }
+  const double det = g[0][0] * (g[1][1] * g[2][2] - g[1][2] * g[2][1]) -
+                     g[0][1] * (g[1][0] * g[2][2] - g[1][2] * g[2][0]) +
+                     g[0][2] * (g[1][0] * g[2][1] - g[1][1] * g[2][0]);
+  const double r = sqrt(g2), r3 = g2 * r;
+  f[0] = ss / g2;
+  f[1] = s3 / r3;
+  f[2] = w2s / r3;
+  f[3] = w2s2 / (g2 * g2);
+  f[4] = det / r3;
+  f[5] = (g[0][0] + g[1][1] + g[2][2]) / r;
+  return true;
+}
+
+// Network output for standardised inputs x; P points to the parameters
+// (shared memory in every caller, read as warp-wide broadcasts).
+__device__ __forceinline__ float mlp_forward(const float* __restrict__ P, const float x[kMlpIn]) {
+  float h1[kMlpH];
+#pragma unroll
+  for (int j = 0; j < kMlpH; ++j) {
+    float a = P[kMlpB1 + j];
+#pragma unroll
+    for (int k = 0; k < kMlpIn; ++k) a = fmaf(P[kMlpW1 + j * kMlpIn + k], x[k], a);
+    h1[j] = fmaxf(a, 0.f);
+  }
+  float y = P[kMlpB3];
+#pragma unroll 4
+  for (int j = 0; j < kMlpH; ++j) {
+    const float4* w = reinterpret_cast<const float4*>(P + kMlpW2 + j * kMlpH);
+    float a = P[kMlpB2 + j];
+#pragma unroll
+    for (int i = 0; i < kMlpH / 4; ++i) {
+      const float4 q = w[i];
+      a = fmaf(q.x, h1[4 * i], a);
+      a = fmaf(q.y, h1[4 * i + 1], a);
+      a = fmaf(q.z, h1[4 * i + 2], a);
+      a = fmaf(q.w, h1[4 * i + 3], a);
+    }
+    y = fmaf(P[kMlpW3 + j], fmaxf(a, 0.f), y);
+  }
+  return y;
+}
+
+// Standardised network input from raw features; false outside the range.
+__device__ __forceinline__ bool mlp_input(const MlpScaling& s, const double f[kMlpIn], float x[kMlpIn]) {
+  bool in = true;
+#pragma unroll
+  for (int k = 0; k < kMlpIn; ++k) {
+    const float v = (float)f[k];
+    in = in && (v >= s.lo[k]) && (v <= s.hi[k]);
+    x[k] = (v - s.mean[k]) * s.istd[k];
+  }
+  return in;
+}
+
+// Device parameters and scaling of a network handle (host functions).
+const float* mlp_device_params(const mf_mlp_t* mlp);
+const MlpScaling& mlp_scaling(const mf_mlp_t* mlp);
+
+}  // namespace mf

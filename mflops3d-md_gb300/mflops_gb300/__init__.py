@@ -73,6 +73,7 @@ _I = ctypes.c_int
 _D = ctypes.c_double
 _DP = ctypes.POINTER(ctypes.c_double)
 _IP = ctypes.POINTER(ctypes.c_int)
+_FP = ctypes.POINTER(ctypes.c_float)
 
 # name -> argtypes (all return int)
 _PROTOS = {
@@ -126,6 +127,23 @@ _PROTOS = {
     "mf_les_destroy": [_P],
     "mf_les_nu": [_P, _I, _D, ctypes.POINTER(_P), _P, _P],
     "mf_les_nu_velocity": [_P, _P, _P, _P, _I, _D, _P, _P, _P, _P, _P],
+    "mf_mlp_create": [ctypes.c_ulonglong, ctypes.POINTER(_P)],
+    "mf_mlp_destroy": [_P],
+    "mf_mlp_num_params": [],
+    "mf_mlp_get_params": [_P, _FP],
+    "mf_mlp_set_params": [_P, _FP],
+    "mf_mlp_set_scaling": [_P, _FP, _FP, _FP, _FP, ctypes.c_float, ctypes.c_float],
+    "mf_mlp_train_step": [_P, _P, _P, _P, _P, ctypes.c_longlong, ctypes.c_float, _FP, _FP, _P],
+    "mf_mlp_predict": [_P, _P, ctypes.c_longlong, _P, _P],
+    "mf_les_features": [_P, ctypes.POINTER(_P), _P, _P, _P],
+    "mf_les_sgs_target": [_P, ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.POINTER(_P), _P, _P],
+    "mf_les_nu_mlp": [_P, _P, _D, ctypes.POINTER(_P), _P, ctypes.POINTER(ctypes.c_longlong), _P],
+    "mf_flow_stage": [_I, _I, _I, _D, _D, _D, _D, ctypes.POINTER(_P), ctypes.POINTER(_P),
+                      ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.POINTER(_P), _P],
+    "mf_flow_divergence": [_I, _I, _I, _D, _P, _P, _P, _P, _P],
+    "mf_flow_correct": [_I, _I, _I, _D, ctypes.POINTER(_P), ctypes.POINTER(_P), _P],
+    "mf_flow_products": [_I, _I, _I, ctypes.POINTER(_P), ctypes.POINTER(_P), _P],
+    "mf_flow_curl": [_I, _I, _I, ctypes.POINTER(_P), ctypes.POINTER(_P), _P],
     "mf_solver3d_profile": [_P, _I],
     "mf_solver3d_set_residual": [_P, _I],
     "mf_solver3d_profile_read": [_P, _I, _DP, ctypes.POINTER(ctypes.c_longlong)],
@@ -674,3 +692,161 @@ class LesModel:
             self.close()
         except Exception:
             pass
+
+
+# ---------------------------------------------------------------------------
+# learned LES coefficient and the box flow that generates its training data
+# (no reference counterpart)
+# ---------------------------------------------------------------------------
+
+def _tptr(t, dtype):
+    """Pointer of a contiguous torch CUDA tensor of the given dtype name."""
+    if t is None:
+        return None
+    if str(t.dtype) != "torch." + dtype or not t.is_contiguous():
+        raise TypeError("expected a contiguous %s tensor" % dtype)
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def _ptrs(seq):
+    return (_P * len(seq))(*[_arg(a) for a in seq])
+
+
+MLP_PARAMS = 4673
+
+
+class Mlp:
+    """6-64-64-1 network for the eddy-viscosity coefficient (FP32 on the GPU)."""
+
+    def __init__(self, seed=0):
+        self._h = ctypes.c_void_p()
+        _check(_lib.mf_mlp_create(int(seed), ctypes.byref(self._h)))
+
+    def params(self):
+        p = np.zeros(MLP_PARAMS, dtype=np.float32)
+        _check(_lib.mf_mlp_get_params(self._h, p.ctypes.data_as(_FP)))
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        _check(_lib.mf_mlp_set_params(self._h, p.ctypes.data_as(_FP)))
+
+    def set_scaling(self, mean, istd, lo, hi, cscale, loss_scale):
+        arr = [np.ascontiguousarray(a, dtype=np.float32) for a in (mean, istd, lo, hi)]
+        self.scaling = dict(mean=arr[0], istd=arr[1], lo=arr[2], hi=arr[3], cscale=float(cscale),
+                            loss_scale=float(loss_scale))
+        _check(_lib.mf_mlp_set_scaling(self._h, *[a.ctypes.data_as(_FP) for a in arr],
+                                       float(cscale), float(loss_scale)))
+
+    def train_step(self, X, base, target, idx=None, n=None, lr=1e-3, want_grad=False,
+                   want_loss=False, stream=None):
+        """One fused gradient + Adam step; returns (loss or None, grad or None)."""
+        if n is None:
+            n = idx.numel() if idx is not None else base.numel()
+        g = np.zeros(MLP_PARAMS, dtype=np.float32) if want_grad else None
+        lo = np.zeros(1, dtype=np.float32) if want_loss else None
+        _check(_lib.mf_mlp_train_step(self._h, _tptr(X, "float32"), _tptr(base, "float32"),
+                                      _tptr(target, "float32"), _tptr(idx, "int32"), int(n),
+                                      float(lr), g.ctypes.data_as(_FP) if want_grad else None,
+                                      lo.ctypes.data_as(_FP) if want_loss else None,
+                                      _stream(stream)))
+        return (float(lo[0]) if want_loss else None), g
+
+    def predict(self, X, out=None, stream=None):
+        import torch
+        n = X.shape[0]
+        if out is None:
+            out = torch.empty(n, dtype=torch.float32, device=X.device)
+        _check(_lib.mf_mlp_predict(self._h, _tptr(X, "float32"), n, _tptr(out, "float32"),
+                                   _stream(stream)))
+        return out
+
+    def close(self):
+        if self._h:
+            _lib.mf_mlp_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _les_features(self, du, stream=None):
+    """(X (N, 6) float32, base (N,) float32), N = nx*ny*nz in x-fastest order."""
+    import torch
+    n = self.shape[0] * self.shape[1] * self.shape[2]
+    X = torch.empty((n, 6), dtype=torch.float32, device="cuda")
+    b = torch.empty(n, dtype=torch.float32, device="cuda")
+    _check(_lib.mf_les_features(self._h, _ptrs([du[i][j] for i in range(3) for j in range(3)]),
+                                _tptr(X, "float32"), _tptr(b, "float32"), _stream(stream)))
+    return X, b
+
+
+def _les_sgs_target(self, ub, uu, du, stream=None):
+    import torch
+    n = self.shape[0] * self.shape[1] * self.shape[2]
+    t = torch.empty(n, dtype=torch.float32, device="cuda")
+    _check(_lib.mf_les_sgs_target(self._h, _ptrs(ub), _ptrs(uu),
+                                  _ptrs([du[i][j] for i in range(3) for j in range(3)]),
+                                  _tptr(t, "float32"), _stream(stream)))
+    return t
+
+
+def _les_nu_mlp(self, mlp, c_fallback, du, out=None, count=False, stream=None):
+    """nu with the network coefficient; returns nu, or (nu, fallback points)."""
+    if out is None:
+        out = empty_device(self.shape)
+    cnt = ctypes.c_longlong(0)
+    _check(_lib.mf_les_nu_mlp(self._h, mlp._h, float(c_fallback),
+                              _ptrs([du[i][j] for i in range(3) for j in range(3)]), _arg(out),
+                              ctypes.byref(cnt) if count else None, _stream(stream)))
+    return (out, cnt.value) if count else out
+
+
+LesModel.features = _les_features
+LesModel.sgs_target = _les_sgs_target
+LesModel.nu_mlp = _les_nu_mlp
+
+
+def flow_stage(nu, dt, a, b, u, w, du, ddu, out, stream=None):
+    nx, ny, nz = u[0].shape
+    _check(_lib.mf_flow_stage(nx, ny, nz, float(nu), float(dt), float(a), float(b), _ptrs(u),
+                              _ptrs(w) if w is not None else None,
+                              _ptrs([du[i][j] for i in range(3) for j in range(3)]),
+                              _ptrs([ddu[i][j] for i in range(3) for j in range(3)]), _ptrs(out),
+                              _stream(stream)))
+    return out
+
+
+def flow_divergence(scale, dudx, dvdy, dwdz, out=None, stream=None):
+    nx, ny, nz = dudx.shape
+    if out is None:
+        out = empty_device((nx - 2, ny - 2, nz - 2))
+    _check(_lib.mf_flow_divergence(nx, ny, nz, float(scale), _arg(dudx), _arg(dvdy), _arg(dwdz),
+                                   _arg(out), _stream(stream)))
+    return out
+
+
+def flow_correct(dt, u, dphi, stream=None):
+    nx, ny, nz = u[0].shape
+    _check(_lib.mf_flow_correct(nx, ny, nz, float(dt), _ptrs(u), _ptrs(dphi), _stream(stream)))
+    return u
+
+
+def flow_products(u, out=None, stream=None):
+    nx, ny, nz = u[0].shape
+    if out is None:
+        out = [empty_device((nx, ny, nz)) for _ in range(6)]
+    _check(_lib.mf_flow_products(nx, ny, nz, _ptrs(u), _ptrs(out), _stream(stream)))
+    return out
+
+
+def flow_curl(dpsi, out=None, stream=None):
+    nx, ny, nz = dpsi[0][0].shape
+    if out is None:
+        out = [empty_device((nx, ny, nz)) for _ in range(3)]
+    _check(_lib.mf_flow_curl(nx, ny, nz, _ptrs([dpsi[i][j] for i in range(3) for j in range(3)]),
+                             _ptrs(out), _stream(stream)))
+    return out
