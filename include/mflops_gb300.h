@@ -376,7 +376,7 @@ int mf_les_nu_mlp(mf_les_t* les, const mf_mlp_t* mlp, double c_fallback, const d
 
 /* ------------------------------------------------------------------------
  * Fine-grid box flow that generates the training data (no reference
- * counterpart): pointwise parts of an explicit RK2 + projection step of a
+ * counterpart): pointwise parts of an explicit Runge-Kutta + projection step of a
  * decaying flow in a no-slip box; derivatives and the Neumann Poisson solve
  * come from the entry points above.  Device fields (nx,ny,nz), FP64.
  * ---------------------------------------------------------------------- */

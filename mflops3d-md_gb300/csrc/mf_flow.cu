@@ -1,7 +1,7 @@
 // Fine-grid flow for the learned LES coefficient's training data (no
 // reference counterpart).  A decaying flow in a closed no-slip box, advanced
-// by an explicit two-stage Runge-Kutta method with a pressure projection
-// after every stage; the derivatives are the compact sweeps of mf_der.cu and
+// by an explicit Runge-Kutta method with a pressure projection after every
+// stage; the derivatives are the compact sweeps of mf_der.cu and
 // the projection is a Neumann Poisson solve of mf_solver.cu, so the pairs
 // are generated by the same operators as the rest of the path.  The kernels
 // here are the pointwise parts of one stage (all FP64):

@@ -25,6 +25,35 @@ __device__ __forceinline__ bool on_edge(int i, int j, int k, int nx, int ny, int
   return e >= 2;
 }
 
+__device__ __forceinline__ void load_grad(const LesGrad& d, long long idx, double g[3][3]) {
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b) g[a][b] = d.g[3 * a + b][idx];
+}
+
+// S:S and the Smagorinsky-form value c sqrt(2 S:S) Delta^2 with every
+// rounding spelled out (no compiler contraction), so that every kernel that
+// evaluates the plain model produces the same bits.
+__device__ __forceinline__ double strain_ss(const double g[3][3]) {
+  double ss = 0.0;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    ss = __fma_rn(g[a][a], g[a][a], ss);
+#pragma unroll
+    for (int b = a + 1; b < 3; ++b) {
+      const double s = __dadd_rn(g[a][b], g[b][a]);
+      ss = __fma_rn(__dmul_rn(0.5, s), s, ss);
+    }
+  }
+  return ss;
+}
+
+__device__ __forceinline__ double smag_nu(double c, double ss, double dx2, double dy2, double dz2) {
+  const double v = __dmul_rn(c, __dsqrt_rn(__dmul_rn(2.0, ss)));
+  return __dmul_rn(v, __ddiv_rn(__dadd_rn(__dadd_rn(dx2, dy2), dz2), 3.0));
+}
+
 __global__ void k_les_nu(LesGrad d, const double* __restrict__ dx2, const double* __restrict__ dy2,
                          const double* __restrict__ dz2, int nx, int ny, int nz, int type, double c,
                          double* __restrict__ nu) {
@@ -44,15 +73,10 @@ __global__ void k_les_nu(LesGrad d, const double* __restrict__ dx2, const double
     for (int b = 0; b < 3; ++b) g[a][b] = d.g[3 * a + b][idx];
   double v = 0.0;
   if (type == 1 || type == 2) {
-    double ss = 0.0;
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      ss += g[a][a] * g[a][a];
-#pragma unroll
-      for (int b = a + 1; b < 3; ++b) ss += 0.5 * (g[a][b] + g[b][a]) * (g[a][b] + g[b][a]);
-    }
+    const double ss = strain_ss(g);
     if (type == 1) {
-      v = c * sqrt(2.0 * ss);
+      nu[idx] = smag_nu(c, ss, dx2[i], dy2[j], dz2[k]);
+      return;
     } else {
       double g2[3][3];
 #pragma unroll
@@ -75,7 +99,7 @@ __global__ void k_les_nu(LesGrad d, const double* __restrict__ dx2, const double
         v = 0.0;
       } else {
         const double rsd = sqrt(sd), rss = sqrt(ss);
-        v = c * (sd * rsd) / (ss * ss * rss + rsd * sqrt(rsd));
+        v = c * (sd * rsd) / (ss * ss * rss + sd * sqrt(rsd));  // sd^1.25 = sd sd^(1/4)
       }
     }
   } else {
@@ -108,24 +132,6 @@ __global__ void k_les_nu(LesGrad d, const double* __restrict__ dx2, const double
     v = (s1 < kLesThresh) ? 0.0 : c * s3 * (s1 - s2) * (s2 - s3) / (s1 * s1);
   }
   nu[idx] = v * ((dx2[i] + dy2[j] + dz2[k]) / 3.0);
-}
-
-__device__ __forceinline__ void load_grad(const LesGrad& d, long long idx, double g[3][3]) {
-#pragma unroll
-  for (int a = 0; a < 3; ++a)
-#pragma unroll
-    for (int b = 0; b < 3; ++b) g[a][b] = d.g[3 * a + b][idx];
-}
-
-__device__ __forceinline__ double strain_ss(const double g[3][3]) {
-  double ss = 0.0;
-#pragma unroll
-  for (int a = 0; a < 3; ++a) {
-    ss += g[a][a] * g[a][a];
-#pragma unroll
-    for (int b = a + 1; b < 3; ++b) ss += 0.5 * (g[a][b] + g[b][a]) * (g[a][b] + g[b][a]);
-  }
-  return ss;
 }
 
 // Training inputs of the learned coefficient: the six invariant features
@@ -224,8 +230,7 @@ __global__ void __launch_bounds__(128) k_les_nu_mlp(LesGrad d, const double* __r
   } else if (n_fallback) {
     atomicAdd(n_fallback, 1ull);
   }
-  const double v = c * sqrt(2.0 * ss);
-  nu[idx] = v * ((dx2[i] + dy2[j] + dz2[k]) / 3.0);
+  nu[idx] = smag_nu(c, ss, dx2[i], dy2[j], dz2[k]);
 }
 
 }  // namespace mf

@@ -8,7 +8,7 @@ Pipeline, every step on the GPU through the library's entry points:
 1. ``BoxFlow``: a decaying flow in the no-slip unit box on a uniform fine
    grid.  Initial condition u = curl(e psi), psi = two Helmholtz smoothings
    of white noise (the 3-D solver with Dirichlet faces) and e a wall envelope;
-   time stepping by explicit two-stage Runge-Kutta (Heun) with a projection
+   time stepping by explicit three-stage SSP Runge-Kutta with a projection
    after each stage (compact derivatives, Neumann Poisson solve).
 2. ``PairMaker.pairs``: F(u_i) and F(u_i u_j) on the LES grid with the
    least-squares spline filter (knots at the LES nodes), the gradients of
@@ -106,14 +106,20 @@ class BoxFlow:
                 self.dc.apply(j, 2, u[i], out=self.ddu[i][j])
 
     def step(self, dt):
-        """Heun: u1 = P(u + dt R(u)), u <- P(u/2 + (u1 + dt R(u1))/2)."""
+        """Three-stage strong-stability-preserving Runge-Kutta (Shu & Osher):
+        u1 = P(u + dt R(u)), u2 = P(3/4 u + 1/4 (u1 + dt R(u1))),
+        u <- P(1/3 u + 2/3 (u2 + dt R(u2))); stable for centred advection up
+        to |lambda dt| = sqrt(3), where two-stage methods are not."""
         self._grads(self.u)
         mf.flow_stage(self.nu, dt, 0.0, 1.0, self.u, None, self.du, self.ddu, self.u1)
         self.project(self.u1)
         self._grads(self.u1)
-        mf.flow_stage(self.nu, dt, 0.5, 0.5, self.u1, self.u, self.du, self.ddu, self.u2)
+        mf.flow_stage(self.nu, dt, 0.75, 0.25, self.u1, self.u, self.du, self.ddu, self.u2)
         self.project(self.u2)
-        self.u, self.u2 = self.u2, self.u
+        self._grads(self.u2)
+        mf.flow_stage(self.nu, dt, 1.0 / 3.0, 2.0 / 3.0, self.u2, self.u, self.du, self.ddu, self.u1)
+        self.project(self.u1)
+        self.u, self.u1 = self.u1, self.u
         self.time += dt
 
     def cfl_dt(self, cfl=0.3):
