@@ -546,6 +546,25 @@ def row_measurements(mf, torch, hbm):
     for name, t in (("smagorinsky", 1), ("wale", 2), ("sigma", 3)):
         ms = time_fn(lambda: les.nu_velocity(*dcs, *vel, t, 0.18), reps=10)
         out["les_%s_96x97x96" % name] = {"us": ms * 1e3}
+    # learned coefficient: one fused training step (gradient of 65,536 points
+    # + Adam; about 3 x 9,088 flop per point for forward and backward) and
+    # the fused inference with fallback on the LES grid, beside the plain
+    # Smagorinsky kernel on the same gradients
+    gen = torch.Generator("cuda").manual_seed(50)
+    npts = 1 << 16
+    X = torch.rand((npts, 6), device="cuda", generator=gen, dtype=torch.float32) * 2 - 1
+    b = torch.rand(npts, device="cuda", generator=gen, dtype=torch.float32)
+    t = 0.02 * b * (1 + X[:, 0])
+    mlp = mf.Mlp(0)
+    inf = np.full(6, np.inf, np.float32)
+    mlp.set_scaling(np.zeros(6), np.ones(6), -inf, inf, 0.02, 1000.0)
+    ms = time_fn(lambda: mlp.train_step(X, b, t, lr=1e-3), reps=50)
+    out["les_mlp_train_step_65536pts"] = {"ms": ms, "TFLOP_per_s": 3 * 9088 * npts / (ms * 1e-3) / 1e12}
+    du = [[field(shape, 60 + 3 * i + j) for j in range(3)] for i in range(3)]
+    ms_m = time_fn(lambda: les.nu_mlp(mlp, 0.027, du), reps=20)
+    ms_p = time_fn(lambda: les.nu(du, 1, 0.027), reps=20)
+    out["les_nu_mlp_96x97x96"] = {"us": ms_m * 1e3, "plain_smagorinsky_us": ms_p * 1e3,
+                                  "network_TFLOP_per_s": 9088 * 96 * 97 * 96 / (ms_m * 1e-3) / 1e12}
     return out
 
 

@@ -10,8 +10,9 @@ Pipeline, every step on the GPU through the library's entry points:
    of white noise (the 3-D solver with Dirichlet faces) and e a wall envelope;
    time stepping by explicit three-stage SSP Runge-Kutta with a projection
    after each stage (compact derivatives, Neumann Poisson solve).
-2. ``PairMaker.pairs``: F(u_i) and F(u_i u_j) on the LES grid with the
-   least-squares spline filter (knots at the LES nodes), the gradients of
+2. ``PairMaker.pairs``: F(u_i) and F(u_i u_j) on the LES grid (a
+   differential filter on the fine grid through the Helmholtz solver, then
+   the least-squares spline filter with knots at the LES nodes), the gradients of
    F(u) with the LES grid's compact derivatives, then the features, the
    factor b = Delta^2 sqrt(2 S:S) and the target nu = -tau^d:S / (2 S:S).
 3. ``fit``: standardisation from the training pairs, cscale = the best
@@ -122,6 +123,20 @@ class BoxFlow:
         self.u, self.u1 = self.u1, self.u
         self.time += dt
 
+    def run(self, steps, cfl=0.3, every=0, callback=None):
+        """Advance `steps` steps at the given CFL number; callback(self, step)
+        every `every` steps.  Raises when the flow leaves its decaying regime
+        (a grid too coarse for the viscosity)."""
+        ke0 = self.stats()[0]
+        for it in range(1, steps + 1):
+            self.step(self.cfl_dt(cfl))
+            if every and it % every == 0:
+                ke = self.stats()[0]
+                if not np.isfinite(ke) or ke > 2.0 * ke0:
+                    raise RuntimeError("box flow unstable at step %d (kinetic energy %g)" % (it, ke))
+                if callback is not None:
+                    callback(self, it)
+
     def cfl_dt(self, cfl=0.3):
         umax = max(float(c.abs().max()) for c in self.u)
         return cfl * (self.grid[1] - self.grid[0]) / max(umax, 1e-12)
@@ -135,9 +150,19 @@ class BoxFlow:
 
 
 class PairMaker:
-    """Filters fine fields to an LES grid and forms training pairs there."""
+    """Filters fine fields to an LES grid and forms training pairs there.
 
-    def __init__(self, fine_grid, nc, margin=2, k=3):
+    The filter is a positive smoothing kernel followed by the transfer to the
+    LES grid: the differential filter v = (1 - Delta^2/24 lap)^-1 f on the
+    fine grid (one Helmholtz solve, (lap + s) v = s f with s = -24/Delta^2,
+    zero on the no-slip walls where velocities and their products vanish),
+    Delta = width x the LES spacing, then the least-squares spline filter to
+    the LES nodes.  The spline filter alone is a projection whose kernel has
+    negative lobes: on a cascading flow its subgrid dissipation comes out
+    with either sign at about half of the points and uncorrelated with the
+    strain, which leaves nothing to learn."""
+
+    def __init__(self, fine_grid, nc, margin=3, k=3, width=2.0):
         self.fine = np.asarray(fine_grid, dtype=np.float64)
         self.nc = nc
         self.coarse = uniform_grid(nc)
@@ -145,9 +170,23 @@ class PairMaker:
         self.dc = mf.DerivativesCoefficients(self.coarse, so=6)
         self.les = mf.LesModel(self.coarse, self.coarse, self.coarse)
         self.margin = margin
+        g = self.fine
+        delta = width * (self.coarse[1] - self.coarse[0])
+        self.sigma = -24.0 / (delta * delta)
+        self.smoother = mf.SolverCoeffs3D(g, g, g, (1,) * 6, 6)
+        n, m = g.size, g.size - 2
+        self.zero_bc = [mf.empty_device((m, m, 2)) for _ in range(3)]
+        self.r = mf.empty_device((m, m, m))
+        self.v = mf.empty_device((n, n, n))
+
+    def smooth(self, f):
+        self.r.copy_(f[1:-1, 1:-1, 1:-1])
+        self.r.mul_(self.sigma)
+        self.smoother.solve_3d(self.r, self.sigma, self.v, *self.zero_bc)
+        return self.v
 
     def filter3(self, f):
-        a = self.filt.apply(f, 0)
+        a = self.filt.apply(self.smooth(f), 0)
         b = self.filt.apply(a, 1)
         return self.filt.apply(b, 2)
 
