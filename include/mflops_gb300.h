@@ -330,8 +330,9 @@ int mf_les_nu_velocity(mf_les_t* les, const mf_der_t* dcx, const mf_der_t* dcy,
  * maps six invariants of the resolved velocity gradient,
  *   S:S/G2, tr(S^3)/G2^1.5, tr(W^2 S)/G2^1.5, tr(W^2 S^2)/G2^2,
  *   det(g)/G2^1.5, tr(g)/G2^0.5            (G2 = g:g),
- * to C(x) in nu_t = C(x) Delta^2 sqrt(2 S:S).  Outside the training range of
- * the features the plain Smagorinsky model is used per point.
+ * to C(x) in nu_t = C(x) Delta^2 sqrt(2 S:S).  Features and network are FP32.
+ * Outside the training range of the features (or where g:g leaves
+ * (1e-30, 1e30)) the plain Smagorinsky model is used per point.
  * ---------------------------------------------------------------------- */
 typedef struct mf_mlp mf_mlp_t;
 

@@ -145,7 +145,7 @@ __global__ void k_les_features(LesGrad d, const double* __restrict__ dx2, const 
   const int i = (int)(idx % nx);
   const long long jk = idx / nx;
   const int j = (int)(jk % ny), k = (int)(jk / ny);
-  double f[kMlpIn] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  float f[kMlpIn] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
   double b = 0.0;
   if (!on_edge(i, j, k, nx, ny, nz)) {
     double g[3][3];
@@ -153,7 +153,7 @@ __global__ void k_les_features(LesGrad d, const double* __restrict__ dx2, const 
     if (grad_features(g, f)) b = sqrt(2.0 * strain_ss(g)) * ((dx2[i] + dy2[j] + dz2[k]) / 3.0);
   }
 #pragma unroll
-  for (int q = 0; q < kMlpIn; ++q) X[idx * kMlpIn + q] = (float)f[q];
+  for (int q = 0; q < kMlpIn; ++q) X[idx * kMlpIn + q] = f[q];
   base[idx] = (float)b;
 }
 
@@ -221,7 +221,7 @@ __global__ void __launch_bounds__(128) k_les_nu_mlp(LesGrad d, const double* __r
   double g[3][3];
   load_grad(d, idx, g);
   const double ss = strain_ss(g);
-  double f[kMlpIn];
+  float f[kMlpIn];
   float x[kMlpIn];
   double c = c_fallback;
   const bool in = grad_features(g, f) && mlp_input(s, f, x);

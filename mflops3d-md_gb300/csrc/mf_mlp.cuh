@@ -11,8 +11,7 @@
 //   f0 = S:S / G2            f1 = tr(S^3) / G2^1.5    f2 = tr(W^2 S) / G2^1.5
 //   f3 = tr(W^2 S^2) / G2^2  f4 = det(g) / G2^1.5     f5 = tr(g) / G2^0.5
 // all invariant under rotations and under scaling of g, and bounded in
-// magnitude by 1 (f5 by sqrt(3)).  They are computed in FP64 and rounded to
-// FP32; the network runs in FP32.
+// magnitude by 1 (f5 by sqrt(3)).  Features and network run in FP32.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -38,23 +37,31 @@ struct MlpScaling {
   float cscale;                      // C = cscale * network output
 };
 
-// Invariant features of one gradient tensor; false when g vanishes.
-__device__ __forceinline__ bool grad_features(const double g[3][3], double f[kMlpIn]) {
-  double g2 = 0.0;
+// Invariant features of one gradient tensor (FP32 arithmetic on the FP32
+// rounding of g: the features only feed the FP32 network, and FP64 would
+// cost about 240 operations per point on the narrow FP64 pipe); false when
+// g:g lies outside (1e-30, 1e30), where the point falls back.
+__device__ __forceinline__ bool grad_features(const double gd[3][3], float f[kMlpIn]) {
+  float g[3][3];
 #pragma unroll
   for (int a = 0; a < 3; ++a)
 #pragma unroll
-    for (int b = 0; b < 3; ++b) g2 += g[a][b] * g[a][b];
-  if (!(g2 > 1e-300)) return false;
-  double S[3][3], W[3][3];
+    for (int b = 0; b < 3; ++b) g[a][b] = (float)gd[a][b];
+  float g2 = 0.f;
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b) g2 = fmaf(g[a][b], g[a][b], g2);
+  if (!(g2 > 1e-30f) || !(g2 < 1e30f)) return false;
+  float S[3][3], W[3][3];
 #pragma unroll
   for (int a = 0; a < 3; ++a)
 #pragma unroll
     for (int b = 0; b < 3; ++b) {
-      S[a][b] = 0.5 * (g[a][b] + g[b][a]);
-      W[a][b] = 0.5 * (g[a][b] - g[b][a]);
+      S[a][b] = 0.5f * (g[a][b] + g[b][a]);
+      W[a][b] = 0.5f * (g[a][b] - g[b][a]);
     }
-  double S2[3][3], W2[3][3];
+  float S2[3][3], W2[3][3];
 #pragma unroll
   for (int a = 0; a < 3; ++a)
 #pragma unroll
@@ -62,26 +69,26 @@ __device__ __forceinline__ bool grad_features(const double g[3][3], double f[kMl
       S2[a][b] = S[a][0] * S[0][b] + S[a][1] * S[1][b] + S[a][2] * S[2][b];
       W2[a][b] = W[a][0] * W[0][b] + W[a][1] * W[1][b] + W[a][2] * W[2][b];
     }
-  double ss = 0.0, s3 = 0.0, w2s = 0.0, w2s2 = 0.0;
+  float ss = 0.f, s3 = 0.f, w2s = 0.f, w2s2 = 0.f;
 #pragma unroll
   for (int a = 0; a < 3; ++a)
 #pragma unroll
     for (int b = 0; b < 3; ++b) {
-      ss += S[a][b] * S[a][b];
-      s3 += S2[a][b] * S[b][a];
-      w2s += W2[a][b] * S[b][a];
-      w2s2 += W2[a][b] * S2[b][a];
+      ss = fmaf(S[a][b], S[a][b], ss);
+      s3 = fmaf(S2[a][b], S[b][a], s3);
+      w2s = fmaf(W2[a][b], S[b][a], w2s);
+      w2s2 = fmaf(W2[a][b], S2[b][a], w2s2);
     }
-  const double det = g[0][0] * (g[1][1] * g[2][2] - g[1][2] * g[2][1]) -
-                     g[0][1] * (g[1][0] * g[2][2] - g[1][2] * g[2][0]) +
-                     g[0][2] * (g[1][0] * g[2][1] - g[1][1] * g[2][0]);
-  const double r = sqrt(g2), r3 = g2 * r;
-  f[0] = ss / g2;
-  f[1] = s3 / r3;
-  f[2] = w2s / r3;
-  f[3] = w2s2 / (g2 * g2);
-  f[4] = det / r3;
-  f[5] = (g[0][0] + g[1][1] + g[2][2]) / r;
+  const float det = g[0][0] * (g[1][1] * g[2][2] - g[1][2] * g[2][1]) -
+                    g[0][1] * (g[1][0] * g[2][2] - g[1][2] * g[2][0]) +
+                    g[0][2] * (g[1][0] * g[2][1] - g[1][1] * g[2][0]);
+  const float ig2 = 1.f / g2, ir = rsqrtf(g2), ir3 = ig2 * ir;
+  f[0] = ss * ig2;
+  f[1] = s3 * ir3;
+  f[2] = w2s * ir3;
+  f[3] = w2s2 * ig2 * ig2;
+  f[4] = det * ir3;
+  f[5] = (g[0][0] + g[1][1] + g[2][2]) * ir;
   return true;
 }
 
@@ -115,11 +122,11 @@ __device__ __forceinline__ float mlp_forward(const float* __restrict__ P, const 
 }
 
 // Standardised network input from raw features; false outside the range.
-__device__ __forceinline__ bool mlp_input(const MlpScaling& s, const double f[kMlpIn], float x[kMlpIn]) {
+__device__ __forceinline__ bool mlp_input(const MlpScaling& s, const float f[kMlpIn], float x[kMlpIn]) {
   bool in = true;
 #pragma unroll
   for (int k = 0; k < kMlpIn; ++k) {
-    const float v = (float)f[k];
+    const float v = f[k];
     in = in && (v >= s.lo[k]) && (v <= s.hi[k]);
     x[k] = (v - s.mean[k]) * s.istd[k];
   }

@@ -42,7 +42,7 @@ def features(g):
     """g: (..., 3, 3) -> (features (..., 6), valid (...))."""
     g = np.asarray(g, dtype=np.float64)
     g2 = np.einsum('...ij,...ij', g, g)
-    valid = g2 > 1e-300
+    valid = (g2 > 1e-30) & (g2 < 1e30)
     g2s = np.where(valid, g2, 1.0)
     S = 0.5 * (g + np.swapaxes(g, -1, -2))
     W = 0.5 * (g - np.swapaxes(g, -1, -2))

@@ -6,7 +6,7 @@ its features' invariance under rotations and scaling of the gradient, and
 Adam's first step against its closed form.  GPU, through the C ABI: the
 fused gradient kernel against the oracle (FP32 kernel vs FP64 oracle:
 max |g - g_ref| <= 2e-4 max |g_ref|, loss within 1e-4), Adam steps, the
-prediction kernel (1e-5), features (1e-6 absolute, FP32 rounding of values
+prediction kernel (1e-5), features (5e-6 absolute: FP32 arithmetic on values
 bounded by sqrt(3)) and SGS target (1e-5 relative) against the oracle, and
 the fused viscosity kernel: network points within 2e-5 of the oracle,
 fallback points bit-identical to the plain Smagorinsky kernel."""
@@ -185,7 +185,7 @@ def test_features_and_target_match_oracle(mf, gpu):
     edge = L.zero_edges(np.ones(shape)) == 0
     f[edge] = 0.0
     bref = np.where(edge, 0.0, np.sqrt(2 * O.strain_ss(g)) * O.delta2(gx, gy, gz))
-    assert np.max(np.abs(X - f)) < 1e-6
+    assert np.max(np.abs(X - f)) < 5e-6
     assert max_rel(b, bref) < 1e-6
     ub = [field(shape, 50 + q) for q in range(3)]
     uu = [field(shape, 60 + q) for q in range(6)]
@@ -201,9 +201,12 @@ def test_nu_mlp_matches_oracle_with_fallback(mf, gpu):
     p = random_params(17, scale=0.5)
     f, _ = O.features(O.grad_tensor(du))
     # training range: the central part of each feature's spread, so that a
-    # good share of the points falls back
-    lo = np.quantile(f.reshape(-1, 6), 0.05, axis=0).astype(np.float32)
-    hi = np.quantile(f.reshape(-1, 6), 0.95, axis=0).astype(np.float32)
+    # good share of the points falls back; each limit lies midway between two
+    # neighbouring feature values, far from both next to FP32 rounding
+    fs = np.sort(f.reshape(-1, 6), axis=0)
+    q0, q1 = int(0.05 * len(fs)), int(0.95 * len(fs))
+    lo = (0.5 * (fs[q0] + fs[q0 + 1])).astype(np.float32)
+    hi = (0.5 * (fs[q1] + fs[q1 + 1])).astype(np.float32)
     m = make_mlp(mf, p, lo, hi)
     les = mf.LesModel(gx, gy, gz)
     ddu = [[mf.to_device(du[i][j]) for j in range(3)] for i in range(3)]
