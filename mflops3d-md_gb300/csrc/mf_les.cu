@@ -5,11 +5,13 @@
 // class_field.f90:366-391; gradients on edges count as zero as well).
 // 72 bytes read + 8 written per point: HBM-bound except the sigma model's
 // FP64 acos/cos, which the narrow FP64 pipe of GB300 makes compute-heavy.
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
 #include "mf_internal.h"
 #include "mf_mlp.cuh"
+#include "mf_tcgen05.cuh"
 
 namespace mf {
 
@@ -34,7 +36,8 @@ __device__ __forceinline__ void load_grad(const LesGrad& d, long long idx, doubl
 
 // S:S and the Smagorinsky-form value c sqrt(2 S:S) Delta^2 with every
 // rounding spelled out (no compiler contraction), so that every kernel that
-// evaluates the plain model produces the same bits.
+// evaluates the plain model produces the same bits.  Delta^2 uses the
+// rounded 1/3 (within an ulp of the division by 3).
 __device__ __forceinline__ double strain_ss(const double g[3][3]) {
   double ss = 0.0;
 #pragma unroll
@@ -49,9 +52,21 @@ __device__ __forceinline__ double strain_ss(const double g[3][3]) {
   return ss;
 }
 
+// sqrt(x) from an FP32 seed and one Newton (Heron) step in FP64,
+// y1 = y0 + (x - y0^2) / (2 y0) with the reciprocal taken in FP32: about
+// 2^-48 relative, against ~20 FP64 operations for the correctly rounded
+// square root on the narrow FP64 pipe.  Outside the FP32 range, sqrt().
+__device__ __forceinline__ double sqrt_heron(double x) {
+  if (!(x > 1e-30 && x < 1e30)) return x > 0.0 ? sqrt(x) : 0.0;
+  const float y0f = sqrtf((float)x);
+  const double y0 = (double)y0f;
+  const double r = __fma_rn(-y0, y0, x);
+  return __fma_rn(r, (double)(0.5f / y0f), y0);
+}
+
 __device__ __forceinline__ double smag_nu(double c, double ss, double dx2, double dy2, double dz2) {
-  const double v = __dmul_rn(c, __dsqrt_rn(__dmul_rn(2.0, ss)));
-  return __dmul_rn(v, __ddiv_rn(__dadd_rn(__dadd_rn(dx2, dy2), dz2), 3.0));
+  const double v = __dmul_rn(c, sqrt_heron(__dmul_rn(2.0, ss)));
+  return __dmul_rn(v, __dmul_rn(__dadd_rn(__dadd_rn(dx2, dy2), dz2), 1.0 / 3.0));
 }
 
 __global__ void k_les_nu(LesGrad d, const double* __restrict__ dx2, const double* __restrict__ dy2,
@@ -197,40 +212,161 @@ __global__ void k_sgs_target(SgsFields s, LesGrad d, int nx, int ny, int nz, flo
 
 // Learned-coefficient eddy viscosity with per-point fallback: where all six
 // features lie inside the training range nu = max(C(x), 0) Delta^2 sqrt(2 S:S)
-// with C from the network (FP32, parameters staged in shared memory), else the
-// plain Smagorinsky value with coefficient c_fallback, bit-identical to
-// k_les_nu type 1.  Edge lines are zero.
+// with C from the network, else the plain Smagorinsky value with coefficient
+// c_fallback, bit-identical to k_les_nu type 1 (smag_nu).  Edge lines are 0.
+//
+// The 64x64 hidden layer runs on the tensor cores, 128 points per tile
+// (persistent CTAs, two per SM): every thread computes its point's strain
+// (FP64), features and first layer (FP32) and writes its h1 row, split
+// 3xTF32 (hi = h1 as stored, the hardware keeps its TF32 part; lo = the
+// rounded remainder), into 128-byte-swizzled K-major tiles; one thread issues
+// 24 tcgen05.mma (128 x 64 x 8: hi*hi + lo*hi + hi*lo over 8 K steps) against
+// W2 tiles staged once per CTA, FP32 accumulation in 64 TMEM columns; every
+// warp reads its 32 lanes back (tcgen05.ld) for the 64 -> 1 output layer.
+// Accuracy ~1e-6 relative, like the FP32 CUDA-core network.
+constexpr uint32_t kNuTcA = 0, kNuTcALo = 32768, kNuTcB = 65536, kNuTcBLo = 81920, kNuTcP = 98304;
+constexpr uint32_t kNuTcBar = kNuTcP + 2320, kNuTcSlot = kNuTcP + 2336;
+constexpr size_t kNuTcSmem = kNuTcP + 2344 + 1024;  // + alignment slack
+
+// Byte offset of FP32 element (row, k) in a K-major 128-byte-swizzled tile
+// of `rows` rows and K = 64 (two 32-wide K blocks of rows x 128 bytes).
+__device__ __forceinline__ uint32_t sw128(int rows, int row, int k) {
+  return (uint32_t)(k >> 5) * rows * 128 + (row >> 3) * 1024 + (row & 7) * 128 +
+         ((((k >> 2) & 7) ^ (row & 7)) << 4) + ((k & 3) << 2);
+}
+
 __global__ void __launch_bounds__(128) k_les_nu_mlp(LesGrad d, const double* __restrict__ dx2,
                                                     const double* __restrict__ dy2,
                                                     const double* __restrict__ dz2, int nx, int ny, int nz,
                                                     const float* __restrict__ params, MlpScaling s,
                                                     double c_fallback, double* __restrict__ nu,
-                                                    unsigned long long* __restrict__ n_fallback) {
-  extern __shared__ __align__(16) float sp[];
-  for (int q = threadIdx.x; q < kMlpParams; q += blockDim.x) sp[q] = params[q];
+                                                    unsigned long long* __restrict__ n_fallback,
+                                                    int* __restrict__ err) {
+  using namespace tcg;
+  extern __shared__ uint8_t smraw[];
+  uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~uintptr_t(1023));
+  float* Ps = reinterpret_cast<float*>(sm + kNuTcP);  // W1[384], b1[64], b2[64], w3[64], b3
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + kNuTcBar);
+  uint32_t* slot = reinterpret_cast<uint32_t*>(sm + kNuTcSlot);
+  const int t = threadIdx.x, warp = t >> 5;
+  for (int q = t; q < kMlpW2; q += 128) Ps[q] = params[q];  // W1, b1
+  for (int q = t; q < kMlpH; q += 128) {
+    Ps[448 + q] = params[kMlpB2 + q];
+    Ps[512 + q] = params[kMlpW3 + q];
+  }
+  if (t == 0) Ps[576] = params[kMlpB3];
+  for (int e = t; e < kMlpH * kMlpH; e += 128) {
+    const float w = params[kMlpW2 + e];
+    const uint32_t off = sw128(64, e >> 6, e & 63);
+    *reinterpret_cast<float*>(sm + kNuTcB + off) = w;
+    *reinterpret_cast<float*>(sm + kNuTcBLo + off) = tf32_lo(w);
+  }
+  if (t == 0) {
+    mbar_init(bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)),
+                 "r"(64));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  fence_before();
   __syncthreads();
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= (long long)nx * ny * nz) return;
-  const int i = (int)(idx % nx);
-  const long long jk = idx / nx;
-  const int j = (int)(jk % ny), k = (int)(jk / ny);
-  if (on_edge(i, j, k, nx, ny, nz)) {
-    nu[idx] = 0.0;
-    return;
+  fence_after();
+  const uint32_t tmem = *slot;
+  const uint32_t idesc = instr_desc(128, 64, true);
+  const long long tot = (long long)nx * ny * nz;
+  const long long ntiles = (tot + 127) / 128;
+  uint32_t phase = 0;
+  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const long long idx = tile * 128 + t;
+    const bool live = idx < tot;
+    int i = 0, j = 0, k = 0;
+    if (live) {
+      i = (int)(idx % nx);
+      const long long jk = idx / nx;
+      j = (int)(jk % ny);
+      k = (int)(jk / ny);
+    }
+    const bool edge = live && on_edge(i, j, k, nx, ny, nz);
+    double ss = 0.0;
+    bool in = false;
+    float h1[kMlpH];
+#pragma unroll
+    for (int q = 0; q < kMlpH; ++q) h1[q] = 0.f;
+    if (live && !edge) {
+      double g[3][3];
+      load_grad(d, idx, g);
+      ss = strain_ss(g);
+      float f[kMlpIn], x[kMlpIn];
+      in = grad_features(g, f) && mlp_input(s, f, x);
+      if (in) {
+#pragma unroll
+        for (int q = 0; q < kMlpH; ++q) {
+          float a = Ps[kMlpB1 + q];
+#pragma unroll
+          for (int m = 0; m < kMlpIn; ++m) a = fmaf(Ps[q * kMlpIn + m], x[m], a);
+          h1[q] = fmaxf(a, 0.f);
+        }
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < kMlpH / 4; ++c) {
+      const uint32_t off = sw128(128, t, 4 * c);
+      *reinterpret_cast<float4*>(sm + kNuTcA + off) = make_float4(h1[4 * c], h1[4 * c + 1], h1[4 * c + 2], h1[4 * c + 3]);
+      *reinterpret_cast<float4*>(sm + kNuTcALo + off) =
+          make_float4(tf32_lo(h1[4 * c]), tf32_lo(h1[4 * c + 1]), tf32_lo(h1[4 * c + 2]), tf32_lo(h1[4 * c + 3]));
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (t == 0) {
+      fence_after();
+      const uint32_t a0 = smem_u32(sm + kNuTcA), al = smem_u32(sm + kNuTcALo);
+      const uint32_t b0 = smem_u32(sm + kNuTcB), bl = smem_u32(sm + kNuTcBLo);
+#pragma unroll
+      for (int kb = 0; kb < 2; ++kb)
+#pragma unroll
+        for (int ks = 0; ks < 4; ++ks) {
+          const uint32_t ao = kb * 16384 + ks * 32, bo = kb * 8192 + ks * 32;
+          mma<true>(tmem, smem_desc(a0 + ao), smem_desc(b0 + bo), idesc, (kb | ks) != 0);
+          mma<true>(tmem, smem_desc(al + ao), smem_desc(b0 + bo), idesc, 1);
+          mma<true>(tmem, smem_desc(a0 + ao), smem_desc(bl + bo), idesc, 1);
+        }
+      mma_commit(bar);
+    }
+    const bool ok = mbar_wait(bar, phase, err, 0);
+    phase ^= 1u;
+    fence_after();
+    float a2[kMlpH];
+    tmem_load32(tmem + ((uint32_t)(warp * 32) << 16), a2);
+    tmem_load32(tmem + ((uint32_t)(warp * 32) << 16) + 32, a2 + 32);
+    if (!ok) break;
+    if (live) {
+      if (edge) {
+        nu[idx] = 0.0;
+      } else {
+        double c = c_fallback;
+        if (in) {
+          float y = Ps[576];
+#pragma unroll
+          for (int q = 0; q < kMlpH; ++q) y = fmaf(Ps[512 + q], fmaxf(a2[q] + Ps[448 + q], 0.f), y);
+          c = (double)fmaxf(s.cscale * y, 0.f);
+        } else if (n_fallback) {
+          atomicAdd(n_fallback, 1ull);
+        }
+        nu[idx] = smag_nu(c, ss, dx2[i], dy2[j], dz2[k]);
+      }
+    }
+    fence_before();
+    __syncthreads();
   }
-  double g[3][3];
-  load_grad(d, idx, g);
-  const double ss = strain_ss(g);
-  float f[kMlpIn];
-  float x[kMlpIn];
-  double c = c_fallback;
-  const bool in = grad_features(g, f) && mlp_input(s, f, x);
-  if (in) {
-    c = (double)fmaxf(s.cscale * mlp_forward(sp, x), 0.f);
-  } else if (n_fallback) {
-    atomicAdd(n_fallback, 1ull);
+  fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(64));
   }
-  nu[idx] = smag_nu(c, ss, dx2[i], dy2[j], dz2[k]);
 }
 
 }  // namespace mf
@@ -242,6 +378,7 @@ struct mf_les {
   DevBuf d2[3];  // squared spacings per axis
   DevBuf grad;   // nine gradient fields for mf_les_nu_velocity
   DevBuf count;  // fallback counter of mf_les_nu_mlp
+  DevBuf err;    // bounded-wait flag of the tensor-core kernel
 };
 
 extern "C" {
@@ -281,6 +418,7 @@ int mf_les_destroy(mf_les_t* les) {
   for (auto& b : les->d2) b.release();
   les->grad.release();
   les->count.release();
+  les->err.release();
   delete les;
   return MF_OK;
 }
@@ -386,14 +524,23 @@ int mf_les_nu_mlp(mf_les_t* les, const mf_mlp_t* mlp, double c_fallback, const d
     MF_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), st));
   }
   const long long tot = (long long)les->n[0] * les->n[1] * les->n[2];
-  k_les_nu_mlp<<<(unsigned)((tot + 127) / 128), 128, sizeof(float) * kMlpParams, st>>>(
-      d, les->d2[0].as<double>(), les->d2[1].as<double>(), les->d2[2].as<double>(), les->n[0], les->n[1],
-      les->n[2], mlp_device_params(mlp), mlp_scaling(mlp), c_fallback, nu, cnt);
+  if ((rc = les->err.ensure(sizeof(int)))) return rc;
+  MF_CUDA(cudaMemsetAsync(les->err.ptr, 0, sizeof(int), st));
+  const long long tiles = (tot + 127) / 128;
+  const unsigned grid = (unsigned)std::min<long long>(tiles, 2LL * num_sms());
+  MF_CUDA(cudaFuncSetAttribute(k_les_nu_mlp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kNuTcSmem));
+  k_les_nu_mlp<<<grid, 128, kNuTcSmem, st>>>(d, les->d2[0].as<double>(), les->d2[1].as<double>(),
+                                             les->d2[2].as<double>(), les->n[0], les->n[1], les->n[2],
+                                             mlp_device_params(mlp), mlp_scaling(mlp), c_fallback, nu, cnt,
+                                             les->err.as<int>());
   MF_CUDA(cudaGetLastError());
   if (n_fallback) {
     unsigned long long h = 0;
+    int e = 0;
     MF_CUDA(cudaMemcpyAsync(&h, cnt, sizeof(h), cudaMemcpyDeviceToHost, st));
+    MF_CUDA(cudaMemcpyAsync(&e, les->err.ptr, sizeof(int), cudaMemcpyDeviceToHost, st));
     MF_CUDA(cudaStreamSynchronize(st));
+    if (e) return set_error(MF_ERR_TIMEOUT, "mf_les_nu_mlp: tensor-core wait expired");
     *n_fallback = (long long)h;
   }
   return MF_OK;
