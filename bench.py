@@ -48,7 +48,7 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=2, help="oracle solves timed for cpu_baseline")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-rows", action="store_true", help="skip the measurements of the other rows")
-    ap.add_argument("--precision", default="auto", choices=["auto", "bf16", "tf32", "tf32_bf16"],
+    ap.add_argument("--precision", default="auto", choices=["auto", "bf16", "tf32"],
                     help="transform format; auto times both and reports the faster")
     ap.add_argument("--probe", default=None, choices=["bf16", "tf32", "fp64"],
                     help="profiling aid: run two untimed solves of the workload in this format "
@@ -236,10 +236,9 @@ def run_gb300(args, rank, world, dist):
     ref_interior = d_ref[1:-1, 1:-1, 1:-1]
     ref_norm = torch.linalg.vector_norm(ref_interior).item()
 
-    precs = {"bf16": mf.MF_PREC_SPLIT_BF16, "tf32": mf.MF_PREC_3XTF32, "tf32_bf16": mf.MF_PREC_TF32_BF16}
+    precs = {"bf16": mf.MF_PREC_SPLIT_BF16, "tf32": mf.MF_PREC_3XTF32}
     names = {"bf16": "split-BF16 three-product (tcgen05 kind::f16, FP32 accum)",
-             "tf32": "3xTF32 (tcgen05 kind::tf32, FP32 accum)",
-             "tf32_bf16": "3xTF32 first solve + split-BF16 correction solves (tcgen05, FP32 accum)"}
+             "tf32": "3xTF32 (tcgen05 kind::tf32, FP32 accum)"}
 
     def err_vs_plain():
         return (torch.linalg.vector_norm(d_solf[1:-1, 1:-1, 1:-1] - ref_interior) / ref_norm).item()
@@ -258,7 +257,7 @@ def run_gb300(args, rank, world, dist):
     # per format: smallest refinement count that reaches 1e-10 against the
     # FP64 solution, and a short timing; the faster format is the headline
     candidates = {}
-    for key in (["bf16", "tf32", "tf32_bf16"] if args.precision == "auto" else [args.precision]):
+    for key in (["bf16", "tf32"] if args.precision == "auto" else [args.precision]):
         errs = {}
         refine = None
         for r in (0, 1, 2, 3, 4):
@@ -410,15 +409,12 @@ def run_gb300(args, rank, world, dist):
     if dominant == "tc_transform":
         achieved = algo_flops / (tc_ms / tc_n * 1e-3) / 1e12
         # TF32 runs at half the BF16 tensor rate on this part (nominal ratio)
-        # TF32 runs at half the BF16 rate; the hybrid format runs one launch of
-        # each per pair, whose ideal time gives the harmonic peak 2 bf16 / 3
-        peak = {"bf16": bf16, "tf32": bf16 / 2.0, "tf32_bf16": 2.0 * bf16 / 3.0}[best]
+        peak = bf16 if best == "bf16" else bf16 / 2.0
         roof = {"kernel": "k_tc_transform", "bound": "tensor", "achieved": achieved, "peak": peak,
                 "unit": "TFLOP/s", "frac": achieved / peak,
-                "traffic": profile_traffic("k_tc_transform_%s_257cube.md" % ("tf32" if best != "bf16" else "bf16")),
+                "traffic": profile_traffic("k_tc_transform_%s_257cube.md" % best),
                 "traffic_source": "ncu dram__bytes_read+write of one launch, profiles/",
-                "peak_source": src + {"bf16": " bf16 burst", "tf32": " bf16 burst / 2 (tf32)",
-                                      "tf32_bf16": " bf16 burst x 2/3 (tf32 and bf16 launches in pairs)"}[best],
+                "peak_source": src + (" bf16 burst" if best == "bf16" else " bf16 burst / 2 (tf32)"),
                 "algorithmic_per_launch": algo_flops}
     else:
         ms, cnt = prof[dominant]
@@ -434,8 +430,7 @@ def run_gb300(args, rank, world, dist):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": {"bf16": "bf16x3+f64", "tf32": "tf32x3+f64", "tf32_bf16": "tf32x3+bf16x3+f64"}[best],
-        "data": "synthetic",
+        "dtype": "bf16x3+f64" if best == "bf16" else "tf32x3+f64", "data": "synthetic",
         "config": {"workload": "poisson_257cube_tanh2y_dirichlet_so6", "nodes": args.nodes,
                    "precision": names[best] + " + FP64 residual refinement",
                    "refine_steps": refine, "l2": "256 MiB flush between steps, per-step CUDA events",

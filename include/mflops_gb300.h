@@ -41,7 +41,6 @@ extern "C" {
 #define MF_PREC_FP64 0        /* plain FP64 (drop-in, matches the reference)       */
 #define MF_PREC_SPLIT_BF16 1  /* split-BF16 three-product on tcgen05, FP32 accum.  */
 #define MF_PREC_3XTF32 2      /* 3xTF32 on tcgen05, FP32 accumulation              */
-#define MF_PREC_TF32_BF16 3   /* 3xTF32 first solve, split-BF16 correction solves  */
 
 /* Arithmetic of the FP64-accurate refinement residual of the mixed path
  * (tridiagonal second-derivative operators): FP64 sweeps (default) or
@@ -155,7 +154,7 @@ int mf_solve_3d_noalloc(mf_solver3d_t* sc, const double* rhs, double sigma, doub
                         int n1, int n2, int n3, void* stream);
 
 /* Same problem with the eigenvector transforms on the tensor cores
- * (precision = MF_PREC_SPLIT_BF16, MF_PREC_3XTF32 or MF_PREC_TF32_BF16) and `refine`
+ * (precision = MF_PREC_SPLIT_BF16 or MF_PREC_3XTF32) and `refine`
  * iterative-refinement steps whose residual is computed in FP64 with the
  * solver's own compact operator.  refine < 0 selects the default count. */
 int mf_solve_3d_mixed(mf_solver3d_t* sc, const double* rhs, double sigma, double* solf,

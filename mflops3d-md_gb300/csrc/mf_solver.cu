@@ -1477,25 +1477,18 @@ static int fold_split(mf_solver3d* sc, bool tf32, const double* rhs, const doubl
 // or 3xTF32).  The cancellation in r_k = r1 - A C is relative to |r1|
 // (~1e-5 |rhs|), so FP32 keeps it to ~1e-12 |rhs|; the FP64 residual of u1
 // carries the accuracy.
-//
-// MF_PREC_TF32_BF16 takes the first solve in 3xTF32 (~1e-6) and the
-// corrections in split-BF16 (~1e-5 relative, but of C ~ 1e-6 |u|, so ~1e-11
-// of u): the split-BF16 transform runs in 31 us against 83 us for 3xTF32 at
-// 257^3, while one refinement step still reaches 1e-10.
 static int solve_mixed_dev(mf_solver3d* sc, const double* rhs, double sigma, double* solf,
                            const double* bcs[3], int prec, int refine, cudaStream_t st) {
-  if (prec != MF_PREC_SPLIT_BF16 && prec != MF_PREC_3XTF32 && prec != MF_PREC_TF32_BF16)
+  if (prec != MF_PREC_SPLIT_BF16 && prec != MF_PREC_3XTF32)
     return set_error(MF_ERR_UNSUPPORTED, "precision mode %d is not available", prec);
-  const bool tf32 = prec != MF_PREC_SPLIT_BF16;           // first solve
-  const bool tf32c = prec == MF_PREC_3XTF32;              // corrections
+  const bool tf32 = prec == MF_PREC_3XTF32;
   int rc;
   if ((rc = mixed_prepare(sc, tf32))) return rc;
-  if (tf32c != tf32 && refine > 0 && (rc = mixed_prepare(sc, tf32c))) return rc;
   const int n1 = sc->n[0], n2 = sc->n[1], n3 = sc->n[2];
   const long long tot = (long long)n1 * n2 * n3;
-  __nv_bfloat16* xh = tf32c ? nullptr : sc->Xa_hi.as<__nv_bfloat16>();
-  __nv_bfloat16* xl = tf32c ? nullptr : sc->Xa_lo.as<__nv_bfloat16>();
-  float* x32 = tf32c ? sc->Xa32.as<float>() : nullptr;
+  __nv_bfloat16* xh = tf32 ? nullptr : sc->Xa_hi.as<__nv_bfloat16>();
+  __nv_bfloat16* xl = tf32 ? nullptr : sc->Xa_lo.as<__nv_bfloat16>();
+  float* x32 = tf32 ? sc->Xa32.as<float>() : nullptr;
   float* u1 = sc->U32.as<float>();
   float* C = sc->C32.as<float>();
   if ((rc = fold_split(sc, tf32, rhs, bcs, st))) return rc;
@@ -1516,7 +1509,7 @@ static int solve_mixed_dev(mf_solver3d* sc, const double* rhs, double sigma, dou
                                               kProfResid32, st)))
         return rc;
     }
-    if ((rc = approx_solve(sc, tf32c, sigma, C, it > 0, st))) return rc;
+    if ((rc = approx_solve(sc, tf32, sigma, C, it > 0, st))) return rc;
   }
   sc->prof.begin(kProfCopy, st);
   k_finalize<<<dim3(blocks_for(n1, 256), n2, 4), 256, 0, st>>>(u1, refine > 0 ? C : nullptr, solf, n1,

@@ -44,7 +44,6 @@ MF_ERR_UNSUPPORTED = 8
 MF_PREC_FP64 = 0
 MF_PREC_SPLIT_BF16 = 1
 MF_PREC_3XTF32 = 2
-MF_PREC_TF32_BF16 = 3
 MF_RESID_FF = 0
 MF_RESID_FP64 = 1
 MD_IFACE_AUTO = 0

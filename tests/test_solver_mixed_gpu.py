@@ -137,36 +137,3 @@ def test_residual_arithmetic_modes_agree(mf, gpu, prec_name, refine):
         got[mode] = mf.to_host(out)[m]
         assert rel_l2(got[mode], ref[m]) < 1e-10
     assert rel_l2(got[mf.MF_RESID_FF], got[mf.MF_RESID_FP64]) < 1e-11
-
-
-@pytest.mark.parametrize("sigma", [0.0, -1e3])
-def test_tf32_first_bf16_corrections_reach_1e10(mf, gpu, sigma):
-    """MF_PREC_TF32_BF16: 3xTF32 first solve, split-BF16 correction solve;
-    one refinement step reaches 1e-10 (the correction is ~1e-6 of u, so its
-    split-BF16 error contributes ~1e-11)."""
-    err = mixed_case(mf, (66, 66, 66), (1,) * 6, sigma, refine=1, prec=mf.MF_PREC_TF32_BF16)
-    print("3xtf32 + split-bf16 correction rel L2 error: %.3e" % err)
-    assert err < 1e-10
-
-
-def test_tf32_bf16_uneven_neumann(mf, gpu):
-    err = mixed_case(mf, (50, 66, 98), (1, 2, 1, 1, 2, 1), -1.0, refine=1, prec=mf.MF_PREC_TF32_BF16)
-    assert err < 1e-10
-
-
-def test_tf32_bf16_matches_fp64_gpu_at_257(mf, gpu):
-    import torch
-    n = 255
-    gx, gy = mesh.uniform_grid(257), mesh.tanh_grid(257, 2.0)
-    sc = mf.SolverCoeffs3D(gx, gy, gx, (1,) * 6, 6)
-    rhs = torch.randn((n, n, n), dtype=torch.float64, device="cuda",
-                      generator=torch.Generator("cuda").manual_seed(5)).permute(2, 1, 0)
-    bc = [mf.empty_device((n, n, 2)) for _ in range(3)]
-    plain = mf.empty_device((257, 257, 257))
-    mixed = mf.empty_device((257, 257, 257))
-    sc.solve_3d(rhs, 0.0, plain, *bc)
-    sc.solve_3d(rhs, 0.0, mixed, *bc, precision=mf.MF_PREC_TF32_BF16, refine=1)
-    sc.device_status()
-    err = (torch.linalg.vector_norm(mixed - plain) / torch.linalg.vector_norm(plain)).item()
-    print("257^3 3xtf32 + split-bf16 correction vs FP64 GPU: %.3e" % err)
-    assert err < 1e-10
