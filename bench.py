@@ -50,9 +50,12 @@ def parse():
     ap.add_argument("--no-rows", action="store_true", help="skip the measurements of the other rows")
     ap.add_argument("--precision", default="auto", choices=["auto", "bf16", "tf32"],
                     help="transform format; auto times both and reports the faster")
-    ap.add_argument("--probe", default=None, choices=["bf16", "tf32", "fp64"],
+    ap.add_argument("--probe", default=None,
+                    choices=["bf16", "tf32", "fp64", "der", "filter", "les_mlp", "mlp_train"],
                     help="profiling aid: run two untimed solves of the workload in this format "
-                         "(refinement steps from --refine) and exit")
+                         "(refinement steps from --refine), or two untimed launches of one row "
+                         "(derivative sweeps at 257^3, the 384 -> 96 filter, the learned viscosity "
+                         "at 160^3, a training step on 65,536 points), and exit")
     ap.add_argument("--refine", type=int, default=1)
     return ap.parse_args()
 
@@ -622,11 +625,64 @@ def row_measurements(mf, torch, hbm):
     return out
 
 
+def run_row_probe(args):
+    """Two untimed launches of one row's kernels on the bench's row shapes
+    (synthetic data), for ncu captures of single kernels."""
+    import torch
+    import mflops_gb300 as mf
+    from oracle import mesh
+
+    def field(shape, seed):
+        gen = torch.Generator("cuda").manual_seed(seed)
+        return torch.rand(tuple(reversed(shape)), dtype=torch.float64, device="cuda",
+                          generator=gen).permute(*reversed(range(len(shape))))
+
+    if args.probe == "der":
+        n = 257
+        dc = mf.DerivativesCoefficients(mesh.tanh_grid(n, 2.0), so=6)
+        f = field((n, n, n), 11)
+        df = mf.empty_device((n, n, n))
+        for _ in range(2):
+            for axis, order in ((0, 1), (1, 1), (2, 1), (0, 2)):
+                dc.apply(axis, order, f, out=df)
+    elif args.probe == "filter":
+        flt = mf.SplineFilter(mesh.uniform_grid(384), mesh.uniform_grid(96), xn=mesh.uniform_grid(96), k=3)
+        f = field((384, 385, 384), 30)
+        fo = mf.empty_device((96, 385, 384))
+        for _ in range(2):
+            flt.apply(f, 0, out=fo)
+    elif args.probe == "les_mlp":
+        shape = (160, 160, 160)
+        g = mesh.uniform_grid(160)
+        les = mf.LesModel(g, g, g)
+        du = [[field(shape, 60 + 3 * i + j) for j in range(3)] for i in range(3)]
+        mlp = mf.Mlp(0)
+        inf = np.full(6, np.inf, np.float32)
+        mlp.set_scaling(np.zeros(6), np.ones(6), -inf, inf, 0.02, 1000.0)
+        for _ in range(2):
+            les.nu_mlp(mlp, 0.027, du)
+    else:
+        gen = torch.Generator("cuda").manual_seed(50)
+        npts = 1 << 16
+        X = torch.rand((npts, 6), device="cuda", generator=gen, dtype=torch.float32) * 2 - 1
+        b = torch.rand(npts, device="cuda", generator=gen, dtype=torch.float32)
+        t = 0.02 * b * (1 + X[:, 0])
+        mlp = mf.Mlp(0)
+        inf = np.full(6, np.inf, np.float32)
+        mlp.set_scaling(np.zeros(6), np.ones(6), -inf, inf, 0.02, 1000.0)
+        for _ in range(2):
+            mlp.train_step(X, b, t, lr=1e-3)
+    torch.cuda.synchronize()
+    print("probe ok", args.probe, flush=True)
+
+
 def run_probe(args):
     """Two untimed solves of the bench workload (for ncu launch lists and
     captures of single kernels)."""
     import torch
     import mflops_gb300 as mf
+    if args.probe not in ("bf16", "tf32", "fp64"):
+        return run_row_probe(args)
     grids, rhs, bcs = workload(args.nodes)
     n = args.nodes - 2
     sc = mf.SolverCoeffs3D(*grids, (1,) * 6, 6)
