@@ -164,8 +164,10 @@ __global__ void k_les_features(LesGrad d, const double* __restrict__ dx2, const 
   double b = 0.0;
   if (!on_edge(i, j, k, nx, ny, nz)) {
     double g[3][3];
+    float gf[3][3], ssf;
     load_grad(d, idx, g);
-    if (grad_features(g, f)) b = sqrt(2.0 * strain_ss(g)) * ((dx2[i] + dy2[j] + dz2[k]) / 3.0);
+    narrow_grad(g, gf);
+    if (grad_features(gf, f, &ssf)) b = (double)sqrtf(2.f * ssf) * ((dx2[i] + dy2[j] + dz2[k]) * (1.0 / 3.0));
   }
 #pragma unroll
   for (int q = 0; q < kMlpIn; ++q) X[idx * kMlpIn + q] = f[q];
@@ -290,17 +292,18 @@ __global__ void __launch_bounds__(128) k_les_nu_mlp(LesGrad d, const double* __r
       k = (int)(jk / ny);
     }
     const bool edge = live && on_edge(i, j, k, nx, ny, nz);
-    double ss = 0.0;
+    double g[3][3];
+    float ssf = 0.f;
     bool in = false;
     float h1[kMlpH];
 #pragma unroll
     for (int q = 0; q < kMlpH; ++q) h1[q] = 0.f;
     if (live && !edge) {
-      double g[3][3];
+      float gf[3][3];
       load_grad(d, idx, g);
-      ss = strain_ss(g);
+      narrow_grad(g, gf);
       float f[kMlpIn], x[kMlpIn];
-      in = grad_features(g, f) && mlp_input(s, f, x);
+      in = grad_features(gf, f, &ssf) && mlp_input(s, f, x);
       if (in) {
 #pragma unroll
         for (int q = 0; q < kMlpH; ++q) {
@@ -346,16 +349,18 @@ __global__ void __launch_bounds__(128) k_les_nu_mlp(LesGrad d, const double* __r
       if (edge) {
         nu[idx] = 0.0;
       } else {
-        double c = c_fallback;
         if (in) {
+          // network points: C sqrt(2 S:S) in FP32 (the network's own accuracy)
           float y = Ps[576];
 #pragma unroll
           for (int q = 0; q < kMlpH; ++q) y = fmaf(Ps[512 + q], fmaxf(a2[q] + Ps[448 + q], 0.f), y);
-          c = (double)fmaxf(s.cscale * y, 0.f);
-        } else if (n_fallback) {
-          atomicAdd(n_fallback, 1ull);
+          const float v = fmaxf(s.cscale * y, 0.f) * sqrtf(2.f * ssf);
+          nu[idx] = (double)v * ((dx2[i] + dy2[j] + dz2[k]) * (1.0 / 3.0));
+        } else {
+          // fallback points: the plain model's exact FP64 value
+          if (n_fallback) atomicAdd(n_fallback, 1ull);
+          nu[idx] = smag_nu(c_fallback, strain_ss(g), dx2[i], dy2[j], dz2[k]);
         }
-        nu[idx] = smag_nu(c, ss, dx2[i], dy2[j], dz2[k]);
       }
     }
     fence_before();

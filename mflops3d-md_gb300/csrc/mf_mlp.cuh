@@ -15,6 +15,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include "mf_line.cuh"
 #include "mflops_gb300.h"
 
 namespace mf {
@@ -37,16 +38,20 @@ struct MlpScaling {
   float cscale;                      // C = cscale * network output
 };
 
-// Invariant features of one gradient tensor (FP32 arithmetic on the FP32
-// rounding of g: the features only feed the FP32 network, and FP64 would
-// cost about 240 operations per point on the narrow FP64 pipe); false when
-// g:g lies outside (1e-30, 1e30), where the point falls back.
-__device__ __forceinline__ bool grad_features(const double gd[3][3], float f[kMlpIn]) {
-  float g[3][3];
+// FP32 rounding of an FP64 gradient tensor on the integer pipe (narrow():
+// GB300's conversion unit runs at the narrow FP64 rate).
+__device__ __forceinline__ void narrow_grad(const double gd[3][3], float g[3][3]) {
 #pragma unroll
   for (int a = 0; a < 3; ++a)
 #pragma unroll
-    for (int b = 0; b < 3; ++b) g[a][b] = (float)gd[a][b];
+    for (int b = 0; b < 3; ++b) g[a][b] = narrow(gd[a][b]);
+}
+
+// Invariant features of one gradient tensor (FP32 arithmetic: the features
+// only feed the FP32 network, and FP64 would cost about 240 operations per
+// point on the narrow FP64 pipe); *ssf receives S:S in FP32.  False when g:g
+// lies outside (1e-30, 1e30), where the point falls back.
+__device__ __forceinline__ bool grad_features(const float g[3][3], float f[kMlpIn], float* ssf) {
   float g2 = 0.f;
 #pragma unroll
   for (int a = 0; a < 3; ++a)
@@ -82,6 +87,7 @@ __device__ __forceinline__ bool grad_features(const double gd[3][3], float f[kMl
   const float det = g[0][0] * (g[1][1] * g[2][2] - g[1][2] * g[2][1]) -
                     g[0][1] * (g[1][0] * g[2][2] - g[1][2] * g[2][0]) +
                     g[0][2] * (g[1][0] * g[2][1] - g[1][1] * g[2][0]);
+  *ssf = ss;
   const float ig2 = 1.f / g2, ir = rsqrtf(g2), ir3 = ig2 * ir;
   f[0] = ss * ig2;
   f[1] = s3 * ir3;
