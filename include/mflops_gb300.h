@@ -153,6 +153,20 @@ int mf_solve_3d_noalloc(mf_solver3d_t* sc, const double* rhs, double sigma, doub
                         const double* bcx, const double* bcy, const double* bcz,
                         int n1, int n2, int n3, void* stream);
 
+/* `count` problems of this operator and sigma (plain FP64) in one pass of
+ * launches: problem b reads rhs + b*rhs_stride and the boundary arrays at
+ * b times their strides, and writes solf + b*solf_stride (element strides;
+ * a stride of 0 shares one input array between all problems).  Each
+ * problem's result equals that of mf_solve_3d.  Device pointers only,
+ * 1 <= count <= 65535.  No reference counterpart (the reference solves one
+ * right-hand side per solve_3d call); used for the influence-matrix columns
+ * and for several right-hand sides of one operator. */
+int mf_solve_3d_batch(mf_solver3d_t* sc, int count, const double* rhs, long long rhs_stride,
+                      double sigma, double* solf, long long solf_stride, const double* bcx,
+                      long long bcx_stride, const double* bcy, long long bcy_stride,
+                      const double* bcz, long long bcz_stride, int n1, int n2, int n3,
+                      void* stream);
+
 /* Same problem with the eigenvector transforms on the tensor cores
  * (precision = MF_PREC_SPLIT_BF16 or MF_PREC_3XTF32) and `refine`
  * iterative-refinement steps whose residual is computed in FP64 with the

@@ -133,6 +133,33 @@ __global__ void k_face_gather(const double* __restrict__ du, double* out, FaceGa
   out[f.row0 + q] += f.scale * (f.m ? v : -v);
 }
 
+// Batched influence columns: problem b has a unit value at point q0 + b of
+// side m of a face array with nf points per side (all else zero).
+__global__ void k_dirac_batch(double* bc, long long nf, int m, long long q0, int B) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= B) return;
+  bc[(long long)b * 2 * nf + (long long)m * nf + q0 + b] = 1.0;
+}
+
+// k_face_gather for B problems: problem blockIdx.y reads du + y * du_stride
+// and adds into out + y * out_stride.
+__global__ void k_face_gather_batch(const double* __restrict__ du, long long du_stride, double* out,
+                                    long long out_stride, FaceGather f) {
+  const int na = (f.l == 0 ? f.ny : f.nx) - 2;
+  const int nb = (f.l == 2 ? f.ny : f.nz) - 2;
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= na * nb) return;
+  du += blockIdx.y * du_stride;
+  out += blockIdx.y * out_stride;
+  const int a = q % na + 1, b = q / na + 1;
+  int i, j, k;
+  if (f.l == 0) { i = f.m ? f.nx - 1 : 0; j = a; k = b; }
+  else if (f.l == 1) { i = a; j = f.m ? f.ny - 1 : 0; k = b; }
+  else { i = a; j = b; k = f.m ? f.nz - 1 : 0; }
+  const double v = du[i + (long long)f.nx * (j + (long long)f.ny * k)];
+  out[f.row0 + q] += f.scale * (f.m ? v : -v);
+}
+
 // bc face (l, m) of a subdomain: copy from the caller's array, then the
 // interface faces get either 0 or the interface solution.
 __global__ void k_face_set(double* bc, long long nf, int m, const double* __restrict__ src,
@@ -283,6 +310,7 @@ struct mf_md {
   std::vector<Sub> sub;  // index i + nd1*(j + nd2*k)
   DevBuf M, ipiv, vec, info, work, zero_int, du[3], rint, ufield;
   DevBuf Minv, vec2;  // row-major inverse of the influence matrix, solve output
+  DevBuf ub, dub[3], bcb;  // batched influence columns: fields, derivatives, Dirac faces
   bool inv_ok = false;
   int iface_mode = MF_MD_IFACE_AUTO;
   cusolverDnHandle_t cs = nullptr;
@@ -455,7 +483,7 @@ int mf_md_destroy(mf_md_t* md) {
       sd.bc[l].release();
     }
   }
-  for (DevBuf* b : {&md->Minv, &md->vec2}) b->release();
+  for (DevBuf* b : {&md->Minv, &md->vec2, &md->ub, &md->dub[0], &md->dub[1], &md->dub[2], &md->bcb}) b->release();
   for (DevBuf* b : {&md->M, &md->ipiv, &md->vec, &md->info, &md->work, &md->zero_int, &md->du[0],
                     &md->du[1], &md->du[2], &md->rint, &md->ufield})
     b->release();
@@ -490,27 +518,72 @@ int mf_md_influence_matrix_set(mf_md_t* md, double sigma, int null_mode, void* s
   // md_influence_matrix_set: a Dirac on every interface point of every
   // subdomain, solved with g = 0; the signed normal derivatives on the
   // subdomain's interface faces, negated, form that point's column.
+  // All Dirac columns of one subdomain face are solved together, in chunks
+  // of B problems: one batched solve (zero right-hand side and zero data on
+  // the other faces shared between the problems), one batched derivative
+  // sweep per axis (the B fields stacked along z, or viewed as (nx*ny, nz, B)
+  // for z lines, all lines plain: the gathered face values come from
+  // interior lines only), and one batched gather into B consecutive columns.
+  (void)u;
   for (int k = 0; k < t.nd[2]; ++k)
     for (int j = 0; j < t.nd[1]; ++j)
       for (int i = 0; i < t.nd[0]; ++i) {
         const int s = md_sub_index(md, i, j, k);
         mf_md::Sub& sd = md->sub[s];
-        const size_t nfull = (size_t)sd.n[0] * sd.n[1] * sd.n[2];
-        MF_CUDA(cudaMemsetAsync(u, 0, nfull * 8, st));
+        const int nx = sd.n[0], ny = sd.n[1], nz = sd.n[2];
+        const long long nfull = (long long)nx * ny * nz;
+        const long long nint = (long long)(nx - 2) * (ny - 2) * (nz - 2);
+        for (int l2 = 0; l2 < 3; ++l2)
+          MF_CUDA(cudaMemsetAsync(sd.bc[l2].ptr, 0, sizeof(double) * 2 * face_points(sd, l2), st));
+        bool need[3] = {false, false, false};
+        for (int l2 = 0; l2 < 3; ++l2)
+          for (int m2 = 0; m2 < 2; ++m2)
+            if (t.get(i, j, k, l2, m2) > 0) need[l2] = true;
+        // chunk size: fields, three derivative fields and the solver's two
+        // work arrays per problem within about 2 GB
+        const long long per = 8 * (4 * nfull + 2 * nint);
+        const int bmax = (int)std::max(1LL, std::min(65535LL, (2LL << 30) / per));
         for (int m = 0; m < 2; ++m)
           for (int l = 0; l < 3; ++l) {
             const int p = t.get(i, j, k, l, m);
             if (p <= 0) continue;
-            for (int q = 0; q < t.size[p - 1]; ++q) {
+            const long long nf = face_points(sd, l);
+            for (long long q0 = 0; q0 < t.size[p - 1]; q0 += bmax) {
+              const int B = (int)std::min<long long>(bmax, t.size[p - 1] - q0);
+              if ((rc = md->ub.ensure((size_t)B * nfull * 8)) || (rc = md->bcb.ensure((size_t)B * 2 * nf * 8)))
+                return rc;
               for (int l2 = 0; l2 < 3; ++l2)
-                MF_CUDA(cudaMemsetAsync(sd.bc[l2].ptr, 0, sizeof(double) * 2 * face_points(sd, l2), st));
-              const long long nf = face_points(sd, l);
-              k_face_set<<<nblk(nf, 128), 128, 0, st>>>(sd.bc[l].as<double>(), nf, m, nullptr, 0, 2,
-                                                        (double)q);
+                if (need[l2] && (rc = md->dub[l2].ensure((size_t)B * nfull * 8))) return rc;
+              double* U = md->ub.as<double>();
+              MF_CUDA(cudaMemsetAsync(U, 0, (size_t)B * nfull * 8, st));
+              MF_CUDA(cudaMemsetAsync(md->bcb.ptr, 0, (size_t)B * 2 * nf * 8, st));
+              k_dirac_batch<<<nblk(B, 128), 128, 0, st>>>(md->bcb.as<double>(), nf, m, q0, B);
               MF_CUDA(cudaGetLastError());
-              if ((rc = md_sub_solve(md, s, md->zero_int.as<double>(), u, st))) return rc;
-              double* col = M + (long long)n * (t.offset[p - 1] + q);
-              if ((rc = md_gather(md, i, j, k, u, col, -1.0, st))) return rc;
+              const double* bc[3] = {sd.bc[0].as<double>(), sd.bc[1].as<double>(), sd.bc[2].as<double>()};
+              long long bs[3] = {0, 0, 0};
+              bc[l] = md->bcb.as<double>();
+              bs[l] = 2 * nf;
+              if ((rc = mf_solve_3d_batch(sd.sc, B, md->zero_int.as<double>(), 0, md->sigma, U, nfull, bc[0], bs[0],
+                                          bc[1], bs[1], bc[2], bs[2], nx - 2, ny - 2, nz - 2, st)))
+                return rc;
+              if (need[0] && (rc = der_launch(sd.dc[0], 0, 1, 1, U, md->dub[0].as<double>(), nx, ny,
+                                              (int)(nz * B), st)))
+                return rc;
+              if (need[1] && (rc = der_launch(sd.dc[1], 1, 1, 1, U, md->dub[1].as<double>(), nx, ny,
+                                              (int)(nz * B), st)))
+                return rc;
+              if (need[2] && (rc = der_launch(sd.dc[2], 1, 1, 1, U, md->dub[2].as<double>(), nx * ny, nz, B, st)))
+                return rc;
+              double* col0 = M + (long long)n * (t.offset[p - 1] + q0);
+              for (int l2 = 0; l2 < 3; ++l2)
+                for (int m2 = 0; m2 < 2; ++m2) {
+                  const int p2 = t.get(i, j, k, l2, m2);
+                  if (p2 <= 0) continue;
+                  FaceGather f{l2, m2, nx, ny, nz, (long long)t.offset[p2 - 1], -1.0};
+                  k_face_gather_batch<<<dim3(nblk(t.size[p2 - 1], 128), B), 128, 0, st>>>(
+                      md->dub[l2].as<double>(), nfull, col0, (long long)n, f);
+                  MF_CUDA(cudaGetLastError());
+                }
             }
           }
       }

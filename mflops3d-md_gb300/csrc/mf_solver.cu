@@ -88,12 +88,23 @@ struct FoldArgs {
   double cx[4], cy[4], cz[4];
 };
 
+// Batched solves: problem blockIdx.y at the given element strides (0 = shared).
+struct FoldBatch {
+  long long rhs = 0, out = 0, bc[3] = {0, 0, 0};
+};
+
 __global__ void k_fold(const double* __restrict__ rhs, double* __restrict__ out,
                        const double* __restrict__ bcx, const double* __restrict__ bcy,
-                       const double* __restrict__ bcz, FoldArgs a, int n1, int n2, int n3) {
+                       const double* __restrict__ bcz, FoldArgs a, int n1, int n2, int n3,
+                       FoldBatch fb = FoldBatch()) {
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long tot = (long long)n1 * n2 * n3;
   if (idx >= tot) return;
+  rhs += blockIdx.y * fb.rhs;
+  out += blockIdx.y * fb.out;
+  bcx += blockIdx.y * fb.bc[0];
+  bcy += blockIdx.y * fb.bc[1];
+  bcz += blockIdx.y * fb.bc[2];
   const int i = (int)(idx % n1);
   const long long jk = idx / n1;
   const int j = (int)(jk % n2), k = (int)(jk / n2);
@@ -137,7 +148,11 @@ constexpr int GBK = 16;
 template <int BT>
 __global__ void __launch_bounds__(256) k_gemm_f64(const double* __restrict__ X, int M, int K,
                                                   const double* __restrict__ A, int N,
-                                                  double* __restrict__ Y, GemmEpi e) {
+                                                  double* __restrict__ Y, GemmEpi e, long long xs = 0,
+                                                  long long ys = 0) {
+  // batched solves: problem blockIdx.z at X + z xs, Y + z ys
+  X += blockIdx.z * xs;
+  Y += blockIdx.z * ys;
   constexpr int R = BT / 16;
   __shared__ double Xs[GBK][BT + 1];
   __shared__ double As[GBK][BT + 1];
@@ -210,9 +225,12 @@ struct FaceArgs {
   double nl[7], nr[7];
 };
 
-__global__ void k_faces(double* solf, const double* __restrict__ bc, FaceArgs f) {
+__global__ void k_faces(double* solf, const double* __restrict__ bc, FaceArgs f, long long s_solf = 0,
+                        long long s_bc = 0) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (long long)f.na * f.nb) return;
+  solf += blockIdx.y * s_solf;  // batched solves: problem blockIdx.y
+  bc += blockIdx.y * s_bc;
   const int a = (int)(t % f.na), b = (int)(t / f.na);
   double* p = solf + (a + 1) * f.sa + (b + 1) * f.sb;  // ghost-left node of this line
   const double blo = bc[t], bhi = bc[t + (long long)f.na * f.nb];
@@ -1118,20 +1136,24 @@ static int axis_upload(AxisDev& d, const SolverAxisHost& h) {
 }
 
 static int gemm_f64(StageProfiler& prof, const double* X, int M, int K, const double* A, int N,
-                    double* Y, const GemmEpi& e, cudaStream_t st) {
-  const long long tiles64 = (long long)blocks_for(M, 64) * blocks_for(N, 64);
+                    double* Y, const GemmEpi& e, cudaStream_t st, int B = 1, long long xs = 0,
+                    long long ys = 0) {
+  const long long tiles64 = (long long)blocks_for(M, 64) * blocks_for(N, 64) * B;
   prof.begin(kProfGemm64, st);
   if (tiles64 >= 2LL * num_sms()) {
-    k_gemm_f64<64><<<dim3(blocks_for(M, 64), blocks_for(N, 64)), 256, 0, st>>>(X, M, K, A, N, Y, e);
+    k_gemm_f64<64><<<dim3(blocks_for(M, 64), blocks_for(N, 64), B), 256, 0, st>>>(X, M, K, A, N, Y, e, xs,
+                                                                                 ys);
   } else {
-    k_gemm_f64<32><<<dim3(blocks_for(M, 32), blocks_for(N, 32)), 256, 0, st>>>(X, M, K, A, N, Y, e);
+    k_gemm_f64<32><<<dim3(blocks_for(M, 32), blocks_for(N, 32), B), 256, 0, st>>>(X, M, K, A, N, Y, e, xs,
+                                                                                 ys);
   }
   prof.end(st);
   MF_CUDA(cudaGetLastError());
   return MF_OK;
 }
 
-static int faces(mf_solver3d* sc, double* solf, const double* bcs[3], cudaStream_t st) {
+static int faces(mf_solver3d* sc, double* solf, const double* bcs[3], cudaStream_t st, int B = 1,
+                 long long s_solf = 0, const long long* s_bc = nullptr) {
   const int n1 = sc->n[0], n2 = sc->n[1], n3 = sc->n[2];
   const long long p1 = n1 + 2, p2 = n2 + 2;
   for (int axis = 0; axis < 3; ++axis) {
@@ -1144,7 +1166,8 @@ static int faces(mf_solver3d* sc, double* solf, const double* bcs[3], cudaStream
     f.bc1 = d.bc[1];
     for (int m = 0; m < 7; ++m) { f.nl[m] = d.neum[m]; f.nr[m] = d.neum[7 + m]; }
     sc->prof.begin(kProfFaces, st);
-    k_faces<<<blocks_for((long long)f.na * f.nb, 128), 128, 0, st>>>(solf, bcs[axis], f);
+    k_faces<<<dim3(blocks_for((long long)f.na * f.nb, 128), B), 128, 0, st>>>(solf, bcs[axis], f, s_solf,
+                                                                             s_bc ? s_bc[axis] : 0);
     sc->prof.end(st);
     MF_CUDA(cudaGetLastError());
   }
@@ -1165,18 +1188,29 @@ static FoldArgs fold_args(mf_solver3d* sc) {
 }
 
 // Plain FP64 solve on device pointers.
-static int solve_plain_dev(mf_solver3d* sc, const double* rhs, double sigma, double* solf,
-                           const double* bcs[3], cudaStream_t st) {
+// B problems of the same operator and sigma in one pass of launches: rhs,
+// solf and the boundary arrays of problem b at b times their element
+// strides (a stride of 0 shares one array between all problems).  Every
+// stage indexes its problem from the grid (blockIdx.y or .z), so the
+// per-problem arithmetic, and the result, is that of B separate solves.
+static int solve_plain_batch(mf_solver3d* sc, int B, const double* rhs, long long s_rhs, double sigma,
+                             double* solf, long long s_solf, const double* bcs[3], const long long s_bc[3],
+                             cudaStream_t st) {
   const int n1 = sc->n[0], n2 = sc->n[1], n3 = sc->n[2];
   const long long tot = (long long)n1 * n2 * n3;
   int rc;
-  if ((rc = sc->w0.ensure(tot * sizeof(double))) || (rc = sc->w1.ensure(tot * sizeof(double))))
+  if ((rc = sc->w0.ensure((size_t)B * tot * sizeof(double))) ||
+      (rc = sc->w1.ensure((size_t)B * tot * sizeof(double))))
     return rc;
   double* w0 = sc->w0.as<double>();
   double* w1 = sc->w1.as<double>();
+  FoldBatch fb;
+  fb.rhs = s_rhs;
+  fb.out = tot;
+  for (int a = 0; a < 3; ++a) fb.bc[a] = s_bc[a];
   sc->prof.begin(kProfFold, st);
-  k_fold<<<blocks_for(tot, 256), 256, 0, st>>>(rhs, w0, bcs[0], bcs[1], bcs[2], fold_args(sc), n1,
-                                               n2, n3);
+  k_fold<<<dim3(blocks_for(tot, 256), B), 256, 0, st>>>(rhs, w0, bcs[0], bcs[1], bcs[2], fold_args(sc), n1,
+                                                        n2, n3, fb);
   sc->prof.end(st);
   MF_CUDA(cudaGetLastError());
   GemmEpi plain;
@@ -1185,8 +1219,8 @@ static int solve_plain_dev(mf_solver3d* sc, const double* rhs, double sigma, dou
   const double* Vf[3] = {sc->ax[0].V.as<double>(), sc->ax[1].V.as<double>(),
                          sc->ax[2].V.as<double>()};
   // forward transforms with V^-1: x, y, z (+ divide)
-  if ((rc = gemm_f64(sc->prof, w0, n2 * n3, n1, Vi[0], n1, w1, plain, st))) return rc;
-  if ((rc = gemm_f64(sc->prof, w1, n3 * n1, n2, Vi[1], n2, w0, plain, st))) return rc;
+  if ((rc = gemm_f64(sc->prof, w0, n2 * n3, n1, Vi[0], n1, w1, plain, st, B, tot, tot))) return rc;
+  if ((rc = gemm_f64(sc->prof, w1, n3 * n1, n2, Vi[1], n2, w0, plain, st, B, tot, tot))) return rc;
   GemmEpi div;
   div.kind = 1;
   div.lx = sc->ax[0].eig.as<double>();
@@ -1196,16 +1230,22 @@ static int solve_plain_dev(mf_solver3d* sc, const double* rhs, double sigma, dou
   div.thresh = kNullThresh;
   div.n1 = n1;
   div.n2 = n2;
-  if ((rc = gemm_f64(sc->prof, w0, n1 * n2, n3, Vi[2], n3, w1, div, st))) return rc;
+  if ((rc = gemm_f64(sc->prof, w0, n1 * n2, n3, Vi[2], n3, w1, div, st, B, tot, tot))) return rc;
   // inverse transforms with V, the last one written into solf's interior
-  if ((rc = gemm_f64(sc->prof, w1, n2 * n3, n1, Vf[0], n1, w0, plain, st))) return rc;
-  if ((rc = gemm_f64(sc->prof, w0, n3 * n1, n2, Vf[1], n2, w1, plain, st))) return rc;
+  if ((rc = gemm_f64(sc->prof, w1, n2 * n3, n1, Vf[0], n1, w0, plain, st, B, tot, tot))) return rc;
+  if ((rc = gemm_f64(sc->prof, w0, n3 * n1, n2, Vf[1], n2, w1, plain, st, B, tot, tot))) return rc;
   GemmEpi out;
   out.kind = 2;
   out.n1 = n1;
   out.n2 = n2;
-  if ((rc = gemm_f64(sc->prof, w1, n1 * n2, n3, Vf[2], n3, solf, out, st))) return rc;
-  return faces(sc, solf, bcs, st);
+  if ((rc = gemm_f64(sc->prof, w1, n1 * n2, n3, Vf[2], n3, solf, out, st, B, tot, s_solf))) return rc;
+  return faces(sc, solf, bcs, st, B, s_solf, s_bc);
+}
+
+static int solve_plain_dev(mf_solver3d* sc, const double* rhs, double sigma, double* solf,
+                           const double* bcs[3], cudaStream_t st) {
+  const long long zero[3] = {0, 0, 0};
+  return solve_plain_batch(sc, 1, rhs, 0, sigma, solf, 0, bcs, zero, st);
 }
 
 // Residual on device pointers, three passes (x, y, z):
@@ -1670,6 +1710,27 @@ int mf_solve_3d(mf_solver3d_t* sc, const double* rhs, double sigma, double* solf
                      [&](const double* r, double* s, const double** bcs, cudaStream_t st) {
                        return solve_plain_dev(sc, r, sigma, s, bcs, st);
                      });
+}
+
+int mf_solve_3d_batch(mf_solver3d_t* sc, int count, const double* rhs, long long rhs_stride, double sigma,
+                      double* solf, long long solf_stride, const double* bcx, long long bcx_stride,
+                      const double* bcy, long long bcy_stride, const double* bcz, long long bcz_stride,
+                      int n1, int n2, int n3, void* stream) {
+  if (!sc || !rhs || !solf || !bcx || !bcy || !bcz || count < 1 || count > 65535 || rhs_stride < 0 ||
+      bcx_stride < 0 || bcy_stride < 0 || bcz_stride < 0)
+    return set_error(MF_ERR_ARG, "mf_solve_3d_batch: bad arguments");
+  if (n1 != sc->n[0] || n2 != sc->n[1] || n3 != sc->n[2])
+    return set_error(MF_ERR_ARG, "mf_solve_3d_batch: shape (%d,%d,%d) differs from the set-up (%d,%d,%d)", n1,
+                     n2, n3, sc->n[0], sc->n[1], sc->n[2]);
+  const long long sfull = (long long)(n1 + 2) * (n2 + 2) * (n3 + 2);
+  if (count > 1 && solf_stride < sfull)
+    return set_error(MF_ERR_ARG, "mf_solve_3d_batch: solutions overlap (stride %lld < %lld)", solf_stride, sfull);
+  for (const void* p : {(const void*)rhs, (const void*)solf, (const void*)bcx, (const void*)bcy, (const void*)bcz})
+    if (!is_device_ptr(p)) return set_error(MF_ERR_ARG, "mf_solve_3d_batch: device arrays required");
+  const double* bcs[3] = {bcx, bcy, bcz};
+  const long long sb[3] = {bcx_stride, bcy_stride, bcz_stride};
+  return solve_plain_batch(sc, count, rhs, rhs_stride, sigma, solf, solf_stride, bcs, sb,
+                           static_cast<cudaStream_t>(stream));
 }
 
 int mf_solve_3d_mixed(mf_solver3d_t* sc, const double* rhs, double sigma, double* solf,

@@ -98,6 +98,8 @@ _PROTOS = {
     "mf_solver3d_destroy": [_P],
     "mf_solve_3d": [_P, _P, _D, _P, _P, _P, _P, _I, _I, _I, _P],
     "mf_solve_3d_noalloc": [_P, _P, _D, _P, _P, _P, _P, _I, _I, _I, _P],
+    "mf_solve_3d_batch": [_P, _I, _P, ctypes.c_longlong, _D, _P, ctypes.c_longlong, _P, ctypes.c_longlong,
+                          _P, ctypes.c_longlong, _P, ctypes.c_longlong, _I, _I, _I, _P],
     "mf_solve_3d_mixed": [_P, _P, _D, _P, _P, _P, _P, _I, _I, _I, _I, _I, _P],
     "mf_solver_3d": [_P, _P, _P, _P, _P, _P, _I, _I, _I, _D, _I, _P],
     "mf_solver_residual": [_P, _P, _P, _D, _P, _P, _P, _P, _I, _I, _I, _P],
@@ -377,6 +379,21 @@ class SolverCoeffs3D:
             _check(_lib.mf_solve_3d_mixed(self._h, _arg(rhs), float(sigma), _arg(solf), _arg(bcx),
                                           _arg(bcy), _arg(bcz), n1, n2, n3, precision, refine,
                                           _stream(stream)))
+        return solf
+
+    def solve_3d_batch(self, rhs, sigma, solf, bcx, bcy, bcz, stream=None):
+        """Batched plain solve: rhs (n1,n2,n3,B) (or (n1,n2,n3), shared), solf
+        (n1+2,n2+2,n3+2,B), boundary arrays (...,2,B) or shared; torch CUDA
+        tensors, x fastest, the batch index slowest."""
+        def arg(t):
+            if t.dim() == 4 and t.shape[3] > 1:
+                return ctypes.c_void_p(t.data_ptr()), t.stride(3)
+            return ctypes.c_void_p(t.data_ptr()), 0
+        count = solf.shape[3] if solf.dim() == 4 else 1
+        (r, rs), (s, ss) = arg(rhs), arg(solf)
+        (bx, bxs), (by, bys), (bz, bzs) = arg(bcx), arg(bcy), arg(bcz)
+        _check(_lib.mf_solve_3d_batch(self._h, count, r, rs, float(sigma), s, ss, bx, bxs, by, bys, bz, bzs,
+                                      *self.n, _stream(stream)))
         return solf
 
     def solve_3d_noalloc(self, rhs, sigma, solf, bcx, bcy, bcz, stream=None):
