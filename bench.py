@@ -547,7 +547,17 @@ def row_measurements(mf, torch, hbm):
               mf.empty_device((md.shape(*c)[0] - 2, md.shape(*c)[2] - 2, 2)),
               mf.empty_device((md.shape(*c)[0] - 2, md.shape(*c)[1] - 2, 2))] for c in subs}
     ms = time_fn(lambda: md.solve(gd, ud, bd), reps=5)
-    out["multidomain_2x2x2_17_25"] = {"ninf": md.ninf(), "influence_setup_s": setup_s, "solve_ms": ms}
+    g_md = torch.cuda.CUDAGraph()
+    cap = torch.cuda.Stream()
+    cap.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(cap):
+        with torch.cuda.graph(g_md, stream=cap, capture_error_mode="relaxed"):
+            md.solve(gd, ud, bd)
+    torch.cuda.current_stream().wait_stream(cap)
+    torch.cuda.synchronize()
+    ms_graph = time_fn(g_md.replay, reps=10)
+    out["multidomain_2x2x2_17_25"] = {"ninf": md.ninf(), "influence_setup_s": setup_s, "solve_ms": ms,
+                                      "solve_graph_ms": ms_graph}
     # spline filter: 384 -> 96 points along x of a 384 x 385 x 384 fine field
     xi = mesh.uniform_grid(384)
     xo = mesh.uniform_grid(96)

@@ -94,3 +94,30 @@ def test_les_and_four_solves_step_replays_from_a_graph(mf, gpu):
     assert torch.equal(nu, nu_e)
     for a, b in zip(outs, eager):
         assert torch.equal(a, b)
+
+
+def test_multidomain_solve_replays_from_a_graph(mf, gpu):
+    import torch
+    nd = (2, 2, 1)
+    grids = [[mesh.tanh_grid(11, 1.0, 0.0, 0.5), mesh.tanh_grid(13, 1.0, 0.5, 1.0)],
+             [mesh.tanh_grid(12, 1.0, 0.0, 0.5), mesh.tanh_grid(10, 1.0, 0.5, 1.0)],
+             [mesh.tanh_grid(11, 1.0)]]
+    md = mf.MultiDomain(nd, (0, 0, 0), *grids, (1,) * 6)
+    md.influence_matrix_set(-5.0)
+    subs = md.subdomains()
+    g = {c: mf.to_device(field(md.shape(*c), 50 + i)) for i, c in enumerate(subs)}
+    bc = {}
+    for i, c in enumerate(subs):
+        nx, ny, nz = md.shape(*c)
+        bc[c] = [mf.to_device(b) for b in bc_arrays(nx - 2, ny - 2, nz - 2, 70 + i)]
+    eager = {c: mf.empty_device(md.shape(*c)) for c in subs}
+    md.solve(g, eager, bc)
+    torch.cuda.synchronize()
+    out = {c: mf.empty_device(md.shape(*c)) for c in subs}
+    graph = capture(torch, lambda: md.solve(g, out, bc))
+    for c in subs:
+        out[c].zero_()
+    graph.replay()
+    torch.cuda.synchronize()
+    for c in subs:
+        assert torch.equal(out[c], eager[c])
