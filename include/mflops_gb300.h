@@ -339,6 +339,19 @@ int mf_les_nu_velocity(mf_les_t* les, const mf_der_t* dcx, const mf_der_t* dcy,
                        const double* v, const double* w, double* nu, void* stream);
 
 /* ------------------------------------------------------------------------
+ * Channel-flow statistics: src/main/post_prod.f90:40-238 (mean, rms and
+ * cross-correlation profiles along y, friction velocity) on nt snapshots of
+ * u, v, w, p already in device memory ((nx,ny,nz) each; host grids).
+ * Outputs (host): moy[4*ny] = mean u, v, w, p normalised by u_tau (p by
+ * u_tau^2); rms[7*ny] = rms u, v, w, p and the uv, uw, vw correlations;
+ * *utau.  so: order of the compact derivative used for du/dy at the walls.
+ * ---------------------------------------------------------------------- */
+int mf_channel_stats(int nt, const double* const* u, const double* const* v, const double* const* w,
+                     const double* const* p, int nx, int ny, int nz, const double* gx, const double* gy,
+                     const double* gz, double re, int so, double* moy, double* rms, double* utau,
+                     void* stream);
+
+/* ------------------------------------------------------------------------
  * Learned LES coefficient.  No reference counterpart: the reference has only
  * the plain models above.  A 6-64-64-1 ReLU network (4,673 FP32 parameters)
  * maps six invariants of the resolved velocity gradient,

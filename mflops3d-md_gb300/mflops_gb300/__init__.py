@@ -146,6 +146,8 @@ _PROTOS = {
     "mf_flow_correct": [_I, _I, _I, _D, ctypes.POINTER(_P), ctypes.POINTER(_P), _P],
     "mf_flow_products": [_I, _I, _I, ctypes.POINTER(_P), ctypes.POINTER(_P), _P],
     "mf_flow_curl": [_I, _I, _I, ctypes.POINTER(_P), ctypes.POINTER(_P), _P],
+    "mf_channel_stats": [_I, ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.POINTER(_P),
+                         _I, _I, _I, _DP, _DP, _DP, _D, _I, _DP, _DP, _DP, _P],
     "mf_solver3d_profile": [_P, _I],
     "mf_solver3d_set_residual": [_P, _I],
     "mf_solver3d_profile_read": [_P, _I, _DP, ctypes.POINTER(ctypes.c_longlong)],
@@ -866,4 +868,24 @@ def flow_curl(dpsi, out=None, stream=None):
         out = [empty_device((nx, ny, nz)) for _ in range(3)]
     _check(_lib.mf_flow_curl(nx, ny, nz, _ptrs([dpsi[i][j] for i in range(3) for j in range(3)]),
                              _ptrs(out), _stream(stream)))
+    return out
+
+
+def channel_stats(us, vs, ws, ps, gx, gy, gz, re, so=6, stream=None):
+    """post_prod statistics of device snapshots (lists of (nx,ny,nz) fields):
+    returns {"moyu".."moyp", "rmsu".."rmsp", "rmsuv", "rmsuw", "rmsvw", "utau"}."""
+    nt = len(us)
+    nx, ny, nz = us[0].shape
+    gxa, gxp = _dptr(gx)
+    gya, gyp = _dptr(gy)
+    gza, gzp = _dptr(gz)
+    moy = np.zeros(4 * ny)
+    rms = np.zeros(7 * ny)
+    utau = ctypes.c_double()
+    _check(_lib.mf_channel_stats(nt, _ptrs(us), _ptrs(vs), _ptrs(ws), _ptrs(ps), nx, ny, nz, gxp, gyp, gzp,
+                                 float(re), int(so), moy.ctypes.data_as(_DP), rms.ctypes.data_as(_DP),
+                                 ctypes.byref(utau), _stream(stream)))
+    out = {"moy" + k: moy[q * ny:(q + 1) * ny] for q, k in enumerate("uvwp")}
+    out.update({"rms" + k: rms[q * ny:(q + 1) * ny] for q, k in enumerate(["u", "v", "w", "p", "uv", "uw", "vw"])})
+    out["utau"] = utau.value
     return out
