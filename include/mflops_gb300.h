@@ -50,6 +50,20 @@ extern "C" {
 #define MF_RESID_FP64 1
 
 const char* mf_last_error(void);
+
+/* Launch-shape autotuner (no reference counterpart).  mode 0 (default):
+ * built-in heuristics; mode 1: the first call for a problem shape times the
+ * candidate launch shapes (FP64 transform tiles 32 or 64; staged or strided
+ * x-line derivative sweeps) with CUDA events on the caller's stream, keeps
+ * the fastest and reuses it (no timing while a stream is being captured, and
+ * none for in-place derivative calls).  The candidates give identical
+ * results.  Decisions can be saved to and loaded from a text file. */
+int mf_tune_set(int mode);
+int mf_tune_get(void);
+int mf_tune_entries(void);
+int mf_tune_clear(void);
+int mf_tune_save(const char* path);
+int mf_tune_load(const char* path);
 int mf_version(void);
 /* 1 when a CUDA device is usable from this process, else 0. */
 int mf_device_available(void);

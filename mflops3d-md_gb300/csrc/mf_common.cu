@@ -2,6 +2,11 @@
 #include <cstdio>
 #include <cstring>
 
+#include <cstdio>
+#include <map>
+#include <mutex>
+#include <tuple>
+
 #include "mf_internal.h"
 #include "mf_setup.h"
 
@@ -30,6 +35,38 @@ int num_sms() {
     cached[dev] = sms;
   }
   return cached[dev];
+}
+
+namespace {
+using TuneKey = std::tuple<int, long long, long long, long long, long long>;
+std::mutex g_tune_mu;
+std::map<TuneKey, int> g_tune;
+int g_tune_mode = 0;
+}  // namespace
+
+int tune_mode() {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  return g_tune_mode;
+}
+
+int tune_lookup(int kind, long long a, long long b, long long c, long long d) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  auto it = g_tune.find(TuneKey(kind, a, b, c, d));
+  return it == g_tune.end() ? -1 : it->second;
+}
+
+void tune_store(int kind, long long a, long long b, long long c, long long d, int choice) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune[TuneKey(kind, a, b, c, d)] = choice;
+}
+
+bool stream_capturing(cudaStream_t st) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cs) != cudaSuccess) {
+    cudaGetLastError();
+    return true;  // be safe: no timing when the state is unknown
+  }
+  return cs != cudaStreamCaptureStatusNone;
 }
 
 int cuda_error(cudaError_t e, const char* what) {
@@ -190,6 +227,59 @@ int mf_solver_axis_setup(const double* grid, int nall, const int bct[2], int so,
   if (neum)
     for (int s = 0; s < 2; ++s)
       for (int m = 0; m < 7; ++m) neum[s + 2 * m] = ax.neum[7 * s + m];
+  return MF_OK;
+}
+
+int mf_tune_set(int mode) {
+  if (mode != 0 && mode != 1) return set_error(MF_ERR_ARG, "mf_tune_set: mode must be 0 or 1");
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune_mode = mode;
+  return MF_OK;
+}
+
+int mf_tune_get(void) { return tune_mode(); }
+
+int mf_tune_entries(void) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  return (int)g_tune.size();
+}
+
+int mf_tune_clear(void) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune.clear();
+  return MF_OK;
+}
+
+int mf_tune_save(const char* path) {
+  if (!path) return set_error(MF_ERR_ARG, "mf_tune_save: null path");
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  FILE* f = std::fopen(path, "w");
+  if (!f) return set_error(MF_ERR_ARG, "mf_tune_save: cannot open %s", path);
+  std::fprintf(f, "# mflops_gb300 launch-shape decisions: kind a b c d choice\n");
+  for (const auto& kv : g_tune)
+    std::fprintf(f, "%d %lld %lld %lld %lld %d\n", std::get<0>(kv.first), std::get<1>(kv.first),
+                 std::get<2>(kv.first), std::get<3>(kv.first), std::get<4>(kv.first), kv.second);
+  std::fclose(f);
+  return MF_OK;
+}
+
+int mf_tune_load(const char* path) {
+  if (!path) return set_error(MF_ERR_ARG, "mf_tune_load: null path");
+  FILE* f = std::fopen(path, "r");
+  if (!f) return set_error(MF_ERR_ARG, "mf_tune_load: cannot open %s", path);
+  char line[256];
+  int n = 0;
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  while (std::fgets(line, sizeof line, f)) {
+    if (line[0] == '#') continue;
+    int kind, choice;
+    long long a, b, c, d;
+    if (std::sscanf(line, "%d %lld %lld %lld %lld %d", &kind, &a, &b, &c, &d, &choice) == 6) {
+      g_tune[TuneKey(kind, a, b, c, d)] = choice;
+      ++n;
+    }
+  }
+  std::fclose(f);
   return MF_OK;
 }
 

@@ -28,6 +28,46 @@ bool is_device_ptr(const void* p);
 // SM count of the current device (152 on GB300), cached per device.
 int num_sms();
 
+// Launch-shape autotuner (mf_tune_*).  Decisions are keyed by a kind and four
+// shape numbers; mode 0 uses the built-in heuristics, mode 1 times the
+// candidates on first use of a shape (CUDA events on the caller's stream,
+// never while the stream is being captured) and keeps the fastest.
+enum TuneKind { kTuneGemm64 = 0, kTuneDerX = 1 };
+int tune_mode();
+int tune_lookup(int kind, long long a, long long b, long long c, long long d);
+void tune_store(int kind, long long a, long long b, long long c, long long d, int choice);
+bool stream_capturing(cudaStream_t st);
+// Times run(c) for c = 0..n-1 (one warm-up and three timed runs each) and
+// returns the fastest choice, or -1 when timing failed.
+template <class Run>
+int tune_measure(cudaStream_t st, int n, Run run) {
+  cudaEvent_t e0, e1;
+  if (cudaEventCreate(&e0) != cudaSuccess) return -1;
+  if (cudaEventCreate(&e1) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return -1;
+  }
+  int best = -1;
+  float best_ms = 0.f;
+  for (int c = 0; c < n; ++c) {
+    if (run(c)) continue;
+    cudaEventRecord(e0, st);
+    bool ok = true;
+    for (int r = 0; r < 3 && ok; ++r) ok = run(c) == 0;
+    cudaEventRecord(e1, st);
+    float ms = 0.f;
+    if (!ok || cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess)
+      continue;
+    if (best < 0 || ms < best_ms) {
+      best = c;
+      best_ms = ms;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return best;
+}
+
 // Growable device buffer owned by a handle.
 struct DevBuf {
   void* ptr = nullptr;

@@ -1137,15 +1137,34 @@ static int axis_upload(AxisDev& d, const SolverAxisHost& h) {
 
 static int gemm_f64(StageProfiler& prof, const double* X, int M, int K, const double* A, int N,
                     double* Y, const GemmEpi& e, cudaStream_t st, int B = 1, long long xs = 0,
-                    long long ys = 0) {
+                    long long ys = 0, bool may_tune = true) {
+  auto run = [&](int use64) -> int {
+    if (use64)
+      k_gemm_f64<64><<<dim3(blocks_for(M, 64), blocks_for(N, 64), B), 256, 0, st>>>(X, M, K, A, N, Y, e, xs,
+                                                                                   ys);
+    else
+      k_gemm_f64<32><<<dim3(blocks_for(M, 32), blocks_for(N, 32), B), 256, 0, st>>>(X, M, K, A, N, Y, e, xs,
+                                                                                   ys);
+    return cudaGetLastError() == cudaSuccess ? 0 : 1;
+  };
+  // tile: 64 when it gives at least two CTAs per SM (heuristic), or the
+  // measured choice for this shape (the variants differ only in speed: each
+  // output sums its K products in the same order; every epilogue is a pure
+  // store, so a timed repeat leaves the same result)
   const long long tiles64 = (long long)blocks_for(M, 64) * blocks_for(N, 64) * B;
+  int use64 = tiles64 >= 2LL * num_sms() ? 1 : 0;
+  if (may_tune && tune_mode() == 1) {
+    int c = tune_lookup(kTuneGemm64, M, N, K, B);
+    if (c < 0 && !stream_capturing(st)) {
+      c = tune_measure(st, 2, run);
+      if (c >= 0) tune_store(kTuneGemm64, M, N, K, B, c);
+    }
+    if (c >= 0) use64 = c;
+  }
   prof.begin(kProfGemm64, st);
-  if (tiles64 >= 2LL * num_sms()) {
-    k_gemm_f64<64><<<dim3(blocks_for(M, 64), blocks_for(N, 64), B), 256, 0, st>>>(X, M, K, A, N, Y, e, xs,
-                                                                                 ys);
-  } else {
-    k_gemm_f64<32><<<dim3(blocks_for(M, 32), blocks_for(N, 32), B), 256, 0, st>>>(X, M, K, A, N, Y, e, xs,
-                                                                                 ys);
+  if (run(use64)) {
+    prof.end(st);
+    return set_error(MF_ERR_CUDA, "k_gemm_f64 launch failed");
   }
   prof.end(st);
   MF_CUDA(cudaGetLastError());
@@ -1811,8 +1830,8 @@ int mf_solve_3d_noalloc(mf_solver3d_t* sc, const double* rhs, double sigma, doub
                          sc->ax[2].Vinv.as<double>()};
   const double* Vf[3] = {sc->ax[0].V.as<double>(), sc->ax[1].V.as<double>(),
                          sc->ax[2].V.as<double>()};
-  if ((rc = gemm_f64(off, w0, n2 * n3, n1, Vi[0], n1, w1, plain, st))) return rc;
-  if ((rc = gemm_f64(off, w1, n3 * n1, n2, Vi[1], n2, w0, plain, st))) return rc;
+  if ((rc = gemm_f64(off, w0, n2 * n3, n1, Vi[0], n1, w1, plain, st, 1, 0, 0, false))) return rc;
+  if ((rc = gemm_f64(off, w1, n3 * n1, n2, Vi[1], n2, w0, plain, st, 1, 0, 0, false))) return rc;
   GemmEpi div;
   div.kind = 1;
   div.lx = sc->ax[0].eig.as<double>();
@@ -1822,14 +1841,14 @@ int mf_solve_3d_noalloc(mf_solver3d_t* sc, const double* rhs, double sigma, doub
   div.thresh = kNullThresh;
   div.n1 = n1;
   div.n2 = n2;
-  if ((rc = gemm_f64(off, w0, n1 * n2, n3, Vi[2], n3, w1, div, st))) return rc;
-  if ((rc = gemm_f64(off, w1, n2 * n3, n1, Vf[0], n1, w0, plain, st))) return rc;
-  if ((rc = gemm_f64(off, w0, n3 * n1, n2, Vf[1], n2, w1, plain, st))) return rc;
+  if ((rc = gemm_f64(off, w0, n1 * n2, n3, Vi[2], n3, w1, div, st, 1, 0, 0, false))) return rc;
+  if ((rc = gemm_f64(off, w1, n2 * n3, n1, Vf[0], n1, w0, plain, st, 1, 0, 0, false))) return rc;
+  if ((rc = gemm_f64(off, w0, n3 * n1, n2, Vf[1], n2, w1, plain, st, 1, 0, 0, false))) return rc;
   GemmEpi out;
   out.kind = 2;
   out.n1 = n1;
   out.n2 = n2;
-  if ((rc = gemm_f64(off, w1, n1 * n2, n3, Vf[2], n3, solf, out, st))) return rc;
+  if ((rc = gemm_f64(off, w1, n1 * n2, n3, Vf[2], n3, solf, out, st, 1, 0, 0, false))) return rc;
   const long long p1 = n1 + 2, p2 = n2 + 2;
   for (int axis = 0; axis < 3; ++axis) {
     const AxisDev& d = sc->ax[axis];

@@ -148,6 +148,12 @@ _PROTOS = {
     "mf_flow_curl": [_I, _I, _I, ctypes.POINTER(_P), ctypes.POINTER(_P), _P],
     "mf_channel_stats": [_I, ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.POINTER(_P),
                          _I, _I, _I, _DP, _DP, _DP, _D, _I, _DP, _DP, _DP, _P],
+    "mf_tune_set": [_I],
+    "mf_tune_get": [],
+    "mf_tune_entries": [],
+    "mf_tune_clear": [],
+    "mf_tune_save": [ctypes.c_char_p],
+    "mf_tune_load": [ctypes.c_char_p],
     "mf_solver3d_profile": [_P, _I],
     "mf_solver3d_set_residual": [_P, _I],
     "mf_solver3d_profile_read": [_P, _I, _DP, ctypes.POINTER(ctypes.c_longlong)],
@@ -889,3 +895,17 @@ def channel_stats(us, vs, ws, ps, gx, gy, gz, re, so=6, stream=None):
     out.update({"rms" + k: rms[q * ny:(q + 1) * ny] for q, k in enumerate(["u", "v", "w", "p", "uv", "uw", "vw"])})
     out["utau"] = utau.value
     return out
+
+
+def tune(mode=None, save=None, load=None, clear=False):
+    """Launch-shape autotuner: mode 0 heuristics, 1 measure on first use;
+    returns (mode, number of cached decisions)."""
+    if clear:
+        _check(_lib.mf_tune_clear())
+    if load is not None:
+        _check(_lib.mf_tune_load(str(load).encode()))
+    if mode is not None:
+        _check(_lib.mf_tune_set(int(mode)))
+    if save is not None:
+        _check(_lib.mf_tune_save(str(save).encode()))
+    return _lib.mf_tune_get(), _lib.mf_tune_entries()
