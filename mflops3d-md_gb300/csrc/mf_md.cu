@@ -130,7 +130,9 @@ __global__ void k_face_gather(const double* __restrict__ du, double* out, FaceGa
   else if (f.l == 1) { i = a; j = f.m ? f.ny - 1 : 0; k = b; }
   else { i = a; j = b; k = f.m ? f.nz - 1 : 0; }
   const double v = du[i + (long long)f.nx * (j + (long long)f.ny * k)];
-  out[f.row0 + q] += f.scale * (f.m ? v : -v);
+  // atomic: the two subdomains of an interface may add concurrently; two
+  // additions onto the zeroed vector give the same sum in either order
+  atomicAdd(out + f.row0 + q, f.scale * (f.m ? v : -v));
 }
 
 // Batched influence columns: problem b has a unit value at point q0 + b of
@@ -306,7 +308,11 @@ struct mf_md {
     mf_solver3d_t* sc = nullptr;
     mf_der_t* dc[3] = {nullptr, nullptr, nullptr};
     DevBuf bc[3];      // face arrays (2 sides each)
+    DevBuf rint, du[3];  // interior right-hand side and derivative scratch of this subdomain
+    cudaStream_t stream = nullptr;  // this subdomain's branch of a solve
+    cudaEvent_t done = nullptr;
   };
+  cudaEvent_t fork = nullptr;
   std::vector<Sub> sub;  // index i + nd1*(j + nd2*k)
   DevBuf M, ipiv, vec, info, work, zero_int, du[3], rint, ufield;
   DevBuf Minv, vec2;  // row-major inverse of the influence matrix, solve output
@@ -336,7 +342,8 @@ static int md_sub_solve(mf_md* md, int s, const double* rint, double* u, cudaStr
 // Normal derivatives of u on every interface face of subdomain (i,j,k),
 // added (times scale, signed like the reference) into out[rows].
 static int md_gather(mf_md* md, int i, int j, int k, const double* u, double* out, double scale,
-                     cudaStream_t st) {
+                     cudaStream_t st, DevBuf* dus = nullptr) {
+  DevBuf* du = dus ? dus : md->du;
   const int s = md_sub_index(md, i, j, k);
   mf_md::Sub& sd = md->sub[s];
   bool need[3] = {false, false, false};
@@ -346,7 +353,7 @@ static int md_gather(mf_md* md, int i, int j, int k, const double* u, double* ou
   int rc;
   for (int l = 0; l < 3; ++l) {
     if (!need[l]) continue;
-    if ((rc = der_launch(sd.dc[l], l, 1, 3, u, md->du[l].as<double>(), sd.n[0], sd.n[1], sd.n[2], st)))
+    if ((rc = der_launch(sd.dc[l], l, 1, 3, u, du[l].as<double>(), sd.n[0], sd.n[1], sd.n[2], st)))
       return rc;
   }
   for (int l = 0; l < 3; ++l)
@@ -354,7 +361,7 @@ static int md_gather(mf_md* md, int i, int j, int k, const double* u, double* ou
       const int p = md->topo.get(i, j, k, l, m);
       if (p <= 0) continue;
       FaceGather f{l, m, sd.n[0], sd.n[1], sd.n[2], (long long)md->topo.offset[p - 1], scale};
-      k_face_gather<<<nblk(md->topo.size[p - 1], 128), 128, 0, st>>>(md->du[l].as<double>(), out, f);
+      k_face_gather<<<nblk(md->topo.size[p - 1], 128), 128, 0, st>>>(du[l].as<double>(), out, f);
       MF_CUDA(cudaGetLastError());
     }
   return MF_OK;
@@ -481,8 +488,13 @@ int mf_md_destroy(mf_md_t* md) {
     for (int l = 0; l < 3; ++l) {
       mf_der_destroy(sd.dc[l]);
       sd.bc[l].release();
+      sd.du[l].release();
     }
+    sd.rint.release();
+    if (sd.stream) cudaStreamDestroy(sd.stream);
+    if (sd.done) cudaEventDestroy(sd.done);
   }
+  if (md->fork) cudaEventDestroy(md->fork);
   for (DevBuf* b : {&md->Minv, &md->vec2, &md->ub, &md->dub[0], &md->dub[1], &md->dub[2], &md->bcb}) b->release();
   for (DevBuf* b : {&md->M, &md->ipiv, &md->vec, &md->info, &md->work, &md->zero_int, &md->du[0],
                     &md->du[1], &md->du[2], &md->rint, &md->ufield})
@@ -651,25 +663,53 @@ int mf_md_solve(mf_md_t* md, const double* const* g, double* const* u, const dou
     for (const void* p : {(const void*)g[s], (const void*)u[s], (const void*)bcx[s],
                           (const void*)bcy[s], (const void*)bcz[s]})
       if (!is_device_ptr(p)) return set_error(MF_ERR_ARG, "mf_md_solve: device pointers only");
-  MF_CUDA(cudaMemsetAsync(vec, 0, sizeof(double) * n, st));
   int rc;
+  // Each subdomain's work runs on its own stream, forked from and joined back
+  // to the caller's stream (inside a CUDA graph: parallel branches).  Streams,
+  // events and per-subdomain scratch are created by the first call.
+  if (!md->fork) {
+    MF_CUDA(cudaEventCreateWithFlags(&md->fork, cudaEventDisableTiming));
+    for (auto& sd : md->sub) {
+      MF_CUDA(cudaStreamCreateWithFlags(&sd.stream, cudaStreamNonBlocking));
+      MF_CUDA(cudaEventCreateWithFlags(&sd.done, cudaEventDisableTiming));
+      const size_t nfull = (size_t)sd.n[0] * sd.n[1] * sd.n[2];
+      if ((rc = sd.rint.ensure(nfull * 8))) return rc;
+      for (int l = 0; l < 3; ++l)
+        if ((rc = sd.du[l].ensure(nfull * 8))) return rc;
+    }
+  }
+  auto fork = [&]() -> int {
+    MF_CUDA(cudaEventRecord(md->fork, st));
+    for (auto& sd : md->sub) MF_CUDA(cudaStreamWaitEvent(sd.stream, md->fork, 0));
+    return MF_OK;
+  };
+  auto join = [&]() -> int {
+    for (auto& sd : md->sub) {
+      MF_CUDA(cudaEventRecord(sd.done, sd.stream));
+      MF_CUDA(cudaStreamWaitEvent(st, sd.done, 0));
+    }
+    return MF_OK;
+  };
+  MF_CUDA(cudaMemsetAsync(vec, 0, sizeof(double) * n, st));
   auto load_bc = [&](int s, int i, int j, int k, int mode) -> int {
     mf_md::Sub& sd = md->sub[s];
     const double* src[3] = {bcx[s], bcy[s], bcz[s]};
     for (int l = 0; l < 3; ++l) {
       const long long nf = face_points(sd, l);
-      MF_CUDA(cudaMemcpyAsync(sd.bc[l].ptr, src[l], sizeof(double) * 2 * nf, cudaMemcpyDeviceToDevice, st));
+      MF_CUDA(cudaMemcpyAsync(sd.bc[l].ptr, src[l], sizeof(double) * 2 * nf, cudaMemcpyDeviceToDevice,
+                              sd.stream));
       for (int m = 0; m < 2; ++m) {
         const int p = t.get(i, j, k, l, m);
         if (p <= 0) continue;
-        k_face_set<<<nblk(nf, 128), 128, 0, st>>>(sd.bc[l].as<double>(), nf, m, vec, t.offset[p - 1],
-                                                  mode, 0.0);
+        k_face_set<<<nblk(nf, 128), 128, 0, sd.stream>>>(sd.bc[l].as<double>(), nf, m, vec, t.offset[p - 1],
+                                                         mode, 0.0);
         MF_CUDA(cudaGetLastError());
       }
     }
     return MF_OK;
   };
   // 1. homogeneous-interface solves and the signed derivative jumps
+  if ((rc = fork())) return rc;
   for (int k = 0; k < t.nd[2]; ++k)
     for (int j = 0; j < t.nd[1]; ++j)
       for (int i = 0; i < t.nd[0]; ++i) {
@@ -677,12 +717,13 @@ int mf_md_solve(mf_md_t* md, const double* const* g, double* const* u, const dou
         mf_md::Sub& sd = md->sub[s];
         if ((rc = load_bc(s, i, j, k, 0))) return rc;
         const long long tot = (long long)(sd.n[0] - 2) * (sd.n[1] - 2) * (sd.n[2] - 2);
-        k_extract_int<<<nblk(tot, 256), 256, 0, st>>>(g[s], md->rint.as<double>(), sd.n[0] - 2,
-                                                       sd.n[1] - 2, sd.n[2] - 2);
+        k_extract_int<<<nblk(tot, 256), 256, 0, sd.stream>>>(g[s], sd.rint.as<double>(), sd.n[0] - 2,
+                                                              sd.n[1] - 2, sd.n[2] - 2);
         MF_CUDA(cudaGetLastError());
-        if ((rc = md_sub_solve(md, s, md->rint.as<double>(), u[s], st))) return rc;
-        if ((rc = md_gather(md, i, j, k, u[s], vec, 1.0, st))) return rc;
+        if ((rc = md_sub_solve(md, s, sd.rint.as<double>(), u[s], sd.stream))) return rc;
+        if ((rc = md_gather(md, i, j, k, u[s], vec, 1.0, sd.stream, sd.du))) return rc;
       }
+  if ((rc = join())) return rc;
   // 2. interface system (null-space handling as md_rhs_nullspace / md_vector_zero_lastpoint)
   if (md->null_mode == 1) {
     k_remove_mean<<<1, 256, 0, st>>>(vec, (int)n);
@@ -699,6 +740,7 @@ int mf_md_solve(mf_md_t* md, const double* const* g, double* const* u, const dou
   if (md->null_mode == 1) k_remove_mean<<<1, 256, 0, st>>>(vec, (int)n);
   MF_CUDA(cudaGetLastError());
   // 3. final solves with the interface values
+  if ((rc = fork())) return rc;
   for (int k = 0; k < t.nd[2]; ++k)
     for (int j = 0; j < t.nd[1]; ++j)
       for (int i = 0; i < t.nd[0]; ++i) {
@@ -706,12 +748,12 @@ int mf_md_solve(mf_md_t* md, const double* const* g, double* const* u, const dou
         mf_md::Sub& sd = md->sub[s];
         if ((rc = load_bc(s, i, j, k, 1))) return rc;
         const long long tot = (long long)(sd.n[0] - 2) * (sd.n[1] - 2) * (sd.n[2] - 2);
-        k_extract_int<<<nblk(tot, 256), 256, 0, st>>>(g[s], md->rint.as<double>(), sd.n[0] - 2,
-                                                       sd.n[1] - 2, sd.n[2] - 2);
+        k_extract_int<<<nblk(tot, 256), 256, 0, sd.stream>>>(g[s], sd.rint.as<double>(), sd.n[0] - 2,
+                                                              sd.n[1] - 2, sd.n[2] - 2);
         MF_CUDA(cudaGetLastError());
-        if ((rc = md_sub_solve(md, s, md->rint.as<double>(), u[s], st))) return rc;
+        if ((rc = md_sub_solve(md, s, sd.rint.as<double>(), u[s], sd.stream))) return rc;
       }
-  return MF_OK;
+  return join();
 }
 
 int mf_md_set_interface_solve(mf_md_t* md, int mode) {
