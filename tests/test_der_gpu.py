@@ -22,8 +22,10 @@ def tol(so):
 
 @pytest.mark.parametrize("so", [4, 6, 8])
 @pytest.mark.parametrize("solver", [False, True])
-@pytest.mark.parametrize("shape", [(17, 13, 11), (33, 29, 9), (65, 65, 65)])
+@pytest.mark.parametrize("shape", [(17, 13, 11), (33, 29, 9), (65, 65, 65), (150, 9, 11), (200, 11, 9)])
 def test_field_derivatives(mf, gpu, so, solver, shape):
+    # x lines: staged through shared memory up to nx = 191 (nx = 150), one
+    # thread per line above (nx = 200)
     f = field(shape, seed=2)
     fd = mf.to_device(f)
     for axis in range(3):

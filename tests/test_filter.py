@@ -82,11 +82,12 @@ def test_filter_errors(mf):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("axis", [0, 1, 2])
-def test_filter_apply_along_axes(mf, gpu, axis):
-    # fine field 3 axes, filtered along one axis onto a coarse grid
+@pytest.mark.parametrize("axis,k", [(0, 3), (1, 3), (2, 3), (0, 1), (2, 2), (0, 4), (1, 5)])
+def test_filter_apply_along_axes(mf, gpu, axis, k):
+    # fine field 3 axes, filtered along one axis onto a coarse grid (the
+    # banded kernel is instantiated per spline degree)
     shape = [21, 19, 17]
-    ni, no, nn, k = 65, 33, 17, 3
+    ni, no, nn = 65, 33, 17
     shape[axis] = ni
     xi = mesh.tanh_grid(ni, 1.5)
     xn = mesh.tanh_grid(nn, 1.0)

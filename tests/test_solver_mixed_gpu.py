@@ -137,3 +137,18 @@ def test_residual_arithmetic_modes_agree(mf, gpu, prec_name, refine):
         got[mode] = mf.to_host(out)[m]
         assert rel_l2(got[mode], ref[m]) < 1e-10
     assert rel_l2(got[mf.MF_RESID_FF], got[mf.MF_RESID_FP64]) < 1e-11
+
+
+
+def test_mixed_rejects_axes_longer_than_256(mf, gpu):
+    # 259 nodes: 257 interior points, above the transforms' 256-point tiles;
+    # the plain path accepts the same problem
+    g = mesh.uniform_grid(259)
+    g2 = mesh.uniform_grid(9)
+    sc = mf.SolverCoeffs3D(g, g2, g2, (1,) * 6, 6)
+    rhs = mf.to_device(np.zeros((257, 7, 7), order="F"))
+    bc = [mf.to_device(np.zeros(s, order="F")) for s in ((7, 7, 2), (257, 7, 2), (257, 7, 2))]
+    solf = mf.empty_device((259, 9, 9))
+    with pytest.raises(RuntimeError, match="256"):
+        sc.solve_3d(rhs, 0.0, solf, *bc, precision=mf.MF_PREC_3XTF32, refine=1)
+    sc.solve_3d(rhs, 0.0, solf, *bc)
