@@ -189,6 +189,18 @@ int mf_solve_3d_mixed(mf_solver3d_t* sc, const double* rhs, double sigma, double
                       const double* bcx, const double* bcy, const double* bcz,
                       int n1, int n2, int n3, int precision, int refine, void* stream);
 
+/* `count` problems through mf_solve_3d_mixed (precision MF_PREC_FP64: the
+ * plain solve) in one call, with host (pinned for overlap) or device arrays
+ * given per problem: the upload of problem b+1 and the download of problem
+ * b-1 run on copy streams while problem b is solved (two device staging
+ * slots).  Each problem's result equals that of a single call; the call
+ * returns when every result is in place.  No reference counterpart (the
+ * reference solves one right-hand side per call). */
+int mf_solve_3d_mixed_many(mf_solver3d_t* sc, int count, const double* const* rhs, double sigma,
+                           double* const* solf, const double* const* bcx, const double* const* bcy,
+                           const double* const* bcz, int n1, int n2, int n3, int precision,
+                           int refine, void* stream);
+
 /* class_field::solver_3d(sc,g,u,bc,sigma), src/class_field/class_field.f90:1072-1109:
  * g,u are (nx,ny,nz) fields (nx = n1+2 ...); the interior of g is the
  * right-hand side and the result is written into u. */

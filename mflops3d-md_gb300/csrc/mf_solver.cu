@@ -60,6 +60,10 @@ struct mf_solver3d {
   int P[3] = {0, 0, 0};
   DevBuf w0, w1;                               // FP64 work arrays (plain path)
   DevBuf st_rhs, st_solf, st_bc[3];            // host staging
+  // mf_solve_3d_mixed_many: two staging slots, copy-in/out streams, events
+  DevBuf pipe_rhs[2], pipe_solf[2], pipe_bc[2][3];
+  cudaStream_t cin = nullptr, cout = nullptr;
+  cudaEvent_t in_ready[2] = {nullptr, nullptr}, solved[2] = {nullptr, nullptr}, out_done[2] = {nullptr, nullptr};
   DevBuf R, R2;                                // FP64 scratch of the residual
   DevBuf U32, C32, R1f;                        // mixed path: u1, correction, r1 (FP32)
   DevBuf Xa_hi, Xa_lo, Xb_hi, Xb_lo;           // split-BF16 planes
@@ -1661,6 +1665,15 @@ int mf_solver3d_destroy(mf_solver3d_t* sc) {
                     &sc->Xb_lo, &sc->Xa32, &sc->Xb32, &sc->err, &sc->foldf, &sc->U32, &sc->C32,
                     &sc->R1f})
     b->release();
+  for (int q = 0; q < 2; ++q) {
+    sc->pipe_rhs[q].release();
+    sc->pipe_solf[q].release();
+    for (int a = 0; a < 3; ++a) sc->pipe_bc[q][a].release();
+    for (cudaEvent_t e : {sc->in_ready[q], sc->solved[q], sc->out_done[q]})
+      if (e) cudaEventDestroy(e);
+  }
+  if (sc->cin) cudaStreamDestroy(sc->cin);
+  if (sc->cout) cudaStreamDestroy(sc->cout);
   delete sc;
   return MF_OK;
 }
@@ -1762,6 +1775,73 @@ int mf_solve_3d_mixed(mf_solver3d_t* sc, const double* rhs, double sigma, double
                      [&](const double* r, double* s, const double** bcs, cudaStream_t st) {
                        return solve_mixed_dev(sc, r, sigma, s, bcs, precision, refine, st);
                      });
+}
+
+int mf_solve_3d_mixed_many(mf_solver3d_t* sc, int count, const double* const* rhs, double sigma,
+                           double* const* solf, const double* const* bcx, const double* const* bcy,
+                           const double* const* bcz, int n1, int n2, int n3, int precision, int refine,
+                           void* stream) {
+  if (!sc || count < 1 || !rhs || !solf || !bcx || !bcy || !bcz)
+    return set_error(MF_ERR_ARG, "mf_solve_3d_mixed_many: bad arguments");
+  if (n1 != sc->n[0] || n2 != sc->n[1] || n3 != sc->n[2])
+    return set_error(MF_ERR_ARG, "mf_solve_3d_mixed_many: shape (%d,%d,%d) differs from the set-up", n1, n2, n3);
+  for (int b = 0; b < count; ++b)
+    if (!rhs[b] || !solf[b] || !bcx[b] || !bcy[b] || !bcz[b])
+      return set_error(MF_ERR_ARG, "mf_solve_3d_mixed_many: null array in problem %d", b);
+  if (refine < 0) refine = 2;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const size_t rb = (size_t)n1 * n2 * n3 * 8, sb = (size_t)(n1 + 2) * (n2 + 2) * (n3 + 2) * 8;
+  const size_t bb[3] = {(size_t)n2 * n3 * 2 * 8, (size_t)n1 * n3 * 2 * 8, (size_t)n1 * n2 * 2 * 8};
+  int rc;
+  if (!sc->cin) {
+    MF_CUDA(cudaStreamCreateWithFlags(&sc->cin, cudaStreamNonBlocking));
+    MF_CUDA(cudaStreamCreateWithFlags(&sc->cout, cudaStreamNonBlocking));
+    for (int q = 0; q < 2; ++q)
+      for (cudaEvent_t* e : {&sc->in_ready[q], &sc->solved[q], &sc->out_done[q]})
+        MF_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+  }
+  for (int q = 0; q < 2; ++q) {
+    if ((rc = sc->pipe_rhs[q].ensure(rb)) || (rc = sc->pipe_solf[q].ensure(sb))) return rc;
+    for (int a = 0; a < 3; ++a)
+      if ((rc = sc->pipe_bc[q][a].ensure(bb[a]))) return rc;
+  }
+  // the copy streams start after the work already queued on the caller's stream
+  MF_CUDA(cudaEventRecord(sc->solved[0], st));
+  MF_CUDA(cudaStreamWaitEvent(sc->cin, sc->solved[0], 0));
+  const double* const* bsrc[3] = {bcx, bcy, bcz};
+  for (int b = 0; b < count; ++b) {
+    const int q = b & 1;
+    if (b >= 2) {  // slot q is free once problem b-2 is solved and downloaded
+      MF_CUDA(cudaStreamWaitEvent(sc->cin, sc->solved[q], 0));
+      MF_CUDA(cudaStreamWaitEvent(sc->cin, sc->out_done[q], 0));
+    }
+    MF_CUDA(cudaMemcpyAsync(sc->pipe_rhs[q].ptr, rhs[b], rb, cudaMemcpyDefault, sc->cin));
+    MF_CUDA(cudaMemcpyAsync(sc->pipe_solf[q].ptr, solf[b], sb, cudaMemcpyDefault, sc->cin));
+    const double* bcs[3];
+    for (int a = 0; a < 3; ++a) {
+      MF_CUDA(cudaMemcpyAsync(sc->pipe_bc[q][a].ptr, bsrc[a][b], bb[a], cudaMemcpyDefault, sc->cin));
+      bcs[a] = sc->pipe_bc[q][a].as<double>();
+    }
+    MF_CUDA(cudaEventRecord(sc->in_ready[q], sc->cin));
+    MF_CUDA(cudaStreamWaitEvent(st, sc->in_ready[q], 0));
+    double* s = sc->pipe_solf[q].as<double>();
+    rc = precision == MF_PREC_FP64
+             ? solve_plain_dev(sc, sc->pipe_rhs[q].as<double>(), sigma, s, bcs, st)
+             : solve_mixed_dev(sc, sc->pipe_rhs[q].as<double>(), sigma, s, bcs, precision, refine, st);
+    if (rc) return rc;
+    MF_CUDA(cudaEventRecord(sc->solved[q], st));
+    MF_CUDA(cudaStreamWaitEvent(sc->cout, sc->solved[q], 0));
+    MF_CUDA(cudaMemcpyAsync(solf[b], s, sb, cudaMemcpyDefault, sc->cout));
+    MF_CUDA(cudaEventRecord(sc->out_done[q], sc->cout));
+  }
+  MF_CUDA(cudaStreamSynchronize(sc->cout));
+  MF_CUDA(cudaStreamSynchronize(st));
+  if (sc->err.ptr) {
+    int herr = 0;
+    MF_CUDA(cudaMemcpy(&herr, sc->err.ptr, sizeof(int), cudaMemcpyDeviceToHost));
+    if (herr) return set_error(MF_ERR_TIMEOUT, "solve_3d: a tensor-core pipeline wait expired");
+  }
+  return MF_OK;
 }
 
 int mf_solver_3d(mf_solver3d_t* sc, const double* g, double* u, const double* bcx,

@@ -98,6 +98,8 @@ _PROTOS = {
     "mf_solver3d_destroy": [_P],
     "mf_solve_3d": [_P, _P, _D, _P, _P, _P, _P, _I, _I, _I, _P],
     "mf_solve_3d_noalloc": [_P, _P, _D, _P, _P, _P, _P, _I, _I, _I, _P],
+    "mf_solve_3d_mixed_many": [_P, _I, ctypes.POINTER(_P), _D, ctypes.POINTER(_P), ctypes.POINTER(_P),
+                               ctypes.POINTER(_P), ctypes.POINTER(_P), _I, _I, _I, _I, _I, _P],
     "mf_solve_3d_batch": [_P, _I, _P, ctypes.c_longlong, _D, _P, ctypes.c_longlong, _P, ctypes.c_longlong,
                           _P, ctypes.c_longlong, _P, ctypes.c_longlong, _I, _I, _I, _P],
     "mf_solve_3d_mixed": [_P, _P, _D, _P, _P, _P, _P, _I, _I, _I, _I, _I, _P],
@@ -387,6 +389,16 @@ class SolverCoeffs3D:
             _check(_lib.mf_solve_3d_mixed(self._h, _arg(rhs), float(sigma), _arg(solf), _arg(bcx),
                                           _arg(bcy), _arg(bcz), n1, n2, n3, precision, refine,
                                           _stream(stream)))
+        return solf
+
+    def solve_3d_many(self, rhs, sigma, solf, bcx, bcy, bcz, precision=MF_PREC_FP64, refine=-1,
+                      stream=None):
+        """Several problems in one call (lists of host or device arrays, one
+        entry per problem); uploads and downloads overlap the solves."""
+        count = len(rhs)
+        mk = lambda seq: (_P * count)(*[_arg(a) for a in seq])
+        _check(_lib.mf_solve_3d_mixed_many(self._h, count, mk(rhs), float(sigma), mk(solf), mk(bcx), mk(bcy),
+                                           mk(bcz), *self.n, int(precision), int(refine), _stream(stream)))
         return solf
 
     def solve_3d_batch(self, rhs, sigma, solf, bcx, bcy, bcz, stream=None):

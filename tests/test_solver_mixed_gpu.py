@@ -152,3 +152,25 @@ def test_mixed_rejects_axes_longer_than_256(mf, gpu):
     with pytest.raises(RuntimeError, match="256"):
         sc.solve_3d(rhs, 0.0, solf, *bc, precision=mf.MF_PREC_3XTF32, refine=1)
     sc.solve_3d(rhs, 0.0, solf, *bc)
+
+
+@pytest.mark.parametrize("prec_name,refine", [("MF_PREC_FP64", -1), ("MF_PREC_3XTF32", 1)])
+def test_many_problems_equal_single_calls(mf, gpu, prec_name, refine):
+    """mf_solve_3d_mixed_many (uploads/downloads overlapping the solves) gives
+    each problem exactly the result of a single call, host arrays in and out."""
+    nall = (34, 30, 26)
+    gx, gy, gz = grids(*nall, kind="tanh")
+    sc = mf.SolverCoeffs3D(gx, gy, gz, (1, 2, 1, 1, 2, 1), 6)
+    n1, n2, n3 = (v - 2 for v in nall)
+    prec = getattr(mf, prec_name)
+    B = 5
+    rhs = [field((n1, n2, n3), 80 + b) for b in range(B)]
+    bcs = [bc_arrays(n1, n2, n3, 90 + b) for b in range(B)]
+    solf0 = [field(nall, 100 + b) for b in range(B)]  # edges and corners are kept
+    outs = [np.asfortranarray(s.copy()) for s in solf0]
+    sc.solve_3d_many(rhs, -4.0, outs, [b[0] for b in bcs], [b[1] for b in bcs], [b[2] for b in bcs],
+                     precision=prec, refine=refine)
+    for b in range(B):
+        one = np.asfortranarray(solf0[b].copy())
+        sc.solve_3d(rhs[b], -4.0, one, *bcs[b], precision=prec, refine=refine)
+        assert np.array_equal(outs[b], one), b
