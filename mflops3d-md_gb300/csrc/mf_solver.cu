@@ -48,6 +48,10 @@ struct AxisDev {
   DevBuf rowsf;                                // FP32 copy of rows
   DevBuf tri;                                  // TriRow[n] when the lhs is tridiagonal
   bool tri_ok = false;
+  // Null mode (the one eigenvalue below the threshold, when there is exactly
+  // one; -1 otherwise): row null_idx of V^-1 and column null_idx of V (FP64)
+  int null_idx = -1;
+  DevBuf null_row, null_col;
 };
 
 }  // namespace mf
@@ -65,6 +69,8 @@ struct mf_solver3d {
   cudaStream_t cin = nullptr, cout = nullptr;
   cudaEvent_t in_ready[2] = {nullptr, nullptr}, solved[2] = {nullptr, nullptr}, out_done[2] = {nullptr, nullptr};
   DevBuf R, R2;                                // FP64 scratch of the residual
+  DevBuf nullpart;                             // null-mode projection: partial sums, coefficient
+  DevBuf R1d;                                  // closed operators: FP64 r1 of the refinement
   DevBuf U32, C32, R1f;                        // mixed path: u1, correction, r1 (FP32)
   DevBuf Xa_hi, Xa_lo, Xb_hi, Xb_lo;           // split-BF16 planes
   DevBuf Xa32, Xb32;                           // 3xTF32 operands (FP32)
@@ -863,6 +869,113 @@ __global__ void k_finalize(const float* __restrict__ u1, const float* __restrict
   }
 }
 
+// Null-mode projection (all-Neumann or periodic operators at sigma = 0).
+// The eigenvalue division zeroes the coefficient of the null mode, so the
+// solution depends on a residual r only through
+//   r_c = r - c v,   c = l . r,   l = l_x (x) l_y (x) l_z,  v = v_x (x) v_y (x) v_z,
+// with l_a the row of V_a^-1 and v_a the column of V_a of the null eigenvalue
+// (l . v = 1), and has c = 0 itself.  A residual keeps the rhs component c,
+// which no iterate can remove; narrowed to FP32 together with it, r would
+// lose its small part to the rounding of c and the refinement would stall.
+// Likewise the operator cannot see an error along v, so the refinement
+// cannot correct the solution's own null coefficient.  Kernels: per-plane
+// partial sums of c, their sum in a fixed order, the projected residual
+// narrowed into the operand of the next approximate solve, and the
+// projection of the FP64 solution in place.
+constexpr int kNullThreads = 256;
+constexpr int kNullRows = 16;  // y rows per CTA of the partial sums
+
+// part[k * G + g] = l_z(k) sum_i l_x(i) sum_{j in chunk g} l_y(j) r(i, j, k),
+// r(i, j, k) = r[i + sy j + sz k].  Grid (n3, G = ceil(n2 / kNullRows));
+// fixed summation order.
+template <class T>
+__global__ void __launch_bounds__(kNullThreads) k_null_part(const T* __restrict__ r, long long sy, long long sz,
+                                                            const double* __restrict__ lx,
+                                                            const double* __restrict__ ly,
+                                                            const double* __restrict__ lz, int n1, int n2,
+                                                            double* __restrict__ part) {
+  __shared__ double red[kNullThreads];
+  const int k = blockIdx.x, j0 = blockIdx.y * kNullRows, j1 = min(n2, j0 + kNullRows);
+  const T* rk = r + sz * k;
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < n1; i += kNullThreads) {
+    double s = 0.0;
+#pragma unroll 4
+    for (int j = j0; j < j1; ++j) s = fma(ly[j], (double)rk[i + sy * j], s);
+    acc = fma(lx[i], s, acc);
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int h = kNullThreads / 2; h > 0; h >>= 1) {
+    if (threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[(long long)k * gridDim.y + blockIdx.y] = red[0] * lz[k];
+}
+
+// part[count] = sum of part[0..count), one CTA, fixed order.
+__global__ void __launch_bounds__(kNullThreads) k_null_sum(double* __restrict__ part, int count) {
+  __shared__ double red[kNullThreads];
+  double acc = 0.0;
+  for (int q = threadIdx.x; q < count; q += kNullThreads) acc += part[q];
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int h = kNullThreads / 2; h > 0; h >>= 1) {
+    if (threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[count] = red[0];
+}
+
+// v = narrow(r - c v_x(i) v_y(j) v_z(k)) (r dense, FP64 or FP32; c = 0 when
+// coef is null) into the operand of the next approximate solve (x32 for 3xTF32, else BF16 hi/lo
+// planes; padded layout i + P1 (j + P2 k)) and, with r32, into the FP32
+// residual copy.  Grid: x over i (blocks of 256), y = j, z strides over k.
+template <class T>
+__global__ void k_null_split(const T* __restrict__ r, const double* __restrict__ coef,
+                             const double* __restrict__ vx, const double* __restrict__ vy,
+                             const double* __restrict__ vz, int n1, int n2, int n3, int P1, int P2,
+                             __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo,
+                             float* __restrict__ x32, float* __restrict__ r32) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+  if (i >= n1) return;
+  const double cxy = coef ? coef[0] * vx[i] * vy[j] : 0.0;
+  const long long plane = (long long)n1 * n2, pplane = (long long)P1 * P2;
+  const long long base = i + (long long)n1 * j, pbase = i + (long long)P1 * j;
+  for (int k = blockIdx.z; k < n3; k += gridDim.z) {
+    const double x = coef ? fma(-cxy, vz[k], (double)r[base + plane * k]) : (double)r[base + plane * k];
+    float v;
+    if constexpr (sizeof(T) == 8)
+      v = narrow(x);
+    else
+      v = (float)x;
+    const long long o = pbase + pplane * k;
+    if (x32) {
+      x32[o] = v;
+    } else {
+      const __nv_bfloat16 h = __float2bfloat16_rn(v);
+      hi[o] = h;
+      lo[o] = __float2bfloat16_rn(v - __bfloat162float(h));
+    }
+    if (r32) r32[base + plane * k] = v;
+  }
+}
+
+// u(i, j, k) -= c v_x(i) v_y(j) v_z(k) in place, u(i, j, k) = u[i + sy j + sz k].
+// Grid as k_null_split.
+__global__ void k_null_remove(double* __restrict__ u, long long sy, long long sz,
+                              const double* __restrict__ coef, const double* __restrict__ vx,
+                              const double* __restrict__ vy, const double* __restrict__ vz, int n1,
+                              int n3) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+  if (i >= n1) return;
+  const double cxy = coef[0] * vx[i] * vy[j];
+  for (int k = blockIdx.z; k < n3; k += gridDim.z) {
+    double& x = u[i + sy * j + sz * k];
+    x = fma(-cxy, vz[k], x);
+  }
+}
+
 // rhs minus the boundary folds, in FP32, split straight into BF16 planes
 // (padded layout).  Only feeds the first approximate solve of the mixed
 // path: the FP64 residual that follows carries the boundary data exactly.
@@ -957,7 +1070,7 @@ __global__ void k_extract_interior(const double* __restrict__ g, double* __restr
 static inline unsigned blocks_for(long long n, int t) { return (unsigned)((n + t - 1) / t); }
 
 // Profiler kinds (see mf_solver3d_profile_read in the C ABI).
-enum ProfKind { kProfTc = 0, kProfResidX = 1, kProfResidYZ = 2, kProfSplit = 3, kProfFold = 4,
+enum ProfKind { kProfTc = 0, kProfResidX = 1, kProfResidYZ = 2, kProfNull = 3, kProfFold = 4,
                 kProfFaces = 5, kProfGemm64 = 6, kProfCopy = 7, kProfTcDivide = 8,
                 kProfTcUpdate = 9, kProfResid32 = 10 };
 
@@ -1029,11 +1142,28 @@ static int axis_set_eigen(AxisDev& d, const std::vector<double>& eig, const std:
   if ((rc = upload(d.Vh32, h32)) || (rc = upload(d.Vl32, l32))) return rc;
   std::vector<float> ef(d.P, 0.f);
   std::vector<uint8_t> nf(d.P, 0);
+  int nnull = 0;
   for (int i = 0; i < d.n; ++i) {
     ef[i] = (float)eig[i];
     nf[i] = std::fabs(eig[i]) < kNullThresh ? 1 : 0;
+    if (nf[i]) {
+      d.null_idx = i;
+      ++nnull;
+    }
   }
   if ((rc = upload(d.eigf, ef)) || (rc = upload(d.nullf, nf))) return rc;
+  if (nnull != 1) {
+    d.null_idx = -1;
+    d.null_row.release();
+    d.null_col.release();
+    return MF_OK;
+  }
+  std::vector<double> row(d.n), col(d.n);
+  for (int i = 0; i < d.n; ++i) {
+    row[i] = Vinv[(size_t)d.null_idx * d.n + i];
+    col[i] = V[(size_t)i * d.n + d.null_idx];
+  }
+  if ((rc = upload(d.null_row, row)) || (rc = upload(d.null_col, col))) return rc;
   return MF_OK;
 }
 
@@ -1530,6 +1660,71 @@ static int fold_split(mf_solver3d* sc, bool tf32, const double* rhs, const doubl
   return MF_OK;
 }
 
+// A closed operator: every axis has exactly one null eigenvalue (Neumann at
+// both ends), so the 3-D operator has a null mode at sigma = 0 and a
+// near-null one at small sigma.  Its refinement residuals are formed in FP64
+// (the FP32 residual update loses ~1e-9 relative on it: the low modes
+// magnify the FP32 rounding of the residual), and at sigma = 0 they are
+// projected (null_project).
+static bool closed_operator(const mf_solver3d* sc) {
+  return sc->ax[0].null_idx >= 0 && sc->ax[1].null_idx >= 0 && sc->ax[2].null_idx >= 0;
+}
+
+// Null coefficient c = l . r of r(i, j, k) = r[i + sy j + sz k], left in
+// the device scalar returned through coef.
+template <class T>
+static int null_coef(mf_solver3d* sc, const T* r, long long sy, long long sz, const double** coef,
+                     cudaStream_t st) {
+  const int n1 = sc->n[0], n2 = sc->n[1], n3 = sc->n[2];
+  const int groups = (n2 + kNullRows - 1) / kNullRows;
+  const int count = n3 * groups;
+  int rc;
+  if ((rc = sc->nullpart.ensure(sizeof(double) * (count + 1)))) return rc;
+  double* part = sc->nullpart.as<double>();
+  k_null_part<T><<<dim3(n3, groups), kNullThreads, 0, st>>>(r, sy, sz, sc->ax[0].null_row.as<double>(),
+                                                            sc->ax[1].null_row.as<double>(),
+                                                            sc->ax[2].null_row.as<double>(), n1, n2, part);
+  k_null_sum<<<1, kNullThreads, 0, st>>>(part, count);
+  *coef = part + count;
+  return MF_OK;
+}
+
+// Dense FP64 residual r, minus its null-mode component when `project`,
+// narrowed into the operand of the next approximate solve.
+static int null_project(mf_solver3d* sc, const double* r, bool project, __nv_bfloat16* hi,
+                        __nv_bfloat16* lo, float* x32, cudaStream_t st) {
+  using T = double;
+  const int n1 = sc->n[0], n2 = sc->n[1], n3 = sc->n[2];
+  const double* coef = nullptr;
+  float* r32 = nullptr;
+  int rc;
+  sc->prof.begin(kProfNull, st);
+  if (project && (rc = null_coef<T>(sc, r, n1, (long long)n1 * n2, &coef, st))) return rc;
+  k_null_split<T><<<dim3(blocks_for(n1, 256), n2, std::min(n3, 16)), 256, 0, st>>>(
+      r, coef, sc->ax[0].null_col.as<double>(), sc->ax[1].null_col.as<double>(),
+      sc->ax[2].null_col.as<double>(), n1, n2, n3, sc->P[0], sc->P[1], hi, lo, x32, r32);
+  sc->prof.end(st);
+  MF_CUDA(cudaGetLastError());
+  return MF_OK;
+}
+
+// Removes the null-mode component of the interior of solf (in place).
+static int null_remove(mf_solver3d* sc, double* solf, cudaStream_t st) {
+  const int n1 = sc->n[0], n2 = sc->n[1], n3 = sc->n[2];
+  const long long sy = n1 + 2, sz = (long long)(n1 + 2) * (n2 + 2);
+  double* u = solf + 1 + sy + sz;
+  const double* coef = nullptr;
+  int rc;
+  sc->prof.begin(kProfNull, st);
+  if ((rc = null_coef<double>(sc, u, sy, sz, &coef, st))) return rc;
+  k_null_remove<<<dim3(blocks_for(n1, 256), n2, std::min(n3, 16)), 256, 0, st>>>(
+      u, sy, sz, coef, sc->ax[0].null_col.as<double>(), sc->ax[1].null_col.as<double>(),
+      sc->ax[2].null_col.as<double>(), n1, n3);
+  sc->prof.end(st);
+  MF_CUDA(cudaGetLastError());
+  return MF_OK;
+}
+
 // Mixed-precision solve:
 //   u1 = S~ (rhs - fold)                        (FP32 fold, tensor-core solve)
 //   r1 = rhs - A u1                             (FP64 residual, boundary data)
@@ -1539,7 +1734,10 @@ static int fold_split(mf_solver3d* sc, bool tf32, const double* rhs, const doubl
 // S~ is the approximate inverse by six tensor-core transforms (split-BF16
 // or 3xTF32).  The cancellation in r_k = r1 - A C is relative to |r1|
 // (~1e-5 |rhs|), so FP32 keeps it to ~1e-12 |rhs|; the FP64 residual of u1
-// carries the accuracy.
+// carries the accuracy.  On a closed operator (closed_operator) every
+// residual is formed in FP64 (r_k = r1 - A C with r1 kept in FP64); at
+// sigma = 0 each is projected (null_project) before it is narrowed, and the
+// null component of the result is removed (null_remove).
 static int solve_mixed_dev(mf_solver3d* sc, const double* rhs, double sigma, double* solf,
                            const double* bcs[3], int prec, int refine, cudaStream_t st) {
   if (prec != MF_PREC_SPLIT_BF16 && prec != MF_PREC_3XTF32)
@@ -1554,10 +1752,23 @@ static int solve_mixed_dev(mf_solver3d* sc, const double* rhs, double sigma, dou
   float* x32 = tf32 ? sc->Xa32.as<float>() : nullptr;
   float* u1 = sc->U32.as<float>();
   float* C = sc->C32.as<float>();
+  const bool closed = closed_operator(sc), project = closed && std::fabs(sigma) < kNullThresh;
+  if (closed && refine > 1 && (rc = sc->R1d.ensure(tot * 8))) return rc;
   if ((rc = fold_split(sc, tf32, rhs, bcs, st))) return rc;
   if ((rc = approx_solve(sc, tf32, sigma, u1, false, st))) return rc;
   for (int it = 0; it < refine; ++it) {
-    if (it == 0) {
+    if (closed) {
+      // FP64 residuals: r1 = rhs - A u1 (kept in R1d when more steps follow),
+      // r_k = r1 - A C; projected at sigma = 0, then narrowed
+      double* r = (it == 0 && refine > 1) ? sc->R1d.as<double>() : sc->R.as<double>();
+      if ((rc = residual_passes<double, float>(sc, it == 0 ? rhs : sc->R1d.as<double>(), it == 0 ? u1 : C,
+                                               sigma, it == 0 ? bcs : nullptr, sc->R.as<double>(),
+                                               sc->R2.as<double>(), r, (__nv_bfloat16*)nullptr,
+                                               (__nv_bfloat16*)nullptr, (float*)nullptr, (float*)nullptr,
+                                               kProfResidX, kProfResidYZ, st)) ||
+          (rc = null_project(sc, r, project, xh, xl, x32, st)))
+        return rc;
+    } else if (it == 0) {
       // the FP32 copy of r1 only feeds later refinement steps
       if ((rc = residual_passes<double, float>(sc, rhs, u1, sigma, bcs, sc->R.as<double>(),
                                                sc->R2.as<double>(), (double*)nullptr, xh, xl, x32,
@@ -1579,6 +1790,7 @@ static int solve_mixed_dev(mf_solver3d* sc, const double* rhs, double sigma, dou
                                                                n2, n3);
   sc->prof.end(st);
   MF_CUDA(cudaGetLastError());
+  if (project && (rc = null_remove(sc, solf, st))) return rc;
   return faces(sc, solf, bcs, st);
 }
 
@@ -1657,13 +1869,13 @@ int mf_solver3d_destroy(mf_solver3d_t* sc) {
   for (auto& d : sc->ax) {
     for (DevBuf* b : {&d.V, &d.Vinv, &d.eig, &d.invl4, &d.rows, &d.Vh, &d.Vl, &d.Vih, &d.Vil,
                       &d.Vh32, &d.Vl32, &d.Vih32, &d.Vil32, &d.eigf, &d.nullf, &d.invl4f,
-                      &d.rowsf, &d.tri})
+                      &d.rowsf, &d.tri, &d.null_row, &d.null_col})
       b->release();
   }
   for (DevBuf* b : {&sc->w0, &sc->w1, &sc->st_rhs, &sc->st_solf, &sc->st_bc[0], &sc->st_bc[1],
                     &sc->st_bc[2], &sc->R, &sc->R2, &sc->Xa_hi, &sc->Xa_lo, &sc->Xb_hi,
                     &sc->Xb_lo, &sc->Xa32, &sc->Xb32, &sc->err, &sc->foldf, &sc->U32, &sc->C32,
-                    &sc->R1f})
+                    &sc->R1f, &sc->nullpart, &sc->R1d})
     b->release();
   for (int q = 0; q < 2; ++q) {
     sc->pipe_rhs[q].release();

@@ -439,7 +439,7 @@ class SolverCoeffs3D:
         _check(_lib.mf_solver3d_set_eigen(self._h, axis, ep, v.ctypes.data_as(_DP),
                                           vi.ctypes.data_as(_DP)))
 
-    PROFILE_KINDS = ("tc_transform", "residual_x", "residual_yz", "split_bf16", "bc_fold",
+    PROFILE_KINDS = ("tc_transform", "residual_x", "residual_yz", "null_projection", "bc_fold",
                      "bc_faces", "fp64_transform", "interior_copy", "tc_transform_divide",
                      "tc_transform_update", "residual_fp32")
 
