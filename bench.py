@@ -623,7 +623,8 @@ def row_measurements(mf, torch, hbm):
     # the solver work of one NS step at 128 x 129 x 128 (periodic-free stand-in:
     # Dirichlet velocity, Neumann pressure): LES viscosity from the velocity,
     # three velocity Helmholtz solves (3xTF32 + 1 refinement) and the pressure
-    # Poisson solve (plain FP64), eagerly and as one CUDA-graph replay
+    # Poisson solve at sigma = 0 (3xTF32 + 1 refinement with the null-mode
+    # projection; plain FP64 beside it), eagerly and as one CUDA-graph replay
     shape = (128, 129, 128)
     gx, gy, gz = mesh.uniform_grid(128), mesh.tanh_grid(129, 2.0), mesh.uniform_grid(128)
     interior = tuple(v - 2 for v in shape)
@@ -638,23 +639,30 @@ def row_measurements(mf, torch, hbm):
     outs = [mf.empty_device(shape) for _ in range(4)]
     nu = mf.empty_device(shape)
 
-    def step():
+    def step(pressure_prec):
         les.nu_velocity(*dcs, *vel, 1, 0.17, out=nu)
         for q in range(3):
             sc_u.solve_3d(rhs[q], -1e6, outs[q], *bcs, precision=mf.MF_PREC_3XTF32, refine=1)
-        sc_p.solve_3d(rhs[3], -1e-3, outs[3], *bcs)
+        sc_p.solve_3d(rhs[3], 0.0, outs[3], *bcs, precision=pressure_prec, refine=1)
 
-    eager = time_fn(step, reps=5)
-    g = torch.cuda.CUDAGraph()
-    cap = torch.cuda.Stream()
-    cap.wait_stream(torch.cuda.current_stream())
-    with torch.cuda.stream(cap):
-        with torch.cuda.graph(g, stream=cap, capture_error_mode="relaxed"):
-            step()
-    torch.cuda.current_stream().wait_stream(cap)
-    torch.cuda.synchronize()
-    replay = time_fn(g.replay, reps=5)
-    out["step_les_3helmholtz_1poisson_128x129x128"] = {"eager_ms": eager, "graph_ms": replay}
+    def graph_of(fn):
+        g = torch.cuda.CUDAGraph()
+        cap = torch.cuda.Stream()
+        cap.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(cap):
+            with torch.cuda.graph(g, stream=cap, capture_error_mode="relaxed"):
+                fn()
+        torch.cuda.current_stream().wait_stream(cap)
+        torch.cuda.synchronize()
+        return g
+
+    row = {}
+    for key, prec in (("", mf.MF_PREC_3XTF32), ("fp64_pressure_", mf.MF_PREC_FP64)):
+        row[key + "eager_ms"] = time_fn(lambda: step(prec), reps=5)
+        g = graph_of(lambda: step(prec))
+        row[key + "graph_ms"] = time_fn(g.replay, reps=5)
+        del g
+    out["step_les_3helmholtz_1poisson_128x129x128"] = row
     return out
 
 

@@ -60,7 +60,7 @@ def test_solve_replays_from_a_graph(mf, gpu, precision, refine):
     assert torch.equal(out, eager)
 
 
-def test_les_and_four_solves_step_replays_from_a_graph(mf, gpu):
+def test_les_and_five_solves_step_replays_from_a_graph(mf, gpu):
     import torch
     n = 33
     g = mesh.tanh_grid(n, 1.5)
@@ -79,12 +79,15 @@ def test_les_and_four_solves_step_replays_from_a_graph(mf, gpu):
         for q in range(3):
             sc_u.solve_3d(rhs[q], -1e3, outs[q], *bcs, precision=2, refine=1)
         sc_p.solve_3d(rhs[3], -1e-3, outs[3], *zbc)
+        # pressure at sigma = 0 through the mixed path: FP64 refinement
+        # residuals, null-mode projection and removal
+        sc_p.solve_3d(rhs[3], 0.0, outs[4], *zbc, precision=mf.MF_PREC_3XTF32, refine=2)
 
-    eager = [mf.empty_device((n, n, n)) for _ in range(4)]
+    eager = [mf.empty_device((n, n, n)) for _ in range(5)]
     nu_e = mf.empty_device((n, n, n))
     step(eager, nu_e)
     torch.cuda.synchronize()
-    outs = [mf.empty_device((n, n, n)) for _ in range(4)]
+    outs = [mf.empty_device((n, n, n)) for _ in range(5)]
     nu = mf.empty_device((n, n, n))
     graph = capture(torch, lambda: step(outs, nu))
     for o in outs + [nu]:
