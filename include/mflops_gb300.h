@@ -450,6 +450,60 @@ int mf_flow_products(int nx, int ny, int nz, const double* const* u, double* con
 /* u = curl(psi) from dpsi[3i+j] = d psi_i / d x_j, 0 on the walls. */
 int mf_flow_curl(int nx, int ny, int nz, const double* const* dpsi, double* const* u, void* stream);
 
+/* ------------------------------------------------------------------------
+ * Navier-Stokes time step on one domain (the caller of the derivative and
+ * solver entry points): src/main/navier3d.f90:48-274 with
+ * src/class_navier/class_navier_3D.f90 -- presolve with the nonlinear terms
+ * and the forcing (:1528-1595, 1169-1222, 1043-1167), boundary gradient
+ * (:695-791), velocity Helmholtz solves (:1597-1761), pressure-increment
+ * Poisson solve (:1764-1845, 342-393), projection (:1847-1959),
+ * extrapolation (:2010-2050), slot rotation and the driver's diagnostics
+ * (navier3d.f90:120-261).  Covered: mpid%dims = 0 (one domain), mapt = 0,
+ * nsubite = 1, les_type = 0, pressure types 1 and 2.  Velocity Dirichlet and
+ * pressure Neumann on all faces; boundary values and sources from the
+ * reference's exact solution `sol` (:927-1041, steady: wt = 0).  Fields are
+ * (nx,ny,nz) FP64 device arrays, x fastest.
+ * ---------------------------------------------------------------------- */
+typedef struct mf_navier mf_navier_t;
+typedef struct {
+  double ts;          /* time step (cmd%ts) */
+  double reynolds;    /* cmd%reynolds */
+  int nlt;            /* nonlinear form: 0 none, 1 advective, 2 skew-symmetric (reference default 2) */
+  int pt;             /* pressure type 1 or 2 (default 1) */
+  int tou;            /* BDF order 1, 2, 3 of the velocity (default 2) */
+  int top;            /* pressure extrapolation order + 1 (default 2) */
+  int so_solver;      /* so(1), default 6 */
+  int so_der;         /* so(2), default 6 */
+  int flow_rate;      /* 1: the flow-rate term of f for u (always on in the reference) */
+  int nmodes;         /* modes of the exact solution (5 in the reference) */
+  int precision;      /* solves: MF_PREC_FP64 (the reference's arithmetic) or a mixed mode */
+  int refine;         /* refinement steps of the mixed solves, < 0: default */
+} mf_navier_params_t;
+/* Fills the reference's defaults (command_line.f90:14-35). */
+int mf_navier_defaults(mf_navier_params_t* p);
+/* navier_initialization (class_navier_3D.f90:2084-2345), one domain: host
+ * grids, all fields zero, time 0. */
+int mf_navier_create(const double* gx, int nx, const double* gy, int ny, const double* gz, int nz,
+                     const mf_navier_params_t* p, mf_navier_t** out);
+int mf_navier_destroy(mf_navier_t* nav);
+/* Field var (0..4 = u, v, w, p, phi) of time level `level` (0 = it(1), the
+ * slot the next step writes, ..., 3 = it(nt), the newest): device pointer,
+ * or a copy from / to host or device memory. */
+int mf_navier_field(mf_navier_t* nav, int var, int level, double** ptr);
+int mf_navier_set_field(mf_navier_t* nav, int var, int level, const double* f, void* stream);
+int mf_navier_get_field(mf_navier_t* nav, int var, int level, double* f, void* stream);
+/* One time step: navier_time, the step, then (diag != NULL) the driver's
+ * diagnostics of level it(nt), which remove the weighted mean of that
+ * level's pressure, then the slot rotation.  diag[12] = div V; V error,
+ * relative, time-accumulated; P error, relative, time-accumulated; kinetic
+ * energy; P and V stationarity (value, relative).  Without diag the step
+ * makes no host synchronisation (capturable in a CUDA graph once the
+ * nonlinear-term cache is warm, e.g. after nt steps; a capture of nt steps
+ * returns the slots to the same order). */
+int mf_navier_step(mf_navier_t* nav, double* diag, void* stream);
+/* Simulated time and the flow-rate state (debit, g; 0 before the first step). */
+int mf_navier_state(mf_navier_t* nav, double* time, double* debit, double* g);
+
 #ifdef __cplusplus
 }
 #endif

@@ -18,7 +18,7 @@ OBJDIR = os.path.join(HERE, "_build")
 LIBNAME = "libmflops_gb300.so"
 SOURCES = ["mf_common.cu", "mf_der.cu", "mf_solver.cu", "mf_tc.cu", "mf_setup.cpp",
            "mf_md.cu", "mf_filter.cu", "mf_les.cu", "mf_mlp.cu", "mf_flow.cu",
-           "mf_stats.cu"]
+           "mf_stats.cu", "mf_navier.cu"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -1,0 +1,961 @@
+// Navier-Stokes time step on one domain: the caller of the derivative and
+// solver entry points, src/main/navier3d.f90:48-274 built from
+// src/class_navier/class_navier_3D.f90 (one domain, mapt = 0, nsubite = 1,
+// les_type = 0, pressure types 1 and 2).
+//
+// Time levels: nt = 4 slots per variable (u, v, w, p, phi) addressed through
+// the permutation it(1..nt) of the reference (it(1) = the slot a step
+// writes, it(nt) = the newest); the host keeps `it` and rotates it after each
+// step (navier3d.f90:256-261).  The nonlinear term of a slot depends only on
+// that slot's u, v, w, which do not change once the slot is final, so it is
+// cached per slot: each step computes it for the newest slot only, where the
+// reference recomputes all nt slots and reads two or three of them
+// (class_navier_3D.f90:1169-1222); the values read are the same.
+//
+// The exact solution `sol` of the reference (class_navier_3D.f90:927-1041) is
+// steady (wt = 0: cos(wt t) = 1, sin(wt t) = 0 at every t), so its boundary
+// values and sources are evaluated once, at set-up, on the device.
+//
+// Stages per step (device work only, on the caller's stream):
+//   flow-rate term   weighted sum of extrapol(u) (k_ns_wsum) -> k_ns_flow
+//   presolve         k_ns_nonlinear (newest slot) + k_ns_presolve
+//   boundary values  k_ns_bc_velocity (+ gradient of extrapol(phi), pt = 1)
+//   velocity solves  k_ns_fu (interior rhs) + three Helmholtz solves
+//   pressure         k_ns_scale, div of rhs_p, k_ns_fphi, k_ns_bc_phi, one
+//                    all-Neumann Poisson solve at sigma = 0
+//   projection       k_ns_pressure, k_ns_velocity
+// Pointwise kernels fuse the edge zeroing of field_zero_edges
+// (class_field.f90:366-391) into their stores.
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "mf_internal.h"
+
+namespace mf {
+namespace {
+
+constexpr int kNsThreads = 256;
+constexpr int kNt = 4;
+constexpr int kDiagSums = 11;
+constexpr int kWRows = 16;  // y rows per CTA of the weighted sums
+
+inline unsigned ns_blocks(long long n) { return (unsigned)((n + kNsThreads - 1) / kNsThreads); }
+
+__device__ __forceinline__ void idx3(long long q, int nx, int ny, int& i, int& j, int& k) {
+  i = (int)(q % nx);
+  const long long r = q / nx;
+  j = (int)(r % ny);
+  k = (int)(r / ny);
+}
+
+// A point on an edge or a corner: at least two indices on the boundary.
+__device__ __forceinline__ bool on_edge(int i, int j, int k, int nx, int ny, int nz) {
+  return (i == 0 || i == nx - 1) + (j == 0 || j == ny - 1) + (k == 0 || k == nz - 1) >= 2;
+}
+
+// Exact solution and sources of the reference at grid points, t with
+// cos(wt t) = 1, sin(wt t) = 0 (wt = 0): ex[0] = u, ex[1] = v, ex[2] = p,
+// ex[3] = rhsu, ex[4] = rhsv (w and rhsw are 0).  Same expression order as
+// sol (class_navier_3D.f90:1005-1036).
+__global__ void k_ns_exact(const double* __restrict__ gx, const double* __restrict__ gy,
+                           const double* __restrict__ gz, int nx, int ny, int nz, int nmodes, double pi,
+                           double rey, double* __restrict__ ex) {
+  const long long n = (long long)nx * ny * nz;
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  int i, j, k;
+  idx3(q, nx, ny, i, j, k);
+  const double x = gx[i], y = gy[j];
+  (void)gz;
+  double u = 0.0, v = 0.0, p = 0.0, fu = 0.0, fv = 0.0;
+  const double a = 1.0, b = 1.0, ct = 1.0, st = 0.0;
+  for (int m = 1; m <= nmodes; ++m) {
+    const double wx = pi * m, wy = pi * m, wp = pi * m, wt = 0.0 * m * pi;
+    const double sx = sin(wx * x), cx = cos(wx * x), sy = sin(wy * y), cy = cos(wy * y);
+    const double cyx = cos(wp * (y - x));
+    u = u + a * sx * cy * ct / wx;
+    v = v - a * cx * sy * ct / wy;
+    p = p + b * sin(wp * (x - y)) * ct;
+    fu = fu + (b * wp * ct * cyx + a * a * (ct * ct) * cx * sx * (sy * sy + cy * cy) / wx +
+               a * ct * sx * cy * (wy * wy / wx + wx) / rey - a * wt * st * sx * cy / wx);
+    fv = fv + (-b * wp * ct * cyx + a * a * (ct * ct) * cy * sy * (sx * sx + cx * cx) / wy -
+               a * ct * cx * sy * (wy + wx * wx / wy) / rey + a * wt * st * cx * sy / wy);
+  }
+  ex[q] = u;
+  ex[n + q] = v;
+  ex[2 * n + q] = p;
+  ex[3 * n + q] = fu;
+  ex[4 * n + q] = fv;
+}
+
+// Face arrays of one variable: bcx (ny-2, nz-2, 2), bcy (nx-2, nz-2, 2),
+// bcz (nx-2, ny-2, 2), stored one after the other (Fortran order each).
+struct Faces {
+  int nx, ny, nz;
+  long long sx, sy, sz;  // sizes of bcx, bcy, bcz
+  __device__ __forceinline__ long long total() const { return sx + sy + sz; }
+  // Face point q -> grid index (i, j, k) and the tangential derivative
+  // axis selector a (0 = x face, 1 = y face, 2 = z face).
+  __device__ __forceinline__ void point(long long q, int& a, int& i, int& j, int& k) const {
+    if (q < sx) {
+      a = 0;
+      const int n2 = ny - 2, n3 = nz - 2;
+      j = (int)(q % n2) + 1;
+      k = (int)((q / n2) % n3) + 1;
+      i = (q / ((long long)n2 * n3)) ? nx - 1 : 0;
+    } else if (q < sx + sy) {
+      q -= sx;
+      a = 1;
+      const int n1 = nx - 2, n3 = nz - 2;
+      i = (int)(q % n1) + 1;
+      k = (int)((q / n1) % n3) + 1;
+      j = (q / ((long long)n1 * n3)) ? ny - 1 : 0;
+    } else {
+      q -= sx + sy;
+      a = 2;
+      const int n1 = nx - 2, n2 = ny - 2;
+      i = (int)(q % n1) + 1;
+      j = (int)((q / n1) % n2) + 1;
+      k = (q / ((long long)n1 * n2)) ? nz - 1 : 0;
+    }
+  }
+};
+
+// Exact face values of u, v (w = 0): bcex[c * total + q] from the exact fields.
+__global__ void k_ns_bc_exact(Faces F, const double* __restrict__ ex, long long n, double* __restrict__ bcex) {
+  const long long tot = F.total();
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= tot) return;
+  int a, i, j, k;
+  F.point(q, a, i, j, k);
+  const long long g = i + (long long)F.nx * (j + (long long)F.ny * k);
+  bcex[q] = ex[g];
+  bcex[tot + q] = ex[n + g];
+  bcex[2 * tot + q] = 0.0;
+}
+
+// navier_bc_velocity + add_boundary_gradient (class_navier_3D.f90:395-433,
+// 695-791): bc of u, v, w = exact values; with d (pt = 1) the tangential
+// components get + d_t(extrapol(phi)) / fac(1): v and w on the x faces, u and
+// w on the y faces, u and v on the z faces.  d[0..2] = d/dx, d/dy, d/dz.
+__global__ void k_ns_bc_velocity(Faces F, const double* __restrict__ bcex, const double* __restrict__ dx,
+                                 const double* __restrict__ dy, const double* __restrict__ dz, double fac1,
+                                 double* __restrict__ bc) {
+  const long long tot = F.total();
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= tot) return;
+  int a, i, j, k;
+  F.point(q, a, i, j, k);
+  const long long g = i + (long long)F.nx * (j + (long long)F.ny * k);
+  for (int c = 0; c < 3; ++c) {
+    double val = bcex[c * tot + q];
+    if (dx && c != a) {
+      const double* d = c == 0 ? dx : c == 1 ? dy : dz;
+      val = val + d[g] / fac1;
+    }
+    bc[c * tot + q] = val;
+  }
+}
+
+// navier_bc_pressure (class_navier_3D.f90:342-393), one domain:
+// bcphi on the faces normal to axis a = rhs_p(a)(face) - fac(1) bc of the
+// normal velocity component.
+__global__ void k_ns_bc_phi(Faces F, const double* __restrict__ rpx, const double* __restrict__ rpy,
+                            const double* __restrict__ rpz, const double* __restrict__ bcvel, double fac1,
+                            double* __restrict__ bcphi) {
+  const long long tot = F.total();
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= tot) return;
+  int a, i, j, k;
+  F.point(q, a, i, j, k);
+  const long long g = i + (long long)F.nx * (j + (long long)F.ny * k);
+  const double* rp = a == 0 ? rpx : a == 1 ? rpy : rpz;
+  bcphi[q] = rp[g] - fac1 * bcvel[a * tot + q];
+}
+
+// Linear combination of up to three time levels (navier_extrapol,
+// class_navier_3D.f90:2010-2050): out = c0 a0 + c1 a1 + c2 a2 (m terms, m = 0
+// gives 0), edges zeroed.
+struct Lin {
+  int m;
+  double c[3];
+  const double* a[3];
+};
+
+__device__ __forceinline__ double lin_at(const Lin& L, long long q) {
+  if (L.m == 0) return 0.0;
+  double acc = L.c[0] * L.a[0][q];
+  if (L.m > 1) acc = acc + L.c[1] * L.a[1][q];
+  if (L.m > 2) acc = acc + L.c[2] * L.a[2][q];
+  return acc;
+}
+
+__global__ void k_ns_extrapol(Lin L, int nx, int ny, int nz, double* __restrict__ out) {
+  const long long n = (long long)nx * ny * nz;
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  int i, j, k;
+  idx3(q, nx, ny, i, j, k);
+  out[q] = on_edge(i, j, k, nx, ny, nz) ? 0.0 : lin_at(L, q);
+}
+
+// x u, x v, x w of one slot (the products of the skew-symmetric form).
+__global__ void k_ns_products(long long n, const double* __restrict__ x, const double* __restrict__ u,
+                              const double* __restrict__ v, const double* __restrict__ w,
+                              double* __restrict__ pu, double* __restrict__ pv, double* __restrict__ pw) {
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const double xv = x[q];
+  pu[q] = xv * u[q];
+  pv[q] = xv * v[q];
+  pw[q] = xv * w[q];
+}
+
+// navier_nonlinear of one slot: nlt 1: u dx + v dy + w dz; nlt 2: half of it
+// plus halves of d(xu)/dx, d(xv)/dy, d(xw)/dz (class_navier_3D.f90:1195-1213);
+// nlt 0: 0.
+__global__ void k_ns_nonlinear(long long n, int nlt, const double* __restrict__ u,
+                               const double* __restrict__ v, const double* __restrict__ w,
+                               const double* __restrict__ dx, const double* __restrict__ dy,
+                               const double* __restrict__ dz, const double* __restrict__ px,
+                               const double* __restrict__ py, const double* __restrict__ pz,
+                               double* __restrict__ out) {
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  if (nlt != 1 && nlt != 2) {
+    out[q] = 0.0;
+    return;
+  }
+  double t = u[q] * dx[q] + v[q] * dy[q] + w[q] * dz[q];
+  if (nlt == 2) {
+    t = t * 0.5;
+    t = t + px[q] * 0.5;
+    t = t + py[q] * 0.5;
+    t = t + pz[q] * 0.5;
+  }
+  out[q] = t;
+}
+
+// navier_presolve_{u,v,w} (class_navier_3D.f90:1528-1595):
+// rhs = zero_edges(f - zero_edges(extrapol(nonlinear))) with f the exact
+// source (src, null for w) plus the flow-rate term g (u only, *g).
+__global__ void k_ns_presolve(Lin L, int nx, int ny, int nz, const double* __restrict__ src,
+                              const double* __restrict__ g, double* __restrict__ rhs) {
+  const long long n = (long long)nx * ny * nz;
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  int i, j, k;
+  idx3(q, nx, ny, i, j, k);
+  if (on_edge(i, j, k, nx, ny, nz)) {
+    rhs[q] = 0.0;
+    return;
+  }
+  double f = src ? src[q] : 0.0;
+  if (g) f = f + g[0];
+  rhs[q] = f - lin_at(L, q);
+}
+
+// navier_solve_{u,v,w} right-hand side (class_navier_3D.f90:1612-1635) at the
+// interior points, written as the solver's interior array:
+// fu = Re (((fac2 x_n + fac3 x_n-1) [+ fac4 x_n-2] [+ grad]) - rhs).
+__global__ void k_ns_fu(int nx, int ny, int nz, const double* __restrict__ x0, const double* __restrict__ x1,
+                        const double* __restrict__ x2, double f2, double f3, double f4,
+                        const double* __restrict__ grad, const double* __restrict__ rhs, double rey,
+                        double* __restrict__ out) {
+  const int n1 = nx - 2, n2 = ny - 2, n3 = nz - 2;
+  const long long n = (long long)n1 * n2 * n3;
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  int i, j, k;
+  idx3(q, n1, n2, i, j, k);
+  const long long g = (i + 1) + (long long)nx * ((j + 1) + (long long)ny * (k + 1));
+  double f = 0.0;
+  f = f + f2 * x0[g] + f3 * x1[g];
+  if (x2) f = f + f4 * x2[g];
+  if (grad) f = f + grad[g];
+  f = f - rhs[g];
+  out[q] = rey * f;
+}
+
+// out = zero_edges(s x)  (navier_phi_rhs, pt <= 2: fac(1) u*).
+__global__ void k_ns_scale(int nx, int ny, int nz, double s, const double* __restrict__ x,
+                           double* __restrict__ out) {
+  const long long n = (long long)nx * ny * nz;
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  int i, j, k;
+  idx3(q, nx, ny, i, j, k);
+  out[q] = on_edge(i, j, k, nx, ny, nz) ? 0.0 : s * x[q];
+}
+
+// navier_solve_phi right-hand side at the interior points
+// (class_navier_3D.f90:1808-1813): sigmap extrapol(phi) + d rhs_px/dx +
+// d rhs_py/dy + d rhs_pz/dz.
+__global__ void k_ns_fphi(int nx, int ny, int nz, double sigmap, const double* __restrict__ ext,
+                          const double* __restrict__ ddx, const double* __restrict__ ddy,
+                          const double* __restrict__ ddz, double* __restrict__ out) {
+  const int n1 = nx - 2, n2 = ny - 2, n3 = nz - 2;
+  const long long n = (long long)n1 * n2 * n3;
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  int i, j, k;
+  idx3(q, n1, n2, i, j, k);
+  const long long g = (i + 1) + (long long)nx * ((j + 1) + (long long)ny * (k + 1));
+  double f = sigmap * ext[g];
+  f = f + ddx[g] + ddy[g] + ddz[g];
+  out[q] = f;
+}
+
+// In-place field_zero_edges.
+__global__ void k_ns_zero_edges(int nx, int ny, int nz, double* __restrict__ f) {
+  const long long n = (long long)nx * ny * nz;
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  int i, j, k;
+  idx3(q, nx, ny, i, j, k);
+  if (on_edge(i, j, k, nx, ny, nz)) f[q] = 0.0;
+}
+
+// navier_projection, pressure (class_navier_3D.f90:1878-1896):
+// p = zero_edges(zero_edges(phi [+ aux]) - (div_x + div_y + div_z) / Re).
+__global__ void k_ns_pressure(int nx, int ny, int nz, const double* __restrict__ phi,
+                              const double* __restrict__ aux, const double* __restrict__ ddx,
+                              const double* __restrict__ ddy, const double* __restrict__ ddz, double rey,
+                              double* __restrict__ p) {
+  const long long n = (long long)nx * ny * nz;
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  int i, j, k;
+  idx3(q, nx, ny, i, j, k);
+  if (on_edge(i, j, k, nx, ny, nz)) {
+    p[q] = 0.0;
+    return;
+  }
+  double v = phi[q];
+  if (aux) v = v + aux[q];
+  const double div = (ddx[q] + ddy[q] + ddz[q]) / rey;
+  p[q] = v - div;
+}
+
+// navier_projection, velocity (:1943-1949): x = zero_edges((rhs_p - dphi) / fac(1)).
+__global__ void k_ns_velocity(int nx, int ny, int nz, const double* __restrict__ rp,
+                              const double* __restrict__ dphi, double fac1, double* __restrict__ x) {
+  const long long n = (long long)nx * ny * nz;
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  int i, j, k;
+  idx3(q, nx, ny, i, j, k);
+  x[q] = on_edge(i, j, k, nx, ny, nz) ? 0.0 : (rp[q] - dphi[q]) / fac1;
+}
+
+// Quadrature weight of integrale / norme2 (class_navier_3D.f90:2419-2603):
+// half widths w_x(i) w_y(j) w_z(k) at the interior and face points, 0 on
+// edges and corners.
+struct Weights {
+  const double *wx, *wy, *wz;
+  int nx, ny, nz;
+  __device__ __forceinline__ double at(int i, int j, int k) const {
+    return on_edge(i, j, k, nx, ny, nz) ? 0.0 : wx[i] * wy[j] * wz[k];
+  }
+};
+
+// Block sums of kS quantities in a fixed order; thread 0 writes them.
+template <int kS>
+__device__ __forceinline__ void block_sums(double (&acc)[kS], double* __restrict__ out) {
+  __shared__ double red[kS][kNsThreads];
+#pragma unroll
+  for (int s = 0; s < kS; ++s) red[s][threadIdx.x] = acc[s];
+  __syncthreads();
+  for (int h = kNsThreads / 2; h > 0; h >>= 1) {
+    if (threadIdx.x < h)
+#pragma unroll
+      for (int s = 0; s < kS; ++s) red[s][threadIdx.x] += red[s][threadIdx.x + h];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (int s = 0; s < kS; ++s) out[s] = red[s][0];
+}
+
+// part[k * G + g] = sum over the y rows of chunk g of plane k of W f.
+// Grid (nz, G = ceil(ny / kWRows)).
+__global__ void __launch_bounds__(kNsThreads) k_ns_wsum(Weights W, const double* __restrict__ f,
+                                                        double* __restrict__ part) {
+  const int k = blockIdx.x, j0 = blockIdx.y * kWRows, j1 = min(W.ny, j0 + kWRows);
+  double acc[1] = {0.0};
+  for (int j = j0; j < j1; ++j)
+    for (int i = threadIdx.x; i < W.nx; i += kNsThreads)
+      acc[0] += W.at(i, j, k) * f[i + (long long)W.nx * (j + (long long)W.ny * k)];
+  block_sums<1>(acc, part + (long long)k * gridDim.y + blockIdx.y);
+}
+
+// out[s] = sum over p of part[p * nsum + s], one CTA, fixed order.
+__global__ void __launch_bounds__(kNsThreads) k_ns_sum_parts(const double* __restrict__ part, int count,
+                                                             int nsum, double* __restrict__ out) {
+  __shared__ double red[kNsThreads];
+  for (int s = 0; s < nsum; ++s) {
+    double acc = 0.0;
+    for (int p = threadIdx.x; p < count; p += kNsThreads) acc += part[(long long)p * nsum + s];
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int h = kNsThreads / 2; h > 0; h >>= 1) {
+      if (threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) out[s] = red[0];
+    __syncthreads();
+  }
+}
+
+// Flow-rate term of f for u (class_navier_3D.f90:1140-1164), one thread:
+// err = integrale(extrapol(u)) / integrale(1); on the first call debit = err
+// (1 when <= 1e-10, a single-precision literal) and g = 3 debit; then
+// g -= (err - debit) fac(1).  state = {g, debit, initialised}.
+__global__ void k_ns_flow(const double* __restrict__ isum, double reft, double fac1, double thresh,
+                          double* __restrict__ state) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double err = isum[0] / reft;
+  if (state[2] == 0.0) {
+    double debit = err;
+    if (debit <= thresh) debit = 1.0;
+    state[1] = debit;
+    state[0] = 3.0 * debit;
+    state[2] = 1.0;
+  }
+  err = err - state[1];
+  state[0] = state[0] - err * fac1;
+}
+
+// Driver diagnostics (navier3d.f90:120-254), weighted sums in three phases.
+struct DiagIn {
+  const double *u, *v, *w, *p, *up, *vp, *wp, *pp;  // levels it(nt) and it(nt-1)
+  const double *dx, *dy, *dz;                       // du/dx, dv/dy, dw/dz of it(nt)
+  const double *ue, *ve, *pex;                      // exact fields
+  double pexm, auxm;                                // means removed in phases 1, 2
+};
+
+// Grid (nz, G); part[(k G + g) kDiagSums + s].
+template <int kPhase>
+__global__ void __launch_bounds__(kNsThreads) k_ns_diag(Weights W, DiagIn D, double* __restrict__ part) {
+  const int k = blockIdx.x, j0 = blockIdx.y * kWRows, j1 = min(W.ny, j0 + kWRows);
+  double acc[kDiagSums];
+#pragma unroll
+  for (int s = 0; s < kDiagSums; ++s) acc[s] = 0.0;
+  for (int j = j0; j < j1; ++j)
+    for (int i = threadIdx.x; i < W.nx; i += kNsThreads) {
+      const double wq = W.at(i, j, k);
+      const long long q = i + (long long)W.nx * (j + (long long)W.ny * k);
+      if (kPhase == 0) {
+        const double div = D.dx[q] + D.dy[q] + D.dz[q];
+        const double ue = D.ue[q], ve = D.ve[q], we = 0.0;
+        const double r1 = sqrt(ue * ue + ve * ve + we * we);
+        const double eu = ue - D.u[q], ev = ve - D.v[q], ew = we - D.w[q];
+        const double r2 = sqrt(eu * eu + ev * ev + ew * ew);
+        const double du = D.u[q] - D.up[q], dv = D.v[q] - D.vp[q], dw = D.w[q] - D.wp[q];
+        acc[0] += wq * div * div;
+        acc[1] += wq * r1 * r1;
+        acc[2] += wq * r2 * r2;
+        acc[3] += wq * D.p[q];
+        acc[4] += wq * D.u[q] * D.u[q];
+        acc[5] += wq * D.v[q] * D.v[q];
+        acc[6] += wq * D.w[q] * D.w[q];
+        acc[7] += wq * du * du;
+        acc[8] += wq * dv * dv;
+        acc[9] += wq * dw * dw;
+        acc[10] += wq * D.pex[q];
+      } else if (kPhase == 1) {
+        const double pe = D.pex[q] - D.pexm;
+        const double e = D.p[q] - pe;
+        acc[0] += wq * e * e;
+        acc[1] += wq * pe * pe;
+        acc[2] += wq * (D.p[q] - D.pp[q]);
+      } else {
+        const double a = (D.p[q] - D.pp[q]) - D.auxm;
+        acc[0] += wq * a * a;
+      }
+    }
+  block_sums<kDiagSums>(acc, part + ((long long)k * gridDim.y + blockIdx.y) * kDiagSums);
+}
+
+// f += s at every point (the driver's removal of the pressure mean).
+__global__ void k_ns_shift(long long n, double s, double* __restrict__ f) {
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < n) f[q] = f[q] + s;
+}
+
+}  // namespace
+}  // namespace mf
+
+using namespace mf;
+
+struct mf_navier {
+  mf_navier_params_t prm;
+  int nx = 0, ny = 0, nz = 0, n1 = 0, n2 = 0, n3 = 0;
+  long long np = 0, nin = 0;
+  double fac[4] = {0, 0, 0, 0};
+  double sigmau = 0.0, sigmap = 0.0, time = 0.0;
+  int it[kNt] = {0, 1, 2, 3};
+  bool nl_ok[kNt] = {false, false, false, false};
+  int rhs_cur = 0;
+  mf_der_t *dcx = nullptr, *dcy = nullptr, *dcz = nullptr;
+  mf_solver3d_t *scu = nullptr, *scp = nullptr;
+  DevBuf fields;  // [5 vars][kNt slots] fields
+  DevBuf nl;      // [3][kNt] cached nonlinear terms
+  DevBuf rhs;     // [3][2] rhs_u(1), rhs_u(2) ...
+  DevBuf rp;      // rhs_px, rhs_py, rhs_pz
+  DevBuf tmp;     // 9 work fields
+  DevBuf fin;     // interior right-hand side of a solve
+  DevBuf exact;   // u, v, p, rhsu, rhsv of the exact solution
+  DevBuf bcex;    // exact face values of u, v, w
+  DevBuf bc;      // face values of u, v, w, phi
+  DevBuf grid;    // gx, gy, gz
+  DevBuf wts;     // half widths wx, wy, wz
+  DevBuf part;    // partial sums
+  DevBuf sums;    // summed values
+  DevBuf state;   // flow-rate term: g, debit, initialised
+  Faces faces{};
+  double reft = 0.0;  // integrale(1)
+  double err_vts = 0.0, err_pre = 0.0;
+
+  double* F(int var, int slot) const { return fields.as<double>() + ((size_t)var * kNt + slot) * np; }
+  double* NL(int c, int slot) const { return nl.as<double>() + ((size_t)c * kNt + slot) * np; }
+  double* RHS(int c, int which) const { return rhs.as<double>() + ((size_t)c * 2 + which) * np; }
+  double* RP(int c) const { return rp.as<double>() + (size_t)c * np; }
+  double* T(int t) const { return tmp.as<double>() + (size_t)t * np; }
+  double* EX(int q) const { return exact.as<double>() + (size_t)q * np; }
+  double* BC(int c) const { return bc.as<double>() + (size_t)c * (faces.sx + faces.sy + faces.sz); }
+  Weights weights() const {
+    const double* w = wts.as<double>();
+    return Weights{w, w + nx, w + nx + ny, nx, ny, nz};
+  }
+};
+
+namespace {
+
+constexpr int kVarU = 0, kVarP = 3, kVarPhi = 4;
+
+// extrapol of var (navier_extrapol, subite = 1) of the given order:
+// -1 -> it(1); 1 -> it(nt); 2 -> 2 it(nt) - it(nt-1); 3 -> 3 it(nt) - 3 it(nt-1) + it(nt-2); else 0.
+Lin extrapol_of(const mf_navier* nv, int order, double* (*slot_ptr)(const mf_navier*, int, int), int var) {
+  Lin L{};
+  const int* it = nv->it;
+  auto P = [&](int s) { return slot_ptr(nv, var, s); };
+  if (order == -1) {
+    L.m = 1; L.c[0] = 1.0; L.a[0] = P(it[0]);
+  } else if (order == 1) {
+    L.m = 1; L.c[0] = 1.0; L.a[0] = P(it[kNt - 1]);
+  } else if (order == 2) {
+    L.m = 2; L.c[0] = 2.0; L.a[0] = P(it[kNt - 1]); L.c[1] = -1.0; L.a[1] = P(it[kNt - 2]);
+  } else if (order == 3) {
+    L.m = 3; L.c[0] = 3.0; L.a[0] = P(it[kNt - 1]); L.c[1] = -3.0; L.a[1] = P(it[kNt - 2]);
+    L.c[2] = 1.0; L.a[2] = P(it[kNt - 3]);
+  } else {
+    L.m = 0;
+  }
+  return L;
+}
+
+double* field_ptr(const mf_navier* nv, int var, int slot) { return nv->F(var, slot); }
+double* nl_ptr(const mf_navier* nv, int c, int slot) { return nv->NL(c, slot); }
+
+int der(const mf_navier* nv, int axis, const double* f, double* df, cudaStream_t st) {
+  const mf_der_t* dc = axis == 0 ? nv->dcx : axis == 1 ? nv->dcy : nv->dcz;
+  return mf_der_apply(dc, axis, 1, f, df, nv->nx, nv->ny, nv->nz, st);
+}
+
+int launch_check(const char* what) {
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? MF_OK : cuda_error(e, what);
+}
+
+int extrapol_into(const mf_navier* nv, const Lin& L, double* out, cudaStream_t st) {
+  k_ns_extrapol<<<ns_blocks(nv->np), kNsThreads, 0, st>>>(L, nv->nx, nv->ny, nv->nz, out);
+  return launch_check("k_ns_extrapol");
+}
+
+// Nonlinear term of component c (0..2) at `slot` into its cache entry.
+int nonlinear(mf_navier* nv, int c, int slot, cudaStream_t st) {
+  const double* x = nv->F(c, slot);
+  const double *u = nv->F(0, slot), *v = nv->F(1, slot), *w = nv->F(2, slot);
+  int rc;
+  if (nv->prm.nlt == 1 || nv->prm.nlt == 2) {
+    if ((rc = der(nv, 0, x, nv->T(0), st)) || (rc = der(nv, 1, x, nv->T(1), st)) ||
+        (rc = der(nv, 2, x, nv->T(2), st)))
+      return rc;
+  }
+  if (nv->prm.nlt == 2) {
+    k_ns_products<<<ns_blocks(nv->np), kNsThreads, 0, st>>>(nv->np, x, u, v, w, nv->T(3), nv->T(4), nv->T(5));
+    if ((rc = launch_check("k_ns_products")) || (rc = der(nv, 0, nv->T(3), nv->T(6), st)) ||
+        (rc = der(nv, 1, nv->T(4), nv->T(7), st)) || (rc = der(nv, 2, nv->T(5), nv->T(8), st)))
+      return rc;
+  }
+  k_ns_nonlinear<<<ns_blocks(nv->np), kNsThreads, 0, st>>>(nv->np, nv->prm.nlt, u, v, w, nv->T(0), nv->T(1),
+                                                           nv->T(2), nv->T(6), nv->T(7), nv->T(8),
+                                                           nv->NL(c, slot));
+  return launch_check("k_ns_nonlinear");
+}
+
+int solve(mf_navier* nv, mf_solver3d_t* sc, double sigma, double* solf, const double* bc3,
+          cudaStream_t st) {
+  const double* bx = bc3;
+  const double* by = bc3 + nv->faces.sx;
+  const double* bz = bc3 + nv->faces.sx + nv->faces.sy;
+  const double* rhs = nv->fin.as<double>();
+  if (nv->prm.precision == MF_PREC_FP64)
+    return mf_solve_3d(sc, rhs, sigma, solf, bx, by, bz, nv->n1, nv->n2, nv->n3, st);
+  return mf_solve_3d_mixed(sc, rhs, sigma, solf, bx, by, bz, nv->n1, nv->n2, nv->n3, nv->prm.precision,
+                           nv->prm.refine, st);
+}
+
+// Weighted sum of f into nv->sums[0] (device).
+int wsum(mf_navier* nv, const double* f, cudaStream_t st) {
+  const int groups = (nv->ny + kWRows - 1) / kWRows;
+  k_ns_wsum<<<dim3(nv->nz, groups), kNsThreads, 0, st>>>(nv->weights(), f, nv->part.as<double>());
+  k_ns_sum_parts<<<1, kNsThreads, 0, st>>>(nv->part.as<double>(), nv->nz * groups, 1, nv->sums.as<double>());
+  return launch_check("k_ns_wsum");
+}
+
+}  // namespace
+
+namespace {
+
+// One time step without the rotation (navier3d.f90:57-102, nsubite = 1).
+int ns_step(mf_navier* nv, cudaStream_t st) {
+  const mf_navier_params_t& P = nv->prm;
+  const int* it = nv->it;
+  const int nw = it[0], s0 = it[kNt - 1], s1 = it[kNt - 2], s2 = it[kNt - 3];
+  const double fac1 = nv->fac[0];
+  const unsigned gb = ns_blocks(nv->np);
+  const long long ftot = nv->faces.sx + nv->faces.sy + nv->faces.sz;
+  const unsigned fb = ns_blocks(ftot);
+  int rc;
+  nv->time += P.ts;  // navier_time
+  // presolve: nonlinear terms of the slots that extrapol('v') reads
+  const Lin nlv0 = extrapol_of(nv, P.tou, nl_ptr, 0);
+  for (int t = 0; t < nlv0.m; ++t) {
+    const int slot = t == 0 ? s0 : t == 1 ? s1 : s2;
+    if (!nv->nl_ok[slot]) {
+      for (int c = 0; c < 3; ++c)
+        if ((rc = nonlinear(nv, c, slot, st))) return rc;
+      nv->nl_ok[slot] = true;
+    }
+  }
+  // flow-rate term of f for u
+  const double* g = nullptr;
+  if (P.flow_rate) {
+    if ((rc = extrapol_into(nv, extrapol_of(nv, P.tou, field_ptr, kVarU), nv->T(0), st)) ||
+        (rc = wsum(nv, nv->T(0), st)))
+      return rc;
+    k_ns_flow<<<1, 1, 0, st>>>(nv->sums.as<double>(), nv->reft, fac1, (double)1e-10f, nv->state.as<double>());
+    if ((rc = launch_check("k_ns_flow"))) return rc;
+    g = nv->state.as<double>();
+  }
+  nv->rhs_cur ^= 1;  // rhs(2) = rhs(1): the other buffer keeps the previous step's
+  for (int c = 0; c < 3; ++c) {
+    const double* src = c == 0 ? nv->EX(3) : c == 1 ? nv->EX(4) : nullptr;
+    k_ns_presolve<<<gb, kNsThreads, 0, st>>>(extrapol_of(nv, P.tou, nl_ptr, c), nv->nx, nv->ny, nv->nz, src,
+                                             c == 0 ? g : nullptr, nv->RHS(c, nv->rhs_cur));
+    if ((rc = launch_check("k_ns_presolve"))) return rc;
+  }
+  // velocity boundary values (+ gradient of extrapol(phi) for pt = 1)
+  const Lin ephi = extrapol_of(nv, P.top - 1, field_ptr, kVarPhi);
+  if (P.pt == 1) {
+    if ((rc = extrapol_into(nv, ephi, nv->T(0), st)) || (rc = der(nv, 0, nv->T(0), nv->T(1), st)) ||
+        (rc = der(nv, 1, nv->T(0), nv->T(2), st)) || (rc = der(nv, 2, nv->T(0), nv->T(3), st)))
+      return rc;
+    k_ns_bc_velocity<<<fb, kNsThreads, 0, st>>>(nv->faces, nv->bcex.as<double>(), nv->T(1), nv->T(2), nv->T(3),
+                                                fac1, nv->bc.as<double>());
+  } else {
+    k_ns_bc_velocity<<<fb, kNsThreads, 0, st>>>(nv->faces, nv->bcex.as<double>(), nullptr, nullptr, nullptr,
+                                                fac1, nv->bc.as<double>());
+  }
+  if ((rc = launch_check("k_ns_bc_velocity"))) return rc;
+  // velocity Helmholtz solves (pt = 2: + gradient of extrapol(p))
+  if (P.pt == 2) {
+    if ((rc = extrapol_into(nv, extrapol_of(nv, P.top - 1, field_ptr, kVarP), nv->T(0), st)) ||
+        (rc = der(nv, 0, nv->T(0), nv->T(1), st)) || (rc = der(nv, 1, nv->T(0), nv->T(2), st)) ||
+        (rc = der(nv, 2, nv->T(0), nv->T(3), st)))
+      return rc;
+  }
+  const unsigned ib = ns_blocks(nv->nin);
+  for (int c = 0; c < 3; ++c) {
+    k_ns_fu<<<ib, kNsThreads, 0, st>>>(nv->nx, nv->ny, nv->nz, nv->F(c, s0), nv->F(c, s1),
+                                       P.tou == 3 ? nv->F(c, s2) : nullptr, nv->fac[1], nv->fac[2], nv->fac[3],
+                                       P.pt == 2 ? nv->T(1 + c) : nullptr, nv->RHS(c, nv->rhs_cur),
+                                       P.reynolds, nv->fin.as<double>());
+    if ((rc = launch_check("k_ns_fu")) || (rc = solve(nv, nv->scu, nv->sigmau, nv->F(c, nw), nv->BC(c), st)))
+      return rc;
+  }
+  // pressure increment: rhs_p = fac(1) u*, Poisson solve with Neumann data
+  for (int c = 0; c < 3; ++c) {
+    k_ns_scale<<<gb, kNsThreads, 0, st>>>(nv->nx, nv->ny, nv->nz, fac1, nv->F(c, nw), nv->RP(c));
+    if ((rc = launch_check("k_ns_scale"))) return rc;
+  }
+  if ((rc = der(nv, 0, nv->RP(0), nv->T(4), st)) || (rc = der(nv, 1, nv->RP(1), nv->T(5), st)) ||
+      (rc = der(nv, 2, nv->RP(2), nv->T(6), st)) || (rc = extrapol_into(nv, ephi, nv->T(0), st)))
+    return rc;
+  k_ns_fphi<<<ib, kNsThreads, 0, st>>>(nv->nx, nv->ny, nv->nz, nv->sigmap, nv->T(0), nv->T(4), nv->T(5),
+                                       nv->T(6), nv->fin.as<double>());
+  k_ns_bc_phi<<<fb, kNsThreads, 0, st>>>(nv->faces, nv->RP(0), nv->RP(1), nv->RP(2), nv->bc.as<double>(), fac1,
+                                         nv->BC(3));
+  if ((rc = launch_check("k_ns_fphi")) || (rc = solve(nv, nv->scp, nv->sigmap, nv->F(kVarPhi, nw), nv->BC(3), st)))
+    return rc;
+  // projection
+  k_ns_zero_edges<<<gb, kNsThreads, 0, st>>>(nv->nx, nv->ny, nv->nz, nv->F(kVarPhi, nw));
+  if ((rc = launch_check("k_ns_zero_edges"))) return rc;
+  if (P.pt == 2 && (rc = extrapol_into(nv, extrapol_of(nv, P.top - 1, field_ptr, kVarP), nv->T(0), st))) return rc;
+  if ((rc = der(nv, 0, nv->F(0, nw), nv->T(1), st)) || (rc = der(nv, 1, nv->F(1, nw), nv->T(2), st)) ||
+      (rc = der(nv, 2, nv->F(2, nw), nv->T(3), st)))
+    return rc;
+  k_ns_pressure<<<gb, kNsThreads, 0, st>>>(nv->nx, nv->ny, nv->nz, nv->F(kVarPhi, nw),
+                                           P.pt == 2 ? nv->T(0) : nullptr, nv->T(1), nv->T(2), nv->T(3), P.reynolds,
+                                           nv->F(kVarP, nw));
+  if ((rc = launch_check("k_ns_pressure")) || (rc = der(nv, 0, nv->F(kVarPhi, nw), nv->T(1), st)) ||
+      (rc = der(nv, 1, nv->F(kVarPhi, nw), nv->T(2), st)) || (rc = der(nv, 2, nv->F(kVarPhi, nw), nv->T(3), st)))
+    return rc;
+  for (int c = 0; c < 3; ++c) {
+    k_ns_velocity<<<gb, kNsThreads, 0, st>>>(nv->nx, nv->ny, nv->nz, nv->RP(c), nv->T(1 + c), fac1, nv->F(c, nw));
+    if ((rc = launch_check("k_ns_velocity"))) return rc;
+  }
+  nv->nl_ok[nw] = false;
+  return MF_OK;
+}
+
+// Driver diagnostics of level it(nt) (navier3d.f90:120-254); diag[12].
+int ns_diagnostics(mf_navier* nv, double* diag, cudaStream_t st) {
+  const int cur = nv->it[kNt - 1], prev = nv->it[kNt - 2];
+  const int groups = (nv->ny + kWRows - 1) / kWRows, count = nv->nz * groups;
+  int rc;
+  if ((rc = der(nv, 0, nv->F(0, cur), nv->T(1), st)) || (rc = der(nv, 1, nv->F(1, cur), nv->T(2), st)) ||
+      (rc = der(nv, 2, nv->F(2, cur), nv->T(3), st)))
+    return rc;
+  DiagIn D{};
+  D.u = nv->F(0, cur); D.v = nv->F(1, cur); D.w = nv->F(2, cur); D.p = nv->F(kVarP, cur);
+  D.up = nv->F(0, prev); D.vp = nv->F(1, prev); D.wp = nv->F(2, prev); D.pp = nv->F(kVarP, prev);
+  D.dx = nv->T(1); D.dy = nv->T(2); D.dz = nv->T(3);
+  D.ue = nv->EX(0); D.ve = nv->EX(1); D.pex = nv->EX(2);
+  double s0[kDiagSums], s1[kDiagSums], s2[kDiagSums];
+  auto run = [&](int phase, double* out) -> int {
+    if (phase == 0)
+      k_ns_diag<0><<<dim3(nv->nz, groups), kNsThreads, 0, st>>>(nv->weights(), D, nv->part.as<double>());
+    else if (phase == 1)
+      k_ns_diag<1><<<dim3(nv->nz, groups), kNsThreads, 0, st>>>(nv->weights(), D, nv->part.as<double>());
+    else
+      k_ns_diag<2><<<dim3(nv->nz, groups), kNsThreads, 0, st>>>(nv->weights(), D, nv->part.as<double>());
+    k_ns_sum_parts<<<1, kNsThreads, 0, st>>>(nv->part.as<double>(), count, kDiagSums, nv->sums.as<double>());
+    int r = launch_check("k_ns_diag");
+    if (r) return r;
+    MF_CUDA(cudaMemcpyAsync(out, nv->sums.ptr, sizeof(double) * kDiagSums, cudaMemcpyDeviceToHost, st));
+    MF_CUDA(cudaStreamSynchronize(st));
+    return MF_OK;
+  };
+  if ((rc = run(0, s0))) return rc;
+  const double reft = nv->reft, ts = nv->prm.ts;
+  const double ref1 = std::sqrt(reft);  // norme(1)
+  diag[0] = std::sqrt(s0[0]) / ref1;
+  const double refv = std::sqrt(s0[1]), errv = std::sqrt(s0[2]);
+  nv->err_vts += errv * errv * ts;
+  diag[1] = errv;
+  diag[2] = errv / refv;
+  diag[3] = std::sqrt(nv->err_vts);
+  // pressure: remove the weighted mean of p(it(nt)) (the driver stores it back)
+  k_ns_shift<<<ns_blocks(nv->np), kNsThreads, 0, st>>>(nv->np, -(s0[3] / reft), nv->F(kVarP, cur));
+  if ((rc = launch_check("k_ns_shift"))) return rc;
+  D.pexm = s0[10] / reft;
+  if ((rc = run(1, s1))) return rc;
+  const double errp = std::sqrt(s1[0]), refp = std::sqrt(s1[1]);
+  nv->err_pre += errp * errp * ts;
+  diag[4] = errp;
+  diag[5] = errp / refp;
+  diag[6] = std::sqrt(nv->err_pre);
+  const double nu = std::sqrt(s0[4]), nvv = std::sqrt(s0[5]), nww = std::sqrt(s0[6]);
+  diag[7] = 0.5 * (nu * nu + nvv * nvv + nww) / reft;
+  D.auxm = s1[2] / reft;
+  if ((rc = run(2, s2))) return rc;
+  const double sp = std::sqrt(s2[0]);
+  diag[8] = sp;
+  diag[9] = sp / reft;
+  const double du = std::sqrt(s0[7]), dv = std::sqrt(s0[8]), dw = std::sqrt(s0[9]);
+  const double sv = std::sqrt(du * du + dv * dv + dw);
+  diag[10] = sv;
+  diag[11] = sv / reft;
+  return MF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mf_navier_defaults(mf_navier_params_t* p) {
+  if (!p) return set_error(MF_ERR_ARG, "mf_navier_defaults: null argument");
+  p->ts = 1.0;
+  p->reynolds = 1.0;
+  p->nlt = 2;
+  p->pt = 1;
+  p->tou = 2;
+  p->top = 2;
+  p->so_solver = 6;
+  p->so_der = 6;
+  p->flow_rate = 1;
+  p->nmodes = 5;
+  p->precision = MF_PREC_FP64;
+  p->refine = -1;
+  return MF_OK;
+}
+
+int mf_navier_destroy(mf_navier_t* nv) {
+  if (!nv) return MF_OK;
+  mf_der_destroy(nv->dcx);
+  mf_der_destroy(nv->dcy);
+  mf_der_destroy(nv->dcz);
+  mf_solver3d_destroy(nv->scu);
+  mf_solver3d_destroy(nv->scp);
+  for (DevBuf* b : {&nv->fields, &nv->nl, &nv->rhs, &nv->rp, &nv->tmp, &nv->fin, &nv->exact, &nv->bcex,
+                    &nv->bc, &nv->grid, &nv->wts, &nv->part, &nv->sums, &nv->state})
+    b->release();
+  delete nv;
+  return MF_OK;
+}
+
+int mf_navier_create(const double* gx, int nx, const double* gy, int ny, const double* gz, int nz,
+                     const mf_navier_params_t* p, mf_navier_t** out) {
+  if (!gx || !gy || !gz || !p || !out) return set_error(MF_ERR_ARG, "mf_navier_create: null argument");
+  *out = nullptr;
+  if (nx < 9 || ny < 9 || nz < 9) return set_error(MF_ERR_ARG, "mf_navier_create: at least 9 nodes per axis");
+  if (!(p->ts > 0.0) || !(p->reynolds > 0.0) || p->nlt < 0 || p->nlt > 2 || (p->pt != 1 && p->pt != 2) ||
+      p->tou < 1 || p->tou > 3 || p->nmodes < 0)
+    return set_error(MF_ERR_ARG, "mf_navier_create: bad parameters (ts, reynolds > 0; nlt 0..2; pt 1, 2; tou 1..3)");
+  if (p->precision != MF_PREC_FP64 && p->precision != MF_PREC_SPLIT_BF16 && p->precision != MF_PREC_3XTF32)
+    return set_error(MF_ERR_ARG, "mf_navier_create: unknown precision %d", p->precision);
+  mf_navier* nv = new mf_navier();
+  nv->prm = *p;
+  nv->nx = nx; nv->ny = ny; nv->nz = nz;
+  nv->n1 = nx - 2; nv->n2 = ny - 2; nv->n3 = nz - 2;
+  nv->np = (long long)nx * ny * nz;
+  nv->nin = (long long)nv->n1 * nv->n2 * nv->n3;
+  const double ts = p->ts;
+  if (p->tou == 1) {
+    nv->fac[0] = 1.0 / ts; nv->fac[1] = -1.0 / ts; nv->fac[2] = 0.0; nv->fac[3] = 0.0;
+  } else if (p->tou == 2) {
+    nv->fac[0] = 1.5 / ts; nv->fac[1] = -2.0 / ts; nv->fac[2] = 0.5 / ts; nv->fac[3] = 0.0;
+  } else {
+    nv->fac[0] = 11.0 / (6.0 * ts); nv->fac[1] = -18.0 / (6.0 * ts);
+    nv->fac[2] = 9.0 / (6.0 * ts); nv->fac[3] = -2.0 / (6.0 * ts);
+  }
+  nv->sigmau = -p->reynolds * nv->fac[0];
+  nv->sigmap = 0.0;
+  nv->faces = Faces{nx, ny, nz, 2LL * nv->n2 * nv->n3, 2LL * nv->n1 * nv->n3, 2LL * nv->n1 * nv->n2};
+  const long long ftot = nv->faces.sx + nv->faces.sy + nv->faces.sz;
+  const int groups = (ny + kWRows - 1) / kWRows;
+  const size_t fb = (size_t)nv->np * sizeof(double);
+  const int bctu[6] = {1, 1, 1, 1, 1, 1}, bctp[6] = {2, 2, 2, 2, 2, 2};
+  int rc;
+  auto fail = [&](int r) {
+    mf_navier_destroy(nv);
+    return r;
+  };
+  if ((rc = mf_der_coeffs_init(gx, nx, 1, p->so_der, &nv->dcx)) ||
+      (rc = mf_der_coeffs_init(gy, ny, 1, p->so_der, &nv->dcy)) ||
+      (rc = mf_der_coeffs_init(gz, nz, 1, p->so_der, &nv->dcz)) ||
+      (rc = mf_solver_coeffs_init_3d(gx, gy, gz, nx, ny, nz, bctu, p->so_solver, &nv->scu)) ||
+      (rc = mf_solver_coeffs_init_3d(gx, gy, gz, nx, ny, nz, bctp, p->so_solver, &nv->scp)))
+    return fail(rc);
+  if ((rc = nv->fields.ensure(fb * 5 * kNt)) || (rc = nv->nl.ensure(fb * 3 * kNt)) ||
+      (rc = nv->rhs.ensure(fb * 6)) || (rc = nv->rp.ensure(fb * 3)) || (rc = nv->tmp.ensure(fb * 9)) ||
+      (rc = nv->fin.ensure((size_t)nv->nin * sizeof(double))) || (rc = nv->exact.ensure(fb * 5)) ||
+      (rc = nv->bcex.ensure(sizeof(double) * 3 * ftot)) || (rc = nv->bc.ensure(sizeof(double) * 4 * ftot)) ||
+      (rc = nv->grid.ensure(sizeof(double) * (nx + ny + nz))) ||
+      (rc = nv->wts.ensure(sizeof(double) * (nx + ny + nz))) ||
+      (rc = nv->part.ensure(sizeof(double) * kDiagSums * (size_t)nz * groups)) ||
+      (rc = nv->sums.ensure(sizeof(double) * kDiagSums)) || (rc = nv->state.ensure(sizeof(double) * 3)))
+    return fail(rc);
+  // host-side set-up: grids, half widths, integrale(1)
+  std::vector<double> g(nx + ny + nz), w(nx + ny + nz);
+  const double* src[3] = {gx, gy, gz};
+  const int n[3] = {nx, ny, nz};
+  for (int a = 0, off = 0; a < 3; off += n[a], ++a) {
+    for (int i = 0; i < n[a]; ++i) g[off + i] = src[a][i];
+    for (int i = 1; i < n[a] - 1; ++i) w[off + i] = (src[a][i + 1] - src[a][i - 1]) * 0.5;
+    w[off] = (src[a][1] - src[a][0]) * 0.5;
+    w[off + n[a] - 1] = (src[a][n[a] - 1] - src[a][n[a] - 2]) * 0.5;
+  }
+  double reft = 0.0;
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        const int b = (i == 0 || i == nx - 1) + (j == 0 || j == ny - 1) + (k == 0 || k == nz - 1);
+        if (b <= 1) reft += w[i] * w[nx + j] * w[nx + ny + k];
+      }
+  nv->reft = reft;
+  cudaStream_t st = nullptr;
+  if (cudaMemcpy(nv->grid.ptr, g.data(), g.size() * 8, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(nv->wts.ptr, w.data(), w.size() * 8, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemset(nv->fields.ptr, 0, fb * 5 * kNt) != cudaSuccess || cudaMemset(nv->rhs.ptr, 0, fb * 6) != cudaSuccess ||
+      cudaMemset(nv->state.ptr, 0, sizeof(double) * 3) != cudaSuccess)
+    return fail(set_error(MF_ERR_CUDA, "mf_navier_create: upload failed"));
+  const double* dg = nv->grid.as<double>();
+  k_ns_exact<<<ns_blocks(nv->np), kNsThreads, 0, st>>>(dg, dg + nx, dg + nx + ny, nx, ny, nz, p->nmodes,
+                                                       4.0 * std::atan(1.0), p->reynolds, nv->exact.as<double>());
+  k_ns_bc_exact<<<ns_blocks(ftot), kNsThreads, 0, st>>>(nv->faces, nv->exact.as<double>(), nv->np,
+                                                        nv->bcex.as<double>());
+  if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess)
+    return fail(set_error(MF_ERR_CUDA, "mf_navier_create: exact-solution kernels failed"));
+  *out = nv;
+  return MF_OK;
+}
+
+int mf_navier_field(mf_navier_t* nv, int var, int level, double** ptr) {
+  if (!nv || !ptr || var < 0 || var > 4 || level < 0 || level >= kNt)
+    return set_error(MF_ERR_ARG, "mf_navier_field: var 0..4, level 0..3");
+  *ptr = nv->F(var, nv->it[level]);
+  return MF_OK;
+}
+
+int mf_navier_set_field(mf_navier_t* nv, int var, int level, const double* f, void* stream) {
+  double* d = nullptr;
+  int rc = mf_navier_field(nv, var, level, &d);
+  if (rc) return rc;
+  if (!f) return set_error(MF_ERR_ARG, "mf_navier_set_field: null field");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  MF_CUDA(cudaMemcpyAsync(d, f, (size_t)nv->np * 8, cudaMemcpyDefault, st));
+  if (!is_device_ptr(f)) MF_CUDA(cudaStreamSynchronize(st));
+  if (var < 3) nv->nl_ok[nv->it[level]] = false;
+  return MF_OK;
+}
+
+int mf_navier_get_field(mf_navier_t* nv, int var, int level, double* f, void* stream) {
+  double* d = nullptr;
+  int rc = mf_navier_field(nv, var, level, &d);
+  if (rc) return rc;
+  if (!f) return set_error(MF_ERR_ARG, "mf_navier_get_field: null field");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  MF_CUDA(cudaMemcpyAsync(f, d, (size_t)nv->np * 8, cudaMemcpyDefault, st));
+  if (!is_device_ptr(f)) MF_CUDA(cudaStreamSynchronize(st));
+  return MF_OK;
+}
+
+int mf_navier_step(mf_navier_t* nv, double* diag, void* stream) {
+  if (!nv) return set_error(MF_ERR_ARG, "mf_navier_step: null handle");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  int rc = ns_step(nv, st);
+  if (rc) return rc;
+  if (diag && (rc = ns_diagnostics(nv, diag, st))) return rc;
+  // slot rotation (navier3d.f90:256-261)
+  const int first = nv->it[0];
+  for (int i = 0; i < kNt - 1; ++i) nv->it[i] = nv->it[i + 1];
+  nv->it[kNt - 1] = first;
+  return MF_OK;
+}
+
+int mf_navier_state(mf_navier_t* nv, double* time, double* debit, double* g) {
+  if (!nv) return set_error(MF_ERR_ARG, "mf_navier_state: null handle");
+  double s[3];
+  MF_CUDA(cudaMemcpy(s, nv->state.ptr, sizeof(s), cudaMemcpyDeviceToHost));
+  if (time) *time = nv->time;
+  if (debit) *debit = s[1];
+  if (g) *g = s[0];
+  return MF_OK;
+}
+
+}  // extern "C"

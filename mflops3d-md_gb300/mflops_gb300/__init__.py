@@ -159,6 +159,14 @@ _PROTOS = {
     "mf_solver3d_profile": [_P, _I],
     "mf_solver3d_set_residual": [_P, _I],
     "mf_solver3d_profile_read": [_P, _I, _DP, ctypes.POINTER(ctypes.c_longlong)],
+    "mf_navier_defaults": [_P],
+    "mf_navier_create": [_DP, _I, _DP, _I, _DP, _I, _P, ctypes.POINTER(_P)],
+    "mf_navier_destroy": [_P],
+    "mf_navier_field": [_P, _I, _I, ctypes.POINTER(_P)],
+    "mf_navier_set_field": [_P, _I, _I, _P, _P],
+    "mf_navier_get_field": [_P, _I, _I, _P, _P],
+    "mf_navier_step": [_P, _DP, _P],
+    "mf_navier_state": [_P, _DP, _DP, _DP],
 }
 
 for _name, _args in _PROTOS.items():
@@ -907,6 +915,82 @@ def channel_stats(us, vs, ws, ps, gx, gy, gz, re, so=6, stream=None):
     out.update({"rms" + k: rms[q * ny:(q + 1) * ny] for q, k in enumerate(["u", "v", "w", "p", "uv", "uw", "vw"])})
     out["utau"] = utau.value
     return out
+
+
+# ---------------------------------------------------------------------------
+# Navier-Stokes time step on one domain (navier3d.f90 / class_navier_3D.f90)
+# ---------------------------------------------------------------------------
+
+class NavierParams(ctypes.Structure):
+    """mf_navier_params_t; defaults are the reference's (command_line.f90)."""
+    _fields_ = [("ts", ctypes.c_double), ("reynolds", ctypes.c_double), ("nlt", ctypes.c_int),
+                ("pt", ctypes.c_int), ("tou", ctypes.c_int), ("top", ctypes.c_int),
+                ("so_solver", ctypes.c_int), ("so_der", ctypes.c_int), ("flow_rate", ctypes.c_int),
+                ("nmodes", ctypes.c_int), ("precision", ctypes.c_int), ("refine", ctypes.c_int)]
+
+
+NAVIER_VARS = {"u": 0, "v": 1, "w": 2, "p": 3, "phi": 4}
+NAVIER_DIAG = ("div", "vel_err", "vel_rel", "vel_acc", "pres_err", "pres_rel", "pres_acc", "kinetic",
+               "station_p", "station_p_rel", "station_v", "station_v_rel")
+
+
+class NavierStokes3D:
+    """One-domain time integration of navier3d (mpid%dims = 0, mapt = 0,
+    nsubite = 1, les_type = 0, pt 1 or 2) on host grids.  Keyword arguments
+    override the reference's defaults (ts, reynolds, nlt, pt, tou, top,
+    so_solver, so_der, flow_rate, nmodes, precision, refine)."""
+
+    def __init__(self, gx, gy, gz, **kw):
+        prm = NavierParams()
+        _check(_lib.mf_navier_defaults(ctypes.byref(prm)))
+        for k, v in kw.items():
+            if not hasattr(prm, k):
+                raise TypeError("unknown parameter %s" % k)
+            setattr(prm, k, v)
+        self.params = prm
+        gx, xp = _dptr(gx)
+        gy, yp = _dptr(gy)
+        gz, zp = _dptr(gz)
+        self.shape = (gx.size, gy.size, gz.size)
+        self._h = ctypes.c_void_p()
+        _check(_lib.mf_navier_create(xp, gx.size, yp, gy.size, zp, gz.size, ctypes.byref(prm),
+                                     ctypes.byref(self._h)))
+
+    def set_field(self, var, level, f, stream=None):
+        """level 0 = it(1) (written by the next step) ... 3 = it(nt) (newest)."""
+        _check(_lib.mf_navier_set_field(self._h, NAVIER_VARS[var], int(level), _arg(f), _stream(stream)))
+
+    def field(self, var, level=3, stream=None):
+        """Device copy of a field (torch tensor, x fastest)."""
+        out = empty_device(self.shape)
+        _check(_lib.mf_navier_get_field(self._h, NAVIER_VARS[var], int(level), _arg(out), _stream(stream)))
+        return out
+
+    def step(self, diagnostics=False, stream=None):
+        """One time step; with diagnostics the driver's printed numbers of
+        level it(nt) (before the rotation) as a dict."""
+        if diagnostics:
+            d = np.zeros(len(NAVIER_DIAG))
+            _check(_lib.mf_navier_step(self._h, d.ctypes.data_as(_DP), _stream(stream)))
+            return dict(zip(NAVIER_DIAG, d))
+        _check(_lib.mf_navier_step(self._h, None, _stream(stream)))
+        return None
+
+    def state(self):
+        t, debit, g = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        _check(_lib.mf_navier_state(self._h, ctypes.byref(t), ctypes.byref(debit), ctypes.byref(g)))
+        return {"time": t.value, "debit": debit.value, "g": g.value}
+
+    def close(self):
+        if self._h:
+            _lib.mf_navier_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def tune(mode=None, save=None, load=None, clear=False):

@@ -1,0 +1,331 @@
+"""Oracle of the single-domain Navier-Stokes time step (test infrastructure only).
+
+Restates, in FP64 NumPy, one subdomain (``mpid%dims == 0``), no mapping
+(``mapt = 0``: ``derxm`` = ``derx``, the ``_nc`` terms are zero,
+src/class_mapping/class_mapping.f90:61-129) and one sub-iteration
+(``nsubite = 1``), the time loop of src/main/navier3d.f90:48-274 built from
+src/class_navier/class_navier_3D.f90:
+
+* state ``type(navier3d)`` (:13-44): nt = 4 time levels u, v, w, p, phi in
+  slots addressed through the permutation ``it``; BDF factors ``fac`` for
+  tou = 1, 2, 3 and sigmau = -Re fac(1), sigmap = 0 (:2133-2155); velocity
+  Dirichlet on all faces, pressure Neumann on all faces (:2157-2160);
+  derivatives with solver-type coefficients, so = (6, 6) (:2273-2278);
+* ``navier_time`` (:2052-2064), ``navier_bc_velocity`` with boundary values
+  from the exact solution ``sol`` (:395-433, 848-925, 927-1041),
+  ``navier_presolve_{u,v,w}`` (:1528-1595) with ``navier_nonlinear``
+  (:1169-1222, nlt = 0, 1, 2) and the forcing ``f`` (:1043-1167, the
+  exact-solution source plus the flow-rate term for u, les_type = 0),
+  ``add_boundary_gradient`` for pt = 1 (:695-791), ``navier_solve_{u,v,w}``
+  (:1597-1761, pt = 1, 2), ``navier_presolve_phi`` / ``navier_phi_rhs``
+  (:1764-1785, 1961-2007), ``navier_solve_phi`` with
+  ``navier_bc_pressure`` (:1787-1845, 342-393), ``navier_projection``
+  (:1847-1959), ``navier_extrapol`` (:2010-2050) and the slot rotation
+  (navier3d.f90:256-261);
+* the driver's per-step diagnostics (navier3d.f90:120-254) with
+  ``integrale`` / ``norme2`` (class_navier_3D.f90:2419-2603); they report the
+  level it(nt) and remove the weighted mean of its pressure, as the driver
+  does.
+
+``navier_LES`` with les_type = 0 computes the velocity gradients and a zero
+viscosity that nothing reads; it is left out.  The 1e-10 of the flow-rate
+term is a default-kind (single precision) literal.
+"""
+import numpy as np
+
+from oracle import derivatives as D
+from oracle import solver as S
+from oracle.les import zero_edges
+
+NT = 4
+THRESH = float(np.float32(1e-10))
+NMODES = 5
+
+
+def sol(x, y, z, t, kind, rey, nmodes=NMODES):
+    """Exact solution and source terms (class_navier_3D.f90:927-1041): a sum
+    of 5 steady modes (wt = 0).  The sources carry each mode's own advection
+    only, so the sum is an exact solution for one mode (nmodes = 1), not for
+    the reference's five."""
+    x, y, z = np.broadcast_arrays(np.asarray(x, float), np.asarray(y, float), np.asarray(z, float))
+    out = np.zeros(x.shape)
+    pi = 4.0 * np.arctan(1.0)
+    for i in range(1, nmodes + 1):
+        a = b = 1.0
+        wx = wy = wp = pi * i
+        wt = 0.0 * i * pi
+        ct, st = np.cos(wt * t), np.sin(wt * t)
+        if kind == "u":
+            out = out + a * np.sin(wx * x) * np.cos(wy * y) * ct / wx
+        elif kind == "v":
+            out = out - a * np.cos(wx * x) * np.sin(wy * y) * ct / wy
+        elif kind == "p":
+            out = out + b * np.sin(wp * (x - y)) * ct
+        elif kind == "rhsu":
+            out = out + (b * wp * ct * np.cos(wp * (y - x))
+                         + a ** 2 * ct ** 2 * np.cos(wx * x) * np.sin(wx * x)
+                         * (np.sin(wy * y) ** 2 + np.cos(wy * y) ** 2) / wx
+                         + a * ct * np.sin(wx * x) * np.cos(wy * y) * (wy ** 2 / wx + wx) / rey
+                         - a * wt * st * np.sin(wx * x) * np.cos(wy * y) / wx)
+        elif kind == "rhsv":
+            out = out + (-b * wp * ct * np.cos(wp * (y - x))
+                         + a ** 2 * ct ** 2 * np.cos(wy * y) * np.sin(wy * y)
+                         * (np.sin(wx * x) ** 2 + np.cos(wx * x) ** 2) / wy
+                         - a * ct * np.cos(wx * x) * np.sin(wy * y) * (wy + wx ** 2 / wy) / rey
+                         + a * wt * st * np.cos(wx * x) * np.sin(wy * y) / wy)
+    return out
+
+
+def bdf_factors(tou, ts):
+    """fac(1:4) of navier_initialization (class_navier_3D.f90:2133-2152)."""
+    if tou == 1:
+        return np.array([1.0 / ts, -1.0 / ts, 0.0, 0.0])
+    if tou == 2:
+        return np.array([1.5 / ts, -2.0 / ts, 0.5 / ts, 0.0])
+    if tou == 3:
+        return np.array([11.0 / (6.0 * ts), -18.0 / (6.0 * ts), 9.0 / (6.0 * ts), -2.0 / (6.0 * ts)])
+    raise ValueError("tou must be 1, 2 or 3")
+
+
+def half_widths(g):
+    """Integration widths of integrale/norme2: (g(i+1)-g(i-1))/2 inside,
+    (g(2)-g(1))/2 and (g(n)-g(n-1))/2 at the ends."""
+    g = np.asarray(g, float)
+    w = np.empty_like(g)
+    w[1:-1] = (g[2:] - g[:-2]) * 0.5
+    w[0] = (g[1] - g[0]) * 0.5
+    w[-1] = (g[-1] - g[-2]) * 0.5
+    return w
+
+
+def quad_weights(gx, gy, gz):
+    """Weights of integrale / norme2 (class_navier_3D.f90:2419-2603): interior
+    points and face points, edges and corners excluded."""
+    wx, wy, wz = half_widths(gx), half_widths(gy), half_widths(gz)
+    W = wx[:, None, None] * wy[None, :, None] * wz[None, None, :]
+    bx = np.zeros(len(gx), int); bx[[0, -1]] = 1
+    by = np.zeros(len(gy), int); by[[0, -1]] = 1
+    bz = np.zeros(len(gz), int); bz[[0, -1]] = 1
+    nb = bx[:, None, None] + by[None, :, None] + bz[None, None, :]
+    return np.where(nb <= 1, W, 0.0)
+
+
+class Navier:
+    """Single-domain state and time step; fields are (nx, ny, nz) arrays."""
+
+    def __init__(self, gx, gy, gz, ts, rey, nlt=2, pt=1, tou=2, top=2, so=(6, 6), flow_rate=True,
+                 nmodes=NMODES):
+        if pt not in (1, 2):
+            raise ValueError("pressure types 1 and 2 are restated")
+        self.gx, self.gy, self.gz = (np.asarray(g, float) for g in (gx, gy, gz))
+        self.nx, self.ny, self.nz = len(gx), len(gy), len(gz)
+        self.ts, self.rey = float(ts), float(rey)
+        self.nlt, self.pt, self.tou, self.top = nlt, pt, tou, top
+        self.flow_rate = flow_rate
+        self.nmodes = nmodes
+        self.fac = bdf_factors(tou, ts)
+        self.sigmau = -self.rey * self.fac[0]
+        self.sigmap = 0.0
+        self.scu = S.Solver3D(self.gx, self.gy, self.gz, (1,) * 6, so[0])
+        self.scp = S.Solver3D(self.gx, self.gy, self.gz, (2,) * 6, so[0])
+        self.dcx = D.DerCoeffs(self.gx, so[1], solver=True)
+        self.dcy = D.DerCoeffs(self.gy, so[1], solver=True)
+        self.dcz = D.DerCoeffs(self.gz, so[1], solver=True)
+        shape = (self.nx, self.ny, self.nz)
+        z = lambda: np.zeros(shape)
+        self.u, self.v, self.w = [z() for _ in range(NT)], [z() for _ in range(NT)], [z() for _ in range(NT)]
+        self.p, self.phi = [z() for _ in range(NT)], [z() for _ in range(NT)]
+        self.rhs = {c: [z(), z()] for c in "uvw"}
+        self.it = list(range(NT))
+        self.time = 0.0
+        self.g = None          # flow-rate term (the saved field g of f), uniform
+        self.debit = None
+        self.W = quad_weights(self.gx, self.gy, self.gz)
+        self.err_vts_t = 0.0
+        self.err_pre_t = 0.0
+
+    # -- helpers ------------------------------------------------------------
+    def derx(self, f):
+        return D.derx(self.dcx, f)
+
+    def dery(self, f):
+        return D.dery(self.dcy, f)
+
+    def derz(self, f):
+        return D.derz(self.dcz, f)
+
+    def integrale(self, f):
+        return float(np.sum(self.W * f))
+
+    def norme(self, f):
+        return float(np.sqrt(np.sum(self.W * f * f)))
+
+    def points(self):
+        return np.meshgrid(self.gx, self.gy, self.gz, indexing="ij")
+
+    def extrapol(self, var, kind):
+        """navier_extrapol with subite = 1 (class_navier_3D.f90:2010-2050)."""
+        order = self.tou if kind == "v" else self.top - 1
+        it = self.it
+        if order == -1:
+            out = 1.0 * var[it[0]]
+        elif order == 1:
+            out = 1.0 * var[it[NT - 1]]
+        elif order == 2:
+            out = 2.0 * var[it[NT - 1]] - 1.0 * var[it[NT - 2]]
+        elif order == 3:
+            out = 3.0 * var[it[NT - 1]] - 3.0 * var[it[NT - 2]] + 1.0 * var[it[NT - 3]]
+        else:
+            out = np.zeros((self.nx, self.ny, self.nz))
+        return zero_edges(out)
+
+    def nonlinear(self, x):
+        """navier_nonlinear: the advection term of every slot, extrapolated."""
+        tmp = []
+        for i in range(NT):
+            if self.nlt == 1:
+                t = self.u[i] * self.derx(x[i]) + self.v[i] * self.dery(x[i]) + self.w[i] * self.derz(x[i])
+            elif self.nlt == 2:
+                t = (self.u[i] * self.derx(x[i]) + self.v[i] * self.dery(x[i])
+                     + self.w[i] * self.derz(x[i])) * 0.5
+                t = t + self.derx(x[i] * self.u[i]) * 0.5
+                t = t + self.dery(x[i] * self.v[i]) * 0.5
+                t = t + self.derz(x[i] * self.w[i]) * 0.5
+            else:
+                t = np.zeros((self.nx, self.ny, self.nz))
+            tmp.append(t)
+        return self.extrapol(tmp, "v")
+
+    def forcing(self, c):
+        """f(nav,mpid,'rhs'//c) with les_type = 0."""
+        X, Y, Z = self.points()
+        F = sol(X, Y, Z, self.time, "rhs" + c, self.rey, self.nmodes)
+        if c == "u" and self.flow_rate:
+            reft = self.integrale(np.ones_like(F))
+            err = self.integrale(self.extrapol(self.u, "v")) / reft
+            if self.g is None:
+                self.debit = err
+                if self.debit <= THRESH:
+                    self.debit = 1.0
+                self.g = 3.0 * self.debit
+            err = err - self.debit
+            self.g = self.g - err * self.fac[0]
+            F = F + self.g
+        return F
+
+    def bc_exact(self, c):
+        """navier_bc_velocity_utils: face values of sol (interior tangential points)."""
+        gx, gy, gz, t = self.gx, self.gy, self.gz, self.time
+        m = self.nmodes
+        bcx = np.stack([sol(g, gy[1:-1, None], gz[None, 1:-1], t, c, self.rey, m) for g in (gx[0], gx[-1])], -1)
+        bcy = np.stack([sol(gx[1:-1, None], g, gz[None, 1:-1], t, c, self.rey, m) for g in (gy[0], gy[-1])], -1)
+        bcz = np.stack([sol(gx[1:-1, None], gy[None, 1:-1], g, t, c, self.rey, m) for g in (gz[0], gz[-1])], -1)
+        return [bcx, bcy, bcz]
+
+    # -- the time step -----------------------------------------------------
+    def step(self):
+        it, fac = self.it, self.fac
+        new, n0, n1, n2 = it[0], it[NT - 1], it[NT - 2], it[NT - 3]
+        self.time += self.ts
+        bc = {c: self.bc_exact(c) for c in "uvw"}
+        levels = {"u": self.u, "v": self.v, "w": self.w}
+        # presolve u, v, w
+        for c in "uvw":
+            self.rhs[c][1] = self.rhs[c][0]
+            nl = self.nonlinear(levels[c])
+            self.rhs[c][0] = zero_edges(self.forcing(c) - nl)
+        # boundary gradient (pt = 1)
+        if self.pt == 1:
+            e = self.extrapol(self.phi, "p")
+            dx, dy, dz = self.derx(e), self.dery(e), self.derz(e)
+            for m, (i, j, k) in enumerate(((0, 0, 0), (-1, -1, -1))):
+                bc["v"][0][:, :, m] += dy[i, 1:-1, 1:-1] / fac[0]
+                bc["w"][0][:, :, m] += dz[i, 1:-1, 1:-1] / fac[0]
+                bc["u"][1][:, :, m] += dx[1:-1, j, 1:-1] / fac[0]
+                bc["w"][1][:, :, m] += dz[1:-1, j, 1:-1] / fac[0]
+                bc["u"][2][:, :, m] += dx[1:-1, 1:-1, k] / fac[0]
+                bc["v"][2][:, :, m] += dy[1:-1, 1:-1, k] / fac[0]
+        # solve u, v, w
+        grads = (self.derx, self.dery, self.derz)
+        for q, c in enumerate("uvw"):
+            lev = levels[c]
+            fu = np.zeros((self.nx, self.ny, self.nz))
+            fu = fu + fac[1] * lev[n0] + fac[2] * lev[n1]
+            if self.tou == 3:
+                fu = fu + fac[3] * lev[n2]
+            if self.pt == 2:
+                fu = fu + grads[q](self.extrapol(self.p, "p"))
+            fu = fu - self.rhs[c][0]
+            fu = self.rey * fu
+            lev[new] = S.solver_3d(self.scu, fu, lev[new], *bc[c], self.sigmau)
+        # presolve phi (pt <= 2)
+        rp = [zero_edges(fac[0] * levels[c][new]) for c in "uvw"]
+        # solve phi
+        fphi = self.sigmap * self.extrapol(self.phi, "p")
+        fphi = fphi + self.derx(rp[0]) + self.dery(rp[1]) + self.derz(rp[2])
+        nx, ny, nz = self.nx, self.ny, self.nz
+        bcphi = [np.stack([rp[0][m * (nx - 1), 1:-1, 1:-1] - fac[0] * bc["u"][0][:, :, m] for m in (0, 1)], -1),
+                 np.stack([rp[1][1:-1, m * (ny - 1), 1:-1] - fac[0] * bc["v"][1][:, :, m] for m in (0, 1)], -1),
+                 np.stack([rp[2][1:-1, 1:-1, m * (nz - 1)] - fac[0] * bc["w"][2][:, :, m] for m in (0, 1)], -1)]
+        self.phi[new] = S.solver_3d(self.scp, fphi, self.phi[new], *bcphi, self.sigmap)
+        # projection
+        self.phi[new] = zero_edges(self.phi[new])
+        if self.pt == 2:
+            aux = self.extrapol(self.p, "p")
+        self.p[new] = self.phi[new].copy()
+        if self.pt == 2:
+            self.p[new] = self.p[new] + aux
+        self.p[new] = zero_edges(self.p[new])
+        div = (self.derx(self.u[new]) + self.dery(self.v[new]) + self.derz(self.w[new])) / self.rey
+        self.p[new] = zero_edges(self.p[new] - div)
+        for q, c in enumerate("uvw"):
+            levels[c][new] = zero_edges((rp[q] - grads[q](self.phi[new])) / fac[0])
+
+    def diagnostics(self):
+        """navier3d.f90:120-254 on level it(nt) (before the rotation), which
+        removes the weighted mean of that level's pressure.  Returns the
+        printed numbers."""
+        it = self.it
+        cur, prev = it[NT - 1], it[NT - 2]
+        ones = np.ones((self.nx, self.ny, self.nz))
+        out = {}
+        ref = self.norme(ones)
+        div = self.derx(self.u[cur]) + self.dery(self.v[cur]) + self.derz(self.w[cur])
+        out["div"] = self.norme(div) / ref
+        X, Y, Z = self.points()
+        ue = [sol(X, Y, Z, self.time, c, self.rey, self.nmodes) for c in "uv"] + [np.zeros_like(X)]
+        pex = sol(X, Y, Z, self.time, "p", self.rey, self.nmodes)
+        ref = self.norme(np.sqrt(ue[0] ** 2 + ue[1] ** 2 + ue[2] ** 2))
+        err = self.norme(np.sqrt((ue[0] - self.u[cur]) ** 2 + (ue[1] - self.v[cur]) ** 2
+                                 + (ue[2] - self.w[cur]) ** 2))
+        self.err_vts_t += err ** 2 * self.ts
+        out["vel"] = (err, err / ref, np.sqrt(self.err_vts_t))
+        ref = self.integrale(ones)
+        mean = self.integrale(self.p[cur])
+        self.p[cur] = self.p[cur] - mean / ref
+        pex = pex - self.integrale(pex) / ref
+        refp = self.norme(pex)
+        err = self.norme(self.p[cur] - pex)
+        self.err_pre_t += err ** 2 * self.ts
+        out["pres"] = (err, err / refp, np.sqrt(self.err_pre_t))
+        reft = self.integrale(ones)
+        ek = 0.5 * (self.norme(self.u[cur]) ** 2 + self.norme(self.v[cur]) ** 2 + self.norme(self.w[cur]))
+        out["kinetic"] = ek / reft
+        aux = self.p[cur] - self.p[prev]
+        aux = aux - self.integrale(aux) / reft
+        e = self.norme(aux)
+        out["station_p"] = (e, e / reft)
+        e2 = (self.norme(self.u[cur] - self.u[prev]) ** 2 + self.norme(self.v[cur] - self.v[prev]) ** 2
+              + self.norme(self.w[cur] - self.w[prev]))
+        out["station_v"] = (np.sqrt(e2), np.sqrt(e2) / reft)
+        return out
+
+    def rotate(self):
+        """Slot rotation at the end of a time step (navier3d.f90:256-261)."""
+        self.it = self.it[1:] + self.it[:1]
+
+    def advance(self, diagnostics=False):
+        self.step()
+        d = self.diagnostics() if diagnostics else None
+        self.rotate()
+        return d
