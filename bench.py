@@ -51,11 +51,12 @@ def parse():
     ap.add_argument("--precision", default="auto", choices=["auto", "bf16", "tf32"],
                     help="transform format; auto times both and reports the faster")
     ap.add_argument("--probe", default=None,
-                    choices=["bf16", "tf32", "fp64", "der", "filter", "les_mlp", "mlp_train"],
+                    choices=["bf16", "tf32", "fp64", "der", "filter", "les_mlp", "mlp_train", "navier"],
                     help="profiling aid: run two untimed solves of the workload in this format "
                          "(refinement steps from --refine), or two untimed launches of one row "
                          "(derivative sweeps at 257^3, the 384 -> 96 filter, the learned viscosity "
-                         "at 160^3, a training step on 65,536 points), and exit")
+                         "at 160^3, a training step on 65,536 points, six Navier-Stokes steps at "
+                         "128x129x128), and exit")
     ap.add_argument("--refine", type=int, default=1)
     return ap.parse_args()
 
@@ -84,6 +85,26 @@ def workload(nodes):
     rhs = np.asfortranarray(rhs / np.std(rhs))
     bcx = np.zeros((n, n, 2), order="F")
     return (gx, gy, gz), rhs, (bcx, bcx.copy(), bcx.copy())
+
+
+def cpu_oracle_navier_step():
+    """One time step of the oracle's Navier-Stokes restatement at 128 x 129 x 128
+    (same options as the GPU row), timed on the host cores: the CPU figure
+    beside the GPU step."""
+    from oracle import mesh
+    from oracle import navier as NS
+    gx, gy, gz = mesh.uniform_grid(128), mesh.tanh_grid(129, 2.0), mesh.uniform_grid(128)
+    nav = NS.Navier(gx, gy, gz, ts=1e-3, rey=180.0)
+    rng = np.random.default_rng(0)
+    for s in range(NS.NT):
+        for f in (nav.u, nav.v, nav.w):
+            f[s] = rng.random((128, 129, 128))
+    t0 = time.perf_counter()
+    nav.advance()
+    dt = time.perf_counter() - t0
+    return {"oracle_cpu_s_per_step": dt, "oracle_cpu_cores": os.cpu_count(),
+            "oracle_sample": "one step of the oracle restatement (NumPy/OpenBLAS; it recomputes the "
+                             "nonlinear terms of all four time slots, as the reference does)"}
 
 
 def cpu_oracle_solve(grids, rhs, bcs):
@@ -416,6 +437,8 @@ def run_gb300(args, rank, world, dist):
                            np.linalg.norm(out[1:-1, 1:-1, 1:-1]))
         plain_vs_oracle = float(np.linalg.norm(mf.to_host(d_ref)[1:-1, 1:-1, 1:-1] - out[1:-1, 1:-1, 1:-1]) /
                                 np.linalg.norm(out[1:-1, 1:-1, 1:-1]))
+        if rows is not None and "navier_step_128x129x128" in rows:
+            rows["navier_step_128x129x128"].update(cpu_oracle_navier_step())
     else:
         plain_vs_oracle = None
 
@@ -663,6 +686,30 @@ def row_measurements(mf, torch, hbm):
         row[key + "graph_ms"] = time_fn(g.replay, reps=5)
         del g
     out["step_les_3helmholtz_1poisson_128x129x128"] = row
+    del rhs, outs, vel, nu
+    # the Navier-Stokes time step of navier3d at 128 x 129 x 128 with the
+    # reference's scheme defaults (pt 1, BDF2, skew-symmetric advection,
+    # flow-rate term), Re = 180, ts = 1e-3, random velocity levels; FP64 solves
+    # and 3xTF32 + 1 refinement, eager steps and a CUDA graph of four steps
+    # (one rotation of the time slots)
+    row = {}
+    for key, prec in (("fp64", mf.MF_PREC_FP64), ("3xtf32", mf.MF_PREC_3XTF32)):
+        nav = mf.NavierStokes3D(gx, gy, gz, ts=1e-3, reynolds=180.0, precision=prec, refine=1)
+        for lev in range(4):
+            for q, var in enumerate("uvw"):
+                nav.set_field(var, lev, field(shape, 90 + 4 * q + lev))
+        for _ in range(4):
+            nav.step()
+        row[key + "_eager_ms"] = time_fn(nav.step, reps=8)
+
+        def four():
+            for _ in range(4):
+                nav.step()
+        g = graph_of(four)
+        row[key + "_graph_ms"] = time_fn(g.replay, reps=3) / 4
+        del g
+        nav.close()
+    out["navier_step_128x129x128"] = row
     return out
 
 
@@ -692,6 +739,15 @@ def run_row_probe(args):
         fo = mf.empty_device((96, 385, 384))
         for _ in range(2):
             flt.apply(f, 0, out=fo)
+    elif args.probe == "navier":
+        shape = (128, 129, 128)
+        nav = mf.NavierStokes3D(mesh.uniform_grid(128), mesh.tanh_grid(129, 2.0), mesh.uniform_grid(128),
+                                ts=1e-3, reynolds=180.0, precision=mf.MF_PREC_3XTF32, refine=1)
+        for lev in range(4):
+            for q, var in enumerate("uvw"):
+                nav.set_field(var, lev, field(shape, 90 + 4 * q + lev))
+        for _ in range(6):  # four steps warm the nonlinear-term cache, two are profiled
+            nav.step()
     elif args.probe == "les_mlp":
         shape = (160, 160, 160)
         g = mesh.uniform_grid(160)

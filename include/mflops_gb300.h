@@ -121,6 +121,14 @@ int mf_dderx(const mf_der_t* dc, const double* f, double* df, int nx, int ny, in
 int mf_ddery(const mf_der_t* dc, const double* f, double* df, int nx, int ny, int nz, void* stream);
 int mf_dderz(const mf_der_t* dc, const double* f, double* df, int nx, int ny, int nz, void* stream);
 
+/* `count` (1..9) sweeps of mf_der_apply in one launch: job q differentiates
+ * f[q] along axis[q] (order[q] 1 or 2) with dc[q] into df[q]; all fields are
+ * (nx,ny,nz) device arrays and df[q] must not alias any f.  The results equal
+ * those of separate mf_der_apply calls.  No reference counterpart: it puts
+ * the lines of independent sweeps of a small field into one grid. */
+int mf_der_apply_many(int count, const mf_der_t* const* dc, const int* axis, const int* order,
+                      const double* const* f, double* const* df, int nx, int ny, int nz, void* stream);
+
 /* Single-pencil forms der/dder/der_s/dder_s (class_derivatives.f90:186-260)
  * on `count` contiguous pencils of length n (x[p*n + i]). */
 int mf_der_lines(const mf_der_t* dc, int order, int solver_variant, const double* x, double* dx,

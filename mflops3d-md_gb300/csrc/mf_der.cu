@@ -306,9 +306,91 @@ int der_launch(const mf_der_t* dc, int axis, int order, int mode, const double* 
   return MF_OK;
 }
 
+// Several sweeps in one launch: up to kMaxDerJobs (field, axis) jobs of one
+// field shape, one thread per line, every job's lines starting on a warp
+// boundary so that no warp mixes jobs.  Small fields give a single sweep too
+// few lines to fill the GPU (128 x 129 x 128: 16,512 lines, 3.4 warps per
+// SM); the jobs of independent sweeps together do.
+constexpr int kMaxDerJobs = 9;
+struct DerJob {
+  LineSet plain, sub;
+  TriSets tri;
+  const double* f;
+  double* df;
+  int na, nb, mode;
+  long long sa, sb, s;
+};
+struct DerJobs {
+  DerJob j[kMaxDerJobs];
+  long long start[kMaxDerJobs + 1];
+  int count;
+};
+
+__global__ void __launch_bounds__(128) der_lines_multi(DerJobs J) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= J.start[J.count]) return;
+  int q = 0;
+  while (q + 1 < J.count && t >= J.start[q + 1]) ++q;
+  const DerJob& d = J.j[q];
+  const long long u = t - J.start[q];
+  if (u >= (long long)d.na * d.nb) return;
+  const int a = (int)(u % d.na), b = (int)(u / d.na);
+  const long long base = a * d.sa + b * d.sb;
+  process_line(line_kind(d.mode, a, d.na, b, d.nb), d.plain, d.sub, d.tri, d.f + base, d.df + base, d.s);
+}
+
 }  // namespace mf
 
 extern "C" {
+
+int mf_der_apply_many(int count, const mf_der_t* const* dc, const int* axis, const int* order,
+                      const double* const* f, double* const* df, int nx, int ny, int nz, void* stream) {
+  if (count < 1 || count > kMaxDerJobs || !dc || !axis || !order || !f || !df)
+    return set_error(MF_ERR_ARG, "mf_der_apply_many: 1..%d jobs with non-null arrays", kMaxDerJobs);
+  if (nx < 2 || ny < 2 || nz < 2) return set_error(MF_ERR_ARG, "mf_der_apply_many: field too small");
+  DerJobs J{};
+  J.count = count;
+  J.start[0] = 0;
+  for (int q = 0; q < count; ++q) {
+    const mf_der_t* d = dc[q];
+    const int ax = axis[q], ord = order[q];
+    if (!d || !f[q] || !df[q] || ax < 0 || ax > 2 || (ord != 1 && ord != 2))
+      return set_error(MF_ERR_ARG, "mf_der_apply_many: bad job %d", q);
+    const int nline = ax == 0 ? nx : ax == 1 ? ny : nz;
+    if (nline != d->n)
+      return set_error(MF_ERR_ARG, "mf_der_apply_many: job %d pencil length %d differs from n=%d", q, nline, d->n);
+    if (!is_device_ptr(f[q]) || !is_device_ptr(df[q]))
+      return set_error(MF_ERR_ARG, "mf_der_apply_many: device fields required");
+    const int set = ord - 1;
+    DerJob& j = J.j[q];
+    j.plain = LineSet{d->dev + d->off[set], d->n};
+    j.sub = LineSet{d->solver ? d->dev + d->off[set + 2] : d->dev + d->off[set], d->n - 2};
+    j.tri = TriSets{nullptr, nullptr};
+    if (d->tri_ok) {
+      const DerTriRow* t = d->tri.as<DerTriRow>();
+      j.tri.plain = t + d->tri_off[set];
+      j.tri.sub = d->solver ? t + d->tri_off[set + 2] : nullptr;
+    }
+    j.f = f[q];
+    j.df = df[q];
+    j.mode = d->solver ? 3 : 0;
+    if (ax == 0) {
+      j.na = ny; j.nb = nz; j.sa = nx; j.sb = (long long)nx * ny; j.s = 1;
+    } else if (ax == 1) {
+      j.na = nx; j.nb = nz; j.sa = 1; j.sb = (long long)nx * ny; j.s = nx;
+    } else {
+      j.na = nx; j.nb = ny; j.sa = 1; j.sb = nx; j.s = (long long)nx * ny;
+    }
+    const long long lines = (long long)j.na * j.nb;
+    J.start[q + 1] = J.start[q] + (lines + 31) / 32 * 32;
+  }
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const unsigned grid = (unsigned)((J.start[count] + 127) / 128);
+  der_lines_multi<<<grid, 128, 0, st>>>(J);
+  MF_CUDA(cudaGetLastError());
+  return MF_OK;
+}
+
 
 int mf_der_apply(const mf_der_t* dc_c, int axis, int order, const double* f, double* df, int nx,
                  int ny, int nz, void* stream) {

@@ -18,7 +18,8 @@
 //
 // Stages per step (device work only, on the caller's stream):
 //   flow-rate term   weighted sum of extrapol(u) (k_ns_wsum) -> k_ns_flow
-//   presolve         k_ns_nonlinear (newest slot) + k_ns_presolve
+//   presolve         k_ns_advect / k_ns_products / k_ns_skew (newest slot,
+//                    eighteen sweeps in two launches) + k_ns_presolve
 //   boundary values  k_ns_bc_velocity (+ gradient of extrapol(phi), pt = 1)
 //   velocity solves  k_ns_fu (interior rhs) + three Helmholtz solves
 //   pressure         k_ns_scale, div of rhs_p, k_ns_fphi, k_ns_bc_phi, one
@@ -200,41 +201,53 @@ __global__ void k_ns_extrapol(Lin L, int nx, int ny, int nz, double* __restrict_
   out[q] = on_edge(i, j, k, nx, ny, nz) ? 0.0 : lin_at(L, q);
 }
 
-// x u, x v, x w of one slot (the products of the skew-symmetric form).
-__global__ void k_ns_products(long long n, const double* __restrict__ x, const double* __restrict__ u,
-                              const double* __restrict__ v, const double* __restrict__ w,
-                              double* __restrict__ pu, double* __restrict__ pv, double* __restrict__ pw) {
+// The three components c of navier_nonlinear at one slot in one launch
+// (blockIdx.y = c).  D holds the nine derivatives d x_c / d x_d at
+// D + (3 d + c) n; out_c = out + c ostride.  nlt 1: u dx + v dy + w dz;
+// nlt 2: half of it (class_navier_3D.f90:1195-1206); nlt 0: 0.
+__global__ void k_ns_advect(long long n, int nlt, const double* __restrict__ u, const double* __restrict__ v,
+                            const double* __restrict__ w, const double* __restrict__ D,
+                            double* __restrict__ out, long long ostride) {
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= n) return;
-  const double xv = x[q];
-  pu[q] = xv * u[q];
-  pv[q] = xv * v[q];
-  pw[q] = xv * w[q];
-}
-
-// navier_nonlinear of one slot: nlt 1: u dx + v dy + w dz; nlt 2: half of it
-// plus halves of d(xu)/dx, d(xv)/dy, d(xw)/dz (class_navier_3D.f90:1195-1213);
-// nlt 0: 0.
-__global__ void k_ns_nonlinear(long long n, int nlt, const double* __restrict__ u,
-                               const double* __restrict__ v, const double* __restrict__ w,
-                               const double* __restrict__ dx, const double* __restrict__ dy,
-                               const double* __restrict__ dz, const double* __restrict__ px,
-                               const double* __restrict__ py, const double* __restrict__ pz,
-                               double* __restrict__ out) {
-  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= n) return;
+  const int c = blockIdx.y;
+  double* o = out + c * ostride;
   if (nlt != 1 && nlt != 2) {
-    out[q] = 0.0;
+    o[q] = 0.0;
     return;
   }
-  double t = u[q] * dx[q] + v[q] * dy[q] + w[q] * dz[q];
-  if (nlt == 2) {
-    t = t * 0.5;
-    t = t + px[q] * 0.5;
-    t = t + py[q] * 0.5;
-    t = t + pz[q] * 0.5;
-  }
-  out[q] = t;
+  double t = u[q] * D[c * n + q] + v[q] * D[(3 + c) * n + q] + w[q] * D[(6 + c) * n + q];
+  if (nlt == 2) t = t * 0.5;
+  o[q] = t;
+}
+
+// Products of the skew-symmetric form: P + (3 d + c) n = x_c u_d with
+// x_c = x + c xstride (u, v, w of one slot), u_d = u, v, w (blockIdx.y = c).
+__global__ void k_ns_products(long long n, const double* __restrict__ x, long long xstride,
+                              const double* __restrict__ u, const double* __restrict__ v,
+                              const double* __restrict__ w, double* __restrict__ P) {
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const int c = blockIdx.y;
+  const double xv = x[c * xstride + q];
+  P[c * n + q] = xv * u[q];
+  P[(3 + c) * n + q] = xv * v[q];
+  P[(6 + c) * n + q] = xv * w[q];
+}
+
+// nlt 2, second half (:1208-1213): out_c += d(x_c u)/dx 0.5, then
+// d(x_c v)/dy 0.5, then d(x_c w)/dz 0.5, with E + (3 d + c) n the
+// derivatives of the products.
+__global__ void k_ns_skew(long long n, const double* __restrict__ E, double* __restrict__ out, long long ostride) {
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const int c = blockIdx.y;
+  double* o = out + c * ostride;
+  double t = o[q];
+  t = t + E[c * n + q] * 0.5;
+  t = t + E[(3 + c) * n + q] * 0.5;
+  t = t + E[(6 + c) * n + q] * 0.5;
+  o[q] = t;
 }
 
 // navier_presolve_{u,v,w} (class_navier_3D.f90:1528-1595):
@@ -504,7 +517,7 @@ struct mf_navier {
   DevBuf nl;      // [3][kNt] cached nonlinear terms
   DevBuf rhs;     // [3][2] rhs_u(1), rhs_u(2) ...
   DevBuf rp;      // rhs_px, rhs_py, rhs_pz
-  DevBuf tmp;     // 9 work fields
+  DevBuf tmp;     // 18 work fields
   DevBuf fin;     // interior right-hand side of a solve
   DevBuf exact;   // u, v, p, rhsu, rhsv of the exact solution
   DevBuf bcex;    // exact face values of u, v, w
@@ -559,11 +572,6 @@ Lin extrapol_of(const mf_navier* nv, int order, double* (*slot_ptr)(const mf_nav
 double* field_ptr(const mf_navier* nv, int var, int slot) { return nv->F(var, slot); }
 double* nl_ptr(const mf_navier* nv, int c, int slot) { return nv->NL(c, slot); }
 
-int der(const mf_navier* nv, int axis, const double* f, double* df, cudaStream_t st) {
-  const mf_der_t* dc = axis == 0 ? nv->dcx : axis == 1 ? nv->dcy : nv->dcz;
-  return mf_der_apply(dc, axis, 1, f, df, nv->nx, nv->ny, nv->nz, st);
-}
-
 int launch_check(const char* what) {
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? MF_OK : cuda_error(e, what);
@@ -574,26 +582,66 @@ int extrapol_into(const mf_navier* nv, const Lin& L, double* out, cudaStream_t s
   return launch_check("k_ns_extrapol");
 }
 
-// Nonlinear term of component c (0..2) at `slot` into its cache entry.
-int nonlinear(mf_navier* nv, int c, int slot, cudaStream_t st) {
-  const double* x = nv->F(c, slot);
+// Independent derivative sweeps of the step's fields, launched together
+// (mf_der_apply_many): the lines of one 128 x 129 x 128 sweep alone fill a
+// GB300 only to ~3 warps per SM.
+struct Sweeps {
+  int n = 0;
+  const mf_der_t* dc[9];
+  int axis[9], order[9];
+  const double* f[9];
+  double* df[9];
+  void add(const mf_navier* nv, int ax, const double* in, double* out) {
+    dc[n] = ax == 0 ? nv->dcx : ax == 1 ? nv->dcy : nv->dcz;
+    axis[n] = ax;
+    order[n] = 1;
+    f[n] = in;
+    df[n] = out;
+    ++n;
+  }
+  int run(const mf_navier* nv, cudaStream_t st) const {
+    return mf_der_apply_many(n, dc, axis, order, f, df, nv->nx, nv->ny, nv->nz, st);
+  }
+};
+
+// Gradient of f: d/dx, d/dy, d/dz into out0, out1, out2.
+int gradient(const mf_navier* nv, const double* f, double* out0, double* out1, double* out2, cudaStream_t st) {
+  Sweeps S;
+  S.add(nv, 0, f, out0);
+  S.add(nv, 1, f, out1);
+  S.add(nv, 2, f, out2);
+  return S.run(nv, st);
+}
+
+// navier_nonlinear of the three components at `slot` into their cache
+// entries: nine sweeps d x_c / d x_d in one launch, and for nlt 2 the nine
+// products x_c u_d and their sweeps in another.
+int nonlinear_slot(mf_navier* nv, int slot, cudaStream_t st) {
+  const long long n = nv->np;
   const double *u = nv->F(0, slot), *v = nv->F(1, slot), *w = nv->F(2, slot);
+  const long long xstride = nv->F(1, slot) - nv->F(0, slot);
+  const long long ostride = nv->NL(1, slot) - nv->NL(0, slot);
+  const dim3 grid(ns_blocks(n), 3);
   int rc;
   if (nv->prm.nlt == 1 || nv->prm.nlt == 2) {
-    if ((rc = der(nv, 0, x, nv->T(0), st)) || (rc = der(nv, 1, x, nv->T(1), st)) ||
-        (rc = der(nv, 2, x, nv->T(2), st)))
-      return rc;
+    Sweeps S;
+    for (int d = 0; d < 3; ++d)
+      for (int c = 0; c < 3; ++c) S.add(nv, d, nv->F(c, slot), nv->T(3 * d + c));
+    if ((rc = S.run(nv, st))) return rc;
   }
+  k_ns_advect<<<grid, kNsThreads, 0, st>>>(n, nv->prm.nlt, u, v, w, nv->T(0), nv->NL(0, slot), ostride);
+  if ((rc = launch_check("k_ns_advect"))) return rc;
   if (nv->prm.nlt == 2) {
-    k_ns_products<<<ns_blocks(nv->np), kNsThreads, 0, st>>>(nv->np, x, u, v, w, nv->T(3), nv->T(4), nv->T(5));
-    if ((rc = launch_check("k_ns_products")) || (rc = der(nv, 0, nv->T(3), nv->T(6), st)) ||
-        (rc = der(nv, 1, nv->T(4), nv->T(7), st)) || (rc = der(nv, 2, nv->T(5), nv->T(8), st)))
-      return rc;
+    k_ns_products<<<grid, kNsThreads, 0, st>>>(n, u, xstride, u, v, w, nv->T(9));
+    if ((rc = launch_check("k_ns_products"))) return rc;
+    Sweeps S;
+    for (int d = 0; d < 3; ++d)
+      for (int c = 0; c < 3; ++c) S.add(nv, d, nv->T(9 + 3 * d + c), nv->T(3 * d + c));
+    if ((rc = S.run(nv, st))) return rc;
+    k_ns_skew<<<grid, kNsThreads, 0, st>>>(n, nv->T(0), nv->NL(0, slot), ostride);
+    if ((rc = launch_check("k_ns_skew"))) return rc;
   }
-  k_ns_nonlinear<<<ns_blocks(nv->np), kNsThreads, 0, st>>>(nv->np, nv->prm.nlt, u, v, w, nv->T(0), nv->T(1),
-                                                           nv->T(2), nv->T(6), nv->T(7), nv->T(8),
-                                                           nv->NL(c, slot));
-  return launch_check("k_ns_nonlinear");
+  return MF_OK;
 }
 
 int solve(mf_navier* nv, mf_solver3d_t* sc, double sigma, double* solf, const double* bc3,
@@ -636,8 +684,7 @@ int ns_step(mf_navier* nv, cudaStream_t st) {
   for (int t = 0; t < nlv0.m; ++t) {
     const int slot = t == 0 ? s0 : t == 1 ? s1 : s2;
     if (!nv->nl_ok[slot]) {
-      for (int c = 0; c < 3; ++c)
-        if ((rc = nonlinear(nv, c, slot, st))) return rc;
+      if ((rc = nonlinear_slot(nv, slot, st))) return rc;
       nv->nl_ok[slot] = true;
     }
   }
@@ -661,8 +708,7 @@ int ns_step(mf_navier* nv, cudaStream_t st) {
   // velocity boundary values (+ gradient of extrapol(phi) for pt = 1)
   const Lin ephi = extrapol_of(nv, P.top - 1, field_ptr, kVarPhi);
   if (P.pt == 1) {
-    if ((rc = extrapol_into(nv, ephi, nv->T(0), st)) || (rc = der(nv, 0, nv->T(0), nv->T(1), st)) ||
-        (rc = der(nv, 1, nv->T(0), nv->T(2), st)) || (rc = der(nv, 2, nv->T(0), nv->T(3), st)))
+    if ((rc = extrapol_into(nv, ephi, nv->T(0), st)) || (rc = gradient(nv, nv->T(0), nv->T(1), nv->T(2), nv->T(3), st)))
       return rc;
     k_ns_bc_velocity<<<fb, kNsThreads, 0, st>>>(nv->faces, nv->bcex.as<double>(), nv->T(1), nv->T(2), nv->T(3),
                                                 fac1, nv->bc.as<double>());
@@ -674,8 +720,7 @@ int ns_step(mf_navier* nv, cudaStream_t st) {
   // velocity Helmholtz solves (pt = 2: + gradient of extrapol(p))
   if (P.pt == 2) {
     if ((rc = extrapol_into(nv, extrapol_of(nv, P.top - 1, field_ptr, kVarP), nv->T(0), st)) ||
-        (rc = der(nv, 0, nv->T(0), nv->T(1), st)) || (rc = der(nv, 1, nv->T(0), nv->T(2), st)) ||
-        (rc = der(nv, 2, nv->T(0), nv->T(3), st)))
+        (rc = gradient(nv, nv->T(0), nv->T(1), nv->T(2), nv->T(3), st)))
       return rc;
   }
   const unsigned ib = ns_blocks(nv->nin);
@@ -692,9 +737,11 @@ int ns_step(mf_navier* nv, cudaStream_t st) {
     k_ns_scale<<<gb, kNsThreads, 0, st>>>(nv->nx, nv->ny, nv->nz, fac1, nv->F(c, nw), nv->RP(c));
     if ((rc = launch_check("k_ns_scale"))) return rc;
   }
-  if ((rc = der(nv, 0, nv->RP(0), nv->T(4), st)) || (rc = der(nv, 1, nv->RP(1), nv->T(5), st)) ||
-      (rc = der(nv, 2, nv->RP(2), nv->T(6), st)) || (rc = extrapol_into(nv, ephi, nv->T(0), st)))
-    return rc;
+  {
+    Sweeps S;
+    for (int c = 0; c < 3; ++c) S.add(nv, c, nv->RP(c), nv->T(4 + c));
+    if ((rc = S.run(nv, st)) || (rc = extrapol_into(nv, ephi, nv->T(0), st))) return rc;
+  }
   k_ns_fphi<<<ib, kNsThreads, 0, st>>>(nv->nx, nv->ny, nv->nz, nv->sigmap, nv->T(0), nv->T(4), nv->T(5),
                                        nv->T(6), nv->fin.as<double>());
   k_ns_bc_phi<<<fb, kNsThreads, 0, st>>>(nv->faces, nv->RP(0), nv->RP(1), nv->RP(2), nv->bc.as<double>(), fac1,
@@ -705,17 +752,19 @@ int ns_step(mf_navier* nv, cudaStream_t st) {
   k_ns_zero_edges<<<gb, kNsThreads, 0, st>>>(nv->nx, nv->ny, nv->nz, nv->F(kVarPhi, nw));
   if ((rc = launch_check("k_ns_zero_edges"))) return rc;
   if (P.pt == 2 && (rc = extrapol_into(nv, extrapol_of(nv, P.top - 1, field_ptr, kVarP), nv->T(0), st))) return rc;
-  if ((rc = der(nv, 0, nv->F(0, nw), nv->T(1), st)) || (rc = der(nv, 1, nv->F(1, nw), nv->T(2), st)) ||
-      (rc = der(nv, 2, nv->F(2, nw), nv->T(3), st)))
-    return rc;
+  {
+    // divergence of u* and gradient of phi: six sweeps in one launch
+    Sweeps S;
+    for (int c = 0; c < 3; ++c) S.add(nv, c, nv->F(c, nw), nv->T(1 + c));
+    for (int c = 0; c < 3; ++c) S.add(nv, c, nv->F(kVarPhi, nw), nv->T(4 + c));
+    if ((rc = S.run(nv, st))) return rc;
+  }
   k_ns_pressure<<<gb, kNsThreads, 0, st>>>(nv->nx, nv->ny, nv->nz, nv->F(kVarPhi, nw),
                                            P.pt == 2 ? nv->T(0) : nullptr, nv->T(1), nv->T(2), nv->T(3), P.reynolds,
                                            nv->F(kVarP, nw));
-  if ((rc = launch_check("k_ns_pressure")) || (rc = der(nv, 0, nv->F(kVarPhi, nw), nv->T(1), st)) ||
-      (rc = der(nv, 1, nv->F(kVarPhi, nw), nv->T(2), st)) || (rc = der(nv, 2, nv->F(kVarPhi, nw), nv->T(3), st)))
-    return rc;
+  if ((rc = launch_check("k_ns_pressure"))) return rc;
   for (int c = 0; c < 3; ++c) {
-    k_ns_velocity<<<gb, kNsThreads, 0, st>>>(nv->nx, nv->ny, nv->nz, nv->RP(c), nv->T(1 + c), fac1, nv->F(c, nw));
+    k_ns_velocity<<<gb, kNsThreads, 0, st>>>(nv->nx, nv->ny, nv->nz, nv->RP(c), nv->T(4 + c), fac1, nv->F(c, nw));
     if ((rc = launch_check("k_ns_velocity"))) return rc;
   }
   nv->nl_ok[nw] = false;
@@ -727,9 +776,11 @@ int ns_diagnostics(mf_navier* nv, double* diag, cudaStream_t st) {
   const int cur = nv->it[kNt - 1], prev = nv->it[kNt - 2];
   const int groups = (nv->ny + kWRows - 1) / kWRows, count = nv->nz * groups;
   int rc;
-  if ((rc = der(nv, 0, nv->F(0, cur), nv->T(1), st)) || (rc = der(nv, 1, nv->F(1, cur), nv->T(2), st)) ||
-      (rc = der(nv, 2, nv->F(2, cur), nv->T(3), st)))
-    return rc;
+  {
+    Sweeps S;
+    for (int c = 0; c < 3; ++c) S.add(nv, c, nv->F(c, cur), nv->T(1 + c));
+    if ((rc = S.run(nv, st))) return rc;
+  }
   DiagIn D{};
   D.u = nv->F(0, cur); D.v = nv->F(1, cur); D.w = nv->F(2, cur); D.p = nv->F(kVarP, cur);
   D.up = nv->F(0, prev); D.vp = nv->F(1, prev); D.wp = nv->F(2, prev); D.pp = nv->F(kVarP, prev);
@@ -862,7 +913,7 @@ int mf_navier_create(const double* gx, int nx, const double* gy, int ny, const d
       (rc = mf_solver_coeffs_init_3d(gx, gy, gz, nx, ny, nz, bctp, p->so_solver, &nv->scp)))
     return fail(rc);
   if ((rc = nv->fields.ensure(fb * 5 * kNt)) || (rc = nv->nl.ensure(fb * 3 * kNt)) ||
-      (rc = nv->rhs.ensure(fb * 6)) || (rc = nv->rp.ensure(fb * 3)) || (rc = nv->tmp.ensure(fb * 9)) ||
+      (rc = nv->rhs.ensure(fb * 6)) || (rc = nv->rp.ensure(fb * 3)) || (rc = nv->tmp.ensure(fb * 18)) ||
       (rc = nv->fin.ensure((size_t)nv->nin * sizeof(double))) || (rc = nv->exact.ensure(fb * 5)) ||
       (rc = nv->bcex.ensure(sizeof(double) * 3 * ftot)) || (rc = nv->bc.ensure(sizeof(double) * 4 * ftot)) ||
       (rc = nv->grid.ensure(sizeof(double) * (nx + ny + nz))) ||

@@ -94,6 +94,8 @@ _PROTOS = {
     "mf_ddery": [_P, _P, _P, _I, _I, _I, _P],
     "mf_dderz": [_P, _P, _P, _I, _I, _I, _P],
     "mf_der_lines": [_P, _I, _I, _P, _P, _I, _P],
+    "mf_der_apply_many": [_I, ctypes.POINTER(_P), _IP, _IP, ctypes.POINTER(_P), ctypes.POINTER(_P), _I, _I, _I,
+                          _P],
     "mf_solver_coeffs_init_3d": [_DP, _DP, _DP, _I, _I, _I, _IP, _I, ctypes.POINTER(_P)],
     "mf_solver3d_destroy": [_P],
     "mf_solve_3d": [_P, _P, _D, _P, _P, _P, _P, _I, _I, _I, _P],
@@ -915,6 +917,19 @@ def channel_stats(us, vs, ws, ps, gx, gy, gz, re, so=6, stream=None):
     out.update({"rms" + k: rms[q * ny:(q + 1) * ny] for q, k in enumerate(["u", "v", "w", "p", "uv", "uw", "vw"])})
     out["utau"] = utau.value
     return out
+
+
+def der_apply_many(jobs, stream=None):
+    """Up to 9 derivative sweeps in one launch: jobs = [(dc, axis, order, f, out)]
+    on device fields of one shape; returns the outputs."""
+    n = len(jobs)
+    nx, ny, nz = jobs[0][3].shape
+    dcs = (_P * n)(*[j[0]._h for j in jobs])
+    axes = (_I * n)(*[int(j[1]) for j in jobs])
+    orders = (_I * n)(*[int(j[2]) for j in jobs])
+    _check(_lib.mf_der_apply_many(n, dcs, axes, orders, _ptrs([j[3] for j in jobs]), _ptrs([j[4] for j in jobs]),
+                                  nx, ny, nz, _stream(stream)))
+    return [j[4] for j in jobs]
 
 
 # ---------------------------------------------------------------------------

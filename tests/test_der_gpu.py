@@ -95,3 +95,21 @@ def test_shape_errors(mf, gpu):
     # the GPU is still usable afterwards
     out = dc.apply(0, 1, mf.to_device(np.ones((11, 3, 3), order="F")))
     assert np.max(np.abs(mf.to_host(out))) < 1e-9
+
+
+def test_der_apply_many_equals_separate_sweeps(mf, gpu):
+    """Nine sweeps of mixed axes, orders and fields in one launch give the
+    results of nine mf_der_apply calls, for plain and solver-type coefficients."""
+    import torch
+    from oracle import mesh
+    shape = (19, 14, 17)
+    for solver in (False, True):
+        dcs = [mf.DerivativesCoefficients(g, solve=solver, so=6)
+               for g in (mesh.tanh_grid(shape[0], 1.0), mesh.tanh_grid(shape[1], 1.5), mesh.uniform_grid(shape[2]))]
+        rng = np.random.default_rng(7)
+        fs = [mf.to_device(rng.standard_normal(shape)) for _ in range(3)]
+        jobs = [(dcs[a], a, 1 + (q % 2), fs[q % 3], mf.empty_device(shape)) for q, a in
+                enumerate((0, 1, 2, 0, 1, 2, 2, 1, 0))]
+        mf.der_apply_many(jobs)
+        for dc, a, order, f, out in jobs:
+            assert torch.equal(out, dc.apply(a, order, f)), (solver, a, order)
