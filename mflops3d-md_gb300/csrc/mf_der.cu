@@ -214,6 +214,11 @@ int mf_der_coeffs_init(const double* grid, int n, int solver_type, int so, mf_de
     delete dc;
     return cuda_error(e, "cudaMemcpy(derivative coefficients)");
   }
+  // the uploads complete before the handle is used on any stream
+  if ((e = cudaDeviceSynchronize()) != cudaSuccess) {
+    mf_der_destroy(dc);
+    return cuda_error(e, "cudaDeviceSynchronize(derivative coefficients)");
+  }
   *out = dc;
   return MF_OK;
 }

@@ -545,6 +545,8 @@ int mf_filter_lsq_init(const double* xi, int ni, const double* wi, const double*
       f->nc = B.nc;
     }
   }
+  if (!rc && cudaDeviceSynchronize() != cudaSuccess)  // uploads complete before use on any stream
+    rc = set_error(MF_ERR_CUDA, "filter set-up: upload failed");
   if (rc) {
     mf_filter_destroy(f);
     return rc;
@@ -561,6 +563,8 @@ int mf_filter_period_init(const double* xi, int ni, const double* xos, int nos, 
   f->ni = ni;
   f->no = nos;
   if (!rc) rc = filter_upload(f);
+  if (!rc && cudaDeviceSynchronize() != cudaSuccess)  // uploads complete before use on any stream
+    rc = set_error(MF_ERR_CUDA, "filter set-up: upload failed");
   if (rc) {
     mf_filter_destroy(f);
     return rc;

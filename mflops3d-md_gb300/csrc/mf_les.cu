@@ -414,6 +414,10 @@ int mf_les_create(const double* gx, int nx, const double* gy, int ny, const doub
       return rc;
     }
   }
+  if (cudaDeviceSynchronize() != cudaSuccess) {  // uploads complete before use on any stream
+    mf_les_destroy(les);
+    return set_error(MF_ERR_CUDA, "mf_les_create: upload failed");
+  }
   *out = les;
   return MF_OK;
 }

@@ -471,7 +471,8 @@ int mf_md_create(const int nd[3], const int periods[3], const double* const* gri
   if (!rc) rc = md->zero_int.ensure(max_field * 8);
   if (!rc) rc = md->ufield.ensure(max_field * 8);
   if (!rc) rc = md->vec.ensure(sizeof(double) * std::max<long long>(1, md->topo.ninf));
-  if (!rc && cudaMemset(md->zero_int.ptr, 0, max_field * 8) != cudaSuccess)
+  if (!rc && (cudaMemset(md->zero_int.ptr, 0, max_field * 8) != cudaSuccess ||
+              cudaDeviceSynchronize() != cudaSuccess))
     rc = set_error(MF_ERR_CUDA, "mf_md_create: memset failed");
   // the dense solver's handle (its first creation in a process loads the
   // library, which belongs to set-up rather than to a matrix assembly)

@@ -269,7 +269,8 @@ int mf_mlp_create(unsigned long long seed, mf_mlp_t** out) {
   }
   if (cudaMemcpy(mlp->params.ptr, p.data(), sizeof(float) * kMlpParams, cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaMemset(mlp->m.ptr, 0, sizeof(float) * kParamsPad) != cudaSuccess ||
-      cudaMemset(mlp->v.ptr, 0, sizeof(float) * kParamsPad) != cudaSuccess) {
+      cudaMemset(mlp->v.ptr, 0, sizeof(float) * kParamsPad) != cudaSuccess ||
+      cudaDeviceSynchronize() != cudaSuccess) {
     mf_mlp_destroy(mlp);
     return set_error(MF_ERR_CUDA, "mf_mlp_create: upload failed");
   }
@@ -297,6 +298,7 @@ int mf_mlp_set_params(mf_mlp_t* mlp, const float* host) {
   MF_CUDA(cudaMemcpy(mlp->params.ptr, host, sizeof(float) * kMlpParams, cudaMemcpyHostToDevice));
   MF_CUDA(cudaMemset(mlp->m.ptr, 0, sizeof(float) * kParamsPad));
   MF_CUDA(cudaMemset(mlp->v.ptr, 0, sizeof(float) * kParamsPad));
+  MF_CUDA(cudaDeviceSynchronize());  // ordered before work on any stream
   mlp->step = 0;
   return MF_OK;
 }

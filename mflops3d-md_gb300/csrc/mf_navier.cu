@@ -21,7 +21,8 @@
 //   presolve         k_ns_advect / k_ns_products / k_ns_skew (newest slot,
 //                    eighteen sweeps in two launches) + k_ns_presolve
 //   boundary values  k_ns_bc_velocity (+ gradient of extrapol(phi), pt = 1)
-//   velocity solves  k_ns_fu (interior rhs) + three Helmholtz solves
+//   velocity solves  k_ns_fu (interior rhs) + three Helmholtz solves, u on
+//                    the caller's stream, v and w on forked streams
 //   pressure         k_ns_scale, div of rhs_p, k_ns_fphi, k_ns_bc_phi, one
 //                    all-Neumann Poisson solve at sigma = 0
 //   projection       k_ns_pressure, k_ns_velocity
@@ -512,13 +513,17 @@ struct mf_navier {
   bool nl_ok[kNt] = {false, false, false, false};
   int rhs_cur = 0;
   mf_der_t *dcx = nullptr, *dcy = nullptr, *dcz = nullptr;
-  mf_solver3d_t *scu = nullptr, *scp = nullptr;
+  // velocity solver sets scu, scv, scw (as the reference keeps them) and the
+  // pressure set; the three velocity solves run on forked streams
+  mf_solver3d_t *scu = nullptr, *scv = nullptr, *scw = nullptr, *scp = nullptr;
+  cudaStream_t side[2] = {nullptr, nullptr};
+  cudaEvent_t fork = nullptr, join[2] = {nullptr, nullptr};
   DevBuf fields;  // [5 vars][kNt slots] fields
   DevBuf nl;      // [3][kNt] cached nonlinear terms
   DevBuf rhs;     // [3][2] rhs_u(1), rhs_u(2) ...
   DevBuf rp;      // rhs_px, rhs_py, rhs_pz
   DevBuf tmp;     // 18 work fields
-  DevBuf fin;     // interior right-hand side of a solve
+  DevBuf fin;     // interior right-hand sides of the solves (three)
   DevBuf exact;   // u, v, p, rhsu, rhsv of the exact solution
   DevBuf bcex;    // exact face values of u, v, w
   DevBuf bc;      // face values of u, v, w, phi
@@ -644,12 +649,11 @@ int nonlinear_slot(mf_navier* nv, int slot, cudaStream_t st) {
   return MF_OK;
 }
 
-int solve(mf_navier* nv, mf_solver3d_t* sc, double sigma, double* solf, const double* bc3,
+int solve(mf_navier* nv, mf_solver3d_t* sc, const double* rhs, double sigma, double* solf, const double* bc3,
           cudaStream_t st) {
   const double* bx = bc3;
   const double* by = bc3 + nv->faces.sx;
   const double* bz = bc3 + nv->faces.sx + nv->faces.sy;
-  const double* rhs = nv->fin.as<double>();
   if (nv->prm.precision == MF_PREC_FP64)
     return mf_solve_3d(sc, rhs, sigma, solf, bx, by, bz, nv->n1, nv->n2, nv->n3, st);
   return mf_solve_3d_mixed(sc, rhs, sigma, solf, bx, by, bz, nv->n1, nv->n2, nv->n3, nv->prm.precision,
@@ -724,13 +728,24 @@ int ns_step(mf_navier* nv, cudaStream_t st) {
       return rc;
   }
   const unsigned ib = ns_blocks(nv->nin);
+  // the three Helmholtz solves: u on the caller's stream, v and w on forked
+  // streams joined back before the pressure stage
+  MF_CUDA(cudaEventRecord(nv->fork, st));
+  for (int q = 0; q < 2; ++q) MF_CUDA(cudaStreamWaitEvent(nv->side[q], nv->fork, 0));
+  mf_solver3d_t* sets[3] = {nv->scu, nv->scv, nv->scw};
   for (int c = 0; c < 3; ++c) {
-    k_ns_fu<<<ib, kNsThreads, 0, st>>>(nv->nx, nv->ny, nv->nz, nv->F(c, s0), nv->F(c, s1),
+    cudaStream_t sc = c == 0 ? st : nv->side[c - 1];
+    double* rhs = nv->fin.as<double>() + (size_t)c * nv->nin;
+    k_ns_fu<<<ib, kNsThreads, 0, sc>>>(nv->nx, nv->ny, nv->nz, nv->F(c, s0), nv->F(c, s1),
                                        P.tou == 3 ? nv->F(c, s2) : nullptr, nv->fac[1], nv->fac[2], nv->fac[3],
                                        P.pt == 2 ? nv->T(1 + c) : nullptr, nv->RHS(c, nv->rhs_cur),
-                                       P.reynolds, nv->fin.as<double>());
-    if ((rc = launch_check("k_ns_fu")) || (rc = solve(nv, nv->scu, nv->sigmau, nv->F(c, nw), nv->BC(c), st)))
+                                       P.reynolds, rhs);
+    if ((rc = launch_check("k_ns_fu")) || (rc = solve(nv, sets[c], rhs, nv->sigmau, nv->F(c, nw), nv->BC(c), sc)))
       return rc;
+  }
+  for (int q = 0; q < 2; ++q) {
+    MF_CUDA(cudaEventRecord(nv->join[q], nv->side[q]));
+    MF_CUDA(cudaStreamWaitEvent(st, nv->join[q], 0));
   }
   // pressure increment: rhs_p = fac(1) u*, Poisson solve with Neumann data
   for (int c = 0; c < 3; ++c) {
@@ -746,7 +761,7 @@ int ns_step(mf_navier* nv, cudaStream_t st) {
                                        nv->T(6), nv->fin.as<double>());
   k_ns_bc_phi<<<fb, kNsThreads, 0, st>>>(nv->faces, nv->RP(0), nv->RP(1), nv->RP(2), nv->bc.as<double>(), fac1,
                                          nv->BC(3));
-  if ((rc = launch_check("k_ns_fphi")) || (rc = solve(nv, nv->scp, nv->sigmap, nv->F(kVarPhi, nw), nv->BC(3), st)))
+  if ((rc = launch_check("k_ns_fphi")) || (rc = solve(nv, nv->scp, nv->fin.as<double>(), nv->sigmap, nv->F(kVarPhi, nw), nv->BC(3), st)))
     return rc;
   // projection
   k_ns_zero_edges<<<gb, kNsThreads, 0, st>>>(nv->nx, nv->ny, nv->nz, nv->F(kVarPhi, nw));
@@ -861,7 +876,14 @@ int mf_navier_destroy(mf_navier_t* nv) {
   mf_der_destroy(nv->dcy);
   mf_der_destroy(nv->dcz);
   mf_solver3d_destroy(nv->scu);
+  mf_solver3d_destroy(nv->scv);
+  mf_solver3d_destroy(nv->scw);
   mf_solver3d_destroy(nv->scp);
+  for (int q = 0; q < 2; ++q) {
+    if (nv->side[q]) cudaStreamDestroy(nv->side[q]);
+    if (nv->join[q]) cudaEventDestroy(nv->join[q]);
+  }
+  if (nv->fork) cudaEventDestroy(nv->fork);
   for (DevBuf* b : {&nv->fields, &nv->nl, &nv->rhs, &nv->rp, &nv->tmp, &nv->fin, &nv->exact, &nv->bcex,
                     &nv->bc, &nv->grid, &nv->wts, &nv->part, &nv->sums, &nv->state})
     b->release();
@@ -910,11 +932,13 @@ int mf_navier_create(const double* gx, int nx, const double* gy, int ny, const d
       (rc = mf_der_coeffs_init(gy, ny, 1, p->so_der, &nv->dcy)) ||
       (rc = mf_der_coeffs_init(gz, nz, 1, p->so_der, &nv->dcz)) ||
       (rc = mf_solver_coeffs_init_3d(gx, gy, gz, nx, ny, nz, bctu, p->so_solver, &nv->scu)) ||
+      (rc = mf_solver_coeffs_init_3d(gx, gy, gz, nx, ny, nz, bctu, p->so_solver, &nv->scv)) ||
+      (rc = mf_solver_coeffs_init_3d(gx, gy, gz, nx, ny, nz, bctu, p->so_solver, &nv->scw)) ||
       (rc = mf_solver_coeffs_init_3d(gx, gy, gz, nx, ny, nz, bctp, p->so_solver, &nv->scp)))
     return fail(rc);
   if ((rc = nv->fields.ensure(fb * 5 * kNt)) || (rc = nv->nl.ensure(fb * 3 * kNt)) ||
       (rc = nv->rhs.ensure(fb * 6)) || (rc = nv->rp.ensure(fb * 3)) || (rc = nv->tmp.ensure(fb * 18)) ||
-      (rc = nv->fin.ensure((size_t)nv->nin * sizeof(double))) || (rc = nv->exact.ensure(fb * 5)) ||
+      (rc = nv->fin.ensure((size_t)nv->nin * sizeof(double) * 3)) || (rc = nv->exact.ensure(fb * 5)) ||
       (rc = nv->bcex.ensure(sizeof(double) * 3 * ftot)) || (rc = nv->bc.ensure(sizeof(double) * 4 * ftot)) ||
       (rc = nv->grid.ensure(sizeof(double) * (nx + ny + nz))) ||
       (rc = nv->wts.ensure(sizeof(double) * (nx + ny + nz))) ||
@@ -939,6 +963,12 @@ int mf_navier_create(const double* gx, int nx, const double* gy, int ny, const d
         if (b <= 1) reft += w[i] * w[nx + j] * w[nx + ny + k];
       }
   nv->reft = reft;
+  for (int q = 0; q < 2; ++q)
+    if (cudaStreamCreateWithFlags(&nv->side[q], cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&nv->join[q], cudaEventDisableTiming) != cudaSuccess)
+      return fail(set_error(MF_ERR_CUDA, "mf_navier_create: stream set-up failed"));
+  if (cudaEventCreateWithFlags(&nv->fork, cudaEventDisableTiming) != cudaSuccess)
+    return fail(set_error(MF_ERR_CUDA, "mf_navier_create: stream set-up failed"));
   cudaStream_t st = nullptr;
   if (cudaMemcpy(nv->grid.ptr, g.data(), g.size() * 8, cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaMemcpy(nv->wts.ptr, w.data(), w.size() * 8, cudaMemcpyHostToDevice) != cudaSuccess ||

@@ -1527,8 +1527,10 @@ static int residual_passes(mf_solver3d* sc, const T* rin, const In* u, double si
 }
 
 // Operand buffers and tensor-core plans of one mixed format (split-BF16 or
-// 3xTF32), created on first use.
-static int mixed_prepare(mf_solver3d* sc, bool tf32) {
+// 3xTF32), created on first use; the zeroing is ordered on the caller's
+// stream st (a legacy-stream memset would not be ordered before work on a
+// non-blocking stream).
+static int mixed_prepare(mf_solver3d* sc, bool tf32, cudaStream_t st) {
   if (tf32 ? sc->mixed32_ready : sc->mixed_ready) return MF_OK;
   for (int a = 0; a < 3; ++a)
     if (sc->P[a] > 256)
@@ -1549,10 +1551,10 @@ static int mixed_prepare(mf_solver3d* sc, bool tf32) {
   for (DevBuf* x : {xa[0], xa[1], xb[0], xb[1]}) {
     if (!x) continue;
     if ((rc = x->ensure(bytes))) return rc;
-    MF_CUDA(cudaMemset(x->ptr, 0, bytes));
+    MF_CUDA(cudaMemsetAsync(x->ptr, 0, bytes, st));
   }
   if ((rc = sc->err.ensure(sizeof(int)))) return rc;
-  MF_CUDA(cudaMemset(sc->err.ptr, 0, sizeof(int)));
+  MF_CUDA(cudaMemsetAsync(sc->err.ptr, 0, sizeof(int), st));
   const int P1 = sc->P[0], P2 = sc->P[1], P3 = sc->P[2];
   struct Spec { DevBuf** x; int axis; bool inv; int M; };
   const Spec specs[6] = {{xa, 0, true, P2 * P3}, {xb, 1, true, P3 * P1}, {xa, 2, true, P1 * P2},
@@ -1744,7 +1746,7 @@ static int solve_mixed_dev(mf_solver3d* sc, const double* rhs, double sigma, dou
     return set_error(MF_ERR_UNSUPPORTED, "precision mode %d is not available", prec);
   const bool tf32 = prec == MF_PREC_3XTF32;
   int rc;
-  if ((rc = mixed_prepare(sc, tf32))) return rc;
+  if ((rc = mixed_prepare(sc, tf32, st))) return rc;
   const int n1 = sc->n[0], n2 = sc->n[1], n3 = sc->n[2];
   const long long tot = (long long)n1 * n2 * n3;
   __nv_bfloat16* xh = tf32 ? nullptr : sc->Xa_hi.as<__nv_bfloat16>();
@@ -1855,6 +1857,10 @@ int mf_solver_coeffs_init_3d(const double* g1, const double* g2, const double* g
     }
     sc->n[a] = host[a].n;
     sc->P[a] = sc->ax[a].P;
+  }
+  if (cudaDeviceSynchronize() != cudaSuccess) {  // uploads complete before use on any stream
+    mf_solver3d_destroy(sc);
+    return set_error(MF_ERR_CUDA, "mf_solver_coeffs_init_3d: upload failed");
   }
   *out = sc;
   return MF_OK;
@@ -2183,7 +2189,9 @@ int mf_solver3d_set_eigen(mf_solver3d_t* sc, int axis, const double* eigen, cons
       Vi[(size_t)i * n + j] = ic[i + (size_t)n * j];
     }
   MF_CUDA(cudaDeviceSynchronize());
-  return axis_set_eigen(d, e, V, Vi);
+  if ((rc = axis_set_eigen(d, e, V, Vi))) return rc;
+  MF_CUDA(cudaDeviceSynchronize());  // uploads complete before use on any stream
+  return MF_OK;
 }
 
 int mf_solver3d_set_residual(mf_solver3d_t* sc, int mode) {
@@ -2200,6 +2208,7 @@ int mf_solver3d_device_status(mf_solver3d_t* sc) {
   int herr = 0;
   MF_CUDA(cudaMemcpy(&herr, sc->err.ptr, sizeof(int), cudaMemcpyDeviceToHost));
   MF_CUDA(cudaMemset(sc->err.ptr, 0, sizeof(int)));
+  MF_CUDA(cudaDeviceSynchronize());  // later work on non-blocking streams sees the reset
   if (herr) return set_error(MF_ERR_TIMEOUT, "tensor-core pipeline wait expired");
   return MF_OK;
 }

@@ -126,3 +126,22 @@ def test_four_step_graph_replays_like_eager_steps(mf, gpu):
         for var in VARS:
             assert torch.equal(graphed.field(var, lev), eager.field(var, lev)), (var, lev)
     assert graphed.state() == eager.state()
+
+
+def test_repeat_runs_are_bit_identical(mf, gpu):
+    """Fresh instances (new solver handles, first mixed solves on the forked
+    streams) started from the same state give bit-identical steps: the
+    handles' set-up work is ordered before their first use on any stream."""
+    import torch
+    kw = dict(CASES["defaults"], precision=mf.MF_PREC_SPLIT_BF16, refine=2)
+    runs = []
+    for _ in range(3):
+        _, nav = make_pair(mf, **kw)
+        for _ in range(3):
+            nav.step()
+        torch.cuda.synchronize()
+        runs.append([nav.field(var, lev) for lev in range(N.NT) for var in VARS])
+        nav.close()
+    for other in runs[1:]:
+        for a, b in zip(runs[0], other):
+            assert torch.equal(a, b)
