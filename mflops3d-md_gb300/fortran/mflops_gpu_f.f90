@@ -10,7 +10,10 @@
 !   solver_coeffs_init_3d(g1,g2,g3,sc,n1,n2,n3,bct,so)   class_solver_3d.f90:380
 !   solve_3d(sc,rhs,sigma,solf,bcx,bcy,bcz,n1,n2,n3)     class_solver_3d.f90:83
 ! and adds array-level forms of the class_field pencil drivers
-! (derx..dderz, class_field.f90:629-978) and of solver_3d (:1072).
+! (derx..dderz, class_field.f90:629-978) and of solver_3d (:1072), and the
+! one-domain Navier-Stokes time step of navier3d.f90:48-261
+! (navier_defaults, navier_initialization_gpu, navier_set_field,
+! navier_get_field, navier_step, navier_destroy).
 !
 ! Arrays are passed by address; host arrays are staged by the library and
 ! the call returns when the result is in host memory.  Errors stop the
@@ -36,11 +39,24 @@ module mflops_gpu_f
      integer :: n1 = 0, n2 = 0, n3 = 0
   end type solver_coeffs_3d
 
-  integer(c_int), parameter, public :: MF_PREC_FP64 = 0, MF_PREC_SPLIT_BF16 = 1
+  integer(c_int), parameter, public :: MF_PREC_FP64 = 0, MF_PREC_SPLIT_BF16 = 1, MF_PREC_3XTF32 = 2
+
+  ! mf_navier_params_t (field order and types as in the C header)
+  type, bind(C), public :: navier_params
+     real(c_double) :: ts, reynolds
+     integer(c_int) :: nlt, pt, tou, top, so_solver, so_der, flow_rate, nmodes, precision, refine
+  end type navier_params
+
+  type, public :: navier3d_gpu
+     type(c_ptr) :: h = c_null_ptr
+     integer :: nx = 0, ny = 0, nz = 0
+  end type navier3d_gpu
 
   public :: der_coeffs_init, der, dder, der_s, dder_s, dertype, der_destroy
   public :: derx, dery, derz, dderx, ddery, dderz
   public :: solver_coeffs_init_3d, solve_3d, solve_3d_mixed, solver_3d, solver_destroy
+  public :: navier_defaults, navier_initialization_gpu, navier_set_field, navier_get_field
+  public :: navier_step, navier_destroy
 
   interface
      function c_last_error() bind(C, name="mf_last_error") result(p)
@@ -140,6 +156,49 @@ module mflops_gpu_f
        type(c_ptr), value :: stream
        integer(c_int) :: rc
      end function c_solver_3d
+
+     function c_navier_defaults(p) bind(C, name="mf_navier_defaults") result(rc)
+       import :: c_int, navier_params
+       type(navier_params), intent(out) :: p
+       integer(c_int) :: rc
+     end function c_navier_defaults
+
+     function c_navier_create(gx, nx, gy, ny, gz, nz, p, nav) bind(C, name="mf_navier_create") result(rc)
+       import :: c_double, c_int, c_ptr, navier_params
+       real(c_double), intent(in) :: gx(*), gy(*), gz(*)
+       integer(c_int), value :: nx, ny, nz
+       type(navier_params), intent(in) :: p
+       type(c_ptr), intent(out) :: nav
+       integer(c_int) :: rc
+     end function c_navier_create
+
+     function c_navier_destroy(nav) bind(C, name="mf_navier_destroy") result(rc)
+       import :: c_int, c_ptr
+       type(c_ptr), value :: nav
+       integer(c_int) :: rc
+     end function c_navier_destroy
+
+     function c_navier_set_field(nav, var, level, f, stream) bind(C, name="mf_navier_set_field") result(rc)
+       import :: c_double, c_int, c_ptr
+       type(c_ptr), value :: nav, stream
+       integer(c_int), value :: var, level
+       real(c_double), intent(in) :: f(*)
+       integer(c_int) :: rc
+     end function c_navier_set_field
+
+     function c_navier_get_field(nav, var, level, f, stream) bind(C, name="mf_navier_get_field") result(rc)
+       import :: c_double, c_int, c_ptr
+       type(c_ptr), value :: nav, stream
+       integer(c_int), value :: var, level
+       real(c_double), intent(out) :: f(*)
+       integer(c_int) :: rc
+     end function c_navier_get_field
+
+     function c_navier_step(nav, diag, stream) bind(C, name="mf_navier_step") result(rc)
+       import :: c_int, c_ptr
+       type(c_ptr), value :: nav, diag, stream
+       integer(c_int) :: rc
+     end function c_navier_step
   end interface
 
 contains
@@ -320,5 +379,58 @@ contains
     call check(c_solver_3d(sc%h, g, u, bcx, bcy, bcz, int(size(u,1), c_int), int(size(u,2), c_int), &
          int(size(u,3), c_int), sigma, MF_PREC_FP64, c_null_ptr), 'solver_3d')
   end subroutine solver_3d
+
+  ! ------------------------------------------------------- Navier-Stokes step
+  ! The reference's defaults (command_line.f90:14-35) in p.
+  subroutine navier_defaults(p)
+    type(navier_params), intent(out) :: p
+    call check(c_navier_defaults(p), 'navier_defaults')
+  end subroutine navier_defaults
+
+  ! navier_initialization for one domain (class_navier_3D.f90:2084-2345).
+  subroutine navier_initialization_gpu(gx, gy, gz, nav, p)
+    real(rk), intent(in) :: gx(:), gy(:), gz(:)
+    type(navier3d_gpu), intent(out) :: nav
+    type(navier_params), intent(in) :: p
+    call check(c_navier_create(gx, int(size(gx), c_int), gy, int(size(gy), c_int), gz, int(size(gz), c_int), &
+         p, nav%h), 'navier_initialization_gpu')
+    nav%nx = size(gx)
+    nav%ny = size(gy)
+    nav%nz = size(gz)
+  end subroutine navier_initialization_gpu
+
+  ! var 0..4 = u, v, w, p, phi; level 0 = it(1) ... 3 = it(nt).
+  subroutine navier_set_field(nav, var, level, f)
+    type(navier3d_gpu), intent(in) :: nav
+    integer, intent(in) :: var, level
+    real(rk), intent(in) :: f(:,:,:)
+    call check(c_navier_set_field(nav%h, int(var, c_int), int(level, c_int), f, c_null_ptr), 'navier_set_field')
+  end subroutine navier_set_field
+
+  subroutine navier_get_field(nav, var, level, f)
+    type(navier3d_gpu), intent(in) :: nav
+    integer, intent(in) :: var, level
+    real(rk), intent(out) :: f(:,:,:)
+    call check(c_navier_get_field(nav%h, int(var, c_int), int(level, c_int), f, c_null_ptr), 'navier_get_field')
+  end subroutine navier_get_field
+
+  ! One iteration of the time loop (navier3d.f90:48-261); diag receives the
+  ! driver's printed numbers (div V, V and P errors, kinetic energy,
+  ! stationarity).
+  subroutine navier_step(nav, diag)
+    type(navier3d_gpu), intent(in) :: nav
+    real(rk), intent(out), target, optional :: diag(12)
+    if (present(diag)) then
+       call check(c_navier_step(nav%h, c_loc(diag), c_null_ptr), 'navier_step')
+    else
+       call check(c_navier_step(nav%h, c_null_ptr, c_null_ptr), 'navier_step')
+    endif
+  end subroutine navier_step
+
+  subroutine navier_destroy(nav)
+    type(navier3d_gpu), intent(inout) :: nav
+    call check(c_navier_destroy(nav%h), 'navier_destroy')
+    nav%h = c_null_ptr
+  end subroutine navier_destroy
 
 end module mflops_gpu_f
