@@ -466,8 +466,9 @@ int mf_flow_curl(int nx, int ny, int nz, const double* const* dpsi, double* cons
  * (:695-791), velocity Helmholtz solves (:1597-1761), pressure-increment
  * Poisson solve (:1764-1845, 342-393), projection (:1847-1959),
  * extrapolation (:2010-2050), slot rotation and the driver's diagnostics
- * (navier3d.f90:120-261).  Covered: mpid%dims = 0 (one domain), mapt = 0,
- * nsubite = 1, les_type = 0, pressure types 1 and 2.  Velocity Dirichlet and
+ * (navier3d.f90:120-261) and the LES term (navier_LES :1225-1455, f :1083-1099).
+ * Covered: mpid%dims = 0 (one domain), mapt = 0, nsubite = 1, pressure types
+ * 1 and 2, les_type 0..3.  Velocity Dirichlet and
  * pressure Neumann on all faces; boundary values and sources from the
  * reference's exact solution `sol` (:927-1041, steady: wt = 0).  Fields are
  * (nx,ny,nz) FP64 device arrays, x fastest.
@@ -486,6 +487,8 @@ typedef struct {
   int nmodes;         /* modes of the exact solution (5 in the reference) */
   int precision;      /* solves: MF_PREC_FP64 (the reference's arithmetic) or a mixed mode */
   int refine;         /* refinement steps of the mixed solves, < 0: default */
+  int les_type;       /* 0 none, 1 Smagorinsky, 2 WALE, 3 sigma (default 0) */
+  double les_c;       /* cmd%les_c; the model coefficient is its square (default 0) */
 } mf_navier_params_t;
 /* Fills the reference's defaults (command_line.f90:14-35). */
 int mf_navier_defaults(mf_navier_params_t* p);

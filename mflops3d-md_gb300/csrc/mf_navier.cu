@@ -1,7 +1,7 @@
 // Navier-Stokes time step on one domain: the caller of the derivative and
 // solver entry points, src/main/navier3d.f90:48-274 built from
 // src/class_navier/class_navier_3D.f90 (one domain, mapt = 0, nsubite = 1,
-// les_type = 0, pressure types 1 and 2).
+// pressure types 1 and 2, les_type 0..3).
 //
 // Time levels: nt = 4 slots per variable (u, v, w, p, phi) addressed through
 // the permutation it(1..nt) of the reference (it(1) = the slot a step
@@ -19,7 +19,9 @@
 // Stages per step (device work only, on the caller's stream):
 //   flow-rate term   weighted sum of extrapol(u) (k_ns_wsum) -> k_ns_flow
 //   presolve         k_ns_advect / k_ns_products / k_ns_skew (newest slot,
-//                    eighteen sweeps in two launches) + k_ns_presolve
+//                    eighteen sweeps in two launches); with LES, the nine
+//                    velocity gradients, the viscosity (k_les_nu) and the
+//                    nine sweeps of nu (du_ij + du_ji); k_ns_presolve
 //   boundary values  k_ns_bc_velocity (+ gradient of extrapol(phi), pt = 1)
 //   velocity solves  k_ns_fu (interior rhs) + three Helmholtz solves, u on
 //                    the caller's stream, v and w on forked streams
@@ -251,11 +253,27 @@ __global__ void k_ns_skew(long long n, const double* __restrict__ E, double* __r
   o[q] = t;
 }
 
+// LES stress products (class_navier_3D.f90:1090-1094):
+// P + (3 j + i) n = nu (du_ij + du_ji), du_ij at D + (3 j + i) n.
+__global__ void k_ns_les_products(long long n, const double* __restrict__ nu, const double* __restrict__ D,
+                                  double* __restrict__ P) {
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const double v = nu[q];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) P[(3 * j + i) * n + q] = v * (D[(3 * j + i) * n + q] + D[(3 * i + j) * n + q]);
+}
+
 // navier_presolve_{u,v,w} (class_navier_3D.f90:1528-1595):
 // rhs = zero_edges(f - zero_edges(extrapol(nonlinear))) with f the exact
-// source (src, null for w) plus the flow-rate term g (u only, *g).
+// source (src, null for w), minus the LES term les_f = -sum_j E_j (E: the
+// three sweeps of component c, E + j n3 with n3 = 3 n, null without LES),
+// plus the flow-rate term g (u only, *g).
 __global__ void k_ns_presolve(Lin L, int nx, int ny, int nz, const double* __restrict__ src,
-                              const double* __restrict__ g, double* __restrict__ rhs) {
+                              const double* __restrict__ E, const double* __restrict__ g,
+                              double* __restrict__ rhs) {
   const long long n = (long long)nx * ny * nz;
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= n) return;
@@ -266,6 +284,13 @@ __global__ void k_ns_presolve(Lin L, int nx, int ny, int nz, const double* __res
     return;
   }
   double f = src ? src[q] : 0.0;
+  if (E) {
+    double lf = 0.0;
+    lf = lf - E[q];
+    lf = lf - E[3 * n + q];
+    lf = lf - E[6 * n + q];
+    f = f - lf;
+  }
   if (g) f = f + g[0];
   rhs[q] = f - lin_at(L, q);
 }
@@ -516,6 +541,8 @@ struct mf_navier {
   // velocity solver sets scu, scv, scw (as the reference keeps them) and the
   // pressure set; the three velocity solves run on forked streams
   mf_solver3d_t *scu = nullptr, *scv = nullptr, *scw = nullptr, *scp = nullptr;
+  mf_les_t* les = nullptr;  // les_type != 0
+  DevBuf nu;                // eddy viscosity of the step
   cudaStream_t side[2] = {nullptr, nullptr};
   cudaEvent_t fork = nullptr, join[2] = {nullptr, nullptr};
   DevBuf fields;  // [5 vars][kNt slots] fields
@@ -702,11 +729,29 @@ int ns_step(mf_navier* nv, cudaStream_t st) {
     if ((rc = launch_check("k_ns_flow"))) return rc;
     g = nv->state.as<double>();
   }
+  // navier_LES on the newest level and the stress sweeps of f
+  if (P.les_type != 0) {
+    Sweeps S;
+    for (int j = 0; j < 3; ++j)
+      for (int i = 0; i < 3; ++i) S.add(nv, j, nv->F(i, s0), nv->T(3 * j + i));
+    if ((rc = S.run(nv, st))) return rc;
+    const double* du[9];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) du[3 * i + j] = nv->T(3 * j + i);
+    if ((rc = mf_les_nu(nv->les, P.les_type, P.les_c * P.les_c, du, nv->nu.as<double>(), st))) return rc;
+    k_ns_les_products<<<gb, kNsThreads, 0, st>>>(nv->np, nv->nu.as<double>(), nv->T(0), nv->T(9));
+    if ((rc = launch_check("k_ns_les_products"))) return rc;
+    Sweeps E;
+    for (int j = 0; j < 3; ++j)
+      for (int i = 0; i < 3; ++i) E.add(nv, j, nv->T(9 + 3 * j + i), nv->T(3 * j + i));
+    if ((rc = E.run(nv, st))) return rc;
+  }
   nv->rhs_cur ^= 1;  // rhs(2) = rhs(1): the other buffer keeps the previous step's
   for (int c = 0; c < 3; ++c) {
     const double* src = c == 0 ? nv->EX(3) : c == 1 ? nv->EX(4) : nullptr;
     k_ns_presolve<<<gb, kNsThreads, 0, st>>>(extrapol_of(nv, P.tou, nl_ptr, c), nv->nx, nv->ny, nv->nz, src,
-                                             c == 0 ? g : nullptr, nv->RHS(c, nv->rhs_cur));
+                                             P.les_type != 0 ? nv->T(c) : nullptr, c == 0 ? g : nullptr,
+                                             nv->RHS(c, nv->rhs_cur));
     if ((rc = launch_check("k_ns_presolve"))) return rc;
   }
   // velocity boundary values (+ gradient of extrapol(phi) for pt = 1)
@@ -867,6 +912,8 @@ int mf_navier_defaults(mf_navier_params_t* p) {
   p->nmodes = 5;
   p->precision = MF_PREC_FP64;
   p->refine = -1;
+  p->les_type = 0;
+  p->les_c = 0.0;
   return MF_OK;
 }
 
@@ -879,6 +926,8 @@ int mf_navier_destroy(mf_navier_t* nv) {
   mf_solver3d_destroy(nv->scv);
   mf_solver3d_destroy(nv->scw);
   mf_solver3d_destroy(nv->scp);
+  mf_les_destroy(nv->les);
+  nv->nu.release();
   for (int q = 0; q < 2; ++q) {
     if (nv->side[q]) cudaStreamDestroy(nv->side[q]);
     if (nv->join[q]) cudaEventDestroy(nv->join[q]);
@@ -897,7 +946,7 @@ int mf_navier_create(const double* gx, int nx, const double* gy, int ny, const d
   *out = nullptr;
   if (nx < 9 || ny < 9 || nz < 9) return set_error(MF_ERR_ARG, "mf_navier_create: at least 9 nodes per axis");
   if (!(p->ts > 0.0) || !(p->reynolds > 0.0) || p->nlt < 0 || p->nlt > 2 || (p->pt != 1 && p->pt != 2) ||
-      p->tou < 1 || p->tou > 3 || p->nmodes < 0)
+      p->tou < 1 || p->tou > 3 || p->nmodes < 0 || p->les_type < 0 || p->les_type > 3)
     return set_error(MF_ERR_ARG, "mf_navier_create: bad parameters (ts, reynolds > 0; nlt 0..2; pt 1, 2; tou 1..3)");
   if (p->precision != MF_PREC_FP64 && p->precision != MF_PREC_SPLIT_BF16 && p->precision != MF_PREC_3XTF32)
     return set_error(MF_ERR_ARG, "mf_navier_create: unknown precision %d", p->precision);
@@ -935,6 +984,9 @@ int mf_navier_create(const double* gx, int nx, const double* gy, int ny, const d
       (rc = mf_solver_coeffs_init_3d(gx, gy, gz, nx, ny, nz, bctu, p->so_solver, &nv->scv)) ||
       (rc = mf_solver_coeffs_init_3d(gx, gy, gz, nx, ny, nz, bctu, p->so_solver, &nv->scw)) ||
       (rc = mf_solver_coeffs_init_3d(gx, gy, gz, nx, ny, nz, bctp, p->so_solver, &nv->scp)))
+    return fail(rc);
+  if (p->les_type != 0 &&
+      ((rc = mf_les_create(gx, nx, gy, ny, gz, nz, &nv->les)) || (rc = nv->nu.ensure(fb))))
     return fail(rc);
   if ((rc = nv->fields.ensure(fb * 5 * kNt)) || (rc = nv->nl.ensure(fb * 3 * kNt)) ||
       (rc = nv->rhs.ensure(fb * 6)) || (rc = nv->rp.ensure(fb * 3)) || (rc = nv->tmp.ensure(fb * 18)) ||

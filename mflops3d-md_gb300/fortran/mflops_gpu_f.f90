@@ -45,6 +45,8 @@ module mflops_gpu_f
   type, bind(C), public :: navier_params
      real(c_double) :: ts, reynolds
      integer(c_int) :: nlt, pt, tou, top, so_solver, so_der, flow_rate, nmodes, precision, refine
+     integer(c_int) :: les_type
+     real(c_double) :: les_c
   end type navier_params
 
   type, public :: navier3d_gpu

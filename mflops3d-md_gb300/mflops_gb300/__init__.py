@@ -941,7 +941,8 @@ class NavierParams(ctypes.Structure):
     _fields_ = [("ts", ctypes.c_double), ("reynolds", ctypes.c_double), ("nlt", ctypes.c_int),
                 ("pt", ctypes.c_int), ("tou", ctypes.c_int), ("top", ctypes.c_int),
                 ("so_solver", ctypes.c_int), ("so_der", ctypes.c_int), ("flow_rate", ctypes.c_int),
-                ("nmodes", ctypes.c_int), ("precision", ctypes.c_int), ("refine", ctypes.c_int)]
+                ("nmodes", ctypes.c_int), ("precision", ctypes.c_int), ("refine", ctypes.c_int),
+                ("les_type", ctypes.c_int), ("les_c", ctypes.c_double)]
 
 
 NAVIER_VARS = {"u": 0, "v": 1, "w": 2, "p": 3, "phi": 4}
@@ -951,9 +952,9 @@ NAVIER_DIAG = ("div", "vel_err", "vel_rel", "vel_acc", "pres_err", "pres_rel", "
 
 class NavierStokes3D:
     """One-domain time integration of navier3d (mpid%dims = 0, mapt = 0,
-    nsubite = 1, les_type = 0, pt 1 or 2) on host grids.  Keyword arguments
+    nsubite = 1, pt 1 or 2, les_type 0..3) on host grids.  Keyword arguments
     override the reference's defaults (ts, reynolds, nlt, pt, tou, top,
-    so_solver, so_der, flow_rate, nmodes, precision, refine)."""
+    so_solver, so_der, flow_rate, nmodes, precision, refine, les_type, les_c)."""
 
     def __init__(self, gx, gy, gz, **kw):
         prm = NavierParams()

@@ -15,7 +15,7 @@ src/class_navier/class_navier_3D.f90:
   from the exact solution ``sol`` (:395-433, 848-925, 927-1041),
   ``navier_presolve_{u,v,w}`` (:1528-1595) with ``navier_nonlinear``
   (:1169-1222, nlt = 0, 1, 2) and the forcing ``f`` (:1043-1167, the
-  exact-solution source plus the flow-rate term for u, les_type = 0),
+  exact-solution source, the LES term and the flow-rate term for u),
   ``add_boundary_gradient`` for pt = 1 (:695-791), ``navier_solve_{u,v,w}``
   (:1597-1761, pt = 1, 2), ``navier_presolve_phi`` / ``navier_phi_rhs``
   (:1764-1785, 1961-2007), ``navier_solve_phi`` with
@@ -27,13 +27,17 @@ src/class_navier/class_navier_3D.f90:
   level it(nt) and remove the weighted mean of its pressure, as the driver
   does.
 
-``navier_LES`` with les_type = 0 computes the velocity gradients and a zero
-viscosity that nothing reads; it is left out.  The 1e-10 of the flow-rate
-term is a default-kind (single precision) literal.
+``navier_LES`` (:1225-1455) runs before the presolve: the nine gradients of
+the newest velocity level (edges zeroed) and, for les_type 1, 2, 3, the eddy
+viscosity of oracle.les with the coefficient les_c**2 (:2138); the forcing
+then subtracts les_f = -sum_j d/dx_j (nu (du_ij + du_ji)) (:1083-1099) before
+the flow-rate term.  The 1e-10 of the flow-rate term is a default-kind
+(single precision) literal.
 """
 import numpy as np
 
 from oracle import derivatives as D
+from oracle import les as L
 from oracle import solver as S
 from oracle.les import zero_edges
 
@@ -114,7 +118,7 @@ class Navier:
     """Single-domain state and time step; fields are (nx, ny, nz) arrays."""
 
     def __init__(self, gx, gy, gz, ts, rey, nlt=2, pt=1, tou=2, top=2, so=(6, 6), flow_rate=True,
-                 nmodes=NMODES):
+                 nmodes=NMODES, les_type=0, les_c=0.0):
         if pt not in (1, 2):
             raise ValueError("pressure types 1 and 2 are restated")
         self.gx, self.gy, self.gz = (np.asarray(g, float) for g in (gx, gy, gz))
@@ -123,6 +127,9 @@ class Navier:
         self.nlt, self.pt, self.tou, self.top = nlt, pt, tou, top
         self.flow_rate = flow_rate
         self.nmodes = nmodes
+        self.les_type, self.les_c = les_type, float(les_c)
+        self.du = None
+        self.les_nu = None
         self.fac = bdf_factors(tou, ts)
         self.sigmau = -self.rey * self.fac[0]
         self.sigmap = 0.0
@@ -197,9 +204,11 @@ class Navier:
         return self.extrapol(tmp, "v")
 
     def forcing(self, c):
-        """f(nav,mpid,'rhs'//c) with les_type = 0."""
+        """f(nav,mpid,'rhs'//c)."""
         X, Y, Z = self.points()
         F = sol(X, Y, Z, self.time, "rhs" + c, self.rey, self.nmodes)
+        if self.les_type:
+            F = F - self.les_forcing(c)
         if c == "u" and self.flow_rate:
             reft = self.integrale(np.ones_like(F))
             err = self.integrale(self.extrapol(self.u, "v")) / reft
@@ -212,6 +221,16 @@ class Navier:
             self.g = self.g - err * self.fac[0]
             F = F + self.g
         return F
+
+    def les_forcing(self, c):
+        """les_f of f() for component c (class_navier_3D.f90:1083-1099)."""
+        i = "uvw".index(c)
+        grads = (self.derx, self.dery, self.derz)
+        lf = np.zeros((self.nx, self.ny, self.nz))
+        for j in range(3):
+            aux = self.les_nu * (self.du[i][j] + self.du[j][i])
+            lf = lf - grads[j](aux)
+        return lf
 
     def bc_exact(self, c):
         """navier_bc_velocity_utils: face values of sol (interior tangential points)."""
@@ -229,6 +248,11 @@ class Navier:
         self.time += self.ts
         bc = {c: self.bc_exact(c) for c in "uvw"}
         levels = {"u": self.u, "v": self.v, "w": self.w}
+        if self.les_type:  # navier_LES on the newest level
+            grads = (self.derx, self.dery, self.derz)
+            vel = (self.u[n0], self.v[n0], self.w[n0])
+            self.du = [[zero_edges(grads[j](vel[i])) for j in range(3)] for i in range(3)]
+            self.les_nu = L.les_nu(self.du, self.gx, self.gy, self.gz, self.les_type, self.les_c ** 2)
         # presolve u, v, w
         for c in "uvw":
             self.rhs[c][1] = self.rhs[c][0]

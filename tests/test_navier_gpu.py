@@ -2,8 +2,9 @@
 restatement of navier3d.f90 / class_navier_3D.f90: every field of every time
 level and the driver's diagnostics after each of six steps (more than one
 rotation of the nt = 4 slots, so the cached nonlinear terms are exercised),
-for the reference's defaults and for other scheme options; the mixed-precision
-solves; a CUDA-graph capture of four steps replayed bit-identically."""
+for the reference's defaults, other scheme options and the three LES models;
+the mixed-precision solves; a CUDA-graph capture of four steps replayed
+bit-identically."""
 import numpy as np
 import pytest
 
@@ -34,7 +35,7 @@ def initial_levels(nav, seed, nmodes):
 
 def make_pair(mf, seed=3, **kw):
     gx, gy, gz = grids()
-    okw = {k: kw[k] for k in ("nlt", "pt", "tou", "top", "flow_rate", "nmodes") if k in kw}
+    okw = {k: kw[k] for k in ("nlt", "pt", "tou", "top", "flow_rate", "nmodes", "les_type", "les_c") if k in kw}
     ora = N.Navier(gx, gy, gz, ts=kw["ts"], rey=kw["reynolds"], **okw)
     initial_levels(ora, seed, okw.get("nmodes", N.NMODES))
     gpu = mf.NavierStokes3D(gx, gy, gz, **kw)
@@ -64,6 +65,11 @@ CASES = {
     "defaults": dict(ts=1e-2, reynolds=50.0),
     "pt2_bdf3_advective": dict(ts=5e-3, reynolds=20.0, pt=2, tou=3, top=3, nlt=1, flow_rate=0),
     "pt1_euler_no_advection": dict(ts=2e-2, reynolds=5.0, pt=1, tou=1, top=1, nlt=0, nmodes=1),
+    # LES cases: parameters for which the explicit LES term stays stable on
+    # these coarse noisy fields (a blowing-up run amplifies rounding)
+    "les_smagorinsky": dict(ts=2e-3, reynolds=100.0, les_type=1, les_c=0.17),
+    "les_wale_pt2": dict(ts=5e-3, reynolds=500.0, pt=2, les_type=2, les_c=0.5),
+    "les_sigma": dict(ts=1e-2, reynolds=100.0, les_type=3, les_c=0.5),
 }
 
 
@@ -71,18 +77,21 @@ CASES = {
 def test_steps_match_the_oracle(mf, gpu, name):
     kw = CASES[name]
     ora, nav = make_pair(mf, **kw)
+    # the sigma model's acos amplifies rounding near coincident singular
+    # values (1e-10 bound on the viscosity itself, tests/test_les.py)
+    tol = 1e-9 if kw.get("les_type") == 3 else 1e-10
     for step in range(6):
         d_ref = ora.advance(diagnostics=True)
         d = nav.step(diagnostics=True)
-        worst = compare(mf, ora, nav, 1e-10)
-        assert d["div"] == pytest.approx(d_ref["div"], rel=1e-9)
+        worst = compare(mf, ora, nav, tol)
+        assert d["div"] == pytest.approx(d_ref["div"], rel=10 * tol)
         for key, pos in (("vel", 0), ("pres", 0)):
-            assert d[key + "_err"] == pytest.approx(d_ref[key][pos], rel=1e-9), (step, key)
-        assert d["vel_acc"] == pytest.approx(d_ref["vel"][2], rel=1e-9)
-        assert d["pres_acc"] == pytest.approx(d_ref["pres"][2], rel=1e-9)
-        assert d["kinetic"] == pytest.approx(d_ref["kinetic"], rel=1e-9)
-        assert d["station_p"] == pytest.approx(d_ref["station_p"][0], rel=1e-9)
-        assert d["station_v"] == pytest.approx(d_ref["station_v"][0], rel=1e-9)
+            assert d[key + "_err"] == pytest.approx(d_ref[key][pos], rel=10 * tol), (step, key)
+        assert d["vel_acc"] == pytest.approx(d_ref["vel"][2], rel=10 * tol)
+        assert d["pres_acc"] == pytest.approx(d_ref["pres"][2], rel=10 * tol)
+        assert d["kinetic"] == pytest.approx(d_ref["kinetic"], rel=10 * tol)
+        assert d["station_p"] == pytest.approx(d_ref["station_p"][0], rel=10 * tol)
+        assert d["station_v"] == pytest.approx(d_ref["station_v"][0], rel=10 * tol)
     st = nav.state()
     assert st["time"] == pytest.approx(ora.time, rel=1e-15)
     if kw.get("flow_rate", 1):

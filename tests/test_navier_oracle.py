@@ -88,3 +88,6 @@ def test_navier_create_rejects_bad_parameters(mf):
     assert mf._lib.mf_navier_defaults(ctypes.byref(prm)) == 0
     assert (prm.nlt, prm.pt, prm.tou, prm.top, prm.so_solver, prm.so_der, prm.nmodes) == (2, 1, 2, 2, 6, 6, 5)
     assert prm.ts == 1.0 and prm.reynolds == 1.0 and prm.flow_rate == 1
+    assert prm.les_type == 0 and prm.les_c == 0.0
+    with pytest.raises(mf.MflopsError):
+        mf.NavierStokes3D(g, g, g, les_type=4)
