@@ -468,7 +468,7 @@ int mf_flow_curl(int nx, int ny, int nz, const double* const* dpsi, double* cons
  * extrapolation (:2010-2050), slot rotation and the driver's diagnostics
  * (navier3d.f90:120-261) and the LES term (navier_LES :1225-1455, f :1083-1099).
  * Covered: mpid%dims = 0 (one domain), mapt = 0, nsubite = 1, pressure types
- * 1 and 2, les_type 0..3.  Velocity Dirichlet and
+ * 1 to 4, les_type 0..3.  Velocity Dirichlet and
  * pressure Neumann on all faces; boundary values and sources from the
  * reference's exact solution `sol` (:927-1041, steady: wt = 0).  Fields are
  * (nx,ny,nz) FP64 device arrays, x fastest.
@@ -478,7 +478,7 @@ typedef struct {
   double ts;          /* time step (cmd%ts) */
   double reynolds;    /* cmd%reynolds */
   int nlt;            /* nonlinear form: 0 none, 1 advective, 2 skew-symmetric (reference default 2) */
-  int pt;             /* pressure type 1 or 2 (default 1) */
+  int pt;             /* pressure type 1..4 (default 1) */
   int tou;            /* BDF order 1, 2, 3 of the velocity (default 2) */
   int top;            /* pressure extrapolation order + 1 (default 2) */
   int so_solver;      /* so(1), default 6 */

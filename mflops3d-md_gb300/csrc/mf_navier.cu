@@ -1,7 +1,7 @@
 // Navier-Stokes time step on one domain: the caller of the derivative and
 // solver entry points, src/main/navier3d.f90:48-274 built from
 // src/class_navier/class_navier_3D.f90 (one domain, mapt = 0, nsubite = 1,
-// pressure types 1 and 2, les_type 0..3).
+// pressure types 1 to 4, les_type 0..3).
 //
 // Time levels: nt = 4 slots per variable (u, v, w, p, phi) addressed through
 // the permutation it(1..nt) of the reference (it(1) = the slot a step
@@ -24,9 +24,12 @@
 //                    nine sweeps of nu (du_ij + du_ji); k_ns_presolve
 //   boundary values  k_ns_bc_velocity (+ gradient of extrapol(phi), pt = 1)
 //   velocity solves  k_ns_fu (interior rhs) + three Helmholtz solves, u on
-//                    the caller's stream, v and w on forked streams
-//   pressure         k_ns_scale, div of rhs_p, k_ns_fphi, k_ns_bc_phi, one
-//                    all-Neumann Poisson solve at sigma = 0
+//                    the caller's stream, v and w on forked streams (before
+//                    the pressure for pt 1, 2; after the projection, with the
+//                    new pressure gradient, for pt 3, 4)
+//   pressure         k_ns_scale / k_ns_phi_rhs, div of rhs_p, k_ns_fphi,
+//                    k_ns_bc_phi (+ k_ns_rot_sums, k_ns_bc_rotrot for pt 3),
+//                    one all-Neumann Poisson solve at sigma = 0
 //   projection       k_ns_pressure, k_ns_velocity
 // Pointwise kernels fuse the edge zeroing of field_zero_edges
 // (class_field.f90:366-391) into their stores.
@@ -328,6 +331,61 @@ __global__ void k_ns_scale(int nx, int ny, int nz, double s, const double* __res
   out[q] = on_edge(i, j, k, nx, ny, nz) ? 0.0 : s * x[q];
 }
 
+// navier_phi_rhs for pt = 3, 4 with subite = 1 (class_navier_3D.f90:1983-2003):
+// pt 3: f1 - fac2 x(it(nt)) - fac3 x(it(nt-1)) - fac4 x(it(nt-2));
+// pt 4: that - f2 + fac1 x(it(nt)) + fac2 x(it(nt-1)) + fac3 x(it(nt-2)) + fac4 x(it(1));
+// edges zeroed.  f1, f2 = rhs(1), rhs(2) of the component.
+__global__ void k_ns_phi_rhs(int nx, int ny, int nz, int pt, const double* __restrict__ f1,
+                             const double* __restrict__ f2, const double* __restrict__ x0,
+                             const double* __restrict__ x1, const double* __restrict__ x2,
+                             const double* __restrict__ x3, double fa, double fb, double fc, double fd,
+                             double* __restrict__ out) {
+  const long long n = (long long)nx * ny * nz;
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  int i, j, k;
+  idx3(q, nx, ny, i, j, k);
+  if (on_edge(i, j, k, nx, ny, nz)) {
+    out[q] = 0.0;
+    return;
+  }
+  double t = f1[q] - fb * x0[q] - fc * x1[q] - fd * x2[q];
+  if (pt == 4) t = t - f2[q] + fa * x0[q] + fb * x1[q] + fc * x2[q] + fd * x3[q];
+  out[q] = t;
+}
+
+// add_boundary_rotrot, first half (class_navier_3D.f90:819-840): with
+// A = d eu/dx, B = d ev/dy, C = d ew/dz of the extrapolated velocity,
+// ax = B + C, ay = A + C, az = A + B.
+__global__ void k_ns_rot_sums(long long n, const double* __restrict__ A, const double* __restrict__ B,
+                              const double* __restrict__ C, double* __restrict__ ax, double* __restrict__ ay,
+                              double* __restrict__ az) {
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  ax[q] = B[q] + C[q];
+  ay[q] = A[q] + C[q];
+  az[q] = A[q] + B[q];
+}
+
+// add_boundary_rotrot, second half: on the faces normal to axis a,
+// bcphi -= (d(a_a)/dx_a - dd1 - dd2) / Re with d[a] = d(a_a)/dx_a and
+// dd[2a], dd[2a+1] the two second derivatives of that face's normal velocity
+// component (x: u_yy, u_zz; y: v_xx, v_zz; z: w_xx, w_yy).
+struct RotRot {
+  const double* d[3];
+  const double* dd[6];
+};
+__global__ void k_ns_bc_rotrot(Faces F, RotRot R, double rey, double* __restrict__ bcphi) {
+  const long long tot = F.total();
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= tot) return;
+  int a, i, j, k;
+  F.point(q, a, i, j, k);
+  const long long g = i + (long long)F.nx * (j + (long long)F.ny * k);
+  const double aux = R.d[a][g] - R.dd[2 * a][g] - R.dd[2 * a + 1][g];
+  bcphi[q] = bcphi[q] - aux / rey;
+}
+
 // navier_solve_phi right-hand side at the interior points
 // (class_navier_3D.f90:1808-1813): sigmap extrapol(phi) + d rhs_px/dx +
 // d rhs_py/dy + d rhs_pz/dz.
@@ -357,7 +415,8 @@ __global__ void k_ns_zero_edges(int nx, int ny, int nz, double* __restrict__ f) 
 }
 
 // navier_projection, pressure (class_navier_3D.f90:1878-1896):
-// p = zero_edges(zero_edges(phi [+ aux]) - (div_x + div_y + div_z) / Re).
+// p = zero_edges(zero_edges(phi [+ aux]) [- (div_x + div_y + div_z) / Re])
+// (no divergence term when ddx is null: pt = 3).
 __global__ void k_ns_pressure(int nx, int ny, int nz, const double* __restrict__ phi,
                               const double* __restrict__ aux, const double* __restrict__ ddx,
                               const double* __restrict__ ddy, const double* __restrict__ ddz, double rey,
@@ -373,8 +432,8 @@ __global__ void k_ns_pressure(int nx, int ny, int nz, const double* __restrict__
   }
   double v = phi[q];
   if (aux) v = v + aux[q];
-  const double div = (ddx[q] + ddy[q] + ddz[q]) / rey;
-  p[q] = v - div;
+  if (ddx) v = v - (ddx[q] + ddy[q] + ddz[q]) / rey;
+  p[q] = v;
 }
 
 // navier_projection, velocity (:1943-1949): x = zero_edges((rhs_p - dphi) / fac(1)).
@@ -623,10 +682,10 @@ struct Sweeps {
   int axis[9], order[9];
   const double* f[9];
   double* df[9];
-  void add(const mf_navier* nv, int ax, const double* in, double* out) {
+  void add(const mf_navier* nv, int ax, const double* in, double* out, int ord = 1) {
     dc[n] = ax == 0 ? nv->dcx : ax == 1 ? nv->dcy : nv->dcz;
     axis[n] = ax;
-    order[n] = 1;
+    order[n] = ord;
     f[n] = in;
     df[n] = out;
     ++n;
@@ -766,36 +825,48 @@ int ns_step(mf_navier* nv, cudaStream_t st) {
                                                 fac1, nv->bc.as<double>());
   }
   if ((rc = launch_check("k_ns_bc_velocity"))) return rc;
-  // velocity Helmholtz solves (pt = 2: + gradient of extrapol(p))
+  const unsigned ib = ns_blocks(nv->nin);
+  // navier_solve_{u,v,w}: the three Helmholtz solves, u on the caller's
+  // stream, v and w on forked streams joined back; grad (or null) is the base
+  // of the three pressure-gradient fields added to the right-hand sides
+  auto velocity_solves = [&](const double* grad) -> int {
+    int r;
+    MF_CUDA(cudaEventRecord(nv->fork, st));
+    for (int q = 0; q < 2; ++q) MF_CUDA(cudaStreamWaitEvent(nv->side[q], nv->fork, 0));
+    mf_solver3d_t* sets[3] = {nv->scu, nv->scv, nv->scw};
+    for (int c = 0; c < 3; ++c) {
+      cudaStream_t sc = c == 0 ? st : nv->side[c - 1];
+      double* rhs = nv->fin.as<double>() + (size_t)c * nv->nin;
+      k_ns_fu<<<ib, kNsThreads, 0, sc>>>(nv->nx, nv->ny, nv->nz, nv->F(c, s0), nv->F(c, s1),
+                                         P.tou == 3 ? nv->F(c, s2) : nullptr, nv->fac[1], nv->fac[2], nv->fac[3],
+                                         grad ? grad + (size_t)c * nv->np : nullptr, nv->RHS(c, nv->rhs_cur),
+                                         P.reynolds, rhs);
+      if ((r = launch_check("k_ns_fu")) || (r = solve(nv, sets[c], rhs, nv->sigmau, nv->F(c, nw), nv->BC(c), sc)))
+        return r;
+    }
+    for (int q = 0; q < 2; ++q) {
+      MF_CUDA(cudaEventRecord(nv->join[q], nv->side[q]));
+      MF_CUDA(cudaStreamWaitEvent(st, nv->join[q], 0));
+    }
+    return MF_OK;
+  };
+  // pt = 1, 2: velocity before the pressure (pt = 2: + gradient of extrapol(p))
   if (P.pt == 2) {
     if ((rc = extrapol_into(nv, extrapol_of(nv, P.top - 1, field_ptr, kVarP), nv->T(0), st)) ||
         (rc = gradient(nv, nv->T(0), nv->T(1), nv->T(2), nv->T(3), st)))
       return rc;
   }
-  const unsigned ib = ns_blocks(nv->nin);
-  // the three Helmholtz solves: u on the caller's stream, v and w on forked
-  // streams joined back before the pressure stage
-  MF_CUDA(cudaEventRecord(nv->fork, st));
-  for (int q = 0; q < 2; ++q) MF_CUDA(cudaStreamWaitEvent(nv->side[q], nv->fork, 0));
-  mf_solver3d_t* sets[3] = {nv->scu, nv->scv, nv->scw};
+  if (P.pt <= 2 && (rc = velocity_solves(P.pt == 2 ? nv->T(1) : nullptr))) return rc;
+  // pressure increment: rhs_p (navier_phi_rhs), Poisson solve with Neumann data
   for (int c = 0; c < 3; ++c) {
-    cudaStream_t sc = c == 0 ? st : nv->side[c - 1];
-    double* rhs = nv->fin.as<double>() + (size_t)c * nv->nin;
-    k_ns_fu<<<ib, kNsThreads, 0, sc>>>(nv->nx, nv->ny, nv->nz, nv->F(c, s0), nv->F(c, s1),
-                                       P.tou == 3 ? nv->F(c, s2) : nullptr, nv->fac[1], nv->fac[2], nv->fac[3],
-                                       P.pt == 2 ? nv->T(1 + c) : nullptr, nv->RHS(c, nv->rhs_cur),
-                                       P.reynolds, rhs);
-    if ((rc = launch_check("k_ns_fu")) || (rc = solve(nv, sets[c], rhs, nv->sigmau, nv->F(c, nw), nv->BC(c), sc)))
-      return rc;
-  }
-  for (int q = 0; q < 2; ++q) {
-    MF_CUDA(cudaEventRecord(nv->join[q], nv->side[q]));
-    MF_CUDA(cudaStreamWaitEvent(st, nv->join[q], 0));
-  }
-  // pressure increment: rhs_p = fac(1) u*, Poisson solve with Neumann data
-  for (int c = 0; c < 3; ++c) {
-    k_ns_scale<<<gb, kNsThreads, 0, st>>>(nv->nx, nv->ny, nv->nz, fac1, nv->F(c, nw), nv->RP(c));
-    if ((rc = launch_check("k_ns_scale"))) return rc;
+    if (P.pt <= 2)
+      k_ns_scale<<<gb, kNsThreads, 0, st>>>(nv->nx, nv->ny, nv->nz, fac1, nv->F(c, nw), nv->RP(c));
+    else
+      k_ns_phi_rhs<<<gb, kNsThreads, 0, st>>>(nv->nx, nv->ny, nv->nz, P.pt, nv->RHS(c, nv->rhs_cur),
+                                              nv->RHS(c, nv->rhs_cur ^ 1), nv->F(c, s0), nv->F(c, s1),
+                                              nv->F(c, s2), nv->F(c, nw), nv->fac[0], nv->fac[1], nv->fac[2],
+                                              nv->fac[3], nv->RP(c));
+    if ((rc = launch_check("k_ns_phi_rhs"))) return rc;
   }
   {
     Sweeps S;
@@ -806,26 +877,69 @@ int ns_step(mf_navier* nv, cudaStream_t st) {
                                        nv->T(6), nv->fin.as<double>());
   k_ns_bc_phi<<<fb, kNsThreads, 0, st>>>(nv->faces, nv->RP(0), nv->RP(1), nv->RP(2), nv->bc.as<double>(), fac1,
                                          nv->BC(3));
-  if ((rc = launch_check("k_ns_fphi")) || (rc = solve(nv, nv->scp, nv->fin.as<double>(), nv->sigmap, nv->F(kVarPhi, nw), nv->BC(3), st)))
-    return rc;
+  if ((rc = launch_check("k_ns_fphi"))) return rc;
+  if (P.pt == 3) {
+    // add_boundary_rotrot: extrapolated velocity (T7..T9), its first
+    // derivatives A, B, C (T10..T12) and six second derivatives, then the
+    // sums, their three sweeps and the face update
+    for (int c = 0; c < 3; ++c)
+      if ((rc = extrapol_into(nv, extrapol_of(nv, P.top - 1, field_ptr, c), nv->T(7 + c), st))) return rc;
+    Sweeps S;
+    S.add(nv, 0, nv->T(7), nv->T(10));
+    S.add(nv, 1, nv->T(8), nv->T(11));
+    S.add(nv, 2, nv->T(9), nv->T(12));
+    S.add(nv, 1, nv->T(7), nv->T(13), 2);  // u_yy
+    S.add(nv, 2, nv->T(7), nv->T(14), 2);  // u_zz
+    S.add(nv, 0, nv->T(8), nv->T(15), 2);  // v_xx
+    S.add(nv, 2, nv->T(8), nv->T(16), 2);  // v_zz
+    S.add(nv, 0, nv->T(9), nv->T(17), 2);  // w_xx
+    S.add(nv, 1, nv->T(9), nv->T(1), 2);   // w_yy
+    if ((rc = S.run(nv, st))) return rc;
+    k_ns_rot_sums<<<gb, kNsThreads, 0, st>>>(nv->np, nv->T(10), nv->T(11), nv->T(12), nv->T(2), nv->T(3), nv->T(4));
+    if ((rc = launch_check("k_ns_rot_sums"))) return rc;
+    Sweeps S2;
+    S2.add(nv, 0, nv->T(2), nv->T(5));
+    S2.add(nv, 1, nv->T(3), nv->T(6));
+    S2.add(nv, 2, nv->T(4), nv->T(0));
+    if ((rc = S2.run(nv, st))) return rc;
+    RotRot R{{nv->T(5), nv->T(6), nv->T(0)}, {nv->T(13), nv->T(14), nv->T(15), nv->T(16), nv->T(17), nv->T(1)}};
+    k_ns_bc_rotrot<<<fb, kNsThreads, 0, st>>>(nv->faces, R, P.reynolds, nv->BC(3));
+    if ((rc = launch_check("k_ns_bc_rotrot"))) return rc;
+  }
+  if ((rc = solve(nv, nv->scp, nv->fin.as<double>(), nv->sigmap, nv->F(kVarPhi, nw), nv->BC(3), st))) return rc;
   // projection
   k_ns_zero_edges<<<gb, kNsThreads, 0, st>>>(nv->nx, nv->ny, nv->nz, nv->F(kVarPhi, nw));
   if ((rc = launch_check("k_ns_zero_edges"))) return rc;
-  if (P.pt == 2 && (rc = extrapol_into(nv, extrapol_of(nv, P.top - 1, field_ptr, kVarP), nv->T(0), st))) return rc;
+  const bool add_p = P.pt == 2 || P.pt == 4;
+  if (add_p && (rc = extrapol_into(nv, extrapol_of(nv, P.top - 1, field_ptr, kVarP), nv->T(0), st))) return rc;
+  if (P.pt == 4)
+    for (int c = 0; c < 3; ++c)
+      if ((rc = extrapol_into(nv, extrapol_of(nv, P.top - 1, field_ptr, c), nv->T(7 + c), st))) return rc;
   {
-    // divergence of u* and gradient of phi: six sweeps in one launch
+    // divergence (of u*, pt <= 2; of the extrapolated velocity, pt = 4) and
+    // gradient of phi: up to six sweeps in one launch
     Sweeps S;
-    for (int c = 0; c < 3; ++c) S.add(nv, c, nv->F(c, nw), nv->T(1 + c));
+    if (P.pt <= 2)
+      for (int c = 0; c < 3; ++c) S.add(nv, c, nv->F(c, nw), nv->T(1 + c));
+    else if (P.pt == 4)
+      for (int c = 0; c < 3; ++c) S.add(nv, c, nv->T(7 + c), nv->T(1 + c));
     for (int c = 0; c < 3; ++c) S.add(nv, c, nv->F(kVarPhi, nw), nv->T(4 + c));
     if ((rc = S.run(nv, st))) return rc;
   }
-  k_ns_pressure<<<gb, kNsThreads, 0, st>>>(nv->nx, nv->ny, nv->nz, nv->F(kVarPhi, nw),
-                                           P.pt == 2 ? nv->T(0) : nullptr, nv->T(1), nv->T(2), nv->T(3), P.reynolds,
-                                           nv->F(kVarP, nw));
+  const bool div = P.pt != 3;
+  k_ns_pressure<<<gb, kNsThreads, 0, st>>>(nv->nx, nv->ny, nv->nz, nv->F(kVarPhi, nw), add_p ? nv->T(0) : nullptr,
+                                           div ? nv->T(1) : nullptr, div ? nv->T(2) : nullptr,
+                                           div ? nv->T(3) : nullptr, P.reynolds, nv->F(kVarP, nw));
   if ((rc = launch_check("k_ns_pressure"))) return rc;
   for (int c = 0; c < 3; ++c) {
     k_ns_velocity<<<gb, kNsThreads, 0, st>>>(nv->nx, nv->ny, nv->nz, nv->RP(c), nv->T(4 + c), fac1, nv->F(c, nw));
     if ((rc = launch_check("k_ns_velocity"))) return rc;
+  }
+  // pt = 3, 4: velocity correction with the gradient of the new pressure
+  if (P.pt >= 3) {
+    if ((rc = gradient(nv, nv->F(kVarP, nw), nv->T(1), nv->T(2), nv->T(3), st)) ||
+        (rc = velocity_solves(nv->T(1))))
+      return rc;
   }
   nv->nl_ok[nw] = false;
   return MF_OK;
@@ -945,9 +1059,9 @@ int mf_navier_create(const double* gx, int nx, const double* gy, int ny, const d
   if (!gx || !gy || !gz || !p || !out) return set_error(MF_ERR_ARG, "mf_navier_create: null argument");
   *out = nullptr;
   if (nx < 9 || ny < 9 || nz < 9) return set_error(MF_ERR_ARG, "mf_navier_create: at least 9 nodes per axis");
-  if (!(p->ts > 0.0) || !(p->reynolds > 0.0) || p->nlt < 0 || p->nlt > 2 || (p->pt != 1 && p->pt != 2) ||
+  if (!(p->ts > 0.0) || !(p->reynolds > 0.0) || p->nlt < 0 || p->nlt > 2 || p->pt < 1 || p->pt > 4 ||
       p->tou < 1 || p->tou > 3 || p->nmodes < 0 || p->les_type < 0 || p->les_type > 3)
-    return set_error(MF_ERR_ARG, "mf_navier_create: bad parameters (ts, reynolds > 0; nlt 0..2; pt 1, 2; tou 1..3)");
+    return set_error(MF_ERR_ARG, "mf_navier_create: bad parameters (ts, reynolds > 0; nlt 0..2; pt 1..4; tou 1..3; les_type 0..3)");
   if (p->precision != MF_PREC_FP64 && p->precision != MF_PREC_SPLIT_BF16 && p->precision != MF_PREC_3XTF32)
     return set_error(MF_ERR_ARG, "mf_navier_create: unknown precision %d", p->precision);
   mf_navier* nv = new mf_navier();

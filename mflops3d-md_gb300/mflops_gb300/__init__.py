@@ -952,7 +952,7 @@ NAVIER_DIAG = ("div", "vel_err", "vel_rel", "vel_acc", "pres_err", "pres_rel", "
 
 class NavierStokes3D:
     """One-domain time integration of navier3d (mpid%dims = 0, mapt = 0,
-    nsubite = 1, pt 1 or 2, les_type 0..3) on host grids.  Keyword arguments
+    nsubite = 1, pt 1..4, les_type 0..3) on host grids.  Keyword arguments
     override the reference's defaults (ts, reynolds, nlt, pt, tou, top,
     so_solver, so_der, flow_rate, nmodes, precision, refine, les_type, les_c)."""
 

@@ -17,10 +17,12 @@ src/class_navier/class_navier_3D.f90:
   (:1169-1222, nlt = 0, 1, 2) and the forcing ``f`` (:1043-1167, the
   exact-solution source, the LES term and the flow-rate term for u),
   ``add_boundary_gradient`` for pt = 1 (:695-791), ``navier_solve_{u,v,w}``
-  (:1597-1761, pt = 1, 2), ``navier_presolve_phi`` / ``navier_phi_rhs``
-  (:1764-1785, 1961-2007), ``navier_solve_phi`` with
-  ``navier_bc_pressure`` (:1787-1845, 342-393), ``navier_projection``
-  (:1847-1959), ``navier_extrapol`` (:2010-2050) and the slot rotation
+  (:1597-1761, before the pressure for pt = 1, 2, after the projection for
+  pt = 3, 4: navier3d.f90:78-102), ``navier_presolve_phi`` /
+  ``navier_phi_rhs`` (:1764-1785, 1961-2007), ``navier_solve_phi`` with
+  ``navier_bc_pressure`` (:1787-1845, 342-393) and ``add_boundary_rotrot``
+  for pt = 3 (:793-846), ``navier_projection`` (:1847-1959),
+  ``navier_extrapol`` (:2010-2050) and the slot rotation
   (navier3d.f90:256-261);
 * the driver's per-step diagnostics (navier3d.f90:120-254) with
   ``integrale`` / ``norme2`` (class_navier_3D.f90:2419-2603); they report the
@@ -119,8 +121,8 @@ class Navier:
 
     def __init__(self, gx, gy, gz, ts, rey, nlt=2, pt=1, tou=2, top=2, so=(6, 6), flow_rate=True,
                  nmodes=NMODES, les_type=0, les_c=0.0):
-        if pt not in (1, 2):
-            raise ValueError("pressure types 1 and 2 are restated")
+        if pt not in (1, 2, 3, 4):
+            raise ValueError("pressure types 1 to 4")
         self.gx, self.gy, self.gz = (np.asarray(g, float) for g in (gx, gy, gz))
         self.nx, self.ny, self.nz = len(gx), len(gy), len(gz)
         self.ts, self.rey = float(ts), float(rey)
@@ -269,21 +271,28 @@ class Navier:
                 bc["w"][1][:, :, m] += dz[1:-1, j, 1:-1] / fac[0]
                 bc["u"][2][:, :, m] += dx[1:-1, 1:-1, k] / fac[0]
                 bc["v"][2][:, :, m] += dy[1:-1, 1:-1, k] / fac[0]
-        # solve u, v, w
         grads = (self.derx, self.dery, self.derz)
-        for q, c in enumerate("uvw"):
-            lev = levels[c]
-            fu = np.zeros((self.nx, self.ny, self.nz))
-            fu = fu + fac[1] * lev[n0] + fac[2] * lev[n1]
-            if self.tou == 3:
-                fu = fu + fac[3] * lev[n2]
-            if self.pt == 2:
-                fu = fu + grads[q](self.extrapol(self.p, "p"))
-            fu = fu - self.rhs[c][0]
-            fu = self.rey * fu
-            lev[new] = S.solver_3d(self.scu, fu, lev[new], *bc[c], self.sigmau)
-        # presolve phi (pt <= 2)
-        rp = [zero_edges(fac[0] * levels[c][new]) for c in "uvw"]
+
+        def solve_velocity():
+            """navier_solve_{u,v,w} (:1597-1761)."""
+            for q, c in enumerate("uvw"):
+                lev = levels[c]
+                fu = np.zeros((self.nx, self.ny, self.nz))
+                fu = fu + fac[1] * lev[n0] + fac[2] * lev[n1]
+                if self.tou == 3:
+                    fu = fu + fac[3] * lev[n2]
+                if self.pt == 2:
+                    fu = fu + grads[q](self.extrapol(self.p, "p"))
+                elif self.pt >= 3:
+                    fu = fu + grads[q](self.p[new])
+                fu = fu - self.rhs[c][0]
+                fu = self.rey * fu
+                lev[new] = S.solver_3d(self.scu, fu, lev[new], *bc[c], self.sigmau)
+
+        if self.pt <= 2:
+            solve_velocity()
+        # presolve phi
+        rp = [self.phi_rhs(levels[c], self.rhs[c]) for c in "uvw"]
         # solve phi
         fphi = self.sigmap * self.extrapol(self.phi, "p")
         fphi = fphi + self.derx(rp[0]) + self.dery(rp[1]) + self.derz(rp[2])
@@ -291,19 +300,57 @@ class Navier:
         bcphi = [np.stack([rp[0][m * (nx - 1), 1:-1, 1:-1] - fac[0] * bc["u"][0][:, :, m] for m in (0, 1)], -1),
                  np.stack([rp[1][1:-1, m * (ny - 1), 1:-1] - fac[0] * bc["v"][1][:, :, m] for m in (0, 1)], -1),
                  np.stack([rp[2][1:-1, 1:-1, m * (nz - 1)] - fac[0] * bc["w"][2][:, :, m] for m in (0, 1)], -1)]
+        if self.pt == 3:
+            self.add_boundary_rotrot(bcphi)
         self.phi[new] = S.solver_3d(self.scp, fphi, self.phi[new], *bcphi, self.sigmap)
         # projection
         self.phi[new] = zero_edges(self.phi[new])
-        if self.pt == 2:
+        if self.pt in (2, 4):
             aux = self.extrapol(self.p, "p")
         self.p[new] = self.phi[new].copy()
-        if self.pt == 2:
+        if self.pt in (2, 4):
             self.p[new] = self.p[new] + aux
         self.p[new] = zero_edges(self.p[new])
-        div = (self.derx(self.u[new]) + self.dery(self.v[new]) + self.derz(self.w[new])) / self.rey
-        self.p[new] = zero_edges(self.p[new] - div)
+        if self.pt <= 2:
+            div = (self.derx(self.u[new]) + self.dery(self.v[new]) + self.derz(self.w[new])) / self.rey
+            self.p[new] = self.p[new] - div
+        elif self.pt == 4:
+            div = (self.derx(self.extrapol(self.u, "p")) + self.dery(self.extrapol(self.v, "p"))
+                   + self.derz(self.extrapol(self.w, "p"))) / self.rey
+            self.p[new] = self.p[new] - div
+        self.p[new] = zero_edges(self.p[new])
         for q, c in enumerate("uvw"):
             levels[c][new] = zero_edges((rp[q] - grads[q](self.phi[new])) / fac[0])
+        # velocity correction (pt >= 3)
+        if self.pt >= 3:
+            solve_velocity()
+
+    def phi_rhs(self, var, fvar):
+        """navier_phi_rhs with subite = 1 (class_navier_3D.f90:1961-2007)."""
+        it, fac = self.it, self.fac
+        if self.pt <= 2:
+            out = fac[0] * var[it[0]]
+        else:
+            out = fvar[0] - fac[1] * var[it[NT - 1]] - fac[2] * var[it[NT - 2]] - fac[3] * var[it[NT - 3]]
+            if self.pt == 4:
+                out = (out - fvar[1] + fac[0] * var[it[NT - 1]] + fac[1] * var[it[NT - 2]]
+                       + fac[2] * var[it[NT - 3]] + fac[3] * var[it[0]])
+        return zero_edges(out)
+
+    def add_boundary_rotrot(self, bcphi):
+        """add_boundary_rotrot (class_navier_3D.f90:793-846): the normal
+        component of curl curl of the extrapolated velocity, over Re, taken
+        from the Neumann data of phi (pt = 3)."""
+        eu, ev, ew = (self.extrapol(f, "p") for f in (self.u, self.v, self.w))
+        dd = (lambda f: D.dderx(self.dcx, f), lambda f: D.ddery(self.dcy, f), lambda f: D.dderz(self.dcz, f))
+        ax = self.derx(self.dery(ev) + self.derz(ew)) - dd[1](eu) - dd[2](eu)
+        ay = self.dery(self.derx(eu) + self.derz(ew)) - dd[0](ev) - dd[2](ev)
+        az = self.derz(self.derx(eu) + self.dery(ev)) - dd[0](ew) - dd[1](ew)
+        nx, ny, nz = self.nx, self.ny, self.nz
+        for m in (0, 1):
+            bcphi[0][:, :, m] = bcphi[0][:, :, m] - ax[m * (nx - 1), 1:-1, 1:-1] / self.rey
+            bcphi[1][:, :, m] = bcphi[1][:, :, m] - ay[1:-1, m * (ny - 1), 1:-1] / self.rey
+            bcphi[2][:, :, m] = bcphi[2][:, :, m] - az[1:-1, 1:-1, m * (nz - 1)] / self.rey
 
     def diagnostics(self):
         """navier3d.f90:120-254 on level it(nt) (before the rotation), which

@@ -65,6 +65,8 @@ CASES = {
     "defaults": dict(ts=1e-2, reynolds=50.0),
     "pt2_bdf3_advective": dict(ts=5e-3, reynolds=20.0, pt=2, tou=3, top=3, nlt=1, flow_rate=0),
     "pt1_euler_no_advection": dict(ts=2e-2, reynolds=5.0, pt=1, tou=1, top=1, nlt=0, nmodes=1),
+    "pt3_rotrot": dict(ts=1e-2, reynolds=50.0, pt=3, top=3),
+    "pt4_bdf3": dict(ts=5e-3, reynolds=50.0, pt=4, tou=3, nlt=1),
     # LES cases: parameters for which the explicit LES term stays stable on
     # these coarse noisy fields (a blowing-up run amplifies rounding)
     "les_smagorinsky": dict(ts=2e-3, reynolds=100.0, les_type=1, les_c=0.17),

@@ -78,7 +78,7 @@ def test_quadrature_weights_skip_edges():
 
 def test_navier_create_rejects_bad_parameters(mf):
     g = mesh.uniform_grid(17)
-    for kw in ({"pt": 3}, {"tou": 4}, {"nlt": 5}, {"ts": 0.0}, {"reynolds": -1.0}, {"precision": 9}):
+    for kw in ({"pt": 5}, {"tou": 4}, {"nlt": 5}, {"ts": 0.0}, {"reynolds": -1.0}, {"precision": 9}):
         with pytest.raises(mf.MflopsError) as e:
             mf.NavierStokes3D(g, g, g, **kw)
         assert e.value.code == mf.MF_ERR_ARG, kw
@@ -91,3 +91,21 @@ def test_navier_create_rejects_bad_parameters(mf):
     assert prm.les_type == 0 and prm.les_c == 0.0
     with pytest.raises(mf.MflopsError):
         mf.NavierStokes3D(g, g, g, les_type=4)
+
+
+@pytest.mark.parametrize("pt", [3, 4])
+def test_velocity_correction_schemes_keep_the_exact_solution(pt):
+    """Pressure types 3 (rot-rot Neumann data) and 4 (increments of the
+    right-hand side) started on the one-mode exact solution stay on it; type 4
+    needs the previous step's right-hand side, set here from the solution."""
+    from oracle.les import zero_edges
+    g = mesh.tanh_grid(21, 1.0)
+    nav = N.Navier(g, g, g, ts=1e-2, rey=10.0, pt=pt, flow_rate=False, nmodes=1)
+    start_on_exact(nav)
+    if pt == 4:
+        levels = {"u": nav.u, "v": nav.v, "w": nav.w}
+        for c in "uvw":
+            nav.rhs[c][0] = zero_edges(nav.forcing(c) - nav.nonlinear(levels[c]))
+    for _ in range(5):
+        d = nav.advance(diagnostics=True)
+    assert d["vel"][1] < 2e-6 and d["pres"][1] < 2e-6 and d["div"] < 2e-6
