@@ -467,8 +467,9 @@ int mf_flow_curl(int nx, int ny, int nz, const double* const* dpsi, double* cons
  * Poisson solve (:1764-1845, 342-393), projection (:1847-1959),
  * extrapolation (:2010-2050), slot rotation and the driver's diagnostics
  * (navier3d.f90:120-261) and the LES term (navier_LES :1225-1455, f :1083-1099).
- * Covered: mpid%dims = 0 (one domain), mapt = 0, nsubite = 1, pressure types
- * 1 to 4, les_type 0..3.  Velocity Dirichlet and
+ * Covered: mpid%dims = 0 (one domain), mapt = 0, pressure types 1 to 4,
+ * les_type 0..3, nsubite sub-iterations with the driver's convergence test
+ * (testconv, navier3d.f90:366-412).  Velocity Dirichlet and
  * pressure Neumann on all faces; boundary values and sources from the
  * reference's exact solution `sol` (:927-1041, steady: wt = 0).  Fields are
  * (nx,ny,nz) FP64 device arrays, x fastest.
@@ -489,6 +490,7 @@ typedef struct {
   int refine;         /* refinement steps of the mixed solves, < 0: default */
   int les_type;       /* 0 none, 1 Smagorinsky, 2 WALE, 3 sigma (default 0) */
   double les_c;       /* cmd%les_c; the model coefficient is its square (default 0) */
+  int nsubite;        /* sub-iterations per time step (default 1) */
 } mf_navier_params_t;
 /* Fills the reference's defaults (command_line.f90:14-35). */
 int mf_navier_defaults(mf_navier_params_t* p);
@@ -503,9 +505,10 @@ int mf_navier_destroy(mf_navier_t* nav);
 int mf_navier_field(mf_navier_t* nav, int var, int level, double** ptr);
 int mf_navier_set_field(mf_navier_t* nav, int var, int level, const double* f, void* stream);
 int mf_navier_get_field(mf_navier_t* nav, int var, int level, double* f, void* stream);
-/* One time step: navier_time, the step, then (diag != NULL) the driver's
- * diagnostics of level it(nt), which remove the weighted mean of that
- * level's pressure, then the slot rotation.  diag[12] = div V; V error,
+/* One time step: navier_time, then per sub-iteration the step and (diag !=
+ * NULL) the driver's diagnostics of level it(nt), which remove the weighted
+ * mean of that level's pressure (diag holds the last sub-iteration's), then
+ * the slot rotation.  diag[12] = div V; V error,
  * relative, time-accumulated; P error, relative, time-accumulated; kinetic
  * energy; P and V stationarity (value, relative).  Without diag the step
  * makes no host synchronisation (capturable in a CUDA graph once the
@@ -514,6 +517,10 @@ int mf_navier_get_field(mf_navier_t* nav, int var, int level, double* f, void* s
 int mf_navier_step(mf_navier_t* nav, double* diag, void* stream);
 /* Simulated time and the flow-rate state (debit, g; 0 before the first step). */
 int mf_navier_state(mf_navier_t* nav, double* time, double* debit, double* g);
+/* Sub-iterations made by the last step (1 when nsubite = 1; with nsubite > 1
+ * the step stops when testconv passes, which synchronises the host once per
+ * sub-iteration). */
+int mf_navier_subiterations(const mf_navier_t* nav, int* n);
 
 #ifdef __cplusplus
 }

@@ -1,7 +1,7 @@
 // Navier-Stokes time step on one domain: the caller of the derivative and
 // solver entry points, src/main/navier3d.f90:48-274 built from
-// src/class_navier/class_navier_3D.f90 (one domain, mapt = 0, nsubite = 1,
-// pressure types 1 to 4, les_type 0..3).
+// src/class_navier/class_navier_3D.f90 (one domain, mapt = 0, pressure types
+// 1 to 4, les_type 0..3, sub-iterations).
 //
 // Time levels: nt = 4 slots per variable (u, v, w, p, phi) addressed through
 // the permutation it(1..nt) of the reference (it(1) = the slot a step
@@ -331,7 +331,7 @@ __global__ void k_ns_scale(int nx, int ny, int nz, double s, const double* __res
   out[q] = on_edge(i, j, k, nx, ny, nz) ? 0.0 : s * x[q];
 }
 
-// navier_phi_rhs for pt = 3, 4 with subite = 1 (class_navier_3D.f90:1983-2003):
+// navier_phi_rhs for pt = 3, 4 (class_navier_3D.f90:1983-2003):
 // pt 3: f1 - fac2 x(it(nt)) - fac3 x(it(nt-1)) - fac4 x(it(nt-2));
 // pt 4: that - f2 + fac1 x(it(nt)) + fac2 x(it(nt-1)) + fac3 x(it(nt-2)) + fac4 x(it(1));
 // edges zeroed.  f1, f2 = rhs(1), rhs(2) of the component.
@@ -349,8 +349,13 @@ __global__ void k_ns_phi_rhs(int nx, int ny, int nz, int pt, const double* __res
     out[q] = 0.0;
     return;
   }
-  double t = f1[q] - fb * x0[q] - fc * x1[q] - fd * x2[q];
-  if (pt == 4) t = t - f2[q] + fa * x0[q] + fb * x1[q] + fc * x2[q] + fd * x3[q];
+  double t;
+  if (pt == 5) {  // pt 4 from the second sub-iteration on: f1 - f2 + fac1 x(it(1))
+    t = f1[q] - f2[q] + fa * x3[q];
+  } else {
+    t = f1[q] - fb * x0[q] - fc * x1[q] - fd * x2[q];
+    if (pt == 4) t = t - f2[q] + fa * x0[q] + fb * x1[q] + fc * x2[q] + fd * x3[q];
+  }
   out[q] = t;
 }
 
@@ -531,6 +536,8 @@ struct DiagIn {
   const double *dx, *dy, *dz;                       // du/dx, dv/dy, dw/dz of it(nt)
   const double *ue, *ve, *pex;                      // exact fields
   double pexm, auxm;                                // means removed in phases 1, 2
+  const double *su, *sv, *sw, *sp;                  // testconv: last sub-iterate
+  double spm;                                       // testconv: mean shift of sp
 };
 
 // Grid (nz, G); part[(k G + g) kDiagSums + s].
@@ -568,9 +575,22 @@ __global__ void __launch_bounds__(kNsThreads) k_ns_diag(Weights W, DiagIn D, dou
         acc[0] += wq * e * e;
         acc[1] += wq * pe * pe;
         acc[2] += wq * (D.p[q] - D.pp[q]);
-      } else {
+      } else if (kPhase == 2) {
         const double a = (D.p[q] - D.pp[q]) - D.auxm;
         acc[0] += wq * a * a;
+      } else if (kPhase == 3) {  // testconv (navier3d.f90:394-403), u..p = it(1)
+        const double u = D.u[q], v = D.v[q], w = D.w[q];
+        const double r = sqrt(u * u + v * v + w * w);
+        const double eu = D.su[q] - u, ev = D.sv[q] - v, ew = D.sw[q] - w;
+        const double e = sqrt(eu * eu + ev * ev + ew * ew);
+        acc[0] += wq * r * r;
+        acc[1] += wq * e * e;
+        acc[2] += wq * (D.p[q] - D.sp[q]);
+      } else {  // testconv (:405-407)
+        const double sp = D.sp[q] + D.spm;
+        const double e = D.p[q] - sp;
+        acc[0] += wq * sp * sp;
+        acc[1] += wq * e * e;
       }
     }
   block_sums<kDiagSums>(acc, part + ((long long)k * gridDim.y + blockIdx.y) * kDiagSums);
@@ -594,6 +614,7 @@ struct mf_navier {
   double fac[4] = {0, 0, 0, 0};
   double sigmau = 0.0, sigmap = 0.0, time = 0.0;
   int it[kNt] = {0, 1, 2, 3};
+  int subite = 1, subiterations = 0;
   bool nl_ok[kNt] = {false, false, false, false};
   int rhs_cur = 0;
   mf_der_t *dcx = nullptr, *dcy = nullptr, *dcz = nullptr;
@@ -618,6 +639,7 @@ struct mf_navier {
   DevBuf part;    // partial sums
   DevBuf sums;    // summed values
   DevBuf state;   // flow-rate term: g, debit, initialised
+  DevBuf sub;     // last sub-iterate u, v, w, p (nsubite > 1)
   Faces faces{};
   double reft = 0.0;  // integrale(1)
   double err_vts = 0.0, err_pre = 0.0;
@@ -639,13 +661,16 @@ namespace {
 
 constexpr int kVarU = 0, kVarP = 3, kVarPhi = 4;
 
-// extrapol of var (navier_extrapol, subite = 1) of the given order:
-// -1 -> it(1); 1 -> it(nt); 2 -> 2 it(nt) - it(nt-1); 3 -> 3 it(nt) - 3 it(nt-1) + it(nt-2); else 0.
+// extrapol of var (navier_extrapol) of the given order: -1 -> it(1); 1 ->
+// it(nt); 2 -> 2 it(nt) - it(nt-1); 3 -> 3 it(nt) - 3 it(nt-1) + it(nt-2);
+// else 0; from the second sub-iteration on it(1) whatever the order.
 Lin extrapol_of(const mf_navier* nv, int order, double* (*slot_ptr)(const mf_navier*, int, int), int var) {
   Lin L{};
   const int* it = nv->it;
   auto P = [&](int s) { return slot_ptr(nv, var, s); };
-  if (order == -1) {
+  if (nv->subite > 1) {  // from the second sub-iteration on: the current iterate
+    L.m = 1; L.c[0] = 1.0; L.a[0] = P(it[0]);
+  } else if (order == -1) {
     L.m = 1; L.c[0] = 1.0; L.a[0] = P(it[0]);
   } else if (order == 1) {
     L.m = 1; L.c[0] = 1.0; L.a[0] = P(it[kNt - 1]);
@@ -768,11 +793,11 @@ int ns_step(mf_navier* nv, cudaStream_t st) {
   const long long ftot = nv->faces.sx + nv->faces.sy + nv->faces.sz;
   const unsigned fb = ns_blocks(ftot);
   int rc;
-  nv->time += P.ts;  // navier_time
   // presolve: nonlinear terms of the slots that extrapol('v') reads
   const Lin nlv0 = extrapol_of(nv, P.tou, nl_ptr, 0);
   for (int t = 0; t < nlv0.m; ++t) {
-    const int slot = t == 0 ? s0 : t == 1 ? s1 : s2;
+    int slot = 0;
+    while (nv->NL(0, slot) != nlv0.a[t]) ++slot;
     if (!nv->nl_ok[slot]) {
       if ((rc = nonlinear_slot(nv, slot, st))) return rc;
       nv->nl_ok[slot] = true;
@@ -862,7 +887,8 @@ int ns_step(mf_navier* nv, cudaStream_t st) {
     if (P.pt <= 2)
       k_ns_scale<<<gb, kNsThreads, 0, st>>>(nv->nx, nv->ny, nv->nz, fac1, nv->F(c, nw), nv->RP(c));
     else
-      k_ns_phi_rhs<<<gb, kNsThreads, 0, st>>>(nv->nx, nv->ny, nv->nz, P.pt, nv->RHS(c, nv->rhs_cur),
+      k_ns_phi_rhs<<<gb, kNsThreads, 0, st>>>(nv->nx, nv->ny, nv->nz,
+                                              P.pt == 4 && nv->subite > 1 ? 5 : P.pt, nv->RHS(c, nv->rhs_cur),
                                               nv->RHS(c, nv->rhs_cur ^ 1), nv->F(c, s0), nv->F(c, s1),
                                               nv->F(c, s2), nv->F(c, nw), nv->fac[0], nv->fac[1], nv->fac[2],
                                               nv->fac[3], nv->RP(c));
@@ -945,10 +971,48 @@ int ns_step(mf_navier* nv, cudaStream_t st) {
   return MF_OK;
 }
 
+// Weighted sums of one k_ns_diag phase into out[kDiagSums] (host; syncs).
+int diag_sums(mf_navier* nv, int phase, const DiagIn& D, double* out, cudaStream_t st) {
+  const int groups = (nv->ny + kWRows - 1) / kWRows, count = nv->nz * groups;
+  const dim3 grid(nv->nz, groups);
+  double* part = nv->part.as<double>();
+  switch (phase) {
+    case 0: k_ns_diag<0><<<grid, kNsThreads, 0, st>>>(nv->weights(), D, part); break;
+    case 1: k_ns_diag<1><<<grid, kNsThreads, 0, st>>>(nv->weights(), D, part); break;
+    case 2: k_ns_diag<2><<<grid, kNsThreads, 0, st>>>(nv->weights(), D, part); break;
+    case 3: k_ns_diag<3><<<grid, kNsThreads, 0, st>>>(nv->weights(), D, part); break;
+    default: k_ns_diag<4><<<grid, kNsThreads, 0, st>>>(nv->weights(), D, part); break;
+  }
+  k_ns_sum_parts<<<1, kNsThreads, 0, st>>>(part, count, kDiagSums, nv->sums.as<double>());
+  int r = launch_check("k_ns_diag");
+  if (r) return r;
+  MF_CUDA(cudaMemcpyAsync(out, nv->sums.ptr, sizeof(double) * kDiagSums, cudaMemcpyDeviceToHost, st));
+  MF_CUDA(cudaStreamSynchronize(st));
+  return MF_OK;
+}
+
+// testconv (navier3d.f90:366-412) of the iterate it(1) against the last
+// sub-iterate: true when both relative changes are below eps.
+int ns_testconv(mf_navier* nv, double eps, bool* test, cudaStream_t st) {
+  const int nw = nv->it[0];
+  DiagIn D{};
+  D.u = nv->F(0, nw); D.v = nv->F(1, nw); D.w = nv->F(2, nw); D.p = nv->F(kVarP, nw);
+  const double* sb = nv->sub.as<double>();
+  D.su = sb; D.sv = sb + nv->np; D.sw = sb + 2 * nv->np; D.sp = sb + 3 * nv->np;
+  double a[kDiagSums], b[kDiagSums];
+  int rc;
+  if ((rc = diag_sums(nv, 3, D, a, st))) return rc;
+  const double e1 = std::sqrt(a[1]) / std::sqrt(a[0]);
+  D.spm = a[2] / nv->reft;
+  if ((rc = diag_sums(nv, 4, D, b, st))) return rc;
+  const double e2 = std::sqrt(b[1]) / std::sqrt(b[0]);
+  *test = e1 < eps && e2 < eps;
+  return MF_OK;
+}
+
 // Driver diagnostics of level it(nt) (navier3d.f90:120-254); diag[12].
 int ns_diagnostics(mf_navier* nv, double* diag, cudaStream_t st) {
   const int cur = nv->it[kNt - 1], prev = nv->it[kNt - 2];
-  const int groups = (nv->ny + kWRows - 1) / kWRows, count = nv->nz * groups;
   int rc;
   {
     Sweeps S;
@@ -961,20 +1025,7 @@ int ns_diagnostics(mf_navier* nv, double* diag, cudaStream_t st) {
   D.dx = nv->T(1); D.dy = nv->T(2); D.dz = nv->T(3);
   D.ue = nv->EX(0); D.ve = nv->EX(1); D.pex = nv->EX(2);
   double s0[kDiagSums], s1[kDiagSums], s2[kDiagSums];
-  auto run = [&](int phase, double* out) -> int {
-    if (phase == 0)
-      k_ns_diag<0><<<dim3(nv->nz, groups), kNsThreads, 0, st>>>(nv->weights(), D, nv->part.as<double>());
-    else if (phase == 1)
-      k_ns_diag<1><<<dim3(nv->nz, groups), kNsThreads, 0, st>>>(nv->weights(), D, nv->part.as<double>());
-    else
-      k_ns_diag<2><<<dim3(nv->nz, groups), kNsThreads, 0, st>>>(nv->weights(), D, nv->part.as<double>());
-    k_ns_sum_parts<<<1, kNsThreads, 0, st>>>(nv->part.as<double>(), count, kDiagSums, nv->sums.as<double>());
-    int r = launch_check("k_ns_diag");
-    if (r) return r;
-    MF_CUDA(cudaMemcpyAsync(out, nv->sums.ptr, sizeof(double) * kDiagSums, cudaMemcpyDeviceToHost, st));
-    MF_CUDA(cudaStreamSynchronize(st));
-    return MF_OK;
-  };
+  auto run = [&](int phase, double* out) { return diag_sums(nv, phase, D, out, st); };
   if ((rc = run(0, s0))) return rc;
   const double reft = nv->reft, ts = nv->prm.ts;
   const double ref1 = std::sqrt(reft);  // norme(1)
@@ -1028,6 +1079,7 @@ int mf_navier_defaults(mf_navier_params_t* p) {
   p->refine = -1;
   p->les_type = 0;
   p->les_c = 0.0;
+  p->nsubite = 1;
   return MF_OK;
 }
 
@@ -1048,7 +1100,7 @@ int mf_navier_destroy(mf_navier_t* nv) {
   }
   if (nv->fork) cudaEventDestroy(nv->fork);
   for (DevBuf* b : {&nv->fields, &nv->nl, &nv->rhs, &nv->rp, &nv->tmp, &nv->fin, &nv->exact, &nv->bcex,
-                    &nv->bc, &nv->grid, &nv->wts, &nv->part, &nv->sums, &nv->state})
+                    &nv->bc, &nv->grid, &nv->wts, &nv->part, &nv->sums, &nv->state, &nv->sub})
     b->release();
   delete nv;
   return MF_OK;
@@ -1060,7 +1112,8 @@ int mf_navier_create(const double* gx, int nx, const double* gy, int ny, const d
   *out = nullptr;
   if (nx < 9 || ny < 9 || nz < 9) return set_error(MF_ERR_ARG, "mf_navier_create: at least 9 nodes per axis");
   if (!(p->ts > 0.0) || !(p->reynolds > 0.0) || p->nlt < 0 || p->nlt > 2 || p->pt < 1 || p->pt > 4 ||
-      p->tou < 1 || p->tou > 3 || p->nmodes < 0 || p->les_type < 0 || p->les_type > 3)
+      p->tou < 1 || p->tou > 3 || p->nmodes < 0 || p->les_type < 0 || p->les_type > 3 ||
+      p->nsubite < 1)
     return set_error(MF_ERR_ARG, "mf_navier_create: bad parameters (ts, reynolds > 0; nlt 0..2; pt 1..4; tou 1..3; les_type 0..3)");
   if (p->precision != MF_PREC_FP64 && p->precision != MF_PREC_SPLIT_BF16 && p->precision != MF_PREC_3XTF32)
     return set_error(MF_ERR_ARG, "mf_navier_create: unknown precision %d", p->precision);
@@ -1102,6 +1155,7 @@ int mf_navier_create(const double* gx, int nx, const double* gy, int ny, const d
   if (p->les_type != 0 &&
       ((rc = mf_les_create(gx, nx, gy, ny, gz, nz, &nv->les)) || (rc = nv->nu.ensure(fb))))
     return fail(rc);
+  if (p->nsubite > 1 && (rc = nv->sub.ensure(fb * 4))) return fail(rc);
   if ((rc = nv->fields.ensure(fb * 5 * kNt)) || (rc = nv->nl.ensure(fb * 3 * kNt)) ||
       (rc = nv->rhs.ensure(fb * 6)) || (rc = nv->rp.ensure(fb * 3)) || (rc = nv->tmp.ensure(fb * 18)) ||
       (rc = nv->fin.ensure((size_t)nv->nin * sizeof(double) * 3)) || (rc = nv->exact.ensure(fb * 5)) ||
@@ -1185,13 +1239,40 @@ int mf_navier_get_field(mf_navier_t* nv, int var, int level, double* f, void* st
 int mf_navier_step(mf_navier_t* nv, double* diag, void* stream) {
   if (!nv) return set_error(MF_ERR_ARG, "mf_navier_step: null handle");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  int rc = ns_step(nv, st);
+  const size_t fb = (size_t)nv->np * sizeof(double);
+  int rc;
+  nv->time += nv->prm.ts;  // navier_time
+  for (int subite = 1; subite <= nv->prm.nsubite; ++subite) {
+    nv->subite = subite;
+    nv->subiterations = subite;
+    if ((rc = ns_step(nv, st))) break;
+    bool test = false;
+    if (subite > 1 && (rc = ns_testconv(nv, 1e-9, &test, st))) break;
+    if (nv->prm.nsubite > 1) {
+      const int nw = nv->it[0];
+      for (int v = 0; v < 4; ++v)
+        if (cudaMemcpyAsync(nv->sub.as<double>() + (size_t)v * nv->np, nv->F(v, nw), fb, cudaMemcpyDeviceToDevice,
+                            st) != cudaSuccess) {
+          rc = set_error(MF_ERR_CUDA, "mf_navier_step: copy of the sub-iterate failed");
+          break;
+        }
+      if (rc) break;
+    }
+    if (diag && (rc = ns_diagnostics(nv, diag, st))) break;
+    if (test) break;
+  }
+  nv->subite = 1;
   if (rc) return rc;
-  if (diag && (rc = ns_diagnostics(nv, diag, st))) return rc;
   // slot rotation (navier3d.f90:256-261)
   const int first = nv->it[0];
   for (int i = 0; i < kNt - 1; ++i) nv->it[i] = nv->it[i + 1];
   nv->it[kNt - 1] = first;
+  return MF_OK;
+}
+
+int mf_navier_subiterations(const mf_navier_t* nv, int* n) {
+  if (!nv || !n) return set_error(MF_ERR_ARG, "mf_navier_subiterations: null argument");
+  *n = nv->subiterations;
   return MF_OK;
 }
 

@@ -47,6 +47,7 @@ module mflops_gpu_f
      integer(c_int) :: nlt, pt, tou, top, so_solver, so_der, flow_rate, nmodes, precision, refine
      integer(c_int) :: les_type
      real(c_double) :: les_c
+     integer(c_int) :: nsubite
   end type navier_params
 
   type, public :: navier3d_gpu

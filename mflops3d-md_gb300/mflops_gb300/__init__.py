@@ -169,6 +169,7 @@ _PROTOS = {
     "mf_navier_get_field": [_P, _I, _I, _P, _P],
     "mf_navier_step": [_P, _DP, _P],
     "mf_navier_state": [_P, _DP, _DP, _DP],
+    "mf_navier_subiterations": [_P, _IP],
 }
 
 for _name, _args in _PROTOS.items():
@@ -942,7 +943,7 @@ class NavierParams(ctypes.Structure):
                 ("pt", ctypes.c_int), ("tou", ctypes.c_int), ("top", ctypes.c_int),
                 ("so_solver", ctypes.c_int), ("so_der", ctypes.c_int), ("flow_rate", ctypes.c_int),
                 ("nmodes", ctypes.c_int), ("precision", ctypes.c_int), ("refine", ctypes.c_int),
-                ("les_type", ctypes.c_int), ("les_c", ctypes.c_double)]
+                ("les_type", ctypes.c_int), ("les_c", ctypes.c_double), ("nsubite", ctypes.c_int)]
 
 
 NAVIER_VARS = {"u": 0, "v": 1, "w": 2, "p": 3, "phi": 4}
@@ -952,9 +953,10 @@ NAVIER_DIAG = ("div", "vel_err", "vel_rel", "vel_acc", "pres_err", "pres_rel", "
 
 class NavierStokes3D:
     """One-domain time integration of navier3d (mpid%dims = 0, mapt = 0,
-    nsubite = 1, pt 1..4, les_type 0..3) on host grids.  Keyword arguments
-    override the reference's defaults (ts, reynolds, nlt, pt, tou, top,
-    so_solver, so_der, flow_rate, nmodes, precision, refine, les_type, les_c)."""
+    pt 1..4, les_type 0..3, nsubite sub-iterations) on host grids.  Keyword
+    arguments override the reference's defaults (ts, reynolds, nlt, pt, tou,
+    top, so_solver, so_der, flow_rate, nmodes, precision, refine, les_type,
+    les_c, nsubite)."""
 
     def __init__(self, gx, gy, gz, **kw):
         prm = NavierParams()
@@ -991,6 +993,12 @@ class NavierStokes3D:
             return dict(zip(NAVIER_DIAG, d))
         _check(_lib.mf_navier_step(self._h, None, _stream(stream)))
         return None
+
+    def subiterations(self):
+        """Sub-iterations made by the last step."""
+        n = ctypes.c_int()
+        _check(_lib.mf_navier_subiterations(self._h, ctypes.byref(n)))
+        return n.value
 
     def state(self):
         t, debit, g = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()

@@ -2,8 +2,10 @@
 
 Restates, in FP64 NumPy, one subdomain (``mpid%dims == 0``), no mapping
 (``mapt = 0``: ``derxm`` = ``derx``, the ``_nc`` terms are zero,
-src/class_mapping/class_mapping.f90:61-129) and one sub-iteration
-(``nsubite = 1``), the time loop of src/main/navier3d.f90:48-274 built from
+src/class_mapping/class_mapping.f90:61-129) and ``nsubite`` sub-iterations
+(convergence test ``testconv``, navier3d.f90:366-412; from the second
+sub-iteration on every extrapolation returns the current iterate it(1)), the
+time loop of src/main/navier3d.f90:48-274 built from
 src/class_navier/class_navier_3D.f90:
 
 * state ``type(navier3d)`` (:13-44): nt = 4 time levels u, v, w, p, phi in
@@ -120,7 +122,7 @@ class Navier:
     """Single-domain state and time step; fields are (nx, ny, nz) arrays."""
 
     def __init__(self, gx, gy, gz, ts, rey, nlt=2, pt=1, tou=2, top=2, so=(6, 6), flow_rate=True,
-                 nmodes=NMODES, les_type=0, les_c=0.0):
+                 nmodes=NMODES, les_type=0, les_c=0.0, nsubite=1):
         if pt not in (1, 2, 3, 4):
             raise ValueError("pressure types 1 to 4")
         self.gx, self.gy, self.gz = (np.asarray(g, float) for g in (gx, gy, gz))
@@ -130,6 +132,8 @@ class Navier:
         self.flow_rate = flow_rate
         self.nmodes = nmodes
         self.les_type, self.les_c = les_type, float(les_c)
+        self.nsubite, self.subite, self.subiterations = int(nsubite), 1, 0
+        self.sub = None
         self.du = None
         self.les_nu = None
         self.fac = bdf_factors(tou, ts)
@@ -176,7 +180,9 @@ class Navier:
         """navier_extrapol with subite = 1 (class_navier_3D.f90:2010-2050)."""
         order = self.tou if kind == "v" else self.top - 1
         it = self.it
-        if order == -1:
+        if self.subite > 1:
+            out = 1.0 * var[it[0]]
+        elif order == -1:
             out = 1.0 * var[it[0]]
         elif order == 1:
             out = 1.0 * var[it[NT - 1]]
@@ -247,7 +253,6 @@ class Navier:
     def step(self):
         it, fac = self.it, self.fac
         new, n0, n1, n2 = it[0], it[NT - 1], it[NT - 2], it[NT - 3]
-        self.time += self.ts
         bc = {c: self.bc_exact(c) for c in "uvw"}
         levels = {"u": self.u, "v": self.v, "w": self.w}
         if self.les_type:  # navier_LES on the newest level
@@ -332,7 +337,9 @@ class Navier:
             out = fac[0] * var[it[0]]
         else:
             out = fvar[0] - fac[1] * var[it[NT - 1]] - fac[2] * var[it[NT - 2]] - fac[3] * var[it[NT - 3]]
-            if self.pt == 4:
+            if self.pt == 4 and self.subite > 1:
+                out = fvar[0] - fvar[1] + fac[0] * var[it[0]]
+            elif self.pt == 4:
                 out = (out - fvar[1] + fac[0] * var[it[NT - 1]] + fac[1] * var[it[NT - 2]]
                        + fac[2] * var[it[NT - 3]] + fac[3] * var[it[0]])
         return zero_edges(out)
@@ -395,8 +402,35 @@ class Navier:
         """Slot rotation at the end of a time step (navier3d.f90:256-261)."""
         self.it = self.it[1:] + self.it[:1]
 
+    def testconv(self, eps=1e-9):
+        """testconv (navier3d.f90:366-412): relative change of the velocity
+        and of the mean-corrected pressure since the last sub-iteration."""
+        new = self.it[0]
+        u, v, w, p = self.u[new], self.v[new], self.w[new], self.p[new]
+        su, sv, sw, sp = self.sub
+        ref = self.norme(np.sqrt(u ** 2 + v ** 2 + w ** 2))
+        e1 = self.norme(np.sqrt((su - u) ** 2 + (sv - v) ** 2 + (sw - w) ** 2)) / ref
+        refi = self.integrale(np.ones((self.nx, self.ny, self.nz)))
+        sp = sp + self.integrale(p - sp) / refi
+        e2 = self.norme(p - sp) / self.norme(sp)
+        return e1 < eps and e2 < eps
+
     def advance(self, diagnostics=False):
-        self.step()
-        d = self.diagnostics() if diagnostics else None
+        """One iteration of the time loop (navier3d.f90:48-261): navier_time,
+        the sub-iterations (step, convergence test, driver diagnostics), the
+        slot rotation.  Returns the last sub-iteration's diagnostics."""
+        self.time += self.ts
+        d = None
+        for subite in range(1, self.nsubite + 1):
+            self.subite = subite
+            self.step()
+            test = subite > 1 and self.testconv()
+            self.sub = [f[self.it[0]].copy() for f in (self.u, self.v, self.w, self.p)]
+            if diagnostics:
+                d = self.diagnostics()
+            self.subiterations = subite
+            if test:
+                break
+        self.subite = 1
         self.rotate()
         return d

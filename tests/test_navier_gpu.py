@@ -35,7 +35,8 @@ def initial_levels(nav, seed, nmodes):
 
 def make_pair(mf, seed=3, **kw):
     gx, gy, gz = grids()
-    okw = {k: kw[k] for k in ("nlt", "pt", "tou", "top", "flow_rate", "nmodes", "les_type", "les_c") if k in kw}
+    okw = {k: kw[k] for k in ("nlt", "pt", "tou", "top", "flow_rate", "nmodes", "les_type", "les_c", "nsubite")
+           if k in kw}
     ora = N.Navier(gx, gy, gz, ts=kw["ts"], rey=kw["reynolds"], **okw)
     initial_levels(ora, seed, okw.get("nmodes", N.NMODES))
     gpu = mf.NavierStokes3D(gx, gy, gz, **kw)
@@ -67,6 +68,8 @@ CASES = {
     "pt1_euler_no_advection": dict(ts=2e-2, reynolds=5.0, pt=1, tou=1, top=1, nlt=0, nmodes=1),
     "pt3_rotrot": dict(ts=1e-2, reynolds=50.0, pt=3, top=3),
     "pt4_bdf3": dict(ts=5e-3, reynolds=50.0, pt=4, tou=3, nlt=1),
+    "pt2_subiterations": dict(ts=1e-2, reynolds=50.0, pt=2, nsubite=3),
+    "pt4_subiterations": dict(ts=1e-2, reynolds=50.0, pt=4, nsubite=3, les_type=1, les_c=0.1),
     # LES cases: parameters for which the explicit LES term stays stable on
     # these coarse noisy fields (a blowing-up run amplifies rounding)
     "les_smagorinsky": dict(ts=2e-3, reynolds=100.0, les_type=1, les_c=0.17),
@@ -156,3 +159,32 @@ def test_repeat_runs_are_bit_identical(mf, gpu):
     for other in runs[1:]:
         for a, b in zip(runs[0], other):
             assert torch.equal(a, b)
+
+
+def test_subiterations_stop_on_the_convergence_test(mf, gpu):
+    """pt 3 started on the one-mode exact solution converges within the
+    sub-iteration cap; the GPU stops after the same number of sub-iterations
+    as the oracle and gives the same fields."""
+    from test_navier_oracle import start_on_exact
+    gx, gy, gz = grids()
+    kw = dict(ts=1e-2, reynolds=10.0, pt=3, flow_rate=0, nmodes=1, nsubite=12)
+    ora = N.Navier(gx, gy, gz, ts=kw["ts"], rey=kw["reynolds"], pt=3, flow_rate=False, nmodes=1, nsubite=12)
+    start_on_exact(ora)
+    nav = mf.NavierStokes3D(gx, gy, gz, **kw)
+    for lev in range(N.NT):
+        for var in VARS:
+            nav.set_field(var, lev, mf.to_device(getattr(ora, var)[ora.it[lev]]))
+    counts = []
+    for _ in range(3):
+        ora.advance()
+        nav.step()
+        assert nav.subiterations() == ora.subiterations
+        counts.append(ora.subiterations)
+    assert max(counts) < 12
+    # w is zero in the exact solution (rounding noise only): errors against
+    # the scale of the velocity, O(1)
+    for lev in range(N.NT):
+        for var in VARS:
+            ref = getattr(ora, var)[ora.it[lev]]
+            err = np.abs(mf.to_host(nav.field(var, lev)) - ref).max()
+            assert err < 1e-10 * max(1.0, np.abs(ref).max()), (var, lev, err)
