@@ -521,6 +521,14 @@ int mf_navier_state(mf_navier_t* nav, double* time, double* debit, double* g);
  * the step stops when testconv passes, which synchronises the host once per
  * sub-iteration). */
 int mf_navier_subiterations(const mf_navier_t* nav, int* n);
+/* Checkpoint of the whole state (restart_write / restart_read,
+ * class_navier_3D.f90:186-340, as one raw binary file instead of a NetCDF
+ * directory): time, slot order, every level's fields, the right-hand-side
+ * history and the flow-rate state, so that a run resumed from it continues
+ * bit-identically.  load needs a handle of the same grids; it returns
+ * MF_ERR_ARG for another grid or a damaged file. */
+int mf_navier_save(mf_navier_t* nav, const char* path, void* stream);
+int mf_navier_load(mf_navier_t* nav, const char* path, void* stream);
 
 #ifdef __cplusplus
 }

@@ -34,6 +34,7 @@
 // Pointwise kernels fuse the edge zeroing of field_zero_edges
 // (class_field.f90:366-391) into their stores.
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <vector>
 
@@ -1267,6 +1268,96 @@ int mf_navier_step(mf_navier_t* nv, double* diag, void* stream) {
   const int first = nv->it[0];
   for (int i = 0; i < kNt - 1; ++i) nv->it[i] = nv->it[i + 1];
   nv->it[kNt - 1] = first;
+  return MF_OK;
+}
+
+// Checkpoint (the role of restart_write / restart_read,
+// class_navier_3D.f90:186-340, as one raw little-endian binary file instead
+// of a NetCDF directory).  Layout: magic "MFNSCHK1", int32 nx, ny, nz, nt,
+// the three grids (FP64), time, int32 it(1..nt) (0-based slots), int32
+// rhs_cur, err_vts, err_pre, the flow-rate state {g, debit, initialised},
+// then the fields u, v, w, p, phi of each slot 0..nt-1 and rhs(1), rhs(2)
+// of u, v, w (FP64, x fastest).  Beyond the reference's restart it keeps the
+// right-hand-side history (read by pt 4) and the flow-rate state (saved
+// variables of f), so a resumed run continues bit-identically.  The nonlinear
+// terms are recomputed after a load.
+constexpr char kChkMagic[8] = {'M', 'F', 'N', 'S', 'C', 'H', 'K', '1'};
+
+int mf_navier_save(mf_navier_t* nv, const char* path, void* stream) {
+  if (!nv || !path) return set_error(MF_ERR_ARG, "mf_navier_save: null argument");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  MF_CUDA(cudaStreamSynchronize(st));
+  FILE* f = std::fopen(path, "wb");
+  if (!f) return set_error(MF_ERR_ARG, "mf_navier_save: cannot open %s", path);
+  std::vector<double> grid(nv->nx + nv->ny + nv->nz), buf(nv->np);
+  double flow[3];
+  bool ok = cudaMemcpy(grid.data(), nv->grid.ptr, grid.size() * 8, cudaMemcpyDeviceToHost) == cudaSuccess &&
+            cudaMemcpy(flow, nv->state.ptr, sizeof(flow), cudaMemcpyDeviceToHost) == cudaSuccess;
+  const int dims[4] = {nv->nx, nv->ny, nv->nz, kNt};
+  ok = ok && std::fwrite(kChkMagic, 1, 8, f) == 8 && std::fwrite(dims, 4, 4, f) == 4 &&
+       std::fwrite(grid.data(), 8, grid.size(), f) == grid.size() && std::fwrite(&nv->time, 8, 1, f) == 1 &&
+       std::fwrite(nv->it, 4, kNt, f) == (size_t)kNt && std::fwrite(&nv->rhs_cur, 4, 1, f) == 1 &&
+       std::fwrite(&nv->err_vts, 8, 1, f) == 1 && std::fwrite(&nv->err_pre, 8, 1, f) == 1 &&
+       std::fwrite(flow, 8, 3, f) == 3;
+  auto put = [&](const double* d) {
+    return ok = ok && cudaMemcpy(buf.data(), d, buf.size() * 8, cudaMemcpyDeviceToHost) == cudaSuccess &&
+                std::fwrite(buf.data(), 8, buf.size(), f) == buf.size();
+  };
+  for (int slot = 0; slot < kNt && ok; ++slot)
+    for (int v = 0; v < 5 && ok; ++v) put(nv->F(v, slot));
+  for (int c = 0; c < 3 && ok; ++c)
+    for (int w = 0; w < 2 && ok; ++w) put(nv->RHS(c, w));
+  ok = (std::fclose(f) == 0) && ok;
+  return ok ? MF_OK : set_error(MF_ERR_CUDA, "mf_navier_save: writing %s failed", path);
+}
+
+int mf_navier_load(mf_navier_t* nv, const char* path, void* stream) {
+  if (!nv || !path) return set_error(MF_ERR_ARG, "mf_navier_load: null argument");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  MF_CUDA(cudaStreamSynchronize(st));
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return set_error(MF_ERR_ARG, "mf_navier_load: cannot open %s", path);
+  char magic[8];
+  int dims[4];
+  std::vector<double> grid(nv->nx + nv->ny + nv->nz), mine(grid.size()), buf(nv->np);
+  bool ok = std::fread(magic, 1, 8, f) == 8 && std::memcmp(magic, kChkMagic, 8) == 0 &&
+            std::fread(dims, 4, 4, f) == 4 && dims[0] == nv->nx && dims[1] == nv->ny && dims[2] == nv->nz &&
+            dims[3] == kNt && std::fread(grid.data(), 8, grid.size(), f) == grid.size() &&
+            cudaMemcpy(mine.data(), nv->grid.ptr, mine.size() * 8, cudaMemcpyDeviceToHost) == cudaSuccess &&
+            std::memcmp(grid.data(), mine.data(), grid.size() * 8) == 0;
+  if (!ok) {
+    std::fclose(f);
+    return set_error(MF_ERR_ARG, "mf_navier_load: %s is not a checkpoint of this grid", path);
+  }
+  double time, evts, epre, flow[3];
+  int it[kNt], rhs_cur;
+  ok = std::fread(&time, 8, 1, f) == 1 && std::fread(it, 4, kNt, f) == (size_t)kNt &&
+       std::fread(&rhs_cur, 4, 1, f) == 1 && std::fread(&evts, 8, 1, f) == 1 && std::fread(&epre, 8, 1, f) == 1 &&
+       std::fread(flow, 8, 3, f) == 3;
+  int seen = 0;
+  for (int i = 0; i < kNt && ok; ++i) {
+    ok = it[i] >= 0 && it[i] < kNt && !(seen & (1 << it[i]));
+    seen |= 1 << (ok ? it[i] : 0);
+  }
+  ok = ok && (rhs_cur == 0 || rhs_cur == 1);
+  auto get = [&](double* d) {
+    return ok = ok && std::fread(buf.data(), 8, buf.size(), f) == buf.size() &&
+                cudaMemcpy(d, buf.data(), buf.size() * 8, cudaMemcpyHostToDevice) == cudaSuccess;
+  };
+  for (int slot = 0; slot < kNt && ok; ++slot)
+    for (int v = 0; v < 5 && ok; ++v) get(nv->F(v, slot));
+  for (int c = 0; c < 3 && ok; ++c)
+    for (int w = 0; w < 2 && ok; ++w) get(nv->RHS(c, w));
+  ok = ok && cudaMemcpy(nv->state.ptr, flow, sizeof(flow), cudaMemcpyHostToDevice) == cudaSuccess &&
+       cudaDeviceSynchronize() == cudaSuccess;
+  std::fclose(f);
+  if (!ok) return set_error(MF_ERR_ARG, "mf_navier_load: %s is truncated or inconsistent", path);
+  nv->time = time;
+  for (int i = 0; i < kNt; ++i) nv->it[i] = it[i];
+  nv->rhs_cur = rhs_cur;
+  nv->err_vts = evts;
+  nv->err_pre = epre;
+  for (int i = 0; i < kNt; ++i) nv->nl_ok[i] = false;
   return MF_OK;
 }
 

@@ -170,6 +170,8 @@ _PROTOS = {
     "mf_navier_step": [_P, _DP, _P],
     "mf_navier_state": [_P, _DP, _DP, _DP],
     "mf_navier_subiterations": [_P, _IP],
+    "mf_navier_save": [_P, ctypes.c_char_p, _P],
+    "mf_navier_load": [_P, ctypes.c_char_p, _P],
 }
 
 for _name, _args in _PROTOS.items():
@@ -993,6 +995,13 @@ class NavierStokes3D:
             return dict(zip(NAVIER_DIAG, d))
         _check(_lib.mf_navier_step(self._h, None, _stream(stream)))
         return None
+
+    def save(self, path, stream=None):
+        """Checkpoint of the whole state (raw binary)."""
+        _check(_lib.mf_navier_save(self._h, str(path).encode(), _stream(stream)))
+
+    def load(self, path, stream=None):
+        _check(_lib.mf_navier_load(self._h, str(path).encode(), _stream(stream)))
 
     def subiterations(self):
         """Sub-iterations made by the last step."""

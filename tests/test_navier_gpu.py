@@ -188,3 +188,35 @@ def test_subiterations_stop_on_the_convergence_test(mf, gpu):
             ref = getattr(ora, var)[ora.it[lev]]
             err = np.abs(mf.to_host(nav.field(var, lev)) - ref).max()
             assert err < 1e-10 * max(1.0, np.abs(ref).max()), (var, lev, err)
+
+
+def test_checkpoint_resumes_bit_identically(mf, gpu, tmp_path):
+    """Save after some steps, continue; a fresh instance loaded from the file
+    continues to the same fields, time and flow-rate state (pt 4: the
+    right-hand-side history is part of the state).  Another grid and a
+    truncated file are refused."""
+    import torch
+    kw = dict(ts=1e-2, reynolds=50.0, pt=4, tou=3)
+    _, a = make_pair(mf, **kw)
+    for _ in range(5):
+        a.step()
+    path = tmp_path / "ns.chk"
+    a.save(path)
+    for _ in range(6):
+        a.step()
+    gx, gy, gz = grids()
+    b = mf.NavierStokes3D(gx, gy, gz, **kw)
+    b.load(path)
+    for _ in range(6):
+        b.step()
+    for lev in range(N.NT):
+        for var in VARS:
+            assert torch.equal(a.field(var, lev), b.field(var, lev)), (var, lev)
+    assert a.state() == b.state()
+    other = mf.NavierStokes3D(gx, gy, mesh.uniform_grid(15), **kw)
+    with pytest.raises(mf.MflopsError):
+        other.load(path)
+    data = path.read_bytes()
+    (tmp_path / "cut.chk").write_bytes(data[: len(data) // 2])
+    with pytest.raises(mf.MflopsError):
+        b.load(tmp_path / "cut.chk")
