@@ -58,6 +58,9 @@ def parse():
                          "at 160^3, a training step on 65,536 points, six Navier-Stokes steps at "
                          "128x129x128), and exit")
     ap.add_argument("--refine", type=int, default=1)
+    ap.add_argument("--md-config2", action="store_true",
+                    help="measure the 2x2x2 multidomain configuration at its full slab sizes "
+                         "(seeded draw from {49, 65, 97}; ~3 minutes of influence-matrix set-up) and exit")
     return ap.parse_args()
 
 
@@ -725,6 +728,48 @@ def row_measurements(mf, torch, hbm):
     return out
 
 
+def run_md_config2(args):
+    """2 x 2 x 2 subdomains with slab sizes drawn (seed 3) from {49, 65, 97},
+    tanh(1.0) slabs on [0, 1]^3: influence-matrix set-up and one solve for
+    the velocity operator (Dirichlet, sigma = -1e6) and the pressure operator
+    (Neumann, sigma = 0, null space), random right-hand sides."""
+    import torch
+    import mflops_gb300 as mf
+    from oracle import mesh
+    rng = np.random.default_rng(3)
+    sizes = rng.choice([49, 65, 97], size=(3, 2))
+    grids = [[mesh.tanh_grid(int(sizes[l][0]), 1.0, 0.0, 0.5), mesh.tanh_grid(int(sizes[l][1]), 1.0, 0.5, 1.0)]
+             for l in range(3)]
+    out = {"workload": "md_2x2x2_slabs_%s" % "_".join("%dx%d" % tuple(sz) for sz in sizes)}
+    for name, sigma, bct, null in (("velocity", -1e6, (1,) * 6, 0), ("pressure", 0.0, (2,) * 6, 1)):
+        md = mf.MultiDomain((2, 2, 2), (0, 0, 0), grids[0], grids[1], grids[2], bct, 6)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        md.influence_matrix_set(sigma, null)
+        torch.cuda.synchronize()
+        setup = time.perf_counter() - t0
+        gen = torch.Generator("cuda").manual_seed(4)
+        g, u, bc = {}, {}, {}
+        for c in md.subdomains():
+            sh = md.shape(*c)
+            g[c] = torch.randn(tuple(reversed(sh)), dtype=torch.float64, device="cuda",
+                               generator=gen).permute(2, 1, 0)
+            u[c] = mf.empty_device(sh)
+            bc[c] = (mf.empty_device((sh[1] - 2, sh[2] - 2, 2)), mf.empty_device((sh[0] - 2, sh[2] - 2, 2)),
+                     mf.empty_device((sh[0] - 2, sh[1] - 2, 2)))
+        md.solve(g, u, bc)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(5):
+            md.solve(g, u, bc)
+        b.record()
+        torch.cuda.synchronize()
+        out[name] = {"ninf": md.ninf(), "setup_s": setup, "solve_ms": a.elapsed_time(b) / 5}
+        md.close()
+    print(json.dumps(out), flush=True)
+
+
 def run_row_probe(args):
     """Two untimed launches of one row's kernels on the bench's row shapes
     (synthetic data), for ncu captures of single kernels."""
@@ -810,6 +855,9 @@ def main():
     args = parse()
     if args.probe:
         run_probe(args)
+        return
+    if args.md_config2:
+        run_md_config2(args)
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

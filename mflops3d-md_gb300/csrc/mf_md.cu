@@ -174,55 +174,132 @@ __global__ void k_face_set(double* bc, long long nf, int m, const double* __rest
   bc[q + nf * m] = v;
 }
 
-// Pivot application, then blocked triangular solves with the LU factor
-// (column-major n x n, unit lower L, upper U) on one right-hand side.
-__global__ void k_apply_pivots(double* x, const int* __restrict__ ipiv, int n) {
-  if (blockIdx.x == 0 && threadIdx.x == 0)
-    for (int k = 0; k < n; ++k) {
-      const int p = ipiv[k] - 1;
-      if (p != k) {
-        const double t = x[k];
-        x[k] = x[p];
-        x[p] = t;
-      }
-    }
-}
-
+// Triangular solves with the LU factor (column-major n x n, unit lower L,
+// upper U) on one right-hand side, in blocks of kTriBlock rows.
+//  * The row interchanges of getrf are turned into one permutation at set-up
+//    and applied as a parallel gather (k_permute), instead of n dependent
+//    swaps.
+//  * The inverses of the diagonal blocks of L and U are formed at set-up
+//    (k_tri_block_inverse), so a block step is one launch (k_tri_step):
+//    every CTA forms s_k = inv(D_k) v_k (a 128 x 128 product from L2), CTA 0
+//    stores it, and each thread updates one row of the trailing part,
+//    v_r -= sum_c T(r, k0 + c) s_k[c], reading the factor once, coalesced.
 constexpr int kTriBlock = 128;
 
-// Solves the diagonal block [k0, k0+nb) in place (one CTA).
-__global__ void k_tri_diag(const double* __restrict__ A, double* x, int n, int k0, int nb, int upper) {
-  __shared__ double xs[kTriBlock];
-  for (int t = threadIdx.x; t < nb; t += blockDim.x) xs[t] = x[k0 + t];
+__global__ void k_permute(const double* __restrict__ x, const int* __restrict__ perm, double* __restrict__ y,
+                          int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) y[i] = x[perm[i]];
+}
+
+// Inverse of diagonal block b (rows/columns k0 = b kTriBlock ... k0 + nb) of
+// L (upper = 0, unit diagonal) or U (upper = 1), by right-looking
+// elimination on the identity in shared memory; out = column-major
+// kTriBlock x kTriBlock per block.  One CTA per block.
+__global__ void __launch_bounds__(256) k_tri_block_inverse(const double* __restrict__ A, int n, int upper,
+                                                           double* __restrict__ out) {
+  extern __shared__ double X[];  // kTriBlock x kTriBlock, row r at X[r * kTriBlock]
+  const int k0 = blockIdx.x * kTriBlock, nb = min(kTriBlock, n - k0);
+  for (int t = threadIdx.x; t < kTriBlock * kTriBlock; t += blockDim.x)
+    X[t] = (t / kTriBlock == t % kTriBlock && t / kTriBlock < nb) ? 1.0 : 0.0;
   __syncthreads();
   if (!upper) {
-    for (int c = 0; c < nb; ++c) {
-      const double xc = xs[c];
-      for (int r = c + 1 + threadIdx.x; r < nb; r += blockDim.x)
-        xs[r] -= A[(k0 + r) + (long long)n * (k0 + c)] * xc;
+    for (int c = 0; c < nb; ++c) {  // row c final; rows below: X[r,:] -= L[r,c] X[c,:]
+      for (int t = threadIdx.x; t < (nb - c - 1) * (c + 1); t += blockDim.x) {
+        const int r = c + 1 + t / (c + 1), j = t % (c + 1);
+        X[r * kTriBlock + j] -= A[(k0 + r) + (long long)n * (k0 + c)] * X[c * kTriBlock + j];
+      }
       __syncthreads();
     }
   } else {
-    for (int c = nb - 1; c >= 0; --c) {
-      if (threadIdx.x == 0) xs[c] /= A[(k0 + c) + (long long)n * (k0 + c)];
+    for (int c = nb - 1; c >= 0; --c) {  // X[c,:] /= U[c,c]; rows above: X[r,:] -= U[r,c] X[c,:]
+      const double d = A[(k0 + c) + (long long)n * (k0 + c)];
+      for (int j = c + threadIdx.x; j < nb; j += blockDim.x) X[c * kTriBlock + j] = X[c * kTriBlock + j] / d;
       __syncthreads();
-      const double xc = xs[c];
-      for (int r = threadIdx.x; r < c; r += blockDim.x)
-        xs[r] -= A[(k0 + r) + (long long)n * (k0 + c)] * xc;
+      for (int t = threadIdx.x; t < c * (nb - c); t += blockDim.x) {
+        const int r = t / (nb - c), j = c + t % (nb - c);
+        X[r * kTriBlock + j] -= A[(k0 + r) + (long long)n * (k0 + c)] * X[c * kTriBlock + j];
+      }
       __syncthreads();
     }
   }
-  for (int t = threadIdx.x; t < nb; t += blockDim.x) x[k0 + t] = xs[t];
+  double* o = out + (size_t)blockIdx.x * kTriBlock * kTriBlock;
+  for (int t = threadIdx.x; t < kTriBlock * kTriBlock; t += blockDim.x) {
+    const int r = t % kTriBlock, c = t / kTriBlock;  // column-major store
+    o[t] = X[r * kTriBlock + c];
+  }
 }
 
-// x[r] -= sum_{c in block} A[r, c] x[c] for rows r in [r0, r1).
-__global__ void k_tri_update(const double* __restrict__ A, double* x, int n, int k0, int nb, int r0,
-                             int r1) {
-  const int r = r0 + blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= r1) return;
+// sol[k0 + r] = (Dinv v[k0 : k0 + nb])_r: the first block of a triangular
+// solve (one CTA).
+__global__ void __launch_bounds__(128) k_tri_first(const double* __restrict__ Dinv, const double* __restrict__ v,
+                                                   double* __restrict__ sol, int k0, int nb) {
+  __shared__ double xs[kTriBlock];
+  for (int t = threadIdx.x; t < nb; t += blockDim.x) xs[t] = v[k0 + t];
+  __syncthreads();
+  for (int r = threadIdx.x; r < nb; r += blockDim.x) {
+    double acc = 0.0;
+    for (int c = 0; c < nb; ++c) acc = fma(Dinv[r + kTriBlock * c], xs[c], acc);
+    sol[k0 + r] = acc;
+  }
+}
+
+// One block step of a blocked triangular solve.  sol[k0 : k0 + nb] is final;
+// rows [r0, r1) of v get v_r -= sum_c A[r, k0 + c] sol[k0 + c] (128 rows per
+// CTA, four column quarters per row, four accumulators each).  The CTA whose
+// rows are the next block [nk0, nk0 + nnb) (it starts at nk0 by
+// construction) then forms sol there = Dnext v, the same four-way split.
+constexpr int kTriQ = 4;                       // column quarters per row
+constexpr int kTriThreads = kTriBlock * kTriQ;  // 512
+__global__ void __launch_bounds__(kTriThreads) k_tri_step(const double* __restrict__ A, double* v, double* sol,
+                                                          int n, int k0, int nb, int r0, int r1,
+                                                          const double* __restrict__ Dnext, int nk0, int nnb) {
+  __shared__ double ss[kTriBlock], part[kTriQ][kTriBlock], vn[kTriBlock];
+  for (int t = threadIdx.x; t < nb; t += blockDim.x) ss[t] = sol[k0 + t];
+  __syncthreads();
+  const int lr = threadIdx.x % kTriBlock, qt = threadIdx.x / kTriBlock;
+  const int first = r0 + blockIdx.x * kTriBlock, r = first + lr;
+  constexpr int kCols = kTriBlock / kTriQ;
   double acc = 0.0;
-  for (int c = 0; c < nb; ++c) acc += A[r + (long long)n * (k0 + c)] * x[k0 + c];
-  x[r] -= acc;
+  if (r < r1) {
+    const int c0 = qt * kCols, c1 = min(nb, c0 + kCols);
+    const double* col = A + r + (long long)n * k0;
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    if (c1 - c0 == kCols) {
+      // full quarter: all loads issued before the products
+      double e[kCols];
+#pragma unroll
+      for (int t = 0; t < kCols; ++t) e[t] = col[(long long)n * (c0 + t)];
+#pragma unroll
+      for (int t = 0; t < kCols; t += 4) {
+        a0 = fma(e[t], ss[c0 + t], a0);
+        a1 = fma(e[t + 1], ss[c0 + t + 1], a1);
+        a2 = fma(e[t + 2], ss[c0 + t + 2], a2);
+        a3 = fma(e[t + 3], ss[c0 + t + 3], a3);
+      }
+    } else {
+      for (int c = c0; c < c1; ++c) a0 = fma(col[(long long)n * c], ss[c], a0);
+    }
+    acc = (a0 + a1) + (a2 + a3);
+  }
+  part[qt][lr] = acc;
+  __syncthreads();
+  if (qt == 0 && r < r1) {
+    const double nv = v[r] - ((part[0][lr] + part[1][lr]) + (part[2][lr] + part[3][lr]));
+    v[r] = nv;
+    vn[lr] = nv;
+  }
+  if (Dnext && first == nk0) {
+    __syncthreads();
+    double s2 = 0.0;
+    if (lr < nnb) {
+      const int c0 = qt * kCols, c1 = min(nnb, c0 + kCols);
+      for (int c2 = c0; c2 < c1; ++c2) s2 = fma(Dnext[lr + kTriBlock * c2], vn[c2], s2);
+    }
+    part[qt][lr] = s2;
+    __syncthreads();
+    if (qt == 0 && lr < nnb) sol[nk0 + lr] = (part[0][lr] + part[1][lr]) + (part[2][lr] + part[3][lr]);
+  }
 }
 
 // Largest interface system whose explicit inverse is formed at set-up.
@@ -315,6 +392,7 @@ struct mf_md {
   cudaEvent_t fork = nullptr;
   std::vector<Sub> sub;  // index i + nd1*(j + nd2*k)
   DevBuf M, ipiv, vec, info, work, zero_int, du[3], rint, ufield;
+  DevBuf perm, dinv, lu_v, lu_y;  // LU solve: row permutation, diagonal-block inverses, work vectors
   DevBuf Minv, vec2;  // row-major inverse of the influence matrix, solve output
   DevBuf ub, dub[3], bcb;  // batched influence columns: fields, derivatives, Dirac faces
   bool inv_ok = false;
@@ -373,20 +451,32 @@ static long long face_points(const mf_md::Sub& sd, int l) {
   return (long long)(sd.n[a] - 2) * (sd.n[b] - 2);
 }
 
-// Blocked triangular solves with the LU factor in md->M.
+// Blocked triangular solves with the LU factor in md->M: x = U^-1 L^-1 P x.
 static int md_lu_solve(mf_md* md, double* x, cudaStream_t st) {
   const int n = (int)md->topo.ninf;
+  const int nblocks = (n + kTriBlock - 1) / kTriBlock;
+  const size_t bs = (size_t)kTriBlock * kTriBlock;
   const double* A = md->M.as<double>();
-  k_apply_pivots<<<1, 1, 0, st>>>(x, md->ipiv.as<int>(), n);
-  for (int k0 = 0; k0 < n; k0 += kTriBlock) {
-    const int nb = std::min(kTriBlock, n - k0);
-    k_tri_diag<<<1, 128, 0, st>>>(A, x, n, k0, nb, 0);
-    if (k0 + nb < n) k_tri_update<<<nblk(n - k0 - nb, 256), 256, 0, st>>>(A, x, n, k0, nb, k0 + nb, n);
+  const double* dl = md->dinv.as<double>();
+  const double* du = dl + (size_t)nblocks * bs;
+  double* v = md->lu_v.as<double>();
+  double* y = md->lu_y.as<double>();
+  auto nbk = [&](int b) { return std::min(kTriBlock, n - b * kTriBlock); };
+  k_permute<<<nblk(n, 256), 256, 0, st>>>(x, md->perm.as<int>(), v, n);
+  // L y = P x: y_0 first, then each step updates the rows below and forms the next block
+  k_tri_first<<<1, kTriBlock, 0, st>>>(dl, v, y, 0, nbk(0));
+  for (int b = 0; b + 1 < nblocks; ++b) {
+    const int k0 = b * kTriBlock, rows = n - k0 - kTriBlock;
+    k_tri_step<<<(rows + kTriBlock - 1) / kTriBlock, kTriThreads, 0, st>>>(
+        A, v, y, n, k0, kTriBlock, k0 + kTriBlock, n, dl + (size_t)(b + 1) * bs, k0 + kTriBlock, nbk(b + 1));
   }
-  for (int k0 = ((n - 1) / kTriBlock) * kTriBlock; k0 >= 0; k0 -= kTriBlock) {
-    const int nb = std::min(kTriBlock, n - k0);
-    k_tri_diag<<<1, 128, 0, st>>>(A, x, n, k0, nb, 1);
-    if (k0 > 0) k_tri_update<<<nblk(k0, 256), 256, 0, st>>>(A, x, n, k0, nb, 0, k0);
+  // U x = y: the last block first, then upwards (y is updated in place)
+  const int kl = (nblocks - 1) * kTriBlock;
+  k_tri_first<<<1, kTriBlock, 0, st>>>(du + (size_t)(nblocks - 1) * bs, y, x, kl, nbk(nblocks - 1));
+  for (int b = nblocks - 1; b > 0; --b) {
+    const int k0 = b * kTriBlock;
+    k_tri_step<<<k0 / kTriBlock, kTriThreads, 0, st>>>(A, y, x, n, k0, nbk(b), 0, k0,
+                                                         du + (size_t)(b - 1) * bs, k0 - kTriBlock, kTriBlock);
   }
   MF_CUDA(cudaGetLastError());
   return MF_OK;
@@ -501,7 +591,8 @@ int mf_md_destroy(mf_md_t* md) {
   }
   if (md->fork) cudaEventDestroy(md->fork);
   for (DevBuf* b : {&md->Minv, &md->vec2, &md->ub, &md->dub[0], &md->dub[1], &md->dub[2], &md->bcb}) b->release();
-  for (DevBuf* b : {&md->M, &md->ipiv, &md->vec, &md->info, &md->work, &md->zero_int, &md->du[0],
+  for (DevBuf* b : {&md->perm, &md->dinv, &md->lu_v, &md->lu_y, &md->M, &md->ipiv, &md->vec, &md->info,
+                    &md->work, &md->zero_int, &md->du[0],
                     &md->du[1], &md->du[2], &md->rint, &md->ufield})
     b->release();
   if (md->cs) cusolverDnDestroy(md->cs);
@@ -625,6 +716,26 @@ int mf_md_influence_matrix_set(mf_md_t* md, double sigma, int null_mode, void* s
   if (hinfo != 0)
     return set_error(MF_ERR_SINGULAR, "influence matrix is singular (getrf info %d)%s", hinfo,
                      null_mode ? "" : "; an all-Neumann problem needs a null-space mode");
+  {
+    // LU solve set-up: the interchanges as one permutation, the inverses of
+    // the diagonal blocks of L and U
+    std::vector<int> piv(n), perm(n);
+    MF_CUDA(cudaMemcpy(piv.data(), md->ipiv.ptr, sizeof(int) * n, cudaMemcpyDeviceToHost));
+    for (long long i = 0; i < n; ++i) perm[i] = (int)i;
+    for (long long k = 0; k < n; ++k) std::swap(perm[k], perm[piv[k] - 1]);
+    const int nblocks = (int)((n + kTriBlock - 1) / kTriBlock);
+    const size_t smem = sizeof(double) * kTriBlock * kTriBlock;
+    if ((rc = md->perm.ensure(sizeof(int) * n)) || (rc = md->lu_v.ensure(sizeof(double) * n)) ||
+        (rc = md->lu_y.ensure(sizeof(double) * n)) ||
+        (rc = md->dinv.ensure(2 * (size_t)nblocks * smem)))
+      return rc;
+    MF_CUDA(cudaMemcpy(md->perm.ptr, perm.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+    MF_CUDA(cudaFuncSetAttribute(k_tri_block_inverse, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_tri_block_inverse<<<nblocks, 256, smem, st>>>(M, (int)n, 0, md->dinv.as<double>());
+    k_tri_block_inverse<<<nblocks, 256, smem, st>>>(M, (int)n, 1,
+                                                    md->dinv.as<double>() + (size_t)nblocks * kTriBlock * kTriBlock);
+    MF_CUDA(cudaGetLastError());
+  }
   // the inverse, row-major: A^T X = I gives X = A^-T column-major, i.e. A^-1
   // stored by rows.  Forming it costs 2 n^3 FP64 flops (three times the LU),
   // a few seconds at n = 12,000 on the FP64 pipe; above that, when it does
