@@ -309,6 +309,20 @@ int mf_md_solve(mf_md_t* md, const double* const* g, double* const* u, const dou
 #define MF_MD_IFACE_LU 1
 int mf_md_set_interface_solve(mf_md_t* md, int mode);
 
+/* On-disk factor cache (the role of md_influence_matrix_filename / _write /
+ * _read, class_md.f90:918-956, which name the cached matrix after the grid
+ * sizes only).  The key is a 64-bit FNV-1a hash of everything the matrix
+ * depends on -- decomposition, periods, every slab's grid, boundary types,
+ * scheme order, sigma and the null mode -- as 16 hex digits.  save writes the
+ * LU factor and pivots of the last mf_md_influence_matrix_set; load reads
+ * them (MF_ERR_ARG for a file of another key, a truncated or a damaged file)
+ * and rebuilds the solve tables; cached loads dir/<key>.mffac when it exists
+ * and builds and writes it otherwise. */
+int mf_md_factor_key(const mf_md_t* md, double sigma, int null_mode, char key[17]);
+int mf_md_save_factor(const mf_md_t* md, const char* path);
+int mf_md_load_factor(mf_md_t* md, double sigma, int null_mode, const char* path, void* stream);
+int mf_md_influence_matrix_cached(mf_md_t* md, double sigma, int null_mode, const char* dir, void* stream);
+
 /* Copies the last interface solution (ninf values) to host memory. */
 int mf_md_interface(const mf_md_t* md, double* lambda);
 

@@ -20,6 +20,8 @@
 #include <cusolverDn.h>
 
 #include <algorithm>
+#include <cstdint>
+#include <cstdio>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -401,12 +403,28 @@ struct mf_md {
   int null_mode = 0;
   double sigma = 0.0;
   bool factored = false;
+  uint64_t geom_key = 0;  // hash of the decomposition, grids, boundary types and order
 };
 
 namespace mf {
 
 static int md_sub_index(const mf_md* md, int i, int j, int k) {
   return i + md->topo.nd[0] * (j + md->topo.nd[1] * k);
+}
+
+// 64-bit FNV-1a over raw bytes (the cache key of an influence matrix).
+static uint64_t fnv1a(uint64_t h, const void* data, size_t bytes) {
+  const unsigned char* p = static_cast<const unsigned char*>(data);
+  for (size_t i = 0; i < bytes; ++i) {
+    h ^= p[i];
+    h *= 1099511628211ULL;
+  }
+  return h;
+}
+
+static uint64_t factor_key(const mf_md* md, double sigma, int null_mode) {
+  uint64_t h = fnv1a(md->geom_key, &sigma, sizeof(sigma));
+  return fnv1a(h, &null_mode, sizeof(null_mode));
 }
 
 // Solves subdomain s with interior rhs `rint` and its internal bc arrays,
@@ -555,6 +573,23 @@ int mf_md_create(const int nd[3], const int periods[3], const double* const* gri
         if (rc) break;
         max_field = std::max(max_field, (size_t)sd.n[0] * sd.n[1] * sd.n[2]);
       }
+  if (!rc) {
+    // cache key of the geometry: decomposition, periods, every slab's grid,
+    // boundary types and scheme order
+    uint64_t h = 1469598103934665603ULL;
+    h = fnv1a(h, "MFMD1", 5);
+    h = fnv1a(h, nd, 3 * sizeof(int));
+    h = fnv1a(h, periods, 3 * sizeof(int));
+    const double* const* grids[3] = {gridx, gridy, gridz};
+    for (int l = 0; l < 3; ++l)
+      for (int q = 0; q < nd[l]; ++q) {
+        h = fnv1a(h, &sizes[l][q], sizeof(int));
+        h = fnv1a(h, grids[l][q], sizeof(double) * sizes[l][q]);
+      }
+    h = fnv1a(h, bct, 6 * sizeof(int));
+    h = fnv1a(h, &so, sizeof(int));
+    md->geom_key = h;
+  }
   if (!rc)
     for (int l = 0; l < 3 && !rc; ++l) rc = md->du[l].ensure(max_field * 8);
   if (!rc) rc = md->rint.ensure(max_field * 8);
@@ -606,6 +641,8 @@ int mf_md_ninf(const mf_md_t* md, long long* ninf, int* it) {
   if (it) *it = md->topo.it;
   return MF_OK;
 }
+
+static int md_factor_finish(mf_md* md, cudaStream_t st);
 
 int mf_md_influence_matrix_set(mf_md_t* md, double sigma, int null_mode, void* stream) {
   if (!md || null_mode < 0 || null_mode > 2)
@@ -716,6 +753,16 @@ int mf_md_influence_matrix_set(mf_md_t* md, double sigma, int null_mode, void* s
   if (hinfo != 0)
     return set_error(MF_ERR_SINGULAR, "influence matrix is singular (getrf info %d)%s", hinfo,
                      null_mode ? "" : "; an all-Neumann problem needs a null-space mode");
+  return md_factor_finish(md, st);
+}
+
+// After the LU factor and the pivots are in md->M, md->ipiv: the set-up of
+// the triangular solves and, when wanted, the explicit inverse.
+static int md_factor_finish(mf_md* md, cudaStream_t st) {
+  const long long n = md->topo.ninf;
+  double* M = md->M.as<double>();
+  int rc, hinfo = 0;
+  cusolverDnSetStream(md->cs, st);
   {
     // LU solve set-up: the interchanges as one permutation, the inverses of
     // the diagonal blocks of L and U
@@ -764,6 +811,100 @@ int mf_md_influence_matrix_set(mf_md_t* md, double sigma, int null_mode, void* s
   }
   md->factored = true;
   return MF_OK;
+}
+
+// Factor cache: one raw little-endian file per influence matrix.  Layout:
+// magic "MFMDLU01", uint64 key, int64 n, sigma, int32 null_mode, then the LU
+// factor (n x n FP64, column-major) and the pivots (n int32), in chunks.
+constexpr char kFacMagic[8] = {'M', 'F', 'M', 'D', 'L', 'U', '0', '1'};
+constexpr size_t kFacChunk = (size_t)32 << 20;  // doubles per transfer (256 MB)
+
+int mf_md_factor_key(const mf_md_t* md, double sigma, int null_mode, char key[17]) {
+  if (!md || !key) return set_error(MF_ERR_ARG, "mf_md_factor_key: null argument");
+  std::snprintf(key, 17, "%016llx", (unsigned long long)factor_key(md, sigma, null_mode));
+  return MF_OK;
+}
+
+int mf_md_save_factor(const mf_md_t* md, const char* path) {
+  if (!md || !path) return set_error(MF_ERR_ARG, "mf_md_save_factor: null argument");
+  if (!md->factored) return set_error(MF_ERR_ARG, "mf_md_save_factor: influence matrix not set");
+  MF_CUDA(cudaDeviceSynchronize());
+  const long long n = md->topo.ninf;
+  FILE* f = std::fopen(path, "wb");
+  if (!f) return set_error(MF_ERR_ARG, "mf_md_save_factor: cannot open %s", path);
+  const uint64_t key = factor_key(md, md->sigma, md->null_mode);
+  bool ok = std::fwrite(kFacMagic, 1, 8, f) == 8 && std::fwrite(&key, 8, 1, f) == 1 &&
+            std::fwrite(&n, 8, 1, f) == 1 && std::fwrite(&md->sigma, 8, 1, f) == 1 &&
+            std::fwrite(&md->null_mode, 4, 1, f) == 1;
+  std::vector<double> buf(std::min<size_t>(kFacChunk, (size_t)n * n));
+  for (size_t off = 0; ok && off < (size_t)n * n; off += buf.size()) {
+    const size_t cnt = std::min<size_t>(buf.size(), (size_t)n * n - off);
+    ok = cudaMemcpy(buf.data(), md->M.as<double>() + off, cnt * 8, cudaMemcpyDeviceToHost) == cudaSuccess &&
+         std::fwrite(buf.data(), 8, cnt, f) == cnt;
+  }
+  std::vector<int> piv(n);
+  ok = ok && cudaMemcpy(piv.data(), md->ipiv.ptr, sizeof(int) * n, cudaMemcpyDeviceToHost) == cudaSuccess &&
+       std::fwrite(piv.data(), 4, n, f) == (size_t)n;
+  ok = (std::fclose(f) == 0) && ok;
+  return ok ? MF_OK : set_error(MF_ERR_CUDA, "mf_md_save_factor: writing %s failed", path);
+}
+
+int mf_md_load_factor(mf_md_t* md, double sigma, int null_mode, const char* path, void* stream) {
+  if (!md || !path || null_mode < 0 || null_mode > 2)
+    return set_error(MF_ERR_ARG, "mf_md_load_factor: bad arguments");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  MF_CUDA(cudaStreamSynchronize(st));
+  const long long n = md->topo.ninf;
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return set_error(MF_ERR_ARG, "mf_md_load_factor: cannot open %s", path);
+  char magic[8];
+  uint64_t key = 0;
+  long long fn = 0;
+  double fsigma = 0.0;
+  int fnull = -1;
+  bool ok = std::fread(magic, 1, 8, f) == 8 && std::memcmp(magic, kFacMagic, 8) == 0 &&
+            std::fread(&key, 8, 1, f) == 1 && std::fread(&fn, 8, 1, f) == 1 && std::fread(&fsigma, 8, 1, f) == 1 &&
+            std::fread(&fnull, 4, 1, f) == 1 && key == factor_key(md, sigma, null_mode) && fn == n;
+  if (!ok) {
+    std::fclose(f);
+    return set_error(MF_ERR_ARG, "mf_md_load_factor: %s is not the factor of this problem", path);
+  }
+  int rc;
+  if ((rc = md->M.ensure(sizeof(double) * n * n)) || (rc = md->ipiv.ensure(sizeof(int) * n)) ||
+      (rc = md->info.ensure(sizeof(int)))) {
+    std::fclose(f);
+    return rc;
+  }
+  md->factored = false;
+  std::vector<double> buf(std::min<size_t>(kFacChunk, (size_t)n * n));
+  for (size_t off = 0; ok && off < (size_t)n * n; off += buf.size()) {
+    const size_t cnt = std::min<size_t>(buf.size(), (size_t)n * n - off);
+    ok = std::fread(buf.data(), 8, cnt, f) == cnt &&
+         cudaMemcpy(md->M.as<double>() + off, buf.data(), cnt * 8, cudaMemcpyHostToDevice) == cudaSuccess;
+  }
+  std::vector<int> piv(n);
+  ok = ok && std::fread(piv.data(), 4, n, f) == (size_t)n;
+  for (long long k = 0; ok && k < n; ++k) ok = piv[k] >= 1 && piv[k] <= n;
+  ok = ok && cudaMemcpy(md->ipiv.ptr, piv.data(), sizeof(int) * n, cudaMemcpyHostToDevice) == cudaSuccess;
+  std::fclose(f);
+  if (!ok) return set_error(MF_ERR_ARG, "mf_md_load_factor: %s is truncated or damaged", path);
+  md->sigma = sigma;
+  md->null_mode = null_mode;
+  return md_factor_finish(md, st);
+}
+
+int mf_md_influence_matrix_cached(mf_md_t* md, double sigma, int null_mode, const char* dir, void* stream) {
+  if (!md || !dir) return set_error(MF_ERR_ARG, "mf_md_influence_matrix_cached: null argument");
+  char key[17];
+  int rc = mf_md_factor_key(md, sigma, null_mode, key);
+  if (rc) return rc;
+  const std::string path = std::string(dir) + "/" + key + ".mffac";
+  if (FILE* f = std::fopen(path.c_str(), "rb")) {
+    std::fclose(f);
+    if (mf_md_load_factor(md, sigma, null_mode, path.c_str(), stream) == MF_OK) return MF_OK;
+  }
+  if ((rc = mf_md_influence_matrix_set(md, sigma, null_mode, stream))) return rc;
+  return mf_md_save_factor(md, path.c_str());
 }
 
 int mf_md_solve(mf_md_t* md, const double* const* g, double* const* u, const double* const* bcx,

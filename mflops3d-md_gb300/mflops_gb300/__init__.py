@@ -120,6 +120,10 @@ _PROTOS = {
                     ctypes.POINTER(_P), ctypes.POINTER(_P), _P],
     "mf_md_interface": [_P, _DP],
     "mf_md_set_interface_solve": [_P, ctypes.c_int],
+    "mf_md_factor_key": [_P, _D, _I, ctypes.c_char_p],
+    "mf_md_save_factor": [_P, ctypes.c_char_p],
+    "mf_md_load_factor": [_P, _D, _I, ctypes.c_char_p, _P],
+    "mf_md_influence_matrix_cached": [_P, _D, _I, ctypes.c_char_p, _P],
     "mf_filter_lsq_matrix": [_DP, _I, _DP, _DP, _I, _DP, _I, _I, _DP, _DP],
     "mf_filter_period_matrix": [_DP, _I, _DP, _I, _DP, _DP],
     "mf_filter_lsq_init": [_DP, _I, _DP, _DP, _I, _DP, _I, _I, ctypes.POINTER(_P)],
@@ -569,8 +573,25 @@ class MultiDomain:
         _check(_lib.mf_md_ninf(self._h, ctypes.byref(n), ctypes.byref(it)))
         return n.value
 
-    def influence_matrix_set(self, sigma, null=0, stream=None):
+    def influence_matrix_set(self, sigma, null=0, stream=None, cache_dir=None):
+        """Builds and factorises the influence matrix; with cache_dir the
+        factor is read from (or written to) cache_dir/<key>.mffac."""
+        if cache_dir is not None:
+            _check(_lib.mf_md_influence_matrix_cached(self._h, float(sigma), int(null), str(cache_dir).encode(),
+                                                      _stream(stream)))
+            return
         _check(_lib.mf_md_influence_matrix_set(self._h, float(sigma), int(null), _stream(stream)))
+
+    def factor_key(self, sigma, null=0):
+        buf = ctypes.create_string_buffer(17)
+        _check(_lib.mf_md_factor_key(self._h, float(sigma), int(null), buf))
+        return buf.value.decode()
+
+    def save_factor(self, path):
+        _check(_lib.mf_md_save_factor(self._h, str(path).encode()))
+
+    def load_factor(self, sigma, null, path, stream=None):
+        _check(_lib.mf_md_load_factor(self._h, float(sigma), int(null), str(path).encode(), _stream(stream)))
 
     def solve(self, g, u, bc, stream=None):
         """g, u: {(i,j,k): device field}; bc: {(i,j,k): (bcx, bcy, bcz)}."""

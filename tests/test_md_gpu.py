@@ -119,3 +119,58 @@ def test_md_interface_forms_agree(mf, gpu):
     b = run(mf, (2, 2, 1), (0, 0, 0), ([11, 15], [13, 9], [11]), -1e3, iface=mf.MD_IFACE_LU)
     assert a[0] < 1e-11 and b[0] < 1e-11
     assert a[1] < 1e-11 and b[1] < 1e-11
+
+
+def test_factor_cache_round_trip(mf, gpu, tmp_path):
+    """The factor written for one (grids, sigma, null mode) reloads into a
+    fresh handle and solves identically; a factor of another sigma or a
+    damaged file is refused; the cached entry point builds once and then
+    loads."""
+    import torch
+    nd = (2, 1, 1)
+    grids = [[mesh.tanh_grid(11, 1.0, 0.0, 0.5), mesh.tanh_grid(13, 1.0, 0.5, 1.0)],
+             [mesh.tanh_grid(12, 1.0)], [mesh.tanh_grid(10, 1.0)]]
+    make = lambda: mf.MultiDomain(nd, (0, 0, 0), grids[0], grids[1], grids[2], (1,) * 6, 6)
+    a = make()
+    a.set_interface_solve(mf.MD_IFACE_LU)
+    a.influence_matrix_set(-3.0, 0)
+    key = a.factor_key(-3.0, 0)
+    assert len(key) == 16 and key != a.factor_key(-4.0, 0) and key != a.factor_key(-3.0, 1)
+    path = tmp_path / (key + ".mffac")
+    a.save_factor(path)
+    b = make()
+    b.set_interface_solve(mf.MD_IFACE_LU)
+    b.load_factor(-3.0, 0, path)
+    rng = np.random.default_rng(9)
+    g, ua, ub, bc = {}, {}, {}, {}
+    for c in a.subdomains():
+        sh = a.shape(*c)
+        g[c] = mf.to_device(rng.standard_normal(sh))
+        ua[c], ub[c] = mf.empty_device(sh), mf.empty_device(sh)
+        bc[c] = tuple(mf.to_device(rng.standard_normal(s)) for s in
+                      ((sh[1] - 2, sh[2] - 2, 2), (sh[0] - 2, sh[2] - 2, 2), (sh[0] - 2, sh[1] - 2, 2)))
+    a.solve(g, ua, bc)
+    b.solve(g, ub, bc)
+    torch.cuda.synchronize()
+    for c in a.subdomains():
+        assert torch.equal(ua[c], ub[c])
+    with pytest.raises(mf.MflopsError):
+        b.load_factor(-4.0, 0, path)
+    data = path.read_bytes()
+    (tmp_path / "cut.mffac").write_bytes(data[: len(data) - 16])
+    with pytest.raises(mf.MflopsError):
+        b.load_factor(-3.0, 0, tmp_path / "cut.mffac")
+    cache = tmp_path / "cache"
+    cache.mkdir()
+    c1 = make()
+    c1.influence_matrix_set(-3.0, 0, cache_dir=cache)
+    assert (cache / (key + ".mffac")).exists()
+    c2 = make()
+    c2.influence_matrix_set(-3.0, 0, cache_dir=cache)
+    uc = {c: mf.empty_device(a.shape(*c)) for c in a.subdomains()}
+    c2.solve(g, uc, bc)
+    ud = {c: mf.empty_device(a.shape(*c)) for c in a.subdomains()}
+    c1.solve(g, ud, bc)
+    torch.cuda.synchronize()
+    for c in a.subdomains():
+        assert torch.equal(uc[c], ud[c])
