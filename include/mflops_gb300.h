@@ -481,7 +481,7 @@ int mf_flow_curl(int nx, int ny, int nz, const double* const* dpsi, double* cons
  * Poisson solve (:1764-1845, 342-393), projection (:1847-1959),
  * extrapolation (:2010-2050), slot rotation and the driver's diagnostics
  * (navier3d.f90:120-261) and the LES term (navier_LES :1225-1455, f :1083-1099).
- * Covered: mpid%dims = 0 (one domain), mapt = 0, pressure types 1 to 4,
+ * Covered: one domain and the multidomain branch (mf_navier_create_md), mapt = 0, pressure types 1 to 4,
  * les_type 0..3, nsubite sub-iterations with the driver's convergence test
  * (testconv, navier3d.f90:366-412).  Velocity Dirichlet and
  * pressure Neumann on all faces; boundary values and sources from the
@@ -505,6 +505,7 @@ typedef struct {
   int les_type;       /* 0 none, 1 Smagorinsky, 2 WALE, 3 sigma (default 0) */
   double les_c;       /* cmd%les_c; the model coefficient is its square (default 0) */
   int nsubite;        /* sub-iterations per time step (default 1) */
+  const char* md_cache_dir;  /* several subdomains: directory of the influence-matrix factor cache, or NULL */
 } mf_navier_params_t;
 /* Fills the reference's defaults (command_line.f90:14-35). */
 int mf_navier_defaults(mf_navier_params_t* p);
@@ -512,6 +513,22 @@ int mf_navier_defaults(mf_navier_params_t* p);
  * grids, all fields zero, time 0. */
 int mf_navier_create(const double* gx, int nx, const double* gy, int ny, const double* gz, int nz,
                      const mf_navier_params_t* p, mf_navier_t** out);
+/* The multidomain branch (mpid%dims /= 0: several subdomains and/or periodic
+ * directions, navier_initialization :2100-2272): nd subdomains per axis
+ * with gridx[i] (nx[i] nodes) ..., as mf_md_create; the velocity and phi
+ * solves go through multidomain_solve (mf_md_solve, FP64; the velocity
+ * influence matrix at sigmau, the pressure one at sigma 0 with the constant
+ * null space), built at creation (or read from p->md_cache_dir).  Sums of
+ * the flow-rate term, diagnostics and testconv run over all subdomains;
+ * subdomain s = i + nd1 (j + nd2 k). */
+int mf_navier_create_md(const int nd[3], const int periods[3], const double* const* gridx, const int* nx,
+                        const double* const* gridy, const int* ny, const double* const* gridz, const int* nz,
+                        const mf_navier_params_t* p, mf_navier_t** out);
+int mf_navier_subdomains(const mf_navier_t* nav, int* count);
+/* Per-subdomain field access (the functions without _sub use subdomain 0). */
+int mf_navier_sub_field(mf_navier_t* nav, int sub, int var, int level, double** ptr);
+int mf_navier_sub_set_field(mf_navier_t* nav, int sub, int var, int level, const double* f, void* stream);
+int mf_navier_sub_get_field(mf_navier_t* nav, int sub, int var, int level, double* f, void* stream);
 int mf_navier_destroy(mf_navier_t* nav);
 /* Field var (0..4 = u, v, w, p, phi) of time level `level` (0 = it(1), the
  * slot the next step writes, ..., 3 = it(nt), the newest): device pointer,

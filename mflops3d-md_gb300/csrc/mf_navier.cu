@@ -300,11 +300,12 @@ __global__ void k_ns_presolve(Lin L, int nx, int ny, int nz, const double* __res
 }
 
 // navier_solve_{u,v,w} right-hand side (class_navier_3D.f90:1612-1635) at the
-// interior points, written as the solver's interior array:
+// interior points, written as the solver's interior array (full = 0) or at
+// the interior points of a full field (full = 1, the multidomain solve):
 // fu = Re (((fac2 x_n + fac3 x_n-1) [+ fac4 x_n-2] [+ grad]) - rhs).
 __global__ void k_ns_fu(int nx, int ny, int nz, const double* __restrict__ x0, const double* __restrict__ x1,
                         const double* __restrict__ x2, double f2, double f3, double f4,
-                        const double* __restrict__ grad, const double* __restrict__ rhs, double rey,
+                        const double* __restrict__ grad, const double* __restrict__ rhs, double rey, int full,
                         double* __restrict__ out) {
   const int n1 = nx - 2, n2 = ny - 2, n3 = nz - 2;
   const long long n = (long long)n1 * n2 * n3;
@@ -318,7 +319,7 @@ __global__ void k_ns_fu(int nx, int ny, int nz, const double* __restrict__ x0, c
   if (x2) f = f + f4 * x2[g];
   if (grad) f = f + grad[g];
   f = f - rhs[g];
-  out[q] = rey * f;
+  out[full ? g : q] = rey * f;
 }
 
 // out = zero_edges(s x)  (navier_phi_rhs, pt <= 2: fac(1) u*).
@@ -397,7 +398,7 @@ __global__ void k_ns_bc_rotrot(Faces F, RotRot R, double rey, double* __restrict
 // d rhs_py/dy + d rhs_pz/dz.
 __global__ void k_ns_fphi(int nx, int ny, int nz, double sigmap, const double* __restrict__ ext,
                           const double* __restrict__ ddx, const double* __restrict__ ddy,
-                          const double* __restrict__ ddz, double* __restrict__ out) {
+                          const double* __restrict__ ddz, int full, double* __restrict__ out) {
   const int n1 = nx - 2, n2 = ny - 2, n3 = nz - 2;
   const long long n = (long long)n1 * n2 * n3;
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -407,7 +408,7 @@ __global__ void k_ns_fphi(int nx, int ny, int nz, double sigmap, const double* _
   const long long g = (i + 1) + (long long)nx * ((j + 1) + (long long)ny * (k + 1));
   double f = sigmap * ext[g];
   f = f + ddx[g] + ddy[g] + ddz[g];
-  out[q] = f;
+  out[full ? g : q] = f;
 }
 
 // In-place field_zero_edges.
@@ -512,6 +513,15 @@ __global__ void __launch_bounds__(kNsThreads) k_ns_sum_parts(const double* __res
   }
 }
 
+// out = x[0] + x[1] + ... + x[n-1] in this order (the per-subdomain sums
+// of the flow-rate integral), one thread.
+__global__ void k_ns_sum_small(const double* __restrict__ x, int n, double* __restrict__ out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double s = 0.0;
+  for (int i = 0; i < n; ++i) s += x[i];
+  out[0] = s;
+}
+
 // Flow-rate term of f for u (class_navier_3D.f90:1140-1164), one thread:
 // err = integrale(extrapol(u)) / integrale(1); on the first call debit = err
 // (1 when <= 1e-10, a single-precision literal) and g = 3 debit; then
@@ -608,30 +618,23 @@ __global__ void k_ns_shift(long long n, double s, double* __restrict__ f) {
 
 using namespace mf;
 
-struct mf_navier {
-  mf_navier_params_t prm;
+// One subdomain of the step: its fields, work arrays and coefficients (one
+// domain: the whole box).
+struct NsDom {
   int nx = 0, ny = 0, nz = 0, n1 = 0, n2 = 0, n3 = 0;
   long long np = 0, nin = 0;
-  double fac[4] = {0, 0, 0, 0};
-  double sigmau = 0.0, sigmap = 0.0, time = 0.0;
-  int it[kNt] = {0, 1, 2, 3};
-  int subite = 1, subiterations = 0;
-  bool nl_ok[kNt] = {false, false, false, false};
-  int rhs_cur = 0;
   mf_der_t *dcx = nullptr, *dcy = nullptr, *dcz = nullptr;
-  // velocity solver sets scu, scv, scw (as the reference keeps them) and the
-  // pressure set; the three velocity solves run on forked streams
-  mf_solver3d_t *scu = nullptr, *scv = nullptr, *scw = nullptr, *scp = nullptr;
+  // one domain: velocity solver sets scu, scv, scw (as the reference keeps
+  // them; the three velocity solves run on forked streams) and the pressure set
+  mf_solver3d_t* sc[4] = {nullptr, nullptr, nullptr, nullptr};
   mf_les_t* les = nullptr;  // les_type != 0
   DevBuf nu;                // eddy viscosity of the step
-  cudaStream_t side[2] = {nullptr, nullptr};
-  cudaEvent_t fork = nullptr, join[2] = {nullptr, nullptr};
   DevBuf fields;  // [5 vars][kNt slots] fields
   DevBuf nl;      // [3][kNt] cached nonlinear terms
   DevBuf rhs;     // [3][2] rhs_u(1), rhs_u(2) ...
   DevBuf rp;      // rhs_px, rhs_py, rhs_pz
   DevBuf tmp;     // 18 work fields
-  DevBuf fin;     // interior right-hand sides of the solves (three)
+  DevBuf fin;     // right-hand sides of the solves: three interior arrays (one domain) or a full field
   DevBuf exact;   // u, v, p, rhsu, rhsv of the exact solution
   DevBuf bcex;    // exact face values of u, v, w
   DevBuf bc;      // face values of u, v, w, phi
@@ -639,11 +642,9 @@ struct mf_navier {
   DevBuf wts;     // half widths wx, wy, wz
   DevBuf part;    // partial sums
   DevBuf sums;    // summed values
-  DevBuf state;   // flow-rate term: g, debit, initialised
   DevBuf sub;     // last sub-iterate u, v, w, p (nsubite > 1)
   Faces faces{};
-  double reft = 0.0;  // integrale(1)
-  double err_vts = 0.0, err_pre = 0.0;
+  double reft = 0.0;  // integrale(1) over this subdomain
 
   double* F(int var, int slot) const { return fields.as<double>() + ((size_t)var * kNt + slot) * np; }
   double* NL(int c, int slot) const { return nl.as<double>() + ((size_t)c * kNt + slot) * np; }
@@ -656,6 +657,35 @@ struct mf_navier {
     const double* w = wts.as<double>();
     return Weights{w, w + nx, w + nx + ny, nx, ny, nz};
   }
+  void release() {
+    mf_der_destroy(dcx);
+    mf_der_destroy(dcy);
+    mf_der_destroy(dcz);
+    for (mf_solver3d_t* s : sc) mf_solver3d_destroy(s);
+    mf_les_destroy(les);
+    for (DevBuf* b : {&nu, &fields, &nl, &rhs, &rp, &tmp, &fin, &exact, &bcex, &bc, &grid, &wts, &part, &sums, &sub})
+      b->release();
+  }
+};
+
+struct mf_navier {
+  mf_navier_params_t prm;
+  double fac[4] = {0, 0, 0, 0};
+  double sigmau = 0.0, sigmap = 0.0, time = 0.0;
+  int it[kNt] = {0, 1, 2, 3};
+  int subite = 1, subiterations = 0;
+  bool nl_ok[kNt] = {false, false, false, false};
+  int rhs_cur = 0;
+  std::vector<NsDom> dom;  // subdomains, index i + nd1 (j + nd2 k)
+  int nd[3] = {1, 1, 1};
+  mf_md_t *mdu = nullptr, *mdp = nullptr;  // multidomain: velocity and pressure influence-matrix solves
+  cudaStream_t side[2] = {nullptr, nullptr};
+  cudaEvent_t fork = nullptr, join[2] = {nullptr, nullptr};
+  DevBuf state;  // flow-rate term: g, debit, initialised
+  DevBuf dsum;   // per-subdomain sums of the flow-rate integral, then their total
+  double reft = 0.0;  // integrale(1) over all subdomains
+  double err_vts = 0.0, err_pre = 0.0;
+  bool md() const { return mdu != nullptr; }
 };
 
 namespace {
@@ -665,10 +695,10 @@ constexpr int kVarU = 0, kVarP = 3, kVarPhi = 4;
 // extrapol of var (navier_extrapol) of the given order: -1 -> it(1); 1 ->
 // it(nt); 2 -> 2 it(nt) - it(nt-1); 3 -> 3 it(nt) - 3 it(nt-1) + it(nt-2);
 // else 0; from the second sub-iteration on it(1) whatever the order.
-Lin extrapol_of(const mf_navier* nv, int order, double* (*slot_ptr)(const mf_navier*, int, int), int var) {
+Lin extrapol_of(const mf_navier* nv, const NsDom& d, int order, bool nonlin, int var) {
   Lin L{};
   const int* it = nv->it;
-  auto P = [&](int s) { return slot_ptr(nv, var, s); };
+  auto P = [&](int s) { return nonlin ? d.NL(var, s) : d.F(var, s); };
   if (nv->subite > 1) {  // from the second sub-iteration on: the current iterate
     L.m = 1; L.c[0] = 1.0; L.a[0] = P(it[0]);
   } else if (order == -1) {
@@ -686,20 +716,29 @@ Lin extrapol_of(const mf_navier* nv, int order, double* (*slot_ptr)(const mf_nav
   return L;
 }
 
-double* field_ptr(const mf_navier* nv, int var, int slot) { return nv->F(var, slot); }
-double* nl_ptr(const mf_navier* nv, int c, int slot) { return nv->NL(c, slot); }
+// Slots whose nonlinear terms extrapol('v') reads.
+int extrapol_slots(const mf_navier* nv, int order, int slots[3]) {
+  const int* it = nv->it;
+  if (nv->subite > 1 || order == -1) {
+    slots[0] = it[0];
+    return 1;
+  }
+  if (order < 1 || order > 3) return 0;
+  for (int t = 0; t < order; ++t) slots[t] = it[kNt - 1 - t];
+  return order;
+}
 
 int launch_check(const char* what) {
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? MF_OK : cuda_error(e, what);
 }
 
-int extrapol_into(const mf_navier* nv, const Lin& L, double* out, cudaStream_t st) {
-  k_ns_extrapol<<<ns_blocks(nv->np), kNsThreads, 0, st>>>(L, nv->nx, nv->ny, nv->nz, out);
+int extrapol_into(const NsDom& d, const Lin& L, double* out, cudaStream_t st) {
+  k_ns_extrapol<<<ns_blocks(d.np), kNsThreads, 0, st>>>(L, d.nx, d.ny, d.nz, out);
   return launch_check("k_ns_extrapol");
 }
 
-// Independent derivative sweeps of the step's fields, launched together
+// Independent derivative sweeps of a subdomain's fields, launched together
 // (mf_der_apply_many): the lines of one 128 x 129 x 128 sweep alone fill a
 // GB300 only to ~3 warps per SM.
 struct Sweeps {
@@ -708,75 +747,80 @@ struct Sweeps {
   int axis[9], order[9];
   const double* f[9];
   double* df[9];
-  void add(const mf_navier* nv, int ax, const double* in, double* out, int ord = 1) {
-    dc[n] = ax == 0 ? nv->dcx : ax == 1 ? nv->dcy : nv->dcz;
+  void add(const NsDom& d, int ax, const double* in, double* out, int ord = 1) {
+    dc[n] = ax == 0 ? d.dcx : ax == 1 ? d.dcy : d.dcz;
     axis[n] = ax;
     order[n] = ord;
     f[n] = in;
     df[n] = out;
     ++n;
   }
-  int run(const mf_navier* nv, cudaStream_t st) const {
-    return mf_der_apply_many(n, dc, axis, order, f, df, nv->nx, nv->ny, nv->nz, st);
+  int run(const NsDom& d, cudaStream_t st) const {
+    return mf_der_apply_many(n, dc, axis, order, f, df, d.nx, d.ny, d.nz, st);
   }
 };
 
 // Gradient of f: d/dx, d/dy, d/dz into out0, out1, out2.
-int gradient(const mf_navier* nv, const double* f, double* out0, double* out1, double* out2, cudaStream_t st) {
+int gradient(const NsDom& d, const double* f, double* out0, double* out1, double* out2, cudaStream_t st) {
   Sweeps S;
-  S.add(nv, 0, f, out0);
-  S.add(nv, 1, f, out1);
-  S.add(nv, 2, f, out2);
-  return S.run(nv, st);
+  S.add(d, 0, f, out0);
+  S.add(d, 1, f, out1);
+  S.add(d, 2, f, out2);
+  return S.run(d, st);
 }
 
 // navier_nonlinear of the three components at `slot` into their cache
 // entries: nine sweeps d x_c / d x_d in one launch, and for nlt 2 the nine
 // products x_c u_d and their sweeps in another.
-int nonlinear_slot(mf_navier* nv, int slot, cudaStream_t st) {
-  const long long n = nv->np;
-  const double *u = nv->F(0, slot), *v = nv->F(1, slot), *w = nv->F(2, slot);
-  const long long xstride = nv->F(1, slot) - nv->F(0, slot);
-  const long long ostride = nv->NL(1, slot) - nv->NL(0, slot);
+int nonlinear_slot(const mf_navier* nv, NsDom& d, int slot, cudaStream_t st) {
+  const long long n = d.np;
+  const double *u = d.F(0, slot), *v = d.F(1, slot), *w = d.F(2, slot);
+  const long long xstride = d.F(1, slot) - d.F(0, slot);
+  const long long ostride = d.NL(1, slot) - d.NL(0, slot);
   const dim3 grid(ns_blocks(n), 3);
+  const int nlt = nv->prm.nlt;
   int rc;
-  if (nv->prm.nlt == 1 || nv->prm.nlt == 2) {
+  if (nlt == 1 || nlt == 2) {
     Sweeps S;
-    for (int d = 0; d < 3; ++d)
-      for (int c = 0; c < 3; ++c) S.add(nv, d, nv->F(c, slot), nv->T(3 * d + c));
-    if ((rc = S.run(nv, st))) return rc;
+    for (int a = 0; a < 3; ++a)
+      for (int c = 0; c < 3; ++c) S.add(d, a, d.F(c, slot), d.T(3 * a + c));
+    if ((rc = S.run(d, st))) return rc;
   }
-  k_ns_advect<<<grid, kNsThreads, 0, st>>>(n, nv->prm.nlt, u, v, w, nv->T(0), nv->NL(0, slot), ostride);
+  k_ns_advect<<<grid, kNsThreads, 0, st>>>(n, nlt, u, v, w, d.T(0), d.NL(0, slot), ostride);
   if ((rc = launch_check("k_ns_advect"))) return rc;
-  if (nv->prm.nlt == 2) {
-    k_ns_products<<<grid, kNsThreads, 0, st>>>(n, u, xstride, u, v, w, nv->T(9));
+  if (nlt == 2) {
+    k_ns_products<<<grid, kNsThreads, 0, st>>>(n, u, xstride, u, v, w, d.T(9));
     if ((rc = launch_check("k_ns_products"))) return rc;
     Sweeps S;
-    for (int d = 0; d < 3; ++d)
-      for (int c = 0; c < 3; ++c) S.add(nv, d, nv->T(9 + 3 * d + c), nv->T(3 * d + c));
-    if ((rc = S.run(nv, st))) return rc;
-    k_ns_skew<<<grid, kNsThreads, 0, st>>>(n, nv->T(0), nv->NL(0, slot), ostride);
+    for (int a = 0; a < 3; ++a)
+      for (int c = 0; c < 3; ++c) S.add(d, a, d.T(9 + 3 * a + c), d.T(3 * a + c));
+    if ((rc = S.run(d, st))) return rc;
+    k_ns_skew<<<grid, kNsThreads, 0, st>>>(n, d.T(0), d.NL(0, slot), ostride);
     if ((rc = launch_check("k_ns_skew"))) return rc;
   }
   return MF_OK;
 }
 
-int solve(mf_navier* nv, mf_solver3d_t* sc, const double* rhs, double sigma, double* solf, const double* bc3,
-          cudaStream_t st) {
-  const double* bx = bc3;
-  const double* by = bc3 + nv->faces.sx;
-  const double* bz = bc3 + nv->faces.sx + nv->faces.sy;
-  if (nv->prm.precision == MF_PREC_FP64)
-    return mf_solve_3d(sc, rhs, sigma, solf, bx, by, bz, nv->n1, nv->n2, nv->n3, st);
-  return mf_solve_3d_mixed(sc, rhs, sigma, solf, bx, by, bz, nv->n1, nv->n2, nv->n3, nv->prm.precision,
-                           nv->prm.refine, st);
+// Face-array pointers of variable c (0..3 = u, v, w, phi) of every subdomain.
+struct FacePtrs {
+  std::vector<const double*> x, y, z;
+};
+FacePtrs face_ptrs(const mf_navier* nv, int c) {
+  FacePtrs p;
+  for (const NsDom& d : nv->dom) {
+    const double* b = d.BC(c);
+    p.x.push_back(b);
+    p.y.push_back(b + d.faces.sx);
+    p.z.push_back(b + d.faces.sx + d.faces.sy);
+  }
+  return p;
 }
 
-// Weighted sum of f into nv->sums[0] (device).
-int wsum(mf_navier* nv, const double* f, cudaStream_t st) {
-  const int groups = (nv->ny + kWRows - 1) / kWRows;
-  k_ns_wsum<<<dim3(nv->nz, groups), kNsThreads, 0, st>>>(nv->weights(), f, nv->part.as<double>());
-  k_ns_sum_parts<<<1, kNsThreads, 0, st>>>(nv->part.as<double>(), nv->nz * groups, 1, nv->sums.as<double>());
+// Weighted sum of f over subdomain d into d.sums[0] (device).
+int wsum(NsDom& d, const double* f, double* out, cudaStream_t st) {
+  const int groups = (d.ny + kWRows - 1) / kWRows;
+  k_ns_wsum<<<dim3(d.nz, groups), kNsThreads, 0, st>>>(d.weights(), f, d.part.as<double>());
+  k_ns_sum_parts<<<1, kNsThreads, 0, st>>>(d.part.as<double>(), d.nz * groups, 1, out);
   return launch_check("k_ns_wsum");
 }
 
@@ -784,211 +828,307 @@ int wsum(mf_navier* nv, const double* f, cudaStream_t st) {
 
 namespace {
 
-// One time step without the rotation (navier3d.f90:57-102, nsubite = 1).
-int ns_step(mf_navier* nv, cudaStream_t st) {
+// One domain: the solver's own solve of the interior right-hand side rhs.
+int solve_one(const mf_navier* nv, const NsDom& d, mf_solver3d_t* sc, const double* rhs, double sigma,
+              double* solf, int c, cudaStream_t st) {
+  const double* b = d.BC(c);
+  const double* bx = b;
+  const double* by = b + d.faces.sx;
+  const double* bz = b + d.faces.sx + d.faces.sy;
+  if (nv->prm.precision == MF_PREC_FP64) return mf_solve_3d(sc, rhs, sigma, solf, bx, by, bz, d.n1, d.n2, d.n3, st);
+  return mf_solve_3d_mixed(sc, rhs, sigma, solf, bx, by, bz, d.n1, d.n2, d.n3, nv->prm.precision, nv->prm.refine,
+                           st);
+}
+
+// Multidomain: one multidomain_solve of variable var (face arrays of c) with
+// the full right-hand-side fields in each subdomain's fin.
+int solve_md(mf_navier* nv, mf_md_t* md, int var, int c, int slot, cudaStream_t st) {
+  std::vector<const double*> g;
+  std::vector<double*> u;
+  for (NsDom& d : nv->dom) {
+    g.push_back(d.fin.as<double>());
+    u.push_back(d.F(var, slot));
+  }
+  FacePtrs b = face_ptrs(nv, c);
+  return mf_md_solve(md, g.data(), u.data(), b.x.data(), b.y.data(), b.z.data(), st);
+}
+
+// navier_solve_{u,v,w}: the three Helmholtz solves into slot it(1); with
+// grad, each subdomain's T(1 + c) is added to the right-hand side.  One
+// domain: u on the caller's stream, v and w on forked streams joined back.
+int velocity_solves(mf_navier* nv, bool grad, cudaStream_t st) {
   const mf_navier_params_t& P = nv->prm;
-  const int* it = nv->it;
-  const int nw = it[0], s0 = it[kNt - 1], s1 = it[kNt - 2], s2 = it[kNt - 3];
-  const double fac1 = nv->fac[0];
-  const unsigned gb = ns_blocks(nv->np);
-  const long long ftot = nv->faces.sx + nv->faces.sy + nv->faces.sz;
-  const unsigned fb = ns_blocks(ftot);
+  const int nw = nv->it[0], s0 = nv->it[kNt - 1], s1 = nv->it[kNt - 2], s2 = nv->it[kNt - 3];
   int rc;
-  // presolve: nonlinear terms of the slots that extrapol('v') reads
-  const Lin nlv0 = extrapol_of(nv, P.tou, nl_ptr, 0);
-  for (int t = 0; t < nlv0.m; ++t) {
-    int slot = 0;
-    while (nv->NL(0, slot) != nlv0.a[t]) ++slot;
-    if (!nv->nl_ok[slot]) {
-      if ((rc = nonlinear_slot(nv, slot, st))) return rc;
-      nv->nl_ok[slot] = true;
+  auto fu = [&](NsDom& d, int c, int full, double* out, cudaStream_t sc) {
+    k_ns_fu<<<ns_blocks(full ? d.np : d.nin), kNsThreads, 0, sc>>>(
+        d.nx, d.ny, d.nz, d.F(c, s0), d.F(c, s1), P.tou == 3 ? d.F(c, s2) : nullptr, nv->fac[1], nv->fac[2],
+        nv->fac[3], grad ? d.T(1 + c) : nullptr, d.RHS(c, nv->rhs_cur), P.reynolds, full, out);
+    return launch_check("k_ns_fu");
+  };
+  if (nv->md()) {
+    for (int c = 0; c < 3; ++c) {
+      for (NsDom& d : nv->dom)
+        if ((rc = fu(d, c, 1, d.fin.as<double>(), st))) return rc;
+      if ((rc = solve_md(nv, nv->mdu, c, c, nw, st))) return rc;
     }
+    return MF_OK;
   }
-  // flow-rate term of f for u
-  const double* g = nullptr;
-  if (P.flow_rate) {
-    if ((rc = extrapol_into(nv, extrapol_of(nv, P.tou, field_ptr, kVarU), nv->T(0), st)) ||
-        (rc = wsum(nv, nv->T(0), st)))
+  NsDom& d = nv->dom[0];
+  MF_CUDA(cudaEventRecord(nv->fork, st));
+  for (int q = 0; q < 2; ++q) MF_CUDA(cudaStreamWaitEvent(nv->side[q], nv->fork, 0));
+  for (int c = 0; c < 3; ++c) {
+    cudaStream_t sc = c == 0 ? st : nv->side[c - 1];
+    double* rhs = d.fin.as<double>() + (size_t)c * d.nin;
+    if ((rc = fu(d, c, 0, rhs, sc)) || (rc = solve_one(nv, d, d.sc[c], rhs, nv->sigmau, d.F(c, nw), c, sc)))
       return rc;
-    k_ns_flow<<<1, 1, 0, st>>>(nv->sums.as<double>(), nv->reft, fac1, (double)1e-10f, nv->state.as<double>());
-    if ((rc = launch_check("k_ns_flow"))) return rc;
-    g = nv->state.as<double>();
   }
-  // navier_LES on the newest level and the stress sweeps of f
+  for (int q = 0; q < 2; ++q) {
+    MF_CUDA(cudaEventRecord(nv->join[q], nv->side[q]));
+    MF_CUDA(cudaStreamWaitEvent(st, nv->join[q], 0));
+  }
+  return MF_OK;
+}
+
+// Presolve of one subdomain: navier_LES and the stress sweeps of f, then
+// rhs = f - extrapol(nonlinear) for u, v, w (class_navier_3D.f90:1528-1595).
+int presolve(const mf_navier* nv, NsDom& d, const double* g, cudaStream_t st) {
+  const mf_navier_params_t& P = nv->prm;
+  const int s0 = nv->it[kNt - 1];
+  const unsigned gb = ns_blocks(d.np);
+  int rc;
   if (P.les_type != 0) {
     Sweeps S;
     for (int j = 0; j < 3; ++j)
-      for (int i = 0; i < 3; ++i) S.add(nv, j, nv->F(i, s0), nv->T(3 * j + i));
-    if ((rc = S.run(nv, st))) return rc;
+      for (int i = 0; i < 3; ++i) S.add(d, j, d.F(i, s0), d.T(3 * j + i));
+    if ((rc = S.run(d, st))) return rc;
     const double* du[9];
     for (int i = 0; i < 3; ++i)
-      for (int j = 0; j < 3; ++j) du[3 * i + j] = nv->T(3 * j + i);
-    if ((rc = mf_les_nu(nv->les, P.les_type, P.les_c * P.les_c, du, nv->nu.as<double>(), st))) return rc;
-    k_ns_les_products<<<gb, kNsThreads, 0, st>>>(nv->np, nv->nu.as<double>(), nv->T(0), nv->T(9));
+      for (int j = 0; j < 3; ++j) du[3 * i + j] = d.T(3 * j + i);
+    if ((rc = mf_les_nu(d.les, P.les_type, P.les_c * P.les_c, du, d.nu.as<double>(), st))) return rc;
+    k_ns_les_products<<<gb, kNsThreads, 0, st>>>(d.np, d.nu.as<double>(), d.T(0), d.T(9));
     if ((rc = launch_check("k_ns_les_products"))) return rc;
     Sweeps E;
     for (int j = 0; j < 3; ++j)
-      for (int i = 0; i < 3; ++i) E.add(nv, j, nv->T(9 + 3 * j + i), nv->T(3 * j + i));
-    if ((rc = E.run(nv, st))) return rc;
+      for (int i = 0; i < 3; ++i) E.add(d, j, d.T(9 + 3 * j + i), d.T(3 * j + i));
+    if ((rc = E.run(d, st))) return rc;
   }
-  nv->rhs_cur ^= 1;  // rhs(2) = rhs(1): the other buffer keeps the previous step's
   for (int c = 0; c < 3; ++c) {
-    const double* src = c == 0 ? nv->EX(3) : c == 1 ? nv->EX(4) : nullptr;
-    k_ns_presolve<<<gb, kNsThreads, 0, st>>>(extrapol_of(nv, P.tou, nl_ptr, c), nv->nx, nv->ny, nv->nz, src,
-                                             P.les_type != 0 ? nv->T(c) : nullptr, c == 0 ? g : nullptr,
-                                             nv->RHS(c, nv->rhs_cur));
+    const double* src = c == 0 ? d.EX(3) : c == 1 ? d.EX(4) : nullptr;
+    k_ns_presolve<<<gb, kNsThreads, 0, st>>>(extrapol_of(nv, d, P.tou, true, c), d.nx, d.ny, d.nz, src,
+                                             P.les_type != 0 ? d.T(c) : nullptr, c == 0 ? g : nullptr,
+                                             d.RHS(c, nv->rhs_cur));
     if ((rc = launch_check("k_ns_presolve"))) return rc;
   }
-  // velocity boundary values (+ gradient of extrapol(phi) for pt = 1)
-  const Lin ephi = extrapol_of(nv, P.top - 1, field_ptr, kVarPhi);
-  if (P.pt == 1) {
-    if ((rc = extrapol_into(nv, ephi, nv->T(0), st)) || (rc = gradient(nv, nv->T(0), nv->T(1), nv->T(2), nv->T(3), st)))
+  return MF_OK;
+}
+
+// Velocity boundary values (+ gradient of extrapol(phi) for pt = 1).
+int velocity_bc(const mf_navier* nv, NsDom& d, cudaStream_t st) {
+  const double fac1 = nv->fac[0];
+  const unsigned fb = ns_blocks(d.faces.sx + d.faces.sy + d.faces.sz);
+  int rc;
+  if (nv->prm.pt == 1) {
+    if ((rc = extrapol_into(d, extrapol_of(nv, d, nv->prm.top - 1, false, kVarPhi), d.T(0), st)) ||
+        (rc = gradient(d, d.T(0), d.T(1), d.T(2), d.T(3), st)))
       return rc;
-    k_ns_bc_velocity<<<fb, kNsThreads, 0, st>>>(nv->faces, nv->bcex.as<double>(), nv->T(1), nv->T(2), nv->T(3),
-                                                fac1, nv->bc.as<double>());
+    k_ns_bc_velocity<<<fb, kNsThreads, 0, st>>>(d.faces, d.bcex.as<double>(), d.T(1), d.T(2), d.T(3), fac1,
+                                                d.bc.as<double>());
   } else {
-    k_ns_bc_velocity<<<fb, kNsThreads, 0, st>>>(nv->faces, nv->bcex.as<double>(), nullptr, nullptr, nullptr,
-                                                fac1, nv->bc.as<double>());
+    k_ns_bc_velocity<<<fb, kNsThreads, 0, st>>>(d.faces, d.bcex.as<double>(), nullptr, nullptr, nullptr, fac1,
+                                                d.bc.as<double>());
   }
-  if ((rc = launch_check("k_ns_bc_velocity"))) return rc;
-  const unsigned ib = ns_blocks(nv->nin);
-  // navier_solve_{u,v,w}: the three Helmholtz solves, u on the caller's
-  // stream, v and w on forked streams joined back; grad (or null) is the base
-  // of the three pressure-gradient fields added to the right-hand sides
-  auto velocity_solves = [&](const double* grad) -> int {
-    int r;
-    MF_CUDA(cudaEventRecord(nv->fork, st));
-    for (int q = 0; q < 2; ++q) MF_CUDA(cudaStreamWaitEvent(nv->side[q], nv->fork, 0));
-    mf_solver3d_t* sets[3] = {nv->scu, nv->scv, nv->scw};
-    for (int c = 0; c < 3; ++c) {
-      cudaStream_t sc = c == 0 ? st : nv->side[c - 1];
-      double* rhs = nv->fin.as<double>() + (size_t)c * nv->nin;
-      k_ns_fu<<<ib, kNsThreads, 0, sc>>>(nv->nx, nv->ny, nv->nz, nv->F(c, s0), nv->F(c, s1),
-                                         P.tou == 3 ? nv->F(c, s2) : nullptr, nv->fac[1], nv->fac[2], nv->fac[3],
-                                         grad ? grad + (size_t)c * nv->np : nullptr, nv->RHS(c, nv->rhs_cur),
-                                         P.reynolds, rhs);
-      if ((r = launch_check("k_ns_fu")) || (r = solve(nv, sets[c], rhs, nv->sigmau, nv->F(c, nw), nv->BC(c), sc)))
-        return r;
-    }
-    for (int q = 0; q < 2; ++q) {
-      MF_CUDA(cudaEventRecord(nv->join[q], nv->side[q]));
-      MF_CUDA(cudaStreamWaitEvent(st, nv->join[q], 0));
-    }
-    return MF_OK;
-  };
-  // pt = 1, 2: velocity before the pressure (pt = 2: + gradient of extrapol(p))
-  if (P.pt == 2) {
-    if ((rc = extrapol_into(nv, extrapol_of(nv, P.top - 1, field_ptr, kVarP), nv->T(0), st)) ||
-        (rc = gradient(nv, nv->T(0), nv->T(1), nv->T(2), nv->T(3), st)))
-      return rc;
-  }
-  if (P.pt <= 2 && (rc = velocity_solves(P.pt == 2 ? nv->T(1) : nullptr))) return rc;
-  // pressure increment: rhs_p (navier_phi_rhs), Poisson solve with Neumann data
+  return launch_check("k_ns_bc_velocity");
+}
+
+// Presolve phi and the right-hand side and Neumann data of the phi solve
+// (navier_phi_rhs, navier_solve_phi, navier_bc_pressure, add_boundary_rotrot).
+int phi_stage(const mf_navier* nv, NsDom& d, cudaStream_t st) {
+  const mf_navier_params_t& P = nv->prm;
+  const int nw = nv->it[0], s0 = nv->it[kNt - 1], s1 = nv->it[kNt - 2], s2 = nv->it[kNt - 3];
+  const double fac1 = nv->fac[0];
+  const unsigned gb = ns_blocks(d.np), fb = ns_blocks(d.faces.sx + d.faces.sy + d.faces.sz);
+  int rc;
   for (int c = 0; c < 3; ++c) {
     if (P.pt <= 2)
-      k_ns_scale<<<gb, kNsThreads, 0, st>>>(nv->nx, nv->ny, nv->nz, fac1, nv->F(c, nw), nv->RP(c));
+      k_ns_scale<<<gb, kNsThreads, 0, st>>>(d.nx, d.ny, d.nz, fac1, d.F(c, nw), d.RP(c));
     else
-      k_ns_phi_rhs<<<gb, kNsThreads, 0, st>>>(nv->nx, nv->ny, nv->nz,
-                                              P.pt == 4 && nv->subite > 1 ? 5 : P.pt, nv->RHS(c, nv->rhs_cur),
-                                              nv->RHS(c, nv->rhs_cur ^ 1), nv->F(c, s0), nv->F(c, s1),
-                                              nv->F(c, s2), nv->F(c, nw), nv->fac[0], nv->fac[1], nv->fac[2],
-                                              nv->fac[3], nv->RP(c));
+      k_ns_phi_rhs<<<gb, kNsThreads, 0, st>>>(d.nx, d.ny, d.nz, P.pt == 4 && nv->subite > 1 ? 5 : P.pt,
+                                              d.RHS(c, nv->rhs_cur), d.RHS(c, nv->rhs_cur ^ 1), d.F(c, s0),
+                                              d.F(c, s1), d.F(c, s2), d.F(c, nw), nv->fac[0], nv->fac[1],
+                                              nv->fac[2], nv->fac[3], d.RP(c));
     if ((rc = launch_check("k_ns_phi_rhs"))) return rc;
   }
   {
     Sweeps S;
-    for (int c = 0; c < 3; ++c) S.add(nv, c, nv->RP(c), nv->T(4 + c));
-    if ((rc = S.run(nv, st)) || (rc = extrapol_into(nv, ephi, nv->T(0), st))) return rc;
+    for (int c = 0; c < 3; ++c) S.add(d, c, d.RP(c), d.T(4 + c));
+    if ((rc = S.run(d, st)) ||
+        (rc = extrapol_into(d, extrapol_of(nv, d, P.top - 1, false, kVarPhi), d.T(0), st)))
+      return rc;
   }
-  k_ns_fphi<<<ib, kNsThreads, 0, st>>>(nv->nx, nv->ny, nv->nz, nv->sigmap, nv->T(0), nv->T(4), nv->T(5),
-                                       nv->T(6), nv->fin.as<double>());
-  k_ns_bc_phi<<<fb, kNsThreads, 0, st>>>(nv->faces, nv->RP(0), nv->RP(1), nv->RP(2), nv->bc.as<double>(), fac1,
-                                         nv->BC(3));
+  const int full = nv->md() ? 1 : 0;
+  k_ns_fphi<<<ns_blocks(full ? d.np : d.nin), kNsThreads, 0, st>>>(d.nx, d.ny, d.nz, nv->sigmap, d.T(0), d.T(4),
+                                                                    d.T(5), d.T(6), full, d.fin.as<double>());
+  k_ns_bc_phi<<<fb, kNsThreads, 0, st>>>(d.faces, d.RP(0), d.RP(1), d.RP(2), d.bc.as<double>(), fac1, d.BC(3));
   if ((rc = launch_check("k_ns_fphi"))) return rc;
   if (P.pt == 3) {
     // add_boundary_rotrot: extrapolated velocity (T7..T9), its first
     // derivatives A, B, C (T10..T12) and six second derivatives, then the
     // sums, their three sweeps and the face update
     for (int c = 0; c < 3; ++c)
-      if ((rc = extrapol_into(nv, extrapol_of(nv, P.top - 1, field_ptr, c), nv->T(7 + c), st))) return rc;
+      if ((rc = extrapol_into(d, extrapol_of(nv, d, P.top - 1, false, c), d.T(7 + c), st))) return rc;
     Sweeps S;
-    S.add(nv, 0, nv->T(7), nv->T(10));
-    S.add(nv, 1, nv->T(8), nv->T(11));
-    S.add(nv, 2, nv->T(9), nv->T(12));
-    S.add(nv, 1, nv->T(7), nv->T(13), 2);  // u_yy
-    S.add(nv, 2, nv->T(7), nv->T(14), 2);  // u_zz
-    S.add(nv, 0, nv->T(8), nv->T(15), 2);  // v_xx
-    S.add(nv, 2, nv->T(8), nv->T(16), 2);  // v_zz
-    S.add(nv, 0, nv->T(9), nv->T(17), 2);  // w_xx
-    S.add(nv, 1, nv->T(9), nv->T(1), 2);   // w_yy
-    if ((rc = S.run(nv, st))) return rc;
-    k_ns_rot_sums<<<gb, kNsThreads, 0, st>>>(nv->np, nv->T(10), nv->T(11), nv->T(12), nv->T(2), nv->T(3), nv->T(4));
+    S.add(d, 0, d.T(7), d.T(10));
+    S.add(d, 1, d.T(8), d.T(11));
+    S.add(d, 2, d.T(9), d.T(12));
+    S.add(d, 1, d.T(7), d.T(13), 2);  // u_yy
+    S.add(d, 2, d.T(7), d.T(14), 2);  // u_zz
+    S.add(d, 0, d.T(8), d.T(15), 2);  // v_xx
+    S.add(d, 2, d.T(8), d.T(16), 2);  // v_zz
+    S.add(d, 0, d.T(9), d.T(17), 2);  // w_xx
+    S.add(d, 1, d.T(9), d.T(1), 2);   // w_yy
+    if ((rc = S.run(d, st))) return rc;
+    k_ns_rot_sums<<<gb, kNsThreads, 0, st>>>(d.np, d.T(10), d.T(11), d.T(12), d.T(2), d.T(3), d.T(4));
     if ((rc = launch_check("k_ns_rot_sums"))) return rc;
     Sweeps S2;
-    S2.add(nv, 0, nv->T(2), nv->T(5));
-    S2.add(nv, 1, nv->T(3), nv->T(6));
-    S2.add(nv, 2, nv->T(4), nv->T(0));
-    if ((rc = S2.run(nv, st))) return rc;
-    RotRot R{{nv->T(5), nv->T(6), nv->T(0)}, {nv->T(13), nv->T(14), nv->T(15), nv->T(16), nv->T(17), nv->T(1)}};
-    k_ns_bc_rotrot<<<fb, kNsThreads, 0, st>>>(nv->faces, R, P.reynolds, nv->BC(3));
+    S2.add(d, 0, d.T(2), d.T(5));
+    S2.add(d, 1, d.T(3), d.T(6));
+    S2.add(d, 2, d.T(4), d.T(0));
+    if ((rc = S2.run(d, st))) return rc;
+    RotRot R{{d.T(5), d.T(6), d.T(0)}, {d.T(13), d.T(14), d.T(15), d.T(16), d.T(17), d.T(1)}};
+    k_ns_bc_rotrot<<<fb, kNsThreads, 0, st>>>(d.faces, R, P.reynolds, d.BC(3));
     if ((rc = launch_check("k_ns_bc_rotrot"))) return rc;
   }
-  if ((rc = solve(nv, nv->scp, nv->fin.as<double>(), nv->sigmap, nv->F(kVarPhi, nw), nv->BC(3), st))) return rc;
-  // projection
-  k_ns_zero_edges<<<gb, kNsThreads, 0, st>>>(nv->nx, nv->ny, nv->nz, nv->F(kVarPhi, nw));
+  return MF_OK;
+}
+
+// navier_projection (class_navier_3D.f90:1847-1959).
+int projection(const mf_navier* nv, NsDom& d, cudaStream_t st) {
+  const mf_navier_params_t& P = nv->prm;
+  const int nw = nv->it[0];
+  const unsigned gb = ns_blocks(d.np);
+  int rc;
+  k_ns_zero_edges<<<gb, kNsThreads, 0, st>>>(d.nx, d.ny, d.nz, d.F(kVarPhi, nw));
   if ((rc = launch_check("k_ns_zero_edges"))) return rc;
   const bool add_p = P.pt == 2 || P.pt == 4;
-  if (add_p && (rc = extrapol_into(nv, extrapol_of(nv, P.top - 1, field_ptr, kVarP), nv->T(0), st))) return rc;
+  if (add_p && (rc = extrapol_into(d, extrapol_of(nv, d, P.top - 1, false, kVarP), d.T(0), st))) return rc;
   if (P.pt == 4)
     for (int c = 0; c < 3; ++c)
-      if ((rc = extrapol_into(nv, extrapol_of(nv, P.top - 1, field_ptr, c), nv->T(7 + c), st))) return rc;
+      if ((rc = extrapol_into(d, extrapol_of(nv, d, P.top - 1, false, c), d.T(7 + c), st))) return rc;
   {
     // divergence (of u*, pt <= 2; of the extrapolated velocity, pt = 4) and
     // gradient of phi: up to six sweeps in one launch
     Sweeps S;
     if (P.pt <= 2)
-      for (int c = 0; c < 3; ++c) S.add(nv, c, nv->F(c, nw), nv->T(1 + c));
+      for (int c = 0; c < 3; ++c) S.add(d, c, d.F(c, nw), d.T(1 + c));
     else if (P.pt == 4)
-      for (int c = 0; c < 3; ++c) S.add(nv, c, nv->T(7 + c), nv->T(1 + c));
-    for (int c = 0; c < 3; ++c) S.add(nv, c, nv->F(kVarPhi, nw), nv->T(4 + c));
-    if ((rc = S.run(nv, st))) return rc;
+      for (int c = 0; c < 3; ++c) S.add(d, c, d.T(7 + c), d.T(1 + c));
+    for (int c = 0; c < 3; ++c) S.add(d, c, d.F(kVarPhi, nw), d.T(4 + c));
+    if ((rc = S.run(d, st))) return rc;
   }
   const bool div = P.pt != 3;
-  k_ns_pressure<<<gb, kNsThreads, 0, st>>>(nv->nx, nv->ny, nv->nz, nv->F(kVarPhi, nw), add_p ? nv->T(0) : nullptr,
-                                           div ? nv->T(1) : nullptr, div ? nv->T(2) : nullptr,
-                                           div ? nv->T(3) : nullptr, P.reynolds, nv->F(kVarP, nw));
+  k_ns_pressure<<<gb, kNsThreads, 0, st>>>(d.nx, d.ny, d.nz, d.F(kVarPhi, nw), add_p ? d.T(0) : nullptr,
+                                           div ? d.T(1) : nullptr, div ? d.T(2) : nullptr, div ? d.T(3) : nullptr,
+                                           P.reynolds, d.F(kVarP, nw));
   if ((rc = launch_check("k_ns_pressure"))) return rc;
   for (int c = 0; c < 3; ++c) {
-    k_ns_velocity<<<gb, kNsThreads, 0, st>>>(nv->nx, nv->ny, nv->nz, nv->RP(c), nv->T(4 + c), fac1, nv->F(c, nw));
+    k_ns_velocity<<<gb, kNsThreads, 0, st>>>(d.nx, d.ny, d.nz, d.RP(c), d.T(4 + c), nv->fac[0], d.F(c, nw));
     if ((rc = launch_check("k_ns_velocity"))) return rc;
   }
+  return MF_OK;
+}
+
+// One pass of the step (navier3d.f90:63-102) over all subdomains.
+int ns_step(mf_navier* nv, cudaStream_t st) {
+  const mf_navier_params_t& P = nv->prm;
+  const int nw = nv->it[0];
+  const int ndom = (int)nv->dom.size();
+  int rc;
+  // nonlinear terms of the slots that extrapol('v') reads
+  int slots[3];
+  const int nslots = extrapol_slots(nv, P.tou, slots);
+  for (int t = 0; t < nslots; ++t)
+    if (!nv->nl_ok[slots[t]]) {
+      for (NsDom& d : nv->dom)
+        if ((rc = nonlinear_slot(nv, d, slots[t], st))) return rc;
+      nv->nl_ok[slots[t]] = true;
+    }
+  // flow-rate term of f for u: integral of extrapol(u) over all subdomains
+  const double* g = nullptr;
+  if (P.flow_rate) {
+    double* ds = nv->dsum.as<double>();
+    for (int q = 0; q < ndom; ++q) {
+      NsDom& d = nv->dom[q];
+      if ((rc = extrapol_into(d, extrapol_of(nv, d, P.tou, false, kVarU), d.T(0), st)) ||
+          (rc = wsum(d, d.T(0), ds + q, st)))
+        return rc;
+    }
+    k_ns_sum_small<<<1, 1, 0, st>>>(ds, ndom, ds + ndom);
+    k_ns_flow<<<1, 1, 0, st>>>(ds + ndom, nv->reft, nv->fac[0], (double)1e-10f, nv->state.as<double>());
+    if ((rc = launch_check("k_ns_flow"))) return rc;
+    g = nv->state.as<double>();
+  }
+  nv->rhs_cur ^= 1;  // rhs(2) = rhs(1): the other buffer keeps the previous step's
+  for (NsDom& d : nv->dom)
+    if ((rc = presolve(nv, d, g, st)) || (rc = velocity_bc(nv, d, st))) return rc;
+  // pt = 1, 2: velocity before the pressure (pt = 2: + gradient of extrapol(p))
+  if (P.pt == 2)
+    for (NsDom& d : nv->dom)
+      if ((rc = extrapol_into(d, extrapol_of(nv, d, P.top - 1, false, kVarP), d.T(0), st)) ||
+          (rc = gradient(d, d.T(0), d.T(1), d.T(2), d.T(3), st)))
+        return rc;
+  if (P.pt <= 2 && (rc = velocity_solves(nv, P.pt == 2, st))) return rc;
+  // pressure increment
+  for (NsDom& d : nv->dom)
+    if ((rc = phi_stage(nv, d, st))) return rc;
+  if (nv->md()) {
+    if ((rc = solve_md(nv, nv->mdp, kVarPhi, 3, nw, st))) return rc;
+  } else {
+    NsDom& d = nv->dom[0];
+    if ((rc = solve_one(nv, d, d.sc[3], d.fin.as<double>(), nv->sigmap, d.F(kVarPhi, nw), 3, st))) return rc;
+  }
+  for (NsDom& d : nv->dom)
+    if ((rc = projection(nv, d, st))) return rc;
   // pt = 3, 4: velocity correction with the gradient of the new pressure
   if (P.pt >= 3) {
-    if ((rc = gradient(nv, nv->F(kVarP, nw), nv->T(1), nv->T(2), nv->T(3), st)) ||
-        (rc = velocity_solves(nv->T(1))))
-      return rc;
+    for (NsDom& d : nv->dom)
+      if ((rc = gradient(d, d.F(kVarP, nw), d.T(1), d.T(2), d.T(3), st))) return rc;
+    if ((rc = velocity_solves(nv, true, st))) return rc;
   }
   nv->nl_ok[nw] = false;
   return MF_OK;
 }
 
-// Weighted sums of one k_ns_diag phase into out[kDiagSums] (host; syncs).
-int diag_sums(mf_navier* nv, int phase, const DiagIn& D, double* out, cudaStream_t st) {
-  const int groups = (nv->ny + kWRows - 1) / kWRows, count = nv->nz * groups;
-  const dim3 grid(nv->nz, groups);
-  double* part = nv->part.as<double>();
-  switch (phase) {
-    case 0: k_ns_diag<0><<<grid, kNsThreads, 0, st>>>(nv->weights(), D, part); break;
-    case 1: k_ns_diag<1><<<grid, kNsThreads, 0, st>>>(nv->weights(), D, part); break;
-    case 2: k_ns_diag<2><<<grid, kNsThreads, 0, st>>>(nv->weights(), D, part); break;
-    case 3: k_ns_diag<3><<<grid, kNsThreads, 0, st>>>(nv->weights(), D, part); break;
-    default: k_ns_diag<4><<<grid, kNsThreads, 0, st>>>(nv->weights(), D, part); break;
+}  // namespace
+
+namespace {
+
+// Weighted sums of one k_ns_diag phase over all subdomains (each subdomain's
+// sums in a fixed order, then added in subdomain order) into out[kDiagSums]
+// on the host; synchronises.
+int diag_sums(mf_navier* nv, int phase, const std::vector<DiagIn>& Ds, double* out, cudaStream_t st) {
+  for (int s = 0; s < kDiagSums; ++s) out[s] = 0.0;
+  for (size_t q = 0; q < nv->dom.size(); ++q) {
+    NsDom& d = nv->dom[q];
+    const DiagIn& D = Ds[q];
+    const int groups = (d.ny + kWRows - 1) / kWRows, count = d.nz * groups;
+    const dim3 grid(d.nz, groups);
+    double* part = d.part.as<double>();
+    switch (phase) {
+      case 0: k_ns_diag<0><<<grid, kNsThreads, 0, st>>>(d.weights(), D, part); break;
+      case 1: k_ns_diag<1><<<grid, kNsThreads, 0, st>>>(d.weights(), D, part); break;
+      case 2: k_ns_diag<2><<<grid, kNsThreads, 0, st>>>(d.weights(), D, part); break;
+      case 3: k_ns_diag<3><<<grid, kNsThreads, 0, st>>>(d.weights(), D, part); break;
+      default: k_ns_diag<4><<<grid, kNsThreads, 0, st>>>(d.weights(), D, part); break;
+    }
+    k_ns_sum_parts<<<1, kNsThreads, 0, st>>>(part, count, kDiagSums, d.sums.as<double>());
+    int r = launch_check("k_ns_diag");
+    if (r) return r;
+    double h[kDiagSums];
+    MF_CUDA(cudaMemcpyAsync(h, d.sums.ptr, sizeof(h), cudaMemcpyDeviceToHost, st));
+    MF_CUDA(cudaStreamSynchronize(st));
+    for (int s = 0; s < kDiagSums; ++s) out[s] += h[s];
   }
-  k_ns_sum_parts<<<1, kNsThreads, 0, st>>>(part, count, kDiagSums, nv->sums.as<double>());
-  int r = launch_check("k_ns_diag");
-  if (r) return r;
-  MF_CUDA(cudaMemcpyAsync(out, nv->sums.ptr, sizeof(double) * kDiagSums, cudaMemcpyDeviceToHost, st));
-  MF_CUDA(cudaStreamSynchronize(st));
   return MF_OK;
 }
 
@@ -996,38 +1136,46 @@ int diag_sums(mf_navier* nv, int phase, const DiagIn& D, double* out, cudaStream
 // sub-iterate: true when both relative changes are below eps.
 int ns_testconv(mf_navier* nv, double eps, bool* test, cudaStream_t st) {
   const int nw = nv->it[0];
-  DiagIn D{};
-  D.u = nv->F(0, nw); D.v = nv->F(1, nw); D.w = nv->F(2, nw); D.p = nv->F(kVarP, nw);
-  const double* sb = nv->sub.as<double>();
-  D.su = sb; D.sv = sb + nv->np; D.sw = sb + 2 * nv->np; D.sp = sb + 3 * nv->np;
+  std::vector<DiagIn> Ds(nv->dom.size());
+  for (size_t q = 0; q < nv->dom.size(); ++q) {
+    NsDom& d = nv->dom[q];
+    DiagIn& D = Ds[q];
+    D = DiagIn{};
+    D.u = d.F(0, nw); D.v = d.F(1, nw); D.w = d.F(2, nw); D.p = d.F(kVarP, nw);
+    const double* sb = d.sub.as<double>();
+    D.su = sb; D.sv = sb + d.np; D.sw = sb + 2 * d.np; D.sp = sb + 3 * d.np;
+  }
   double a[kDiagSums], b[kDiagSums];
   int rc;
-  if ((rc = diag_sums(nv, 3, D, a, st))) return rc;
+  if ((rc = diag_sums(nv, 3, Ds, a, st))) return rc;
   const double e1 = std::sqrt(a[1]) / std::sqrt(a[0]);
-  D.spm = a[2] / nv->reft;
-  if ((rc = diag_sums(nv, 4, D, b, st))) return rc;
+  for (DiagIn& D : Ds) D.spm = a[2] / nv->reft;
+  if ((rc = diag_sums(nv, 4, Ds, b, st))) return rc;
   const double e2 = std::sqrt(b[1]) / std::sqrt(b[0]);
   *test = e1 < eps && e2 < eps;
   return MF_OK;
 }
 
-// Driver diagnostics of level it(nt) (navier3d.f90:120-254); diag[12].
+// Driver diagnostics of level it(nt) (navier3d.f90:120-254) over all
+// subdomains; diag[12].
 int ns_diagnostics(mf_navier* nv, double* diag, cudaStream_t st) {
   const int cur = nv->it[kNt - 1], prev = nv->it[kNt - 2];
   int rc;
-  {
+  std::vector<DiagIn> Ds(nv->dom.size());
+  for (size_t q = 0; q < nv->dom.size(); ++q) {
+    NsDom& d = nv->dom[q];
     Sweeps S;
-    for (int c = 0; c < 3; ++c) S.add(nv, c, nv->F(c, cur), nv->T(1 + c));
-    if ((rc = S.run(nv, st))) return rc;
+    for (int c = 0; c < 3; ++c) S.add(d, c, d.F(c, cur), d.T(1 + c));
+    if ((rc = S.run(d, st))) return rc;
+    DiagIn& D = Ds[q];
+    D = DiagIn{};
+    D.u = d.F(0, cur); D.v = d.F(1, cur); D.w = d.F(2, cur); D.p = d.F(kVarP, cur);
+    D.up = d.F(0, prev); D.vp = d.F(1, prev); D.wp = d.F(2, prev); D.pp = d.F(kVarP, prev);
+    D.dx = d.T(1); D.dy = d.T(2); D.dz = d.T(3);
+    D.ue = d.EX(0); D.ve = d.EX(1); D.pex = d.EX(2);
   }
-  DiagIn D{};
-  D.u = nv->F(0, cur); D.v = nv->F(1, cur); D.w = nv->F(2, cur); D.p = nv->F(kVarP, cur);
-  D.up = nv->F(0, prev); D.vp = nv->F(1, prev); D.wp = nv->F(2, prev); D.pp = nv->F(kVarP, prev);
-  D.dx = nv->T(1); D.dy = nv->T(2); D.dz = nv->T(3);
-  D.ue = nv->EX(0); D.ve = nv->EX(1); D.pex = nv->EX(2);
   double s0[kDiagSums], s1[kDiagSums], s2[kDiagSums];
-  auto run = [&](int phase, double* out) { return diag_sums(nv, phase, D, out, st); };
-  if ((rc = run(0, s0))) return rc;
+  if ((rc = diag_sums(nv, 0, Ds, s0, st))) return rc;
   const double reft = nv->reft, ts = nv->prm.ts;
   const double ref1 = std::sqrt(reft);  // norme(1)
   diag[0] = std::sqrt(s0[0]) / ref1;
@@ -1037,10 +1185,12 @@ int ns_diagnostics(mf_navier* nv, double* diag, cudaStream_t st) {
   diag[2] = errv / refv;
   diag[3] = std::sqrt(nv->err_vts);
   // pressure: remove the weighted mean of p(it(nt)) (the driver stores it back)
-  k_ns_shift<<<ns_blocks(nv->np), kNsThreads, 0, st>>>(nv->np, -(s0[3] / reft), nv->F(kVarP, cur));
-  if ((rc = launch_check("k_ns_shift"))) return rc;
-  D.pexm = s0[10] / reft;
-  if ((rc = run(1, s1))) return rc;
+  for (NsDom& d : nv->dom) {
+    k_ns_shift<<<ns_blocks(d.np), kNsThreads, 0, st>>>(d.np, -(s0[3] / reft), d.F(kVarP, cur));
+    if ((rc = launch_check("k_ns_shift"))) return rc;
+  }
+  for (DiagIn& D : Ds) D.pexm = s0[10] / reft;
+  if ((rc = diag_sums(nv, 1, Ds, s1, st))) return rc;
   const double errp = std::sqrt(s1[0]), refp = std::sqrt(s1[1]);
   nv->err_pre += errp * errp * ts;
   diag[4] = errp;
@@ -1048,8 +1198,8 @@ int ns_diagnostics(mf_navier* nv, double* diag, cudaStream_t st) {
   diag[6] = std::sqrt(nv->err_pre);
   const double nu = std::sqrt(s0[4]), nvv = std::sqrt(s0[5]), nww = std::sqrt(s0[6]);
   diag[7] = 0.5 * (nu * nu + nvv * nvv + nww) / reft;
-  D.auxm = s1[2] / reft;
-  if ((rc = run(2, s2))) return rc;
+  for (DiagIn& D : Ds) D.auxm = s1[2] / reft;
+  if ((rc = diag_sums(nv, 2, Ds, s2, st))) return rc;
   const double sp = std::sqrt(s2[0]);
   diag[8] = sp;
   diag[9] = sp / reft;
@@ -1057,6 +1207,155 @@ int ns_diagnostics(mf_navier* nv, double* diag, cudaStream_t st) {
   const double sv = std::sqrt(du * du + dv * dv + dw);
   diag[10] = sv;
   diag[11] = sv / reft;
+  return MF_OK;
+}
+
+// Set-up of one subdomain's coefficients, buffers and exact solution.
+int dom_setup(NsDom& d, const mf_navier_params_t* p, const double* gx, int nx, const double* gy, int ny,
+              const double* gz, int nz, bool md) {
+  d.nx = nx; d.ny = ny; d.nz = nz;
+  d.n1 = nx - 2; d.n2 = ny - 2; d.n3 = nz - 2;
+  d.np = (long long)nx * ny * nz;
+  d.nin = (long long)d.n1 * d.n2 * d.n3;
+  d.faces = Faces{nx, ny, nz, 2LL * d.n2 * d.n3, 2LL * d.n1 * d.n3, 2LL * d.n1 * d.n2};
+  const long long ftot = d.faces.sx + d.faces.sy + d.faces.sz;
+  const int groups = (ny + kWRows - 1) / kWRows;
+  const size_t fb = (size_t)d.np * sizeof(double);
+  const int bctu[6] = {1, 1, 1, 1, 1, 1}, bctp[6] = {2, 2, 2, 2, 2, 2};
+  int rc;
+  if ((rc = mf_der_coeffs_init(gx, nx, 1, p->so_der, &d.dcx)) || (rc = mf_der_coeffs_init(gy, ny, 1, p->so_der, &d.dcy)) ||
+      (rc = mf_der_coeffs_init(gz, nz, 1, p->so_der, &d.dcz)))
+    return rc;
+  if (!md)
+    for (int q = 0; q < 4; ++q)
+      if ((rc = mf_solver_coeffs_init_3d(gx, gy, gz, nx, ny, nz, q < 3 ? bctu : bctp, p->so_solver, &d.sc[q])))
+        return rc;
+  if (p->les_type != 0 && ((rc = mf_les_create(gx, nx, gy, ny, gz, nz, &d.les)) || (rc = d.nu.ensure(fb))))
+    return rc;
+  if (p->nsubite > 1 && (rc = d.sub.ensure(fb * 4))) return rc;
+  if ((rc = d.fields.ensure(fb * 5 * kNt)) || (rc = d.nl.ensure(fb * 3 * kNt)) || (rc = d.rhs.ensure(fb * 6)) ||
+      (rc = d.rp.ensure(fb * 3)) || (rc = d.tmp.ensure(fb * 18)) ||
+      (rc = d.fin.ensure(md ? fb : (size_t)d.nin * sizeof(double) * 3)) || (rc = d.exact.ensure(fb * 5)) ||
+      (rc = d.bcex.ensure(sizeof(double) * 3 * ftot)) || (rc = d.bc.ensure(sizeof(double) * 4 * ftot)) ||
+      (rc = d.grid.ensure(sizeof(double) * (nx + ny + nz))) || (rc = d.wts.ensure(sizeof(double) * (nx + ny + nz))) ||
+      (rc = d.part.ensure(sizeof(double) * kDiagSums * (size_t)nz * groups)) ||
+      (rc = d.sums.ensure(sizeof(double) * kDiagSums)))
+    return rc;
+  // host-side set-up: grids, half widths, integrale(1) of this subdomain
+  std::vector<double> g(nx + ny + nz), w(nx + ny + nz);
+  const double* src[3] = {gx, gy, gz};
+  const int n[3] = {nx, ny, nz};
+  for (int a = 0, off = 0; a < 3; off += n[a], ++a) {
+    for (int i = 0; i < n[a]; ++i) g[off + i] = src[a][i];
+    for (int i = 1; i < n[a] - 1; ++i) w[off + i] = (src[a][i + 1] - src[a][i - 1]) * 0.5;
+    w[off] = (src[a][1] - src[a][0]) * 0.5;
+    w[off + n[a] - 1] = (src[a][n[a] - 1] - src[a][n[a] - 2]) * 0.5;
+  }
+  double reft = 0.0;
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        const int b = (i == 0 || i == nx - 1) + (j == 0 || j == ny - 1) + (k == 0 || k == nz - 1);
+        if (b <= 1) reft += w[i] * w[nx + j] * w[nx + ny + k];
+      }
+  d.reft = reft;
+  if (cudaMemcpy(d.grid.ptr, g.data(), g.size() * 8, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(d.wts.ptr, w.data(), w.size() * 8, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemset(d.fields.ptr, 0, fb * 5 * kNt) != cudaSuccess || cudaMemset(d.rhs.ptr, 0, fb * 6) != cudaSuccess)
+    return set_error(MF_ERR_CUDA, "mf_navier_create: upload failed");
+  const double* dg = d.grid.as<double>();
+  k_ns_exact<<<ns_blocks(d.np), kNsThreads>>>(dg, dg + nx, dg + nx + ny, nx, ny, nz, p->nmodes, 4.0 * std::atan(1.0),
+                                              p->reynolds, d.exact.as<double>());
+  k_ns_bc_exact<<<ns_blocks(ftot), kNsThreads>>>(d.faces, d.exact.as<double>(), d.np, d.bcex.as<double>());
+  if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess)
+    return set_error(MF_ERR_CUDA, "mf_navier_create: exact-solution kernels failed");
+  return MF_OK;
+}
+
+int navier_check_params(const mf_navier_params_t* p) {
+  if (!(p->ts > 0.0) || !(p->reynolds > 0.0) || p->nlt < 0 || p->nlt > 2 || p->pt < 1 || p->pt > 4 ||
+      p->tou < 1 || p->tou > 3 || p->nmodes < 0 || p->les_type < 0 || p->les_type > 3 || p->nsubite < 1)
+    return set_error(MF_ERR_ARG,
+                     "mf_navier_create: bad parameters (ts, reynolds > 0; nlt 0..2; pt 1..4; tou 1..3; les_type 0..3)");
+  if (p->precision != MF_PREC_FP64 && p->precision != MF_PREC_SPLIT_BF16 && p->precision != MF_PREC_3XTF32)
+    return set_error(MF_ERR_ARG, "mf_navier_create: unknown precision %d", p->precision);
+  return MF_OK;
+}
+
+int navier_build(const int nd[3], const int periods[3], const double* const* gx, const int* nx,
+                 const double* const* gy, const int* ny, const double* const* gz, const int* nz,
+                 const mf_navier_params_t* p, mf_navier_t** out) {
+  *out = nullptr;
+  int rc;
+  if ((rc = navier_check_params(p))) return rc;
+  for (int l = 0; l < 3; ++l)
+    if (nd[l] < 1) return set_error(MF_ERR_ARG, "mf_navier_create: at least one subdomain per axis");
+  const int* sizes[3] = {nx, ny, nz};
+  for (int l = 0; l < 3; ++l)
+    for (int q = 0; q < nd[l]; ++q)
+      if (sizes[l][q] < 9) return set_error(MF_ERR_ARG, "mf_navier_create: at least 9 nodes per axis");
+  const bool md = nd[0] * nd[1] * nd[2] > 1 || periods[0] || periods[1] || periods[2];
+  mf_navier* nv = new mf_navier();
+  nv->prm = *p;
+  for (int l = 0; l < 3; ++l) nv->nd[l] = nd[l];
+  const double ts = p->ts;
+  if (p->tou == 1) {
+    nv->fac[0] = 1.0 / ts; nv->fac[1] = -1.0 / ts; nv->fac[2] = 0.0; nv->fac[3] = 0.0;
+  } else if (p->tou == 2) {
+    nv->fac[0] = 1.5 / ts; nv->fac[1] = -2.0 / ts; nv->fac[2] = 0.5 / ts; nv->fac[3] = 0.0;
+  } else {
+    nv->fac[0] = 11.0 / (6.0 * ts); nv->fac[1] = -18.0 / (6.0 * ts);
+    nv->fac[2] = 9.0 / (6.0 * ts); nv->fac[3] = -2.0 / (6.0 * ts);
+  }
+  nv->sigmau = -p->reynolds * nv->fac[0];
+  nv->sigmap = 0.0;
+  auto fail = [&](int r) {
+    mf_navier_destroy(nv);
+    return r;
+  };
+  nv->dom.resize((size_t)nd[0] * nd[1] * nd[2]);
+  for (int k = 0; k < nd[2]; ++k)
+    for (int j = 0; j < nd[1]; ++j)
+      for (int i = 0; i < nd[0]; ++i) {
+        NsDom& d = nv->dom[i + nd[0] * (j + nd[1] * k)];
+        if ((rc = dom_setup(d, p, gx[i], nx[i], gy[j], ny[j], gz[k], nz[k], md))) return fail(rc);
+      }
+  for (const NsDom& d : nv->dom) nv->reft += d.reft;
+  if ((rc = nv->state.ensure(sizeof(double) * 3)) || (rc = nv->dsum.ensure(sizeof(double) * (nv->dom.size() + 1))))
+    return fail(rc);
+  if (cudaMemset(nv->state.ptr, 0, sizeof(double) * 3) != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess)
+    return fail(set_error(MF_ERR_CUDA, "mf_navier_create: upload failed"));
+  if (md) {
+    // the influence matrices of the velocity (Dirichlet outer faces, sigmau)
+    // and of the pressure (Neumann, sigma 0, constant null space)
+    const int bctu[6] = {1, 1, 1, 1, 1, 1}, bctp[6] = {2, 2, 2, 2, 2, 2};
+    if ((rc = mf_md_create(nd, periods, gx, nx, gy, ny, gz, nz, bctu, p->so_solver, &nv->mdu)) ||
+        (rc = mf_md_create(nd, periods, gx, nx, gy, ny, gz, nz, bctp, p->so_solver, &nv->mdp)))
+      return fail(rc);
+    auto build = [&](mf_md_t* m, double sigma, int null_mode) {
+      return p->md_cache_dir ? mf_md_influence_matrix_cached(m, sigma, null_mode, p->md_cache_dir, nullptr)
+                             : mf_md_influence_matrix_set(m, sigma, null_mode, nullptr);
+    };
+    if ((rc = build(nv->mdu, nv->sigmau, 0)) || (rc = build(nv->mdp, 0.0, 1))) return fail(rc);
+    if (cudaDeviceSynchronize() != cudaSuccess) return fail(set_error(MF_ERR_CUDA, "influence matrices failed"));
+  } else {
+    for (int q = 0; q < 2; ++q)
+      if (cudaStreamCreateWithFlags(&nv->side[q], cudaStreamNonBlocking) != cudaSuccess ||
+          cudaEventCreateWithFlags(&nv->join[q], cudaEventDisableTiming) != cudaSuccess)
+        return fail(set_error(MF_ERR_CUDA, "mf_navier_create: stream set-up failed"));
+    if (cudaEventCreateWithFlags(&nv->fork, cudaEventDisableTiming) != cudaSuccess)
+      return fail(set_error(MF_ERR_CUDA, "mf_navier_create: stream set-up failed"));
+  }
+  *out = nv;
+  return MF_OK;
+}
+
+int dom_field(mf_navier* nv, int sub, int var, int level, double** ptr, NsDom** dp) {
+  if (!nv || !ptr || sub < 0 || sub >= (int)nv->dom.size() || var < 0 || var > 4 || level < 0 || level >= kNt)
+    return set_error(MF_ERR_ARG, "mf_navier field access: subdomain, var 0..4, level 0..3");
+  NsDom& d = nv->dom[sub];
+  *ptr = d.F(var, nv->it[level]);
+  if (dp) *dp = &d;
   return MF_OK;
 }
 
@@ -1081,28 +1380,22 @@ int mf_navier_defaults(mf_navier_params_t* p) {
   p->les_type = 0;
   p->les_c = 0.0;
   p->nsubite = 1;
+  p->md_cache_dir = nullptr;
   return MF_OK;
 }
 
 int mf_navier_destroy(mf_navier_t* nv) {
   if (!nv) return MF_OK;
-  mf_der_destroy(nv->dcx);
-  mf_der_destroy(nv->dcy);
-  mf_der_destroy(nv->dcz);
-  mf_solver3d_destroy(nv->scu);
-  mf_solver3d_destroy(nv->scv);
-  mf_solver3d_destroy(nv->scw);
-  mf_solver3d_destroy(nv->scp);
-  mf_les_destroy(nv->les);
-  nv->nu.release();
+  for (NsDom& d : nv->dom) d.release();
+  mf_md_destroy(nv->mdu);
+  mf_md_destroy(nv->mdp);
   for (int q = 0; q < 2; ++q) {
     if (nv->side[q]) cudaStreamDestroy(nv->side[q]);
     if (nv->join[q]) cudaEventDestroy(nv->join[q]);
   }
   if (nv->fork) cudaEventDestroy(nv->fork);
-  for (DevBuf* b : {&nv->fields, &nv->nl, &nv->rhs, &nv->rp, &nv->tmp, &nv->fin, &nv->exact, &nv->bcex,
-                    &nv->bc, &nv->grid, &nv->wts, &nv->part, &nv->sums, &nv->state, &nv->sub})
-    b->release();
+  nv->state.release();
+  nv->dsum.release();
   delete nv;
   return MF_OK;
 }
@@ -1110,138 +1403,69 @@ int mf_navier_destroy(mf_navier_t* nv) {
 int mf_navier_create(const double* gx, int nx, const double* gy, int ny, const double* gz, int nz,
                      const mf_navier_params_t* p, mf_navier_t** out) {
   if (!gx || !gy || !gz || !p || !out) return set_error(MF_ERR_ARG, "mf_navier_create: null argument");
-  *out = nullptr;
-  if (nx < 9 || ny < 9 || nz < 9) return set_error(MF_ERR_ARG, "mf_navier_create: at least 9 nodes per axis");
-  if (!(p->ts > 0.0) || !(p->reynolds > 0.0) || p->nlt < 0 || p->nlt > 2 || p->pt < 1 || p->pt > 4 ||
-      p->tou < 1 || p->tou > 3 || p->nmodes < 0 || p->les_type < 0 || p->les_type > 3 ||
-      p->nsubite < 1)
-    return set_error(MF_ERR_ARG, "mf_navier_create: bad parameters (ts, reynolds > 0; nlt 0..2; pt 1..4; tou 1..3; les_type 0..3)");
-  if (p->precision != MF_PREC_FP64 && p->precision != MF_PREC_SPLIT_BF16 && p->precision != MF_PREC_3XTF32)
-    return set_error(MF_ERR_ARG, "mf_navier_create: unknown precision %d", p->precision);
-  mf_navier* nv = new mf_navier();
-  nv->prm = *p;
-  nv->nx = nx; nv->ny = ny; nv->nz = nz;
-  nv->n1 = nx - 2; nv->n2 = ny - 2; nv->n3 = nz - 2;
-  nv->np = (long long)nx * ny * nz;
-  nv->nin = (long long)nv->n1 * nv->n2 * nv->n3;
-  const double ts = p->ts;
-  if (p->tou == 1) {
-    nv->fac[0] = 1.0 / ts; nv->fac[1] = -1.0 / ts; nv->fac[2] = 0.0; nv->fac[3] = 0.0;
-  } else if (p->tou == 2) {
-    nv->fac[0] = 1.5 / ts; nv->fac[1] = -2.0 / ts; nv->fac[2] = 0.5 / ts; nv->fac[3] = 0.0;
-  } else {
-    nv->fac[0] = 11.0 / (6.0 * ts); nv->fac[1] = -18.0 / (6.0 * ts);
-    nv->fac[2] = 9.0 / (6.0 * ts); nv->fac[3] = -2.0 / (6.0 * ts);
-  }
-  nv->sigmau = -p->reynolds * nv->fac[0];
-  nv->sigmap = 0.0;
-  nv->faces = Faces{nx, ny, nz, 2LL * nv->n2 * nv->n3, 2LL * nv->n1 * nv->n3, 2LL * nv->n1 * nv->n2};
-  const long long ftot = nv->faces.sx + nv->faces.sy + nv->faces.sz;
-  const int groups = (ny + kWRows - 1) / kWRows;
-  const size_t fb = (size_t)nv->np * sizeof(double);
-  const int bctu[6] = {1, 1, 1, 1, 1, 1}, bctp[6] = {2, 2, 2, 2, 2, 2};
-  int rc;
-  auto fail = [&](int r) {
-    mf_navier_destroy(nv);
-    return r;
-  };
-  if ((rc = mf_der_coeffs_init(gx, nx, 1, p->so_der, &nv->dcx)) ||
-      (rc = mf_der_coeffs_init(gy, ny, 1, p->so_der, &nv->dcy)) ||
-      (rc = mf_der_coeffs_init(gz, nz, 1, p->so_der, &nv->dcz)) ||
-      (rc = mf_solver_coeffs_init_3d(gx, gy, gz, nx, ny, nz, bctu, p->so_solver, &nv->scu)) ||
-      (rc = mf_solver_coeffs_init_3d(gx, gy, gz, nx, ny, nz, bctu, p->so_solver, &nv->scv)) ||
-      (rc = mf_solver_coeffs_init_3d(gx, gy, gz, nx, ny, nz, bctu, p->so_solver, &nv->scw)) ||
-      (rc = mf_solver_coeffs_init_3d(gx, gy, gz, nx, ny, nz, bctp, p->so_solver, &nv->scp)))
-    return fail(rc);
-  if (p->les_type != 0 &&
-      ((rc = mf_les_create(gx, nx, gy, ny, gz, nz, &nv->les)) || (rc = nv->nu.ensure(fb))))
-    return fail(rc);
-  if (p->nsubite > 1 && (rc = nv->sub.ensure(fb * 4))) return fail(rc);
-  if ((rc = nv->fields.ensure(fb * 5 * kNt)) || (rc = nv->nl.ensure(fb * 3 * kNt)) ||
-      (rc = nv->rhs.ensure(fb * 6)) || (rc = nv->rp.ensure(fb * 3)) || (rc = nv->tmp.ensure(fb * 18)) ||
-      (rc = nv->fin.ensure((size_t)nv->nin * sizeof(double) * 3)) || (rc = nv->exact.ensure(fb * 5)) ||
-      (rc = nv->bcex.ensure(sizeof(double) * 3 * ftot)) || (rc = nv->bc.ensure(sizeof(double) * 4 * ftot)) ||
-      (rc = nv->grid.ensure(sizeof(double) * (nx + ny + nz))) ||
-      (rc = nv->wts.ensure(sizeof(double) * (nx + ny + nz))) ||
-      (rc = nv->part.ensure(sizeof(double) * kDiagSums * (size_t)nz * groups)) ||
-      (rc = nv->sums.ensure(sizeof(double) * kDiagSums)) || (rc = nv->state.ensure(sizeof(double) * 3)))
-    return fail(rc);
-  // host-side set-up: grids, half widths, integrale(1)
-  std::vector<double> g(nx + ny + nz), w(nx + ny + nz);
-  const double* src[3] = {gx, gy, gz};
-  const int n[3] = {nx, ny, nz};
-  for (int a = 0, off = 0; a < 3; off += n[a], ++a) {
-    for (int i = 0; i < n[a]; ++i) g[off + i] = src[a][i];
-    for (int i = 1; i < n[a] - 1; ++i) w[off + i] = (src[a][i + 1] - src[a][i - 1]) * 0.5;
-    w[off] = (src[a][1] - src[a][0]) * 0.5;
-    w[off + n[a] - 1] = (src[a][n[a] - 1] - src[a][n[a] - 2]) * 0.5;
-  }
-  double reft = 0.0;
-  for (int k = 0; k < nz; ++k)
-    for (int j = 0; j < ny; ++j)
-      for (int i = 0; i < nx; ++i) {
-        const int b = (i == 0 || i == nx - 1) + (j == 0 || j == ny - 1) + (k == 0 || k == nz - 1);
-        if (b <= 1) reft += w[i] * w[nx + j] * w[nx + ny + k];
-      }
-  nv->reft = reft;
-  for (int q = 0; q < 2; ++q)
-    if (cudaStreamCreateWithFlags(&nv->side[q], cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreateWithFlags(&nv->join[q], cudaEventDisableTiming) != cudaSuccess)
-      return fail(set_error(MF_ERR_CUDA, "mf_navier_create: stream set-up failed"));
-  if (cudaEventCreateWithFlags(&nv->fork, cudaEventDisableTiming) != cudaSuccess)
-    return fail(set_error(MF_ERR_CUDA, "mf_navier_create: stream set-up failed"));
-  cudaStream_t st = nullptr;
-  if (cudaMemcpy(nv->grid.ptr, g.data(), g.size() * 8, cudaMemcpyHostToDevice) != cudaSuccess ||
-      cudaMemcpy(nv->wts.ptr, w.data(), w.size() * 8, cudaMemcpyHostToDevice) != cudaSuccess ||
-      cudaMemset(nv->fields.ptr, 0, fb * 5 * kNt) != cudaSuccess || cudaMemset(nv->rhs.ptr, 0, fb * 6) != cudaSuccess ||
-      cudaMemset(nv->state.ptr, 0, sizeof(double) * 3) != cudaSuccess)
-    return fail(set_error(MF_ERR_CUDA, "mf_navier_create: upload failed"));
-  const double* dg = nv->grid.as<double>();
-  k_ns_exact<<<ns_blocks(nv->np), kNsThreads, 0, st>>>(dg, dg + nx, dg + nx + ny, nx, ny, nz, p->nmodes,
-                                                       4.0 * std::atan(1.0), p->reynolds, nv->exact.as<double>());
-  k_ns_bc_exact<<<ns_blocks(ftot), kNsThreads, 0, st>>>(nv->faces, nv->exact.as<double>(), nv->np,
-                                                        nv->bcex.as<double>());
-  if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess)
-    return fail(set_error(MF_ERR_CUDA, "mf_navier_create: exact-solution kernels failed"));
-  *out = nv;
+  const int nd[3] = {1, 1, 1}, periods[3] = {0, 0, 0};
+  return navier_build(nd, periods, &gx, &nx, &gy, &ny, &gz, &nz, p, out);
+}
+
+int mf_navier_create_md(const int nd[3], const int periods[3], const double* const* gridx, const int* nx,
+                        const double* const* gridy, const int* ny, const double* const* gridz, const int* nz,
+                        const mf_navier_params_t* p, mf_navier_t** out) {
+  if (!nd || !periods || !gridx || !nx || !gridy || !ny || !gridz || !nz || !p || !out)
+    return set_error(MF_ERR_ARG, "mf_navier_create_md: null argument");
+  return navier_build(nd, periods, gridx, nx, gridy, ny, gridz, nz, p, out);
+}
+
+int mf_navier_subdomains(const mf_navier_t* nv, int* count) {
+  if (!nv || !count) return set_error(MF_ERR_ARG, "mf_navier_subdomains: null argument");
+  *count = (int)nv->dom.size();
   return MF_OK;
+}
+
+int mf_navier_sub_field(mf_navier_t* nv, int sub, int var, int level, double** ptr) {
+  return dom_field(nv, sub, var, level, ptr, nullptr);
 }
 
 int mf_navier_field(mf_navier_t* nv, int var, int level, double** ptr) {
-  if (!nv || !ptr || var < 0 || var > 4 || level < 0 || level >= kNt)
-    return set_error(MF_ERR_ARG, "mf_navier_field: var 0..4, level 0..3");
-  *ptr = nv->F(var, nv->it[level]);
-  return MF_OK;
+  return dom_field(nv, 0, var, level, ptr, nullptr);
 }
 
-int mf_navier_set_field(mf_navier_t* nv, int var, int level, const double* f, void* stream) {
+int mf_navier_sub_set_field(mf_navier_t* nv, int sub, int var, int level, const double* f, void* stream) {
   double* d = nullptr;
-  int rc = mf_navier_field(nv, var, level, &d);
+  NsDom* dm = nullptr;
+  int rc = dom_field(nv, sub, var, level, &d, &dm);
   if (rc) return rc;
   if (!f) return set_error(MF_ERR_ARG, "mf_navier_set_field: null field");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  MF_CUDA(cudaMemcpyAsync(d, f, (size_t)nv->np * 8, cudaMemcpyDefault, st));
+  MF_CUDA(cudaMemcpyAsync(d, f, (size_t)dm->np * 8, cudaMemcpyDefault, st));
   if (!is_device_ptr(f)) MF_CUDA(cudaStreamSynchronize(st));
   if (var < 3) nv->nl_ok[nv->it[level]] = false;
   return MF_OK;
 }
 
-int mf_navier_get_field(mf_navier_t* nv, int var, int level, double* f, void* stream) {
+int mf_navier_set_field(mf_navier_t* nv, int var, int level, const double* f, void* stream) {
+  return mf_navier_sub_set_field(nv, 0, var, level, f, stream);
+}
+
+int mf_navier_sub_get_field(mf_navier_t* nv, int sub, int var, int level, double* f, void* stream) {
   double* d = nullptr;
-  int rc = mf_navier_field(nv, var, level, &d);
+  NsDom* dm = nullptr;
+  int rc = dom_field(nv, sub, var, level, &d, &dm);
   if (rc) return rc;
   if (!f) return set_error(MF_ERR_ARG, "mf_navier_get_field: null field");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  MF_CUDA(cudaMemcpyAsync(f, d, (size_t)nv->np * 8, cudaMemcpyDefault, st));
+  MF_CUDA(cudaMemcpyAsync(f, d, (size_t)dm->np * 8, cudaMemcpyDefault, st));
   if (!is_device_ptr(f)) MF_CUDA(cudaStreamSynchronize(st));
   return MF_OK;
+}
+
+int mf_navier_get_field(mf_navier_t* nv, int var, int level, double* f, void* stream) {
+  return mf_navier_sub_get_field(nv, 0, var, level, f, stream);
 }
 
 int mf_navier_step(mf_navier_t* nv, double* diag, void* stream) {
   if (!nv) return set_error(MF_ERR_ARG, "mf_navier_step: null handle");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  const size_t fb = (size_t)nv->np * sizeof(double);
-  int rc;
+  int rc = MF_OK;
   nv->time += nv->prm.ts;  // navier_time
   for (int subite = 1; subite <= nv->prm.nsubite; ++subite) {
     nv->subite = subite;
@@ -1251,12 +1475,13 @@ int mf_navier_step(mf_navier_t* nv, double* diag, void* stream) {
     if (subite > 1 && (rc = ns_testconv(nv, 1e-9, &test, st))) break;
     if (nv->prm.nsubite > 1) {
       const int nw = nv->it[0];
-      for (int v = 0; v < 4; ++v)
-        if (cudaMemcpyAsync(nv->sub.as<double>() + (size_t)v * nv->np, nv->F(v, nw), fb, cudaMemcpyDeviceToDevice,
-                            st) != cudaSuccess) {
-          rc = set_error(MF_ERR_CUDA, "mf_navier_step: copy of the sub-iterate failed");
-          break;
-        }
+      for (NsDom& d : nv->dom) {
+        for (int v = 0; v < 4 && !rc; ++v)
+          if (cudaMemcpyAsync(d.sub.as<double>() + (size_t)v * d.np, d.F(v, nw), (size_t)d.np * 8,
+                              cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+            rc = set_error(MF_ERR_CUDA, "mf_navier_step: copy of the sub-iterate failed");
+        if (rc) break;
+      }
       if (rc) break;
     }
     if (diag && (rc = ns_diagnostics(nv, diag, st))) break;
@@ -1268,96 +1493,6 @@ int mf_navier_step(mf_navier_t* nv, double* diag, void* stream) {
   const int first = nv->it[0];
   for (int i = 0; i < kNt - 1; ++i) nv->it[i] = nv->it[i + 1];
   nv->it[kNt - 1] = first;
-  return MF_OK;
-}
-
-// Checkpoint (the role of restart_write / restart_read,
-// class_navier_3D.f90:186-340, as one raw little-endian binary file instead
-// of a NetCDF directory).  Layout: magic "MFNSCHK1", int32 nx, ny, nz, nt,
-// the three grids (FP64), time, int32 it(1..nt) (0-based slots), int32
-// rhs_cur, err_vts, err_pre, the flow-rate state {g, debit, initialised},
-// then the fields u, v, w, p, phi of each slot 0..nt-1 and rhs(1), rhs(2)
-// of u, v, w (FP64, x fastest).  Beyond the reference's restart it keeps the
-// right-hand-side history (read by pt 4) and the flow-rate state (saved
-// variables of f), so a resumed run continues bit-identically.  The nonlinear
-// terms are recomputed after a load.
-constexpr char kChkMagic[8] = {'M', 'F', 'N', 'S', 'C', 'H', 'K', '1'};
-
-int mf_navier_save(mf_navier_t* nv, const char* path, void* stream) {
-  if (!nv || !path) return set_error(MF_ERR_ARG, "mf_navier_save: null argument");
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
-  MF_CUDA(cudaStreamSynchronize(st));
-  FILE* f = std::fopen(path, "wb");
-  if (!f) return set_error(MF_ERR_ARG, "mf_navier_save: cannot open %s", path);
-  std::vector<double> grid(nv->nx + nv->ny + nv->nz), buf(nv->np);
-  double flow[3];
-  bool ok = cudaMemcpy(grid.data(), nv->grid.ptr, grid.size() * 8, cudaMemcpyDeviceToHost) == cudaSuccess &&
-            cudaMemcpy(flow, nv->state.ptr, sizeof(flow), cudaMemcpyDeviceToHost) == cudaSuccess;
-  const int dims[4] = {nv->nx, nv->ny, nv->nz, kNt};
-  ok = ok && std::fwrite(kChkMagic, 1, 8, f) == 8 && std::fwrite(dims, 4, 4, f) == 4 &&
-       std::fwrite(grid.data(), 8, grid.size(), f) == grid.size() && std::fwrite(&nv->time, 8, 1, f) == 1 &&
-       std::fwrite(nv->it, 4, kNt, f) == (size_t)kNt && std::fwrite(&nv->rhs_cur, 4, 1, f) == 1 &&
-       std::fwrite(&nv->err_vts, 8, 1, f) == 1 && std::fwrite(&nv->err_pre, 8, 1, f) == 1 &&
-       std::fwrite(flow, 8, 3, f) == 3;
-  auto put = [&](const double* d) {
-    return ok = ok && cudaMemcpy(buf.data(), d, buf.size() * 8, cudaMemcpyDeviceToHost) == cudaSuccess &&
-                std::fwrite(buf.data(), 8, buf.size(), f) == buf.size();
-  };
-  for (int slot = 0; slot < kNt && ok; ++slot)
-    for (int v = 0; v < 5 && ok; ++v) put(nv->F(v, slot));
-  for (int c = 0; c < 3 && ok; ++c)
-    for (int w = 0; w < 2 && ok; ++w) put(nv->RHS(c, w));
-  ok = (std::fclose(f) == 0) && ok;
-  return ok ? MF_OK : set_error(MF_ERR_CUDA, "mf_navier_save: writing %s failed", path);
-}
-
-int mf_navier_load(mf_navier_t* nv, const char* path, void* stream) {
-  if (!nv || !path) return set_error(MF_ERR_ARG, "mf_navier_load: null argument");
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
-  MF_CUDA(cudaStreamSynchronize(st));
-  FILE* f = std::fopen(path, "rb");
-  if (!f) return set_error(MF_ERR_ARG, "mf_navier_load: cannot open %s", path);
-  char magic[8];
-  int dims[4];
-  std::vector<double> grid(nv->nx + nv->ny + nv->nz), mine(grid.size()), buf(nv->np);
-  bool ok = std::fread(magic, 1, 8, f) == 8 && std::memcmp(magic, kChkMagic, 8) == 0 &&
-            std::fread(dims, 4, 4, f) == 4 && dims[0] == nv->nx && dims[1] == nv->ny && dims[2] == nv->nz &&
-            dims[3] == kNt && std::fread(grid.data(), 8, grid.size(), f) == grid.size() &&
-            cudaMemcpy(mine.data(), nv->grid.ptr, mine.size() * 8, cudaMemcpyDeviceToHost) == cudaSuccess &&
-            std::memcmp(grid.data(), mine.data(), grid.size() * 8) == 0;
-  if (!ok) {
-    std::fclose(f);
-    return set_error(MF_ERR_ARG, "mf_navier_load: %s is not a checkpoint of this grid", path);
-  }
-  double time, evts, epre, flow[3];
-  int it[kNt], rhs_cur;
-  ok = std::fread(&time, 8, 1, f) == 1 && std::fread(it, 4, kNt, f) == (size_t)kNt &&
-       std::fread(&rhs_cur, 4, 1, f) == 1 && std::fread(&evts, 8, 1, f) == 1 && std::fread(&epre, 8, 1, f) == 1 &&
-       std::fread(flow, 8, 3, f) == 3;
-  int seen = 0;
-  for (int i = 0; i < kNt && ok; ++i) {
-    ok = it[i] >= 0 && it[i] < kNt && !(seen & (1 << it[i]));
-    seen |= 1 << (ok ? it[i] : 0);
-  }
-  ok = ok && (rhs_cur == 0 || rhs_cur == 1);
-  auto get = [&](double* d) {
-    return ok = ok && std::fread(buf.data(), 8, buf.size(), f) == buf.size() &&
-                cudaMemcpy(d, buf.data(), buf.size() * 8, cudaMemcpyHostToDevice) == cudaSuccess;
-  };
-  for (int slot = 0; slot < kNt && ok; ++slot)
-    for (int v = 0; v < 5 && ok; ++v) get(nv->F(v, slot));
-  for (int c = 0; c < 3 && ok; ++c)
-    for (int w = 0; w < 2 && ok; ++w) get(nv->RHS(c, w));
-  ok = ok && cudaMemcpy(nv->state.ptr, flow, sizeof(flow), cudaMemcpyHostToDevice) == cudaSuccess &&
-       cudaDeviceSynchronize() == cudaSuccess;
-  std::fclose(f);
-  if (!ok) return set_error(MF_ERR_ARG, "mf_navier_load: %s is truncated or inconsistent", path);
-  nv->time = time;
-  for (int i = 0; i < kNt; ++i) nv->it[i] = it[i];
-  nv->rhs_cur = rhs_cur;
-  nv->err_vts = evts;
-  nv->err_pre = epre;
-  for (int i = 0; i < kNt; ++i) nv->nl_ok[i] = false;
   return MF_OK;
 }
 
@@ -1374,6 +1509,111 @@ int mf_navier_state(mf_navier_t* nv, double* time, double* debit, double* g) {
   if (time) *time = nv->time;
   if (debit) *debit = s[1];
   if (g) *g = s[0];
+  return MF_OK;
+}
+
+// Checkpoint (the role of restart_write / restart_read,
+// class_navier_3D.f90:186-340, as one raw little-endian binary file instead
+// of a NetCDF directory).  Layout: magic "MFNSCHK2", int32 nt, int32 number
+// of subdomains, per subdomain int32 nx, ny, nz and its three grids (FP64),
+// time, int32 it(1..nt) (0-based slots), int32 rhs_cur, err_vts, err_pre,
+// the flow-rate state {g, debit, initialised}, then per subdomain the fields
+// u, v, w, p, phi of each slot 0..nt-1 and rhs(1), rhs(2) of u, v, w (FP64,
+// x fastest).  Beyond the reference's restart it keeps the right-hand-side
+// history (read by pt 4) and the flow-rate state (saved variables of f), so
+// a resumed run continues bit-identically.  The nonlinear terms are
+// recomputed after a load.
+constexpr char kChkMagic[8] = {'M', 'F', 'N', 'S', 'C', 'H', 'K', '2'};
+
+int mf_navier_save(mf_navier_t* nv, const char* path, void* stream) {
+  if (!nv || !path) return set_error(MF_ERR_ARG, "mf_navier_save: null argument");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  MF_CUDA(cudaStreamSynchronize(st));
+  FILE* f = std::fopen(path, "wb");
+  if (!f) return set_error(MF_ERR_ARG, "mf_navier_save: cannot open %s", path);
+  double flow[3];
+  bool ok = cudaMemcpy(flow, nv->state.ptr, sizeof(flow), cudaMemcpyDeviceToHost) == cudaSuccess;
+  const int head[2] = {kNt, (int)nv->dom.size()};
+  ok = ok && std::fwrite(kChkMagic, 1, 8, f) == 8 && std::fwrite(head, 4, 2, f) == 2;
+  for (const NsDom& d : nv->dom) {
+    std::vector<double> grid(d.nx + d.ny + d.nz);
+    const int dims[3] = {d.nx, d.ny, d.nz};
+    ok = ok && cudaMemcpy(grid.data(), d.grid.ptr, grid.size() * 8, cudaMemcpyDeviceToHost) == cudaSuccess &&
+         std::fwrite(dims, 4, 3, f) == 3 && std::fwrite(grid.data(), 8, grid.size(), f) == grid.size();
+  }
+  ok = ok && std::fwrite(&nv->time, 8, 1, f) == 1 && std::fwrite(nv->it, 4, kNt, f) == (size_t)kNt &&
+       std::fwrite(&nv->rhs_cur, 4, 1, f) == 1 && std::fwrite(&nv->err_vts, 8, 1, f) == 1 &&
+       std::fwrite(&nv->err_pre, 8, 1, f) == 1 && std::fwrite(flow, 8, 3, f) == 3;
+  for (const NsDom& d : nv->dom) {
+    std::vector<double> buf(d.np);
+    auto put = [&](const double* src) {
+      return ok = ok && cudaMemcpy(buf.data(), src, buf.size() * 8, cudaMemcpyDeviceToHost) == cudaSuccess &&
+                  std::fwrite(buf.data(), 8, buf.size(), f) == buf.size();
+    };
+    for (int slot = 0; slot < kNt && ok; ++slot)
+      for (int v = 0; v < 5 && ok; ++v) put(d.F(v, slot));
+    for (int c = 0; c < 3 && ok; ++c)
+      for (int w = 0; w < 2 && ok; ++w) put(d.RHS(c, w));
+  }
+  ok = (std::fclose(f) == 0) && ok;
+  return ok ? MF_OK : set_error(MF_ERR_CUDA, "mf_navier_save: writing %s failed", path);
+}
+
+int mf_navier_load(mf_navier_t* nv, const char* path, void* stream) {
+  if (!nv || !path) return set_error(MF_ERR_ARG, "mf_navier_load: null argument");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  MF_CUDA(cudaStreamSynchronize(st));
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return set_error(MF_ERR_ARG, "mf_navier_load: cannot open %s", path);
+  char magic[8];
+  int head[2];
+  bool ok = std::fread(magic, 1, 8, f) == 8 && std::memcmp(magic, kChkMagic, 8) == 0 &&
+            std::fread(head, 4, 2, f) == 2 && head[0] == kNt && head[1] == (int)nv->dom.size();
+  for (size_t q = 0; ok && q < nv->dom.size(); ++q) {
+    const NsDom& d = nv->dom[q];
+    int dims[3];
+    std::vector<double> grid(d.nx + d.ny + d.nz), mine(grid.size());
+    ok = std::fread(dims, 4, 3, f) == 3 && dims[0] == d.nx && dims[1] == d.ny && dims[2] == d.nz &&
+         std::fread(grid.data(), 8, grid.size(), f) == grid.size() &&
+         cudaMemcpy(mine.data(), d.grid.ptr, mine.size() * 8, cudaMemcpyDeviceToHost) == cudaSuccess &&
+         std::memcmp(grid.data(), mine.data(), grid.size() * 8) == 0;
+  }
+  if (!ok) {
+    std::fclose(f);
+    return set_error(MF_ERR_ARG, "mf_navier_load: %s is not a checkpoint of these grids", path);
+  }
+  double time, evts, epre, flow[3];
+  int it[kNt], rhs_cur;
+  ok = std::fread(&time, 8, 1, f) == 1 && std::fread(it, 4, kNt, f) == (size_t)kNt &&
+       std::fread(&rhs_cur, 4, 1, f) == 1 && std::fread(&evts, 8, 1, f) == 1 && std::fread(&epre, 8, 1, f) == 1 &&
+       std::fread(flow, 8, 3, f) == 3;
+  int seen = 0;
+  for (int i = 0; i < kNt && ok; ++i) {
+    ok = it[i] >= 0 && it[i] < kNt && !(seen & (1 << it[i]));
+    seen |= 1 << (ok ? it[i] : 0);
+  }
+  ok = ok && (rhs_cur == 0 || rhs_cur == 1);
+  for (NsDom& d : nv->dom) {
+    std::vector<double> buf(d.np);
+    auto get = [&](double* dst) {
+      return ok = ok && std::fread(buf.data(), 8, buf.size(), f) == buf.size() &&
+                  cudaMemcpy(dst, buf.data(), buf.size() * 8, cudaMemcpyHostToDevice) == cudaSuccess;
+    };
+    for (int slot = 0; slot < kNt && ok; ++slot)
+      for (int v = 0; v < 5 && ok; ++v) get(d.F(v, slot));
+    for (int c = 0; c < 3 && ok; ++c)
+      for (int w = 0; w < 2 && ok; ++w) get(d.RHS(c, w));
+  }
+  ok = ok && cudaMemcpy(nv->state.ptr, flow, sizeof(flow), cudaMemcpyHostToDevice) == cudaSuccess &&
+       cudaDeviceSynchronize() == cudaSuccess;
+  std::fclose(f);
+  if (!ok) return set_error(MF_ERR_ARG, "mf_navier_load: %s is truncated or inconsistent", path);
+  nv->time = time;
+  for (int i = 0; i < kNt; ++i) nv->it[i] = it[i];
+  nv->rhs_cur = rhs_cur;
+  nv->err_vts = evts;
+  nv->err_pre = epre;
+  for (int i = 0; i < kNt; ++i) nv->nl_ok[i] = false;
   return MF_OK;
 }
 

@@ -48,6 +48,7 @@ module mflops_gpu_f
      integer(c_int) :: les_type
      real(c_double) :: les_c
      integer(c_int) :: nsubite
+     type(c_ptr) :: md_cache_dir
   end type navier_params
 
   type, public :: navier3d_gpu

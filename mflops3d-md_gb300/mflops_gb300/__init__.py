@@ -174,6 +174,12 @@ _PROTOS = {
     "mf_navier_step": [_P, _DP, _P],
     "mf_navier_state": [_P, _DP, _DP, _DP],
     "mf_navier_subiterations": [_P, _IP],
+    "mf_navier_create_md": [_IP, _IP, ctypes.POINTER(_DP), _IP, ctypes.POINTER(_DP), _IP, ctypes.POINTER(_DP), _IP,
+                            _P, ctypes.POINTER(_P)],
+    "mf_navier_subdomains": [_P, _IP],
+    "mf_navier_sub_field": [_P, _I, _I, _I, ctypes.POINTER(_P)],
+    "mf_navier_sub_set_field": [_P, _I, _I, _I, _P, _P],
+    "mf_navier_sub_get_field": [_P, _I, _I, _I, _P, _P],
     "mf_navier_save": [_P, ctypes.c_char_p, _P],
     "mf_navier_load": [_P, ctypes.c_char_p, _P],
 }
@@ -966,7 +972,8 @@ class NavierParams(ctypes.Structure):
                 ("pt", ctypes.c_int), ("tou", ctypes.c_int), ("top", ctypes.c_int),
                 ("so_solver", ctypes.c_int), ("so_der", ctypes.c_int), ("flow_rate", ctypes.c_int),
                 ("nmodes", ctypes.c_int), ("precision", ctypes.c_int), ("refine", ctypes.c_int),
-                ("les_type", ctypes.c_int), ("les_c", ctypes.c_double), ("nsubite", ctypes.c_int)]
+                ("les_type", ctypes.c_int), ("les_c", ctypes.c_double), ("nsubite", ctypes.c_int),
+                ("md_cache_dir", ctypes.c_char_p)]
 
 
 NAVIER_VARS = {"u": 0, "v": 1, "w": 2, "p": 3, "phi": 4}
@@ -981,30 +988,46 @@ class NavierStokes3D:
     top, so_solver, so_der, flow_rate, nmodes, precision, refine, les_type,
     les_c, nsubite)."""
 
-    def __init__(self, gx, gy, gz, **kw):
+    def __init__(self, gx, gy, gz, nd=None, periods=(0, 0, 0), **kw):
+        """One domain: gx, gy, gz are grids.  Multidomain branch: nd = (nd1,
+        nd2, nd3) and gx, gy, gz lists of slab grids (subdomain s = i + nd1
+        (j + nd2 k)), periods per axis."""
         prm = NavierParams()
         _check(_lib.mf_navier_defaults(ctypes.byref(prm)))
         for k, v in kw.items():
             if not hasattr(prm, k):
                 raise TypeError("unknown parameter %s" % k)
-            setattr(prm, k, v)
+            setattr(prm, k, v.encode() if k == "md_cache_dir" and isinstance(v, str) else v)
         self.params = prm
-        gx, xp = _dptr(gx)
-        gy, yp = _dptr(gy)
-        gz, zp = _dptr(gz)
-        self.shape = (gx.size, gy.size, gz.size)
         self._h = ctypes.c_void_p()
-        _check(_lib.mf_navier_create(xp, gx.size, yp, gy.size, zp, gz.size, ctypes.byref(prm),
-                                     ctypes.byref(self._h)))
+        if nd is None:
+            gx, xp = _dptr(gx)
+            gy, yp = _dptr(gy)
+            gz, zp = _dptr(gz)
+            self.shapes = [(gx.size, gy.size, gz.size)]
+            _check(_lib.mf_navier_create(xp, gx.size, yp, gy.size, zp, gz.size, ctypes.byref(prm),
+                                         ctypes.byref(self._h)))
+        else:
+            self._keep = [[np.ascontiguousarray(g, dtype=np.float64) for g in lst] for lst in (gx, gy, gz)]
+            arrs = [(_DP * len(lst))(*[g.ctypes.data_as(_DP) for g in lst]) for lst in self._keep]
+            sizes = [[g.size for g in lst] for lst in self._keep]
+            self.shapes = [(sizes[0][i], sizes[1][j], sizes[2][k]) for k in range(nd[2]) for j in range(nd[1])
+                           for i in range(nd[0])]
+            _check(_lib.mf_navier_create_md(_ivec(nd), _ivec(periods), arrs[0], _ivec(sizes[0]), arrs[1],
+                                            _ivec(sizes[1]), arrs[2], _ivec(sizes[2]), ctypes.byref(prm),
+                                            ctypes.byref(self._h)))
+        self.shape = self.shapes[0]
 
-    def set_field(self, var, level, f, stream=None):
+    def set_field(self, var, level, f, stream=None, sub=0):
         """level 0 = it(1) (written by the next step) ... 3 = it(nt) (newest)."""
-        _check(_lib.mf_navier_set_field(self._h, NAVIER_VARS[var], int(level), _arg(f), _stream(stream)))
+        _check(_lib.mf_navier_sub_set_field(self._h, int(sub), NAVIER_VARS[var], int(level), _arg(f),
+                                            _stream(stream)))
 
-    def field(self, var, level=3, stream=None):
+    def field(self, var, level=3, stream=None, sub=0):
         """Device copy of a field (torch tensor, x fastest)."""
-        out = empty_device(self.shape)
-        _check(_lib.mf_navier_get_field(self._h, NAVIER_VARS[var], int(level), _arg(out), _stream(stream)))
+        out = empty_device(self.shapes[sub])
+        _check(_lib.mf_navier_sub_get_field(self._h, int(sub), NAVIER_VARS[var], int(level), _arg(out),
+                                            _stream(stream)))
         return out
 
     def step(self, diagnostics=False, stream=None):

@@ -211,23 +211,27 @@ class Navier:
             tmp.append(t)
         return self.extrapol(tmp, "v")
 
-    def forcing(self, c):
-        """f(nav,mpid,'rhs'//c)."""
+    def flow_update(self, isum, reft):
+        """Flow-rate term of f (class_navier_3D.f90:1140-1164) from the
+        integral of extrapol(u) and of 1 (over all subdomains)."""
+        err = isum / reft
+        if self.g is None:
+            self.debit = err
+            if self.debit <= THRESH:
+                self.debit = 1.0
+            self.g = 3.0 * self.debit
+        err = err - self.debit
+        self.g = self.g - err * self.fac[0]
+        return self.g
+
+    def forcing(self, c, g=None):
+        """f(nav,mpid,'rhs'//c); g is the flow-rate term (u only)."""
         X, Y, Z = self.points()
         F = sol(X, Y, Z, self.time, "rhs" + c, self.rey, self.nmodes)
         if self.les_type:
             F = F - self.les_forcing(c)
         if c == "u" and self.flow_rate:
-            reft = self.integrale(np.ones_like(F))
-            err = self.integrale(self.extrapol(self.u, "v")) / reft
-            if self.g is None:
-                self.debit = err
-                if self.debit <= THRESH:
-                    self.debit = 1.0
-                self.g = 3.0 * self.debit
-            err = err - self.debit
-            self.g = self.g - err * self.fac[0]
-            F = F + self.g
+            F = F + g
         return F
 
     def les_forcing(self, c):
@@ -249,23 +253,47 @@ class Navier:
         bcz = np.stack([sol(gx[1:-1, None], gy[None, 1:-1], g, t, c, self.rey, m) for g in (gz[0], gz[-1])], -1)
         return [bcx, bcy, bcz]
 
-    # -- the time step -----------------------------------------------------
+    # -- the time step, in stages (a multidomain driver interleaves them with
+    # the collective solves and sums) ------------------------------------
     def step(self):
+        """One pass of the step for one domain."""
+        g = None
+        if self.flow_rate:
+            ones = np.ones((self.nx, self.ny, self.nz))
+            g = self.flow_update(self.integrale(self.extrapol(self.u, "v")), self.integrale(ones))
+        self.stage_presolve(g)
+        if self.pt <= 2:
+            self.velocity_solves()
+        self.stage_phi()
+        self.set_phi(S.solver_3d(self.scp, self.fphi, self.phi[self.it[0]], *self.bcphi, self.sigmap))
+        self.stage_projection()
+        if self.pt >= 3:
+            self.velocity_solves()
+
+    def velocity_solves(self):
+        new = self.it[0]
+        levels = (self.u, self.v, self.w)
+        for q in range(3):
+            fu, bc = self.velocity_rhs(q)
+            levels[q][new] = S.solver_3d(self.scu, fu, levels[q][new], *bc, self.sigmau)
+
+    def stage_presolve(self, g):
+        """Boundary values, navier_LES, presolve u, v, w and (pt = 1) the
+        boundary gradient (navier3d.f90:63-80)."""
         it, fac = self.it, self.fac
-        new, n0, n1, n2 = it[0], it[NT - 1], it[NT - 2], it[NT - 3]
-        bc = {c: self.bc_exact(c) for c in "uvw"}
+        n0 = it[NT - 1]
+        self.bc = {c: self.bc_exact(c) for c in "uvw"}
+        bc = self.bc
         levels = {"u": self.u, "v": self.v, "w": self.w}
         if self.les_type:  # navier_LES on the newest level
             grads = (self.derx, self.dery, self.derz)
             vel = (self.u[n0], self.v[n0], self.w[n0])
             self.du = [[zero_edges(grads[j](vel[i])) for j in range(3)] for i in range(3)]
             self.les_nu = L.les_nu(self.du, self.gx, self.gy, self.gz, self.les_type, self.les_c ** 2)
-        # presolve u, v, w
         for c in "uvw":
             self.rhs[c][1] = self.rhs[c][0]
             nl = self.nonlinear(levels[c])
-            self.rhs[c][0] = zero_edges(self.forcing(c) - nl)
-        # boundary gradient (pt = 1)
+            self.rhs[c][0] = zero_edges(self.forcing(c, g) - nl)
         if self.pt == 1:
             e = self.extrapol(self.phi, "p")
             dx, dy, dz = self.derx(e), self.dery(e), self.derz(e)
@@ -276,29 +304,40 @@ class Navier:
                 bc["w"][1][:, :, m] += dz[1:-1, j, 1:-1] / fac[0]
                 bc["u"][2][:, :, m] += dx[1:-1, 1:-1, k] / fac[0]
                 bc["v"][2][:, :, m] += dy[1:-1, 1:-1, k] / fac[0]
+
+    def velocity_rhs(self, q):
+        """navier_solve_{u,v,w} (:1597-1761): the right-hand side field and
+        the boundary arrays of component q."""
+        it, fac = self.it, self.fac
+        new, n0, n1, n2 = it[0], it[NT - 1], it[NT - 2], it[NT - 3]
+        c = "uvw"[q]
+        lev = (self.u, self.v, self.w)[q]
         grads = (self.derx, self.dery, self.derz)
+        fu = np.zeros((self.nx, self.ny, self.nz))
+        fu = fu + fac[1] * lev[n0] + fac[2] * lev[n1]
+        if self.tou == 3:
+            fu = fu + fac[3] * lev[n2]
+        if self.pt == 2:
+            fu = fu + grads[q](self.extrapol(self.p, "p"))
+        elif self.pt >= 3:
+            fu = fu + grads[q](self.p[new])
+        fu = fu - self.rhs[c][0]
+        fu = self.rey * fu
+        return fu, self.bc[c]
 
-        def solve_velocity():
-            """navier_solve_{u,v,w} (:1597-1761)."""
-            for q, c in enumerate("uvw"):
-                lev = levels[c]
-                fu = np.zeros((self.nx, self.ny, self.nz))
-                fu = fu + fac[1] * lev[n0] + fac[2] * lev[n1]
-                if self.tou == 3:
-                    fu = fu + fac[3] * lev[n2]
-                if self.pt == 2:
-                    fu = fu + grads[q](self.extrapol(self.p, "p"))
-                elif self.pt >= 3:
-                    fu = fu + grads[q](self.p[new])
-                fu = fu - self.rhs[c][0]
-                fu = self.rey * fu
-                lev[new] = S.solver_3d(self.scu, fu, lev[new], *bc[c], self.sigmau)
+    def set_velocity(self, q, field):
+        (self.u, self.v, self.w)[q][self.it[0]] = field
 
-        if self.pt <= 2:
-            solve_velocity()
-        # presolve phi
+    def set_phi(self, field):
+        self.phi[self.it[0]] = field
+
+    def stage_phi(self):
+        """Presolve phi, the right-hand side and the Neumann data of the
+        phi solve (:1764-1845, 342-393, 793-846)."""
+        fac = self.fac
+        levels = {"u": self.u, "v": self.v, "w": self.w}
+        bc = self.bc
         rp = [self.phi_rhs(levels[c], self.rhs[c]) for c in "uvw"]
-        # solve phi
         fphi = self.sigmap * self.extrapol(self.phi, "p")
         fphi = fphi + self.derx(rp[0]) + self.dery(rp[1]) + self.derz(rp[2])
         nx, ny, nz = self.nx, self.ny, self.nz
@@ -307,8 +346,14 @@ class Navier:
                  np.stack([rp[2][1:-1, 1:-1, m * (nz - 1)] - fac[0] * bc["w"][2][:, :, m] for m in (0, 1)], -1)]
         if self.pt == 3:
             self.add_boundary_rotrot(bcphi)
-        self.phi[new] = S.solver_3d(self.scp, fphi, self.phi[new], *bcphi, self.sigmap)
-        # projection
+        self.rp, self.fphi, self.bcphi = rp, fphi, bcphi
+
+    def stage_projection(self):
+        """navier_projection (:1847-1959)."""
+        new, fac = self.it[0], self.fac
+        levels = {"u": self.u, "v": self.v, "w": self.w}
+        grads = (self.derx, self.dery, self.derz)
+        rp = self.rp
         self.phi[new] = zero_edges(self.phi[new])
         if self.pt in (2, 4):
             aux = self.extrapol(self.p, "p")
@@ -326,9 +371,6 @@ class Navier:
         self.p[new] = zero_edges(self.p[new])
         for q, c in enumerate("uvw"):
             levels[c][new] = zero_edges((rp[q] - grads[q](self.phi[new])) / fac[0])
-        # velocity correction (pt >= 3)
-        if self.pt >= 3:
-            solve_velocity()
 
     def phi_rhs(self, var, fvar):
         """navier_phi_rhs with subite = 1 (class_navier_3D.f90:1961-2007)."""
@@ -434,3 +476,150 @@ class Navier:
         self.subite = 1
         self.rotate()
         return d
+
+
+class NavierMD:
+    """Multidomain branch of the step (``mpid%dims /= 0``, navier3d.f90 with
+    class_navier_3D.f90): one ``Navier`` per subdomain for the local stages;
+    the velocity solves and the phi solve through ``multidomain_solve``
+    (oracle.md.MultiDomain; velocity Dirichlet on the outer faces with
+    sigmau, pressure Neumann with sigma 0 and the constant null space,
+    psm = 1: class_navier_3D.f90:1641-1648, 1829-1834, 2157-2160); sums over
+    all subdomains for the flow-rate term, the diagnostics and testconv
+    (md_mpi_reduce_double_sum).  Interface faces take no boundary values
+    (erase_boundary_inter :626-648): the solve ignores them."""
+
+    def __init__(self, nd, periods, gx, gy, gz, ts, rey, so=(6, 6), **kw):
+        from oracle import md as omd
+        self.mdu = omd.MultiDomain(nd, periods, gx, gy, gz, (1,) * 6, so[0], so[1])
+        self.mdp = omd.MultiDomain(nd, periods, gx, gy, gz, (2,) * 6, so[0], so[1])
+        self.subs = self.mdu.subdomains()
+        self.dom = {c: Navier(gx[c[0]], gy[c[1]], gz[c[2]], ts, rey, so=so, **kw) for c in self.subs}
+        d0 = self.dom[self.subs[0]]
+        self.pt, self.flow_rate, self.nsubite, self.ts = d0.pt, d0.flow_rate, d0.nsubite, d0.ts
+        self.sigmau = d0.sigmau
+        self.mdu.influence_matrix(self.sigmau, 0)
+        self.mdp.influence_matrix(0.0, 1)
+        self.err_vts_t = 0.0
+        self.err_pre_t = 0.0
+        self.subiterations = 0
+
+    def doms(self):
+        return [self.dom[c] for c in self.subs]
+
+    def sum_integrale(self, fields):
+        return sum(d.integrale(f) for d, f in zip(self.doms(), fields))
+
+    def sum_norme(self, fields):
+        return float(np.sqrt(sum(float(np.sum(d.W * f * f)) for d, f in zip(self.doms(), fields))))
+
+    def ones(self):
+        return [np.ones((d.nx, d.ny, d.nz)) for d in self.doms()]
+
+    def velocity_solves(self):
+        for q in range(3):
+            rhs, bc = {}, {}
+            for c in self.subs:
+                rhs[c], bc[c] = self.dom[c].velocity_rhs(q)
+            sol, _ = self.mdu.solve(rhs, bc, self.sigmau)
+            for c in self.subs:
+                self.dom[c].set_velocity(q, sol[c])
+
+    def step(self):
+        doms = self.doms()
+        g = None
+        if self.flow_rate:
+            isum = self.sum_integrale([d.extrapol(d.u, "v") for d in doms])
+            g = doms[0].flow_update(isum, self.sum_integrale(self.ones()))
+            for d in doms[1:]:
+                d.g, d.debit = doms[0].g, doms[0].debit
+        for d in doms:
+            d.stage_presolve(g)
+        if self.pt <= 2:
+            self.velocity_solves()
+        for d in doms:
+            d.stage_phi()
+        sol, _ = self.mdp.solve({c: self.dom[c].fphi for c in self.subs},
+                                {c: self.dom[c].bcphi for c in self.subs}, 0.0)
+        for c in self.subs:
+            self.dom[c].set_phi(sol[c])
+        for d in doms:
+            d.stage_projection()
+        if self.pt >= 3:
+            self.velocity_solves()
+
+    def testconv(self, eps=1e-9):
+        doms = self.doms()
+        new = doms[0].it[0]
+        vel = [(d.u[new], d.v[new], d.w[new]) for d in doms]
+        ref = self.sum_norme([np.sqrt(u ** 2 + v ** 2 + w ** 2) for u, v, w in vel])
+        e1 = self.sum_norme([np.sqrt((d.sub[0] - u) ** 2 + (d.sub[1] - v) ** 2 + (d.sub[2] - w) ** 2)
+                             for d, (u, v, w) in zip(doms, vel)]) / ref
+        refi = self.sum_integrale(self.ones())
+        m = self.sum_integrale([d.p[new] - d.sub[3] for d in doms]) / refi
+        sp = [d.sub[3] + m for d in doms]
+        e2 = self.sum_norme([d.p[new] - s for d, s in zip(doms, sp)]) / self.sum_norme(sp)
+        return e1 < eps and e2 < eps
+
+    def diagnostics(self):
+        """navier3d.f90:120-254 with the sums over all subdomains."""
+        doms = self.doms()
+        cur, prev = doms[0].it[NT - 1], doms[0].it[NT - 2]
+        out = {}
+        ones = self.ones()
+        ref = self.sum_norme(ones)
+        out["div"] = self.sum_norme([d.derx(d.u[cur]) + d.dery(d.v[cur]) + d.derz(d.w[cur]) for d in doms]) / ref
+        ue, pex = [], []
+        for d in doms:
+            X, Y, Z = d.points()
+            ue.append([sol(X, Y, Z, d.time, c, d.rey, d.nmodes) for c in "uv"] + [np.zeros_like(X)])
+            pex.append(sol(X, Y, Z, d.time, "p", d.rey, d.nmodes))
+        ref = self.sum_norme([np.sqrt(e[0] ** 2 + e[1] ** 2 + e[2] ** 2) for e in ue])
+        err = self.sum_norme([np.sqrt((e[0] - d.u[cur]) ** 2 + (e[1] - d.v[cur]) ** 2 + (e[2] - d.w[cur]) ** 2)
+                              for d, e in zip(doms, ue)])
+        self.err_vts_t += err ** 2 * self.ts
+        out["vel"] = (err, err / ref, np.sqrt(self.err_vts_t))
+        ref = self.sum_integrale(ones)
+        mean = self.sum_integrale([d.p[cur] for d in doms])
+        for d in doms:
+            d.p[cur] = d.p[cur] - mean / ref
+        pm = self.sum_integrale(pex)
+        pex = [x - pm / ref for x in pex]
+        refp = self.sum_norme(pex)
+        err = self.sum_norme([d.p[cur] - x for d, x in zip(doms, pex)])
+        self.err_pre_t += err ** 2 * self.ts
+        out["pres"] = (err, err / refp, np.sqrt(self.err_pre_t))
+        reft = ref
+        nu_, nv_, nw_ = (self.sum_norme([getattr(d, a)[cur] for d in doms]) for a in "uvw")
+        out["kinetic"] = 0.5 * (nu_ ** 2 + nv_ ** 2 + nw_) / reft
+        aux = [d.p[cur] - d.p[prev] for d in doms]
+        am = self.sum_integrale(aux)
+        e = self.sum_norme([a - am / reft for a in aux])
+        out["station_p"] = (e, e / reft)
+        e2 = (self.sum_norme([d.u[cur] - d.u[prev] for d in doms]) ** 2
+              + self.sum_norme([d.v[cur] - d.v[prev] for d in doms]) ** 2
+              + self.sum_norme([d.w[cur] - d.w[prev] for d in doms]))
+        out["station_v"] = (np.sqrt(e2), np.sqrt(e2) / reft)
+        return out
+
+    def advance(self, diagnostics=False):
+        doms = self.doms()
+        for d in doms:
+            d.time += d.ts
+        out = None
+        for subite in range(1, self.nsubite + 1):
+            for d in doms:
+                d.subite = subite
+            self.step()
+            test = subite > 1 and self.testconv()
+            for d in doms:
+                d.sub = [f[d.it[0]].copy() for f in (d.u, d.v, d.w, d.p)]
+            if diagnostics:
+                out = self.diagnostics()
+            self.subiterations = subite
+            if test:
+                break
+        for d in doms:
+            d.subite = 1
+            d.rotate()
+        return out
