@@ -58,6 +58,9 @@ def parse():
                          "at 160^3, a training step on 65,536 points, six Navier-Stokes steps at "
                          "128x129x128), and exit")
     ap.add_argument("--refine", type=int, default=1)
+    ap.add_argument("--navier-config4", action="store_true",
+                    help="time the NS step of the periodic (x, z) channel at 128x129x128 (two ~32k-unknown "
+                         "influence matrices built first, minutes) and exit")
     ap.add_argument("--md-config2", action="store_true",
                     help="measure the 2x2x2 multidomain configuration at its full slab sizes "
                          "(seeded draw from {49, 65, 97}; ~3 minutes of influence-matrix set-up) and exit")
@@ -725,7 +728,31 @@ def row_measurements(mf, torch, hbm):
         nav.step()
     out["navier_step_les_96x97x96"] = {"eager_ms": time_fn(nav.step, reps=8)}
     nav.close()
+    out["navier_step_channel_periodic_xz_64x65x64"] = navier_channel(mf, torch, 64, time_fn, field)
     return out
+
+
+def navier_channel(mf, torch, n, time_fn, field, steps=8):
+    """The multidomain branch of the NS step on one box periodic in x and z
+    (the reference runs its channel this way): n x (n+1) x n nodes, x, z
+    uniform on [0, 2], y tanh(2.0); influence-matrix set-up time and the
+    step time (3xTF32 + 1 refinement is not used here: the multidomain solves
+    are FP64)."""
+    from oracle import mesh
+    gx, gy, gz = [mesh.uniform_grid(n, 0.0, 2.0)], [mesh.tanh_grid(n + 1, 2.0)], [mesh.uniform_grid(n, 0.0, 2.0)]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    nav = mf.NavierStokes3D(gx, gy, gz, nd=(1, 1, 1), periods=(1, 0, 1), ts=1e-3, reynolds=180.0)
+    torch.cuda.synchronize()
+    setup = time.perf_counter() - t0
+    for lev in range(4):
+        for q, var in enumerate("uvw"):
+            nav.set_field(var, lev, field((n, n + 1, n), 140 + 4 * q + lev))
+    for _ in range(4):
+        nav.step()
+    ms = time_fn(nav.step, reps=steps)
+    nav.close()
+    return {"setup_s": setup, "eager_ms": ms}
 
 
 def run_md_config2(args):
@@ -858,6 +885,28 @@ def main():
         return
     if args.md_config2:
         run_md_config2(args)
+        return
+    if args.navier_config4:
+        import torch
+        import mflops_gb300 as mf
+
+        def time_fn(fn, reps=5):
+            fn()
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            for _ in range(reps):
+                fn()
+            b.record()
+            torch.cuda.synchronize()
+            return a.elapsed_time(b) / reps
+
+        def field(shape, seed):
+            gen = torch.Generator("cuda").manual_seed(seed)
+            return torch.rand(tuple(reversed(shape)), dtype=torch.float64, device="cuda",
+                              generator=gen).permute(*reversed(range(len(shape))))
+        print(json.dumps({"navier_step_channel_periodic_xz_128x129x128":
+                          navier_channel(mf, torch, 128, time_fn, field, steps=4)}), flush=True)
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
