@@ -323,6 +323,17 @@ int mf_md_save_factor(const mf_md_t* md, const char* path);
 int mf_md_load_factor(mf_md_t* md, double sigma, int null_mode, const char* path, void* stream);
 int mf_md_influence_matrix_cached(mf_md_t* md, double sigma, int null_mode, const char* dir, void* stream);
 
+/* How mf_md_influence_matrix_set forms the influence columns (no reference
+ * counterpart: the reference solves one subdomain problem per Dirac column,
+ * class_field.f90:1396-1510).  MF_MD_ASSEMBLY_EIGEN (default): in each
+ * subdomain solver's eigenbasis, where a Dirac datum is separable, one
+ * face-to-face block of n^5 FP64 work per pair of interface faces.
+ * MF_MD_ASSEMBLY_SOLVES: batched subdomain solves of all Dirac columns and
+ * derivative sweeps, n^4 work per column.  The two agree to rounding. */
+#define MF_MD_ASSEMBLY_EIGEN 0
+#define MF_MD_ASSEMBLY_SOLVES 1
+int mf_md_set_assembly(mf_md_t* md, int mode);
+
 /* Copies the last interface solution (ninf values) to host memory. */
 int mf_md_interface(const mf_md_t* md, double* lambda);
 

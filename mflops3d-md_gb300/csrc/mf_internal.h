@@ -77,6 +77,21 @@ struct DevBuf {
   template <class T> T* as() const { return static_cast<T*>(ptr); }
 };
 
+// Read-only view of one axis of a solver's set-up (device arrays): n
+// interior points, eigenvectors V (row-major n x n, V[i n + p]) and their
+// inverse, eigenvalues, the four fold columns of inv_lhs (invl4[c n + i],
+// c = 0..3 for the columns 1, 2, n-1, n) with their ddr factors bcc, the
+// boundary types of the two ends and the Neumann extrapolation weights
+// (neum[0..6] left, neum[7..13] right).
+struct SolverAxisView {
+  int n;
+  const double *V, *Vinv, *eig, *invl4;
+  double bcc[4];
+  int bc[2];
+  double neum[14];
+};
+int solver_axis_view(const ::mf_solver3d* sc, int axis, SolverAxisView* out);
+
 // Copies host -> device buffer (growing it) on stream; returns MF_OK or error.
 int stage_in(DevBuf& buf, const void* host, size_t bytes, cudaStream_t s);
 

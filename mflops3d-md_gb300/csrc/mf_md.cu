@@ -304,6 +304,110 @@ __global__ void __launch_bounds__(kTriThreads) k_tri_step(const double* __restri
   }
 }
 
+// Influence-matrix assembly in the eigenbasis of the subdomain solver.  A
+// Dirac datum at point (s1, s2) of face (l, m) folds into the right-hand
+// side phi_{l,m}(i_l) delta(s1) delta(s2) (phi = -inv_lhs(:, ends) ddr bc),
+// whose transform is separable: psi(p_l) Vinv_b1[q, s1] Vinv_b2[r, s2] with
+// psi = Vinv_l phi.  The column entries are the normal derivatives of the
+// solution on the interface faces, i.e. linear functionals omega(p) =
+// sum_i W_eff[i] V[i, p] of the transformed solution along the target axis
+// (W_eff: the face row of the full-line derivative, with the Neumann end
+// extrapolated from the interior).  So a face-to-face block is
+//   same axis:  (V_b1 (x) V_b2) diag(G) (Vinv_b1 (x) Vinv_b2),
+//               G(q, r) = sum_p omega(p) psi(p) / den(p, q, r),
+//   cross axes: sum_{p_k} V_k[i_k, p_k] H[i_l, i_l2, p_k] Vinv_k[p_k, i'_k],
+// n^5 work per block instead of one n^4 solve per Dirac column.
+struct Lam3 {
+  const double* lam[3];  // eigenvalues of the x, y, z axes
+};
+
+// 1 / (lam_x + lam_y + lam_z + sigma), 0 for the null mode (the eigenvalue
+// division of solve_3d, class_solver_3d.f90:202-225).
+__device__ __forceinline__ double inv_den(const Lam3& L, const int idx[3], double sigma) {
+  const double a = L.lam[0][idx[0]], b = L.lam[1][idx[1]], c = L.lam[2][idx[2]];
+  if (fmax(fmax(fabs(sigma), fabs(a)), fmax(fabs(b), fabs(c))) < (double)1e-11f) return 0.0;
+  return 1.0 / (((a + b) + c) + sigma);
+}
+
+// G[q + n1 r] = sum_p w[p] / den, with p on axis l, q on b1, r on b2.
+__global__ void k_inf_g(Lam3 L, double sigma, int l, int b1, int b2, int nl, int n1, int n2,
+                        const double* __restrict__ w, double* __restrict__ G) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n1 * n2) return;
+  int idx[3];
+  idx[b1] = t % n1;
+  idx[b2] = t / n1;
+  double acc = 0.0;
+  for (int p = 0; p < nl; ++p) {
+    idx[l] = p;
+    acc = fma(w[p], inv_den(L, idx, sigma), acc);
+  }
+  G[t] = acc;
+}
+
+// F[p_l + nl (i2 + n2 p_k)] = sum_{p2} Y[p2 n2 + i2] / den(p_l, p2, p_k),
+// axes l, l2, k; Y = diag(omega) Vinv_l2.
+__global__ void k_inf_f(Lam3 L, double sigma, int l, int l2, int k, int nl, int n2, int nk,
+                        const double* __restrict__ Y, double* __restrict__ F) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)nl * n2 * nk) return;
+  const int pl = (int)(t % nl), i2 = (int)((t / nl) % n2), pk = (int)(t / ((long long)nl * n2));
+  int idx[3];
+  idx[l] = pl;
+  idx[k] = pk;
+  double acc = 0.0;
+  for (int p2 = 0; p2 < n2; ++p2) {
+    idx[l2] = p2;
+    acc = fma(Y[p2 * n2 + i2], inv_den(L, idx, sigma), acc);
+  }
+  F[t] = acc;
+}
+
+// H[i_l + nl (i2 + n2 p_k)] = sum_{p_l} Z[i_l nl + p_l] F[p_l + nl (i2 + n2 p_k)], Z = V_l diag(psi).
+__global__ void k_inf_h(const double* __restrict__ Z, const double* __restrict__ F, int nl, int n2, int nk,
+                        double* __restrict__ H) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)nl * n2 * nk) return;
+  const int il = (int)(t % nl);
+  const long long rest = t / nl;
+  const double* f = F + rest * nl;
+  double acc = 0.0;
+  for (int p = 0; p < nl; ++p) acc = fma(Z[il * nl + p], f[p], acc);
+  H[t] = acc;
+}
+
+// Placement of a batched product in a linear array:
+// index = r0 + i ri + b1 rb1 + b2 rb2 + ld (c0 + j cj + b1 cb1 + b2 cb2).
+struct Place {
+  long long r0, ri, rb1, rb2, c0, cj, cb1, cb2, ld;
+  double scale;
+  int add;  // 1: out += scale v; 0: out = scale v
+};
+
+// out_b[i, j] = sum_q A[i K + q] u_b[q] B[q nj + j] for batch b = (b1, b2),
+// u_b[q] = U[b1 us1 + b2 us2 + q uq].  Grid (ceil(ni nj / 256), nb1 nb2).
+__global__ void __launch_bounds__(256) k_inf_adb(const double* __restrict__ A, const double* __restrict__ B, int ni,
+                                                 int nj, int K, const double* __restrict__ U, long long us1,
+                                                 long long us2, long long uq, int nb1, double* out, Place P) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ni * nj) return;
+  const int j = t % nj, i = t / nj;
+  const int b1 = (int)(blockIdx.y % nb1), b2 = (int)(blockIdx.y / nb1);
+  const double* u = U + b1 * us1 + b2 * us2;
+  const double* a = A + (long long)i * K;
+  double acc = 0.0;
+  for (int q = 0; q < K; ++q) acc = fma(a[q] * u[q * uq], B[(long long)q * nj + j], acc);
+  const long long o = P.r0 + i * P.ri + b1 * P.rb1 + b2 * P.rb2 + P.ld * (P.c0 + j * P.cj + b1 * P.cb1 + b2 * P.cb2);
+  out[o] = P.add ? out[o] + P.scale * acc : P.scale * acc;
+}
+
+// M[(row0 + q) + ld (col0 + q)] += v for q < npts (the Dirac's own end value
+// on the derivative line through it).
+__global__ void k_inf_direct(double* M, long long ld, long long row0, long long col0, long long npts, double v) {
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < npts) M[(row0 + q) + ld * (col0 + q)] += v;
+}
+
 // Largest interface system whose explicit inverse is formed at set-up.
 constexpr long long kMaxInverseRows = 12000;
 
@@ -404,6 +508,8 @@ struct mf_md {
   double sigma = 0.0;
   bool factored = false;
   uint64_t geom_key = 0;  // hash of the decomposition, grids, boundary types and order
+  int assembly = MF_MD_ASSEMBLY_EIGEN;
+  DevBuf inf_w[5];  // eigenbasis assembly: small vectors/matrices, G, stage, F, H
 };
 
 namespace mf {
@@ -642,34 +748,17 @@ int mf_md_ninf(const mf_md_t* md, long long* ninf, int* it) {
   return MF_OK;
 }
 
-static int md_factor_finish(mf_md* md, cudaStream_t st);
-
-int mf_md_influence_matrix_set(mf_md_t* md, double sigma, int null_mode, void* stream) {
-  if (!md || null_mode < 0 || null_mode > 2)
-    return set_error(MF_ERR_ARG, "mf_md_influence_matrix_set: bad arguments");
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
+// Influence columns by solves: all Dirac columns of one subdomain face
+// solved together, in chunks of B problems: one batched solve (zero
+// right-hand side and zero data on the other faces shared between the
+// problems), one batched derivative sweep per axis (the B fields stacked
+// along z, or viewed as (nx*ny, nz, B) for z lines, all lines plain: the
+// gathered face values come from interior lines only), and one batched
+// gather into B consecutive columns.
+static int md_assemble_solves(mf_md* md, double* M, cudaStream_t st) {
   const long long n = md->topo.ninf;
-  if (n == 0) return set_error(MF_ERR_ARG, "mf_md_influence_matrix_set: no interface");
-  md->sigma = sigma;
-  md->null_mode = null_mode;
-  int rc;
-  if ((rc = md->M.ensure(sizeof(double) * n * n)) || (rc = md->ipiv.ensure(sizeof(int) * n)) ||
-      (rc = md->info.ensure(sizeof(int))))
-    return rc;
-  MF_CUDA(cudaMemsetAsync(md->M.ptr, 0, sizeof(double) * n * n, st));
-  double* M = md->M.as<double>();
-  double* u = md->ufield.as<double>();
   const MdTopology& t = md->topo;
-  // md_influence_matrix_set: a Dirac on every interface point of every
-  // subdomain, solved with g = 0; the signed normal derivatives on the
-  // subdomain's interface faces, negated, form that point's column.
-  // All Dirac columns of one subdomain face are solved together, in chunks
-  // of B problems: one batched solve (zero right-hand side and zero data on
-  // the other faces shared between the problems), one batched derivative
-  // sweep per axis (the B fields stacked along z, or viewed as (nx*ny, nz, B)
-  // for z lines, all lines plain: the gathered face values come from
-  // interior lines only), and one batched gather into B consecutive columns.
-  (void)u;
+  int rc;
   for (int k = 0; k < t.nd[2]; ++k)
     for (int j = 0; j < t.nd[1]; ++j)
       for (int i = 0; i < t.nd[0]; ++i) {
@@ -732,6 +821,177 @@ int mf_md_influence_matrix_set(mf_md_t* md, double sigma, int null_mode, void* s
             }
           }
       }
+  return MF_OK;
+}
+
+// Influence columns in the eigenbasis of each subdomain solver (see
+// k_inf_g): per subdomain and pair of interface faces one block of n^5
+// work.  The face-row derivative weights come from the subdomain's own
+// derivative coefficients applied to unit vectors, the Neumann ends are the
+// solver's extrapolation of the interior, and every block is placed
+// straight into the matrix with the sign of the gathered derivatives.
+static int md_assemble_eigen(mf_md* md, double* M, cudaStream_t st) {
+  const long long n = md->topo.ninf;
+  const MdTopology& t = md->topo;
+  int rc;
+  // the batched products put one face-point pair per CTA row (grid.y): fall
+  // back to the solves beyond 65,535
+  for (const mf_md::Sub& sd : md->sub)
+    for (int a = 0; a < 3; ++a)
+      for (int b = 0; b < 3; ++b)
+        if ((long long)(sd.n[a] - 2) * (sd.n[b] - 2) > 65535) return md_assemble_solves(md, M, st);
+  for (int k = 0; k < t.nd[2]; ++k)
+    for (int j = 0; j < t.nd[1]; ++j)
+      for (int i = 0; i < t.nd[0]; ++i) {
+        bool any = false;
+        for (int l = 0; l < 3; ++l)
+          for (int m = 0; m < 2; ++m) any = any || t.get(i, j, k, l, m) > 0;
+        if (!any) continue;
+        mf_md::Sub& sd = md->sub[md_sub_index(md, i, j, k)];
+        SolverAxisView ax[3];
+        std::vector<double> V[3], Vi[3], omega[3][2], psi[3][2], W[3][2];
+        for (int a = 0; a < 3; ++a) {
+          if ((rc = solver_axis_view(sd.sc, a, &ax[a]))) return rc;
+          const int na = ax[a].n, L = na + 2;
+          V[a].resize((size_t)na * na);
+          Vi[a].resize((size_t)na * na);
+          std::vector<double> l4((size_t)4 * na);
+          MF_CUDA(cudaMemcpy(V[a].data(), ax[a].V, sizeof(double) * na * na, cudaMemcpyDeviceToHost));
+          MF_CUDA(cudaMemcpy(Vi[a].data(), ax[a].Vinv, sizeof(double) * na * na, cudaMemcpyDeviceToHost));
+          MF_CUDA(cudaMemcpy(l4.data(), ax[a].invl4, sizeof(double) * 4 * na, cudaMemcpyDeviceToHost));
+          // rows 0 and L-1 of the full-line derivative (plain lines, as the
+          // gathered face derivatives), from unit pencils
+          std::vector<double> I((size_t)L * L, 0.0), D((size_t)L * L);
+          for (int q = 0; q < L; ++q) I[(size_t)q * L + q] = 1.0;
+          if ((rc = mf_der_lines(sd.dc[a], 1, 0, I.data(), D.data(), L, st))) return rc;
+          for (int m2 = 0; m2 < 2; ++m2) {
+            W[a][m2].resize(L);
+            for (int q = 0; q < L; ++q) W[a][m2][q] = D[(size_t)q * L + (m2 ? L - 1 : 0)];
+            std::vector<double> weff(W[a][m2].begin() + 1, W[a][m2].begin() + 1 + na);
+            const double* d = ax[a].neum;
+            if (ax[a].bc[0] == 2 || ax[a].bc[0] == 3)
+              for (int mm = 1; mm <= 6 && mm - 1 < na; ++mm) weff[mm - 1] += W[a][m2][0] * (-d[mm] * (1.0 / d[0]));
+            if (ax[a].bc[1] == 2 || ax[a].bc[1] == 3)
+              for (int mm = 0; mm < 6; ++mm)
+                if (na - 6 + mm >= 0) weff[na - 6 + mm] += W[a][m2][L - 1] * (-d[7 + mm] * (1.0 / d[13]));
+            omega[a][m2].assign(na, 0.0);
+            for (int p = 0; p < na; ++p) {
+              double acc = 0.0;
+              for (int q = 0; q < na; ++q) acc += weff[q] * V[a][(size_t)q * na + p];
+              omega[a][m2][p] = acc;
+            }
+          }
+          for (int m = 0; m < 2; ++m) {
+            const int c0 = m ? 2 : 0, c1 = m ? 3 : 1;
+            std::vector<double> phi(na);
+            for (int q = 0; q < na; ++q)
+              phi[q] = -(l4[(size_t)c0 * na + q] * ax[a].bcc[c0] + l4[(size_t)c1 * na + q] * ax[a].bcc[c1]);
+            psi[a][m].assign(na, 0.0);
+            for (int p = 0; p < na; ++p) {
+              double acc = 0.0;
+              for (int q = 0; q < na; ++q) acc += Vi[a][(size_t)p * na + q] * phi[q];
+              psi[a][m][p] = acc;
+            }
+          }
+        }
+        const Lam3 L3{{ax[0].eig, ax[1].eig, ax[2].eig}};
+        const long long n3max = (long long)std::max({ax[0].n, ax[1].n, ax[2].n});
+        if ((rc = md->inf_w[0].ensure(sizeof(double) * 2 * n3max * n3max)) ||
+            (rc = md->inf_w[1].ensure(sizeof(double) * n3max * n3max)) ||
+            (rc = md->inf_w[2].ensure(sizeof(double) * n3max * n3max * n3max)) ||
+            (rc = md->inf_w[3].ensure(sizeof(double) * n3max * n3max * n3max)) ||
+            (rc = md->inf_w[4].ensure(sizeof(double) * n3max * n3max * n3max)))
+          return rc;
+        double* small = md->inf_w[0].as<double>();
+        double* G = md->inf_w[1].as<double>();
+        double* Ust = md->inf_w[2].as<double>();
+        double* F = md->inf_w[3].as<double>();
+        double* H = md->inf_w[4].as<double>();
+        for (int m = 0; m < 2; ++m)
+          for (int l = 0; l < 3; ++l) {
+            const int p = t.get(i, j, k, l, m);
+            if (p <= 0) continue;
+            const long long col0 = t.offset[p - 1];
+            for (int m2 = 0; m2 < 2; ++m2)
+              for (int l2 = 0; l2 < 3; ++l2) {
+                const int p2 = t.get(i, j, k, l2, m2);
+                if (p2 <= 0) continue;
+                const long long row0 = t.offset[p2 - 1];
+                const double scale = m2 ? -1.0 : 1.0;
+                if (l2 == l) {
+                  const int b1 = l == 0 ? 1 : 0, b2 = l == 2 ? 1 : 2;
+                  const int nl = ax[l].n, n1 = ax[b1].n, n2 = ax[b2].n;
+                  std::vector<double> w(nl);
+                  for (int q = 0; q < nl; ++q) w[q] = omega[l][m2][q] * psi[l][m][q];
+                  MF_CUDA(cudaMemcpyAsync(small, w.data(), sizeof(double) * nl, cudaMemcpyHostToDevice, st));
+                  k_inf_g<<<nblk((long long)n1 * n2, 256), 256, 0, st>>>(L3, md->sigma, l, b1, b2, nl, n1, n2, small, G);
+                  const Place PA{0, n1, 1, 0, 0, (long long)n1 * n2, 0, 0, 1, 1.0, 0};
+                  k_inf_adb<<<dim3(nblk((long long)n2 * n2, 256), n1), 256, 0, st>>>(
+                      ax[b2].V, ax[b2].Vinv, n2, n2, n2, G, 1, 0, n1, n1, Ust, PA);
+                  const Place PB{row0, 1, n1, 0, col0, 1, 0, n1, n, scale, 1};
+                  k_inf_adb<<<dim3(nblk((long long)n1 * n1, 256), n2 * n2), 256, 0, st>>>(
+                      ax[b1].V, ax[b1].Vinv, n1, n1, n1, Ust, n1, (long long)n1 * n2, 1, n2, M, PB);
+                  k_inf_direct<<<nblk((long long)n1 * n2, 256), 256, 0, st>>>(
+                      M, n, row0, col0, (long long)n1 * n2, scale * W[l][m2][m ? nl + 1 : 0]);
+                } else {
+                  const int k3 = 3 - l - l2;
+                  const int nl = ax[l].n, n2 = ax[l2].n, nk = ax[k3].n;
+                  std::vector<double> YZ((size_t)n2 * n2 + (size_t)nl * nl);
+                  for (int q = 0; q < n2; ++q)
+                    for (int c = 0; c < n2; ++c) YZ[(size_t)q * n2 + c] = omega[l2][m2][q] * Vi[l2][(size_t)q * n2 + c];
+                  double* Zh = YZ.data() + (size_t)n2 * n2;
+                  for (int r = 0; r < nl; ++r)
+                    for (int q = 0; q < nl; ++q) Zh[(size_t)r * nl + q] = V[l][(size_t)r * nl + q] * psi[l][m][q];
+                  MF_CUDA(cudaMemcpyAsync(small, YZ.data(), sizeof(double) * YZ.size(), cudaMemcpyHostToDevice, st));
+                  MF_CUDA(cudaStreamSynchronize(st));  // YZ is a host temporary
+                  const long long cube = (long long)nl * n2 * nk;
+                  k_inf_f<<<nblk(cube, 256), 256, 0, st>>>(L3, md->sigma, l, l2, k3, nl, n2, nk, small, F);
+                  k_inf_h<<<nblk(cube, 256), 256, 0, st>>>(small + (size_t)n2 * n2, F, nl, n2, nk, H);
+                  long long ri, rb1, cj, cb2;
+                  if (l < k3) { rb1 = 1; ri = nl; } else { ri = 1; rb1 = nk; }
+                  if (l2 < k3) { cb2 = 1; cj = n2; } else { cj = 1; cb2 = nk; }
+                  const Place PC{row0, ri, rb1, 0, col0, cj, 0, cb2, n, scale, 1};
+                  k_inf_adb<<<dim3(nblk((long long)nk * nk, 256), nl * n2), 256, 0, st>>>(
+                      ax[k3].V, ax[k3].Vinv, nk, nk, nk, H, 1, nl, (long long)nl * n2, nl, M, PC);
+                }
+                MF_CUDA(cudaGetLastError());
+                MF_CUDA(cudaStreamSynchronize(st));  // the host vectors of this block are reused
+              }
+          }
+      }
+  return MF_OK;
+}
+
+static int md_factor_finish(mf_md* md, cudaStream_t st);
+
+int mf_md_influence_matrix_set(mf_md_t* md, double sigma, int null_mode, void* stream) {
+  if (!md || null_mode < 0 || null_mode > 2)
+    return set_error(MF_ERR_ARG, "mf_md_influence_matrix_set: bad arguments");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const long long n = md->topo.ninf;
+  if (n == 0) return set_error(MF_ERR_ARG, "mf_md_influence_matrix_set: no interface");
+  md->sigma = sigma;
+  md->null_mode = null_mode;
+  int rc;
+  if ((rc = md->M.ensure(sizeof(double) * n * n)) || (rc = md->ipiv.ensure(sizeof(int) * n)) ||
+      (rc = md->info.ensure(sizeof(int))))
+    return rc;
+  MF_CUDA(cudaMemsetAsync(md->M.ptr, 0, sizeof(double) * n * n, st));
+  double* M = md->M.as<double>();
+  double* u = md->ufield.as<double>();
+  const MdTopology& t = md->topo;
+  // md_influence_matrix_set: a Dirac on every interface point of every
+  // subdomain, solved with g = 0; the signed normal derivatives on the
+  // subdomain's interface faces, negated, form that point's column.
+  // All Dirac columns of one subdomain face are solved together, in chunks
+  // of B problems: one batched solve (zero right-hand side and zero data on
+  // the other faces shared between the problems), one batched derivative
+  // sweep per axis (the B fields stacked along z, or viewed as (nx*ny, nz, B)
+  // for z lines, all lines plain: the gathered face values come from
+  // interior lines only), and one batched gather into B consecutive columns.
+  (void)u;
+  if ((rc = md->assembly == MF_MD_ASSEMBLY_SOLVES ? md_assemble_solves(md, M, st) : md_assemble_eigen(md, M, st)))
+    return rc;
   if (null_mode >= 1) {
     k_pin_row0<<<nblk(n, 256), 256, 0, st>>>(M, (int)n);
     MF_CUDA(cudaGetLastError());
@@ -1011,6 +1271,13 @@ int mf_md_solve(mf_md_t* md, const double* const* g, double* const* u, const dou
         if ((rc = md_sub_solve(md, s, sd.rint.as<double>(), u[s], sd.stream))) return rc;
       }
   return join();
+}
+
+int mf_md_set_assembly(mf_md_t* md, int mode) {
+  if (!md || (mode != MF_MD_ASSEMBLY_EIGEN && mode != MF_MD_ASSEMBLY_SOLVES))
+    return set_error(MF_ERR_ARG, "mf_md_set_assembly: bad arguments");
+  md->assembly = mode;
+  return MF_OK;
 }
 
 int mf_md_set_interface_solve(mf_md_t* md, int mode) {

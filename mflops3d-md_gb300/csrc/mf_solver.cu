@@ -1797,6 +1797,21 @@ static int solve_mixed_dev(mf_solver3d* sc, const double* rhs, double sigma, dou
 }
 
 // ---------------------------------------------------------------------------
+int solver_axis_view(const ::mf_solver3d* sc, int axis, SolverAxisView* out) {
+  if (!sc || !out || axis < 0 || axis > 2) return set_error(MF_ERR_ARG, "solver_axis_view: bad arguments");
+  const AxisDev& d = sc->ax[axis];
+  out->n = d.n;
+  out->V = d.V.as<double>();
+  out->Vinv = d.Vinv.as<double>();
+  out->eig = d.eig.as<double>();
+  out->invl4 = d.invl4.as<double>();
+  for (int c = 0; c < 4; ++c) out->bcc[c] = d.bcc[c];
+  out->bc[0] = d.bc[0];
+  out->bc[1] = d.bc[1];
+  for (int m = 0; m < 14; ++m) out->neum[m] = d.neum[m];
+  return MF_OK;
+}
+
 // Allocation-free plain solve (mf_solve_3d_noalloc).
 //
 // For callers that must not allocate device memory while they run: code

@@ -48,6 +48,8 @@ MF_RESID_FF = 0
 MF_RESID_FP64 = 1
 MD_IFACE_AUTO = 0
 MD_IFACE_LU = 1
+MD_ASSEMBLY_EIGEN = 0
+MD_ASSEMBLY_SOLVES = 1
 
 
 class MflopsError(RuntimeError):
@@ -120,6 +122,7 @@ _PROTOS = {
                     ctypes.POINTER(_P), ctypes.POINTER(_P), _P],
     "mf_md_interface": [_P, _DP],
     "mf_md_set_interface_solve": [_P, ctypes.c_int],
+    "mf_md_set_assembly": [_P, ctypes.c_int],
     "mf_md_factor_key": [_P, _D, _I, ctypes.c_char_p],
     "mf_md_save_factor": [_P, ctypes.c_char_p],
     "mf_md_load_factor": [_P, _D, _I, ctypes.c_char_p, _P],
@@ -608,6 +611,10 @@ class MultiDomain:
                                 mk([bc[c][0] for c in subs]), mk([bc[c][1] for c in subs]),
                                 mk([bc[c][2] for c in subs]), _stream(stream)))
         return u
+
+    def set_assembly(self, mode):
+        """MD_ASSEMBLY_EIGEN (default) or MD_ASSEMBLY_SOLVES."""
+        _check(_lib.mf_md_set_assembly(self._h, int(mode)))
 
     def set_interface_solve(self, mode):
         """MD_IFACE_AUTO (inverse when small enough) or MD_IFACE_LU."""
