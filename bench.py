@@ -729,10 +729,12 @@ def row_measurements(mf, torch, hbm):
     out["navier_step_les_96x97x96"] = {"eager_ms": time_fn(nav.step, reps=8)}
     nav.close()
     out["navier_step_channel_periodic_xz_64x65x64"] = navier_channel(mf, torch, 64, time_fn, field)
+    out["navier_step_channel_periodic_xz_64x65x64"]["tf32_subdomain_solves"] = navier_channel(
+        mf, torch, 64, time_fn, field, precision=mf.MF_PREC_3XTF32, refine=1)
     return out
 
 
-def navier_channel(mf, torch, n, time_fn, field, steps=8):
+def navier_channel(mf, torch, n, time_fn, field, steps=8, **kw):
     """The multidomain branch of the NS step on one box periodic in x and z
     (the reference runs its channel this way): n x (n+1) x n nodes, x, z
     uniform on [0, 2], y tanh(2.0); influence-matrix set-up time and the
@@ -742,7 +744,7 @@ def navier_channel(mf, torch, n, time_fn, field, steps=8):
     gx, gy, gz = [mesh.uniform_grid(n, 0.0, 2.0)], [mesh.tanh_grid(n + 1, 2.0)], [mesh.uniform_grid(n, 0.0, 2.0)]
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    nav = mf.NavierStokes3D(gx, gy, gz, nd=(1, 1, 1), periods=(1, 0, 1), ts=1e-3, reynolds=180.0)
+    nav = mf.NavierStokes3D(gx, gy, gz, nd=(1, 1, 1), periods=(1, 0, 1), ts=1e-3, reynolds=180.0, **kw)
     torch.cuda.synchronize()
     setup = time.perf_counter() - t0
     for lev in range(4):
@@ -905,8 +907,11 @@ def main():
             gen = torch.Generator("cuda").manual_seed(seed)
             return torch.rand(tuple(reversed(shape)), dtype=torch.float64, device="cuda",
                               generator=gen).permute(*reversed(range(len(shape))))
-        print(json.dumps({"navier_step_channel_periodic_xz_128x129x128":
-                          navier_channel(mf, torch, 128, time_fn, field, steps=4)}), flush=True)
+        row = navier_channel(mf, torch, 128, time_fn, field, steps=4)
+        row["tf32_subdomain_solves_inverse_interface"] = navier_channel(
+            mf, torch, 128, time_fn, field, steps=4, precision=mf.MF_PREC_3XTF32, refine=1,
+            md_interface=mf.MD_IFACE_INVERSE)
+        print(json.dumps({"navier_step_channel_periodic_xz_128x129x128": row}), flush=True)
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -307,7 +307,14 @@ int mf_md_solve(mf_md_t* md, const double* const* g, double* const* u, const dou
  * by mf_md_influence_matrix_set, so select MF_MD_IFACE_AUTO before it. */
 #define MF_MD_IFACE_AUTO 0
 #define MF_MD_IFACE_LU 1
+/* MF_MD_IFACE_INVERSE: the inverse at any size when it fits in device memory
+ * (2 n^3 FP64 flops at set-up, then one n^2 read per solve; for long runs). */
+#define MF_MD_IFACE_INVERSE 2
 int mf_md_set_interface_solve(mf_md_t* md, int mode);
+/* Precision of the subdomain solves inside mf_md_solve (MF_PREC_FP64, the
+ * default, or a mixed mode with `refine` steps); the influence matrix is
+ * FP64 either way. */
+int mf_md_set_precision(mf_md_t* md, int precision, int refine);
 
 /* On-disk factor cache (the role of md_influence_matrix_filename / _write /
  * _read, class_md.f90:918-956, which name the cached matrix after the grid
@@ -517,6 +524,7 @@ typedef struct {
   double les_c;       /* cmd%les_c; the model coefficient is its square (default 0) */
   int nsubite;        /* sub-iterations per time step (default 1) */
   const char* md_cache_dir;  /* several subdomains: directory of the influence-matrix factor cache, or NULL */
+  int md_interface;   /* several subdomains: MF_MD_IFACE_* of the interface solves (default AUTO) */
 } mf_navier_params_t;
 /* Fills the reference's defaults (command_line.f90:14-35). */
 int mf_navier_defaults(mf_navier_params_t* p);

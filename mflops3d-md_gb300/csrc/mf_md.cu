@@ -509,6 +509,7 @@ struct mf_md {
   bool factored = false;
   uint64_t geom_key = 0;  // hash of the decomposition, grids, boundary types and order
   int assembly = MF_MD_ASSEMBLY_EIGEN;
+  int precision = MF_PREC_FP64, refine = -1;  // subdomain solves of mf_md_solve
   DevBuf inf_w[5];  // eigenbasis assembly: small vectors/matrices, G, stage, F, H
 };
 
@@ -537,6 +538,10 @@ static uint64_t factor_key(const mf_md* md, double sigma, int null_mode) {
 // writing the full field u (interior + faces).
 static int md_sub_solve(mf_md* md, int s, const double* rint, double* u, cudaStream_t st) {
   mf_md::Sub& sd = md->sub[s];
+  if (md->precision != MF_PREC_FP64)
+    return mf_solve_3d_mixed(sd.sc, rint, md->sigma, u, sd.bc[0].as<double>(), sd.bc[1].as<double>(),
+                             sd.bc[2].as<double>(), sd.n[0] - 2, sd.n[1] - 2, sd.n[2] - 2, md->precision,
+                             md->refine, st);
   return mf_solve_3d(sd.sc, rint, md->sigma, u, sd.bc[0].as<double>(), sd.bc[1].as<double>(),
                      sd.bc[2].as<double>(), sd.n[0] - 2, sd.n[1] - 2, sd.n[2] - 2, st);
 }
@@ -1049,7 +1054,7 @@ static int md_factor_finish(mf_md* md, cudaStream_t st) {
   // not fit, or when the triangular form is selected, the solves stay on the
   // LU factors.
   md->inv_ok = false;
-  if (md->iface_mode == MF_MD_IFACE_AUTO && n <= kMaxInverseRows) {
+  if ((md->iface_mode == MF_MD_IFACE_AUTO && n <= kMaxInverseRows) || md->iface_mode == MF_MD_IFACE_INVERSE) {
     const size_t bytes = sizeof(double) * (size_t)n * (size_t)n;
     size_t freeb = 0, totalb = 0;
     MF_CUDA(cudaMemGetInfo(&freeb, &totalb));
@@ -1246,7 +1251,7 @@ int mf_md_solve(mf_md_t* md, const double* const* g, double* const* u, const dou
     k_remove_mean<<<1, 256, 0, st>>>(vec, (int)n);
   }
   if (md->null_mode >= 1) k_set_scalar<<<1, 1, 0, st>>>(vec, 0, 0.0);
-  if (md->inv_ok && md->iface_mode == MF_MD_IFACE_AUTO) {
+  if (md->inv_ok && md->iface_mode != MF_MD_IFACE_LU) {
     k_gemv_rows<<<nblk(32LL * n, 256), 256, 0, st>>>(md->Minv.as<double>(), vec, md->vec2.as<double>(),
                                                       (int)n);
     MF_CUDA(cudaGetLastError());
@@ -1280,8 +1285,16 @@ int mf_md_set_assembly(mf_md_t* md, int mode) {
   return MF_OK;
 }
 
+int mf_md_set_precision(mf_md_t* md, int precision, int refine) {
+  if (!md || (precision != MF_PREC_FP64 && precision != MF_PREC_SPLIT_BF16 && precision != MF_PREC_3XTF32))
+    return set_error(MF_ERR_ARG, "mf_md_set_precision: bad arguments");
+  md->precision = precision;
+  md->refine = refine;
+  return MF_OK;
+}
+
 int mf_md_set_interface_solve(mf_md_t* md, int mode) {
-  if (!md || (mode != MF_MD_IFACE_AUTO && mode != MF_MD_IFACE_LU))
+  if (!md || (mode != MF_MD_IFACE_AUTO && mode != MF_MD_IFACE_LU && mode != MF_MD_IFACE_INVERSE))
     return set_error(MF_ERR_ARG, "mf_md_set_interface_solve: bad arguments");
   md->iface_mode = mode;
   return MF_OK;

@@ -1336,6 +1336,10 @@ int navier_build(const int nd[3], const int periods[3], const double* const* gx,
       return p->md_cache_dir ? mf_md_influence_matrix_cached(m, sigma, null_mode, p->md_cache_dir, nullptr)
                              : mf_md_influence_matrix_set(m, sigma, null_mode, nullptr);
     };
+    for (mf_md_t* m : {nv->mdu, nv->mdp})
+      if ((rc = mf_md_set_interface_solve(m, p->md_interface)) ||
+          (rc = mf_md_set_precision(m, p->precision, p->refine)))
+        return fail(rc);
     if ((rc = build(nv->mdu, nv->sigmau, 0)) || (rc = build(nv->mdp, 0.0, 1))) return fail(rc);
     if (cudaDeviceSynchronize() != cudaSuccess) return fail(set_error(MF_ERR_CUDA, "influence matrices failed"));
   } else {
@@ -1381,6 +1385,7 @@ int mf_navier_defaults(mf_navier_params_t* p) {
   p->les_c = 0.0;
   p->nsubite = 1;
   p->md_cache_dir = nullptr;
+  p->md_interface = MF_MD_IFACE_AUTO;
   return MF_OK;
 }
 

@@ -49,6 +49,7 @@ module mflops_gpu_f
      real(c_double) :: les_c
      integer(c_int) :: nsubite
      type(c_ptr) :: md_cache_dir
+     integer(c_int) :: md_interface
   end type navier_params
 
   type, public :: navier3d_gpu

@@ -48,6 +48,7 @@ MF_RESID_FF = 0
 MF_RESID_FP64 = 1
 MD_IFACE_AUTO = 0
 MD_IFACE_LU = 1
+MD_IFACE_INVERSE = 2
 MD_ASSEMBLY_EIGEN = 0
 MD_ASSEMBLY_SOLVES = 1
 
@@ -123,6 +124,7 @@ _PROTOS = {
     "mf_md_interface": [_P, _DP],
     "mf_md_set_interface_solve": [_P, ctypes.c_int],
     "mf_md_set_assembly": [_P, ctypes.c_int],
+    "mf_md_set_precision": [_P, ctypes.c_int, ctypes.c_int],
     "mf_md_factor_key": [_P, _D, _I, ctypes.c_char_p],
     "mf_md_save_factor": [_P, ctypes.c_char_p],
     "mf_md_load_factor": [_P, _D, _I, ctypes.c_char_p, _P],
@@ -612,6 +614,10 @@ class MultiDomain:
                                 mk([bc[c][2] for c in subs]), _stream(stream)))
         return u
 
+    def set_precision(self, precision, refine=-1):
+        """Precision of the subdomain solves (FP64 default, or a mixed mode)."""
+        _check(_lib.mf_md_set_precision(self._h, int(precision), int(refine)))
+
     def set_assembly(self, mode):
         """MD_ASSEMBLY_EIGEN (default) or MD_ASSEMBLY_SOLVES."""
         _check(_lib.mf_md_set_assembly(self._h, int(mode)))
@@ -980,7 +986,7 @@ class NavierParams(ctypes.Structure):
                 ("so_solver", ctypes.c_int), ("so_der", ctypes.c_int), ("flow_rate", ctypes.c_int),
                 ("nmodes", ctypes.c_int), ("precision", ctypes.c_int), ("refine", ctypes.c_int),
                 ("les_type", ctypes.c_int), ("les_c", ctypes.c_double), ("nsubite", ctypes.c_int),
-                ("md_cache_dir", ctypes.c_char_p)]
+                ("md_cache_dir", ctypes.c_char_p), ("md_interface", ctypes.c_int)]
 
 
 NAVIER_VARS = {"u": 0, "v": 1, "w": 2, "p": 3, "phi": 4}

@@ -51,12 +51,14 @@ def problem(grids, subs, sigma, bct):
     return g, bc, ex
 
 
-def run(mf, nd, periods, nodes, sigma, bct=(1,) * 6, null=0, iface=0):
+def run(mf, nd, periods, nodes, sigma, bct=(1,) * 6, null=0, iface=0, precision=None):
     grids = tuple(slabs(nd[l], nodes[l]) for l in range(3))
     ref = omd.MultiDomain(nd, periods, *grids, bct)
     ref.influence_matrix(sigma, null)
     dev = mf.MultiDomain(nd, periods, *grids, bct)
     dev.set_interface_solve(iface)
+    if precision is not None:
+        dev.set_precision(*precision)
     dev.influence_matrix_set(sigma, null)
     subs = dev.subdomains()
     g, bc, ex = problem(grids, subs, sigma, bct)
@@ -119,6 +121,17 @@ def test_md_interface_forms_agree(mf, gpu):
     b = run(mf, (2, 2, 1), (0, 0, 0), ([11, 15], [13, 9], [11]), -1e3, iface=mf.MD_IFACE_LU)
     assert a[0] < 1e-11 and b[0] < 1e-11
     assert a[1] < 1e-11 and b[1] < 1e-11
+
+
+@pytest.mark.parametrize("nd,periods", [((2, 2, 1), (0, 0, 0)), ((2, 1, 1), (1, 0, 0))])
+def test_md_mixed_subdomain_solves_forced_inverse(mf, gpu, nd, periods):
+    """Subdomain solves with 3xTF32 transforms + two FP64 refinement steps and
+    the interface through the explicit inverse (forced) against the FP64
+    oracle: the influence matrix stays FP64, the subdomain fields carry the
+    refined solves' accuracy."""
+    err, lerr, _, _ = run(mf, nd, periods, (11, 11, 11), -3.0, iface=mf.MD_IFACE_INVERSE,
+                          precision=(mf.MF_PREC_3XTF32, 2))
+    assert err < 1e-10 and lerr < 1e-10, (err, lerr)
 
 
 def test_factor_cache_round_trip(mf, gpu, tmp_path):

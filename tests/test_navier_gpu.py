@@ -279,3 +279,20 @@ def test_multidomain_steps_match_the_oracle(mf, gpu, name):
     if kw.get("nsubite", 1) > 1:
         assert nav.subiterations() == ora.subiterations
     print("%s: worst field max-rel %.2e after 4 steps" % (name, worst))
+
+
+def test_multidomain_mixed_subdomain_solves(mf, gpu):
+    """The multidomain branch with 3xTF32 subdomain solves (FP64 influence
+    matrices, the explicit interface inverse) against the FP64 oracle."""
+    grid_key, kw = MD_CASES["periodic_xz_pt2"]
+    kw = dict(kw, precision=mf.MF_PREC_3XTF32, refine=1, md_interface=mf.MD_IFACE_INVERSE)
+    ora, nav = make_md_pair(mf, grid_key, kw)
+    for _ in range(4):
+        ora.advance()
+        nav.step()
+    for s, c in enumerate(ora.subs):
+        dom = ora.dom[c]
+        for lev in range(N.NT):
+            for var in VARS:
+                err = max_rel(mf.to_host(nav.field(var, lev, sub=s)), getattr(dom, var)[dom.it[lev]])
+                assert err < 1e-8, (s, var, lev, err)
