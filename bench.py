@@ -321,6 +321,12 @@ def run_gb300(args, rank, world, dist):
         mixed()
     resid_ff = {"ms_per_solve": statistics.median(timed(mixed, 5))}
     resid_ff["rel_l2_vs_fp64_gpu"] = err_vs_plain()
+    # and with the FP64 sweeps one thread per line (the two-sided sweeps are the default)
+    sc.set_residual(mf.MF_RESID_FP64_LINE)
+    for _ in range(3):
+        mixed()
+    resid_line = {"ms_per_solve": statistics.median(timed(mixed, 5))}
+    resid_line["rel_l2_vs_fp64_gpu"] = err_vs_plain()
     sc.set_residual(mf.MF_RESID_FP64)
 
     # clock sampler first, so that its samples cover the timed region; the
@@ -492,6 +498,7 @@ def run_gb300(args, rank, world, dist):
                      "fp64_gpu_vs_cpu_oracle": plain_vs_oracle,
                      "rel_l2_by_refine_steps": {str(k): v for k, v in errs.items()}},
         "residual_double_fp32_sweeps": resid_ff,
+        "residual_fp64_sweeps_one_thread_per_line": resid_line,
         "formats": {k: {"precision": names[k], "refine_steps": c["refine"],
                         "ms_per_solve": c["ms"], "solves_per_s": 1e3 / c["ms"],
                         "rel_l2_by_refine_steps": {str(r): v for r, v in c["errs"].items()}}

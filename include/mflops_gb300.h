@@ -47,7 +47,8 @@ extern "C" {
  * double-FP32 throughout (error-free products and sums on the FP32 pipe).
  * Both evaluate the cancelling stencil sums in moment form. */
 #define MF_RESID_FF 0
-#define MF_RESID_FP64 1
+#define MF_RESID_FP64 1       /* FP64 sweeps; two lanes per line (twisted factorisation) on the y, z passes */
+#define MF_RESID_FP64_LINE 2  /* FP64 sweeps, one thread per line */
 
 const char* mf_last_error(void);
 
@@ -227,11 +228,12 @@ int mf_solver_3d(mf_solver3d_t* sc, const double* g, double* u,
 int mf_solver3d_set_eigen(mf_solver3d_t* sc, int axis, const double* eigen, const double* vect,
                           const double* inv_vect);
 
+/* Selects the residual arithmetic (MF_RESID_FP64, default; MF_RESID_FP64_LINE;
+ * MF_RESID_FF) used by the mixed solves of this handle; no counterpart in
+ * the reference. */
+int mf_solver3d_set_residual(mf_solver3d_t* sc, int mode);
 /* Reads and clears the device-side error flag of the tensor-core pipeline
  * (MF_ERR_TIMEOUT if a bounded wait expired since the last call). Syncs. */
-/* Selects the residual arithmetic (MF_RESID_FF or MF_RESID_FP64) used by the
- * mixed solves of this handle; no counterpart in the reference. */
-int mf_solver3d_set_residual(mf_solver3d_t* sc, int mode);
 int mf_solver3d_device_status(mf_solver3d_t* sc);
 
 /* Per-kernel CUDA-event timers of a solver handle (stage timers in the

@@ -47,6 +47,7 @@ struct AxisDev {
   DevBuf invl4f;                               // FP32 copy of invl4
   DevBuf rowsf;                                // FP32 copy of rows
   DevBuf tri;                                  // TriRow[n] when the lhs is tridiagonal
+  DevBuf trib;                                 // bottom table of the two-sided sweeps (TriRow[n-1-(n-1)/2])
   bool tri_ok = false;
   // Null mode (the one eigenvalue below the threshold, when there is exactly
   // one; -1 otherwise): row null_idx of V^-1 and column null_idx of V (FP64)
@@ -386,7 +387,7 @@ struct TriRow {
   float rh, rl;        // rho_i as hi + lo floats
   double ft, dt;       // f_i c_{i-1} / c_i,  d_i / c_i
   double cbc;          // boundary coefficient / c_i (rows 0, 1, n-2, n-1)
-  double pad;
+  double tw;           // twist row of the two-sided sweeps: 1 / (1 - dt_m et_{m+1})
   float fth, ftl, dth, dtl, cbh, cbl;  // ft, dt, cbc as hi + lo floats
   float pad2[2];
 };
@@ -617,6 +618,157 @@ __global__ void __launch_bounds__(128) k_resid_tri(ResidPass<double> p, const Tr
   fin.pstride = p.pstride;
   fin.r32 = r32 ? r32 + base : nullptr;
   solve_line_tri(R, p.n, u + base, scratch + base, p.s, blo, bhi, fin);
+}
+
+// ---- the same residual with two lanes per line (twisted factorisation)
+//
+// With T = L U (L unit lower bidiagonal, sub ft; U unit upper bidiagonal,
+// super dt) the sweeps solve T y = S.  One lane eliminates rows 0..m from
+// the top as above (x_i = S_i - ft_i x_{i-1}); its partner eliminates rows
+// n-1..m+1 from the bottom with the U L factors of the same T
+// (z_i = S_i / q_i - gt_i z_{i+1}, pivots q_i, gt_i = T_{i,i+1} / q_i,
+// et_i = T_{i,i-1} / q_i), each on half the line.  At the twist the two
+// meet: y_m = tw (x_m - dt_m z_{m+1}), y_{m+1} = tw (z_{m+1} - et_{m+1} x_m),
+// tw = 1 / (1 - dt_m et_{m+1}); then each lane substitutes back over its
+// own half (y_i = x_i - dt_i y_{i+1} upwards, y_i = z_i - et_i y_{i-1}
+// downwards).  The bottom lane reads the line mirrored (negative stride)
+// with a table stored in that order (weights reversed and scaled by 1/q_i,
+// gt in `ft`, et in `dt`), so both lanes of a warp run the same
+// instructions: the dependent chain is half as long and the pass has twice
+// the warps of one thread per line, for the same FP64 work.  A warp holds
+// 16 lines: lanes 0-15 the top halves, lanes 16-31 the bottom halves.
+constexpr int kTw = 4;   // rows loaded ahead in the forward elimination of the two-sided sweeps
+constexpr int kTwB = 2;  // ... and in their back substitution
+
+__device__ __forceinline__ void solve_line_twist(const TriRow* __restrict__ R, int n, int cnt,
+                                                 const float* u, double* xs, long long s, double bcv,
+                                                 const ResidFin<double, float>& fin, unsigned mask) {
+  float f[7];
+#pragma unroll
+  for (int m = 0; m < 7; ++m) f[m] = u[(long long)m * s];
+  // rows 0 and 1 of this side: 7-wide stencils on its first seven nodes
+  double x0 = moment_sum<7>(R[0], f, f[0], 0) + R[0].cbc * (bcv - widen(f[0]));
+  double x1 = moment_sum<7>(R[1], f, f[1], 1) + R[1].cbc * (bcv - widen(f[1])) - R[1].ft * x0;
+  xs[0] = x0;
+  xs[s] = x1;
+  double xm = x1;
+  float w[5] = {f[0], f[1], f[2], f[3], f[4]};
+  float pf[kTw];  // pf[k] = u(i + 3 + k)
+#pragma unroll
+  for (int k = 0; k < kTw; ++k) pf[k] = (5 + k < 7) ? f[5 + k] : (5 + k < n) ? u[(long long)(5 + k) * s] : 0.f;
+  int i = 2;
+  for (; i + kTw <= cnt; i += kTw) {
+    float nb[kTw];
+#pragma unroll
+    for (int k = 0; k < kTw; ++k) {
+      const int j = i + 3 + kTw + k;
+      nb[k] = (j < n) ? u[(long long)j * s] : 0.f;
+    }
+#pragma unroll
+    for (int k = 0; k < kTw; ++k) {
+      const TriRow& r = R[i + k];
+      const double x = moment_sum<5>(r, w, w[2], 2) - r.ft * xm;
+      xs[(long long)(i + k) * s] = x;
+      xm = x;
+      w[0] = w[1]; w[1] = w[2]; w[2] = w[3]; w[3] = w[4]; w[4] = pf[k];
+    }
+#pragma unroll
+    for (int k = 0; k < kTw; ++k) pf[k] = nb[k];
+  }
+  for (; i < cnt; ++i) {
+    const TriRow& r = R[i];
+    const double x = moment_sum<5>(r, w, w[2], 2) - r.ft * xm;
+    xs[(long long)i * s] = x;
+    xm = x;
+    w[0] = w[1]; w[1] = w[2]; w[2] = w[3]; w[3] = w[4];
+    if (i + 3 < n) w[4] = u[(long long)(i + 3) * s];
+  }
+  // the twist: this side's last eliminated value and the partner's
+  const double other = __shfl_xor_sync(mask, xm, 16);
+  const bool need_u = fin.mode == 0;
+  auto uval = [&](long long o) { return need_u ? widen(fin.u[o]) : 0.0; };
+  i = cnt - 1;
+  const TriRow& rt = R[i];
+  double y1 = rt.tw * (xm - rt.dt * other);
+  fin.put(i, (long long)i * s, y1, fin.rin[(long long)i * s], uval((long long)i * s));
+  // back substitution over this side's rows cnt-2..0, loads kTwB rows ahead
+  i = cnt - 2;
+  double rb[kTwB], rr[kTwB];
+  float ru[kTwB];
+#pragma unroll
+  for (int k = 0; k < kTwB; ++k) {
+    const bool in = i - k >= 0;
+    const long long o = (long long)(i - k) * s;
+    rb[k] = in ? xs[o] : 0.0;
+    rr[k] = in ? fin.rin[o] : 0.0;
+    ru[k] = (in && need_u) ? fin.u[o] : 0.f;
+  }
+  for (; i - (kTwB - 1) >= 0; i -= kTwB) {
+    double nb[kTwB], nr[kTwB];
+    float nu[kTwB];
+#pragma unroll
+    for (int k = 0; k < kTwB; ++k) {
+      const int j = i - kTwB - k;
+      const long long o = (long long)j * s;
+      nb[k] = (j >= 0) ? xs[o] : 0.0;
+      nr[k] = (j >= 0) ? fin.rin[o] : 0.0;
+      nu[k] = (j >= 0 && need_u) ? fin.u[o] : 0.f;
+    }
+#pragma unroll
+    for (int k = 0; k < kTwB; ++k) {
+      const double yy = rb[k] - R[i - k].dt * y1;
+      fin.put(i - k, (long long)(i - k) * s, yy, rr[k], widen(ru[k]));
+      y1 = yy;
+    }
+#pragma unroll
+    for (int k = 0; k < kTwB; ++k) {
+      rb[k] = nb[k];
+      rr[k] = nr[k];
+      ru[k] = nu[k];
+    }
+  }
+  for (; i >= 0; --i) {
+    const long long o = (long long)i * s;
+    const double yy = xs[o] - R[i].dt * y1;
+    fin.put(i, o, yy, fin.rin[o], uval(o));
+    y1 = yy;
+  }
+}
+
+// Rt: the top table (TriRow[n], rows 0..m used); Rb: the bottom table in
+// mirrored order (TriRow[n - 1 - m], entry k = row n-1-k); m = (n-1)/2.
+__global__ void __launch_bounds__(128) k_resid_twist(ResidPass<double> p, const TriRow* __restrict__ Rt,
+                                                     const TriRow* __restrict__ Rb, const float* u,
+                                                     const double* rin, double* scratch, double* rout,
+                                                     __nv_bfloat16* hi, __nv_bfloat16* lo, float* x32,
+                                                     float* r32) {
+  const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const bool top = lane < 16;
+  const long long lines = (long long)p.na * p.nb;
+  const long long t = (g >> 5) * 16 + (lane & 15);
+  const bool valid = t < lines;
+  const unsigned mask = __ballot_sync(0xffffffffu, valid);  // both lanes of a line agree
+  if (!valid) return;
+  const int a = (int)(t % p.na), b = (int)(t / p.na);
+  const int m = (p.n - 1) >> 1;
+  const int cnt = top ? m + 1 : p.n - 1 - m;
+  const long long base = a * p.sa + b * p.sb + (top ? 0 : (long long)(p.n - 1) * p.s);
+  const long long s = top ? p.s : -p.s;
+  const double bcv = p.bc ? p.bc[t + (top ? 0 : lines)] : 0.0;
+  ResidFin<double, float> fin;
+  fin.mode = p.mode;
+  fin.rin = rin + base;
+  fin.u = u + base;
+  fin.sigma = p.sigma;
+  fin.out = rout ? rout + base : nullptr;
+  const long long pbase = a * p.pa + b * p.pb + (top ? 0 : (long long)(p.n - 1) * p.pstride);
+  fin.hi = hi ? hi + pbase : nullptr;
+  fin.lo = lo ? lo + pbase : nullptr;
+  fin.x32 = x32 ? x32 + pbase : nullptr;
+  fin.pstride = top ? p.pstride : -p.pstride;
+  fin.r32 = r32 ? r32 + base : nullptr;
+  solve_line_twist(top ? Rt : Rb, p.n, cnt, u + base, scratch + base, s, bcv, fin, mask);
 }
 
 // ---- the same residual entirely on the FP32 pipe (double-float sweeps)
@@ -1203,9 +1355,47 @@ static int build_tri_rows(AxisDev& d, const std::vector<double>& rows) {
     split(t.dt, t.dth, t.dtl);
     split(t.cbc, t.cbh, t.cbl);
   }
+  // bottom table of the two-sided sweeps: T = L U has T_{i,i-1} = ft_i,
+  // T_ii = 1 + ft_i dt_{i-1}, T_{i,i+1} = dt_i; its U L pivots from the
+  // bottom q_{n-1} = T_{n-1,n-1}, q_i = T_ii - T_{i,i+1} T_{i+1,i} / q_{i+1}
+  // (rows n-1..m+1); entry k holds row i = n-1-k with the weights (and cbc)
+  // divided by q_i in reversed stencil order, gt_i = dt_i / q_i as ft and
+  // et_i = ft_i / q_i as dt.
+  const int m = (n - 1) / 2, cb = n - 1 - m;
+  std::vector<long double> q(n, 1.0L);
+  auto tdiag = [&](int i) { return 1.0L + (i > 0 ? (long double)tr[i].ft * (long double)tr[i - 1].dt : 0.0L); };
+  q[n - 1] = tdiag(n - 1);
+  for (int i = n - 2; i > m; --i) q[i] = tdiag(i) - (long double)tr[i].dt * (long double)tr[i + 1].ft / q[i + 1];
+  std::vector<TriRow> tb(cb);
+  for (int k = 0; k < cb; ++k) {
+    const int i = n - 1 - k;
+    const double* r = &rows[(size_t)kRow * i];
+    const long double iq = 1.0L / q[i];
+    TriRow& t = tb[k];
+    std::memset(&t, 0, sizeof(t));
+    const int width = (i >= n - 2) ? 7 : 5;
+    t.cbc = (double)((long double)tr[i].cbc * iq);
+    long double rho = (long double)t.cbc;
+    for (int mm = 0; mm < width; ++mm) {
+      const double w = (double)((long double)(r[5 + (width - 1 - mm)] * r[2]) * iq);
+      rho += (long double)w;
+      t.wh[mm] = (float)w;
+      t.wl[mm] = (float)(w - (double)t.wh[mm]);
+    }
+    const double rd = (double)rho;
+    t.rh = (float)rd;
+    t.rl = (float)(rd - (double)t.rh);
+    t.ft = (double)((long double)tr[i].dt * iq);
+    t.dt = (double)((long double)tr[i].ft * iq);
+  }
+  const long double tw = 1.0L / (1.0L - (long double)tr[m].dt * (long double)tb[cb - 1].dt);
+  tr[m].tw = (double)tw;
+  tb[cb - 1].tw = (double)tw;
   int rc = d.tri.ensure(sizeof(TriRow) * n);
+  if (!rc) rc = d.trib.ensure(sizeof(TriRow) * cb);
   if (rc) return rc;
   MF_CUDA(cudaMemcpy(d.tri.ptr, tr.data(), sizeof(TriRow) * n, cudaMemcpyHostToDevice));
+  MF_CUDA(cudaMemcpy(d.trib.ptr, tb.data(), sizeof(TriRow) * cb, cudaMemcpyHostToDevice));
   return MF_OK;
 }
 
@@ -1490,9 +1680,22 @@ static int residual_passes(mf_solver3d* sc, const T* rin, const In* u, double si
                     __nv_bfloat16* h, __nv_bfloat16* l, float* x, float* r32p) -> int {
     sc->prof.begin(kind, st);
     if constexpr (sizeof(T) == 8 && sizeof(In) == 4) {
-      if (tri) {
+      // The x pass (unit stride along the line) stays one thread per line:
+      // with two lanes per line its per-lane sector streams outgrow L1
+      // (257^3 on GB300: 0.41 ms two-sided, ~0.33 ms one thread per line,
+      // while the y and z passes drop from 0.25 to 0.19 ms each).
+      if (tri && (sc->resid_mode == MF_RESID_FP64_LINE || p.s == 1)) {
         k_resid_tri<<<blocks_for((long long)p.na * p.nb, 128), 128, 0, st>>>(
             p, sc->ax[axis_of_pass].tri.template as<TriRow>(), u, in_r, scratch, rout, h, l, x, r32p);
+        sc->prof.end(st);
+        MF_CUDA(cudaGetLastError());
+        return MF_OK;
+      }
+      if (tri) {
+        const AxisDev& d = sc->ax[axis_of_pass];
+        k_resid_twist<<<blocks_for(2 * (long long)p.na * p.nb, 128), 128, 0, st>>>(
+            p, d.tri.template as<TriRow>(), d.trib.template as<TriRow>(), u, in_r, scratch, rout, h, l, x,
+            r32p);
         sc->prof.end(st);
         MF_CUDA(cudaGetLastError());
         return MF_OK;
@@ -2210,7 +2413,7 @@ int mf_solver3d_set_eigen(mf_solver3d_t* sc, int axis, const double* eigen, cons
 }
 
 int mf_solver3d_set_residual(mf_solver3d_t* sc, int mode) {
-  if (!sc || (mode != MF_RESID_FF && mode != MF_RESID_FP64))
+  if (!sc || (mode != MF_RESID_FF && mode != MF_RESID_FP64 && mode != MF_RESID_FP64_LINE))
     return set_error(MF_ERR_ARG, "mf_solver3d_set_residual: bad arguments");
   sc->resid_mode = mode;
   return MF_OK;

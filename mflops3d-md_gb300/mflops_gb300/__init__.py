@@ -46,6 +46,7 @@ MF_PREC_SPLIT_BF16 = 1
 MF_PREC_3XTF32 = 2
 MF_RESID_FF = 0
 MF_RESID_FP64 = 1
+MF_RESID_FP64_LINE = 2
 MD_IFACE_AUTO = 0
 MD_IFACE_LU = 1
 MD_IFACE_INVERSE = 2
@@ -488,7 +489,8 @@ class SolverCoeffs3D:
         _check(_lib.mf_solver3d_device_status(self._h))
 
     def set_residual(self, mode):
-        """Residual arithmetic of the mixed path: MF_RESID_FF or MF_RESID_FP64."""
+        """Residual arithmetic of the mixed path: MF_RESID_FP64 (two lanes per
+        line, default), MF_RESID_FP64_LINE (one thread per line) or MF_RESID_FF."""
         _check(_lib.mf_solver3d_set_residual(self._h, int(mode)))
 
     def residual(self, g, u, sigma, bcx, bcy, bcz, r, stream=None):

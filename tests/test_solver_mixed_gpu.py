@@ -129,7 +129,7 @@ def test_residual_arithmetic_modes_agree(mf, gpu, prec_name, refine):
     ref = S.solve_3d(sc_ref, rhs, -30.0, solf0, bcx, bcy, bcz)
     m = solf_mask(n1, n2, n3)
     got = {}
-    for mode in (mf.MF_RESID_FF, mf.MF_RESID_FP64):
+    for mode in (mf.MF_RESID_FF, mf.MF_RESID_FP64, mf.MF_RESID_FP64_LINE):
         sc.set_residual(mode)
         out = sc.solve_3d(mf.to_device(rhs), -30.0, mf.to_device(solf0), mf.to_device(bcx),
                           mf.to_device(bcy), mf.to_device(bcz), precision=getattr(mf, prec_name),
@@ -137,6 +137,39 @@ def test_residual_arithmetic_modes_agree(mf, gpu, prec_name, refine):
         got[mode] = mf.to_host(out)[m]
         assert rel_l2(got[mode], ref[m]) < 1e-10
     assert rel_l2(got[mf.MF_RESID_FF], got[mf.MF_RESID_FP64]) < 1e-11
+    assert rel_l2(got[mf.MF_RESID_FP64_LINE], got[mf.MF_RESID_FP64]) < 1e-11
+
+
+@pytest.mark.parametrize("nall,bct,kind", [((10, 11, 12), (1,) * 6, "tanh"),
+                                           ((11, 10, 13), (2, 1, 1, 2, 2, 2), "tanh"),
+                                           ((35, 36, 34), (1, 2, 2, 1, 1, 1), "uniform"),
+                                           ((130, 67, 41), (1,) * 6, "tanh")])
+def test_two_sided_residual_matches_line_residual(mf, gpu, nall, bct, kind):
+    """The residual with two lanes per line (top and bottom elimination meeting
+    at the twist row; odd and even axis lengths, the shortest axes the
+    moment form accepts, Neumann ends, inhomogeneous boundary data) gives the
+    one-thread-per-line solution to the refined solves' accuracy (the two
+    residual evaluations round differently), and both refine to the FP64
+    oracle."""
+    gx, gy, gz = grids(*nall, kind=kind)
+    n1, n2, n3 = (v - 2 for v in nall)
+    sc_ref = S.Solver3D(gx, gy, gz, bct, 6)
+    sc = mf.SolverCoeffs3D(gx, gy, gz, bct, 6)
+    rhs = field((n1, n2, n3), 21)
+    bcx, bcy, bcz = bc_arrays(n1, n2, n3, 22)
+    solf0 = np.zeros((n1 + 2, n2 + 2, n3 + 2), order="F")
+    sigma = -7.0
+    ref = S.solve_3d(sc_ref, rhs, sigma, solf0, bcx, bcy, bcz)
+    m = solf_mask(n1, n2, n3)
+    got = {}
+    for mode in (mf.MF_RESID_FP64, mf.MF_RESID_FP64_LINE):
+        sc.set_residual(mode)
+        out = sc.solve_3d(mf.to_device(rhs), sigma, mf.to_device(solf0), mf.to_device(bcx),
+                          mf.to_device(bcy), mf.to_device(bcz), precision=mf.MF_PREC_3XTF32, refine=2)
+        sc.device_status()
+        got[mode] = mf.to_host(out)[m]
+        assert rel_l2(got[mode], ref[m]) < 1e-10, (mode, rel_l2(got[mode], ref[m]))
+    assert rel_l2(got[mf.MF_RESID_FP64], got[mf.MF_RESID_FP64_LINE]) < 1e-11
 
 
 
