@@ -737,6 +737,7 @@ __device__ __forceinline__ void solve_line_twist(const TriRow* __restrict__ R, i
 
 // Rt: the top table (TriRow[n], rows 0..m used); Rb: the bottom table in
 // mirrored order (TriRow[n - 1 - m], entry k = row n-1-k); m = (n-1)/2.
+template <int MODE>
 __global__ void __launch_bounds__(128) k_resid_twist(ResidPass<double> p, const TriRow* __restrict__ Rt,
                                                      const TriRow* __restrict__ Rb, const float* u,
                                                      const double* rin, double* scratch, double* rout,
@@ -757,7 +758,7 @@ __global__ void __launch_bounds__(128) k_resid_twist(ResidPass<double> p, const 
   const long long s = top ? p.s : -p.s;
   const double bcv = p.bc ? p.bc[t + (top ? 0 : lines)] : 0.0;
   ResidFin<double, float> fin;
-  fin.mode = p.mode;
+  fin.mode = MODE;  // compile-time: the other modes' stores drop out
   fin.rin = rin + base;
   fin.u = u + base;
   fin.sigma = p.sigma;
@@ -1693,7 +1694,9 @@ static int residual_passes(mf_solver3d* sc, const T* rin, const In* u, double si
       }
       if (tri) {
         const AxisDev& d = sc->ax[axis_of_pass];
-        k_resid_twist<<<blocks_for(2 * (long long)p.na * p.nb, 128), 128, 0, st>>>(
+        auto kern = p.mode == 0 ? k_resid_twist<0> : p.mode == 1 ? k_resid_twist<1>
+                  : p.mode == 2 ? k_resid_twist<2> : k_resid_twist<3>;
+        kern<<<blocks_for(2 * (long long)p.na * p.nb, 128), 128, 0, st>>>(
             p, d.tri.template as<TriRow>(), d.trib.template as<TriRow>(), u, in_r, scratch, rout, h, l, x,
             r32p);
         sc->prof.end(st);
