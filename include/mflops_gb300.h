@@ -299,6 +299,15 @@ int mf_md_influence_matrix_set(mf_md_t* md, double sigma, int null_mode, void* s
  * (interface faces ignored).  Device pointers. */
 int mf_md_solve(mf_md_t* md, const double* const* g, double* const* u, const double* const* bcx,
                 const double* const* bcy, const double* const* bcz, void* stream);
+/* multidomain_solve for nrhs (1..4) right-hand sides of the same operator
+ * (the reference calls it once per velocity component,
+ * class_navier_3D.f90:1643-1648,1699-1704,1753-1758): g, u, bcx, bcy, bcz
+ * hold nrhs x (subdomain count) pointers, right-hand side major.  Results
+ * equal nrhs calls of mf_md_solve; the interface systems are solved together,
+ * one pass over the explicit inverse for all of them. */
+int mf_md_solve_many(mf_md_t* md, int nrhs, const double* const* g, double* const* u,
+                     const double* const* bcx, const double* const* bcy, const double* const* bcz,
+                     void* stream);
 
 /* Interface-system solve form (no reference counterpart: the reference solves
  * it with a PETSc KSP, class_md.f90:379-438).  MF_MD_IFACE_AUTO (default):

@@ -411,25 +411,46 @@ __global__ void k_inf_direct(double* M, long long ld, long long row0, long long 
 // Largest interface system whose explicit inverse is formed at set-up.
 constexpr long long kMaxInverseRows = 12000;
 
-// y = A x with A row-major n x n (the interface inverse): one warp per row,
-// lanes stride the contiguous row, shuffle reduction.
-__global__ void k_gemv_rows(const double* __restrict__ A, const double* __restrict__ x,
-                            double* __restrict__ y, int n) {
+// Y[:, r] = A X[:, r] for K right-hand sides (columns of length n) with the
+// row-major A (the interface inverse): one warp per row, lanes stride the
+// contiguous row, shuffle reduction.  Each row of A is read once for all K
+// columns.  Per column each lane accumulates columns lane + 64 i into one
+// sum and lane + 32 + 64 i into another before the warp reduces: the same
+// order for every K, so a column's result does not depend on how many
+// columns share the call.  (Staging the columns of X through shared memory,
+// 16 rows per CTA, measured no faster in the 128 x 129 x 128 channel step.)
+constexpr int kMdMaxRhs = 4;
+template <int K>
+__global__ void k_gemm_rows(const double* __restrict__ A, const double* __restrict__ X,
+                            double* __restrict__ Y, int n) {
   const int warp = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
   const int lane = threadIdx.x & 31;
   if (warp >= n) return;
   const double* row = A + (long long)warp * n;
-  double a0 = 0.0, a1 = 0.0;
+  double a0[K], a1[K];
+#pragma unroll
+  for (int r = 0; r < K; ++r) a0[r] = a1[r] = 0.0;
   int c = lane;
   for (; c + 32 < n; c += 64) {
-    a0 = fma(row[c], x[c], a0);
-    a1 = fma(row[c + 32], x[c + 32], a1);
-  }
-  if (c < n) a0 = fma(row[c], x[c], a0);
-  double v = a0 + a1;
+    const double e0 = row[c], e1 = row[c + 32];
 #pragma unroll
-  for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
-  if (lane == 0) y[warp] = v;
+    for (int r = 0; r < K; ++r) {
+      a0[r] = fma(e0, X[(long long)r * n + c], a0[r]);
+      a1[r] = fma(e1, X[(long long)r * n + c + 32], a1[r]);
+    }
+  }
+  if (c < n) {
+    const double e0 = row[c];
+#pragma unroll
+    for (int r = 0; r < K; ++r) a0[r] = fma(e0, X[(long long)r * n + c], a0[r]);
+  }
+#pragma unroll
+  for (int r = 0; r < K; ++r) {
+    double v = a0[r] + a1[r];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    if (lane == 0) Y[(long long)r * n + warp] = v;
+  }
 }
 
 // Identity matrix, n x n column-major.
@@ -706,7 +727,7 @@ int mf_md_create(const int nd[3], const int periods[3], const double* const* gri
   if (!rc) rc = md->rint.ensure(max_field * 8);
   if (!rc) rc = md->zero_int.ensure(max_field * 8);
   if (!rc) rc = md->ufield.ensure(max_field * 8);
-  if (!rc) rc = md->vec.ensure(sizeof(double) * std::max<long long>(1, md->topo.ninf));
+  if (!rc) rc = md->vec.ensure(sizeof(double) * kMdMaxRhs * std::max<long long>(1, md->topo.ninf));
   if (!rc && (cudaMemset(md->zero_int.ptr, 0, max_field * 8) != cudaSuccess ||
               cudaDeviceSynchronize() != cudaSuccess))
     rc = set_error(MF_ERR_CUDA, "mf_md_create: memset failed");
@@ -1058,7 +1079,7 @@ static int md_factor_finish(mf_md* md, cudaStream_t st) {
     const size_t bytes = sizeof(double) * (size_t)n * (size_t)n;
     size_t freeb = 0, totalb = 0;
     MF_CUDA(cudaMemGetInfo(&freeb, &totalb));
-    if (bytes < freeb / 2 && md->Minv.ensure(bytes) == MF_OK && md->vec2.ensure(sizeof(double) * n) == MF_OK) {
+    if (bytes < freeb / 2 && md->Minv.ensure(bytes) == MF_OK && md->vec2.ensure(sizeof(double) * kMdMaxRhs * n) == MF_OK) {
       double* X = md->Minv.as<double>();
       k_identity<<<nblk((long long)n * n, 256), 256, 0, st>>>(X, (int)n);
       MF_CUDA(cudaGetLastError());
@@ -1172,16 +1193,22 @@ int mf_md_influence_matrix_cached(mf_md_t* md, double sigma, int null_mode, cons
   return mf_md_save_factor(md, path.c_str());
 }
 
-int mf_md_solve(mf_md_t* md, const double* const* g, double* const* u, const double* const* bcx,
-                const double* const* bcy, const double* const* bcz, void* stream) {
-  if (!md || !g || !u || !bcx || !bcy || !bcz) return set_error(MF_ERR_ARG, "mf_md_solve: null argument");
+// multidomain_solve for nrhs right-hand sides of the same operator; the
+// pointer arrays hold nrhs x (subdomain count) entries, right-hand side
+// major.  The subdomain work of the right-hand sides runs one after the other
+// on each subdomain's stream; the interface system is solved for all of them
+// in one pass over the inverse (or column by column on the LU factors).
+static int md_solve_impl(mf_md_t* md, int nrhs, const double* const* g, double* const* u,
+                         const double* const* bcx, const double* const* bcy, const double* const* bcz,
+                         void* stream) {
+  if (!md || !g || !u || !bcx || !bcy || !bcz || nrhs < 1 || nrhs > kMdMaxRhs)
+    return set_error(MF_ERR_ARG, "mf_md_solve: bad arguments");
   if (!md->factored) return set_error(MF_ERR_ARG, "mf_md_solve: influence matrix not set");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const MdTopology& t = md->topo;
   const long long n = t.ninf;
-  double* vec = md->vec.as<double>();
   const int ns = (int)md->sub.size();
-  for (int s = 0; s < ns; ++s)
+  for (int s = 0; s < ns * nrhs; ++s)
     for (const void* p : {(const void*)g[s], (const void*)u[s], (const void*)bcx[s],
                           (const void*)bcy[s], (const void*)bcz[s]})
       if (!is_device_ptr(p)) return set_error(MF_ERR_ARG, "mf_md_solve: device pointers only");
@@ -1212,10 +1239,12 @@ int mf_md_solve(mf_md_t* md, const double* const* g, double* const* u, const dou
     }
     return MF_OK;
   };
-  MF_CUDA(cudaMemsetAsync(vec, 0, sizeof(double) * n, st));
+  MF_CUDA(cudaMemsetAsync(md->vec.ptr, 0, sizeof(double) * n * nrhs, st));
+  double* vec = nullptr;  // interface vector of the right-hand side in hand
+  int q = 0;              // its pointer-array offset, r * ns
   auto load_bc = [&](int s, int i, int j, int k, int mode) -> int {
     mf_md::Sub& sd = md->sub[s];
-    const double* src[3] = {bcx[s], bcy[s], bcz[s]};
+    const double* src[3] = {bcx[q + s], bcy[q + s], bcz[q + s]};
     for (int l = 0; l < 3; ++l) {
       const long long nf = face_points(sd, l);
       MF_CUDA(cudaMemcpyAsync(sd.bc[l].ptr, src[l], sizeof(double) * 2 * nf, cudaMemcpyDeviceToDevice,
@@ -1232,50 +1261,77 @@ int mf_md_solve(mf_md_t* md, const double* const* g, double* const* u, const dou
   };
   // 1. homogeneous-interface solves and the signed derivative jumps
   if ((rc = fork())) return rc;
-  for (int k = 0; k < t.nd[2]; ++k)
-    for (int j = 0; j < t.nd[1]; ++j)
-      for (int i = 0; i < t.nd[0]; ++i) {
-        const int s = md_sub_index(md, i, j, k);
-        mf_md::Sub& sd = md->sub[s];
-        if ((rc = load_bc(s, i, j, k, 0))) return rc;
-        const long long tot = (long long)(sd.n[0] - 2) * (sd.n[1] - 2) * (sd.n[2] - 2);
-        k_extract_int<<<nblk(tot, 256), 256, 0, sd.stream>>>(g[s], sd.rint.as<double>(), sd.n[0] - 2,
-                                                              sd.n[1] - 2, sd.n[2] - 2);
-        MF_CUDA(cudaGetLastError());
-        if ((rc = md_sub_solve(md, s, sd.rint.as<double>(), u[s], sd.stream))) return rc;
-        if ((rc = md_gather(md, i, j, k, u[s], vec, 1.0, sd.stream, sd.du))) return rc;
-      }
+  for (int r = 0; r < nrhs; ++r) {
+    vec = md->vec.as<double>() + (size_t)r * n;
+    q = r * ns;
+    for (int k = 0; k < t.nd[2]; ++k)
+      for (int j = 0; j < t.nd[1]; ++j)
+        for (int i = 0; i < t.nd[0]; ++i) {
+          const int s = md_sub_index(md, i, j, k);
+          mf_md::Sub& sd = md->sub[s];
+          if ((rc = load_bc(s, i, j, k, 0))) return rc;
+          const long long tot = (long long)(sd.n[0] - 2) * (sd.n[1] - 2) * (sd.n[2] - 2);
+          k_extract_int<<<nblk(tot, 256), 256, 0, sd.stream>>>(g[q + s], sd.rint.as<double>(), sd.n[0] - 2,
+                                                                sd.n[1] - 2, sd.n[2] - 2);
+          MF_CUDA(cudaGetLastError());
+          if ((rc = md_sub_solve(md, s, sd.rint.as<double>(), u[q + s], sd.stream))) return rc;
+          if ((rc = md_gather(md, i, j, k, u[q + s], vec, 1.0, sd.stream, sd.du))) return rc;
+        }
+  }
   if ((rc = join())) return rc;
-  // 2. interface system (null-space handling as md_rhs_nullspace / md_vector_zero_lastpoint)
-  if (md->null_mode == 1) {
-    k_remove_mean<<<1, 256, 0, st>>>(vec, (int)n);
+  // 2. interface systems (null-space handling as md_rhs_nullspace / md_vector_zero_lastpoint)
+  double* vecs = md->vec.as<double>();
+  for (int r = 0; r < nrhs; ++r) {
+    if (md->null_mode == 1) k_remove_mean<<<1, 256, 0, st>>>(vecs + (size_t)r * n, (int)n);
+    if (md->null_mode >= 1) k_set_scalar<<<1, 1, 0, st>>>(vecs + (size_t)r * n, 0, 0.0);
   }
-  if (md->null_mode >= 1) k_set_scalar<<<1, 1, 0, st>>>(vec, 0, 0.0);
   if (md->inv_ok && md->iface_mode != MF_MD_IFACE_LU) {
-    k_gemv_rows<<<nblk(32LL * n, 256), 256, 0, st>>>(md->Minv.as<double>(), vec, md->vec2.as<double>(),
-                                                      (int)n);
+    const double* A = md->Minv.as<double>();
+    double* y = md->vec2.as<double>();
+    const unsigned blocks = nblk(32LL * n, 256);
+    if (nrhs == 1) k_gemm_rows<1><<<blocks, 256, 0, st>>>(A, vecs, y, (int)n);
+    if (nrhs == 2) k_gemm_rows<2><<<blocks, 256, 0, st>>>(A, vecs, y, (int)n);
+    if (nrhs == 3) k_gemm_rows<3><<<blocks, 256, 0, st>>>(A, vecs, y, (int)n);
+    if (nrhs == 4) k_gemm_rows<4><<<blocks, 256, 0, st>>>(A, vecs, y, (int)n);
     MF_CUDA(cudaGetLastError());
-    MF_CUDA(cudaMemcpyAsync(vec, md->vec2.ptr, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
-  } else if ((rc = md_lu_solve(md, vec, st))) {
-    return rc;
+    MF_CUDA(cudaMemcpyAsync(vecs, y, sizeof(double) * n * nrhs, cudaMemcpyDeviceToDevice, st));
+  } else {
+    for (int r = 0; r < nrhs; ++r)
+      if ((rc = md_lu_solve(md, vecs + (size_t)r * n, st))) return rc;
   }
-  if (md->null_mode == 1) k_remove_mean<<<1, 256, 0, st>>>(vec, (int)n);
+  if (md->null_mode == 1)
+    for (int r = 0; r < nrhs; ++r) k_remove_mean<<<1, 256, 0, st>>>(vecs + (size_t)r * n, (int)n);
   MF_CUDA(cudaGetLastError());
   // 3. final solves with the interface values
   if ((rc = fork())) return rc;
-  for (int k = 0; k < t.nd[2]; ++k)
-    for (int j = 0; j < t.nd[1]; ++j)
-      for (int i = 0; i < t.nd[0]; ++i) {
-        const int s = md_sub_index(md, i, j, k);
-        mf_md::Sub& sd = md->sub[s];
-        if ((rc = load_bc(s, i, j, k, 1))) return rc;
-        const long long tot = (long long)(sd.n[0] - 2) * (sd.n[1] - 2) * (sd.n[2] - 2);
-        k_extract_int<<<nblk(tot, 256), 256, 0, sd.stream>>>(g[s], sd.rint.as<double>(), sd.n[0] - 2,
-                                                              sd.n[1] - 2, sd.n[2] - 2);
-        MF_CUDA(cudaGetLastError());
-        if ((rc = md_sub_solve(md, s, sd.rint.as<double>(), u[s], sd.stream))) return rc;
-      }
+  for (int r = 0; r < nrhs; ++r) {
+    vec = vecs + (size_t)r * n;
+    q = r * ns;
+    for (int k = 0; k < t.nd[2]; ++k)
+      for (int j = 0; j < t.nd[1]; ++j)
+        for (int i = 0; i < t.nd[0]; ++i) {
+          const int s = md_sub_index(md, i, j, k);
+          mf_md::Sub& sd = md->sub[s];
+          if ((rc = load_bc(s, i, j, k, 1))) return rc;
+          const long long tot = (long long)(sd.n[0] - 2) * (sd.n[1] - 2) * (sd.n[2] - 2);
+          k_extract_int<<<nblk(tot, 256), 256, 0, sd.stream>>>(g[q + s], sd.rint.as<double>(), sd.n[0] - 2,
+                                                                sd.n[1] - 2, sd.n[2] - 2);
+          MF_CUDA(cudaGetLastError());
+          if ((rc = md_sub_solve(md, s, sd.rint.as<double>(), u[q + s], sd.stream))) return rc;
+        }
+  }
   return join();
+}
+
+int mf_md_solve(mf_md_t* md, const double* const* g, double* const* u, const double* const* bcx,
+                const double* const* bcy, const double* const* bcz, void* stream) {
+  return md_solve_impl(md, 1, g, u, bcx, bcy, bcz, stream);
+}
+
+int mf_md_solve_many(mf_md_t* md, int nrhs, const double* const* g, double* const* u,
+                     const double* const* bcx, const double* const* bcy, const double* const* bcz,
+                     void* stream) {
+  return md_solve_impl(md, nrhs, g, u, bcx, bcy, bcz, stream);
 }
 
 int mf_md_set_assembly(mf_md_t* md, int mode) {

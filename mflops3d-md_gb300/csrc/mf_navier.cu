@@ -634,7 +634,7 @@ struct NsDom {
   DevBuf rhs;     // [3][2] rhs_u(1), rhs_u(2) ...
   DevBuf rp;      // rhs_px, rhs_py, rhs_pz
   DevBuf tmp;     // 18 work fields
-  DevBuf fin;     // right-hand sides of the solves: three interior arrays (one domain) or a full field
+  DevBuf fin;     // right-hand sides of the solves: three interior arrays (one domain) or three full fields
   DevBuf exact;   // u, v, p, rhsu, rhsv of the exact solution
   DevBuf bcex;    // exact face values of u, v, w
   DevBuf bc;      // face values of u, v, w, phi
@@ -867,12 +867,24 @@ int velocity_solves(mf_navier* nv, bool grad, cudaStream_t st) {
     return launch_check("k_ns_fu");
   };
   if (nv->md()) {
+    // the three right-hand sides first, then one multidomain solve for all
+    // of them (one pass over the interface inverse)
+    std::vector<const double*> g;
+    std::vector<double*> u;
+    std::vector<const double*> bx, by, bz;
     for (int c = 0; c < 3; ++c) {
-      for (NsDom& d : nv->dom)
-        if ((rc = fu(d, c, 1, d.fin.as<double>(), st))) return rc;
-      if ((rc = solve_md(nv, nv->mdu, c, c, nw, st))) return rc;
+      for (NsDom& d : nv->dom) {
+        double* rhs = d.fin.as<double>() + (size_t)c * d.np;
+        if ((rc = fu(d, c, 1, rhs, st))) return rc;
+        g.push_back(rhs);
+        u.push_back(d.F(c, nw));
+      }
+      FacePtrs b = face_ptrs(nv, c);
+      bx.insert(bx.end(), b.x.begin(), b.x.end());
+      by.insert(by.end(), b.y.begin(), b.y.end());
+      bz.insert(bz.end(), b.z.begin(), b.z.end());
     }
-    return MF_OK;
+    return mf_md_solve_many(nv->mdu, 3, g.data(), u.data(), bx.data(), by.data(), bz.data(), st);
   }
   NsDom& d = nv->dom[0];
   MF_CUDA(cudaEventRecord(nv->fork, st));
@@ -1235,7 +1247,7 @@ int dom_setup(NsDom& d, const mf_navier_params_t* p, const double* gx, int nx, c
   if (p->nsubite > 1 && (rc = d.sub.ensure(fb * 4))) return rc;
   if ((rc = d.fields.ensure(fb * 5 * kNt)) || (rc = d.nl.ensure(fb * 3 * kNt)) || (rc = d.rhs.ensure(fb * 6)) ||
       (rc = d.rp.ensure(fb * 3)) || (rc = d.tmp.ensure(fb * 18)) ||
-      (rc = d.fin.ensure(md ? fb : (size_t)d.nin * sizeof(double) * 3)) || (rc = d.exact.ensure(fb * 5)) ||
+      (rc = d.fin.ensure(md ? 3 * fb : (size_t)d.nin * sizeof(double) * 3)) || (rc = d.exact.ensure(fb * 5)) ||
       (rc = d.bcex.ensure(sizeof(double) * 3 * ftot)) || (rc = d.bc.ensure(sizeof(double) * 4 * ftot)) ||
       (rc = d.grid.ensure(sizeof(double) * (nx + ny + nz))) || (rc = d.wts.ensure(sizeof(double) * (nx + ny + nz))) ||
       (rc = d.part.ensure(sizeof(double) * kDiagSums * (size_t)nz * groups)) ||

@@ -122,6 +122,8 @@ _PROTOS = {
     "mf_md_influence_matrix_set": [_P, _D, _I, _P],
     "mf_md_solve": [_P, ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.POINTER(_P),
                     ctypes.POINTER(_P), ctypes.POINTER(_P), _P],
+    "mf_md_solve_many": [_P, ctypes.c_int, ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.POINTER(_P),
+                         ctypes.POINTER(_P), ctypes.POINTER(_P), _P],
     "mf_md_interface": [_P, _DP],
     "mf_md_set_interface_solve": [_P, ctypes.c_int],
     "mf_md_set_assembly": [_P, ctypes.c_int],
@@ -616,6 +618,18 @@ class MultiDomain:
                                 mk([bc[c][2] for c in subs]), _stream(stream)))
         return u
 
+    def solve_many(self, gs, us, bcs, stream=None):
+        """Several right-hand sides of the same operator in one call
+        (mf_md_solve_many): gs, us, bcs are lists of the dicts of solve()."""
+        subs = self.subdomains()
+        k = len(gs)
+        mk = lambda seq: (_P * (k * len(subs)))(*[_arg(a) for a in seq])
+        flat = lambda f: [f(r, c) for r in range(k) for c in subs]
+        _check(_lib.mf_md_solve_many(self._h, k, mk(flat(lambda r, c: gs[r][c])), mk(flat(lambda r, c: us[r][c])),
+                                     mk(flat(lambda r, c: bcs[r][c][0])), mk(flat(lambda r, c: bcs[r][c][1])),
+                                     mk(flat(lambda r, c: bcs[r][c][2])), _stream(stream)))
+        return us
+
     def set_precision(self, precision, refine=-1):
         """Precision of the subdomain solves (FP64 default, or a mixed mode)."""
         _check(_lib.mf_md_set_precision(self._h, int(precision), int(refine)))
@@ -625,7 +639,8 @@ class MultiDomain:
         _check(_lib.mf_md_set_assembly(self._h, int(mode)))
 
     def set_interface_solve(self, mode):
-        """MD_IFACE_AUTO (inverse when small enough) or MD_IFACE_LU."""
+        """MD_IFACE_AUTO (inverse when small enough), MD_IFACE_LU or
+        MD_IFACE_INVERSE (the inverse at any size that fits)."""
         _check(_lib.mf_md_set_interface_solve(self._h, int(mode)))
 
     def interface(self):

@@ -134,6 +134,35 @@ def test_md_mixed_subdomain_solves_forced_inverse(mf, gpu, nd, periods):
     assert err < 1e-10 and lerr < 1e-10, (err, lerr)
 
 
+@pytest.mark.parametrize("iface", ["MD_IFACE_INVERSE", "MD_IFACE_LU"])
+def test_md_solve_many_equals_single_solves(mf, gpu, iface):
+    """Three right-hand sides in one mf_md_solve_many call (subdomain work per
+    right-hand side in turn, the interface systems together) give the three
+    single solves bit for bit."""
+    nd, periods, nodes, sigma = (2, 2, 1), (0, 0, 0), (11, 11, 11), -3.0
+    grids = tuple(slabs(nd[l], nodes[l]) for l in range(3))
+    bct = (1,) * 6
+    dev = mf.MultiDomain(nd, periods, *grids, bct)
+    dev.set_interface_solve(getattr(mf, iface))
+    dev.influence_matrix_set(sigma, 0)
+    subs = dev.subdomains()
+    gs, bcs, singles, many = [], [], [], []
+    for r in range(3):
+        g, bc, _ = problem(grids, subs, sigma, bct)
+        rng = np.random.default_rng(40 + r)
+        g = {c: g[c] * (1.0 + r) + 0.1 * rng.standard_normal(g[c].shape) for c in subs}
+        gs.append({c: mf.to_device(np.asfortranarray(g[c])) for c in subs})
+        bcs.append({c: [mf.to_device(b * (1.0 - 0.3 * r)) for b in bc[c]] for c in subs})
+        u1 = {c: mf.empty_device(g[c].shape) for c in subs}
+        dev.solve(gs[r], u1, bcs[r])
+        singles.append({c: mf.to_host(u1[c]) for c in subs})
+        many.append({c: mf.empty_device(g[c].shape) for c in subs})
+    dev.solve_many(gs, many, bcs)
+    for r in range(3):
+        for c in subs:
+            assert np.array_equal(mf.to_host(many[r][c]), singles[r][c]), (r, c)
+
+
 def test_factor_cache_round_trip(mf, gpu, tmp_path):
     """The factor written for one (grids, sigma, null mode) reloads into a
     fresh handle and solves identically; a factor of another sigma or a
