@@ -51,7 +51,7 @@ def parse():
     ap.add_argument("--precision", default="auto", choices=["auto", "bf16", "tf32"],
                     help="transform format; auto times both and reports the faster")
     ap.add_argument("--probe", default=None,
-                    choices=["bf16", "tf32", "fp64", "der", "filter", "les_mlp", "mlp_train", "navier"],
+                    choices=["bf16", "tf32", "fp64", "der", "filter", "les_mlp", "mlp_train", "navier", "channel"],
                     help="profiling aid: run two untimed solves of the workload in this format "
                          "(refinement steps from --refine), or two untimed launches of one row "
                          "(derivative sweeps at 257^3, the 384 -> 96 filter, the learned viscosity "
@@ -867,6 +867,37 @@ def run_row_probe(args):
                 nav.set_field(var, lev, field(shape, 90 + 4 * q + lev))
         for _ in range(6):  # four steps warm the nonlinear-term cache, two are profiled
             nav.step()
+    elif args.probe == "channel":
+        # the periodic-channel multidomain step at 64 x 65 x 64, 3xTF32 +
+        # 1 refinement subdomain solves: eager and CUDA-graph step times, then
+        # two steps between cudaProfilerStart/Stop (for a launch list taken
+        # with ncu --profile-from-start off)
+        n = 64
+        gx, gy, gz = mesh.uniform_grid(n, 0.0, 2.0), mesh.tanh_grid(n + 1, 2.0), mesh.uniform_grid(n, 0.0, 2.0)
+        nav = mf.NavierStokes3D([gx], [gy], [gz], nd=(1, 1, 1), periods=(1, 0, 1), ts=1e-3, reynolds=180.0,
+                                precision=mf.MF_PREC_3XTF32, refine=1)
+        start = [mf.to_device(c) for c in channel_initial(gx, gy, gz)]
+        for lev in range(4):
+            for q, var in enumerate("uvw"):
+                nav.set_field(var, lev, start[q])
+        for _ in range(4):
+            nav.step()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0 = time.perf_counter()
+        a.record()
+        for _ in range(8):
+            nav.step()
+        b.record()
+        b.synchronize()
+        wall = (time.perf_counter() - t0) / 8 * 1e3
+        print("channel 64 eager step: %.3f ms (events), %.3f ms (host wall)" % (a.elapsed_time(b) / 8, wall),
+              flush=True)
+        torch.cuda.cudart().cudaProfilerStart()
+        for _ in range(2):
+            nav.step()
+        torch.cuda.synchronize()
+        torch.cuda.cudart().cudaProfilerStop()
     elif args.probe == "les_mlp":
         shape = (160, 160, 160)
         g = mesh.uniform_grid(160)

@@ -137,6 +137,53 @@ __global__ void k_face_gather(const double* __restrict__ du, double* out, FaceGa
   atomicAdd(out + f.row0 + q, f.scale * (f.m ? v : -v));
 }
 
+// Signed face derivatives of u added into the interface vector, from the
+// face rows of the line's derivative operator: for each line of the face
+// grid, du_0 = sum_r W[r] u_r and du_{L-1} = sum_r W[L + r] u_r (plain lines,
+// the operator the influence matrix is assembled with), kDotLanes lanes per
+// line and a shuffle reduction.  row0[m] < 0: side m is not an interface.
+// One read of the field per axis instead of a full derivative sweep whose
+// interior rows are not used.
+struct FaceDot {
+  int l;                // face axis
+  int nx, ny, nz;       // subdomain nodes
+  long long row0[2];    // first interface row of sides 0 and 1, or -1
+  double scale;
+};
+constexpr int kDotLanes = 8;
+__global__ void k_face_dot(const double* __restrict__ u, const double* __restrict__ W, double* out,
+                           FaceDot f) {
+  const int na = (f.l == 0 ? f.ny : f.nx) - 2;
+  const int nb = (f.l == 2 ? f.ny : f.nz) - 2;
+  const int L = f.l == 0 ? f.nx : f.l == 1 ? f.ny : f.nz;
+  const long long q = ((long long)blockIdx.x * blockDim.x + threadIdx.x) / kDotLanes;
+  const int sub = threadIdx.x % kDotLanes;
+  const bool live = q < (long long)na * nb;
+  double lo = 0.0, hi = 0.0;
+  if (live) {
+    const int a = (int)(q % na) + 1, b = (int)(q / na) + 1;
+    long long base, s;
+    if (f.l == 0) { base = (long long)f.nx * (a + (long long)f.ny * b); s = 1; }
+    else if (f.l == 1) { base = a + (long long)f.nx * f.ny * b; s = f.nx; }
+    else { base = a + (long long)f.nx * b; s = (long long)f.nx * f.ny; }
+    for (int r = sub; r < L; r += kDotLanes) {
+      const double v = u[base + r * s];
+      lo = fma(W[r], v, lo);
+      hi = fma(W[L + r], v, hi);
+    }
+  }
+#pragma unroll
+  for (int off = kDotLanes / 2; off > 0; off >>= 1) {
+    lo += __shfl_xor_sync(0xffffffffu, lo, off);
+    hi += __shfl_xor_sync(0xffffffffu, hi, off);
+  }
+  if (!live || sub != 0) return;
+  // atomic: the two subdomains of an interface may add concurrently; two
+  // additions onto the zeroed vector give the same sum in either order
+  if (f.row0[0] >= 0) atomicAdd(out + f.row0[0] + q, -f.scale * lo);
+  if (f.row0[1] >= 0) atomicAdd(out + f.row0[1] + q, f.scale * hi);
+}
+
 // Batched influence columns: problem b has a unit value at point q0 + b of
 // side m of a face array with nf points per side (all else zero).
 __global__ void k_dirac_batch(double* bc, long long nf, int m, long long q0, int B) {
@@ -412,44 +459,62 @@ __global__ void k_inf_direct(double* M, long long ld, long long row0, long long 
 constexpr long long kMaxInverseRows = 12000;
 
 // Y[:, r] = A X[:, r] for K right-hand sides (columns of length n) with the
-// row-major A (the interface inverse): one warp per row, lanes stride the
-// contiguous row, shuffle reduction.  Each row of A is read once for all K
-// columns.  Per column each lane accumulates columns lane + 64 i into one
-// sum and lane + 32 + 64 i into another before the warp reduces: the same
-// order for every K, so a column's result does not depend on how many
-// columns share the call.  (Staging the columns of X through shared memory,
-// 16 rows per CTA, measured no faster in the 128 x 129 x 128 channel step.)
+// row-major A (the interface inverse): one warp per row, kGemvRows rows per
+// CTA.  Each row of A is read once for all K columns; the columns of X are
+// staged through shared memory in chunks of kGemvChunk entries, so X comes
+// from L2 once per CTA rather than once per row (without it, a 64 x 65 x 64
+// channel step's three-column product took 4.7 times the HBM time of its
+// 0.49 GB inverse).  Per column each lane accumulates columns lane + 64 i
+// into one sum and lane + 32 + 64 i into another before the warp reduces:
+// the same order for every K, so a column's result does not depend on how
+// many columns share the call.
 constexpr int kMdMaxRhs = 4;
+constexpr int kGemvRows = 16;
+constexpr int kGemvChunk = 512;  // a multiple of 64
 template <int K>
-__global__ void k_gemm_rows(const double* __restrict__ A, const double* __restrict__ X,
-                            double* __restrict__ Y, int n) {
-  const int warp = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
-  const int lane = threadIdx.x & 31;
-  if (warp >= n) return;
-  const double* row = A + (long long)warp * n;
+__global__ void __launch_bounds__(32 * kGemvRows) k_gemm_rows(const double* __restrict__ A,
+                                                              const double* __restrict__ X,
+                                                              double* __restrict__ Y, int n) {
+  __shared__ double xs[K][kGemvChunk];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long long ri = (long long)blockIdx.x * kGemvRows + w;
+  const bool live = ri < n;
+  const double* row = A + (live ? ri : 0) * (long long)n;
   double a0[K], a1[K];
 #pragma unroll
   for (int r = 0; r < K; ++r) a0[r] = a1[r] = 0.0;
-  int c = lane;
-  for (; c + 32 < n; c += 64) {
-    const double e0 = row[c], e1 = row[c + 32];
+  for (int c0 = 0; c0 < n; c0 += kGemvChunk) {
+    const int len = min(kGemvChunk, n - c0);
+    __syncthreads();  // the previous chunk is consumed
+    for (int e = threadIdx.x; e < K * kGemvChunk; e += blockDim.x) {
+      const int r = e / kGemvChunk, c = e % kGemvChunk;
+      xs[r][c] = c < len ? X[(long long)r * n + c0 + c] : 0.0;
+    }
+    __syncthreads();
+    if (!live) continue;
+    const double* rc = row + c0;
+    int c = lane;
+    for (; c + 32 < len; c += 64) {
+      const double e0 = rc[c], e1 = rc[c + 32];
 #pragma unroll
-    for (int r = 0; r < K; ++r) {
-      a0[r] = fma(e0, X[(long long)r * n + c], a0[r]);
-      a1[r] = fma(e1, X[(long long)r * n + c + 32], a1[r]);
+      for (int r = 0; r < K; ++r) {
+        a0[r] = fma(e0, xs[r][c], a0[r]);
+        a1[r] = fma(e1, xs[r][c + 32], a1[r]);
+      }
+    }
+    if (c < len) {
+      const double e0 = rc[c];
+#pragma unroll
+      for (int r = 0; r < K; ++r) a0[r] = fma(e0, xs[r][c], a0[r]);
     }
   }
-  if (c < n) {
-    const double e0 = row[c];
-#pragma unroll
-    for (int r = 0; r < K; ++r) a0[r] = fma(e0, X[(long long)r * n + c], a0[r]);
-  }
+  if (!live) return;
 #pragma unroll
   for (int r = 0; r < K; ++r) {
     double v = a0[r] + a1[r];
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
-    if (lane == 0) Y[(long long)r * n + warp] = v;
+    if (lane == 0) Y[(long long)r * n + ri] = v;
   }
 }
 
@@ -512,13 +577,14 @@ struct mf_md {
     mf_solver3d_t* sc = nullptr;
     mf_der_t* dc[3] = {nullptr, nullptr, nullptr};
     DevBuf bc[3];      // face arrays (2 sides each)
-    DevBuf rint, du[3];  // interior right-hand side and derivative scratch of this subdomain
+    DevBuf rint;         // interior right-hand side of this subdomain
+    DevBuf facew[3];     // rows 0 and n-1 of the plain first-derivative operator along each axis
     cudaStream_t stream = nullptr;  // this subdomain's branch of a solve
     cudaEvent_t done = nullptr;
   };
   cudaEvent_t fork = nullptr;
   std::vector<Sub> sub;  // index i + nd1*(j + nd2*k)
-  DevBuf M, ipiv, vec, info, work, zero_int, du[3], rint, ufield;
+  DevBuf M, ipiv, vec, info, work, zero_int, rint, ufield;
   DevBuf perm, dinv, lu_v, lu_y;  // LU solve: row permutation, diagonal-block inverses, work vectors
   DevBuf Minv, vec2;  // row-major inverse of the influence matrix, solve output
   DevBuf ub, dub[3], bcb;  // batched influence columns: fields, derivatives, Dirac faces
@@ -568,30 +634,45 @@ static int md_sub_solve(mf_md* md, int s, const double* rint, double* u, cudaStr
 }
 
 // Normal derivatives of u on every interface face of subdomain (i,j,k),
-// added (times scale, signed like the reference) into out[rows].
+// added (times scale, signed like the reference) into out[rows]: one
+// k_face_dot pass per axis with an interface face.
 static int md_gather(mf_md* md, int i, int j, int k, const double* u, double* out, double scale,
-                     cudaStream_t st, DevBuf* dus = nullptr) {
-  DevBuf* du = dus ? dus : md->du;
+                     cudaStream_t st) {
   const int s = md_sub_index(md, i, j, k);
   mf_md::Sub& sd = md->sub[s];
-  bool need[3] = {false, false, false};
-  for (int l = 0; l < 3; ++l)
-    for (int m = 0; m < 2; ++m)
-      if (md->topo.get(i, j, k, l, m) > 0) need[l] = true;
-  int rc;
   for (int l = 0; l < 3; ++l) {
-    if (!need[l]) continue;
-    if ((rc = der_launch(sd.dc[l], l, 1, 3, u, du[l].as<double>(), sd.n[0], sd.n[1], sd.n[2], st)))
-      return rc;
-  }
-  for (int l = 0; l < 3; ++l)
+    FaceDot f{l, sd.n[0], sd.n[1], sd.n[2], {-1, -1}, scale};
+    bool any = false;
     for (int m = 0; m < 2; ++m) {
       const int p = md->topo.get(i, j, k, l, m);
       if (p <= 0) continue;
-      FaceGather f{l, m, sd.n[0], sd.n[1], sd.n[2], (long long)md->topo.offset[p - 1], scale};
-      k_face_gather<<<nblk(md->topo.size[p - 1], 128), 128, 0, st>>>(du[l].as<double>(), out, f);
-      MF_CUDA(cudaGetLastError());
+      f.row0[m] = md->topo.offset[p - 1];
+      any = true;
     }
+    if (!any) continue;
+    const int a = l == 0 ? 1 : 0, b = l == 2 ? 1 : 2;
+    const long long lines = (long long)(sd.n[a] - 2) * (sd.n[b] - 2);
+    k_face_dot<<<nblk(lines * kDotLanes, 256), 256, 0, st>>>(u, sd.facew[l].as<double>(), out, f);
+    MF_CUDA(cudaGetLastError());
+  }
+  return MF_OK;
+}
+
+// Rows 0 and L-1 of the plain first-derivative operator of subdomain sd
+// along axis a (L nodes), from the derivative of the L unit pencils; stored
+// on the device as [row 0 | row L-1] for k_face_dot.
+static int face_weights(mf_md::Sub& sd, int a) {
+  const int L = sd.n[a];
+  std::vector<double> I((size_t)L * L, 0.0), D((size_t)L * L), w((size_t)2 * L);
+  for (int q = 0; q < L; ++q) I[(size_t)q * L + q] = 1.0;
+  int rc = mf_der_lines(sd.dc[a], 1, 0, I.data(), D.data(), L, nullptr);
+  if (rc) return rc;
+  for (int q = 0; q < L; ++q) {
+    w[q] = D[(size_t)q * L];
+    w[(size_t)L + q] = D[(size_t)q * L + L - 1];
+  }
+  if ((rc = sd.facew[a].ensure(sizeof(double) * 2 * L))) return rc;
+  MF_CUDA(cudaMemcpy(sd.facew[a].ptr, w.data(), sizeof(double) * 2 * L, cudaMemcpyHostToDevice));
   return MF_OK;
 }
 
@@ -701,6 +782,8 @@ int mf_md_create(const int nd[3], const int periods[3], const double* const* gri
           break;
         for (int l = 0; l < 3 && !rc; ++l) rc = mf_der_coeffs_init(g[l], sd.n[l], 1, so, &sd.dc[l]);
         if (rc) break;
+        for (int l = 0; l < 3 && !rc; ++l) rc = face_weights(sd, l);
+        if (rc) break;
         for (int l = 0; l < 3 && !rc; ++l) rc = sd.bc[l].ensure(sizeof(double) * 2 * face_points(sd, l));
         if (rc) break;
         max_field = std::max(max_field, (size_t)sd.n[0] * sd.n[1] * sd.n[2]);
@@ -723,7 +806,6 @@ int mf_md_create(const int nd[3], const int periods[3], const double* const* gri
     md->geom_key = h;
   }
   if (!rc)
-    for (int l = 0; l < 3 && !rc; ++l) rc = md->du[l].ensure(max_field * 8);
   if (!rc) rc = md->rint.ensure(max_field * 8);
   if (!rc) rc = md->zero_int.ensure(max_field * 8);
   if (!rc) rc = md->ufield.ensure(max_field * 8);
@@ -750,7 +832,7 @@ int mf_md_destroy(mf_md_t* md) {
     for (int l = 0; l < 3; ++l) {
       mf_der_destroy(sd.dc[l]);
       sd.bc[l].release();
-      sd.du[l].release();
+      sd.facew[l].release();
     }
     sd.rint.release();
     if (sd.stream) cudaStreamDestroy(sd.stream);
@@ -759,8 +841,7 @@ int mf_md_destroy(mf_md_t* md) {
   if (md->fork) cudaEventDestroy(md->fork);
   for (DevBuf* b : {&md->Minv, &md->vec2, &md->ub, &md->dub[0], &md->dub[1], &md->dub[2], &md->bcb}) b->release();
   for (DevBuf* b : {&md->perm, &md->dinv, &md->lu_v, &md->lu_y, &md->M, &md->ipiv, &md->vec, &md->info,
-                    &md->work, &md->zero_int, &md->du[0],
-                    &md->du[1], &md->du[2], &md->rint, &md->ufield})
+                    &md->work, &md->zero_int, &md->rint, &md->ufield})
     b->release();
   if (md->cs) cusolverDnDestroy(md->cs);
   delete md;
@@ -1223,8 +1304,6 @@ static int md_solve_impl(mf_md_t* md, int nrhs, const double* const* g, double* 
       MF_CUDA(cudaEventCreateWithFlags(&sd.done, cudaEventDisableTiming));
       const size_t nfull = (size_t)sd.n[0] * sd.n[1] * sd.n[2];
       if ((rc = sd.rint.ensure(nfull * 8))) return rc;
-      for (int l = 0; l < 3; ++l)
-        if ((rc = sd.du[l].ensure(nfull * 8))) return rc;
     }
   }
   auto fork = [&]() -> int {
@@ -1275,7 +1354,7 @@ static int md_solve_impl(mf_md_t* md, int nrhs, const double* const* g, double* 
                                                                 sd.n[1] - 2, sd.n[2] - 2);
           MF_CUDA(cudaGetLastError());
           if ((rc = md_sub_solve(md, s, sd.rint.as<double>(), u[q + s], sd.stream))) return rc;
-          if ((rc = md_gather(md, i, j, k, u[q + s], vec, 1.0, sd.stream, sd.du))) return rc;
+          if ((rc = md_gather(md, i, j, k, u[q + s], vec, 1.0, sd.stream))) return rc;
         }
   }
   if ((rc = join())) return rc;
@@ -1288,11 +1367,11 @@ static int md_solve_impl(mf_md_t* md, int nrhs, const double* const* g, double* 
   if (md->inv_ok && md->iface_mode != MF_MD_IFACE_LU) {
     const double* A = md->Minv.as<double>();
     double* y = md->vec2.as<double>();
-    const unsigned blocks = nblk(32LL * n, 256);
-    if (nrhs == 1) k_gemm_rows<1><<<blocks, 256, 0, st>>>(A, vecs, y, (int)n);
-    if (nrhs == 2) k_gemm_rows<2><<<blocks, 256, 0, st>>>(A, vecs, y, (int)n);
-    if (nrhs == 3) k_gemm_rows<3><<<blocks, 256, 0, st>>>(A, vecs, y, (int)n);
-    if (nrhs == 4) k_gemm_rows<4><<<blocks, 256, 0, st>>>(A, vecs, y, (int)n);
+    const unsigned blocks = nblk(n, kGemvRows), threads = 32 * kGemvRows;
+    if (nrhs == 1) k_gemm_rows<1><<<blocks, threads, 0, st>>>(A, vecs, y, (int)n);
+    if (nrhs == 2) k_gemm_rows<2><<<blocks, threads, 0, st>>>(A, vecs, y, (int)n);
+    if (nrhs == 3) k_gemm_rows<3><<<blocks, threads, 0, st>>>(A, vecs, y, (int)n);
+    if (nrhs == 4) k_gemm_rows<4><<<blocks, threads, 0, st>>>(A, vecs, y, (int)n);
     MF_CUDA(cudaGetLastError());
     MF_CUDA(cudaMemcpyAsync(vecs, y, sizeof(double) * n * nrhs, cudaMemcpyDeviceToDevice, st));
   } else {
