@@ -121,22 +121,6 @@ struct FaceGather {
   double scale;
 };
 
-__global__ void k_face_gather(const double* __restrict__ du, double* out, FaceGather f) {
-  const int na = (f.l == 0 ? f.ny : f.nx) - 2;
-  const int nb = (f.l == 2 ? f.ny : f.nz) - 2;
-  const int q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= na * nb) return;
-  const int a = q % na + 1, b = q / na + 1;
-  int i, j, k;
-  if (f.l == 0) { i = f.m ? f.nx - 1 : 0; j = a; k = b; }
-  else if (f.l == 1) { i = a; j = f.m ? f.ny - 1 : 0; k = b; }
-  else { i = a; j = b; k = f.m ? f.nz - 1 : 0; }
-  const double v = du[i + (long long)f.nx * (j + (long long)f.ny * k)];
-  // atomic: the two subdomains of an interface may add concurrently; two
-  // additions onto the zeroed vector give the same sum in either order
-  atomicAdd(out + f.row0 + q, f.scale * (f.m ? v : -v));
-}
-
 // Signed face derivatives of u added into the interface vector, from the
 // face rows of the line's derivative operator: for each line of the face
 // grid, du_0 = sum_r W[r] u_r and du_{L-1} = sum_r W[L + r] u_r (plain lines,
@@ -192,8 +176,9 @@ __global__ void k_dirac_batch(double* bc, long long nf, int m, long long q0, int
   bc[(long long)b * 2 * nf + (long long)m * nf + q0 + b] = 1.0;
 }
 
-// k_face_gather for B problems: problem blockIdx.y reads du + y * du_stride
-// and adds into out + y * out_stride.
+// Signed face values of B derivative fields (the Dirac-column assembly):
+// problem blockIdx.y reads du + y * du_stride and adds into out + y *
+// out_stride; face point q of side m of axis l, negated on side 0.
 __global__ void k_face_gather_batch(const double* __restrict__ du, long long du_stride, double* out,
                                     long long out_stride, FaceGather f) {
   const int na = (f.l == 0 ? f.ny : f.nx) - 2;
