@@ -37,3 +37,24 @@ def test_no_device_is_reported_cleanly(mf):
         assert e.code in (mf.MF_ERR_CUDA, mf.MF_ERR_ALLOC)
     else:
         raise AssertionError("handle creation must fail loudly without a GPU")
+
+
+def test_argument_errors_need_no_device(mf):
+    """Entry points reject bad arguments with MF_ERR_ARG before touching the
+    device (null handles, right-hand-side counts outside 1..4, unknown modes)."""
+    lib = ctypes.CDLL(mf.lib_path())
+    P = ctypes.c_void_p
+    PP = ctypes.POINTER(ctypes.c_void_p)
+    lib.mf_md_solve_many.argtypes = [P, ctypes.c_int, PP, PP, PP, PP, PP, P]
+    lib.mf_md_solve.argtypes = [P, PP, PP, PP, PP, PP, P]
+    lib.mf_md_set_precision.argtypes = [P, ctypes.c_int, ctypes.c_int]
+    lib.mf_md_set_interface_solve.argtypes = [P, ctypes.c_int]
+    lib.mf_solver3d_set_residual.argtypes = [P, ctypes.c_int]
+    arr = (ctypes.c_void_p * 8)()
+    for nrhs in (0, 1, 3, 5):
+        assert lib.mf_md_solve_many(None, nrhs, arr, arr, arr, arr, arr, None) == mf.MF_ERR_ARG
+    assert lib.mf_md_solve(None, arr, arr, arr, arr, arr, None) == mf.MF_ERR_ARG
+    assert lib.mf_md_set_precision(None, mf.MF_PREC_3XTF32, 1) == mf.MF_ERR_ARG
+    assert lib.mf_md_set_interface_solve(None, mf.MD_IFACE_INVERSE) == mf.MF_ERR_ARG
+    for mode in (mf.MF_RESID_FF, mf.MF_RESID_FP64, mf.MF_RESID_FP64_LINE):
+        assert lib.mf_solver3d_set_residual(None, mode) == mf.MF_ERR_ARG
