@@ -577,6 +577,143 @@ int eig_real(int n, const double* a_in, double* w, double* v_out, double* max_im
   return 0;
 }
 
+namespace {
+
+// Double-double numbers (unevaluated sums hi + lo) for the few products of
+// the eigen refinement below whose sums cancel: Knuth's TwoSum and an
+// fma-based TwoProduct, both exact in IEEE-754 arithmetic (the host code is
+// built without floating-point contraction, so nothing else is fused).
+struct DD { double hi, lo; };
+inline DD dd_quick(double a, double b) { const double s = a + b; return {s, b - (s - a)}; }
+inline DD dd_add(DD a, DD b) {
+  const double s = a.hi + b.hi, bb = s - a.hi;
+  const double e = (a.hi - (s - bb)) + (b.hi - bb);
+  const double t = a.lo + b.lo, tb = t - a.lo;
+  const double f = (a.lo - (t - tb)) + (b.lo - tb);
+  DD r = dd_quick(s, e + t);
+  return dd_quick(r.hi, r.lo + f);
+}
+inline DD dd_prod(double a, double b) { const double p = a * b; return {p, std::fma(a, b, -p)}; }
+inline DD dd_mul(DD a, DD b) {
+  DD p = dd_prod(a.hi, b.hi);
+  return dd_quick(p.hi, p.lo + (a.hi * b.lo + a.lo * b.hi));
+}
+inline DD dd_neg(DD a) { return {-a.hi, -a.lo}; }
+inline DD dd_div(DD a, DD b) {
+  const double q1 = a.hi / b.hi;
+  DD r = dd_add(a, dd_neg(dd_mul(b, {q1, 0.0})));
+  const double q2 = r.hi / b.hi;
+  r = dd_add(r, dd_neg(dd_mul(b, {q2, 0.0})));
+  const double q3 = r.hi / b.hi;
+  return dd_add(dd_quick(q1, q2), {q3, 0.0});
+}
+
+}  // namespace
+
+// One first-order refinement of T = V diag(w) V^-1 for T = lhs^-1 rhs.
+//
+// The QR eigen-solver (like LAPACK's dgeev, which the reference calls at
+// class_solver_3d.f90:535) returns eigenvalues with an absolute error of
+// order eps*|T|; the small ones, which a Poisson solution weights most, then
+// carry a relative error of eps*lambda_max/lambda_min (~1e-11 on a stretched
+// 257-node axis), and near a null eigenvalue the eigenvectors are off by
+// as much.  Here A = V^-1 T V is formed with T V = lhs^-1 (rhs V) and the
+// product by V^-1 in double-double (lhs by a band LU without pivoting in
+// double-double; its bandwidths are read off the matrix), so its diagonal
+// gives eigenvalues with a relative error of order eps*cond(V) and its off-
+// diagonal the first-order correction of the basis:
+//   w'_i = A_ii,  V' = V (I + G),  G_ij = A_ij / (w'_j - w'_i)  (i != j),
+// then V'^-1 by the FP64 inverse.  The refinement is skipped (the tables
+// stay as they are) when some |G_ij| > 1e-6, i.e. when the first-order step
+// would not be small.  Row-major n x n arrays; returns whether it applied.
+static bool refine_eigen(int n, const double* lhs, const double* rhs, std::vector<double>& v,
+                         std::vector<double>& vinv, std::vector<double>& w) {
+  int kl = 0, ku = 0;
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j)
+      if (lhs[(size_t)i * n + j] != 0.0) { kl = std::max(kl, i - j); ku = std::max(ku, j - i); }
+  std::vector<DD> lu((size_t)n * n);
+  for (size_t p = 0; p < (size_t)n * n; ++p) lu[p] = {lhs[p], 0.0};
+  auto LU = [&](int i, int j) -> DD& { return lu[(size_t)i * n + j]; };
+  for (int k = 0; k < n; ++k) {
+    if (LU(k, k).hi == 0.0) return false;
+    for (int i = k + 1; i <= std::min(n - 1, k + kl); ++i) {
+      const DD m = dd_div(LU(i, k), LU(k, k));
+      LU(i, k) = m;
+      for (int j = k + 1; j <= std::min(n - 1, k + ku); ++j)
+        LU(i, j) = dd_add(LU(i, j), dd_neg(dd_mul(m, LU(k, j))));
+    }
+  }
+  // TV, column j = lhs^-1 (rhs v_j), stored column by column
+  std::vector<DD> tv((size_t)n * n), b(n);
+  for (int j = 0; j < n; ++j) {
+    for (int i = 0; i < n; ++i) {
+      DD s = {0.0, 0.0};
+      const double* ri = &rhs[(size_t)i * n];
+      for (int k = 0; k < n; ++k)
+        if (ri[k] != 0.0) s = dd_add(s, dd_prod(ri[k], v[(size_t)k * n + j]));
+      b[i] = s;
+    }
+    for (int i = 1; i < n; ++i)
+      for (int k = std::max(0, i - kl); k < i; ++k) b[i] = dd_add(b[i], dd_neg(dd_mul(LU(i, k), b[k])));
+    for (int i = n - 1; i >= 0; --i) {
+      for (int k = i + 1; k <= std::min(n - 1, i + ku); ++k)
+        b[i] = dd_add(b[i], dd_neg(dd_mul(LU(i, k), b[k])));
+      b[i] = dd_div(b[i], LU(i, i));
+    }
+    std::copy(b.begin(), b.end(), tv.begin() + (size_t)j * n);
+  }
+  // A = V^-1 TV in double-double, then w' and G
+  std::vector<double> a((size_t)n * n), wn(n);
+  for (int i = 0; i < n; ++i) {
+    const double* wi = &vinv[(size_t)i * n];
+    for (int j = 0; j < n; ++j) {
+      const DD* tj = &tv[(size_t)j * n];
+      DD s = {0.0, 0.0};
+      for (int k = 0; k < n; ++k) {
+        DD p = dd_prod(wi[k], tj[k].hi);
+        p.lo += wi[k] * tj[k].lo;
+        s = dd_add(s, p);
+      }
+      a[(size_t)i * n + j] = s.hi + s.lo;
+    }
+    wn[i] = a[(size_t)i * n + i];
+  }
+  std::vector<double> g((size_t)n * n, 0.0);
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) {
+      if (i == j) continue;
+      const double aij = a[(size_t)i * n + j];
+      const double gap = wn[j] - wn[i];
+      if (std::fabs(aij) <= 1e-3 * std::fabs(gap)) {
+        g[(size_t)i * n + j] = aij / gap;
+        continue;
+      }
+      // near-degenerate pair (stretched grids have them among the high
+      // modes, localised at either wall): no first-order rotation exists;
+      // the coupling is left in place when it is negligible next to the
+      // eigenvalues, otherwise the tables stay unrefined
+      if (!(std::fabs(aij) <= 1e-13 * std::max(std::fabs(wn[i]), std::fabs(wn[j])))) return false;
+    }
+  std::vector<double> vn(v);
+  for (int r = 0; r < n; ++r) {
+    const double* vr = &v[(size_t)r * n];
+    double* out = &vn[(size_t)r * n];
+    for (int i = 0; i < n; ++i) {
+      const double vri = vr[i];
+      if (vri == 0.0) continue;
+      const double* gi = &g[(size_t)i * n];
+      for (int j = 0; j < n; ++j) out[j] += vri * gi[j];
+    }
+  }
+  std::vector<double> vi(vn);
+  if (!invert(n, vi.data())) return false;
+  v.swap(vn);
+  vinv.swap(vi);
+  w.swap(wn);
+  return true;
+}
+
 int solver_axis_setup(const double* grid, int nall, const int bct[2], int so,
                       SolverAxisHost& o, std::string& msg) {
   if (nall < 9) { msg = "solver axis needs at least 9 nodes"; return MF_ERR_ARG; }
@@ -616,6 +753,7 @@ int solver_axis_setup(const double* grid, int nall, const int bct[2], int so,
   if (rc != 0) { msg = "eigenvalue QR iteration did not converge"; return MF_ERR_NOT_CONVERGED; }
   o.inv_vect = o.vect;
   if (!invert(n, o.inv_vect.data())) { msg = "singular eigenvector matrix"; return MF_ERR_SINGULAR; }
+  o.eigen_refined = refine_eigen(n, lhs.data(), rhs.data(), o.vect, o.inv_vect, o.eigen);
   o.neum.assign(14, 0.0);
   if (!solver_extrapolation_coeffs(grid, nall, bct, so, o.neum.data())) {
     msg = "singular extrapolation system";

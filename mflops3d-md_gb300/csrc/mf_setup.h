@@ -61,6 +61,7 @@ struct SolverAxisHost {
   std::vector<double> vect, inv_vect;  // [n][n] row-major, V and V^-1
   std::vector<double> neum;            // [2][7]
   double max_imag = 0.0;
+  bool eigen_refined = false;          // the double-double refinement applied
 };
 // Returns 0 on success or an MF_ERR_* code; msg receives a description.
 int solver_axis_setup(const double* grid, int nall, const int bct[2], int so,
