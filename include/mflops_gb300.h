@@ -73,6 +73,36 @@ int mf_device_available(void);
  * Host-only set-up routines (no GPU needed).
  * ---------------------------------------------------------------------- */
 
+/* 1D grids of src/class_mesh/class_mesh.f90 (type mesh_grid, grid1d):
+ * n nodes on [xa, xb].  kind MF_GRID_UNIFORM: xa + i*pas.  MF_GRID_ARCSIN:
+ * the grid mesh_grid_init builds (:181-200), x = xa + (xb-xa)*
+ * (asin(-alpha*cos(pi*(xi-xa)/(xb-xa)))/asin(alpha) + 1)/2 with
+ * alpha = 1 - param/n^2 (the reference's param is beta = 33.3).
+ * MF_GRID_TANH: the tanh stretching of :203, x = xa + (xb-xa)*
+ * (1 + tanh(param*(2*(xi-xa)/(xb-xa) - 1))/tanh(param))/2 (param 0 gives
+ * the uniform grid).  xi = xa + i*(xb-xa)/(n-1). */
+#define MF_GRID_UNIFORM 0
+#define MF_GRID_ARCSIN 1
+#define MF_GRID_TANH 2
+int mf_grid1d(int kind, int n, double xa, double xb, double param, double* grid);
+
+/* dgrid1d of mesh_grid_init (class_mesh.f90:268-276): one-sided spacing at
+ * the two ends, centred half-differences inside. */
+int mf_grid_spacing(int n, const double* grid, double* dgrid);
+
+/* mesh_grid_init(grid, choice, nx, ny, nz, mpid), class_mesh.f90:113-339:
+ * the interval of direction choice ('x', 'y': [-0.5, 0.5]; 'z':
+ * [-0.25, 0.25]), cut into ndomains equal slabs of which slab dom_coord is
+ * taken (the md_mpi_getcoord / md_mpi_getnumberdomains part, :157-170),
+ * then grid1d(n) of the given kind and, if dgrid1d is not NULL, its
+ * spacing.  The reference always builds MF_GRID_ARCSIN with param 33.3.
+ * The 3-D copies grid3d/dgrid3d are broadcasts of grid1d; callers that
+ * need them broadcast the 1D arrays.  derivatives_coefficients_init and
+ * solver_init_3d (:316-386) pass grid1d on to mf_der_coeffs_init and
+ * mf_solver_coeffs_init_3d. */
+int mf_mesh_grid_init(char choice, int n, int dom_coord, int ndomains, int kind, double param,
+                      double* grid1d, double* dgrid1d);
+
 /* One row of the compact scheme; replaces der_coeffs_generic of
  * src/class_derivatives/class_derivatives_coefficient.f90:31-191. */
 int mf_der_coeffs_generic(const double h0[7], int cl, int der, int so,
@@ -160,10 +190,11 @@ int mf_solve_3d(mf_solver3d_t* sc, const double* rhs, double sigma, double* solf
                 int n1, int n2, int n3, void* stream);
 
 /* Allocation-free variant of mf_solve_3d (plain FP64), with no counterpart
- * in the reference.  It is for callers that cannot allocate device memory
- * while they run: code captured into a CUDA graph (cudaMalloc is not
- * permitted during stream capture) and hosts whose device memory belongs to
- * another allocator that forbids the library from calling cudaMalloc.  Its
+ * in the reference.  It is for callers that cannot let a library call
+ * cudaMalloc: applications whose device memory belongs to their own pool
+ * allocator, which budgets every byte and forbids other allocations, and
+ * latency-bound host loops that cannot afford cudaMalloc's implicit
+ * device-wide synchronisation.  Its
  * two work arrays live in a fixed 4 MiB file-scope device array, so the
  * interior n1*n2*n3 is limited to 262144 points (64^3); larger sizes return
  * MF_ERR_UNSUPPORTED.  All pointers must be device memory (MF_ERR_ARG

@@ -8,6 +8,8 @@
 #include <tuple>
 
 #include "mf_internal.h"
+
+#include <cmath>
 #include "mf_setup.h"
 
 namespace mf {
@@ -198,6 +200,59 @@ int mf_pentalu(int n, double* dl) {
   for (int i = 0; i < n; ++i)
     for (int m = 0; m < 5; ++m) dl[i + n * m] = l[5 * i + m];
   return MF_OK;
+}
+
+int mf_grid1d(int kind, int n, double xa, double xb, double param, double* grid) {
+  if (n < 2 || !grid || !(xb > xa) || kind < MF_GRID_UNIFORM || kind > MF_GRID_TANH)
+    return set_error(MF_ERR_ARG, "mf_grid1d: bad arguments (kind=%d n=%d [%g,%g])", kind, n, xa, xb);
+  const double pas = (xb - xa) / double(n - 1);
+  const double pi = 4.0 * std::atan(1.0);
+  if (kind == MF_GRID_ARCSIN) {
+    const double alpha = 1.0 - param / double(n * n);
+    if (!(std::fabs(alpha) < 1.0) || alpha == 0.0)
+      return set_error(MF_ERR_ARG, "mf_grid1d: arcsin parameter beta=%g gives alpha=%g outside (0,1)", param, alpha);
+    const double asa = std::asin(alpha);
+    for (int i = 0; i < n; ++i) {
+      const double xi = xa + double(i) * pas;
+      grid[i] = xa + (xb - xa) * (std::asin(-alpha * std::cos(pi * (xi - xa) / (xb - xa))) / asa + 1.0) * 0.5;
+    }
+  } else if (kind == MF_GRID_TANH && param != 0.0) {
+    const double ta = std::tanh(param);
+    for (int i = 0; i < n; ++i) {
+      const double xi = xa + double(i) * pas;
+      grid[i] = xa + (xb - xa) * (1.0 + std::tanh(param * (2.0 * (xi - xa) / (xb - xa) - 1.0)) / ta) / 2.0;
+    }
+  } else {
+    for (int i = 0; i < n; ++i) grid[i] = xa + double(i) * pas;
+  }
+  return MF_OK;
+}
+
+int mf_grid_spacing(int n, const double* grid, double* dgrid) {
+  if (n < 2 || !grid || !dgrid) return set_error(MF_ERR_ARG, "mf_grid_spacing: n must be >= 2");
+  dgrid[0] = grid[1] - grid[0];
+  dgrid[n - 1] = grid[n - 1] - grid[n - 2];
+  for (int i = 1; i < n - 1; ++i) dgrid[i] = (grid[i + 1] - grid[i - 1]) * 0.5;
+  return MF_OK;
+}
+
+int mf_mesh_grid_init(char choice, int n, int dom_coord, int ndomains, int kind, double param,
+                      double* grid1d, double* dgrid1d) {
+  if (choice != 'x' && choice != 'y' && choice != 'z')
+    return set_error(MF_ERR_ARG, "mf_mesh_grid_init: choice must be 'x', 'y' or 'z'");
+  if (ndomains < 1 || dom_coord < 0 || dom_coord >= ndomains)
+    return set_error(MF_ERR_ARG, "mf_mesh_grid_init: subdomain %d of %d", dom_coord, ndomains);
+  const double aux = 0.5;
+  double xa = -aux, xb = aux;
+  if (choice == 'z') { xa = -aux * 0.5; xb = aux * 0.5; }
+  if (ndomains > 1) {
+    const double size_dom = (xb - xa) / double(ndomains);
+    xa = xa + double(dom_coord) * size_dom;
+    xb = xa + size_dom;
+  }
+  int rc = mf_grid1d(kind, n, xa, xb, param, grid1d);
+  if (rc) return rc;
+  return dgrid1d ? mf_grid_spacing(n, grid1d, dgrid1d) : MF_OK;
 }
 
 int mf_solver_axis_setup(const double* grid, int nall, const int bct[2], int so, double* ddl,

@@ -62,6 +62,8 @@ module mflops_gpu_f
   public :: solver_coeffs_init_3d, solve_3d, solve_3d_mixed, solver_3d, solver_destroy
   public :: navier_defaults, navier_initialization_gpu, navier_set_field, navier_get_field
   public :: navier_step, navier_destroy
+  public :: mesh_grid_init
+  integer(c_int), parameter, public :: MF_GRID_UNIFORM = 0, MF_GRID_ARCSIN = 1, MF_GRID_TANH = 2
 
   interface
      function c_last_error() bind(C, name="mf_last_error") result(p)
@@ -204,6 +206,16 @@ module mflops_gpu_f
        type(c_ptr), value :: nav, diag, stream
        integer(c_int) :: rc
      end function c_navier_step
+
+     function c_mesh_grid_init(choice, n, dom_coord, ndomains, kind, param, grid1d, dgrid1d) &
+          bind(C, name="mf_mesh_grid_init") result(rc)
+       import :: c_char, c_int, c_double
+       character(kind=c_char), value :: choice
+       integer(c_int), value :: n, dom_coord, ndomains, kind
+       real(c_double), value :: param
+       real(c_double), intent(out) :: grid1d(*), dgrid1d(*)
+       integer(c_int) :: rc
+     end function c_mesh_grid_init
   end interface
 
 contains
@@ -224,6 +236,27 @@ contains
     print '(a,a,a)', where, ': ', trim(text)
     stop
   end subroutine check
+
+  ! ---------------------------------------------------------------- grids
+  ! mesh_grid_init (class_mesh.f90:113-339) on plain arrays: grid1d(n) and
+  ! dgrid1d(n) of direction choice ('x', 'y' or 'z') for subdomain dom_coord
+  ! (0-based) of ndomains along it.  Default: the reference's arcsin grid
+  ! (beta = 33.3); kind/param select MF_GRID_UNIFORM or MF_GRID_TANH.
+  subroutine mesh_grid_init(grid1d, dgrid1d, choice, n, dom_coord, ndomains, kind, param)
+    integer, intent(in) :: n
+    real(rk), intent(out) :: grid1d(n), dgrid1d(n)
+    character(len=1), intent(in) :: choice
+    integer, intent(in), optional :: dom_coord, ndomains, kind
+    real(rk), intent(in), optional :: param
+    integer(c_int) :: c, nd, k
+    real(c_double) :: p
+    c = 0; nd = 1; k = MF_GRID_ARCSIN; p = 33.3_rk
+    if (present(dom_coord)) c = int(dom_coord, c_int)
+    if (present(ndomains)) nd = int(ndomains, c_int)
+    if (present(kind)) k = int(kind, c_int)
+    if (present(param)) p = param
+    call check(c_mesh_grid_init(choice, int(n, c_int), c, nd, k, p, grid1d, dgrid1d), 'mesh_grid_init')
+  end subroutine mesh_grid_init
 
   ! ---------------------------------------------------------------- derivatives
   subroutine der_coeffs_init(grid, dc, n, solve, so)

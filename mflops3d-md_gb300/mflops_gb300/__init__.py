@@ -87,6 +87,9 @@ _PROTOS = {
     "mf_der_line_coeffs": [_DP, _I, _I, _I, _DP, _DP],
     "mf_pentalu": [_I, _DP],
     "mf_solver_axis_setup": [_DP, _I, _IP, _I, _DP, _DP, _DP, _DP, _DP, _DP, _DP],
+    "mf_grid1d": [_I, _I, _D, _D, _D, _DP],
+    "mf_grid_spacing": [_I, _DP, _DP],
+    "mf_mesh_grid_init": [ctypes.c_char, _I, _I, _I, _I, _D, _DP, _DP],
     "mf_der_coeffs_init": [_DP, _I, _I, _I, ctypes.POINTER(_P)],
     "mf_der_destroy": [_P],
     "mf_dertype": [_P, _IP],
@@ -245,6 +248,30 @@ def pentalu(dl):
     a = np.asfortranarray(np.array(dl, dtype=np.float64))
     _check(_lib.mf_pentalu(a.shape[0], a.ctypes.data_as(_DP)))
     return a
+
+
+MF_GRID_UNIFORM = 0
+MF_GRID_ARCSIN = 1
+MF_GRID_TANH = 2
+
+
+def grid1d(kind, n, xa=0.0, xb=1.0, param=0.0):
+    """1D grid of class_mesh.f90 (uniform, the reference's arcsin grid with
+    param = beta, or the tanh stretching of :203 with param = alpha)."""
+    g = np.zeros(int(n))
+    _check(_lib.mf_grid1d(int(kind), int(n), float(xa), float(xb), float(param),
+                          g.ctypes.data_as(_DP)))
+    return g
+
+
+def mesh_grid_init(choice, n, dom_coord=0, ndomains=1, kind=MF_GRID_ARCSIN, param=33.3):
+    """mesh_grid_init (class_mesh.f90:113-339): (grid1d, dgrid1d) of direction
+    'x', 'y' or 'z' for subdomain dom_coord of ndomains."""
+    g = np.zeros(int(n))
+    d = np.zeros(int(n))
+    _check(_lib.mf_mesh_grid_init(str(choice).encode()[:1], int(n), int(dom_coord), int(ndomains),
+                                  int(kind), float(param), g.ctypes.data_as(_DP), d.ctypes.data_as(_DP)))
+    return g, d
 
 
 def solver_axis_setup(grid, bct, so=6):
