@@ -1610,21 +1610,33 @@ int mf_navier_load(mf_navier_t* nv, const char* path, void* stream) {
     seen |= 1 << (ok ? it[i] : 0);
   }
   ok = ok && (rhs_cur == 0 || rhs_cur == 1);
+  // every field is read and the file checked to its end before anything is
+  // uploaded: a truncated or inconsistent file leaves the running state as
+  // it was
+  const int per_dom = kNt * 5 + 6;
+  std::vector<std::vector<double>> fields;
+  for (size_t q = 0; q < nv->dom.size() && ok; ++q)
+    for (int k = 0; k < per_dom && ok; ++k) {
+      fields.emplace_back(nv->dom[q].np);
+      ok = std::fread(fields.back().data(), 8, fields.back().size(), f) == fields.back().size();
+    }
+  ok = ok && std::fgetc(f) == EOF;
+  std::fclose(f);
+  if (!ok) return set_error(MF_ERR_ARG, "mf_navier_load: %s is truncated or inconsistent", path);
+  size_t idx = 0;
   for (NsDom& d : nv->dom) {
-    std::vector<double> buf(d.np);
-    auto get = [&](double* dst) {
-      return ok = ok && std::fread(buf.data(), 8, buf.size(), f) == buf.size() &&
-                  cudaMemcpy(dst, buf.data(), buf.size() * 8, cudaMemcpyHostToDevice) == cudaSuccess;
+    auto put = [&](double* dst) {
+      const std::vector<double>& b = fields[idx++];
+      ok = ok && cudaMemcpy(dst, b.data(), b.size() * 8, cudaMemcpyHostToDevice) == cudaSuccess;
     };
-    for (int slot = 0; slot < kNt && ok; ++slot)
-      for (int v = 0; v < 5 && ok; ++v) get(d.F(v, slot));
-    for (int c = 0; c < 3 && ok; ++c)
-      for (int w = 0; w < 2 && ok; ++w) get(d.RHS(c, w));
+    for (int slot = 0; slot < kNt; ++slot)
+      for (int v = 0; v < 5; ++v) put(d.F(v, slot));
+    for (int c = 0; c < 3; ++c)
+      for (int w = 0; w < 2; ++w) put(d.RHS(c, w));
   }
   ok = ok && cudaMemcpy(nv->state.ptr, flow, sizeof(flow), cudaMemcpyHostToDevice) == cudaSuccess &&
        cudaDeviceSynchronize() == cudaSuccess;
-  std::fclose(f);
-  if (!ok) return set_error(MF_ERR_ARG, "mf_navier_load: %s is truncated or inconsistent", path);
+  if (!ok) return set_error(MF_ERR_CUDA, "mf_navier_load: upload of %s failed", path);
   nv->time = time;
   for (int i = 0; i < kNt; ++i) nv->it[i] = it[i];
   nv->rhs_cur = rhs_cur;

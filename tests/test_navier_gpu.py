@@ -216,10 +216,19 @@ def test_checkpoint_resumes_bit_identically(mf, gpu, tmp_path):
     other = mf.NavierStokes3D(gx, gy, mesh.uniform_grid(15), **kw)
     with pytest.raises(mf.MflopsError):
         other.load(path)
+    # a refused file leaves the running state as it was: truncated inside the
+    # field data (after the header and several fields) or with extra bytes
     data = path.read_bytes()
+    before = {(var, lev): b.field(var, lev).clone() for lev in range(N.NT) for var in VARS}
+    state = b.state()
     (tmp_path / "cut.chk").write_bytes(data[: len(data) // 2])
-    with pytest.raises(mf.MflopsError):
-        b.load(tmp_path / "cut.chk")
+    (tmp_path / "long.chk").write_bytes(data + b"\0" * 8)
+    for bad in ("cut.chk", "long.chk"):
+        with pytest.raises(mf.MflopsError):
+            b.load(tmp_path / bad)
+        for (var, lev), t in before.items():
+            assert torch.equal(b.field(var, lev), t), (bad, var, lev)
+        assert b.state() == state
 
 
 MD_GRIDS = {
