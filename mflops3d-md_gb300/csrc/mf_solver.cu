@@ -2020,12 +2020,13 @@ int solver_axis_view(const ::mf_solver3d* sc, int axis, SolverAxisView* out) {
 
 // Allocation-free plain solve (mf_solve_3d_noalloc).
 //
-// For callers that must not allocate device memory while they run: code
-// being captured into a CUDA graph (cudaMalloc is not permitted during
-// stream capture) and hosts whose memory is owned by another allocator that
-// forbids the library from calling cudaMalloc.  The two FP64 work arrays of
-// the plain path live in this fixed file-scope array instead of the handle's
-// buffers.  Every GPU that loads the library holds it until exit.
+// For callers that cannot let a library call cudaMalloc: applications whose
+// device memory is owned by their own pool allocator, which budgets every
+// byte and forbids other allocations, and latency-bound host loops in which
+// cudaMalloc's implicit device-wide synchronisation cannot be afforded.  The
+// two FP64 work arrays of the plain path live in this fixed file-scope array
+// instead of the handle's buffers.  Every GPU that loads the library holds
+// it until exit.
 constexpr long long kNoAllocMaxPoints = 1LL << 18;  // interior points n1*n2*n3 (64^3)
 static __device__ __align__(256) double g_noalloc_scratch[2 * kNoAllocMaxPoints];  // 4 MiB
 

@@ -1,9 +1,11 @@
 """The allocation-free solve entry point (mf_solve_3d_noalloc) against the
 regular plain FP64 entry point, through the C ABI.
 
-The entry point exists for callers that cannot allocate device memory while
-they run (CUDA-graph capture, hosts whose allocator forbids cudaMalloc); its
-work arrays live in a fixed file-scope device array shared by all calls.
+The entry point exists for callers that cannot let a library call
+cudaMalloc (applications whose pool allocator owns and budgets all device
+memory; host loops that cannot afford cudaMalloc's implicit device
+synchronisation); its work arrays live in a fixed file-scope device array of
+2 x 262144 doubles shared by all calls.
 This file is collected last so that a failure here comes after every other
 test has run; it also passes alone in a fresh process.
 Tolerance: the two entry points run the same kernels on the same data, so
@@ -34,6 +36,24 @@ def test_noalloc_matches_regular_entry_point_twice(mf, gpu):
         w, g = mf.to_host(want), mf.to_host(got)
         assert max_rel(g, w, m) < 1e-12
         assert np.array_equal(g[~m], solf0[~m])
+
+
+def test_noalloc_at_the_size_limit(mf, gpu):
+    # 64^3 = 262144 interior points: both work arrays filled to their last
+    # entry; two calls with different data and sigma
+    nall = (66, 66, 66)
+    gx, gy, gz = grids(*nall)
+    n = 64
+    sc = mf.SolverCoeffs3D(gx, gy, gz, (2, 1, 1, 1, 1, 2), 6)
+    m = solf_mask(n, n, n)
+    for seed, sigma in ((31, -20.0), (41, 0.0)):
+        rhs = mf.to_device(field((n, n, n), seed))
+        bcs = [mf.to_device(b) for b in bc_arrays(n, n, n, seed + 1)]
+        solf0 = field((n + 2, n + 2, n + 2), seed + 2)
+        want = sc.solve_3d(rhs, sigma, mf.to_device(solf0), *bcs)
+        got = sc.solve_3d_noalloc(rhs, sigma, mf.to_device(solf0), *bcs)
+        gpu.cuda.synchronize()
+        assert max_rel(mf.to_host(got), mf.to_host(want), m) < 1e-12
 
 
 def test_noalloc_rejects_sizes_and_host_data(mf, gpu):
