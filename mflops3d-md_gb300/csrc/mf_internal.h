@@ -32,7 +32,7 @@ int num_sms();
 // shape numbers; mode 0 uses the built-in heuristics, mode 1 times the
 // candidates on first use of a shape (CUDA events on the caller's stream,
 // never while the stream is being captured) and keeps the fastest.
-enum TuneKind { kTuneGemm64 = 0, kTuneDerX = 1 };
+enum TuneKind { kTuneGemm64 = 0, kTuneDerX = 1, kTuneTcTf32 = 2 };
 int tune_mode();
 int tune_lookup(int kind, long long a, long long b, long long c, long long d);
 void tune_store(int kind, long long a, long long b, long long c, long long d, int choice);

@@ -56,9 +56,17 @@ namespace mf {
 
 struct TcPlan {
   CUtensorMap x_hi, x_lo, b_hi, b_lo;  // x_lo unused for 3xTF32
+  CUtensorMap b_hi_w, b_lo_w;          // 3xTF32 with N % 128 == 0: 128-row boxes of B
   int M = 0, N = 0, K = 0;
   bool tf32 = false;
+  bool wide = false;                   // the 128-column plan is available
 };
+
+// 3xTF32 plan choice: 0 = default (128-column slices where N % 128 == 0),
+// 1 = 64-column slices with B resident, 2 = 128-column slices when possible.
+static int g_tf32_plan = 0;
+void tc_set_tf32_plan(int plan) { g_tf32_plan = plan; }
+int tc_get_tf32_plan() { return g_tf32_plan; }
 
 namespace {
 
@@ -375,11 +383,13 @@ __global__ void __launch_bounds__(Cfg<kTf32>::kThreads, 1)
       for (int cc = c_lo; cc < c_hi; cc += 32) {
         tmem_load32(trow + cc, v);
         if constexpr (kTf32) {
+          // (s + h1) + h2: h1 = hi*hi over the first half of K at +NW, h2
+          // over the second half at +2NW
           float w[32];
-          tmem_load32(trow + 2 * NW + cc, w);
+          tmem_load32(trow + NW + cc, w);
 #pragma unroll
           for (int x = 0; x < 32; ++x) v[x] += w[x];
-          tmem_load32(trow + NW + cc, w);
+          tmem_load32(trow + 2 * NW + cc, w);
 #pragma unroll
           for (int x = 0; x < 32; ++x) v[x] += w[x];
         }
@@ -444,6 +454,280 @@ __global__ void __launch_bounds__(Cfg<kTf32>::kThreads, 1)
   if (warp == 1) {
     fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols));
+  }
+}
+
+// ---------------------------------------------------------------------------
+// 3xTF32 with 128-column N slices ("wide" plan).
+//
+// Same products and the same three accumulators per output as above, but a
+// CTA owns 128 columns of N (two slices for N = 256), so every tcgen05.mma
+// is M128 N128 K8: twice the work per instruction of the N64 form, whose
+// rate in the kernel is bound by the single issuing thread.  The slice of B
+// (hi and lo planes, 256 KB for K = 256) no longer fits in shared memory
+// beside the ring, so it streams with the X tiles: a ring stage holds the
+// FP32 X tile (16 KB) and both B planes of the same 32 K values (2 x 16 KB);
+// B is 512 KB in all and stays in L2.  TMEM: the three accumulators of one
+// tile (h1 = hi*hi over the first half of K, h2 = over the second half,
+// s = hi*lo + lo*hi; 3 x 128 columns) and four A operand slots of 16 K
+// values (4 x 32 columns).  The accumulators are single-buffered: the next
+// tile's first MMAs wait until the epilogue warps have read s and h1, its
+// second half until they have read h2; the stores follow.  The epilogue
+// sums (s + h1) + h2 in the same order as the narrow form, so both forms
+// give identical results.
+constexpr int kWideNW = 128;
+constexpr int kWideStages = 4;
+constexpr int kWideEpiWarps = 8;
+constexpr int kWideCvtWarps = 4;
+constexpr int kWideThreads = 64 + 32 * (kWideEpiWarps + kWideCvtWarps);
+constexpr uint32_t kWideTile = kBlockM * 128;          // 16 KB: 128 rows x 32 FP32
+constexpr uint32_t kWideStage = 3 * kWideTile;          // X tile + B hi + B lo
+constexpr uint32_t kWideSmem = kWideStages * kWideStage + 1024;
+constexpr uint32_t kWideH1 = 0, kWideH2 = 128, kWideS = 256, kWideSlot = 384;
+// four operand slots of 16 K values (hi at +0, lo at +16): the converters
+// may run three half-stages ahead of the MMAs
+constexpr int kWideSlots = 4;
+constexpr uint32_t kWideSlotCols = 32;
+
+__global__ void __launch_bounds__(kWideThreads, 1)
+    k_tc_tf32_wide(const __grid_constant__ CUtensorMap tx, const __grid_constant__ CUtensorMap tb_hi,
+                   const __grid_constant__ CUtensorMap tb_lo, int M, int N, int K, TcEpilogue e,
+                   int* err) {
+  extern __shared__ uint8_t smem_raw[];
+  __shared__ uint64_t full_bar[kWideStages], empty_bar[kWideStages];
+  __shared__ uint64_t cvt_bar[kWideSlots], op_free[kWideSlots];
+  __shared__ uint64_t acc_full, acc_free, h2_free;
+  __shared__ uint32_t tmem_slot;
+  __shared__ float s_lz[256];
+  __shared__ uint8_t s_nz[256];
+  uint8_t* smem = reinterpret_cast<uint8_t*>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
+  constexpr int kCvtThreads = 32 * kWideCvtWarps, kEpiThreads = 32 * kWideEpiWarps;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (e.kind == 1)
+    for (int k = threadIdx.x; k < 256; k += blockDim.x) {
+      s_lz[k] = k < e.n3 ? e.lam_z[k] + e.sigma : 0.f;
+      s_nz[k] = k < e.n3 ? e.null_z[k] : 0;
+    }
+  const int NS = N / kWideNW, nk = K / 32, half = nk / 2;
+  const int slice = blockIdx.x % NS;
+  const int cta_rank = blockIdx.x / NS, cta_count = gridDim.x / NS;
+  const int mtiles = M / kBlockM;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kWideStages; ++s) {
+      mbar_init(&full_bar[s], 1);
+      // the converters read the X tile, the MMAs the B planes
+      mbar_init(&empty_bar[s], kCvtThreads + 1);
+    }
+    for (int o = 0; o < kWideSlots; ++o) {
+      mbar_init(&cvt_bar[o], kCvtThreads);
+      mbar_init(&op_free[o], 1);
+    }
+    mbar_init(&acc_full, 1);
+    mbar_init(&acc_free, kEpiThreads);  // s and h1 read
+    mbar_init(&h2_free, kEpiThreads);   // h2 read
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&tmem_slot)),
+                 "r"(512));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  fence_before();
+  __syncthreads();
+  fence_after();
+  const uint32_t tmem = tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      int it = 0, s = 0;
+      uint32_t ph = 0;
+      bool ok = true;
+      int pt = cta_rank, pc = 0;
+      auto prefetch_next = [&]() {
+        if (pt >= mtiles) return;
+        tma_prefetch_2d(&tx, pc * 32, pt * kBlockM);
+        if (++pc == nk) {
+          pc = 0;
+          pt += cta_count;
+        }
+      };
+      for (int q = 0; q < kPrefetchAhead; ++q) prefetch_next();
+      for (int t = cta_rank; t < mtiles && ok; t += cta_count) {
+        for (int c = 0; c < nk; ++c) {
+          prefetch_next();
+          if (it >= kWideStages && !(ok = mbar_wait(&empty_bar[s], ph ^ 1u, err))) break;
+          uint8_t* st = smem + (size_t)s * kWideStage;
+          mbar_expect_tx(&full_bar[s], kWideStage);
+          tma_load_2d(st, &tx, &full_bar[s], c * 32, t * kBlockM);
+          tma_load_2d(st + kWideTile, &tb_hi, &full_bar[s], c * 32, slice * kWideNW);
+          tma_load_2d(st + 2 * kWideTile, &tb_lo, &full_bar[s], c * 32, slice * kWideNW);
+          ++it;
+          if (++s == kWideStages) {
+            s = 0;
+            ph ^= 1u;
+          }
+        }
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      const uint32_t idesc = instr_desc(kBlockM, kWideNW, true);
+      const uint64_t b0 = smem_desc(smem_u32(smem + kWideTile));
+      const uint32_t stage_step = kWideStage >> 4, lo_off = kWideTile >> 4;
+      int s = 0, o = 0, tc = 0;
+      uint32_t ph = 0, pho = 0;
+      bool ok = true;
+      for (int t = cta_rank; t < mtiles && ok; t += cta_count, ++tc) {
+        const uint32_t prev = (uint32_t)(tc - 1) & 1u;
+        if (tc > 0 && !(ok = mbar_wait(&acc_free, prev, err))) break;
+        fence_after();
+        for (int c = 0; c < nk && ok; ++c) {
+          // h2 of the previous tile is read while the first half of K runs
+          if (c == half && tc > 0) {
+            if (!(ok = mbar_wait(&h2_free, prev, err))) break;
+            fence_after();
+          }
+          if (!(ok = mbar_wait(&full_bar[s], ph, err))) break;
+          const uint64_t bh = b0 + (uint64_t)(s * stage_step), bl = bh + lo_off;
+          const uint32_t dh = tmem + (c < half ? kWideH1 : kWideH2), ds = tmem + kWideS;
+          const uint32_t acc_h = (c == 0 || c == half) ? 0u : 1u, acc_s = c == 0 ? 0u : 1u;
+          // two half-stages of 16 K values, each in its own operand slot
+          for (int hs = 0; hs < 2 && ok; ++hs) {
+            if (!(ok = mbar_wait(&cvt_bar[o], pho, err))) break;
+            fence_after();
+            const uint32_t ahi = tmem + kWideSlot + (uint32_t)(kWideSlotCols * o), alo = ahi + 16;
+#pragma unroll
+            for (int kk = 0; kk < 2; ++kk) {
+              const int k8 = 2 * hs + kk;
+              const bool lead = hs == 0 && kk == 0;  // first K step of this chunk
+              mma_tf32_ta(dh, ahi + 8 * kk, bh + 2 * k8, idesc, lead ? acc_h : 1u);
+              mma_tf32_ta(ds, ahi + 8 * kk, bl + 2 * k8, idesc, lead ? acc_s : 1u);
+              mma_tf32_ta(ds, alo + 8 * kk, bh + 2 * k8, idesc, 1u);
+            }
+            mma_commit(&op_free[o]);
+            if (++o == kWideSlots) {
+              o = 0;
+              pho ^= 1u;
+            }
+          }
+          if (!ok) break;
+          mma_commit(&empty_bar[s]);
+          if (++s == kWideStages) {
+            s = 0;
+            ph ^= 1u;
+          }
+        }
+        if (ok) mma_commit(&acc_full);
+      }
+    }
+  } else if (warp < 2 + kWideEpiWarps) {
+    const int q = warp & 3;             // TMEM lane quarter of this warp
+    const int part = (warp - 2) >> 2;   // which 64 of the 128 columns
+    const int row = q * 32 + lane;
+    const uint32_t lanes = static_cast<uint32_t>(q * 32) << 16;
+    const int c0 = 64 * part;
+    int tc = 0;
+    for (int t = cta_rank; t < mtiles; t += cta_count, ++tc) {
+      if (!mbar_wait(&acc_full, (uint32_t)tc & 1u, err, 128)) break;
+      __syncwarp();
+      fence_after();
+      const int m = t * kBlockM + row;
+      int i = 0, j = 0;
+      bool valid = false, nxy = false;
+      float lxy = 0.f;
+      if (e.kind != 0) {
+        i = m % e.P1;
+        j = m / e.P1;
+        valid = (i < e.n1) && (j < e.n2);
+        if (e.kind == 1 && valid) {
+          lxy = e.lam_x[i] + e.lam_y[j];
+          nxy = e.sigma_null && e.null_x[i] && e.null_y[j];
+        }
+      }
+      // v = (s + h1) + h2, the order of the narrow form.  s and h1 are
+      // released first (the next tile writes them from its first K step),
+      // h2 after its read (the next tile writes it from the second half)
+      float v[64], w[32];
+#pragma unroll
+      for (int hh = 0; hh < 2; ++hh) {
+        tmem_load32(tmem + lanes + c0 + 32 * hh + kWideS, v + 32 * hh);
+        tmem_load32(tmem + lanes + c0 + 32 * hh + kWideH1, w);
+#pragma unroll
+        for (int x = 0; x < 32; ++x) v[32 * hh + x] += w[x];
+      }
+      fence_before();
+      mbar_arrive(&acc_free);
+#pragma unroll
+      for (int hh = 0; hh < 2; ++hh) {
+        tmem_load32(tmem + lanes + c0 + 32 * hh + kWideH2, w);
+#pragma unroll
+        for (int x = 0; x < 32; ++x) v[32 * hh + x] += w[x];
+      }
+      fence_before();
+      mbar_arrive(&h2_free);
+#pragma unroll
+      for (int hh = 0; hh < 2; ++hh)
+        epilogue_cols<true>(e, v + 32 * hh, M, m, slice * kWideNW + c0 + 32 * hh, i, j, valid, lxy, nxy,
+                            s_lz, s_nz);
+    }
+  } else {
+    // converter warps: as in k_tc_transform<true>, with the X tile at the
+    // start of each (wider) ring stage
+    const int row = 32 * (warp & 3) + lane;
+    const uint32_t lane_base = static_cast<uint32_t>(32 * (warp & 3)) << 16;
+    int s = 0, o = 0, ih = 0;  // ring stage, operand slot, half-stages converted
+    uint32_t ph = 0, pho = 0;
+    bool ok = true;
+    for (int t = cta_rank; t < mtiles && ok; t += cta_count) {
+      for (int c = 0; c < nk; ++c) {
+        if (!(ok = mbar_wait(&full_bar[s], ph, err, 32))) break;
+        const float4* rowp =
+            reinterpret_cast<const float4*>(smem + (size_t)s * kWideStage + (size_t)row * 128);
+        float hi[32], lo[32];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const float4 x = rowp[j ^ (row & 7)];
+          hi[4 * j + 0] = x.x;
+          hi[4 * j + 1] = x.y;
+          hi[4 * j + 2] = x.z;
+          hi[4 * j + 3] = x.w;
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_arrive(&empty_bar[s]);
+#pragma unroll
+        for (int x = 0; x < 32; ++x) lo[x] = tf32_lo(hi[x]);
+        // two half-stages, each into the next operand slot once the MMAs
+        // that read its previous contents have completed
+#pragma unroll
+        for (int hs = 0; hs < 2; ++hs) {
+          if (ih >= kWideSlots && !(ok = mbar_wait(&op_free[o], pho ^ 1u, err, 32))) break;
+          const uint32_t slot = tmem + lane_base + kWideSlot + (uint32_t)(kWideSlotCols * o);
+          tmem_store16(slot, hi + 16 * hs);
+          tmem_store16(slot + 16, lo + 16 * hs);
+          fence_before();
+          mbar_arrive(&cvt_bar[o]);
+          ++ih;
+          if (++o == kWideSlots) {
+            o = 0;
+            pho ^= 1u;
+          }
+        }
+        if (!ok) break;
+        if (++s == kWideStages) {
+          s = 0;
+          ph ^= 1u;
+        }
+      }
+    }
+  }
+  __syncwarp();
+  fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
   }
 }
 
@@ -527,6 +811,14 @@ int tc_plan_create(TcPlan** out, bool tf32, const void* x_hi, const void* x_lo, 
     delete p;
     return rc;
   }
+  if (tf32 && N % kWideNW == 0) {
+    if ((rc = make_map(&p->b_hi_w, b_hi, true, N, K, kWideNW)) ||
+        (rc = make_map(&p->b_lo_w, b_lo, true, N, K, kWideNW))) {
+      delete p;
+      return rc;
+    }
+    p->wide = true;
+  }
   *out = p;
   return MF_OK;
 }
@@ -554,10 +846,46 @@ static int launch(const TcPlan* p, const TcEpilogue& e, int* dev_err, cudaStream
   return MF_OK;
 }
 
-int tc_transform(const TcPlan* p, const TcEpilogue& e, int* dev_err, cudaStream_t st) {
+static int launch_wide(const TcPlan* p, const TcEpilogue& e, int* dev_err, cudaStream_t st) {
+  static int num_sms = 0;
+  if (!num_sms) {
+    int dev = 0;
+    MF_CUDA(cudaGetDevice(&dev));
+    MF_CUDA(cudaFuncSetAttribute(k_tc_tf32_wide, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)kWideSmem));
+    int sms = 0;
+    MF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    num_sms = sms;
+  }
+  const int NS = p->N / kWideNW;
+  const int mtiles = p->M / kBlockM;
+  const int grid = std::min(num_sms / NS, mtiles) * NS;
+  k_tc_tf32_wide<<<grid, kWideThreads, kWideSmem, st>>>(p->x_hi, p->b_hi_w, p->b_lo_w, p->M, p->N,
+                                                         p->K, e, dev_err);
+  MF_CUDA(cudaGetLastError());
+  return MF_OK;
+}
+
+bool tc_has_wide(const TcPlan* p) { return p->tf32 && p->wide; }
+
+int tc_transform(const TcPlan* p, const TcEpilogue& e, int* dev_err, cudaStream_t st, int plan) {
   if (p->tf32 ? !e.y32 && e.kind != 2 : (!e.y_hi || !e.y_lo) && e.kind != 2)
     return set_error(MF_ERR_ARG, "tensor-core transform: output does not match the operand format");
+  if (plan == 0) plan = g_tf32_plan;
+  if (p->tf32 && p->wide && plan != 1) return launch_wide(p, e, dev_err, st);
   return p->tf32 ? launch<true>(p, e, dev_err, st) : launch<false>(p, e, dev_err, st);
 }
 
 }  // namespace mf
+
+extern "C" {
+
+int mf_tc_tf32_plan_set(int plan) {
+  if (plan < 0 || plan > 2) return mf::set_error(MF_ERR_ARG, "mf_tc_tf32_plan_set: plan must be 0, 1 or 2");
+  mf::tc_set_tf32_plan(plan);
+  return MF_OK;
+}
+
+int mf_tc_tf32_plan_get(void) { return mf::tc_get_tf32_plan(); }
+
+}  // extern "C"
