@@ -685,6 +685,7 @@ struct mf_navier {
   DevBuf dsum;   // per-subdomain sums of the flow-rate integral, then their total
   double reft = 0.0;  // integrale(1) over all subdomains
   double err_vts = 0.0, err_pre = 0.0;
+  const mf_mlp_t* les_mlp = nullptr;  // les_type 4: the caller's network (not owned)
   bool md() const { return mdu != nullptr; }
 };
 
@@ -917,7 +918,16 @@ int presolve(const mf_navier* nv, NsDom& d, const double* g, cudaStream_t st) {
     const double* du[9];
     for (int i = 0; i < 3; ++i)
       for (int j = 0; j < 3; ++j) du[3 * i + j] = d.T(3 * j + i);
-    if ((rc = mf_les_nu(d.les, P.les_type, P.les_c * P.les_c, du, d.nu.as<double>(), st))) return rc;
+    // les_type 4: the learned coefficient where the features are inside the
+    // network's training range, Smagorinsky with les_c^2 elsewhere
+    if (P.les_type == MF_LES_LEARNED) {
+      if (!nv->les_mlp)
+        return set_error(MF_ERR_ARG, "mf_navier_step: les_type 4 needs a network (mf_navier_set_les_network)");
+      if ((rc = mf_les_nu_mlp(d.les, nv->les_mlp, P.les_c * P.les_c, du, d.nu.as<double>(), nullptr, st)))
+        return rc;
+    } else if ((rc = mf_les_nu(d.les, P.les_type, P.les_c * P.les_c, du, d.nu.as<double>(), st))) {
+      return rc;
+    }
     k_ns_les_products<<<gb, kNsThreads, 0, st>>>(d.np, d.nu.as<double>(), d.T(0), d.T(9));
     if ((rc = launch_check("k_ns_les_products"))) return rc;
     Sweeps E;
@@ -1286,9 +1296,9 @@ int dom_setup(NsDom& d, const mf_navier_params_t* p, const double* gx, int nx, c
 
 int navier_check_params(const mf_navier_params_t* p) {
   if (!(p->ts > 0.0) || !(p->reynolds > 0.0) || p->nlt < 0 || p->nlt > 2 || p->pt < 1 || p->pt > 4 ||
-      p->tou < 1 || p->tou > 3 || p->nmodes < 0 || p->les_type < 0 || p->les_type > 3 || p->nsubite < 1)
+      p->tou < 1 || p->tou > 3 || p->nmodes < 0 || p->les_type < 0 || p->les_type > MF_LES_LEARNED || p->nsubite < 1)
     return set_error(MF_ERR_ARG,
-                     "mf_navier_create: bad parameters (ts, reynolds > 0; nlt 0..2; pt 1..4; tou 1..3; les_type 0..3)");
+                     "mf_navier_create: bad parameters (ts, reynolds > 0; nlt 0..2; pt 1..4; tou 1..3; les_type 0..4)");
   if (p->precision != MF_PREC_FP64 && p->precision != MF_PREC_SPLIT_BF16 && p->precision != MF_PREC_3XTF32)
     return set_error(MF_ERR_ARG, "mf_navier_create: unknown precision %d", p->precision);
   return MF_OK;
@@ -1516,6 +1526,15 @@ int mf_navier_step(mf_navier_t* nv, double* diag, void* stream) {
 int mf_navier_subiterations(const mf_navier_t* nv, int* n) {
   if (!nv || !n) return set_error(MF_ERR_ARG, "mf_navier_subiterations: null argument");
   *n = nv->subiterations;
+  return MF_OK;
+}
+
+int mf_navier_set_les_network(mf_navier_t* nv, const mf_mlp_t* mlp) {
+  if (!nv) return set_error(MF_ERR_ARG, "mf_navier_set_les_network: null handle");
+  if (nv->prm.les_type != MF_LES_LEARNED)
+    return set_error(MF_ERR_ARG, "mf_navier_set_les_network: the step was created with les_type %d, not 4",
+                     nv->prm.les_type);
+  nv->les_mlp = mlp;
   return MF_OK;
 }
 

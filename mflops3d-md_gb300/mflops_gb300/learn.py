@@ -30,10 +30,14 @@ def uniform_grid(n):
 class BoxFlow:
     """Fine-grid decaying flow in the no-slip unit box (FP64, device fields)."""
 
-    def __init__(self, n, nu, seed, k0=30.0, so=6):
+    def __init__(self, n, nu, seed, k0=30.0, so=6, precision=None, refine=2):
         import torch
         self.n = n
         self.nu = nu
+        # projection solves: plain FP64 by default, or a mixed mode with
+        # `refine` FP64-residual refinement steps (axes up to 256 points)
+        self.precision = mf.MF_PREC_FP64 if precision is None else precision
+        self.refine = refine
         self.grid = uniform_grid(n)
         g = self.grid
         self.dc = mf.DerivativesCoefficients(g, so=so)
@@ -87,7 +91,8 @@ class BoxFlow:
         mf.flow_divergence(1.0, *self.dphi, out=self.rhs)
         # a small negative shift keeps the constant mode regular; constants
         # have no gradient, so the correction does not depend on it
-        self.poisson.solve_3d(self.rhs, -1e-3, self.phi, *self.zero_bc)
+        self.poisson.solve_3d(self.rhs, -1e-3, self.phi, *self.zero_bc, precision=self.precision,
+                              refine=self.refine if self.precision != mf.MF_PREC_FP64 else -1)
         for j in range(3):
             self.dc.apply(j, 1, self.phi, out=self.dphi[j])
         mf.flow_correct(1.0, u, self.dphi)
@@ -264,3 +269,116 @@ def evaluate(mlp, scaling, X, base, target):
     return dict(mse_mlp=mse(nu_m), mse_const=mse(nu_c), mse_zero=float((t * t).mean()),
                 corr_mlp=corr(nu_m), corr_const=corr(nu_c), inside=float(inside.double().mean()),
                 n=int(t.numel()))
+
+
+# ---------------------------------------------------------------------------
+# A-posteriori judgement: LES runs of the time step against the filtered fine run
+# ---------------------------------------------------------------------------
+
+def profile_and_spectrum(u, margin=1):
+    """(mean profile, spectrum) of a velocity field on a box grid: the
+    kinetic energy averaged over x-z planes as a function of y, and the
+    energy spectrum along x (squared moduli of the FFT of each interior x
+    line, averaged over the interior y, z points and the three components).
+    Both as float64 torch tensors."""
+    import torch
+    m = margin
+    ke = sum(c * c for c in u) * 0.5
+    prof = ke[:, m:ke.shape[1] - m, :].mean(dim=(0, 2))
+    spec = 0.0
+    for c in u:
+        inner = c[1:-1, m:c.shape[1] - m, m:c.shape[2] - m]
+        spec = spec + (torch.fft.rfft(inner, dim=0).abs() ** 2).mean(dim=(1, 2))
+    return prof, spec / 3.0
+
+
+def profile_error(a, b):
+    """rel-L2 distance of two mean profiles."""
+    return float((a - b).norm() / b.norm())
+
+
+def spectrum_error(a, b, kmax=None):
+    """Mean |log(E_a(k) / E_b(k))| over the wavenumbers 1..kmax."""
+    import torch
+    k = slice(1, kmax) if kmax else slice(1, None)
+    return float(torch.log(a[k] / b[k]).abs().mean())
+
+
+class APosteriori:
+    """LES runs of the Navier-Stokes time step (mf_navier_step, one domain,
+    no-slip walls, no forcing: nmodes = 0, no flow-rate term) on the LES grid,
+    started from the filtered fine field and compared with the filtered fine
+    run at the same times.  Models: none (les_type 0), Smagorinsky with the
+    training's best constant (les_c^2 = c0), and the learned coefficient
+    (les_type 4, Smagorinsky with c0 where the features leave the training
+    range).  The plain model is the judge: the network's errors are reported
+    next to it."""
+
+    def __init__(self, fine_flow, pairs, mlp, scaling, precision=None, refine=1):
+        self.fine = fine_flow
+        self.pairs = pairs
+        self.mlp = mlp
+        self.c0 = scaling["c0"]
+        self.precision = mf.MF_PREC_3XTF32 if precision is None else precision
+        self.refine = refine
+
+    def filtered(self):
+        return [self.pairs.filter3(c).clone() for c in self.fine.u]
+
+    def _les(self, start, les_type, dt):
+        g = self.pairs.coarse
+        kw = dict(ts=dt, reynolds=1.0 / self.fine.nu, nmodes=0, flow_rate=0, precision=self.precision,
+                  refine=self.refine)
+        if les_type:
+            kw.update(les_type=les_type, les_c=float(np.sqrt(max(self.c0, 0.0))))
+        nav = mf.NavierStokes3D(g, g, g, **kw)
+        if les_type == mf.MF_LES_LEARNED:
+            nav.set_les_network(self.mlp)
+        for lev in range(4):
+            for q, var in enumerate("uvw"):
+                nav.set_field(var, lev, start[q])
+        return nav
+
+    def run(self, t_end, checkpoints=4, dt_les=None, cfl=0.3, models=(0, 1, 4)):
+        """Advance the fine flow and the LES runs to t_end; at `checkpoints`
+        equally spaced times compare mean profile and spectrum.  Returns a
+        dict per model: lists of (time, profile error, spectrum error) and
+        the final divergence norm, plus the LES step time in ms."""
+        import torch
+        start = self.filtered()
+        h = self.pairs.coarse[1] - self.pairs.coarse[0]
+        umax = max(float(c.abs().max()) for c in start)
+        dt = dt_les or cfl * h / max(umax, 1e-12)
+        per = max(1, int(round(t_end / checkpoints / dt)))
+        dt = t_end / checkpoints / per
+        runs = {m: self._les(start, m, dt) for m in models}
+        out = {m: {"errors": []} for m in models}
+        t = self.fine.time
+        t0 = t
+        step_ms = {m: 0.0 for m in models}
+        for c in range(1, checkpoints + 1):
+            target = t0 + c * t_end / checkpoints
+            while self.fine.time < target - 1e-12:
+                self.fine.step(min(self.fine.cfl_dt(cfl), target - self.fine.time))
+            ref = profile_and_spectrum(self.filtered())
+            for m, nav in runs.items():
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record()
+                for _ in range(per):
+                    nav.step()
+                b.record()
+                torch.cuda.synchronize()
+                step_ms[m] += a.elapsed_time(b) / per / checkpoints
+                les = profile_and_spectrum([nav.field(v, 3) for v in "uvw"])
+                kmax = les[1].numel() // 2
+                out[m]["errors"].append((target, profile_error(les[0], ref[0]),
+                                         spectrum_error(les[1], ref[1], kmax)))
+        for m, nav in runs.items():
+            d = nav.step(diagnostics=True)
+            out[m]["divergence"] = d["div"]
+            out[m]["step_ms"] = step_ms[m]
+            out[m]["profile_error_mean"] = float(np.mean([e[1] for e in out[m]["errors"]]))
+            out[m]["spectrum_error_mean"] = float(np.mean([e[2] for e in out[m]["errors"]]))
+            nav.close()
+        out["dt_les"] = dt
+        return out

@@ -33,7 +33,9 @@ src/class_navier/class_navier_3D.f90:
 
 ``navier_LES`` (:1225-1455) runs before the presolve: the nine gradients of
 the newest velocity level (edges zeroed) and, for les_type 1, 2, 3, the eddy
-viscosity of oracle.les with the coefficient les_c**2 (:2138); the forcing
+viscosity of oracle.les with the coefficient les_c**2 (:2138) -- for
+les_type 4 the learned coefficient of oracle.mlp.nu_mlp with that
+Smagorinsky value as the fallback (no reference counterpart); the forcing
 then subtracts les_f = -sum_j d/dx_j (nu (du_ij + du_ji)) (:1083-1099) before
 the flow-rate term.  The 1e-10 of the flow-rate term is a default-kind
 (single precision) literal.
@@ -42,6 +44,7 @@ import numpy as np
 
 from oracle import derivatives as D
 from oracle import les as L
+from oracle import mlp as M
 from oracle import solver as S
 from oracle.les import zero_edges
 
@@ -136,6 +139,7 @@ class Navier:
         self.sub = None
         self.du = None
         self.les_nu = None
+        self.les_network = None  # les_type 4: dict(params, mean, istd, lo, hi, cscale)
         self.fac = bdf_factors(tou, ts)
         self.sigmau = -self.rey * self.fac[0]
         self.sigmap = 0.0
@@ -289,7 +293,15 @@ class Navier:
             grads = (self.derx, self.dery, self.derz)
             vel = (self.u[n0], self.v[n0], self.w[n0])
             self.du = [[zero_edges(grads[j](vel[i])) for j in range(3)] for i in range(3)]
-            self.les_nu = L.les_nu(self.du, self.gx, self.gy, self.gz, self.les_type, self.les_c ** 2)
+            if self.les_type == 4:
+                # the learned coefficient (network parameters and scaling in
+                # self.les_network, oracle.mlp.nu_mlp), Smagorinsky with
+                # les_c**2 outside the training range
+                net = self.les_network
+                self.les_nu, _ = M.nu_mlp(net["params"], self.du, self.gx, self.gy, self.gz, net["mean"],
+                                          net["istd"], net["lo"], net["hi"], net["cscale"], self.les_c ** 2)
+            else:
+                self.les_nu = L.les_nu(self.du, self.gx, self.gy, self.gz, self.les_type, self.les_c ** 2)
         for c in "uvw":
             self.rhs[c][1] = self.rhs[c][0]
             nl = self.nonlinear(levels[c])

@@ -105,6 +105,38 @@ def test_steps_match_the_oracle(mf, gpu, name):
     print("%s: worst field max-rel %.2e after 6 steps" % (name, worst))
 
 
+def test_learned_les_steps_match_the_oracle(mf, gpu):
+    """les_type 4: the eddy viscosity from a (seeded, untrained) network of
+    the learned coefficient inside the step, against the oracle step with the
+    FP64 network.  The GPU network runs in FP32 with a 3xTF32 hidden layer
+    (coefficient ~1e-6 relative), so the fields agree to about that (1e-6;
+    the pressure, through the projection, is the most sensitive: 1.3e-7
+    measured after four steps); the training range is unbounded here, so no
+    point sits on the fallback boundary (the fallback itself is covered by
+    tests/test_learned_les.py)."""
+    kw = dict(ts=2e-3, reynolds=100.0, les_type=4, les_c=0.17)
+    ora, nav = make_pair(mf, **kw)
+    net = mf.Mlp(7)
+    inf = np.full(6, np.inf, np.float32)
+    mean = np.array([0.3, 0.0, 0.0, 0.1, 0.0, 0.0])
+    istd = np.array([3.0, 5.0, 5.0, 3.0, 5.0, 5.0])
+    net.set_scaling(mean, istd, -inf, inf, 0.03, 1.0)
+    nav.set_les_network(net)
+    ora.les_network = dict(params=net.params().astype(np.float64), mean=mean.astype(np.float32).astype(np.float64),
+                           istd=istd.astype(np.float32).astype(np.float64), lo=-np.inf, hi=np.inf,
+                           cscale=float(np.float32(0.03)))
+    for _ in range(4):
+        ora.advance()
+        nav.step()
+    worst = compare(mf, ora, nav, 1e-6)
+    print("learned LES: worst field max-rel %.2e after 4 steps" % worst)
+    # the LES term is active: the learned viscosity differs from zero
+    assert float(np.abs(ora.les_nu).max()) > 0.0
+    bare = mf.NavierStokes3D(*grids(), **kw)
+    with pytest.raises(mf.MflopsError):
+        bare.step()
+
+
 @pytest.mark.parametrize("prec_name,refine", [("MF_PREC_3XTF32", 1), ("MF_PREC_SPLIT_BF16", 2)])
 def test_mixed_precision_solves(mf, gpu, prec_name, refine):
     kw = dict(CASES["defaults"], precision=getattr(mf, prec_name), refine=refine)
