@@ -336,6 +336,244 @@ __global__ void __launch_bounds__(kTriThreads) k_tri_step(const double* __restri
   }
 }
 
+// ---------------------------------------------------------------------------
+// Persistent triangular solves (default when cooperative launch is available)
+//
+// The block steps above pay a launch and a grid-wide drain per 128 rows.  On
+// GB300 the solve is bound by the FP64 pipe (n^2/2 FMAs per triangle, about
+// 1.8 ms at n = 46,860), not by the 8 n^2 bytes of the factor, so what
+// matters is keeping every SM's FP64 units busy while the chain of diagonal
+// blocks advances.  One cooperative launch per triangle does it:
+//  * blocks of kPb = 64 rows; logical step t is block t (L, forward) or
+//    block nb-1-t (U, backward); CTA g owns the steps t = g mod G and keeps
+//    their right-hand sides acc_t (K vectors) in shared memory;
+//  * when sol_t is published (global store, fence, release flag), every CTA
+//    applies panel t to its owned blocks further down (64 x 64 FP64 products
+//    read coalesced from the column-major factor);
+//  * the diagonal chain is shortened with set-up products
+//    W_t = inv(D_t) T(t, t-1): sol_t = z_t - W_t sol_{t-1}, where
+//    z_t = inv(D_t) acc_t is formed as soon as acc_t has received every panel
+//    but the last, off the critical path.  The owner of t+1 forms and
+//    publishes sol_{t+1} right after it receives sol_t, before its other
+//    work, so one 64 x 64 product and one flag hop separate consecutive
+//    blocks;
+//  * flags are zeroed by a memset before each launch; every wait is bounded
+//    (about a second of clock) and raises *err instead of hanging.
+// The products sum in a fixed order, so results are reproducible run to run.
+constexpr int kPb = 64;
+constexpr int kPThreads = 256;
+constexpr int kPMaxOwned = 48;   // steps per CTA: nb <= kPMaxOwned * grid
+constexpr long long kPWaitCycles = 2000000000LL;
+
+// Inverse of diagonal block b (kPb rows) of L (unit) or U, as
+// k_tri_block_inverse; out = column-major kPb x kPb per block.
+__global__ void __launch_bounds__(256) k_pdinv(const double* __restrict__ A, int n, int upper,
+                                               double* __restrict__ out) {
+  __shared__ double X[kPb * kPb];  // row r at X[r * kPb]
+  const int k0 = blockIdx.x * kPb, nb = min(kPb, n - k0);
+  for (int t = threadIdx.x; t < kPb * kPb; t += blockDim.x)
+    X[t] = (t / kPb == t % kPb && t / kPb < nb) ? 1.0 : 0.0;
+  __syncthreads();
+  if (!upper) {
+    for (int c = 0; c < nb; ++c) {
+      for (int t = threadIdx.x; t < (nb - c - 1) * (c + 1); t += blockDim.x) {
+        const int r = c + 1 + t / (c + 1), j = t % (c + 1);
+        X[r * kPb + j] -= A[(k0 + r) + (long long)n * (k0 + c)] * X[c * kPb + j];
+      }
+      __syncthreads();
+    }
+  } else {
+    for (int c = nb - 1; c >= 0; --c) {
+      const double d = A[(k0 + c) + (long long)n * (k0 + c)];
+      for (int j = c + threadIdx.x; j < nb; j += blockDim.x) X[c * kPb + j] = X[c * kPb + j] / d;
+      __syncthreads();
+      for (int t = threadIdx.x; t < c * (nb - c); t += blockDim.x) {
+        const int r = t / (nb - c), j = c + t % (nb - c);
+        X[r * kPb + j] -= A[(k0 + r) + (long long)n * (k0 + c)] * X[c * kPb + j];
+      }
+      __syncthreads();
+    }
+  }
+  double* o = out + (size_t)blockIdx.x * kPb * kPb;
+  for (int t = threadIdx.x; t < kPb * kPb; t += blockDim.x) o[t] = X[(t % kPb) * kPb + t / kPb];
+}
+
+// W_b = inv(D_b) T(b, b-1) (L) or inv(D_b) T(b, b+1) (U), column-major
+// kPb x kPb, zero outside the blocks' extents; one CTA per block (the first
+// block of L and the last of U have none and stay zero).
+__global__ void __launch_bounds__(256) k_pw(const double* __restrict__ A, int n, int upper,
+                                            const double* __restrict__ dinv, double* __restrict__ W) {
+  __shared__ double D[kPb * kPb], T[kPb * kPb];
+  const int b = blockIdx.x, nbk = (n + kPb - 1) / kPb;
+  const int ob = upper ? b + 1 : b - 1;
+  double* o = W + (size_t)b * kPb * kPb;
+  if (ob < 0 || ob >= nbk) {
+    for (int t = threadIdx.x; t < kPb * kPb; t += blockDim.x) o[t] = 0.0;
+    return;
+  }
+  const int r0 = b * kPb, rn = min(kPb, n - r0), c0 = ob * kPb, cn = min(kPb, n - c0);
+  for (int t = threadIdx.x; t < kPb * kPb; t += blockDim.x) {
+    const int r = t % kPb, c = t / kPb;
+    D[t] = dinv[(size_t)b * kPb * kPb + t];
+    T[t] = (r < rn && c < cn) ? A[(r0 + r) + (long long)n * (c0 + c)] : 0.0;
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < kPb * kPb; t += blockDim.x) {
+    const int r = t % kPb, c = t / kPb;
+    double s = 0.0;
+    for (int k = 0; k < kPb; ++k) s = fma(D[r + kPb * k], T[k + kPb * c], s);
+    o[t] = s;
+  }
+}
+
+// out[k][r] (=|-=) sum_c M(r, c) x[k][c] for a 64 x 64 column-major tile M
+// with leading dimension ld (rows >= rn and columns >= cn are not read), K
+// vectors x in shared memory.  Thread t: row t % 64, columns 16 (t / 64) ..
+// +15; the four partial sums are added in a fixed order.
+template <int K>
+__device__ __forceinline__ void tile_gemv(const double* __restrict__ M, long long ld, int rn, int cn,
+                                          const double (*x)[kPb], double (*part)[K][kPb], double (*out)[kPb],
+                                          bool subtract) {
+  const int r = threadIdx.x & (kPb - 1), g = threadIdx.x >> 6;
+  double acc[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) acc[k] = 0.0;
+  if (r < rn) {
+    double e[16];
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+      const int c = 16 * g + q;
+      e[q] = c < cn ? M[r + ld * c] : 0.0;
+    }
+#pragma unroll
+    for (int q = 0; q < 16; ++q)
+#pragma unroll
+      for (int k = 0; k < K; ++k) acc[k] = fma(e[q], x[k][16 * g + q], acc[k]);
+  }
+#pragma unroll
+  for (int k = 0; k < K; ++k) part[g][k][r] = acc[k];
+  __syncthreads();
+  if (threadIdx.x < kPb * K) {
+    const int rr = threadIdx.x % kPb, k = threadIdx.x / kPb;
+    const double s = (part[0][k][rr] + part[1][k][rr]) + (part[2][k][rr] + part[3][k][rr]);
+    out[k][rr] = subtract ? out[k][rr] - s : s;
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ int flag_acquire(const int* f) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(f) : "memory");
+  return v;
+}
+__device__ __forceinline__ void flag_release(int* f, int v) {
+  asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(f), "r"(v) : "memory");
+}
+
+// One triangle: sol = inv(T) v for the unit lower L (upper = 0) or U
+// (upper = 1) of the column-major factor A; K right-hand sides, vector k at
+// v + k n and sol + k n.  flags[nb] zero on entry.
+template <int K>
+__global__ void __launch_bounds__(kPThreads) k_tri_persist(const double* __restrict__ A, int n, int upper,
+                                                           const double* __restrict__ dinv,
+                                                           const double* __restrict__ W,
+                                                           const double* __restrict__ v, double* sol, int* flags,
+                                                           int* err) {
+  extern __shared__ double sm[];
+  const int nb = (n + kPb - 1) / kPb, G = gridDim.x, g = blockIdx.x;
+  const int owned = (nb - g + G - 1) / G;           // steps g, g + G, ...
+  double (*acc)[K][kPb] = reinterpret_cast<double (*)[K][kPb]>(sm);                // [owned]
+  double (*z)[K][kPb] = reinterpret_cast<double (*)[K][kPb]>(sm + (size_t)owned * K * kPb);
+  double (*cur)[kPb] = reinterpret_cast<double (*)[kPb]>(sm + (size_t)2 * owned * K * kPb);  // [K]
+  double (*nxt)[kPb] = cur + K;
+  double (*part)[K][kPb] = reinterpret_cast<double (*)[K][kPb]>(nxt + K);              // [4]
+  __shared__ int s_fail;
+  auto blk = [&](int t) { return upper ? nb - 1 - t : t; };
+  auto rows = [&](int t) { return min(kPb, n - blk(t) * kPb); };
+  auto mine = [&](int t) { return t < nb && t % G == g; };
+  auto slot = [&](int t) { return t / G; };
+  // publish cur (= sol_t) and raise flag t
+  auto publish = [&](int t, double (*x)[kPb]) {
+    const int r0 = blk(t) * kPb, rn = rows(t);
+    for (int q = threadIdx.x; q < K * kPb; q += blockDim.x) {
+      const int k = q / kPb, r = q % kPb;
+      if (r < rn) __stcg(sol + (size_t)k * n + r0 + r, x[k][r]);
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) flag_release(flags + t, 1);
+  };
+  // z_t = inv(D_t) acc_t
+  auto form_z = [&](int t) {
+    tile_gemv<K>(dinv + (size_t)blk(t) * kPb * kPb, kPb, rows(t), rows(t), acc[slot(t)], part, z[slot(t)], false);
+  };
+  if (threadIdx.x == 0) s_fail = 0;
+  for (int s = 0; s < owned; ++s) {
+    const int t = g + s * G, r0 = blk(t) * kPb, rn = rows(t);
+    for (int q = threadIdx.x; q < K * kPb; q += blockDim.x) {
+      const int k = q / kPb, r = q % kPb;
+      acc[s][k][r] = r < rn ? v[(size_t)k * n + r0 + r] : 0.0;
+    }
+  }
+  __syncthreads();
+  if (mine(0)) {
+    form_z(0);
+    for (int q = threadIdx.x; q < K * kPb; q += blockDim.x) cur[q / kPb][q % kPb] = z[0][q / kPb][q % kPb];
+    __syncthreads();
+    publish(0, cur);
+  }
+  if (mine(1)) form_z(1);
+  for (int t = 0; t + 1 < nb; ++t) {
+    // sol_t into cur (computed here when this CTA owns t)
+    if (!mine(t)) {
+      if (threadIdx.x == 0) {
+        const long long c0 = clock64();
+        while (flag_acquire(flags + t) == 0) {
+          __nanosleep(64);
+          if (clock64() - c0 > kPWaitCycles) {
+            atomicExch(err, 1);
+            s_fail = 1;
+            break;
+          }
+        }
+      }
+      __syncthreads();
+      if (s_fail) return;
+      const int r0 = blk(t) * kPb, rn = rows(t);
+      for (int q = threadIdx.x; q < K * kPb; q += blockDim.x) {
+        const int k = q / kPb, r = q % kPb;
+        cur[k][r] = r < rn ? __ldcg(sol + (size_t)k * n + r0 + r) : 0.0;
+      }
+      __syncthreads();
+    }
+    // the critical block first: sol_{t+1} = z_{t+1} - W_{t+1} sol_t
+    if (mine(t + 1)) {
+      const int s1 = slot(t + 1);
+      for (int q = threadIdx.x; q < K * kPb; q += blockDim.x) nxt[q / kPb][q % kPb] = z[s1][q / kPb][q % kPb];
+      __syncthreads();
+      tile_gemv<K>(W + (size_t)blk(t + 1) * kPb * kPb, kPb, rows(t + 1), rows(t), cur, part, nxt, true);
+      publish(t + 1, nxt);
+    }
+    // panel t on the owned blocks two or more steps ahead
+    const int cb = blk(t) * kPb, cn = rows(t);
+    for (int s = 0; s < owned; ++s) {
+      const int u = g + s * G;
+      if (u < t + 2) continue;
+      tile_gemv<K>(A + (size_t)blk(u) * kPb + (size_t)n * cb, n, rows(u), cn, cur, part, acc[s], true);
+    }
+    if (mine(t + 2)) form_z(t + 2);
+    // the block published above is the next step's sol
+    if (mine(t + 1)) {
+      for (int q = threadIdx.x; q < K * kPb; q += blockDim.x) cur[q / kPb][q % kPb] = nxt[q / kPb][q % kPb];
+      __syncthreads();
+    }
+  }
+}
+
+static size_t tri_persist_smem(int owned, int K) {
+  return sizeof(double) * ((size_t)2 * owned * K * kPb + 2 * K * kPb + 4 * K * kPb);
+}
+
 // Influence-matrix assembly in the eigenbasis of the subdomain solver.  A
 // Dirac datum at point (s1, s2) of face (l, m) folds into the right-hand
 // side phi_{l,m}(i_l) delta(s1) delta(s2) (phi = -inv_lhs(:, ends) ddr bc),
@@ -571,6 +809,9 @@ struct mf_md {
   std::vector<Sub> sub;  // index i + nd1*(j + nd2*k)
   DevBuf M, ipiv, vec, info, work, zero_int, rint, ufield;
   DevBuf perm, dinv, lu_v, lu_y;  // LU solve: row permutation, diagonal-block inverses, work vectors
+  DevBuf pdinv, pw, pflags, perr; // persistent LU solve: 64-row block inverses, W blocks, flags, error flag
+  bool persist_ok = false;
+  int tri_form = 0;               // 0 persistent when possible, 1 one launch per block step
   DevBuf Minv, vec2;  // row-major inverse of the influence matrix, solve output
   DevBuf ub, dub[3], bcb;  // batched influence columns: fields, derivatives, Dirac faces
   bool inv_ok = false;
@@ -665,6 +906,66 @@ static int face_weights(mf_md::Sub& sd, int a) {
 static long long face_points(const mf_md::Sub& sd, int l) {
   const int a = l == 0 ? 1 : 0, b = l == 2 ? 1 : 2;
   return (long long)(sd.n[a] - 2) * (sd.n[b] - 2);
+}
+
+template <int K>
+static int launch_tri_persist(mf_md* md, int upper, const double* v, double* sol, cudaStream_t st, bool* done) {
+  *done = false;
+  const int n = (int)md->topo.ninf, nb = (n + kPb - 1) / kPb;
+  static int sms = 0, occ[5] = {0, 0, 0, 0, 0};
+  if (!sms) {
+    int dev = 0;
+    MF_CUDA(cudaGetDevice(&dev));
+    MF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  }
+  // grid: one CTA per SM, fewer when there are fewer blocks
+  const int G = std::min(nb, sms);
+  const int owned = (nb + G - 1) / G;
+  if (owned > kPMaxOwned) return MF_OK;
+  const size_t smem = tri_persist_smem(owned, K);
+  if (smem > 200 * 1024) return MF_OK;
+  MF_CUDA(cudaFuncSetAttribute(k_tri_persist<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  if (!occ[K]) {
+    int o = 0;
+    MF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_tri_persist<K>, kPThreads, smem));
+    occ[K] = o;
+  }
+  if (occ[K] < 1) return MF_OK;  // not co-resident: the block steps take over
+  const size_t half = (size_t)nb * kPb * kPb;
+  const double* A = md->M.as<double>();
+  const double* dinv = md->pdinv.as<double>() + (upper ? half : 0);
+  const double* W = md->pw.as<double>() + (upper ? half : 0);
+  int* flags = md->pflags.as<int>() + (upper ? nb : 0);
+  int* err = md->perr.as<int>();
+  MF_CUDA(cudaMemsetAsync(flags, 0, sizeof(int) * nb, st));
+  int nn = n, up = upper;
+  void* args[] = {(void*)&A, (void*)&nn, (void*)&up, (void*)&dinv, (void*)&W, (void*)&v, (void*)&sol,
+                  (void*)&flags, (void*)&err};
+  MF_CUDA(cudaLaunchCooperativeKernel((const void*)k_tri_persist<K>, dim3(G), dim3(kPThreads), args, smem, st));
+  *done = true;
+  return MF_OK;
+}
+
+// Persistent triangular solves of K right-hand sides stored one after the
+// other at x (n each): x = U^-1 L^-1 P x.  *done is false when the
+// persistent form does not apply (the caller then uses md_lu_solve).
+template <int K>
+static int md_lu_solve_persist(mf_md* md, double* x, cudaStream_t st, bool* done) {
+  *done = false;
+  if (!md->persist_ok) return MF_OK;
+  const int n = (int)md->topo.ninf;
+  double* v = md->lu_v.as<double>();
+  double* y = md->lu_y.as<double>();
+  for (int k = 0; k < K; ++k)
+    k_permute<<<nblk(n, 256), 256, 0, st>>>(x + (size_t)k * n, md->perm.as<int>(), v + (size_t)k * n, n);
+  MF_CUDA(cudaGetLastError());
+  bool d1 = false, d2 = false;
+  int rc = launch_tri_persist<K>(md, 0, v, y, st, &d1);
+  if (rc || !d1) return rc;
+  if ((rc = launch_tri_persist<K>(md, 1, y, x, st, &d2))) return rc;
+  if (!d2) return set_error(MF_ERR_CUDA, "persistent triangular solve: second launch not possible");
+  *done = true;
+  return MF_OK;
 }
 
 // Blocked triangular solves with the LU factor in md->M: x = U^-1 L^-1 P x.
@@ -825,6 +1126,8 @@ int mf_md_destroy(mf_md_t* md) {
   }
   if (md->fork) cudaEventDestroy(md->fork);
   for (DevBuf* b : {&md->Minv, &md->vec2, &md->ub, &md->dub[0], &md->dub[1], &md->dub[2], &md->bcb}) b->release();
+  for (DevBuf* b : {&md->pdinv, &md->pw, &md->pflags, &md->perr})
+    b->release();
   for (DevBuf* b : {&md->perm, &md->dinv, &md->lu_v, &md->lu_y, &md->M, &md->ipiv, &md->vec, &md->info,
                     &md->work, &md->zero_int, &md->rint, &md->ufield})
     b->release();
@@ -1129,6 +1432,33 @@ static int md_factor_finish(mf_md* md, cudaStream_t st) {
         (rc = md->dinv.ensure(2 * (size_t)nblocks * smem)))
       return rc;
     MF_CUDA(cudaMemcpy(md->perm.ptr, perm.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+    // persistent solves: 64-row block inverses and the W blocks of both factors
+    {
+      int coop = 0, dev = 0;
+      MF_CUDA(cudaGetDevice(&dev));
+      MF_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+      const int pnb = (int)((n + kPb - 1) / kPb);
+      const size_t pbs = (size_t)kPb * kPb * sizeof(double);
+      md->persist_ok = false;
+      if (coop && (rc = md->pdinv.ensure(2 * (size_t)pnb * pbs)) == MF_OK &&
+          (rc = md->pw.ensure(2 * (size_t)pnb * pbs)) == MF_OK &&
+          (rc = md->pflags.ensure(2 * sizeof(int) * pnb)) == MF_OK &&
+          (rc = md->perr.ensure(sizeof(int))) == MF_OK &&
+          (rc = md->lu_v.ensure(sizeof(double) * kMdMaxRhs * n)) == MF_OK &&
+          (rc = md->lu_y.ensure(sizeof(double) * kMdMaxRhs * n)) == MF_OK) {
+        double* pd = md->pdinv.as<double>();
+        double* pw = md->pw.as<double>();
+        const size_t half = (size_t)pnb * kPb * kPb;
+        k_pdinv<<<pnb, 256, 0, st>>>(M, (int)n, 0, pd);
+        k_pdinv<<<pnb, 256, 0, st>>>(M, (int)n, 1, pd + half);
+        k_pw<<<pnb, 256, 0, st>>>(M, (int)n, 0, pd, pw);
+        k_pw<<<pnb, 256, 0, st>>>(M, (int)n, 1, pd + half, pw + half);
+        MF_CUDA(cudaMemsetAsync(md->perr.ptr, 0, sizeof(int), st));
+        MF_CUDA(cudaGetLastError());
+        md->persist_ok = true;
+      }
+      if (rc) return rc;
+    }
     MF_CUDA(cudaFuncSetAttribute(k_tri_block_inverse, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k_tri_block_inverse<<<nblocks, 256, smem, st>>>(M, (int)n, 0, md->dinv.as<double>());
     k_tri_block_inverse<<<nblocks, 256, smem, st>>>(M, (int)n, 1,
@@ -1360,7 +1690,15 @@ static int md_solve_impl(mf_md_t* md, int nrhs, const double* const* g, double* 
     MF_CUDA(cudaGetLastError());
     MF_CUDA(cudaMemcpyAsync(vecs, y, sizeof(double) * n * nrhs, cudaMemcpyDeviceToDevice, st));
   } else {
-    for (int r = 0; r < nrhs; ++r)
+    bool done = false;
+    if (md->tri_form != 1) {
+      if (nrhs == 1) rc = md_lu_solve_persist<1>(md, vecs, st, &done);
+      if (nrhs == 2) rc = md_lu_solve_persist<2>(md, vecs, st, &done);
+      if (nrhs == 3) rc = md_lu_solve_persist<3>(md, vecs, st, &done);
+      if (nrhs == 4) rc = md_lu_solve_persist<4>(md, vecs, st, &done);
+      if (rc) return rc;
+    }
+    for (int r = 0; r < nrhs && !done; ++r)
       if ((rc = md_lu_solve(md, vecs + (size_t)r * n, st))) return rc;
   }
   if (md->null_mode == 1)
@@ -1417,6 +1755,23 @@ int mf_md_set_interface_solve(mf_md_t* md, int mode) {
   if (!md || (mode != MF_MD_IFACE_AUTO && mode != MF_MD_IFACE_LU && mode != MF_MD_IFACE_INVERSE))
     return set_error(MF_ERR_ARG, "mf_md_set_interface_solve: bad arguments");
   md->iface_mode = mode;
+  return MF_OK;
+}
+
+int mf_md_set_triangular_form(mf_md_t* md, int form) {
+  if (!md || (form != MF_MD_TRI_PERSISTENT && form != MF_MD_TRI_STEPS))
+    return set_error(MF_ERR_ARG, "mf_md_set_triangular_form: bad arguments");
+  md->tri_form = form;
+  return MF_OK;
+}
+
+int mf_md_device_status(const mf_md_t* md) {
+  if (!md) return set_error(MF_ERR_ARG, "mf_md_device_status: null handle");
+  if (!md->perr.ptr) return MF_OK;
+  int e = 0;
+  MF_CUDA(cudaDeviceSynchronize());
+  MF_CUDA(cudaMemcpy(&e, md->perr.ptr, sizeof(int), cudaMemcpyDeviceToHost));
+  if (e) return set_error(MF_ERR_TIMEOUT, "multidomain triangular solve: a block wait expired");
   return MF_OK;
 }
 

@@ -255,3 +255,61 @@ def test_eigen_assembly_matches_solve_assembly(mf, gpu, nd, periods, bct, sigma,
         if null:  # the null-space solution is defined up to a constant
             a, b = a - a.mean(), b - b.mean()
         assert max_rel(a, b) < 1e-11, (c, max_rel(a, b))
+
+
+def _random_solve(mf, dev, seed):
+    import torch
+    gen = torch.Generator("cuda").manual_seed(seed)
+    g, u, bc = {}, {}, {}
+    for c in dev.subdomains():
+        sh = dev.shape(*c)
+        g[c] = torch.randn(tuple(reversed(sh)), dtype=torch.float64, device="cuda",
+                           generator=gen).permute(2, 1, 0)
+        u[c] = mf.empty_device(sh)
+        bc[c] = (mf.empty_device((sh[1] - 2, sh[2] - 2, 2)), mf.empty_device((sh[0] - 2, sh[2] - 2, 2)),
+                 mf.empty_device((sh[0] - 2, sh[1] - 2, 2)))
+        for b in bc[c]:
+            b.zero_()
+    return g, u, bc
+
+
+@pytest.mark.parametrize("sigma,bct,null", [(-1e3, (1,) * 6, 0), (0.0, (2,) * 6, 1)])
+def test_persistent_triangular_solves(mf, gpu, sigma, bct, null):
+    """The persistent triangular solves (one cooperative launch per triangle)
+    against the block-step form on an interface system large enough that
+    every CTA owns several 64-row blocks (2 x 2 x 2 slabs of 41 nodes,
+    18,252 unknowns): same interface values and fields to 1e-11, for one and
+    for three right-hand sides, velocity-like and pressure-like (null space)
+    operators; the device status stays clean."""
+    import torch
+    grids = tuple(slabs(2, 41) for _ in range(3))
+    dev = mf.MultiDomain((2, 2, 2), (0, 0, 0), *grids, bct)
+    dev.set_interface_solve(mf.MD_IFACE_LU)
+    dev.influence_matrix_set(sigma, null)
+    assert dev.ninf() > 152 * 64
+    g, u, bc = _random_solve(mf, dev, 11)
+    lam = {}
+    fields = {}
+    for form in (mf.MD_TRI_STEPS, mf.MD_TRI_PERSISTENT):
+        dev.set_triangular_form(form)
+        dev.solve(g, u, bc)
+        dev.device_status()
+        lam[form] = dev.interface()
+        fields[form] = {c: u[c].clone() for c in u}
+    assert max_rel(lam[mf.MD_TRI_PERSISTENT], lam[mf.MD_TRI_STEPS]) < 1e-11
+    for c in u:
+        a, b = fields[mf.MD_TRI_PERSISTENT][c], fields[mf.MD_TRI_STEPS][c]
+        assert float((a - b).abs().max() / b.abs().max()) < 1e-11
+    # several right-hand sides in one call (K = 3 in the persistent kernel)
+    sets = [_random_solve(mf, dev, 20 + q) for q in range(3)]
+    outs = {}
+    for form in (mf.MD_TRI_STEPS, mf.MD_TRI_PERSISTENT):
+        dev.set_triangular_form(form)
+        dev.solve_many([s[0] for s in sets], [s[1] for s in sets], [s[2] for s in sets])
+        dev.device_status()
+        outs[form] = [{c: s[1][c].clone() for c in s[1]} for s in sets]
+    for q in range(3):
+        for c in sets[q][1]:
+            a, b = outs[mf.MD_TRI_PERSISTENT][q][c], outs[mf.MD_TRI_STEPS][q][c]
+            assert float((a - b).abs().max() / b.abs().max()) < 1e-11
+    torch.cuda.synchronize()
