@@ -48,6 +48,9 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=2, help="oracle solves timed for cpu_baseline")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-rows", action="store_true", help="skip the measurements of the other rows")
+    ap.add_argument("--no-md-rows", action="store_true",
+                    help="skip the full-size multidomain rows (config 2 velocity operator and the "
+                         "128x129x128 periodic channel step: about two minutes of influence-matrix set-up)")
     ap.add_argument("--precision", default="auto", choices=["auto", "bf16", "tf32"],
                     help="transform format; auto times both and reports the faster")
     ap.add_argument("--probe", default=None,
@@ -58,9 +61,15 @@ def parse():
                          "at 160^3, a training step on 65,536 points, six Navier-Stokes steps at "
                          "128x129x128), and exit")
     ap.add_argument("--refine", type=int, default=1)
+    ap.add_argument("--tf32-plan", type=int, default=0, choices=[0, 1, 2],
+                    help="3xTF32 transform plan: 0 default, 1 64-column slices (matrix resident), "
+                         "2 128-column slices (matrix streamed)")
     ap.add_argument("--navier-config4", action="store_true",
                     help="time the NS step of the periodic (x, z) channel at 128x129x128 (two ~32k-unknown "
                          "influence matrices built first, minutes) and exit")
+    ap.add_argument("--les-config5", action="store_true",
+                    help="train the learned LES closure on a fine 257^3 box flow and judge it a posteriori "
+                         "against the plain model on the 65^3 LES grid, print the JSON and exit")
     ap.add_argument("--md-config2", action="store_true",
                     help="measure the 2x2x2 multidomain configuration at its full slab sizes "
                          "(seeded draw from {49, 65, 97}; ~3 minutes of influence-matrix set-up) and exit")
@@ -248,6 +257,7 @@ def run_gb300(args, rank, world, dist):
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     dev_stream = torch.cuda.current_stream()
+    mf.tc_tf32_plan(args.tf32_plan)
     grids, rhs, bcs = workload(args.nodes)
     n = args.nodes - 2
     sc = mf.SolverCoeffs3D(*grids, (1,) * 6, 6)
@@ -435,7 +445,7 @@ def run_gb300(args, rank, world, dist):
     # the other rows first: the CPU baseline leaves the host's BLAS threads
     # busy for a while, which would slow the host-side launches of the rows
     hbm, bf16, src = peaks()
-    rows = None if args.no_rows else row_measurements(mf, torch, hbm)
+    rows = None if args.no_rows else row_measurements(mf, torch, hbm, md_rows=not args.no_md_rows)
 
     # CPU baseline: the oracle restatement on the host cores, bounded sample
     cpu = None
@@ -568,7 +578,7 @@ def profile_traffic(name):
     return None
 
 
-def row_measurements(mf, torch, hbm):
+def row_measurements(mf, torch, hbm, md_rows=True):
     """Short event-timed measurements of the other rows of the path, each on
     the shapes of the reference's configurations (synthetic data)."""
     from oracle import mesh
@@ -749,6 +759,8 @@ def row_measurements(mf, torch, hbm):
         g = graph_of(four)
         row[key + "_graph_ms"] = time_fn(g.replay, reps=3) / 4
         del g
+        d = nav.step(diagnostics=True)
+        row[key + "_divergence"] = d["div"]
         nav.close()
     out["navier_step_128x129x128"] = row
     # the same step with the Smagorinsky LES term on the LES grid of the
@@ -761,11 +773,44 @@ def row_measurements(mf, torch, hbm):
             nav.set_field(var, lev, field((96, 97, 96), 120 + 4 * q + lev))
     for _ in range(4):
         nav.step()
-    out["navier_step_les_96x97x96"] = {"eager_ms": time_fn(nav.step, reps=8)}
+    out["navier_step_les_96x97x96"] = {"eager_ms": time_fn(nav.step, reps=8),
+                                       "divergence": nav.step(diagnostics=True)["div"]}
     nav.close()
+    # the same step with the learned coefficient (les_type 4): the eddy
+    # viscosity from the network (FP32 features and layers, 3xTF32 tcgen05
+    # hidden layer) inside the LES stage, Smagorinsky outside its training
+    # range; the network here is seeded, not trained (the a-posteriori run,
+    # --les-config5, trains it)
+    nav = mf.NavierStokes3D(*gl, ts=1e-3, reynolds=180.0, precision=mf.MF_PREC_3XTF32, refine=1,
+                            les_type=mf.MF_LES_LEARNED, les_c=0.17)
+    net = mf.Mlp(1)
+    lim = np.full(6, 3.0, np.float32)
+    net.set_scaling(np.zeros(6), np.ones(6), -lim, lim, 0.02, 1.0)
+    nav.set_les_network(net)
+    for lev in range(4):
+        for q, var in enumerate("uvw"):
+            nav.set_field(var, lev, field((96, 97, 96), 120 + 4 * q + lev))
+    for _ in range(4):
+        nav.step()
+    ms = time_fn(nav.step, reps=8)
+    out["navier_step_learned_les_96x97x96"] = {"eager_ms": ms, "steps_per_s": 1e3 / ms,
+                                               "divergence": nav.step(diagnostics=True)["div"]}
+    nav.close()
+    net.close()
     out["navier_step_channel_periodic_xz_64x65x64"] = navier_channel(mf, torch, 64, time_fn, field)
     out["navier_step_channel_periodic_xz_64x65x64"]["tf32_subdomain_solves"] = navier_channel(
         mf, torch, 64, time_fn, field, precision=mf.MF_PREC_3XTF32, refine=1)
+    if not md_rows:
+        return out
+    # the periodic channel at the config-4 size, 128 x 129 x 128: two
+    # influence matrices of ~32k unknowns (LU factors; the interface solves
+    # are the persistent triangular solves), 3xTF32 + 1 refinement subdomain
+    # solves
+    row = navier_channel(mf, torch, 128, time_fn, field, steps=4, precision=mf.MF_PREC_3XTF32, refine=1)
+    row["steps_per_s"] = 1e3 / row["eager_ms"]
+    out["navier_step_channel_periodic_xz_128x129x128"] = row
+    # config 2 at its full slab sizes, velocity operator
+    out["multidomain_2x2x2_config2"] = md_config2(mf, torch, operators=("velocity",))
     return out
 
 
@@ -814,24 +859,28 @@ def navier_channel(mf, torch, n, time_fn, field, steps=8, **kw):
     for _ in range(4):
         nav.step()
     ms = time_fn(nav.step, reps=steps)
+    d = nav.step(diagnostics=True)
     nav.close()
-    return {"setup_s": setup, "eager_ms": ms}
+    return {"setup_s": setup, "eager_ms": ms, "divergence": d["div"], "kinetic": d["kinetic"]}
 
 
-def run_md_config2(args):
+def md_config2(mf, torch, operators=("velocity", "pressure")):
     """2 x 2 x 2 subdomains with slab sizes drawn (seed 3) from {49, 65, 97},
-    tanh(1.0) slabs on [0, 1]^3: influence-matrix set-up and one solve for
-    the velocity operator (Dirichlet, sigma = -1e6) and the pressure operator
-    (Neumann, sigma = 0, null space), random right-hand sides."""
-    import torch
-    import mflops_gb300 as mf
+    tanh(1.0) slabs on [0, 1]^3: influence-matrix set-up and solves for the
+    velocity operator (Dirichlet, sigma = -1e6) and the pressure operator
+    (Neumann, sigma = 0, null space), random right-hand sides.  Per
+    operator: one right-hand side with the persistent triangular solves (the
+    default) and with one launch per block step, and three right-hand sides
+    in one call (the three velocity components of a time step)."""
     from oracle import mesh
     rng = np.random.default_rng(3)
     sizes = rng.choice([49, 65, 97], size=(3, 2))
     grids = [[mesh.tanh_grid(int(sizes[l][0]), 1.0, 0.0, 0.5), mesh.tanh_grid(int(sizes[l][1]), 1.0, 0.5, 1.0)]
              for l in range(3)]
     out = {"workload": "md_2x2x2_slabs_%s" % "_".join("%dx%d" % tuple(sz) for sz in sizes)}
-    for name, sigma, bct, null in (("velocity", -1e6, (1,) * 6, 0), ("pressure", 0.0, (2,) * 6, 1)):
+    ops = {"velocity": (-1e6, (1,) * 6, 0), "pressure": (0.0, (2,) * 6, 1)}
+    for name in operators:
+        sigma, bct, null = ops[name]
         md = mf.MultiDomain((2, 2, 2), (0, 0, 0), grids[0], grids[1], grids[2], bct, 6)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -839,25 +888,89 @@ def run_md_config2(args):
         torch.cuda.synchronize()
         setup = time.perf_counter() - t0
         gen = torch.Generator("cuda").manual_seed(4)
-        g, u, bc = {}, {}, {}
-        for c in md.subdomains():
-            sh = md.shape(*c)
-            g[c] = torch.randn(tuple(reversed(sh)), dtype=torch.float64, device="cuda",
-                               generator=gen).permute(2, 1, 0)
-            u[c] = mf.empty_device(sh)
-            bc[c] = (mf.empty_device((sh[1] - 2, sh[2] - 2, 2)), mf.empty_device((sh[0] - 2, sh[2] - 2, 2)),
-                     mf.empty_device((sh[0] - 2, sh[1] - 2, 2)))
-        md.solve(g, u, bc)
-        torch.cuda.synchronize()
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record()
-        for _ in range(5):
-            md.solve(g, u, bc)
-        b.record()
-        torch.cuda.synchronize()
-        out[name] = {"ninf": md.ninf(), "setup_s": setup, "solve_ms": a.elapsed_time(b) / 5}
+
+        def rhs():
+            g, u, bc = {}, {}, {}
+            for c in md.subdomains():
+                sh = md.shape(*c)
+                g[c] = torch.randn(tuple(reversed(sh)), dtype=torch.float64, device="cuda",
+                                   generator=gen).permute(2, 1, 0)
+                u[c] = mf.empty_device(sh)
+                bc[c] = tuple(torch.zeros(shp, dtype=torch.float64, device="cuda").permute(2, 1, 0)
+                              for shp in ((2, sh[2] - 2, sh[1] - 2), (2, sh[2] - 2, sh[0] - 2),
+                                          (2, sh[1] - 2, sh[0] - 2)))
+            return g, u, bc
+
+        g, u, bc = rhs()
+        row = {"ninf": md.ninf(), "setup_s": setup}
+
+        def timed(fn, reps):
+            fn()
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            for _ in range(reps):
+                fn()
+            b.record()
+            torch.cuda.synchronize()
+            return a.elapsed_time(b) / reps
+
+        for key, form in (("solve_ms", mf.MD_TRI_PERSISTENT), ("solve_ms_block_steps", mf.MD_TRI_STEPS)):
+            md.set_triangular_form(form)
+            row[key] = timed(lambda: md.solve(g, u, bc), 5 if form == mf.MD_TRI_PERSISTENT else 2)
+        md.set_triangular_form(mf.MD_TRI_PERSISTENT)
+        sets = [rhs() for _ in range(3)]
+        row["solve_many_3_ms"] = timed(lambda: md.solve_many([s_[0] for s_ in sets], [s_[1] for s_ in sets],
+                                                             [s_[2] for s_ in sets]), 3)
+        md.device_status()
+        row["interface_bytes_per_solve"] = 16.0 * md.ninf() ** 2 / 2.0  # L and U read once
+        out[name] = row
         md.close()
-    print(json.dumps(out), flush=True)
+        del g, u, bc, sets
+    return out
+
+
+def les_a_posteriori(mf, torch, nf=257, nc=65, nu=1e-3, seed_train=1, seed_test=2):
+    """The learned LES closure end to end at the config-5 ratio of grids
+    (fine nf^3 to LES nc^3, 4:1 like 384 -> 96): a decaying no-slip box flow
+    on the fine grid (FP64 fields, 3xTF32 + 2 FP64-refinement projections),
+    training pairs filtered to the LES grid, the network trained by the
+    library's kernels; then LES runs of the time step (les_type 0, 1 with the
+    best constant, 4 with the network) from the filtered held-out flow,
+    compared with the filtered fine run (mean kinetic-energy profile along y,
+    spectrum along x)."""
+    from mflops_gb300 import learn
+    t0 = time.perf_counter()
+    k0 = 30.0 * (nf - 1) / 96.0
+    fl = learn.BoxFlow(nf, nu, seed=seed_train, k0=k0, precision=mf.MF_PREC_3XTF32, refine=2)
+    pm = learn.PairMaker(fl.grid, nc, margin=3)
+    parts = []
+    fl.run(400, every=50, callback=lambda f, it: parts.append(pm.pairs(f.u)) if it >= 300 else None)
+    X, b, t = [torch.cat([p_[q] for p_ in parts]) for q in range(3)]
+    del parts
+    net = mf.Mlp(0)
+    sc, hist = learn.fit(net, X, b, t, steps=2000, batch=8192, lr=2e-3, log_every=1000)
+    t_train = time.perf_counter() - t0
+    del fl, X, b, t
+    fl = learn.BoxFlow(nf, nu, seed=seed_test, k0=k0, precision=mf.MF_PREC_3XTF32, refine=2)
+    fl.run(300, every=50)
+    ap = learn.APosteriori(fl, pm, net, sc)
+    res = ap.run(100 * fl.cfl_dt(0.3), checkpoints=4)
+    names = {0: "no_model", 1: "smagorinsky_best_constant", 4: "learned"}
+    out = {"grids": "fine %d^3 -> LES %d^3, no-slip box, nu %g" % (nf, nc, nu), "c0": sc["c0"],
+           "train_s": t_train, "total_s": time.perf_counter() - t0, "dt_les": res["dt_les"]}
+    for m, key in names.items():
+        r = res[m]
+        out[key] = {"profile_error": r["profile_error_mean"], "spectrum_error": r["spectrum_error_mean"],
+                    "step_ms": r["step_ms"], "divergence": r["divergence"]}
+    net.close()
+    return out
+
+
+def run_md_config2(args):
+    import torch
+    import mflops_gb300 as mf
+    print(json.dumps(md_config2(mf, torch)), flush=True)
 
 
 def run_row_probe(args):
@@ -958,6 +1071,7 @@ def run_probe(args):
     import mflops_gb300 as mf
     if args.probe not in ("bf16", "tf32", "fp64"):
         return run_row_probe(args)
+    mf.tc_tf32_plan(args.tf32_plan)
     grids, rhs, bcs = workload(args.nodes)
     n = args.nodes - 2
     sc = mf.SolverCoeffs3D(*grids, (1,) * 6, 6)
@@ -979,6 +1093,11 @@ def main():
         return
     if args.md_config2:
         run_md_config2(args)
+        return
+    if args.les_config5:
+        import torch
+        import mflops_gb300 as mf
+        print(json.dumps({"learned_les_a_posteriori": les_a_posteriori(mf, torch)}), flush=True)
         return
     if args.navier_config4:
         import torch

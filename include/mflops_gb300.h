@@ -65,6 +65,14 @@ int mf_tune_entries(void);
 int mf_tune_clear(void);
 int mf_tune_save(const char* path);
 int mf_tune_load(const char* path);
+/* Slice width of the 3xTF32 tensor-core transform (no reference
+ * counterpart): 0 the default (128-column slices with the matrix streamed
+ * through the TMA ring wherever the padded axis is a multiple of 128, or,
+ * with mf_tune_set(1), the faster plan measured per shape), 1 64-column
+ * slices with the matrix resident in shared memory, 2 128-column slices
+ * where possible.  Both plans give identical results.  Process-wide. */
+int mf_tc_tf32_plan_set(int plan);
+int mf_tc_tf32_plan_get(void);
 int mf_version(void);
 /* 1 when a CUDA device is usable from this process, else 0. */
 int mf_device_available(void);
@@ -353,6 +361,18 @@ int mf_md_solve_many(mf_md_t* md, int nrhs, const double* const* g, double* cons
  * (2 n^3 FP64 flops at set-up, then one n^2 read per solve; for long runs). */
 #define MF_MD_IFACE_INVERSE 2
 int mf_md_set_interface_solve(mf_md_t* md, int mode);
+/* Form of the triangular solves on the LU factors (no reference
+ * counterpart): MF_MD_TRI_PERSISTENT (default) one cooperative launch per
+ * triangle, CTAs advancing through 64-row blocks behind release/acquire
+ * flags (every wait bounded; mf_md_device_status reports an expired one);
+ * MF_MD_TRI_STEPS one launch per 128-row block step.  Used also when the
+ * persistent form cannot be launched. */
+#define MF_MD_TRI_PERSISTENT 0
+#define MF_MD_TRI_STEPS 1
+int mf_md_set_triangular_form(mf_md_t* md, int form);
+/* Synchronises and returns MF_ERR_TIMEOUT if a persistent triangular solve
+ * gave up waiting (the results of that solve are then not valid). */
+int mf_md_device_status(const mf_md_t* md);
 /* Precision of the subdomain solves inside mf_md_solve (MF_PREC_FP64, the
  * default, or a mixed mode with `refine` steps); the influence matrix is
  * FP64 either way. */
@@ -542,7 +562,7 @@ int mf_flow_curl(int nx, int ny, int nz, const double* const* dpsi, double* cons
  * extrapolation (:2010-2050), slot rotation and the driver's diagnostics
  * (navier3d.f90:120-261) and the LES term (navier_LES :1225-1455, f :1083-1099).
  * Covered: one domain and the multidomain branch (mf_navier_create_md), mapt = 0, pressure types 1 to 4,
- * les_type 0..3, nsubite sub-iterations with the driver's convergence test
+ * les_type 0..4, nsubite sub-iterations with the driver's convergence test
  * (testconv, navier3d.f90:366-412).  Velocity Dirichlet and
  * pressure Neumann on all faces; boundary values and sources from the
  * reference's exact solution `sol` (:927-1041, steady: wt = 0).  Fields are
@@ -562,7 +582,7 @@ typedef struct {
   int nmodes;         /* modes of the exact solution (5 in the reference) */
   int precision;      /* solves: MF_PREC_FP64 (the reference's arithmetic) or a mixed mode */
   int refine;         /* refinement steps of the mixed solves, < 0: default */
-  int les_type;       /* 0 none, 1 Smagorinsky, 2 WALE, 3 sigma (default 0) */
+  int les_type;       /* 0 none, 1 Smagorinsky, 2 WALE, 3 sigma (default 0), 4 learned (MF_LES_LEARNED) */
   double les_c;       /* cmd%les_c; the model coefficient is its square (default 0) */
   int nsubite;        /* sub-iterations per time step (default 1) */
   const char* md_cache_dir;  /* several subdomains: directory of the influence-matrix factor cache, or NULL */
@@ -609,6 +629,14 @@ int mf_navier_get_field(mf_navier_t* nav, int var, int level, double* f, void* s
 int mf_navier_step(mf_navier_t* nav, double* diag, void* stream);
 /* Simulated time and the flow-rate state (debit, g; 0 before the first step). */
 int mf_navier_state(mf_navier_t* nav, double* time, double* debit, double* g);
+/* les_type 4 (MF_LES_LEARNED, no reference counterpart): the eddy viscosity
+ * of navier_LES comes from the learned coefficient, nu = C(x) Delta^2
+ * sqrt(2 S:S) with C from the network (mf_les_nu_mlp, on the same nine
+ * gradients the LES stage computes), and from Smagorinsky with les_c^2
+ * wherever the features leave the network's training range.  The network
+ * stays owned by the caller and must outlive the steps that use it. */
+#define MF_LES_LEARNED 4
+int mf_navier_set_les_network(mf_navier_t* nav, const mf_mlp_t* mlp);
 /* Sub-iterations made by the last step (1 when nsubite = 1; with nsubite > 1
  * the step stops when testconv passes, which synchronises the host once per
  * sub-iteration). */

@@ -1197,6 +1197,78 @@ __global__ void k_fold_split(const double* __restrict__ rhs, FoldArgsF a, __nv_b
 }
 
 // c * bc face products of the fold, in FP32: out[c][face point].
+// The same fold with kFoldJ rows j per thread: grid x over i (128-thread
+// blocks), y over groups of kFoldJ rows, z strides over k.  The y-face
+// products of (i, k) are loaded once and used for the thread's kFoldJ rows
+// (the one-row form re-reads them for every j, ~250 MB of L2 traffic at
+// 257^3), the z-face products of (i, j) and the y-rows of inv_lhs stay in
+// registers for the whole k loop.  Same operations in the same order per
+// point as k_fold_split, so the results are identical.
+constexpr int kFoldJ = 8;
+constexpr int kFoldKz = 16;
+__global__ void __launch_bounds__(128) k_fold_split_rows(const double* __restrict__ rhs, FoldArgsF a,
+                                                         __nv_bfloat16* hi, __nv_bfloat16* lo, float* x32,
+                                                         int n1, int n2, int n3, int P1, int P2, int P3) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, j0 = blockIdx.y * kFoldJ;
+  if (i >= P1) return;
+  const bool in_i = i < n1;
+  const long long sx = (long long)n2 * n3, sy = (long long)n1 * n3, sz = (long long)n1 * n2;
+  float cx[4] = {0.f, 0.f, 0.f, 0.f}, cy[kFoldJ][4], fz[kFoldJ][4];
+  if (in_i)
+#pragma unroll
+    for (int c = 0; c < 4; ++c) cx[c] = a.ix[c][i];
+#pragma unroll
+  for (int jj = 0; jj < kFoldJ; ++jj) {
+    const int j = j0 + jj;
+    const bool ok = in_i && j < n2;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      cy[jj][c] = ok ? a.iy[c][j] : 0.f;
+      fz[jj][c] = ok ? a.bz[c * sz + i + (long long)n1 * j] : 0.f;
+    }
+  }
+  for (int k = blockIdx.z; k < P3; k += gridDim.z) {
+    const bool in_k = in_i && k < n3;
+    float by[4] = {0.f, 0.f, 0.f, 0.f}, iz[4] = {0.f, 0.f, 0.f, 0.f};
+    double r[kFoldJ];
+    if (in_k) {
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        by[c] = a.by[c * sy + i + (long long)n1 * k];
+        iz[c] = a.iz[c][k];
+      }
+    }
+#pragma unroll
+    for (int jj = 0; jj < kFoldJ; ++jj) {
+      const int j = j0 + jj;
+      r[jj] = (in_k && j < n2) ? rhs[i + (long long)n1 * (j + (long long)n2 * k)] : 0.0;
+    }
+#pragma unroll
+    for (int jj = 0; jj < kFoldJ; ++jj) {
+      const int j = j0 + jj;
+      float v = 0.f;
+      if (in_k && j < n2) {
+        v = narrow(r[jj]);
+        const long long fx = j + (long long)n2 * k;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          v -= cx[c] * a.bx[c * sx + fx];
+          v -= cy[jj][c] * by[c];
+          v -= iz[c] * fz[jj][c];
+        }
+      }
+      const long long idx = i + (long long)P1 * (j + (long long)P2 * k);
+      if (x32) {
+        x32[idx] = v;
+      } else {
+        const __nv_bfloat16 h = __float2bfloat16_rn(v);
+        hi[idx] = h;
+        lo[idx] = __float2bfloat16_rn(v - __bfloat162float(h));
+      }
+    }
+  }
+}
+
 __global__ void k_fold_faces(const double* __restrict__ bc, double4 cc, float* out, long long nf) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nf) return;
@@ -1780,8 +1852,28 @@ static int mixed_prepare(mf_solver3d* sc, bool tf32, cudaStream_t st) {
 }
 
 static int tc_run(mf_solver3d* sc, bool tf32, int t, const TcEpilogue& e, cudaStream_t st) {
+  const TcPlan* p = (tf32 ? sc->plan32 : sc->plan)[t];
+  int plan = 0;
+  // 3xTF32 slice width: the process setting, or with the tuner on the
+  // measured choice for this shape.  The two plans give identical results;
+  // only epilogues that store (not the accumulating update) are repeated
+  // for timing.
+  if (tf32 && tc_has_wide(p) && tc_get_tf32_plan() == 0 && tune_mode() == 1 &&
+      (e.kind != 2 || !e.accumulate)) {
+    const int axis = t % 3, M = (axis == 0 ? sc->P[1] * sc->P[2] : axis == 1 ? sc->P[2] * sc->P[0]
+                                                                             : sc->P[0] * sc->P[1]);
+    const int N = sc->ax[axis].P;
+    int c = tune_lookup(kTuneTcTf32, M, N, N, 0);
+    if (c < 0 && !stream_capturing(st)) {
+      c = tune_measure(st, 2, [&](int v) {
+        return tc_transform(p, e, sc->err.as<int>(), st, v ? 2 : 1) == MF_OK ? 0 : 1;
+      });
+      if (c >= 0) tune_store(kTuneTcTf32, M, N, N, 0, c);
+    }
+    if (c >= 0) plan = c ? 2 : 1;
+  }
   sc->prof.begin(e.kind == 0 ? kProfTc : e.kind == 1 ? kProfTcDivide : kProfTcUpdate, st);
-  int rc = tc_transform((tf32 ? sc->plan32 : sc->plan)[t], e, sc->err.as<int>(), st);
+  int rc = tc_transform(p, e, sc->err.as<int>(), st, plan);
   sc->prof.end(st);
   return rc;
 }
@@ -1859,7 +1951,7 @@ static int fold_split(mf_solver3d* sc, bool tf32, const double* rhs, const doubl
   args.bx = fa[0];
   args.by = fa[1];
   args.bz = fa[2];
-  k_fold_split<<<dim3(blocks_for(sc->P[0], 256), sc->P[1], 4), 256, 0, st>>>(
+  k_fold_split_rows<<<dim3(blocks_for(sc->P[0], 128), sc->P[1] / kFoldJ, kFoldKz), 128, 0, st>>>(
       rhs, args, tf32 ? nullptr : sc->Xa_hi.as<__nv_bfloat16>(),
       tf32 ? nullptr : sc->Xa_lo.as<__nv_bfloat16>(), tf32 ? sc->Xa32.as<float>() : nullptr,
       (int)n1, (int)n2, (int)n3, sc->P[0], sc->P[1], sc->P[2]);

@@ -40,6 +40,14 @@ struct TcPlan;  // opaque: tensor maps for one transform
 int tc_plan_create(TcPlan** plan, bool tf32, const void* x_hi, const void* x_lo, const void* b_hi,
                    const void* b_lo, int M, int N, int K);
 void tc_plan_destroy(TcPlan* plan);
-int tc_transform(const TcPlan* plan, const TcEpilogue& epi, int* dev_err, cudaStream_t st);
+// plan: 0 the process default (tc_set_tf32_plan), 1 / 2 as below.
+int tc_transform(const TcPlan* plan, const TcEpilogue& epi, int* dev_err, cudaStream_t st,
+                 int tf32_plan = 0);
+// The 128-column 3xTF32 plan exists for this transform (N % 128 == 0).
+bool tc_has_wide(const TcPlan* plan);
+// 3xTF32 plan: 0 default, 1 64-column slices (B resident), 2 128-column
+// slices (B streamed) where N % 128 == 0.  Process-wide.
+void tc_set_tf32_plan(int plan);
+int tc_get_tf32_plan();
 
 }  // namespace mf

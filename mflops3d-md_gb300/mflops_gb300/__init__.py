@@ -42,6 +42,7 @@ MF_ERR_ALLOC = 7
 MF_ERR_UNSUPPORTED = 8
 
 MF_PREC_FP64 = 0
+MF_LES_LEARNED = 4
 MF_PREC_SPLIT_BF16 = 1
 MF_PREC_3XTF32 = 2
 MF_RESID_FF = 0
@@ -50,6 +51,8 @@ MF_RESID_FP64_LINE = 2
 MD_IFACE_AUTO = 0
 MD_IFACE_LU = 1
 MD_IFACE_INVERSE = 2
+MD_TRI_PERSISTENT = 0
+MD_TRI_STEPS = 1
 MD_ASSEMBLY_EIGEN = 0
 MD_ASSEMBLY_SOLVES = 1
 
@@ -88,6 +91,8 @@ _PROTOS = {
     "mf_pentalu": [_I, _DP],
     "mf_solver_axis_setup": [_DP, _I, _IP, _I, _DP, _DP, _DP, _DP, _DP, _DP, _DP],
     "mf_grid1d": [_I, _I, _D, _D, _D, _DP],
+    "mf_tc_tf32_plan_set": [_I],
+    "mf_tc_tf32_plan_get": [],
     "mf_grid_spacing": [_I, _DP, _DP],
     "mf_mesh_grid_init": [ctypes.c_char, _I, _I, _I, _I, _D, _DP, _DP],
     "mf_der_coeffs_init": [_DP, _I, _I, _I, ctypes.POINTER(_P)],
@@ -185,6 +190,9 @@ _PROTOS = {
     "mf_navier_step": [_P, _DP, _P],
     "mf_navier_state": [_P, _DP, _DP, _DP],
     "mf_navier_subiterations": [_P, _IP],
+    "mf_navier_set_les_network": [_P, _P],
+    "mf_md_set_triangular_form": [_P, _I],
+    "mf_md_device_status": [_P],
     "mf_navier_create_md": [_IP, _IP, ctypes.POINTER(_DP), _IP, ctypes.POINTER(_DP), _IP, ctypes.POINTER(_DP), _IP,
                             _P, ctypes.POINTER(_P)],
     "mf_navier_subdomains": [_P, _IP],
@@ -248,6 +256,14 @@ def pentalu(dl):
     a = np.asfortranarray(np.array(dl, dtype=np.float64))
     _check(_lib.mf_pentalu(a.shape[0], a.ctypes.data_as(_DP)))
     return a
+
+
+def tc_tf32_plan(plan=None):
+    """Get (and with an argument set) the 3xTF32 transform plan: 0 default,
+    1 64-column slices (matrix resident), 2 128-column slices (streamed)."""
+    if plan is not None:
+        _check(_lib.mf_tc_tf32_plan_set(int(plan)))
+    return _lib.mf_tc_tf32_plan_get()
 
 
 MF_GRID_UNIFORM = 0
@@ -669,6 +685,16 @@ class MultiDomain:
         """MD_IFACE_AUTO (inverse when small enough), MD_IFACE_LU or
         MD_IFACE_INVERSE (the inverse at any size that fits)."""
         _check(_lib.mf_md_set_interface_solve(self._h, int(mode)))
+
+    def set_triangular_form(self, form):
+        """MD_TRI_PERSISTENT (default: one cooperative launch per triangle)
+        or MD_TRI_STEPS (one launch per block step) for the LU solves."""
+        _check(_lib.mf_md_set_triangular_form(self._h, int(form)))
+
+    def device_status(self):
+        """Raises MflopsError (MF_ERR_TIMEOUT) if a persistent triangular
+        solve gave up waiting."""
+        _check(_lib.mf_md_device_status(self._h))
 
     def interface(self):
         lam = np.zeros(self.ninf())
@@ -1103,6 +1129,13 @@ class NavierStokes3D:
 
     def load(self, path, stream=None):
         _check(_lib.mf_navier_load(self._h, str(path).encode(), _stream(stream)))
+
+    def set_les_network(self, mlp):
+        """les_type 4: the network (an Mlp with its scaling set) whose
+        coefficient gives the eddy viscosity; Smagorinsky with les_c^2 where
+        the features leave its training range.  The step keeps a reference."""
+        _check(_lib.mf_navier_set_les_network(self._h, mlp._h))
+        self._les_mlp = mlp
 
     def subiterations(self):
         """Sub-iterations made by the last step."""
