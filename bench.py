@@ -501,9 +501,14 @@ def run_gb300(args, rank, world, dist):
         achieved = algo_flops / (tc_ms / tc_n * 1e-3) / 1e12
         # TF32 runs at half the BF16 tensor rate on this part (nominal ratio)
         peak = bf16 if best == "bf16" else bf16 / 2.0
-        roof = {"kernel": "k_tc_transform", "bound": "tensor", "achieved": achieved, "peak": peak,
+        # the 3xTF32 transform runs as k_tc_tf32_wide (128-column slices) when
+        # the padded axis is a multiple of 128 and the plan is not forced narrow
+        wide = best == "tf32" and mf.tc_tf32_plan() != 1 and (n + 63) // 64 * 64 % 128 == 0
+        kname = "k_tc_tf32_wide" if wide else "k_tc_transform"
+        roof = {"kernel": kname, "bound": "tensor", "achieved": achieved, "peak": peak,
                 "unit": "TFLOP/s", "frac": achieved / peak,
-                "traffic": profile_traffic("k_tc_transform_%s_257cube.md" % best),
+                "traffic": profile_traffic("k_tc_tf32_wide_257cube.md" if wide else
+                                           "k_tc_transform_%s_257cube.md" % best),
                 "traffic_source": "ncu dram__bytes_read+write of one launch, profiles/",
                 "peak_source": src + (" bf16 burst" if best == "bf16" else " bf16 burst / 2 (tf32)"),
                 "algorithmic_per_launch": algo_flops}
@@ -533,6 +538,9 @@ def run_gb300(args, rank, world, dist):
                    "precision": names[best] + " + FP64 residual refinement",
                    "refine_steps": refine, "l2": "256 MiB flush between steps, per-step CUDA events",
                    "launch": "one CUDA-graph replay of the captured solve per step",
+                   "tf32_plan": {0: "default (128-column slices where the padded axis allows)",
+                                 1: "64-column slices, matrix resident",
+                                 2: "128-column slices, matrix streamed"}[mf.tc_tf32_plan()],
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "eager_ms_per_step": sum(eager_ms) / args.steps,
         "residual_double_fp32_sweeps": resid_ff,

@@ -469,12 +469,16 @@ __global__ void __launch_bounds__(Cfg<kTf32>::kThreads, 1)
 // FP32 X tile (16 KB) and both B planes of the same 32 K values (2 x 16 KB);
 // B is 512 KB in all and stays in L2.  TMEM: the three accumulators of one
 // tile (h1 = hi*hi over the first half of K, h2 = over the second half,
-// s = hi*lo + lo*hi; 3 x 128 columns) and four A operand slots of 16 K
-// values (4 x 32 columns).  The accumulators are single-buffered: the next
-// tile's first MMAs wait until the epilogue warps have read s and h1, its
-// second half until they have read h2; the stores follow.  The epilogue
-// sums (s + h1) + h2 in the same order as the narrow form, so both forms
-// give identical results.
+// s = hi*lo + lo*hi; 3 x 128 columns) and eight slots for the lo part of
+// the A operand (8 x 16 columns).  The hi part is the landed FP32 tile
+// itself (the tensor core reads FP32 as TF32 by ignoring the low mantissa
+// bits), so the hi*hi and hi*lo MMAs take A from shared memory and the
+// converter warps only form and store lo.  The accumulators are
+// single-buffered: the next tile's first MMAs wait until the epilogue warps
+// have read s and h1, its second half until they have read h2; the stores
+// follow.  Each output sums the same products in the same accumulators as
+// the narrow form and the epilogue adds (s + h1) + h2 in the same order,
+// so both forms give identical results.
 constexpr int kWideNW = 128;
 constexpr int kWideStages = 4;
 constexpr int kWideEpiWarps = 8;
@@ -484,10 +488,10 @@ constexpr uint32_t kWideTile = kBlockM * 128;          // 16 KB: 128 rows x 32 F
 constexpr uint32_t kWideStage = 3 * kWideTile;          // X tile + B hi + B lo
 constexpr uint32_t kWideSmem = kWideStages * kWideStage + 1024;
 constexpr uint32_t kWideH1 = 0, kWideH2 = 128, kWideS = 256, kWideSlot = 384;
-// four operand slots of 16 K values (hi at +0, lo at +16): the converters
-// may run three half-stages ahead of the MMAs
-constexpr int kWideSlots = 4;
-constexpr uint32_t kWideSlotCols = 32;
+// eight operand slots of the lo parts of 16 K values: the converters may
+// run seven half-stages ahead of the MMAs
+constexpr int kWideSlots = 8;
+constexpr uint32_t kWideSlotCols = 16;
 
 __global__ void __launch_bounds__(kWideThreads, 1)
     k_tc_tf32_wide(const __grid_constant__ CUtensorMap tx, const __grid_constant__ CUtensorMap tb_hi,
@@ -574,6 +578,7 @@ __global__ void __launch_bounds__(kWideThreads, 1)
   } else if (warp == 1) {
     if (lane == 0) {
       const uint32_t idesc = instr_desc(kBlockM, kWideNW, true);
+      const uint64_t a0 = smem_desc(smem_u32(smem));
       const uint64_t b0 = smem_desc(smem_u32(smem + kWideTile));
       const uint32_t stage_step = kWideStage >> 4, lo_off = kWideTile >> 4;
       int s = 0, o = 0, tc = 0;
@@ -591,19 +596,21 @@ __global__ void __launch_bounds__(kWideThreads, 1)
           }
           if (!(ok = mbar_wait(&full_bar[s], ph, err))) break;
           const uint64_t bh = b0 + (uint64_t)(s * stage_step), bl = bh + lo_off;
+          const uint64_t ah = a0 + (uint64_t)(s * stage_step);
           const uint32_t dh = tmem + (c < half ? kWideH1 : kWideH2), ds = tmem + kWideS;
           const uint32_t acc_h = (c == 0 || c == half) ? 0u : 1u, acc_s = c == 0 ? 0u : 1u;
           // two half-stages of 16 K values, each in its own operand slot
           for (int hs = 0; hs < 2 && ok; ++hs) {
             if (!(ok = mbar_wait(&cvt_bar[o], pho, err))) break;
             fence_after();
-            const uint32_t ahi = tmem + kWideSlot + (uint32_t)(kWideSlotCols * o), alo = ahi + 16;
+            const uint32_t alo = tmem + kWideSlot + (uint32_t)(kWideSlotCols * o);
 #pragma unroll
             for (int kk = 0; kk < 2; ++kk) {
               const int k8 = 2 * hs + kk;
               const bool lead = hs == 0 && kk == 0;  // first K step of this chunk
-              mma_tf32_ta(dh, ahi + 8 * kk, bh + 2 * k8, idesc, lead ? acc_h : 1u);
-              mma_tf32_ta(ds, ahi + 8 * kk, bl + 2 * k8, idesc, lead ? acc_s : 1u);
+              // hi: the landed FP32 tile itself, read as TF32 by the tensor core
+              mma<true>(dh, ah + 2 * k8, bh + 2 * k8, idesc, lead ? acc_h : 1u);
+              mma<true>(ds, ah + 2 * k8, bl + 2 * k8, idesc, lead ? acc_s : 1u);
               mma_tf32_ta(ds, alo + 8 * kk, bh + 2 * k8, idesc, 1u);
             }
             mma_commit(&op_free[o]);
@@ -704,8 +711,7 @@ __global__ void __launch_bounds__(kWideThreads, 1)
         for (int hs = 0; hs < 2; ++hs) {
           if (ih >= kWideSlots && !(ok = mbar_wait(&op_free[o], pho ^ 1u, err, 32))) break;
           const uint32_t slot = tmem + lane_base + kWideSlot + (uint32_t)(kWideSlotCols * o);
-          tmem_store16(slot, hi + 16 * hs);
-          tmem_store16(slot + 16, lo + 16 * hs);
+          tmem_store16(slot, lo + 16 * hs);
           fence_before();
           mbar_arrive(&cvt_bar[o]);
           ++ih;
