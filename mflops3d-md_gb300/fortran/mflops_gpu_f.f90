@@ -62,6 +62,14 @@ module mflops_gpu_f
   public :: solver_coeffs_init_3d, solve_3d, solve_3d_mixed, solver_3d, solver_destroy
   public :: navier_defaults, navier_initialization_gpu, navier_set_field, navier_get_field
   public :: navier_step, navier_destroy
+  public :: les_network_init, les_network_destroy, navier_set_les_network
+  integer(c_int), parameter, public :: MF_LES_LEARNED = 4
+
+  ! learned LES coefficient network (les_type 4): parameters and scaling
+  ! come from training (mflops_gb300.learn) and are loaded here
+  type, public :: les_network
+     type(c_ptr) :: h = c_null_ptr
+  end type les_network
   public :: mesh_grid_init
   integer(c_int), parameter, public :: MF_GRID_UNIFORM = 0, MF_GRID_ARCSIN = 1, MF_GRID_TANH = 2
 
@@ -207,6 +215,41 @@ module mflops_gpu_f
        integer(c_int) :: rc
      end function c_navier_step
 
+     function c_mlp_create(seed, mlp) bind(C, name="mf_mlp_create") result(rc)
+       import :: c_int, c_long_long, c_ptr
+       integer(c_long_long), value :: seed
+       type(c_ptr), intent(out) :: mlp
+       integer(c_int) :: rc
+     end function c_mlp_create
+
+     function c_mlp_destroy(mlp) bind(C, name="mf_mlp_destroy") result(rc)
+       import :: c_int, c_ptr
+       type(c_ptr), value :: mlp
+       integer(c_int) :: rc
+     end function c_mlp_destroy
+
+     function c_mlp_set_params(mlp, params) bind(C, name="mf_mlp_set_params") result(rc)
+       import :: c_int, c_ptr, c_float
+       type(c_ptr), value :: mlp
+       real(c_float), intent(in) :: params(*)
+       integer(c_int) :: rc
+     end function c_mlp_set_params
+
+     function c_mlp_set_scaling(mlp, mean, istd, lo, hi, cscale, loss_scale) &
+          bind(C, name="mf_mlp_set_scaling") result(rc)
+       import :: c_int, c_ptr, c_float
+       type(c_ptr), value :: mlp
+       real(c_float), intent(in) :: mean(*), istd(*), lo(*), hi(*)
+       real(c_float), value :: cscale, loss_scale
+       integer(c_int) :: rc
+     end function c_mlp_set_scaling
+
+     function c_navier_set_les_network(nav, mlp) bind(C, name="mf_navier_set_les_network") result(rc)
+       import :: c_int, c_ptr
+       type(c_ptr), value :: nav, mlp
+       integer(c_int) :: rc
+     end function c_navier_set_les_network
+
      function c_mesh_grid_init(choice, n, dom_coord, ndomains, kind, param, grid1d, dgrid1d) &
           bind(C, name="mf_mesh_grid_init") result(rc)
        import :: c_char, c_int, c_double
@@ -236,6 +279,32 @@ contains
     print '(a,a,a)', where, ': ', trim(text)
     stop
   end subroutine check
+
+  ! ------------------------------------------------- learned LES coefficient
+  ! A network of the learned eddy-viscosity coefficient: params(4673) and the
+  ! six-feature scaling as written by the training (mflops_gb300.learn).
+  subroutine les_network_init(net, params, mean, istd, lo, hi, cscale)
+    type(les_network), intent(out) :: net
+    real(c_float), intent(in) :: params(4673), mean(6), istd(6), lo(6), hi(6)
+    real(c_float), intent(in) :: cscale
+    call check(c_mlp_create(0_c_long_long, net%h), 'les_network_init')
+    call check(c_mlp_set_params(net%h, params), 'les_network_init')
+    call check(c_mlp_set_scaling(net%h, mean, istd, lo, hi, cscale, 1.0_c_float), 'les_network_init')
+  end subroutine les_network_init
+
+  subroutine les_network_destroy(net)
+    type(les_network), intent(inout) :: net
+    if (c_associated(net%h)) call check(c_mlp_destroy(net%h), 'les_network_destroy')
+    net%h = c_null_ptr
+  end subroutine les_network_destroy
+
+  ! les_type 4: the step's eddy viscosity from the network (Smagorinsky with
+  ! les_c**2 outside its training range); net must outlive the steps.
+  subroutine navier_set_les_network(nav, net)
+    type(navier3d_gpu), intent(in) :: nav
+    type(les_network), intent(in) :: net
+    call check(c_navier_set_les_network(nav%h, net%h), 'navier_set_les_network')
+  end subroutine navier_set_les_network
 
   ! ---------------------------------------------------------------- grids
   ! mesh_grid_init (class_mesh.f90:113-339) on plain arrays: grid1d(n) and
