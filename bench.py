@@ -34,6 +34,10 @@ for _p in (ROOT, PKG):
     if _p not in sys.path:
         sys.path.insert(0, _p)
 
+# FP64 FMA/multiply instructions per second of a GB300 (1.19 TFLOP/s with
+# FMA counted as two flops, measured with a DFMA loop on this pool's parts;
+# MEASURED_PEAKS.json carries no FP64 figure)
+FP64_INSTR_PER_S = 0.595e12
 METRIC = "257^3 Poisson solves/s: split-precision+refinement vs FP64 plain @1e-10 rel err"
 UNIT = "solves/s"
 
@@ -615,10 +619,16 @@ def row_measurements(mf, torch, hbm, md_rows=True):
     dc = mf.DerivativesCoefficients(g, so=6)
     f = field((n, n, n), 11)
     df = mf.empty_device((n, n, n))
+    # the sweeps are bound by the FP64 pipe, not HBM: 7 FP64 instructions
+    # per point with the tridiagonal rows of the order-6 scheme (forward: one
+    # multiply and four FMAs of the explicit stencil, one FMA of the
+    # elimination; back: one FMA), against the part's FP64 rate
     for name, axis, order in (("derx", 0, 1), ("dery", 1, 1), ("derz", 2, 1), ("dderx", 0, 2)):
         ms = time_fn(lambda: dc.apply(axis, order, f, out=df))
         gbs = 16.0 * n ** 3 / (ms * 1e-3) / 1e9
-        out["derivative_%s_257cube" % name] = {"ms": ms, "GB_per_s": gbs, "frac_of_hbm": gbs / hbm}
+        fp64 = 7.0 * n ** 3 / (ms * 1e-3)
+        out["derivative_%s_257cube" % name] = {"ms": ms, "GB_per_s": gbs, "frac_of_hbm": gbs / hbm,
+                                               "fp64_instr_per_s": fp64, "frac_of_fp64_pipe": fp64 / FP64_INSTR_PER_S}
     del f, df
     # configuration 1: 65^3, tanh(1.5) on all axes, Dirichlet, so = 6
     n = 65
