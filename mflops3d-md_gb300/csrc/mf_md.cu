@@ -487,7 +487,6 @@ __global__ void __launch_bounds__(kPThreads) k_tri_persist(const double* __restr
   double (*cur)[kPb] = reinterpret_cast<double (*)[kPb]>(sm + (size_t)2 * owned * K * kPb);  // [K]
   double (*nxt)[kPb] = cur + K;
   double (*part)[K][kPb] = reinterpret_cast<double (*)[K][kPb]>(nxt + K);              // [4]
-  double* wsm = reinterpret_cast<double*>(part + 4);                                     // kPb * kPb
   __shared__ int s_fail;
   auto blk = [&](int t) { return upper ? nb - 1 - t : t; };
   auto rows = [&](int t) { return min(kPb, n - blk(t) * kPb); };
@@ -525,12 +524,6 @@ __global__ void __launch_bounds__(kPThreads) k_tri_persist(const double* __restr
   }
   if (mine(1)) form_z(1);
   for (int t = 0; t + 1 < nb; ++t) {
-    // the W tile of the critical product does not depend on sol_t: load it
-    // before the wait
-    if (mine(t + 1)) {
-      const double* Wt = W + (size_t)blk(t + 1) * kPb * kPb;
-      for (int q = threadIdx.x; q < kPb * kPb; q += blockDim.x) wsm[q] = __ldcg(Wt + q);
-    }
     // sol_t into cur (computed here when this CTA owns t)
     if (!mine(t)) {
       if (threadIdx.x == 0) {
@@ -558,8 +551,7 @@ __global__ void __launch_bounds__(kPThreads) k_tri_persist(const double* __restr
       const int s1 = slot(t + 1);
       for (int q = threadIdx.x; q < K * kPb; q += blockDim.x) nxt[q / kPb][q % kPb] = z[s1][q / kPb][q % kPb];
       __syncthreads();
-      __syncthreads();
-      tile_gemv<K>(wsm, kPb, rows(t + 1), rows(t), cur, part, nxt, true);
+      tile_gemv<K>(W + (size_t)blk(t + 1) * kPb * kPb, kPb, rows(t + 1), rows(t), cur, part, nxt, true);
       publish(t + 1, nxt);
     }
     // panel t on the owned blocks two or more steps ahead
@@ -579,7 +571,7 @@ __global__ void __launch_bounds__(kPThreads) k_tri_persist(const double* __restr
 }
 
 static size_t tri_persist_smem(int owned, int K) {
-  return sizeof(double) * ((size_t)2 * owned * K * kPb + 2 * K * kPb + 4 * K * kPb + kPb * kPb);
+  return sizeof(double) * ((size_t)2 * owned * K * kPb + 2 * K * kPb + 4 * K * kPb);
 }
 
 // Influence-matrix assembly in the eigenbasis of the subdomain solver.  A
@@ -920,27 +912,25 @@ template <int K>
 static int launch_tri_persist(mf_md* md, int upper, const double* v, double* sol, cudaStream_t st, bool* done) {
   *done = false;
   const int n = (int)md->topo.ninf, nb = (n + kPb - 1) / kPb;
-  static int sms = 0;
+  static int sms = 0, occ[5] = {0, 0, 0, 0, 0};
   if (!sms) {
     int dev = 0;
     MF_CUDA(cudaGetDevice(&dev));
     MF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   }
-  // grid: up to two CTAs per SM (a CTA's panel products wait on memory; a
-  // second CTA keeps the SM's loads in flight), fewer with fewer blocks
-  MF_CUDA(cudaFuncSetAttribute(k_tri_persist<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-  int per_sm = 2, G = 0, owned = 0;
-  size_t smem = 0;
-  for (; per_sm >= 1; --per_sm) {
-    G = std::min(nb, sms * per_sm);
-    owned = (nb + G - 1) / G;
-    smem = tri_persist_smem(owned, K);
-    if (owned > kPMaxOwned || smem > 200 * 1024) continue;
+  // grid: one CTA per SM, fewer when there are fewer blocks
+  const int G = std::min(nb, sms);
+  const int owned = (nb + G - 1) / G;
+  if (owned > kPMaxOwned) return MF_OK;
+  const size_t smem = tri_persist_smem(owned, K);
+  if (smem > 200 * 1024) return MF_OK;
+  MF_CUDA(cudaFuncSetAttribute(k_tri_persist<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  if (!occ[K]) {
     int o = 0;
     MF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_tri_persist<K>, kPThreads, smem));
-    if (o >= per_sm) break;
+    occ[K] = o;
   }
-  if (per_sm < 1) return MF_OK;  // not co-resident: the block steps take over
+  if (occ[K] < 1) return MF_OK;  // not co-resident: the block steps take over
   const size_t half = (size_t)nb * kPb * kPb;
   const double* A = md->M.as<double>();
   const double* dinv = md->pdinv.as<double>() + (upper ? half : 0);

@@ -323,7 +323,15 @@ class APosteriori:
         self.refine = refine
 
     def filtered(self):
-        return [self.pairs.filter3(c).clone() for c in self.fine.u]
+        """The fine velocity filtered to the LES grid, its wall values set to
+        the no-slip data the time step imposes (the filter leaves them at
+        ~1% of the velocity scale)."""
+        out = [self.pairs.filter3(c).clone() for c in self.fine.u]
+        for c in out:
+            c[0].zero_(); c[-1].zero_()
+            c[:, 0].zero_(); c[:, -1].zero_()
+            c[:, :, 0].zero_(); c[:, :, -1].zero_()
+        return out
 
     def _les(self, start, les_type, dt):
         g = self.pairs.coarse
