@@ -759,15 +759,14 @@ def row_measurements(mf, torch, hbm, md_rows=True):
     del rhs, outs, vel, nu
     # the Navier-Stokes time step of navier3d at 128 x 129 x 128 with the
     # reference's scheme defaults (pt 1, BDF2, skew-symmetric advection,
-    # flow-rate term), Re = 180, ts = 1e-3, random velocity levels; FP64 solves
-    # and 3xTF32 + 1 refinement, eager steps and a CUDA graph of four steps
-    # (one rotation of the time slots)
+    # flow-rate term), Re = 180, ts = 1e-3, levels on the reference's exact
+    # solution plus a 5% seeded perturbation; FP64 solves and 3xTF32 + 1
+    # refinement, eager steps and a CUDA graph of four steps (one rotation of
+    # the time slots)
     row = {}
     for key, prec in (("fp64", mf.MF_PREC_FP64), ("3xtf32", mf.MF_PREC_3XTF32)):
         nav = mf.NavierStokes3D(gx, gy, gz, ts=1e-3, reynolds=180.0, precision=prec, refine=1)
-        for lev in range(4):
-            for q, var in enumerate("uvw"):
-                nav.set_field(var, lev, field(shape, 90 + 4 * q + lev))
+        exact_levels(mf, nav, gx, gy, gz, 180.0, 90)
         for _ in range(4):
             nav.step()
         row[key + "_eager_ms"] = time_fn(nav.step, reps=8)
@@ -787,9 +786,7 @@ def row_measurements(mf, torch, hbm, md_rows=True):
     gl = (mesh.uniform_grid(96), mesh.tanh_grid(97, 2.0), mesh.uniform_grid(96))
     nav = mf.NavierStokes3D(*gl, ts=1e-3, reynolds=180.0, precision=mf.MF_PREC_3XTF32, refine=1,
                             les_type=1, les_c=0.17)
-    for lev in range(4):
-        for q, var in enumerate("uvw"):
-            nav.set_field(var, lev, field((96, 97, 96), 120 + 4 * q + lev))
+    exact_levels(mf, nav, *gl, 180.0, 120)
     for _ in range(4):
         nav.step()
     out["navier_step_les_96x97x96"] = {"eager_ms": time_fn(nav.step, reps=8),
@@ -806,9 +803,7 @@ def row_measurements(mf, torch, hbm, md_rows=True):
     lim = np.full(6, 3.0, np.float32)
     net.set_scaling(np.zeros(6), np.ones(6), -lim, lim, 0.02, 1.0)
     nav.set_les_network(net)
-    for lev in range(4):
-        for q, var in enumerate("uvw"):
-            nav.set_field(var, lev, field((96, 97, 96), 120 + 4 * q + lev))
+    exact_levels(mf, nav, *gl, 180.0, 120)
     for _ in range(4):
         nav.step()
     ms = time_fn(nav.step, reps=8)
@@ -833,6 +828,21 @@ def row_measurements(mf, torch, hbm, md_rows=True):
     # the learned closure judged a posteriori (fine 193^3 -> LES 49^3)
     out["learned_les_a_posteriori"] = les_a_posteriori(mf, torch)
     return out
+
+
+def exact_levels(mf, nav, gx, gy, gz, reynolds, seed, amplitude=0.05):
+    """Time levels of the one-domain step set to the reference's exact
+    solution (the step's boundary data and sources come from it) plus a
+    seeded perturbation of `amplitude`, different in every level."""
+    from oracle import navier as N
+    rng = np.random.default_rng(seed)
+    X, Y, Z = np.meshgrid(gx, gy, gz, indexing="ij")
+    base = {v: N.sol(X, Y, Z, 0.0, v, reynolds) for v in ("u", "v", "p")}
+    for lev in range(4):
+        for var in ("u", "v", "w", "p", "phi"):
+            f = base.get("p" if var == "phi" else var, np.zeros(X.shape))
+            f = np.asfortranarray(f + amplitude * rng.standard_normal(X.shape))
+            nav.set_field(var, lev, mf.to_device(f))
 
 
 def channel_initial(gx, gy, gz, seed=6, amplitude=0.1, modes=4):
@@ -1027,12 +1037,9 @@ def run_row_probe(args):
         for _ in range(2):
             flt.apply(f, 0, out=fo)
     elif args.probe == "navier":
-        shape = (128, 129, 128)
-        nav = mf.NavierStokes3D(mesh.uniform_grid(128), mesh.tanh_grid(129, 2.0), mesh.uniform_grid(128),
-                                ts=1e-3, reynolds=180.0, precision=mf.MF_PREC_3XTF32, refine=1)
-        for lev in range(4):
-            for q, var in enumerate("uvw"):
-                nav.set_field(var, lev, field(shape, 90 + 4 * q + lev))
+        gs = (mesh.uniform_grid(128), mesh.tanh_grid(129, 2.0), mesh.uniform_grid(128))
+        nav = mf.NavierStokes3D(*gs, ts=1e-3, reynolds=180.0, precision=mf.MF_PREC_3XTF32, refine=1)
+        exact_levels(mf, nav, *gs, 180.0, 90)
         for _ in range(6):  # four steps warm the nonlinear-term cache, two are profiled
             nav.step()
     elif args.probe == "channel":
