@@ -1141,69 +1141,15 @@ struct FoldArgsF {
   const float* bz;
 };
 
-// Grid: x over i (blocks of 256, P1 <= 256 is a multiple of 64), y = j < P2,
-// z strides over k (kPlanes planes per thread).  The x- and z-face terms
-// that do not depend on k (inv_lhs_x(i), inv_lhs_y(j), bc_z(i, j)) are
-// loaded once per thread; per point only rhs, bc_x(j, k), bc_y(i, k) and
-// inv_lhs_z(k) are read.
-__global__ void k_fold_split(const double* __restrict__ rhs, FoldArgsF a, __nv_bfloat16* hi,
-                             __nv_bfloat16* lo, float* x32, int n1, int n2, int n3, int P1, int P2,
-                             int P3) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
-  if (i >= P1) return;
-  const bool in_ij = i < n1 && j < n2;
-  const long long sx = (long long)n2 * n3, sy = (long long)n1 * n3, sz = (long long)n1 * n2;
-  float cx[4] = {0.f, 0.f, 0.f, 0.f}, cy[4] = {0.f, 0.f, 0.f, 0.f}, fz[4] = {0.f, 0.f, 0.f, 0.f};
-  if (in_ij) {
-#pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      cx[c] = a.ix[c][i];
-      cy[c] = a.iy[c][j];
-      fz[c] = a.bz[c * sz + i + (long long)n1 * j];
-    }
-  }
-  for (int k0 = blockIdx.z * kPlanes; k0 < P3; k0 += gridDim.z * kPlanes) {
-    double r[kPlanes];
-#pragma unroll
-    for (int q = 0; q < kPlanes; ++q) {
-      const int k = k0 + q;
-      r[q] = (in_ij && k < n3) ? rhs[i + (long long)n1 * (j + (long long)n2 * k)] : 0.0;
-    }
-#pragma unroll
-    for (int q = 0; q < kPlanes; ++q) {
-      const int k = k0 + q;
-      if (k >= P3) break;
-      float v = 0.f;
-      if (in_ij && k < n3) {
-        v = narrow(r[q]);
-        const long long fx = j + (long long)n2 * k, fy = i + (long long)n1 * k;
-#pragma unroll
-        for (int c = 0; c < 4; ++c) {
-          v -= cx[c] * a.bx[c * sx + fx];
-          v -= cy[c] * a.by[c * sy + fy];
-          v -= a.iz[c][k] * fz[c];
-        }
-      }
-      const long long idx = i + (long long)P1 * (j + (long long)P2 * k);
-      if (x32) {
-        x32[idx] = v;
-      } else {
-        const __nv_bfloat16 h = __float2bfloat16_rn(v);
-        hi[idx] = h;
-        lo[idx] = __float2bfloat16_rn(v - __bfloat162float(h));
-      }
-    }
-  }
-}
-
-// c * bc face products of the fold, in FP32: out[c][face point].
-// The same fold with kFoldJ rows j per thread: grid x over i (128-thread
-// blocks), y over groups of kFoldJ rows, z strides over k.  The y-face
-// products of (i, k) are loaded once and used for the thread's kFoldJ rows
-// (the one-row form re-reads them for every j, ~250 MB of L2 traffic at
-// 257^3), the z-face products of (i, j) and the y-rows of inv_lhs stay in
-// registers for the whole k loop.  Same operations in the same order per
-// point as k_fold_split, so the results are identical.
+// Fold of the boundary data into the right-hand side and store of the first
+// transform's operand (mixed path): v = narrow(rhs) - sum over the four
+// boundary columns of each axis of inv_lhs(:, c) * (ddr_c * bc), then FP32
+// or split BF16 in the padded rotating layout.  kFoldJ rows j per thread:
+// grid x over i (128-thread blocks), y over groups of kFoldJ rows, z strides
+// over k.  The y-face products of (i, k) are loaded once and used for the
+// thread's kFoldJ rows (one row per thread would re-read them for every j,
+// ~250 MB of L2 traffic at 257^3); the z-face products of (i, j) and the
+// y-rows of inv_lhs stay in registers for the whole k loop.
 constexpr int kFoldJ = 8;
 constexpr int kFoldKz = 16;
 __global__ void __launch_bounds__(128) k_fold_split_rows(const double* __restrict__ rhs, FoldArgsF a,
