@@ -782,11 +782,15 @@ def row_measurements(mf, torch, hbm, md_rows=True):
         nav.close()
     out["navier_step_128x129x128"] = row
     # the same step with the Smagorinsky LES term on the LES grid of the
-    # learned-coefficient configuration (96 x 97 x 96), 3xTF32 solves
+    # learned-coefficient configuration (96 x 97 x 96), 3xTF32 solves, on a
+    # decaying flow in the no-slip box (nmodes 0, box_initial): started from
+    # the manufactured solution, the reference's scheme departs from it at
+    # the second step on this grid and diverges within ten steps (the oracle
+    # does the same), models or not
     gl = (mesh.uniform_grid(96), mesh.tanh_grid(97, 2.0), mesh.uniform_grid(96))
     nav = mf.NavierStokes3D(*gl, ts=1e-3, reynolds=180.0, precision=mf.MF_PREC_3XTF32, refine=1,
-                            les_type=1, les_c=0.17)
-    exact_levels(mf, nav, *gl, 180.0, 120)
+                            les_type=1, les_c=0.17, nmodes=0)
+    box_levels(mf, nav, *gl)
     for _ in range(4):
         nav.step()
     out["navier_step_les_96x97x96"] = {"eager_ms": time_fn(nav.step, reps=8),
@@ -798,12 +802,12 @@ def row_measurements(mf, torch, hbm, md_rows=True):
     # range; the network here is seeded, not trained (the a-posteriori run,
     # --les-config5, trains it)
     nav = mf.NavierStokes3D(*gl, ts=1e-3, reynolds=180.0, precision=mf.MF_PREC_3XTF32, refine=1,
-                            les_type=mf.MF_LES_LEARNED, les_c=0.17)
+                            les_type=mf.MF_LES_LEARNED, les_c=0.17, nmodes=0)
     net = mf.Mlp(1)
     lim = np.full(6, 3.0, np.float32)
     net.set_scaling(np.zeros(6), np.ones(6), -lim, lim, 0.02, 1.0)
     nav.set_les_network(net)
-    exact_levels(mf, nav, *gl, 180.0, 120)
+    box_levels(mf, nav, *gl)
     for _ in range(4):
         nav.step()
     ms = time_fn(nav.step, reps=8)
@@ -843,6 +847,45 @@ def exact_levels(mf, nav, gx, gy, gz, reynolds, seed, amplitude=0.05):
             f = base.get("p" if var == "phi" else var, np.zeros(X.shape))
             f = np.asfortranarray(f + amplitude * rng.standard_normal(X.shape))
             nav.set_field(var, lev, mf.to_device(f))
+
+
+def box_initial(gx, gy, gz, seed=7, modes=6):
+    """Start field of the decaying no-slip box flow: the curl of a seeded
+    vector potential of low Fourier modes, damped by (s (1 - s))^2 towards
+    every face (zero velocity on the walls), derivatives by second-order
+    differences on the grids, scaled to max |u| = 1 (an advective CFL of 0.1
+    at ts 1e-3 on 96 uniform points).  The first step projects out the
+    discrete divergence.  Arrays (nx, ny, nz), x fastest."""
+    rng = np.random.default_rng(seed)
+    X, Y, Z = np.meshgrid(gx, gy, gz, indexing="ij")
+    env = (16.0 * X * (1.0 - X) * Y * (1.0 - Y) * Z * (1.0 - Z)) ** 2
+    A = []
+    for _ in range(3):
+        a = np.zeros_like(X)
+        for _ in range(modes):
+            k = rng.integers(1, 4, size=3)
+            ph = rng.uniform(0, 2 * np.pi, size=3)
+            a += rng.normal() * (np.cos(2 * np.pi * k[0] * X + ph[0]) * np.cos(2 * np.pi * k[1] * Y + ph[1])
+                                 * np.cos(2 * np.pi * k[2] * Z + ph[2]))
+        A.append(a * env)
+    d = lambda f, g, ax: np.gradient(f, g, axis=ax, edge_order=2)
+    u = d(A[2], gy, 1) - d(A[1], gz, 2)
+    v = d(A[0], gz, 2) - d(A[2], gx, 0)
+    w = d(A[1], gx, 0) - d(A[0], gy, 1)
+    top = max(np.abs(c).max() for c in (u, v, w))
+    return [np.asfortranarray(c / top) for c in (u, v, w)]
+
+
+def box_levels(mf, nav, gx, gy, gz, seed=7):
+    """All four time levels of a one-domain step without manufactured
+    sources (nmodes = 0) set to box_initial; pressure and its increment zero."""
+    start = [mf.to_device(c) for c in box_initial(gx, gy, gz, seed)]
+    zero = mf.to_device(np.zeros((len(gx), len(gy), len(gz)), order="F"))
+    for lev in range(4):
+        for q, var in enumerate("uvw"):
+            nav.set_field(var, lev, start[q])
+        nav.set_field("p", lev, zero)
+        nav.set_field("phi", lev, zero)
 
 
 def channel_initial(gx, gy, gz, seed=6, amplitude=0.1, modes=4):
@@ -905,15 +948,19 @@ def md_config2(mf, torch, operators=("velocity", "pressure")):
     tanh(1.0) slabs on [0, 1]^3: influence-matrix set-up and solves for the
     velocity operator (Dirichlet, sigma = -1e6) and the pressure operator
     (Neumann, sigma = 0, null space), random right-hand sides.  Per
-    operator: one right-hand side with the persistent triangular solves (the
-    default) and with one launch per block step, and three right-hand sides
-    in one call (the three velocity components of a time step)."""
+    operator: one right-hand side in the default interface form (the
+    inverted LU factors above 12,000 unknowns) and on the LU factors (the
+    persistent triangular solves, one launch per block step), three
+    right-hand sides in one call (the three velocity components of a time
+    step), and the interface system alone (md_solve) against the HBM time of
+    one read of the n x n FP64 factors."""
     from oracle import mesh
     rng = np.random.default_rng(3)
     sizes = rng.choice([49, 65, 97], size=(3, 2))
     grids = [[mesh.tanh_grid(int(sizes[l][0]), 1.0, 0.0, 0.5), mesh.tanh_grid(int(sizes[l][1]), 1.0, 0.5, 1.0)]
              for l in range(3)]
     out = {"workload": "md_2x2x2_slabs_%s" % "_".join("%dx%d" % tuple(sz) for sz in sizes)}
+    hbm = peaks()[0]
     ops = {"velocity": (-1e6, (1,) * 6, 0), "pressure": (0.0, (2,) * 6, 1)}
     for name in operators:
         sigma, bct, null = ops[name]
@@ -951,15 +998,31 @@ def md_config2(mf, torch, operators=("velocity", "pressure")):
             torch.cuda.synchronize()
             return a.elapsed_time(b) / reps
 
-        for key, form in (("solve_ms", mf.MD_TRI_PERSISTENT), ("solve_ms_block_steps", mf.MD_TRI_STEPS)):
-            md.set_triangular_form(form)
-            row[key] = timed(lambda: md.solve(g, u, bc), 5 if form == mf.MD_TRI_PERSISTENT else 2)
-        md.set_triangular_form(mf.MD_TRI_PERSISTENT)
+        form_names = {mf.MD_IFACE_INVERSE: "inverse", mf.MD_IFACE_TRIANGULAR_INVERSE: "inverted_lu_factors",
+                      mf.MD_IFACE_LU: "lu_triangular_solves"}
+        row["interface_form"] = form_names[md.interface_form()]
+        n = md.ninf()
+        row["interface_bytes_per_solve"] = 8.0 * n * n  # the n x n FP64 factors (or inverse) read once
+        iv = torch.randn(3, n, dtype=torch.float64, device="cuda", generator=gen)
+        row["solve_ms"] = timed(lambda: md.solve(g, u, bc), 5)
         sets = [rhs() for _ in range(3)]
         row["solve_many_3_ms"] = timed(lambda: md.solve_many([s_[0] for s_ in sets], [s_[1] for s_ in sets],
                                                              [s_[2] for s_ in sets]), 3)
+        for k in (1, 3):
+            t_ms = timed(lambda: md.interface_solve(iv[:k]), 5)
+            row["interface_ms_%d" % k] = t_ms
+            row["interface_frac_of_hbm_%d" % k] = row["interface_bytes_per_solve"] / (t_ms * 1e-3) / 1e9 / hbm
+        x_default = md.interface_solve(iv).clone()
+        md.set_interface_solve(mf.MD_IFACE_LU)
+        x_lu = md.interface_solve(iv)
+        row["interface_rel_diff_vs_lu"] = float((x_default - x_lu).abs().max() / x_lu.abs().max())
+        for key, form in (("solve_ms_lu_persistent", mf.MD_TRI_PERSISTENT),
+                          ("solve_ms_lu_block_steps", mf.MD_TRI_STEPS)):
+            md.set_triangular_form(form)
+            row[key] = timed(lambda: md.solve(g, u, bc), 3 if form == mf.MD_TRI_PERSISTENT else 2)
+        md.set_triangular_form(mf.MD_TRI_PERSISTENT)
+        row["interface_ms_1_lu_persistent"] = timed(lambda: md.interface_solve(iv[:1]), 3)
         md.device_status()
-        row["interface_bytes_per_solve"] = 16.0 * md.ninf() ** 2 / 2.0  # L and U read once
         out[name] = row
         md.close()
         del g, u, bc, sets

@@ -348,19 +348,43 @@ int mf_md_solve_many(mf_md_t* md, int nrhs, const double* const* g, double* cons
                      const double* const* bcx, const double* const* bcy, const double* const* bcz,
                      void* stream);
 
+/* md_solve (class_md.f90:379-438): the interface system alone for nrhs
+ * (1..4) right-hand sides stored one after the other at rhs (ninf each,
+ * device), solutions to sol, in the form mf_md_interface_form reports, with
+ * the operator's null-space handling (md_rhs_nullspace,
+ * md_vector_zero_lastpoint).  mf_md_solve calls the same step between its two
+ * rounds of subdomain solves. */
+int mf_md_interface_solve(mf_md_t* md, int nrhs, const double* rhs, double* sol, void* stream);
+
 /* Interface-system solve form (no reference counterpart: the reference solves
  * it with a PETSc KSP, class_md.f90:379-438).  MF_MD_IFACE_AUTO (default):
- * one FP64 matrix-vector product with the inverse formed at set-up when
- * ninf <= 12,000 and it fits in device memory, else the triangular solves.
- * MF_MD_IFACE_LU: always the two triangular solves on the getrf factors.
- * Takes effect at the next mf_md_solve; the inverse, when wanted, is formed
- * by mf_md_influence_matrix_set, so select MF_MD_IFACE_AUTO before it. */
+ * when ninf <= 12,000 one FP64 matrix-vector product with the inverse formed
+ * at set-up; above, two row-parallel triangular products with the inverted LU
+ * factors (MF_MD_IFACE_TRIANGULAR_INVERSE); the triangular solves on the LU
+ * factors when neither fits in device memory.  MF_MD_IFACE_LU: always the two
+ * triangular solves on the getrf factors.  Takes effect at the next
+ * mf_md_solve; the inverse forms are built by mf_md_influence_matrix_set (and
+ * mf_md_load_factor), so select the mode before it. */
 #define MF_MD_IFACE_AUTO 0
 #define MF_MD_IFACE_LU 1
 /* MF_MD_IFACE_INVERSE: the inverse at any size when it fits in device memory
  * (2 n^3 FP64 flops at set-up, then one n^2 read per solve; for long runs). */
 #define MF_MD_IFACE_INVERSE 2
+/* MF_MD_IFACE_TRIANGULAR_INVERSE: the inverted LU factors at any size when
+ * they fit (2 n^3 / 3 FP64 flops at set-up, as the getrf; then the same n^2
+ * read per solve as MF_MD_IFACE_INVERSE, in two launches).  The factors are
+ * stored as double-float pairs (FP32 hi + lo, 8 bytes an entry, scaled by a
+ * power of two) and the products run on the FP32 pipe, about 2^-48 relative
+ * per term; MF_MD_IFACE_TRIANGULAR_INVERSE_FP64 keeps FP64 entries and FP64
+ * FMAs (bound by GB300's FP64 rate, one FMA per 8 bytes read).  A factor with
+ * a non-finite entry stays FP64. */
+#define MF_MD_IFACE_TRIANGULAR_INVERSE 3
+#define MF_MD_IFACE_TRIANGULAR_INVERSE_FP64 4
 int mf_md_set_interface_solve(mf_md_t* md, int mode);
+/* The form the next solve takes (MF_MD_IFACE_INVERSE, _TRIANGULAR_INVERSE,
+ * _TRIANGULAR_INVERSE_FP64 or _LU), after mf_md_influence_matrix_set or
+ * mf_md_load_factor. */
+int mf_md_interface_form(const mf_md_t* md, int* form);
 /* Form of the triangular solves on the LU factors (no reference
  * counterpart): MF_MD_TRI_PERSISTENT (default) one cooperative launch per
  * triangle, CTAs advancing through 64-row blocks behind release/acquire

@@ -74,7 +74,7 @@ def build(verbose=False):
     if not os.path.exists(out) or os.path.getmtime(out) < max(os.path.getmtime(o) for o in objs):
         cuda_lib = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "lib64")
         cmd = ([_nvcc()] + ARCH + ["-shared", "-o", out] + objs +
-               ["-cudart", "static", "-L" + cuda_lib, "-lcusolver",
+               ["-cudart", "static", "-L" + cuda_lib, "-lcusolver", "-lcublas",
                 "-Xlinker", "-rpath", "-Xlinker", cuda_lib])
         if verbose:
             print(" ".join(cmd), flush=True)

@@ -11,15 +11,19 @@
 // device; the neighbour exchange becomes a gather of signed face derivatives
 // into the interface vector and a scatter of the interface solution into the
 // subdomains' boundary arrays (device kernels).  The PETSc KSP is replaced by
-// a dense FP64 LU factorised once (cuSOLVER getrf at set-up), from which the
-// inverse is formed once as well (getrs against the identity); each call then
-// solves the interface system with one FP64 matrix-vector product, a read of
-// the n x n inverse at HBM rate, instead of two triangular solves whose rows
-// depend on one another.  The blocked triangular solves remain as the path
-// used when the inverse does not fit in device memory.
+// a dense FP64 LU factorised once (cuSOLVER getrf at set-up).  Up to 12,000
+// unknowns the inverse is formed from it (getrs against the identity) and a
+// solve is one FP64 matrix-vector product; above that the two factors are
+// inverted in place (trtri, a third of the inverse's flops) and a solve is two
+// row-parallel triangular products.  Either way a solve reads n x n FP64 once
+// at HBM rate, instead of two triangular solves whose rows depend on one
+// another.  The blocked triangular solves on the LU factors remain as the
+// path used when neither fits in device memory.
+#include <cublas_v2.h>
 #include <cusolverDn.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
@@ -741,6 +745,308 @@ __global__ void __launch_bounds__(32 * kGemvRows) k_gemm_rows(const double* __re
   }
 }
 
+// In-place transpose of the n x n matrix A (column-major to row-major, set-up
+// only): CTA (bx, by), bx < by, swaps the 32 x 32 tiles (bx, by) and (by, bx)
+// through shared memory, bx == by transposes its tile, bx > by returns.  Both
+// tiles are read before either is written.  With L given, entries below the
+// diagonal are taken from L instead of A (the two inverted factors, each
+// inverted in its own copy, merge into one array on the way).
+__global__ void __launch_bounds__(256) k_transpose_square(double* A, const double* __restrict__ L, int n) {
+  const int bx = blockIdx.x, by = blockIdx.y;
+  if (bx > by) return;
+  __shared__ double t1[32][33], t2[32][33];
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const long long N = n;
+  for (int k = ty; k < 32; k += 8) {
+    const long long i1 = bx * 32 + tx, j1 = by * 32 + k, i2 = by * 32 + tx, j2 = bx * 32 + k;
+    if (i1 < N && j1 < N) t1[k][tx] = (L && i1 > j1) ? L[i1 + N * j1] : A[i1 + N * j1];
+    if (i2 < N && j2 < N) t2[k][tx] = (L && i2 > j2) ? L[i2 + N * j2] : A[i2 + N * j2];
+  }
+  __syncthreads();
+  for (int k = ty; k < 32; k += 8) {
+    const long long i1 = bx * 32 + tx, j1 = by * 32 + k, i2 = by * 32 + tx, j2 = bx * 32 + k;
+    if (i1 < N && j1 < N) A[i1 + N * j1] = t2[tx][k];
+    if (bx != by && i2 < N && j2 < N) A[i2 + N * j2] = t1[tx][k];
+  }
+}
+
+// Unit diagonal written into the n x n column-major A (the copy of the LU
+// factor whose lower part is inverted as L).
+__global__ void k_unit_diagonal(double* A, int n) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) A[i + (long long)n * i] = 1.0;
+}
+
+// Products with the inverted LU factors of the interface system, both held
+// row-major in one n x n array T: its strict lower part is L^-1 below the unit
+// diagonal, its upper part with the diagonal U^-1.  UPPER = false: Y[:, r] =
+// X[:, r] + (strict lower of T) X[:, r]; UPPER = true: Y[:, r] = (upper of T)
+// X[:, r], for K right-hand sides (columns of length n).  Unlike the
+// triangular solves on the factors, every row is independent: each warp owns
+// rows r0 + w and r0 + 16 + w of its CTA and reads T[row, lo : hi) once for
+// all K columns (lo = 0, hi = row below the diagonal; lo = row, hi = n
+// above), four 256-byte loads in flight per row; X is staged through shared
+// memory in chunks over the columns the CTA's rows need.  The lane and
+// accumulator of a column depend only on the row pair and the chunk, so a
+// column's result does not depend on K.
+constexpr int kTmvRows = 32;     // rows per CTA, two per warp
+constexpr int kTmvChunk = 1024;  // columns of X staged at a time
+template <int K, bool UPPER>
+__global__ void __launch_bounds__(512) k_trimv_rows(const double* __restrict__ T, const double* __restrict__ X,
+                                                    double* __restrict__ Y, int n) {
+  __shared__ double xs[K][kTmvChunk];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // heaviest row blocks first (the longest rows of L^-1 are the last ones)
+  const int r0 = (UPPER ? blockIdx.x : gridDim.x - 1 - blockIdx.x) * kTmvRows;
+  const int ra = r0 + w, rb = r0 + 16 + w;
+  const bool la = ra < n, lb = rb < n;
+  const int rlast = min(r0 + kTmvRows, n) - 1;
+  const int clo = UPPER ? r0 : 0, chi = UPPER ? n : rlast;  // columns any row of the CTA needs
+  const int loa = UPPER ? ra : 0, hia = la ? (UPPER ? n : ra) : 0;
+  const int lob = UPPER ? rb : 0, hib = lb ? (UPPER ? n : rb) : 0;
+  const double* rowa = T + (long long)(la ? ra : 0) * n;
+  const double* rowb = T + (long long)(lb ? rb : 0) * n;
+  double sa[2][K], sb[2][K];
+#pragma unroll
+  for (int r = 0; r < K; ++r) sa[0][r] = sa[1][r] = sb[0][r] = sb[1][r] = 0.0;
+  for (int c0 = clo; c0 < chi; c0 += kTmvChunk) {
+    const int len = min(kTmvChunk, chi - c0);
+    __syncthreads();  // the previous chunk is consumed
+    for (int e = threadIdx.x; e < K * kTmvChunk; e += blockDim.x) {
+      const int r = e / kTmvChunk, c = e % kTmvChunk;
+      xs[r][c] = c < len ? X[(long long)r * n + c0 + c] : 0.0;
+    }
+    __syncthreads();
+    // local column ranges [ba, ea), [bb, eb) within the chunk, and their union
+    const int ba = max(loa, c0) - c0, ea = min(hia, c0 + len) - c0;
+    const int bb = max(lob, c0) - c0, eb = min(hib, c0 + len) - c0;
+    const int b = min(ba < ea ? ba : len, bb < eb ? bb : len), e = max(ea, eb);
+    for (int c = b + lane; c < e; c += 128) {
+      double va[4], vb[4];
+      bool pa[4], pb[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int cq = c + 32 * q;
+        pa[q] = cq >= ba && cq < ea;
+        pb[q] = cq >= bb && cq < eb;
+        va[q] = pa[q] ? rowa[c0 + cq] : 0.0;
+        vb[q] = pb[q] ? rowb[c0 + cq] : 0.0;
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int cq = c + 32 * q;
+#pragma unroll
+        for (int r = 0; r < K; ++r) {
+          if (pa[q]) sa[q & 1][r] = fma(va[q], xs[r][cq], sa[q & 1][r]);
+          if (pb[q]) sb[q & 1][r] = fma(vb[q], xs[r][cq], sb[q & 1][r]);
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < K; ++r) {
+    double a = sa[0][r] + sa[1][r], bsum = sb[0][r] + sb[1][r];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      a += __shfl_down_sync(0xffffffffu, a, off);
+      bsum += __shfl_down_sync(0xffffffffu, bsum, off);
+    }
+    if (lane == 0) {
+      if (la) Y[(long long)r * n + ra] = UPPER ? a : X[(long long)r * n + ra] + a;
+      if (lb) Y[(long long)r * n + rb] = UPPER ? bsum : X[(long long)r * n + rb] + bsum;
+    }
+  }
+}
+
+// The same products in double-float arithmetic on the FP32 pipe (GB300
+// issues FP64 FMAs at about a sixtieth of its FP32 rate, and at one FMA per
+// 8-byte element the FP64 form above is bound by that pipe, not by HBM).
+// T holds each entry a as the pair (hi, lo) of FP32 values with hi = fl32(a),
+// lo = fl32(a - hi) (8 bytes, as the FP64 entry it replaced); X arrives split
+// the same way after scaling by a power of two per column (k_df_prep); T is
+// scaled by one power of two at set-up (its largest entry in [1, 2), undone
+// by tscale), so no product or sum leaves the FP32 range.  Per element: p = hi_a hi_x (its rounding
+// error recovered exactly by an FMA, the cross terms hi_a lo_x + lo_a hi_x
+// added to it) is summed into a (hi, lo) accumulator with Knuth's TwoSum
+// (Knuth, TAOCP vol. 2, 4.2.2), every operation an explicit round-to-nearest
+// intrinsic so that no multiply is contracted into the sums.  The warp's
+// partial sums are reduced in FP64 and scaled back; the unit diagonal of L^-1
+// adds the FP64 entry itself (Xp).  Accuracy about 2^-48 per element against
+// FP64's 2^-53.
+struct DfAcc {
+  float h, l;
+};
+__device__ __forceinline__ void df_fma(DfAcc& s, float2 a, float2 x) {
+  const float p = __fmul_rn(a.x, x.x);
+  float e = __fmaf_rn(a.x, x.x, -p);
+  e = __fmaf_rn(a.x, x.y, e);
+  e = __fmaf_rn(a.y, x.x, e);
+  const float t = __fadd_rn(s.h, p);
+  const float bv = __fsub_rn(t, s.h);
+  const float err = __fadd_rn(__fsub_rn(s.h, __fsub_rn(t, bv)), __fsub_rn(p, bv));
+  s.h = t;
+  s.l = __fadd_rn(s.l, __fadd_rn(err, e));
+}
+
+template <int K, bool UPPER>
+__global__ void __launch_bounds__(512) k_trimv_rows_df(const float2* __restrict__ T, const float2* __restrict__ X,
+                                                       const double* __restrict__ Xp,
+                                                       const double* __restrict__ unscale, double tscale,
+                                                       double* __restrict__ Y, int n) {
+  __shared__ float2 xs[K][kTmvChunk];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // heaviest row blocks first (the longest rows of L^-1 are the last ones)
+  const int blk = UPPER ? blockIdx.x : gridDim.x - 1 - blockIdx.x;
+  const int r0 = blk * kTmvRows;
+  const int ra = r0 + w, rb = r0 + 16 + w;
+  const bool la = ra < n, lb = rb < n;
+  const int rlast = min(r0 + kTmvRows, n) - 1;
+  const int clo = UPPER ? r0 : 0, chi = UPPER ? n : rlast;
+  const int loa = UPPER ? ra : 0, hia = la ? (UPPER ? n : ra) : 0;
+  const int lob = UPPER ? rb : 0, hib = lb ? (UPPER ? n : rb) : 0;
+  const float2* rowa = T + (long long)(la ? ra : 0) * n;
+  const float2* rowb = T + (long long)(lb ? rb : 0) * n;
+  DfAcc sa[2][K], sb[2][K];
+#pragma unroll
+  for (int r = 0; r < K; ++r)
+#pragma unroll
+    for (int h = 0; h < 2; ++h) sa[h][r] = sb[h][r] = DfAcc{0.f, 0.f};
+  const float2 zero2 = make_float2(0.f, 0.f);
+  for (int c0 = clo; c0 < chi; c0 += kTmvChunk) {
+    const int len = min(kTmvChunk, chi - c0);
+    // local column ranges [ba, ea), [bb, eb) within the chunk, and their union
+    const int ba = max(loa, c0) - c0, ea = min(hia, c0 + len) - c0;
+    const int bb = max(lob, c0) - c0, eb = min(hib, c0 + len) - c0;
+    const int b = min(ba < ea ? ba : len, bb < eb ? bb : len), e = max(ea, eb);
+    // one right-hand side (bound by HBM): the first loads of the chunk go out
+    // before X is staged and each iteration issues the next one's before its
+    // arithmetic.  More right-hand sides are bound by the FP32 issue rate and
+    // keep the registers for two CTAs per SM instead
+    constexpr bool kAhead = K == 1;
+    float2 va[4], vb[4];
+    int c = b + lane;
+    if (kAhead) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int cq = c + 32 * q;
+        va[q] = (cq >= ba && cq < ea) ? rowa[c0 + cq] : zero2;
+        vb[q] = (cq >= bb && cq < eb) ? rowb[c0 + cq] : zero2;
+      }
+    }
+    __syncthreads();  // the previous chunk is consumed
+    for (int i = threadIdx.x; i < K * kTmvChunk; i += blockDim.x) {
+      const int r = i / kTmvChunk, cc = i % kTmvChunk;
+      xs[r][cc] = cc < len ? X[(long long)r * n + c0 + cc] : zero2;
+    }
+    __syncthreads();
+    for (; c < e; c += 128) {
+      float2 na[4], nb[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int cq = (kAhead ? c + 128 : c) + 32 * q;
+        na[q] = (cq >= ba && cq < ea) ? rowa[c0 + cq] : zero2;
+        nb[q] = (cq >= bb && cq < eb) ? rowb[c0 + cq] : zero2;
+      }
+      if (!kAhead) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          va[q] = na[q];
+          vb[q] = nb[q];
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int cq = c + 32 * q;
+        const bool pa = cq >= ba && cq < ea, pb = cq >= bb && cq < eb;
+#pragma unroll
+        for (int r = 0; r < K; ++r) {
+          const float2 xv = (pa || pb) ? xs[r][cq] : zero2;
+          if (pa) df_fma(sa[q & 1][r], va[q], xv);
+          if (pb) df_fma(sb[q & 1][r], vb[q], xv);
+        }
+      }
+      if (kAhead) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          va[q] = na[q];
+          vb[q] = nb[q];
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < K; ++r) {
+    double a = ((double)sa[0][r].h + (double)sa[1][r].h) + ((double)sa[0][r].l + (double)sa[1][r].l);
+    double bsum = ((double)sb[0][r].h + (double)sb[1][r].h) + ((double)sb[0][r].l + (double)sb[1][r].l);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      a += __shfl_down_sync(0xffffffffu, a, off);
+      bsum += __shfl_down_sync(0xffffffffu, bsum, off);
+    }
+    if (lane == 0) {
+      const double u = unscale[r] * tscale;
+      if (la) Y[(long long)r * n + ra] = UPPER ? a * u : Xp[(long long)r * n + ra] + a * u;
+      if (lb) Y[(long long)r * n + rb] = UPPER ? bsum * u : Xp[(long long)r * n + rb] + bsum * u;
+    }
+  }
+}
+
+// Right-hand side r (CTA r) for k_trimv_rows_df: x = in[perm[i]] (perm may be
+// null), written to xp in FP64 when xp is given, and split after scaling by
+// 2^-e (2^e <= max |x| < 2^(e+1); no scaling for a zero or non-finite
+// maximum) into xdf = (hi, lo); unscale[r] = 2^e.
+__global__ void __launch_bounds__(1024) k_df_prep(const double* __restrict__ in, const int* __restrict__ perm,
+                                                  double* __restrict__ xp, float2* __restrict__ xdf,
+                                                  double* __restrict__ unscale, int n) {
+  __shared__ double part[32];
+  const double* x = in + (size_t)blockIdx.x * n;
+  double m = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) m = fmax(m, fabs(x[perm ? perm[i] : i]));
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, off));
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = m;
+  __syncthreads();
+  m = part[0];
+  for (int q = 1; q < (int)(blockDim.x >> 5); ++q) m = fmax(m, part[q]);
+  const bool ok = m > 0.0 && m <= 1.7e308;
+  const int ex = ok ? ilogb(m) : 0;
+  const double s = scalbn(1.0, -ex);
+  if (threadIdx.x == 0) unscale[blockIdx.x] = scalbn(1.0, ex);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double v = x[perm ? perm[i] : i];
+    if (xp) xp[(size_t)blockIdx.x * n + i] = v;
+    const double ws = v * s;
+    const float h = __double2float_rn(ws);
+    xdf[(size_t)blockIdx.x * n + i] = make_float2(h, __double2float_rn(ws - (double)h));
+  }
+}
+
+// Set-up of the double-float factors: the largest |entry| of T (as the bits
+// of a non-negative double, whose order is the numbers' order; NaN compares
+// above every finite value), then the in-place conversion of each FP64 entry
+// a, scaled by the power of two s that brings that maximum into [1, 2), into
+// the pair (fl32(a s), fl32(a s - fl32(a s))).  Entries below 2^-126 of the
+// largest fall into FP32's subnormal range, a contribution below 2^-126 of
+// the row's largest product.
+__global__ void k_df_range(const double* __restrict__ T, long long count, unsigned long long* __restrict__ maxbits) {
+  double m = 0.0;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < count;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double a = fabs(T[i]);
+    m = (a != a || a > m) ? a : m;
+  }
+  atomicMax(maxbits, (unsigned long long)__double_as_longlong(m));
+}
+__global__ void k_df_convert(double* T, long long count, double s) {
+  float2* out = reinterpret_cast<float2*>(T);
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < count;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double a = T[i] * s;
+    const float h = __double2float_rn(a);
+    out[i] = make_float2(h, __double2float_rn(a - (double)h));
+  }
+}
+
 // Identity matrix, n x n column-major.
 __global__ void k_identity(double* A, int n) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -815,8 +1121,13 @@ struct mf_md {
   DevBuf Minv, vec2;  // row-major inverse of the influence matrix, solve output
   DevBuf ub, dub[3], bcb;  // batched influence columns: fields, derivatives, Dirac faces
   bool inv_ok = false;
+  bool trinv_ok = false;  // Minv holds the inverted LU factors, row-major (k_trimv_rows)
+  bool trinv_df = false;  // ... as double-float pairs (k_trimv_rows_df), scaled by 1 / trinv_tscale
+  double trinv_tscale = 1.0;
+  DevBuf xdf, unscale, dfmax;  // double-float right-hand sides, their scales, the factors' max |entry|
   int iface_mode = MF_MD_IFACE_AUTO;
   cusolverDnHandle_t cs = nullptr;
+  cublasHandle_t cb = nullptr;  // set-up only: the blocked triangular inverses
   int null_mode = 0;
   double sigma = 0.0;
   bool factored = false;
@@ -1132,6 +1443,7 @@ int mf_md_destroy(mf_md_t* md) {
                     &md->work, &md->zero_int, &md->rint, &md->ufield})
     b->release();
   if (md->cs) cusolverDnDestroy(md->cs);
+  if (md->cb) cublasDestroy(md->cb);
   delete md;
   return MF_OK;
 }
@@ -1413,6 +1725,62 @@ int mf_md_influence_matrix_set(mf_md_t* md, double sigma, int null_mode, void* s
 
 // After the LU factor and the pivots are in md->M, md->ipiv: the set-up of
 // the triangular solves and, when wanted, the explicit inverse.
+// In-place inverse of the n x n upper (or lower) triangular block at A
+// (column-major, leading dimension lda, non-unit diagonal).  cuSOLVER's trtri
+// is called on blocks of at most 2^28 entries (above 2^31 it fails: 46,860^2
+// does; the lower limit puts systems above 16,384 unknowns, 18,252 in the
+// tests, through the blocked form); a larger block is split in halves, both
+// inverted the same way, and
+// the off-diagonal block formed by two in-place triangular products:
+// U12 <- -U11^-1 U12 U22^-1, L21 <- -L22^-1 L21 L11^-1.  n^3 / 3 flops either
+// way.
+static int tri_invert(mf_md* md, double* A, long long lda, long long n, bool upper, cudaStream_t st) {
+  if (n * n <= (1LL << 28)) {
+    const cublasFillMode_t fill = upper ? CUBLAS_FILL_MODE_UPPER : CUBLAS_FILL_MODE_LOWER;
+    size_t dws = 0, hws = 0;
+    if (cusolverDnXtrtri_bufferSize(md->cs, fill, CUBLAS_DIAG_NON_UNIT, n, CUDA_R_64F, A, lda, &dws, &hws) !=
+        CUSOLVER_STATUS_SUCCESS)
+      return set_error(MF_ERR_CUDA, "trtri buffer query failed (n %lld)", n);
+    int rc;
+    if ((rc = md->work.ensure(std::max(dws, (size_t)8)))) return rc;
+    std::vector<char> hwork(std::max(hws, (size_t)8));
+    if (cusolverDnXtrtri(md->cs, fill, CUBLAS_DIAG_NON_UNIT, n, CUDA_R_64F, A, lda, md->work.ptr, dws, hwork.data(),
+                         hws, md->info.as<int>()) != CUSOLVER_STATUS_SUCCESS)
+      return set_error(MF_ERR_CUDA, "trtri (inverse of an LU factor block, n %lld) failed", n);
+    int hinfo = 0;
+    MF_CUDA(cudaMemcpyAsync(&hinfo, md->info.ptr, sizeof(int), cudaMemcpyDeviceToHost, st));
+    MF_CUDA(cudaStreamSynchronize(st));  // the host workspace lives until here
+    if (hinfo != 0) return set_error(MF_ERR_SINGULAR, "trtri info %d", hinfo);
+    return MF_OK;
+  }
+  const long long n1 = (n / 2 + 31) / 32 * 32, n2 = n - n1;
+  double* A11 = A;
+  double* A22 = A + n1 + lda * n1;
+  int rc;
+  if ((rc = tri_invert(md, A11, lda, n1, upper, st)) || (rc = tri_invert(md, A22, lda, n2, upper, st))) return rc;
+  if (!md->cb && cublasCreate(&md->cb) != CUBLAS_STATUS_SUCCESS)
+    return set_error(MF_ERR_CUDA, "cublasCreate failed");
+  cublasSetStream(md->cb, st);
+  const double one = 1.0, minus = -1.0;
+  const cublasFillMode_t fill = upper ? CUBLAS_FILL_MODE_UPPER : CUBLAS_FILL_MODE_LOWER;
+  bool ok;
+  if (upper) {  // A12: n1 x n2 at column n1
+    double* B = A + lda * n1;
+    ok = cublasDtrmm_64(md->cb, CUBLAS_SIDE_LEFT, fill, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n1, n2, &one, A11, lda,
+                        B, lda, B, lda) == CUBLAS_STATUS_SUCCESS &&
+         cublasDtrmm_64(md->cb, CUBLAS_SIDE_RIGHT, fill, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n1, n2, &minus, A22,
+                        lda, B, lda, B, lda) == CUBLAS_STATUS_SUCCESS;
+  } else {  // A21: n2 x n1 at row n1
+    double* B = A + n1;
+    ok = cublasDtrmm_64(md->cb, CUBLAS_SIDE_RIGHT, fill, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n2, n1, &one, A11, lda,
+                        B, lda, B, lda) == CUBLAS_STATUS_SUCCESS &&
+         cublasDtrmm_64(md->cb, CUBLAS_SIDE_LEFT, fill, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n2, n1, &minus, A22,
+                        lda, B, lda, B, lda) == CUBLAS_STATUS_SUCCESS;
+  }
+  if (!ok) return set_error(MF_ERR_CUDA, "trmm (blocked triangular inverse) failed");
+  return MF_OK;
+}
+
 static int md_factor_finish(mf_md* md, cudaStream_t st) {
   const long long n = md->topo.ninf;
   double* M = md->M.as<double>();
@@ -1488,6 +1856,71 @@ static int md_factor_finish(mf_md* md, cudaStream_t st) {
       md->inv_ok = true;
     } else {
       (void)cudaGetLastError();  // a refused allocation is not an error here
+      md->Minv.release();
+    }
+  }
+  // the inverted factors, row-major (above 12,000 unknowns by default): U
+  // inverted in one copy of the LU factor, L in another with its diagonal set
+  // to one (trtri, n^3 / 3 FP64 flops each: together the cost of the getrf;
+  // each call is trusted with its own triangle only), the strict lower part of
+  // the second merged into the first while it is transposed so that a row is
+  // contiguous.  A solve reads the n x n array once, as the triangular solves
+  // do, but its rows are independent.  The LU factor stays as it is (factor
+  // cache, the MF_MD_IFACE_LU form).
+  md->trinv_ok = md->trinv_df = false;
+  if (!md->inv_ok && ((md->iface_mode == MF_MD_IFACE_AUTO && n > kMaxInverseRows) ||
+                      md->iface_mode == MF_MD_IFACE_TRIANGULAR_INVERSE ||
+                      md->iface_mode == MF_MD_IFACE_TRIANGULAR_INVERSE_FP64)) {
+    const size_t bytes = sizeof(double) * (size_t)n * (size_t)n;
+    size_t freeb = 0, totalb = 0;
+    MF_CUDA(cudaMemGetInfo(&freeb, &totalb));
+    DevBuf lcopy;
+    struct Release {
+      DevBuf& b;
+      ~Release() { b.release(); }
+    } release_lcopy{lcopy};  // every return below frees the copy of L
+    if (bytes < freeb / 3 && md->Minv.ensure(bytes) == MF_OK && lcopy.ensure(bytes) == MF_OK &&
+        md->vec2.ensure(sizeof(double) * kMdMaxRhs * n) == MF_OK) {
+      double* T = md->Minv.as<double>();
+      double* Lc = lcopy.as<double>();
+      MF_CUDA(cudaMemcpyAsync(T, M, bytes, cudaMemcpyDeviceToDevice, st));
+      MF_CUDA(cudaMemcpyAsync(Lc, M, bytes, cudaMemcpyDeviceToDevice, st));
+      k_unit_diagonal<<<nblk(n, 256), 256, 0, st>>>(Lc, (int)n);
+      MF_CUDA(cudaGetLastError());
+      if ((rc = tri_invert(md, T, n, n, true, st)) || (rc = tri_invert(md, Lc, n, n, false, st))) return rc;
+      const unsigned tiles = (unsigned)((n + 31) / 32);
+      k_transpose_square<<<dim3(tiles, tiles), 256, 0, st>>>(T, Lc, (int)n);
+      MF_CUDA(cudaGetLastError());
+      MF_CUDA(cudaStreamSynchronize(st));  // before the copy of L is freed
+      lcopy.release();
+      md->trinv_ok = true;
+      // double-float pairs in place, unless FP64 arithmetic is asked for or
+      // the factors hold a non-finite entry
+      rc = MF_OK;
+      if (md->iface_mode != MF_MD_IFACE_TRIANGULAR_INVERSE_FP64 &&
+          (rc = md->dfmax.ensure(sizeof(unsigned long long))) == MF_OK &&
+          (rc = md->xdf.ensure(sizeof(float2) * kMdMaxRhs * n)) == MF_OK &&
+          (rc = md->unscale.ensure(sizeof(double) * kMdMaxRhs)) == MF_OK) {
+        const long long count = n * n;
+        MF_CUDA(cudaMemsetAsync(md->dfmax.ptr, 0, sizeof(unsigned long long), st));
+        k_df_range<<<1216, 256, 0, st>>>(T, count, md->dfmax.as<unsigned long long>());
+        MF_CUDA(cudaGetLastError());
+        unsigned long long bits = 0;
+        MF_CUDA(cudaMemcpyAsync(&bits, md->dfmax.ptr, sizeof(bits), cudaMemcpyDeviceToHost, st));
+        MF_CUDA(cudaStreamSynchronize(st));
+        double tmax;
+        std::memcpy(&tmax, &bits, sizeof(tmax));
+        if (tmax > 0.0 && tmax <= 1.7e308) {
+          const int ex = std::ilogb(tmax);
+          k_df_convert<<<1216, 256, 0, st>>>(T, count, std::scalbn(1.0, -ex));
+          MF_CUDA(cudaGetLastError());
+          md->trinv_tscale = std::scalbn(1.0, ex);
+          md->trinv_df = true;
+        }
+      }
+      if (rc) return rc;
+    } else {
+      (void)cudaGetLastError();
       md->Minv.release();
     }
   }
@@ -1594,6 +2027,89 @@ int mf_md_influence_matrix_cached(mf_md_t* md, double sigma, int null_mode, cons
 // major.  The subdomain work of the right-hand sides runs one after the other
 // on each subdomain's stream; the interface system is solved for all of them
 // in one pass over the inverse (or column by column on the LU factors).
+// The interface systems of nrhs right-hand sides stored one after the other
+// at vecs (n each), solved in place in the form selected at set-up; null-space
+// handling as md_rhs_nullspace / md_vector_zero_lastpoint (class_md.f90).
+static int md_interface_system(mf_md* md, int nrhs, double* vecs, cudaStream_t st) {
+  const long long n = md->topo.ninf;
+  int rc = MF_OK;
+  for (int r = 0; r < nrhs; ++r) {
+    if (md->null_mode == 1) k_remove_mean<<<1, 256, 0, st>>>(vecs + (size_t)r * n, (int)n);
+    if (md->null_mode >= 1) k_set_scalar<<<1, 1, 0, st>>>(vecs + (size_t)r * n, 0, 0.0);
+  }
+  if (md->inv_ok && md->iface_mode != MF_MD_IFACE_LU) {
+    const double* A = md->Minv.as<double>();
+    double* y = md->vec2.as<double>();
+    const unsigned blocks = nblk(n, kGemvRows), threads = 32 * kGemvRows;
+    if (nrhs == 1) k_gemm_rows<1><<<blocks, threads, 0, st>>>(A, vecs, y, (int)n);
+    if (nrhs == 2) k_gemm_rows<2><<<blocks, threads, 0, st>>>(A, vecs, y, (int)n);
+    if (nrhs == 3) k_gemm_rows<3><<<blocks, threads, 0, st>>>(A, vecs, y, (int)n);
+    if (nrhs == 4) k_gemm_rows<4><<<blocks, threads, 0, st>>>(A, vecs, y, (int)n);
+    MF_CUDA(cudaGetLastError());
+    MF_CUDA(cudaMemcpyAsync(vecs, y, sizeof(double) * n * nrhs, cudaMemcpyDeviceToDevice, st));
+  } else if (md->trinv_ok && md->trinv_df && md->iface_mode != MF_MD_IFACE_LU) {
+    // x = U^-1 (L^-1 (P x)) in double-float: the pivots gathered (FP64 copy
+    // for the unit diagonal) and split, the lower product into vecs, its
+    // result split, the upper product into vecs
+    const float2* T = reinterpret_cast<const float2*>(md->Minv.as<double>());
+    double* y = md->vec2.as<double>();
+    float2* xd = md->xdf.as<float2>();
+    double* us = md->unscale.as<double>();
+    const double ts = md->trinv_tscale;
+    const int* perm = md->perm.as<int>();
+    const unsigned blocks = nblk(n, kTmvRows);
+    k_df_prep<<<nrhs, 1024, 0, st>>>(vecs, perm, y, xd, us, (int)n);
+    switch (nrhs) {
+      case 1: k_trimv_rows_df<1, false><<<blocks, 512, 0, st>>>(T, xd, y, us, ts, vecs, (int)n); break;
+      case 2: k_trimv_rows_df<2, false><<<blocks, 512, 0, st>>>(T, xd, y, us, ts, vecs, (int)n); break;
+      case 3: k_trimv_rows_df<3, false><<<blocks, 512, 0, st>>>(T, xd, y, us, ts, vecs, (int)n); break;
+      default: k_trimv_rows_df<4, false><<<blocks, 512, 0, st>>>(T, xd, y, us, ts, vecs, (int)n); break;
+    }
+    k_df_prep<<<nrhs, 1024, 0, st>>>(vecs, nullptr, nullptr, xd, us, (int)n);
+    switch (nrhs) {
+      case 1: k_trimv_rows_df<1, true><<<blocks, 512, 0, st>>>(T, xd, nullptr, us, ts, vecs, (int)n); break;
+      case 2: k_trimv_rows_df<2, true><<<blocks, 512, 0, st>>>(T, xd, nullptr, us, ts, vecs, (int)n); break;
+      case 3: k_trimv_rows_df<3, true><<<blocks, 512, 0, st>>>(T, xd, nullptr, us, ts, vecs, (int)n); break;
+      default: k_trimv_rows_df<4, true><<<blocks, 512, 0, st>>>(T, xd, nullptr, us, ts, vecs, (int)n); break;
+    }
+    MF_CUDA(cudaGetLastError());
+  } else if (md->trinv_ok && md->iface_mode != MF_MD_IFACE_LU) {
+    // x = U^-1 (L^-1 (P x)): the pivots as a gather, then two row-parallel products
+    const double* T = md->Minv.as<double>();
+    double* y = md->vec2.as<double>();
+    for (int r = 0; r < nrhs; ++r)
+      k_permute<<<nblk(n, 256), 256, 0, st>>>(vecs + (size_t)r * n, md->perm.as<int>(), y + (size_t)r * n, (int)n);
+    const unsigned blocks = nblk(n, kTmvRows);
+    switch (nrhs) {
+      case 1: k_trimv_rows<1, false><<<blocks, 512, 0, st>>>(T, y, vecs, (int)n);
+              k_trimv_rows<1, true><<<blocks, 512, 0, st>>>(T, vecs, y, (int)n); break;
+      case 2: k_trimv_rows<2, false><<<blocks, 512, 0, st>>>(T, y, vecs, (int)n);
+              k_trimv_rows<2, true><<<blocks, 512, 0, st>>>(T, vecs, y, (int)n); break;
+      case 3: k_trimv_rows<3, false><<<blocks, 512, 0, st>>>(T, y, vecs, (int)n);
+              k_trimv_rows<3, true><<<blocks, 512, 0, st>>>(T, vecs, y, (int)n); break;
+      default: k_trimv_rows<4, false><<<blocks, 512, 0, st>>>(T, y, vecs, (int)n);
+               k_trimv_rows<4, true><<<blocks, 512, 0, st>>>(T, vecs, y, (int)n); break;
+    }
+    MF_CUDA(cudaGetLastError());
+    MF_CUDA(cudaMemcpyAsync(vecs, y, sizeof(double) * n * nrhs, cudaMemcpyDeviceToDevice, st));
+  } else {
+    bool done = false;
+    if (md->tri_form != 1) {
+      if (nrhs == 1) rc = md_lu_solve_persist<1>(md, vecs, st, &done);
+      if (nrhs == 2) rc = md_lu_solve_persist<2>(md, vecs, st, &done);
+      if (nrhs == 3) rc = md_lu_solve_persist<3>(md, vecs, st, &done);
+      if (nrhs == 4) rc = md_lu_solve_persist<4>(md, vecs, st, &done);
+      if (rc) return rc;
+    }
+    for (int r = 0; r < nrhs && !done; ++r)
+      if ((rc = md_lu_solve(md, vecs + (size_t)r * n, st))) return rc;
+  }
+  if (md->null_mode == 1)
+    for (int r = 0; r < nrhs; ++r) k_remove_mean<<<1, 256, 0, st>>>(vecs + (size_t)r * n, (int)n);
+  MF_CUDA(cudaGetLastError());
+  return MF_OK;
+}
+
 static int md_solve_impl(mf_md_t* md, int nrhs, const double* const* g, double* const* u,
                          const double* const* bcx, const double* const* bcy, const double* const* bcz,
                          void* stream) {
@@ -1673,37 +2189,9 @@ static int md_solve_impl(mf_md_t* md, int nrhs, const double* const* g, double* 
         }
   }
   if ((rc = join())) return rc;
-  // 2. interface systems (null-space handling as md_rhs_nullspace / md_vector_zero_lastpoint)
+  // 2. interface systems
   double* vecs = md->vec.as<double>();
-  for (int r = 0; r < nrhs; ++r) {
-    if (md->null_mode == 1) k_remove_mean<<<1, 256, 0, st>>>(vecs + (size_t)r * n, (int)n);
-    if (md->null_mode >= 1) k_set_scalar<<<1, 1, 0, st>>>(vecs + (size_t)r * n, 0, 0.0);
-  }
-  if (md->inv_ok && md->iface_mode != MF_MD_IFACE_LU) {
-    const double* A = md->Minv.as<double>();
-    double* y = md->vec2.as<double>();
-    const unsigned blocks = nblk(n, kGemvRows), threads = 32 * kGemvRows;
-    if (nrhs == 1) k_gemm_rows<1><<<blocks, threads, 0, st>>>(A, vecs, y, (int)n);
-    if (nrhs == 2) k_gemm_rows<2><<<blocks, threads, 0, st>>>(A, vecs, y, (int)n);
-    if (nrhs == 3) k_gemm_rows<3><<<blocks, threads, 0, st>>>(A, vecs, y, (int)n);
-    if (nrhs == 4) k_gemm_rows<4><<<blocks, threads, 0, st>>>(A, vecs, y, (int)n);
-    MF_CUDA(cudaGetLastError());
-    MF_CUDA(cudaMemcpyAsync(vecs, y, sizeof(double) * n * nrhs, cudaMemcpyDeviceToDevice, st));
-  } else {
-    bool done = false;
-    if (md->tri_form != 1) {
-      if (nrhs == 1) rc = md_lu_solve_persist<1>(md, vecs, st, &done);
-      if (nrhs == 2) rc = md_lu_solve_persist<2>(md, vecs, st, &done);
-      if (nrhs == 3) rc = md_lu_solve_persist<3>(md, vecs, st, &done);
-      if (nrhs == 4) rc = md_lu_solve_persist<4>(md, vecs, st, &done);
-      if (rc) return rc;
-    }
-    for (int r = 0; r < nrhs && !done; ++r)
-      if ((rc = md_lu_solve(md, vecs + (size_t)r * n, st))) return rc;
-  }
-  if (md->null_mode == 1)
-    for (int r = 0; r < nrhs; ++r) k_remove_mean<<<1, 256, 0, st>>>(vecs + (size_t)r * n, (int)n);
-  MF_CUDA(cudaGetLastError());
+  if ((rc = md_interface_system(md, nrhs, vecs, st))) return rc;
   // 3. final solves with the interface values
   if ((rc = fork())) return rc;
   for (int r = 0; r < nrhs; ++r) {
@@ -1743,6 +2231,22 @@ int mf_md_set_assembly(mf_md_t* md, int mode) {
   return MF_OK;
 }
 
+int mf_md_interface_solve(mf_md_t* md, int nrhs, const double* rhs, double* sol, void* stream) {
+  if (!md || !rhs || !sol || nrhs < 1 || nrhs > kMdMaxRhs)
+    return set_error(MF_ERR_ARG, "mf_md_interface_solve: bad arguments");
+  if (!md->factored) return set_error(MF_ERR_ARG, "mf_md_interface_solve: influence matrix not set");
+  if (!is_device_ptr(rhs) || !is_device_ptr(sol))
+    return set_error(MF_ERR_ARG, "mf_md_interface_solve: device pointers only");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const size_t bytes = sizeof(double) * (size_t)md->topo.ninf * nrhs;
+  double* vecs = md->vec.as<double>();
+  MF_CUDA(cudaMemcpyAsync(vecs, rhs, bytes, cudaMemcpyDeviceToDevice, st));
+  int rc = md_interface_system(md, nrhs, vecs, st);
+  if (rc) return rc;
+  MF_CUDA(cudaMemcpyAsync(sol, vecs, bytes, cudaMemcpyDeviceToDevice, st));
+  return MF_OK;
+}
+
 int mf_md_set_precision(mf_md_t* md, int precision, int refine) {
   if (!md || (precision != MF_PREC_FP64 && precision != MF_PREC_SPLIT_BF16 && precision != MF_PREC_3XTF32))
     return set_error(MF_ERR_ARG, "mf_md_set_precision: bad arguments");
@@ -1752,9 +2256,20 @@ int mf_md_set_precision(mf_md_t* md, int precision, int refine) {
 }
 
 int mf_md_set_interface_solve(mf_md_t* md, int mode) {
-  if (!md || (mode != MF_MD_IFACE_AUTO && mode != MF_MD_IFACE_LU && mode != MF_MD_IFACE_INVERSE))
+  if (!md || (mode != MF_MD_IFACE_AUTO && mode != MF_MD_IFACE_LU && mode != MF_MD_IFACE_INVERSE &&
+              mode != MF_MD_IFACE_TRIANGULAR_INVERSE && mode != MF_MD_IFACE_TRIANGULAR_INVERSE_FP64))
     return set_error(MF_ERR_ARG, "mf_md_set_interface_solve: bad arguments");
   md->iface_mode = mode;
+  return MF_OK;
+}
+
+int mf_md_interface_form(const mf_md_t* md, int* form) {
+  if (!md || !form) return set_error(MF_ERR_ARG, "mf_md_interface_form: null argument");
+  if (!md->factored) return set_error(MF_ERR_ARG, "mf_md_interface_form: influence matrix not set");
+  *form = MF_MD_IFACE_LU;
+  if (md->iface_mode != MF_MD_IFACE_LU && md->inv_ok) *form = MF_MD_IFACE_INVERSE;
+  if (md->iface_mode != MF_MD_IFACE_LU && md->trinv_ok)
+    *form = md->trinv_df ? MF_MD_IFACE_TRIANGULAR_INVERSE : MF_MD_IFACE_TRIANGULAR_INVERSE_FP64;
   return MF_OK;
 }
 

@@ -51,6 +51,8 @@ MF_RESID_FP64_LINE = 2
 MD_IFACE_AUTO = 0
 MD_IFACE_LU = 1
 MD_IFACE_INVERSE = 2
+MD_IFACE_TRIANGULAR_INVERSE = 3
+MD_IFACE_TRIANGULAR_INVERSE_FP64 = 4
 MD_TRI_PERSISTENT = 0
 MD_TRI_STEPS = 1
 MD_ASSEMBLY_EIGEN = 0
@@ -192,6 +194,8 @@ _PROTOS = {
     "mf_navier_subiterations": [_P, _IP],
     "mf_navier_set_les_network": [_P, _P],
     "mf_md_set_triangular_form": [_P, _I],
+    "mf_md_interface_form": [_P, _P],
+    "mf_md_interface_solve": [_P, _I, _P, _P, _P],
     "mf_md_device_status": [_P],
     "mf_navier_create_md": [_IP, _IP, ctypes.POINTER(_DP), _IP, ctypes.POINTER(_DP), _IP, ctypes.POINTER(_DP), _IP,
                             _P, ctypes.POINTER(_P)],
@@ -682,9 +686,35 @@ class MultiDomain:
         _check(_lib.mf_md_set_assembly(self._h, int(mode)))
 
     def set_interface_solve(self, mode):
-        """MD_IFACE_AUTO (inverse when small enough), MD_IFACE_LU or
-        MD_IFACE_INVERSE (the inverse at any size that fits)."""
+        """MD_IFACE_AUTO (the inverse up to 12,000 unknowns, the inverted
+        LU factors above), MD_IFACE_LU, MD_IFACE_INVERSE (the inverse at any
+        size that fits), MD_IFACE_TRIANGULAR_INVERSE (the inverted factors
+        at any size that fits, double-float products on the FP32 pipe) or
+        MD_IFACE_TRIANGULAR_INVERSE_FP64 (the same with FP64 entries and
+        FMAs)."""
         _check(_lib.mf_md_set_interface_solve(self._h, int(mode)))
+
+    def interface_solve(self, rhs, out=None, stream=None):
+        """md_solve: the interface system alone for a (ninf,) or (nrhs, ninf)
+        FP64 device tensor of right-hand sides (nrhs <= 4); returns the
+        solutions in the same shape."""
+        nrhs = 1 if rhs.dim() == 1 else rhs.shape[0]
+        if out is None:
+            out = rhs.new_empty(rhs.shape)
+        for a in (rhs, out):
+            if a.dtype.__repr__() != "torch.float64" or not a.is_contiguous() or a.shape != rhs.shape:
+                raise ValueError("interface_solve: contiguous float64 tensors of one shape expected")
+        _check(_lib.mf_md_interface_solve(self._h, int(nrhs), ctypes.c_void_p(rhs.data_ptr()),
+                                          ctypes.c_void_p(out.data_ptr()), _stream(stream)))
+        return out
+
+    def interface_form(self):
+        """The form the next solve takes: MD_IFACE_INVERSE,
+        MD_IFACE_TRIANGULAR_INVERSE, MD_IFACE_TRIANGULAR_INVERSE_FP64 or
+        MD_IFACE_LU."""
+        f = ctypes.c_int()
+        _check(_lib.mf_md_interface_form(self._h, ctypes.byref(f)))
+        return f.value
 
     def set_triangular_form(self, form):
         """MD_TRI_PERSISTENT (default: one cooperative launch per triangle)

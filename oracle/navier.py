@@ -121,6 +121,13 @@ def quad_weights(gx, gy, gz):
     return np.where(nb <= 1, W, 0.0)
 
 
+def _ratio(a, b):
+    """a / b in IEEE arithmetic (inf or NaN for b = 0, as the reference's
+    Fortran division gives when there is no manufactured solution)."""
+    with np.errstate(divide="ignore", invalid="ignore"):
+        return float(np.float64(a) / np.float64(b))
+
+
 class Navier:
     """Single-domain state and time step; fields are (nx, ny, nz) arrays."""
 
@@ -431,7 +438,7 @@ class Navier:
         err = self.norme(np.sqrt((ue[0] - self.u[cur]) ** 2 + (ue[1] - self.v[cur]) ** 2
                                  + (ue[2] - self.w[cur]) ** 2))
         self.err_vts_t += err ** 2 * self.ts
-        out["vel"] = (err, err / ref, np.sqrt(self.err_vts_t))
+        out["vel"] = (err, _ratio(err, ref), np.sqrt(self.err_vts_t))
         ref = self.integrale(ones)
         mean = self.integrale(self.p[cur])
         self.p[cur] = self.p[cur] - mean / ref
@@ -439,7 +446,7 @@ class Navier:
         refp = self.norme(pex)
         err = self.norme(self.p[cur] - pex)
         self.err_pre_t += err ** 2 * self.ts
-        out["pres"] = (err, err / refp, np.sqrt(self.err_pre_t))
+        out["pres"] = (err, _ratio(err, refp), np.sqrt(self.err_pre_t))
         reft = self.integrale(ones)
         ek = 0.5 * (self.norme(self.u[cur]) ** 2 + self.norme(self.v[cur]) ** 2 + self.norme(self.w[cur]))
         out["kinetic"] = ek / reft
@@ -590,7 +597,7 @@ class NavierMD:
         err = self.sum_norme([np.sqrt((e[0] - d.u[cur]) ** 2 + (e[1] - d.v[cur]) ** 2 + (e[2] - d.w[cur]) ** 2)
                               for d, e in zip(doms, ue)])
         self.err_vts_t += err ** 2 * self.ts
-        out["vel"] = (err, err / ref, np.sqrt(self.err_vts_t))
+        out["vel"] = (err, _ratio(err, ref), np.sqrt(self.err_vts_t))
         ref = self.sum_integrale(ones)
         mean = self.sum_integrale([d.p[cur] for d in doms])
         for d in doms:
@@ -600,7 +607,7 @@ class NavierMD:
         refp = self.sum_norme(pex)
         err = self.sum_norme([d.p[cur] - x for d, x in zip(doms, pex)])
         self.err_pre_t += err ** 2 * self.ts
-        out["pres"] = (err, err / refp, np.sqrt(self.err_pre_t))
+        out["pres"] = (err, _ratio(err, refp), np.sqrt(self.err_pre_t))
         reft = ref
         nu_, nv_, nw_ = (self.sum_norme([getattr(d, a)[cur] for d in doms]) for a in "uvw")
         out["kinetic"] = 0.5 * (nu_ ** 2 + nv_ ** 2 + nw_) / reft

@@ -56,5 +56,12 @@ def test_argument_errors_need_no_device(mf):
     assert lib.mf_md_solve(None, arr, arr, arr, arr, arr, None) == mf.MF_ERR_ARG
     assert lib.mf_md_set_precision(None, mf.MF_PREC_3XTF32, 1) == mf.MF_ERR_ARG
     assert lib.mf_md_set_interface_solve(None, mf.MD_IFACE_INVERSE) == mf.MF_ERR_ARG
+    assert lib.mf_md_set_interface_solve(None, mf.MD_IFACE_TRIANGULAR_INVERSE) == mf.MF_ERR_ARG
+    assert lib.mf_md_set_interface_solve(None, mf.MD_IFACE_TRIANGULAR_INVERSE_FP64) == mf.MF_ERR_ARG
+    lib.mf_md_interface_form.argtypes = [P, P]
+    assert lib.mf_md_interface_form(None, None) == mf.MF_ERR_ARG
+    lib.mf_md_interface_solve.argtypes = [P, ctypes.c_int, P, P, P]
+    for nrhs in (0, 1, 5):
+        assert lib.mf_md_interface_solve(None, nrhs, None, None, None) == mf.MF_ERR_ARG
     for mode in (mf.MF_RESID_FF, mf.MF_RESID_FP64, mf.MF_RESID_FP64_LINE):
         assert lib.mf_solver3d_set_residual(None, mode) == mf.MF_ERR_ARG

@@ -2,8 +2,9 @@
 class_field.f90:1295-1388) against the FP64 oracle, through the C ABI.
 Tolerance: max |gpu - oracle| <= 1e-11 * max |oracle| per subdomain field
 (the interface solve adds an LU on top of the 1e-12 subdomain solves).
-Both interface-solve forms are checked: the inverse formed at set-up (the
-default for small systems) and the triangular solves on the LU factors."""
+The three interface-solve forms are checked: the inverse formed at set-up
+(the default for small systems), the inverted LU factors (the default for
+large ones) and the triangular solves on the LU factors."""
 import numpy as np
 import pytest
 
@@ -101,16 +102,20 @@ def test_md_pure_neumann_null_space(mf, gpu, null):
     assert err < 1e-10 and lerr < 1e-10, (err, lerr)
 
 
+@pytest.mark.parametrize("iface", ["MD_IFACE_LU", "MD_IFACE_TRIANGULAR_INVERSE",
+                                   "MD_IFACE_TRIANGULAR_INVERSE_FP64"])
 @pytest.mark.parametrize("nd,periods", [((2, 2, 2), (0, 0, 0)), ((2, 1, 1), (1, 0, 0))])
-def test_md_triangular_interface_solve(mf, gpu, nd, periods):
-    err, lerr, _, _ = run(mf, nd, periods, (11, 11, 11), -3.0, iface=mf.MD_IFACE_LU)
+def test_md_triangular_interface_solve(mf, gpu, nd, periods, iface):
+    err, lerr, _, _ = run(mf, nd, periods, (11, 11, 11), -3.0, iface=getattr(mf, iface))
     assert err < 1e-11 and lerr < 1e-11, (err, lerr)
 
 
+@pytest.mark.parametrize("iface", ["MD_IFACE_LU", "MD_IFACE_TRIANGULAR_INVERSE",
+                                   "MD_IFACE_TRIANGULAR_INVERSE_FP64"])
 @pytest.mark.parametrize("null", [1, 2])
-def test_md_null_space_triangular_interface_solve(mf, gpu, null):
+def test_md_null_space_triangular_interface_solve(mf, gpu, null, iface):
     err, lerr, _, _ = run(mf, (2, 1, 1), (0, 0, 0), (11, 11, 11), 0.0, bct=(2,) * 6, null=null,
-                          iface=mf.MD_IFACE_LU)
+                          iface=getattr(mf, iface))
     assert err < 1e-10 and lerr < 1e-10, (err, lerr)
 
 
@@ -134,7 +139,8 @@ def test_md_mixed_subdomain_solves_forced_inverse(mf, gpu, nd, periods):
     assert err < 1e-10 and lerr < 1e-10, (err, lerr)
 
 
-@pytest.mark.parametrize("iface", ["MD_IFACE_INVERSE", "MD_IFACE_LU"])
+@pytest.mark.parametrize("iface", ["MD_IFACE_INVERSE", "MD_IFACE_LU", "MD_IFACE_TRIANGULAR_INVERSE",
+                                   "MD_IFACE_TRIANGULAR_INVERSE_FP64"])
 def test_md_solve_many_equals_single_solves(mf, gpu, iface):
     """Three right-hand sides in one mf_md_solve_many call (subdomain work per
     right-hand side in turn, the interface systems together) give the three
@@ -313,3 +319,72 @@ def test_persistent_triangular_solves(mf, gpu, sigma, bct, null):
             a, b = outs[mf.MD_TRI_PERSISTENT][q][c], outs[mf.MD_TRI_STEPS][q][c]
             assert float((a - b).abs().max() / b.abs().max()) < 1e-11
     torch.cuda.synchronize()
+
+
+@pytest.mark.parametrize("sigma,bct,null", [(-1e3, (1,) * 6, 0), (0.0, (2,) * 6, 1)])
+def test_inverted_factors_large_system(mf, gpu, sigma, bct, null):
+    """Above 12,000 unknowns the default interface form is the inverted LU
+    factors (trtri at set-up, two row-parallel double-float products per
+    solve): on the 18,252-unknown system of 2 x 2 x 2 slabs of 41 nodes it
+    gives the triangular solves' interface values and fields to 1e-11, for
+    one and for three right-hand sides, velocity-like and pressure-like
+    operators."""
+    import torch
+    grids = tuple(slabs(2, 41) for _ in range(3))
+    dev = mf.MultiDomain((2, 2, 2), (0, 0, 0), *grids, bct)
+    dev.influence_matrix_set(sigma, null)
+    assert dev.ninf() > 12000
+    assert dev.interface_form() == mf.MD_IFACE_TRIANGULAR_INVERSE
+    g, u, bc = _random_solve(mf, dev, 11)
+    lam, fields = {}, {}
+    for form in (mf.MD_IFACE_AUTO, mf.MD_IFACE_LU):
+        dev.set_interface_solve(form)
+        dev.solve(g, u, bc)
+        lam[form] = dev.interface()
+        fields[form] = {c: u[c].clone() for c in u}
+    assert dev.interface_form() == mf.MD_IFACE_LU
+    assert max_rel(lam[mf.MD_IFACE_AUTO], lam[mf.MD_IFACE_LU]) < 1e-11
+    for c in u:
+        a, b = fields[mf.MD_IFACE_AUTO][c], fields[mf.MD_IFACE_LU][c]
+        assert float((a - b).abs().max() / b.abs().max()) < 1e-11
+    sets = [_random_solve(mf, dev, 20 + q) for q in range(3)]
+    outs = {}
+    for form in (mf.MD_IFACE_AUTO, mf.MD_IFACE_LU):
+        dev.set_interface_solve(form)
+        dev.solve_many([s[0] for s in sets], [s[1] for s in sets], [s[2] for s in sets])
+        outs[form] = [{c: s[1][c].clone() for c in s[1]} for s in sets]
+    for q in range(3):
+        for c in sets[q][1]:
+            a, b = outs[mf.MD_IFACE_AUTO][q][c], outs[mf.MD_IFACE_LU][q][c]
+            assert float((a - b).abs().max() / b.abs().max()) < 1e-11
+    dev.device_status()
+    torch.cuda.synchronize()
+
+
+@pytest.mark.parametrize("null", [0, 1, 2])
+@pytest.mark.parametrize("iface", ["MD_IFACE_INVERSE", "MD_IFACE_LU", "MD_IFACE_TRIANGULAR_INVERSE",
+                                   "MD_IFACE_TRIANGULAR_INVERSE_FP64"])
+def test_interface_solve_matches_oracle(mf, gpu, iface, null):
+    """md_solve alone (mf_md_interface_solve): the interface system of a
+    2 x 2 x 1 decomposition for one and for three random right-hand sides,
+    in each form, against the oracle's dense solve of its own influence
+    matrix (with the same null-space handling) to 1e-10."""
+    import torch
+    nd, periods = (2, 2, 1), (0, 0, 0)
+    bct = (2,) * 6 if null else (1,) * 6
+    sigma = 0.0 if null else -3.0
+    grids = tuple(slabs(nd[l], 11) for l in range(3))
+    ref = omd.MultiDomain(nd, periods, *grids, bct)
+    ref.influence_matrix(sigma, null)
+    dev = mf.MultiDomain(nd, periods, *grids, bct)
+    dev.set_interface_solve(getattr(mf, iface))
+    dev.influence_matrix_set(sigma, null)
+    assert dev.interface_form() == getattr(mf, iface)
+    rng = np.random.default_rng(5 + null)
+    rhs = rng.standard_normal((3, dev.ninf()))
+    want = np.stack([ref.interface_solve(r) for r in rhs])
+    one = dev.interface_solve(torch.from_numpy(rhs[0].copy()).cuda())
+    three = dev.interface_solve(torch.from_numpy(rhs).cuda())
+    assert max_rel(one.cpu().numpy(), want[0]) < 1e-10
+    for q in range(3):
+        assert max_rel(three[q].cpu().numpy(), want[q]) < 1e-10, q

@@ -274,6 +274,9 @@ MD_GRIDS = {
 MD_CASES = {
     "2x1x1_defaults": ("2x1x1", dict(ts=1e-2, reynolds=50.0)),
     "periodic_xz_pt2": ("periodic_xz", dict(ts=1e-2, reynolds=50.0, pt=2)),
+    # the channel rows' settings: reference defaults (pt 1, flow-rate term),
+    # no manufactured sources, Re 180, ts 1e-3
+    "periodic_xz_channel": ("periodic_xz", dict(ts=1e-3, reynolds=180.0, nmodes=0)),
     "2x1x2_periodic_x_pt3_les_sub": ("2x1x2_periodic_x", dict(ts=1e-2, reynolds=100.0, pt=3, les_type=1,
                                                                les_c=0.1, nsubite=2)),
 }
