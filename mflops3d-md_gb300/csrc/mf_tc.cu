@@ -313,12 +313,17 @@ __global__ void __launch_bounds__(Cfg<kTf32>::kThreads, 1)
               // and lo*hi into the small-product sum
               const uint32_t dh = d + (uint32_t)((c < nk / 2 ? 1 : 2) * NW);
               const uint32_t acc_h = (c == 0 || c == nk / 2) ? 0u : 1u, acc_l = c == 0 ? 0u : 1u;
+              // the small-product sum takes the four hi*lo products of the
+              // stage, then its four lo*hi products (the order of the wide
+              // form, which issues the hi products before the lo operand is
+              // converted)
 #pragma unroll
               for (int kk = 0; kk < 4; ++kk) {
                 mma_tf32_ta(dh, ahi + 8 * kk, bh + 2 * kk, idesc, kk ? 1u : acc_h);
                 mma_tf32_ta(d, ahi + 8 * kk, bl + 2 * kk, idesc, kk ? 1u : acc_l);
-                mma_tf32_ta(d, alo + 8 * kk, bh + 2 * kk, idesc, 1u);
               }
+#pragma unroll
+              for (int kk = 0; kk < 4; ++kk) mma_tf32_ta(d, alo + 8 * kk, bh + 2 * kk, idesc, 1u);
               mma_commit(&op_free[o]);
               if (++o == kOpSlots) {
                 o = 0;
@@ -595,24 +600,27 @@ __global__ void __launch_bounds__(kWideThreads, 1)
             fence_after();
           }
           if (!(ok = mbar_wait(&full_bar[s], ph, err))) break;
+          fence_after();
           const uint64_t bh = b0 + (uint64_t)(s * stage_step), bl = bh + lo_off;
           const uint64_t ah = a0 + (uint64_t)(s * stage_step);
           const uint32_t dh = tmem + (c < half ? kWideH1 : kWideH2), ds = tmem + kWideS;
           const uint32_t acc_h = (c == 0 || c == half) ? 0u : 1u, acc_s = c == 0 ? 0u : 1u;
-          // two half-stages of 16 K values, each in its own operand slot
+          // the hi*hi and hi*lo products of the stage need only the landed
+          // tile (hi: the FP32 tile itself, read as TF32 by the tensor core),
+          // so they go first and keep the tensor pipe busy while the
+          // converters form the lo operand
+#pragma unroll
+          for (int k8 = 0; k8 < 4; ++k8) {
+            mma<true>(dh, ah + 2 * k8, bh + 2 * k8, idesc, k8 ? 1u : acc_h);
+            mma<true>(ds, ah + 2 * k8, bl + 2 * k8, idesc, k8 ? 1u : acc_s);
+          }
+          // then lo*hi, per half-stage of 16 K values in its operand slot
           for (int hs = 0; hs < 2 && ok; ++hs) {
             if (!(ok = mbar_wait(&cvt_bar[o], pho, err))) break;
             fence_after();
             const uint32_t alo = tmem + kWideSlot + (uint32_t)(kWideSlotCols * o);
 #pragma unroll
-            for (int kk = 0; kk < 2; ++kk) {
-              const int k8 = 2 * hs + kk;
-              const bool lead = hs == 0 && kk == 0;  // first K step of this chunk
-              // hi: the landed FP32 tile itself, read as TF32 by the tensor core
-              mma<true>(dh, ah + 2 * k8, bh + 2 * k8, idesc, lead ? acc_h : 1u);
-              mma<true>(ds, ah + 2 * k8, bl + 2 * k8, idesc, lead ? acc_s : 1u);
-              mma_tf32_ta(ds, alo + 8 * kk, bh + 2 * k8, idesc, 1u);
-            }
+            for (int kk = 0; kk < 2; ++kk) mma_tf32_ta(ds, alo + 8 * kk, bh + 2 * (2 * hs + kk), idesc, 1u);
             mma_commit(&op_free[o]);
             if (++o == kWideSlots) {
               o = 0;
