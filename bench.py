@@ -59,12 +59,14 @@ def parse():
     ap.add_argument("--precision", default="auto", choices=["auto", "bf16", "tf32"],
                     help="transform format; auto times both and reports the faster")
     ap.add_argument("--probe", default=None,
-                    choices=["bf16", "tf32", "fp64", "der", "filter", "les_mlp", "mlp_train", "navier", "channel"],
+                    choices=["bf16", "tf32", "fp64", "der", "filter", "les_mlp", "mlp_train", "navier", "channel",
+                             "interface"],
                     help="profiling aid: run two untimed solves of the workload in this format "
                          "(refinement steps from --refine), or two untimed launches of one row "
                          "(derivative sweeps at 257^3, the 384 -> 96 filter, the learned viscosity "
                          "at 160^3, a training step on 65,536 points, six Navier-Stokes steps at "
-                         "128x129x128), and exit")
+                         "128x129x128, multidomain interface solves with the inverted factors at "
+                         "18,252 unknowns), and exit")
     ap.add_argument("--refine", type=int, default=1)
     ap.add_argument("--tf32-plan", type=int, default=0, choices=[0, 1, 2],
                     help="3xTF32 transform plan: 0 default, 1 64-column slices (matrix resident), "
@@ -350,6 +352,34 @@ def run_gb300(args, rank, world, dist):
     resid_line["rel_l2_vs_fp64_gpu"] = err_vs_plain()
     sc.set_residual(mf.MF_RESID_FP64)
 
+    # the launch-shape autotuner: with mode 1 the first solve measures the
+    # candidates per shape (3xTF32 slice width, FP64 transform tiles) on this
+    # stream; the decisions and the tuned solve's time are recorded, then the
+    # headline runs with the built-in choices as before
+    mf.tune(clear=True)
+    mf.tune(mode=1)
+    for _ in range(4):
+        mixed()
+    tuned_ms = statistics.median(timed(mixed, 5))
+    kinds = {0: ("fp64_transform_tile", {0: "32-wide", 1: "64-wide"}),
+             1: ("x_line_derivative", {0: "staged", 1: "strided"}),
+             2: ("tf32_transform_slices", {0: "64-column, matrix resident", 1: "128-column, matrix streamed"})}
+    decisions = []
+    with tempfile.TemporaryDirectory() as td:
+        path = os.path.join(td, "tune.txt")
+        mf.tune(save=path)
+        for ln in open(path):
+            if ln.startswith("#"):
+                continue
+            kind, a, b, c, d, choice = (int(v) for v in ln.split())
+            name, labels = kinds.get(kind, ("kind%d" % kind, {}))
+            decisions.append({"kind": name, "shape": [a, b, c, d], "choice": labels.get(choice, choice)})
+    mf.tune(mode=0)
+    mf.tune(clear=True)
+    autotune = {"tuned_ms_per_solve": tuned_ms, "decisions": decisions,
+                "note": "mf_tune_set(1): candidates timed with CUDA events on first use per shape; "
+                        "identical results whichever is chosen"}
+
     # clock sampler first, so that its samples cover the timed region; the
     # warm-up runs at least W steps and at least 0.3 s
     clocks = ClockSampler(local)
@@ -550,6 +580,7 @@ def run_gb300(args, rank, world, dist):
         "eager_ms_per_step": sum(eager_ms) / args.steps,
         "residual_double_fp32_sweeps": resid_ff,
         "residual_fp64_sweeps_one_thread_per_line": resid_line,
+        "autotune": autotune,
         "formats": {k: {"precision": names[k], "refine_steps": c["refine"],
                         "ms_per_solve": c["ms"], "solves_per_s": 1e3 / c["ms"],
                         "rel_l2_by_refine_steps": {str(r): v for r, v in c["errs"].items()}}
@@ -1141,6 +1172,21 @@ def run_row_probe(args):
             nav.step()
         torch.cuda.synchronize()
         torch.cuda.cudart().cudaProfilerStop()
+    elif args.probe == "interface":
+        # the interface system alone (md_solve) with the inverted LU factors
+        # (double-float products) on 2 x 2 x 2 slabs of 41 tanh(1.0) nodes,
+        # 18,252 unknowns (2.7 GB of factors): two solves of one right-hand
+        # side, then two of three
+        edges = np.linspace(0.0, 1.0, 3)
+        gs = [mesh.tanh_grid(41, 1.0, edges[q], edges[q + 1]) for q in range(2)]
+        md = mf.MultiDomain((2, 2, 2), (0, 0, 0), gs, gs, gs, (1,) * 6, 6)
+        md.influence_matrix_set(-1e3, 0)
+        gen = torch.Generator("cuda").manual_seed(5)
+        iv = torch.randn(3, md.ninf(), dtype=torch.float64, device="cuda", generator=gen)
+        for k in (1, 1, 3, 3):
+            md.interface_solve(iv[:k])
+        torch.cuda.synchronize()
+        md.close()
     elif args.probe == "les_mlp":
         shape = (160, 160, 160)
         g = mesh.uniform_grid(160)
@@ -1220,10 +1266,11 @@ def main():
             gen = torch.Generator("cuda").manual_seed(seed)
             return torch.rand(tuple(reversed(shape)), dtype=torch.float64, device="cuda",
                               generator=gen).permute(*reversed(range(len(shape))))
+        # FP64 subdomain solves, then 3xTF32 + 1 refinement; interface solves
+        # in the default form (the inverted LU factors at ~32k unknowns)
         row = navier_channel(mf, torch, 128, time_fn, field, steps=4)
-        row["tf32_subdomain_solves_inverse_interface"] = navier_channel(
-            mf, torch, 128, time_fn, field, steps=4, precision=mf.MF_PREC_3XTF32, refine=1,
-            md_interface=mf.MD_IFACE_INVERSE)
+        row["tf32_subdomain_solves"] = navier_channel(
+            mf, torch, 128, time_fn, field, steps=4, precision=mf.MF_PREC_3XTF32, refine=1)
         print(json.dumps({"navier_step_channel_periodic_xz_128x129x128": row}), flush=True)
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
