@@ -1043,10 +1043,20 @@ def md_config2(mf, torch, operators=("velocity", "pressure")):
             t_ms = timed(lambda: md.interface_solve(iv[:k]), 5)
             row["interface_ms_%d" % k] = t_ms
             row["interface_frac_of_hbm_%d" % k] = row["interface_bytes_per_solve"] / (t_ms * 1e-3) / 1e9 / hbm
-        x_default = md.interface_solve(iv).clone()
+        # the default form against the LU solves, into two distinct outputs
+        # filled with NaN beforehand (an output the call did not write would
+        # show as NaN, not as agreement)
+        x_default = torch.full_like(iv, float("nan"))
+        x_lu = torch.full_like(iv, float("nan"))
+        forms = [md.interface_form()]
+        row["interface_check_default_ms"] = timed(lambda: md.interface_solve(iv, out=x_default), 1)
         md.set_interface_solve(mf.MD_IFACE_LU)
-        x_lu = md.interface_solve(iv)
+        forms.append(md.interface_form())
+        row["interface_check_lu_ms"] = timed(lambda: md.interface_solve(iv, out=x_lu), 1)
+        row["interface_check_forms"] = [form_names[f] for f in forms]
+        torch.cuda.synchronize()
         row["interface_rel_diff_vs_lu"] = float((x_default - x_lu).abs().max() / x_lu.abs().max())
+        row["interface_lu_output_written"] = bool(torch.isfinite(x_lu).all()) and not torch.equal(x_lu, iv)
         for key, form in (("solve_ms_lu_persistent", mf.MD_TRI_PERSISTENT),
                           ("solve_ms_lu_block_steps", mf.MD_TRI_STEPS)):
             md.set_triangular_form(form)

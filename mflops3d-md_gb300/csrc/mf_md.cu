@@ -939,7 +939,27 @@ __global__ void __launch_bounds__(512) k_trimv_rows_df(const float2* __restrict_
       xs[r][cc] = cc < len ? X[(long long)r * n + c0 + cc] : zero2;
     }
     __syncthreads();
+    // columns where both rows are inside their ranges: all but the edges
+    const int fb = max(ba, bb), fe = min(ea, eb);
     for (; c < e; c += 128) {
+      if (!kAhead && c >= fb && c + 96 < fe) {
+        // every column of this step lies in both rows' ranges: no predicates
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          va[q] = rowa[c0 + c + 32 * q];
+          vb[q] = rowb[c0 + c + 32 * q];
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+#pragma unroll
+          for (int r = 0; r < K; ++r) {
+            const float2 xv = xs[r][c + 32 * q];
+            df_fma(sa[q & 1][r], va[q], xv);
+            df_fma(sb[q & 1][r], vb[q], xv);
+          }
+        }
+        continue;
+      }
       float2 na[4], nb[4];
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
