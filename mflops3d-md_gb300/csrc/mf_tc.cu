@@ -474,8 +474,8 @@ __global__ void __launch_bounds__(Cfg<kTf32>::kThreads, 1)
 // FP32 X tile (16 KB) and both B planes of the same 32 K values (2 x 16 KB);
 // B is 512 KB in all and stays in L2.  TMEM: the three accumulators of one
 // tile (h1 = hi*hi over the first half of K, h2 = over the second half,
-// s = hi*lo + lo*hi; 3 x 128 columns) and eight slots for the lo part of
-// the A operand (8 x 16 columns).  The hi part is the landed FP32 tile
+// s = hi*lo + lo*hi; 3 x 128 columns) and four slots for the lo part of
+// the A operand (4 x 32 columns, one stage each).  The hi part is the landed FP32 tile
 // itself (the tensor core reads FP32 as TF32 by ignoring the low mantissa
 // bits), so the hi*hi and hi*lo MMAs take A from shared memory and the
 // converter warps only form and store lo.  The accumulators are
@@ -493,10 +493,13 @@ constexpr uint32_t kWideTile = kBlockM * 128;          // 16 KB: 128 rows x 32 F
 constexpr uint32_t kWideStage = 3 * kWideTile;          // X tile + B hi + B lo
 constexpr uint32_t kWideSmem = kWideStages * kWideStage + 1024;
 constexpr uint32_t kWideH1 = 0, kWideH2 = 128, kWideS = 256, kWideSlot = 384;
-// eight operand slots of the lo parts of 16 K values: the converters may
-// run seven half-stages ahead of the MMAs
-constexpr int kWideSlots = 8;
-constexpr uint32_t kWideSlotCols = 16;
+// one operand slot per ring stage, each the lo part of that stage's 32 K
+// values.  A slot needs no barrier of its own: the converters write slot s
+// only after stage s has landed again, which the producer issued only after
+// the stage's previous use was released, and that release (empty_bar) waits
+// for the commit that follows the MMAs which read the slot
+constexpr int kWideSlots = kWideStages;
+constexpr uint32_t kWideSlotCols = 32;
 
 __global__ void __launch_bounds__(kWideThreads, 1)
     k_tc_tf32_wide(const __grid_constant__ CUtensorMap tx, const __grid_constant__ CUtensorMap tb_hi,
@@ -504,7 +507,7 @@ __global__ void __launch_bounds__(kWideThreads, 1)
                    int* err) {
   extern __shared__ uint8_t smem_raw[];
   __shared__ uint64_t full_bar[kWideStages], empty_bar[kWideStages];
-  __shared__ uint64_t cvt_bar[kWideSlots], op_free[kWideSlots];
+  __shared__ uint64_t cvt_bar[kWideSlots];
   __shared__ uint64_t acc_full, acc_free, h2_free;
   __shared__ uint32_t tmem_slot;
   __shared__ float s_lz[256];
@@ -528,10 +531,7 @@ __global__ void __launch_bounds__(kWideThreads, 1)
       // the converters read the X tile, the MMAs the B planes
       mbar_init(&empty_bar[s], kCvtThreads + 1);
     }
-    for (int o = 0; o < kWideSlots; ++o) {
-      mbar_init(&cvt_bar[o], kCvtThreads);
-      mbar_init(&op_free[o], 1);
-    }
+    for (int o = 0; o < kWideSlots; ++o) mbar_init(&cvt_bar[o], kCvtThreads);
     mbar_init(&acc_full, 1);
     mbar_init(&acc_free, kEpiThreads);  // s and h1 read
     mbar_init(&h2_free, kEpiThreads);   // h2 read
@@ -586,8 +586,8 @@ __global__ void __launch_bounds__(kWideThreads, 1)
       const uint64_t a0 = smem_desc(smem_u32(smem));
       const uint64_t b0 = smem_desc(smem_u32(smem + kWideTile));
       const uint32_t stage_step = kWideStage >> 4, lo_off = kWideTile >> 4;
-      int s = 0, o = 0, tc = 0;
-      uint32_t ph = 0, pho = 0;
+      int s = 0, tc = 0;  // ring stage = operand slot
+      uint32_t ph = 0;
       bool ok = true;
       for (int t = cta_rank; t < mtiles && ok; t += cta_count, ++tc) {
         const uint32_t prev = (uint32_t)(tc - 1) & 1u;
@@ -614,20 +614,14 @@ __global__ void __launch_bounds__(kWideThreads, 1)
             mma<true>(dh, ah + 2 * k8, bh + 2 * k8, idesc, k8 ? 1u : acc_h);
             mma<true>(ds, ah + 2 * k8, bl + 2 * k8, idesc, k8 ? 1u : acc_s);
           }
-          // then lo*hi, per half-stage of 16 K values in its operand slot
-          for (int hs = 0; hs < 2 && ok; ++hs) {
-            if (!(ok = mbar_wait(&cvt_bar[o], pho, err))) break;
-            fence_after();
-            const uint32_t alo = tmem + kWideSlot + (uint32_t)(kWideSlotCols * o);
+          // then lo*hi, from the stage's operand slot once converted
+          if (!(ok = mbar_wait(&cvt_bar[s], ph, err))) break;
+          fence_after();
+          {
+            const uint32_t alo = tmem + kWideSlot + (uint32_t)(kWideSlotCols * s);
 #pragma unroll
-            for (int kk = 0; kk < 2; ++kk) mma_tf32_ta(ds, alo + 8 * kk, bh + 2 * (2 * hs + kk), idesc, 1u);
-            mma_commit(&op_free[o]);
-            if (++o == kWideSlots) {
-              o = 0;
-              pho ^= 1u;
-            }
+            for (int k8 = 0; k8 < 4; ++k8) mma_tf32_ta(ds, alo + 8 * k8, bh + 2 * k8, idesc, 1u);
           }
-          if (!ok) break;
           mma_commit(&empty_bar[s]);
           if (++s == kWideStages) {
             s = 0;
@@ -692,8 +686,8 @@ __global__ void __launch_bounds__(kWideThreads, 1)
     // start of each (wider) ring stage
     const int row = 32 * (warp & 3) + lane;
     const uint32_t lane_base = static_cast<uint32_t>(32 * (warp & 3)) << 16;
-    int s = 0, o = 0, ih = 0;  // ring stage, operand slot, half-stages converted
-    uint32_t ph = 0, pho = 0;
+    int s = 0;  // ring stage = operand slot
+    uint32_t ph = 0;
     bool ok = true;
     for (int t = cta_rank; t < mtiles && ok; t += cta_count) {
       for (int c = 0; c < nk; ++c) {
@@ -713,22 +707,11 @@ __global__ void __launch_bounds__(kWideThreads, 1)
         mbar_arrive(&empty_bar[s]);
 #pragma unroll
         for (int x = 0; x < 32; ++x) lo[x] = tf32_lo(hi[x]);
-        // two half-stages, each into the next operand slot once the MMAs
-        // that read its previous contents have completed
-#pragma unroll
-        for (int hs = 0; hs < 2; ++hs) {
-          if (ih >= kWideSlots && !(ok = mbar_wait(&op_free[o], pho ^ 1u, err, 32))) break;
-          const uint32_t slot = tmem + lane_base + kWideSlot + (uint32_t)(kWideSlotCols * o);
-          tmem_store16(slot, lo + 16 * hs);
-          fence_before();
-          mbar_arrive(&cvt_bar[o]);
-          ++ih;
-          if (++o == kWideSlots) {
-            o = 0;
-            pho ^= 1u;
-          }
-        }
-        if (!ok) break;
+        // into this stage's operand slot (free: see kWideSlots)
+        fence_after();
+        tmem_store32(tmem + lane_base + kWideSlot + (uint32_t)(kWideSlotCols * s), lo);
+        fence_before();
+        mbar_arrive(&cvt_bar[s]);
         if (++s == kWideStages) {
           s = 0;
           ph ^= 1u;
