@@ -471,7 +471,9 @@ def run_gb300(args, rank, world, dist):
     t0 = time.perf_counter()
     many()
     e2e_dt = (time.perf_counter() - t0) / e2e_many
-    h2d = pin_rhs.nbytes + pin_solf.nbytes + sum(b.nbytes for b in pin_bc)
+    # uploads: the right-hand side, the boundary arrays and the 12 edge lines
+    # of the solution array (the solve writes every other entry of it)
+    h2d = pin_rhs.nbytes + sum(b.nbytes for b in pin_bc) + 8 * 4 * 3 * (n + 2)
     d2h = pin_solf.nbytes
 
     if rank != 0:

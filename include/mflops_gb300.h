@@ -15,6 +15,9 @@
  *  - Field pointers may be HOST or DEVICE memory; the library inspects each
  *    pointer.  Host pointers are staged through device buffers owned by the
  *    handle and the call returns after the result is back in host memory.
+ *    Of a host solution array (solve_3d's solf) only the 12 edge lines go
+ *    to the device: the solve writes its interior and faces, and the edges
+ *    come back unchanged, as in the reference.
  *    Device-pointer calls are asynchronous on `stream` (a cudaStream_t, NULL
  *    for the legacy default stream).
  *  - A handle may be used by one host thread at a time; distinct handles

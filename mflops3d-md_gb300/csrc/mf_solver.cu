@@ -2160,6 +2160,39 @@ int mf_solver3d_destroy(mf_solver3d_t* sc) {
 
 // Shared front end of the solve entry points: validates, stages host
 // pointers, runs `body` on device pointers, copies solf back.
+// Host solution array -> device staging buffer, edges only: of the
+// (n1+2)(n2+2)(n3+2) field a solve writes the interior (the last transform's
+// epilogue or k_finalize) and the face interiors (k_faces) before anything
+// reads them, and leaves the 12 edge lines (corners included) as they were,
+// as the reference's copy and boundary insert do.  So only the edges travel
+// to the device (4 (N1 + N2 + N3) values instead of N1 N2 N3); the download
+// of the whole array then returns the caller's edges unchanged.
+static int stage_edges(DevBuf& buf, const double* src, int N1, int N2, int N3, cudaStream_t st) {
+  const size_t e = sizeof(double);
+  const long long P = (long long)N1 * N2;
+  int rc;
+  if ((rc = buf.ensure((size_t)P * N3 * e))) return rc;
+  double* dst = buf.as<double>();
+  for (int k : {0, N3 - 1})
+    for (int j : {0, N2 - 1}) {  // x-edges: contiguous
+      const long long off = (long long)j * N1 + (long long)k * P;
+      MF_CUDA(cudaMemcpyAsync(dst + off, src + off, (size_t)N1 * e, cudaMemcpyDefault, st));
+    }
+  for (int k : {0, N3 - 1})
+    for (int i : {0, N1 - 1}) {  // y-edges: stride N1
+      const long long off = i + (long long)k * P;
+      MF_CUDA(cudaMemcpy2DAsync(dst + off, (size_t)N1 * e, src + off, (size_t)N1 * e, e, (size_t)N2,
+                                cudaMemcpyDefault, st));
+    }
+  for (int j : {0, N2 - 1})
+    for (int i : {0, N1 - 1}) {  // z-edges: stride N1 N2
+      const long long off = i + (long long)j * N1;
+      MF_CUDA(cudaMemcpy2DAsync(dst + off, (size_t)P * e, src + off, (size_t)P * e, e, (size_t)N3,
+                                cudaMemcpyDefault, st));
+    }
+  return MF_OK;
+}
+
 template <class Body>
 static int solve_front(mf_solver3d_t* sc, const double* rhs, double* solf, const double* bcx,
                        const double* bcy, const double* bcz, int n1, int n2, int n3, void* stream,
@@ -2194,7 +2227,7 @@ static int solve_front(mf_solver3d_t* sc, const double* rhs, double* solf, const
   double* s = solf;
   const bool host_solf = !is_device_ptr(solf);
   if (host_solf) {
-    if ((rc = stage_in(sc->st_solf, solf, sb, st))) return rc;
+    if ((rc = stage_edges(sc->st_solf, solf, n1 + 2, n2 + 2, n3 + 2, st))) return rc;
     s = sc->st_solf.as<double>();
     any_host = true;
   }
@@ -2294,7 +2327,11 @@ int mf_solve_3d_mixed_many(mf_solver3d_t* sc, int count, const double* const* rh
       MF_CUDA(cudaStreamWaitEvent(sc->cin, sc->out_done[q], 0));
     }
     MF_CUDA(cudaMemcpyAsync(sc->pipe_rhs[q].ptr, rhs[b], rb, cudaMemcpyDefault, sc->cin));
-    MF_CUDA(cudaMemcpyAsync(sc->pipe_solf[q].ptr, solf[b], sb, cudaMemcpyDefault, sc->cin));
+    if (is_device_ptr(solf[b])) {
+      MF_CUDA(cudaMemcpyAsync(sc->pipe_solf[q].ptr, solf[b], sb, cudaMemcpyDefault, sc->cin));
+    } else if ((rc = stage_edges(sc->pipe_solf[q], solf[b], n1 + 2, n2 + 2, n3 + 2, sc->cin))) {
+      return rc;
+    }
     const double* bcs[3];
     for (int a = 0; a < 3; ++a) {
       MF_CUDA(cudaMemcpyAsync(sc->pipe_bc[q][a].ptr, bsrc[a][b], bb[a], cudaMemcpyDefault, sc->cin));

@@ -190,7 +190,9 @@ def test_mixed_rejects_axes_longer_than_256(mf, gpu):
 @pytest.mark.parametrize("prec_name,refine", [("MF_PREC_FP64", -1), ("MF_PREC_3XTF32", 1)])
 def test_many_problems_equal_single_calls(mf, gpu, prec_name, refine):
     """mf_solve_3d_mixed_many (uploads/downloads overlapping the solves) gives
-    each problem exactly the result of a single call, host arrays in and out."""
+    each problem exactly the result of a single call, host arrays in and out,
+    and of the same call on device arrays; the host paths upload only the
+    edges of the solution array, which come back as they were."""
     nall = (34, 30, 26)
     gx, gy, gz = grids(*nall, kind="tanh")
     sc = mf.SolverCoeffs3D(gx, gy, gz, (1, 2, 1, 1, 2, 1), 6)
@@ -203,10 +205,23 @@ def test_many_problems_equal_single_calls(mf, gpu, prec_name, refine):
     outs = [np.asfortranarray(s.copy()) for s in solf0]
     sc.solve_3d_many(rhs, -4.0, outs, [b[0] for b in bcs], [b[1] for b in bcs], [b[2] for b in bcs],
                      precision=prec, refine=refine)
+    edge = np.zeros(nall, dtype=bool)
+    for a in range(3):
+        for c in range(a + 1, 3):
+            for ia in (0, -1):
+                for ic in (0, -1):
+                    sl = [slice(None)] * 3
+                    sl[a], sl[c] = ia, ic
+                    edge[tuple(sl)] = True
     for b in range(B):
         one = np.asfortranarray(solf0[b].copy())
         sc.solve_3d(rhs[b], -4.0, one, *bcs[b], precision=prec, refine=refine)
         assert np.array_equal(outs[b], one), b
+        dev = mf.to_device(solf0[b])
+        sc.solve_3d(mf.to_device(rhs[b]), -4.0, dev, *[mf.to_device(x) for x in bcs[b]], precision=prec,
+                    refine=refine)
+        assert np.array_equal(mf.to_host(dev), one), b
+        assert np.array_equal(one[edge], solf0[b][edge]), b
 
 
 @pytest.mark.parametrize("prec_name,refine", [("MF_PREC_3XTF32", 1), ("MF_PREC_3XTF32", 2),
