@@ -1065,6 +1065,19 @@ def md_config2(mf, torch, operators=("velocity", "pressure")):
             row[key] = timed(lambda: md.solve(g, u, bc), 3 if form == mf.MD_TRI_PERSISTENT else 2)
         md.set_triangular_form(mf.MD_TRI_PERSISTENT)
         row["interface_ms_1_lu_persistent"] = timed(lambda: md.interface_solve(iv[:1]), 3)
+        md.set_interface_solve(mf.MD_IFACE_AUTO)
+        # beside the configuration's FP64: the subdomain solves in 3xTF32 + 1
+        # refinement step (the influence matrix and the interface stay FP64)
+        md.solve(g, u, bc)
+        u_fp64 = {c: u[c].clone() for c in u}
+        md.set_precision(mf.MF_PREC_3XTF32, 1)
+        row["solve_ms_3xtf32_subdomains"] = timed(lambda: md.solve(g, u, bc), 5)
+        md.solve(g, u, bc)
+        torch.cuda.synchronize()
+        row["rel_diff_3xtf32_subdomains"] = max(float((u[c] - u_fp64[c]).abs().max() / u_fp64[c].abs().max())
+                                                for c in u)
+        md.set_precision(mf.MF_PREC_FP64, -1)
+        del u_fp64
         md.device_status()
         out[name] = row
         md.close()
