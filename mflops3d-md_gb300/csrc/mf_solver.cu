@@ -1136,9 +1136,10 @@ struct FoldArgsF {
   const float* ix[4];
   const float* iy[4];
   const float* iz[4];
-  const float* bx;  // c * bc products, [4][n2*n3] etc.
-  const float* by;
+  const float* bx;  // c * bc products: x faces [4][n3][bxp] (rows padded to bxp, plane stride bxs)
+  const float* by;  // y faces [4][n1*n3], z faces [4][n1*n2]
   const float* bz;
+  long long bxp, bxs;
 };
 
 // Fold of the boundary data into the right-hand side and store of the first
@@ -1158,7 +1159,7 @@ __global__ void __launch_bounds__(128) k_fold_split_rows(const double* __restric
   const int i = blockIdx.x * blockDim.x + threadIdx.x, j0 = blockIdx.y * kFoldJ;
   if (i >= P1) return;
   const bool in_i = i < n1;
-  const long long sx = (long long)n2 * n3, sy = (long long)n1 * n3, sz = (long long)n1 * n2;
+  const long long sy = (long long)n1 * n3, sz = (long long)n1 * n2;
   float cx[4] = {0.f, 0.f, 0.f, 0.f}, cy[kFoldJ][4], fz[kFoldJ][4];
   if (in_i)
 #pragma unroll
@@ -1189,40 +1190,60 @@ __global__ void __launch_bounds__(128) k_fold_split_rows(const double* __restric
       const int j = j0 + jj;
       r[jj] = (in_k && j < n2) ? rhs[i + (long long)n1 * (j + (long long)n2 * k)] : 0.0;
     }
+    // per row jj: v = narrow(rhs), then for each boundary column c the
+    // x-, y- and z-face terms, in that order; the x-face products of the
+    // eight rows come as two aligned float4 (the same for the whole warp)
+    float v[kFoldJ];
+#pragma unroll
+    for (int jj = 0; jj < kFoldJ; ++jj) v[jj] = narrow(r[jj]);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      float bxv[kFoldJ];
+      if (in_k) {
+        const float4* q = reinterpret_cast<const float4*>(a.bx + c * a.bxs + a.bxp * k + j0);
+        const float4 q0 = q[0], q1 = q[1];
+        bxv[0] = q0.x; bxv[1] = q0.y; bxv[2] = q0.z; bxv[3] = q0.w;
+        bxv[4] = q1.x; bxv[5] = q1.y; bxv[6] = q1.z; bxv[7] = q1.w;
+      } else {
+#pragma unroll
+        for (int jj = 0; jj < kFoldJ; ++jj) bxv[jj] = 0.f;
+      }
+#pragma unroll
+      for (int jj = 0; jj < kFoldJ; ++jj) {
+        v[jj] -= cx[c] * bxv[jj];
+        v[jj] -= cy[jj][c] * by[c];
+        v[jj] -= iz[c] * fz[jj][c];
+      }
+    }
 #pragma unroll
     for (int jj = 0; jj < kFoldJ; ++jj) {
       const int j = j0 + jj;
-      float v = 0.f;
-      if (in_k && j < n2) {
-        v = narrow(r[jj]);
-        const long long fx = j + (long long)n2 * k;
-#pragma unroll
-        for (int c = 0; c < 4; ++c) {
-          v -= cx[c] * a.bx[c * sx + fx];
-          v -= cy[jj][c] * by[c];
-          v -= iz[c] * fz[jj][c];
-        }
-      }
+      const float vv = (in_k && j < n2) ? v[jj] : 0.f;  // padding stays zero
       const long long idx = i + (long long)P1 * (j + (long long)P2 * k);
       if (x32) {
-        x32[idx] = v;
+        x32[idx] = vv;
       } else {
-        const __nv_bfloat16 h = __float2bfloat16_rn(v);
+        const __nv_bfloat16 h = __float2bfloat16_rn(vv);
         hi[idx] = h;
-        lo[idx] = __float2bfloat16_rn(v - __bfloat162float(h));
+        lo[idx] = __float2bfloat16_rn(vv - __bfloat162float(h));
       }
     }
   }
 }
 
-__global__ void k_fold_faces(const double* __restrict__ bc, double4 cc, float* out, long long nf) {
+// The four products of a face pair, plane c at out + c ps; face point t
+// (rows of length r) at (t % r) + rp (t / r): rows padded to rp for aligned
+// vector loads (rp = r, ps = nf: unpadded).
+__global__ void k_fold_faces(const double* __restrict__ bc, double4 cc, float* out, long long nf, long long r,
+                             long long rp, long long ps) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nf) return;
   const double lo = bc[t], hi = bc[t + nf];
-  out[t] = (float)(cc.x * lo);
-  out[t + nf] = (float)(cc.y * lo);
-  out[t + 2 * nf] = (float)(cc.z * hi);
-  out[t + 3 * nf] = (float)(cc.w * hi);
+  const long long o = (t % r) + rp * (t / r);
+  out[o] = (float)(cc.x * lo);
+  out[o + ps] = (float)(cc.y * lo);
+  out[o + 2 * ps] = (float)(cc.z * hi);
+  out[o + 3 * ps] = (float)(cc.w * hi);
 }
 
 
@@ -1878,15 +1899,20 @@ static int fold_split(mf_solver3d* sc, bool tf32, const double* rhs, const doubl
                       cudaStream_t st) {
   const long long n1 = sc->n[0], n2 = sc->n[1], n3 = sc->n[2];
   const long long nf[3] = {n2 * n3, n1 * n3, n1 * n2};
+  // x-face rows (j) padded to a multiple of 8 floats covering the padded
+  // axis: the fold reads eight j of a row, up to P2 - 1, as two aligned float4
+  const long long bxp = (std::max<long long>(n2, sc->P[1]) + 7) / 8 * 8, bxs = bxp * n3;
+  const long long ps[3] = {bxs, nf[1], nf[2]};
   int rc;
-  if ((rc = sc->foldf.ensure(sizeof(float) * 4 * (nf[0] + nf[1] + nf[2])))) return rc;
+  if ((rc = sc->foldf.ensure(sizeof(float) * 4 * (ps[0] + ps[1] + ps[2])))) return rc;
   float* f = sc->foldf.as<float>();
-  float* fa[3] = {f, f + 4 * nf[0], f + 4 * (nf[0] + nf[1])};
+  float* fa[3] = {f, f + 4 * ps[0], f + 4 * (ps[0] + ps[1])};
   sc->prof.begin(kProfFold, st);
   for (int a = 0; a < 3; ++a) {
     const AxisDev& d = sc->ax[a];
+    const long long r = a == 0 ? n2 : nf[a], rp = a == 0 ? bxp : nf[a];
     k_fold_faces<<<blocks_for(nf[a], 256), 256, 0, st>>>(
-        bcs[a], make_double4(d.bcc[0], d.bcc[1], d.bcc[2], d.bcc[3]), fa[a], nf[a]);
+        bcs[a], make_double4(d.bcc[0], d.bcc[1], d.bcc[2], d.bcc[3]), fa[a], nf[a], r, rp, ps[a]);
   }
   FoldArgsF args;
   for (int c = 0; c < 4; ++c) {
@@ -1897,6 +1923,8 @@ static int fold_split(mf_solver3d* sc, bool tf32, const double* rhs, const doubl
   args.bx = fa[0];
   args.by = fa[1];
   args.bz = fa[2];
+  args.bxp = bxp;
+  args.bxs = bxs;
   k_fold_split_rows<<<dim3(blocks_for(sc->P[0], 128), sc->P[1] / kFoldJ, kFoldKz), 128, 0, st>>>(
       rhs, args, tf32 ? nullptr : sc->Xa_hi.as<__nv_bfloat16>(),
       tf32 ? nullptr : sc->Xa_lo.as<__nv_bfloat16>(), tf32 ? sc->Xa32.as<float>() : nullptr,
