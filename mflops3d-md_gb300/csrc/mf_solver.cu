@@ -59,16 +59,21 @@ struct AxisDev {
 
 using namespace mf;
 
+// Staging slots of mf_solve_3d_mixed_many: with three, the upload of a
+// problem need not wait for the download of the one two places before it
+// (the host link carries both directions at once).
+constexpr int kPipeSlots = 3;
+
 struct mf_solver3d {
   AxisDev ax[3];
   int n[3] = {0, 0, 0};
   int P[3] = {0, 0, 0};
   DevBuf w0, w1;                               // FP64 work arrays (plain path)
   DevBuf st_rhs, st_solf, st_bc[3];            // host staging
-  // mf_solve_3d_mixed_many: two staging slots, copy-in/out streams, events
-  DevBuf pipe_rhs[2], pipe_solf[2], pipe_bc[2][3];
+  // mf_solve_3d_mixed_many: kPipeSlots staging slots, copy-in/out streams, events
+  DevBuf pipe_rhs[kPipeSlots], pipe_solf[kPipeSlots], pipe_bc[kPipeSlots][3];
   cudaStream_t cin = nullptr, cout = nullptr;
-  cudaEvent_t in_ready[2] = {nullptr, nullptr}, solved[2] = {nullptr, nullptr}, out_done[2] = {nullptr, nullptr};
+  cudaEvent_t in_ready[kPipeSlots] = {}, solved[kPipeSlots] = {}, out_done[kPipeSlots] = {};
   DevBuf R, R2;                                // FP64 scratch of the residual
   DevBuf nullpart;                             // null-mode projection: partial sums, coefficient
   DevBuf R1d;                                  // closed operators: FP64 r1 of the refinement
@@ -2171,7 +2176,7 @@ int mf_solver3d_destroy(mf_solver3d_t* sc) {
                     &sc->Xb_lo, &sc->Xa32, &sc->Xb32, &sc->err, &sc->foldf, &sc->U32, &sc->C32,
                     &sc->R1f, &sc->nullpart, &sc->R1d})
     b->release();
-  for (int q = 0; q < 2; ++q) {
+  for (int q = 0; q < kPipeSlots; ++q) {
     sc->pipe_rhs[q].release();
     sc->pipe_solf[q].release();
     for (int a = 0; a < 3; ++a) sc->pipe_bc[q][a].release();
@@ -2335,11 +2340,11 @@ int mf_solve_3d_mixed_many(mf_solver3d_t* sc, int count, const double* const* rh
   if (!sc->cin) {
     MF_CUDA(cudaStreamCreateWithFlags(&sc->cin, cudaStreamNonBlocking));
     MF_CUDA(cudaStreamCreateWithFlags(&sc->cout, cudaStreamNonBlocking));
-    for (int q = 0; q < 2; ++q)
+    for (int q = 0; q < kPipeSlots; ++q)
       for (cudaEvent_t* e : {&sc->in_ready[q], &sc->solved[q], &sc->out_done[q]})
         MF_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
   }
-  for (int q = 0; q < 2; ++q) {
+  for (int q = 0; q < kPipeSlots; ++q) {
     if ((rc = sc->pipe_rhs[q].ensure(rb)) || (rc = sc->pipe_solf[q].ensure(sb))) return rc;
     for (int a = 0; a < 3; ++a)
       if ((rc = sc->pipe_bc[q][a].ensure(bb[a]))) return rc;
@@ -2349,8 +2354,8 @@ int mf_solve_3d_mixed_many(mf_solver3d_t* sc, int count, const double* const* rh
   MF_CUDA(cudaStreamWaitEvent(sc->cin, sc->solved[0], 0));
   const double* const* bsrc[3] = {bcx, bcy, bcz};
   for (int b = 0; b < count; ++b) {
-    const int q = b & 1;
-    if (b >= 2) {  // slot q is free once problem b-2 is solved and downloaded
+    const int q = b % kPipeSlots;
+    if (b >= kPipeSlots) {  // slot q is free once problem b - kPipeSlots is solved and downloaded
       MF_CUDA(cudaStreamWaitEvent(sc->cin, sc->solved[q], 0));
       MF_CUDA(cudaStreamWaitEvent(sc->cin, sc->out_done[q], 0));
     }
