@@ -243,10 +243,15 @@ int mf_solve_3d_mixed(mf_solver3d_t* sc, const double* rhs, double sigma, double
 /* `count` problems through mf_solve_3d_mixed (precision MF_PREC_FP64: the
  * plain solve) in one call, with host (pinned for overlap) or device arrays
  * given per problem: the upload of problem b+1 and the download of problem
- * b-1 run on copy streams while problem b is solved (two device staging
- * slots).  Each problem's result equals that of a single call; the call
- * returns when every result is in place.  No reference counterpart (the
- * reference solves one right-hand side per call). */
+ * b-1 run on copy streams while problem b is solved (three device staging
+ * slots).  In the mixed modes every problem after the first of a call is
+ * one replay of its slot's CUDA graph, captured on first use and again
+ * when sigma, the precision, the refinement count, the transform plan, the
+ * tuner mode or the residual form change (not while the per-kernel timers
+ * of mf_solver3d_profile are on).  Each problem's result equals that of a
+ * single call; the call returns when every result is in place.  No
+ * reference counterpart (the reference solves one right-hand side per
+ * call). */
 int mf_solve_3d_mixed_many(mf_solver3d_t* sc, int count, const double* const* rhs, double sigma,
                            double* const* solf, const double* const* bcx, const double* const* bcy,
                            const double* const* bcz, int n1, int n2, int n3, int precision,

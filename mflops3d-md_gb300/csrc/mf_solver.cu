@@ -74,6 +74,14 @@ struct mf_solver3d {
   DevBuf pipe_rhs[kPipeSlots], pipe_solf[kPipeSlots], pipe_bc[kPipeSlots][3];
   cudaStream_t cin = nullptr, cout = nullptr;
   cudaEvent_t in_ready[kPipeSlots] = {}, solved[kPipeSlots] = {}, out_done[kPipeSlots] = {};
+  // ... and per slot a CUDA graph of the mixed solve on that slot's buffers,
+  // with the settings it was captured under
+  struct PipeGraph {
+    cudaGraphExec_t exec = nullptr;
+    double sigma = 0.0;
+    int precision = -1, refine = -1, plan = -1, tune = -1, resid = -1;
+  } pipe_graph[kPipeSlots];
+  cudaStream_t gcap = nullptr;  // capture stream of those graphs
   DevBuf R, R2;                                // FP64 scratch of the residual
   DevBuf nullpart;                             // null-mode projection: partial sums, coefficient
   DevBuf R1d;                                  // closed operators: FP64 r1 of the refinement
@@ -2182,9 +2190,11 @@ int mf_solver3d_destroy(mf_solver3d_t* sc) {
     for (int a = 0; a < 3; ++a) sc->pipe_bc[q][a].release();
     for (cudaEvent_t e : {sc->in_ready[q], sc->solved[q], sc->out_done[q]})
       if (e) cudaEventDestroy(e);
+    if (sc->pipe_graph[q].exec) cudaGraphExecDestroy(sc->pipe_graph[q].exec);
   }
   if (sc->cin) cudaStreamDestroy(sc->cin);
   if (sc->cout) cudaStreamDestroy(sc->cout);
+  if (sc->gcap) cudaStreamDestroy(sc->gcap);
   delete sc;
   return MF_OK;
 }
@@ -2373,6 +2383,51 @@ int mf_solve_3d_mixed_many(mf_solver3d_t* sc, int count, const double* const* rh
     MF_CUDA(cudaEventRecord(sc->in_ready[q], sc->cin));
     MF_CUDA(cudaStreamWaitEvent(st, sc->in_ready[q], 0));
     double* s = sc->pipe_solf[q].as<double>();
+    if (precision != MF_PREC_FP64 && b > 0 && !sc->prof.on) {
+      // Mixed solves after the first of the call (which has made every
+      // buffer and plan these settings need) replay the slot's graph,
+      // captured on first use or when a setting changed; a capture that
+      // fails leaves the eager launches below to do the work.
+      mf_solver3d::PipeGraph& G = sc->pipe_graph[q];
+      const int plan = tc_get_tf32_plan(), tmode = tune_mode();
+      if (!G.exec || G.sigma != sigma || G.precision != precision || G.refine != refine || G.plan != plan ||
+          G.tune != tmode || G.resid != sc->resid_mode) {
+        if (G.exec) {
+          MF_CUDA(cudaGraphExecDestroy(G.exec));
+          G.exec = nullptr;
+        }
+        if (!sc->gcap) MF_CUDA(cudaStreamCreateWithFlags(&sc->gcap, cudaStreamNonBlocking));
+        if (cudaStreamBeginCapture(sc->gcap, cudaStreamCaptureModeRelaxed) == cudaSuccess) {
+          const int crc = solve_mixed_dev(sc, sc->pipe_rhs[q].as<double>(), sigma, s, bcs, precision, refine,
+                                          sc->gcap);
+          cudaGraph_t graph = nullptr;
+          const cudaError_t e = cudaStreamEndCapture(sc->gcap, &graph);
+          if (crc == MF_OK && e == cudaSuccess && graph &&
+              cudaGraphInstantiate(&G.exec, graph, 0) == cudaSuccess) {
+            G.sigma = sigma;
+            G.precision = precision;
+            G.refine = refine;
+            G.plan = plan;
+            G.tune = tmode;
+            G.resid = sc->resid_mode;
+          } else {
+            G.exec = nullptr;
+          }
+          if (graph) cudaGraphDestroy(graph);
+          (void)cudaGetLastError();
+        } else {
+          (void)cudaGetLastError();
+        }
+      }
+      if (G.exec) {
+        MF_CUDA(cudaGraphLaunch(G.exec, st));
+        MF_CUDA(cudaEventRecord(sc->solved[q], st));
+        MF_CUDA(cudaStreamWaitEvent(sc->cout, sc->solved[q], 0));
+        MF_CUDA(cudaMemcpyAsync(solf[b], s, sb, cudaMemcpyDefault, sc->cout));
+        MF_CUDA(cudaEventRecord(sc->out_done[q], sc->cout));
+        continue;
+      }
+    }
     rc = precision == MF_PREC_FP64
              ? solve_plain_dev(sc, sc->pipe_rhs[q].as<double>(), sigma, s, bcs, st)
              : solve_mixed_dev(sc, sc->pipe_rhs[q].as<double>(), sigma, s, bcs, precision, refine, st);

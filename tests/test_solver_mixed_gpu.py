@@ -192,19 +192,22 @@ def test_many_problems_equal_single_calls(mf, gpu, prec_name, refine):
     """mf_solve_3d_mixed_many (uploads/downloads overlapping the solves) gives
     each problem exactly the result of a single call, host arrays in and out,
     and of the same call on device arrays; the host paths upload only the
-    edges of the solution array, which come back as they were."""
+    edges of the solution array, which come back as they were.  Two calls in
+    a row: the second replays every slot's graph."""
     nall = (34, 30, 26)
     gx, gy, gz = grids(*nall, kind="tanh")
     sc = mf.SolverCoeffs3D(gx, gy, gz, (1, 2, 1, 1, 2, 1), 6)
     n1, n2, n3 = (v - 2 for v in nall)
     prec = getattr(mf, prec_name)
-    B = 5
+    B = 8  # mixed: problem 0 eager, 1-3 capture each staging slot's graph, 4-7 replay them
     rhs = [field((n1, n2, n3), 80 + b) for b in range(B)]
     bcs = [bc_arrays(n1, n2, n3, 90 + b) for b in range(B)]
     solf0 = [field(nall, 100 + b) for b in range(B)]  # edges and corners are kept
     outs = [np.asfortranarray(s.copy()) for s in solf0]
-    sc.solve_3d_many(rhs, -4.0, outs, [b[0] for b in bcs], [b[1] for b in bcs], [b[2] for b in bcs],
-                     precision=prec, refine=refine)
+    for _ in range(2):
+        outs = [np.asfortranarray(s.copy()) for s in solf0]
+        sc.solve_3d_many(rhs, -4.0, outs, [b[0] for b in bcs], [b[1] for b in bcs], [b[2] for b in bcs],
+                         precision=prec, refine=refine)
     edge = np.zeros(nall, dtype=bool)
     for a in range(3):
         for c in range(a + 1, 3):
