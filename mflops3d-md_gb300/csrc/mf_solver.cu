@@ -311,7 +311,8 @@ struct ResidFin {
   // Final store of row i with the row's rin (and, mode 0, u) value given.
   __device__ __forceinline__ void put(int i, long long idx, T y, T r, T uv) const {
     if (mode == 0) {
-      out[idx] = r - sigma * uv - y;
+      // at sigma = 0 the same value without the product (and u is not loaded)
+      out[idx] = sigma != T(0) ? r - sigma * uv - y : r - y;
     } else if (mode == 1) {
       out[idx] = r - y;
     } else {
@@ -501,9 +502,11 @@ __device__ __forceinline__ double moment_sum(const TriRow& r, const float (&v)[W
   return widen(sh) + widen(l + se + pl);
 }
 
+// xs holds the forward values of this line at stride xq (s, or the number of
+// lines when they are stored row-major across lines)
 __device__ __forceinline__ void solve_line_tri(const TriRow* __restrict__ R, int n, const float* u,
-                                               double* xs, long long s, double lo, double hi,
-                                               const ResidFin<double, float>& fin) {
+                                               double* xs, long long s, long long xq, double lo,
+                                               double hi, const ResidFin<double, float>& fin) {
   float f[7], g[7];
 #pragma unroll
   for (int m = 0; m < 7; ++m) {
@@ -514,7 +517,7 @@ __device__ __forceinline__ void solve_line_tri(const TriRow* __restrict__ R, int
   double x0 = moment_sum<7>(R[0], f, f[0], 0) + R[0].cbc * (lo - widen(f[0]));
   double x1 = moment_sum<7>(R[1], f, f[1], 1) + R[1].cbc * (lo - widen(f[1])) - R[1].ft * x0;
   xs[0] = x0;
-  xs[s] = x1;
+  xs[xq] = x1;
   double xm = x1;
   float w[5] = {f[0], f[1], f[2], f[3], f[4]};
   // interior rows 2..n-3; pf[k] = u(i + 3 + k)
@@ -533,7 +536,7 @@ __device__ __forceinline__ void solve_line_tri(const TriRow* __restrict__ R, int
     for (int k = 0; k < kAhead; ++k) {
       const TriRow& r = R[i + k];
       const double x = moment_sum<5>(r, w, w[2], 2) - r.ft * xm;
-      xs[(long long)(i + k) * s] = x;
+      xs[(long long)(i + k) * xq] = x;
       xm = x;
       w[0] = w[1]; w[1] = w[2]; w[2] = w[3]; w[3] = w[4]; w[4] = pf[k];
     }
@@ -543,7 +546,7 @@ __device__ __forceinline__ void solve_line_tri(const TriRow* __restrict__ R, int
   for (; i < n - 2; ++i) {
     const TriRow& r = R[i];
     const double x = moment_sum<5>(r, w, w[2], 2) - r.ft * xm;
-    xs[(long long)i * s] = x;
+    xs[(long long)i * xq] = x;
     xm = x;
     w[0] = w[1]; w[1] = w[2]; w[2] = w[3]; w[3] = w[4];
     if (i + 3 < n) w[4] = u[(long long)(i + 3) * s];
@@ -555,7 +558,7 @@ __device__ __forceinline__ void solve_line_tri(const TriRow* __restrict__ R, int
   const double xB = moment_sum<7>(rB, g, g[6], 6) + rB.cbc * (hi - widen(g[6])) - rB.ft * xA;
   // back substitution with the final combination of each row; the forward
   // value, rin and (first pass) u of row i - k are loaded kAhead rows ahead
-  const bool need_u = fin.mode == 0;
+  const bool need_u = fin.mode == 0 && fin.sigma != 0.0;  // u enters only through sigma u
   auto uval = [&](long long o) { return need_u ? widen(fin.u[o]) : 0.0; };
   double y1 = xB;
   fin.put(n - 1, (long long)(n - 1) * s, xB, fin.rin[(long long)(n - 1) * s], uval((long long)(n - 1) * s));
@@ -569,7 +572,7 @@ __device__ __forceinline__ void solve_line_tri(const TriRow* __restrict__ R, int
   for (int k = 0; k < kAhead; ++k) {
     const bool in = i - k >= 0;
     const long long o = (long long)(i - k) * s;
-    rb[k] = in ? xs[o] : 0.0;
+    rb[k] = in ? xs[(long long)(i - k) * xq] : 0.0;
     rr[k] = in ? fin.rin[o] : 0.0;
     ru[k] = (in && need_u) ? fin.u[o] : 0.f;
   }
@@ -580,7 +583,7 @@ __device__ __forceinline__ void solve_line_tri(const TriRow* __restrict__ R, int
     for (int k = 0; k < kAhead; ++k) {
       const int j = i - kAhead - k;
       const long long o = (long long)j * s;
-      nb[k] = (j >= 0) ? xs[o] : 0.0;
+      nb[k] = (j >= 0) ? xs[(long long)j * xq] : 0.0;
       nr[k] = (j >= 0) ? fin.rin[o] : 0.0;
       nu[k] = (j >= 0 && need_u) ? fin.u[o] : 0.f;
     }
@@ -599,7 +602,7 @@ __device__ __forceinline__ void solve_line_tri(const TriRow* __restrict__ R, int
   }
   for (; i >= 0; --i) {
     const long long o = (long long)i * s;
-    const double yy = xs[o] - R[i].dt * y1;
+    const double yy = xs[(long long)i * xq] - R[i].dt * y1;
     fin.put(i, o, yy, fin.rin[o], uval(o));
     y1 = yy;
   }
@@ -607,7 +610,7 @@ __device__ __forceinline__ void solve_line_tri(const TriRow* __restrict__ R, int
 
 __global__ void __launch_bounds__(128) k_resid_tri(ResidPass<double> p, const TriRow* __restrict__ R,
                                                    const float* u, const double* rin, double* scratch,
-                                                   double* rout, __nv_bfloat16* hi,
+                                                   long long xq, double* rout, __nv_bfloat16* hi,
                                                    __nv_bfloat16* lo, float* x32, float* r32) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (long long)p.na * p.nb) return;
@@ -630,7 +633,12 @@ __global__ void __launch_bounds__(128) k_resid_tri(ResidPass<double> p, const Tr
   fin.x32 = x32 ? x32 + pbase : nullptr;
   fin.pstride = p.pstride;
   fin.r32 = r32 ? r32 + base : nullptr;
-  solve_line_tri(R, p.n, u + base, scratch + base, p.s, blo, bhi, fin);
+  // xq != 0: the forward values go to a separate scratch array, row i of
+  // line t at i * xq + t, so a warp's 32 lines touch consecutive addresses
+  if (xq)
+    solve_line_tri(R, p.n, u + base, scratch + t, p.s, xq, blo, bhi, fin);
+  else
+    solve_line_tri(R, p.n, u + base, scratch + base, p.s, p.s, blo, bhi, fin);
 }
 
 // ---- the same residual with two lanes per line (twisted factorisation)
@@ -654,8 +662,9 @@ constexpr int kTw = 4;   // rows loaded ahead in the forward elimination of the 
 constexpr int kTwB = 2;  // ... and in their back substitution
 
 __device__ __forceinline__ void solve_line_twist(const TriRow* __restrict__ R, int n, int cnt,
-                                                 const float* u, double* xs, long long s, double bcv,
-                                                 const ResidFin<double, float>& fin, unsigned mask) {
+                                                 const float* u, double* xs, long long s, long long xq,
+                                                 double bcv, const ResidFin<double, float>& fin,
+                                                 unsigned mask) {
   float f[7];
 #pragma unroll
   for (int m = 0; m < 7; ++m) f[m] = u[(long long)m * s];
@@ -663,7 +672,7 @@ __device__ __forceinline__ void solve_line_twist(const TriRow* __restrict__ R, i
   double x0 = moment_sum<7>(R[0], f, f[0], 0) + R[0].cbc * (bcv - widen(f[0]));
   double x1 = moment_sum<7>(R[1], f, f[1], 1) + R[1].cbc * (bcv - widen(f[1])) - R[1].ft * x0;
   xs[0] = x0;
-  xs[s] = x1;
+  xs[xq] = x1;
   double xm = x1;
   float w[5] = {f[0], f[1], f[2], f[3], f[4]};
   float pf[kTw];  // pf[k] = u(i + 3 + k)
@@ -681,7 +690,7 @@ __device__ __forceinline__ void solve_line_twist(const TriRow* __restrict__ R, i
     for (int k = 0; k < kTw; ++k) {
       const TriRow& r = R[i + k];
       const double x = moment_sum<5>(r, w, w[2], 2) - r.ft * xm;
-      xs[(long long)(i + k) * s] = x;
+      xs[(long long)(i + k) * xq] = x;
       xm = x;
       w[0] = w[1]; w[1] = w[2]; w[2] = w[3]; w[3] = w[4]; w[4] = pf[k];
     }
@@ -691,14 +700,14 @@ __device__ __forceinline__ void solve_line_twist(const TriRow* __restrict__ R, i
   for (; i < cnt; ++i) {
     const TriRow& r = R[i];
     const double x = moment_sum<5>(r, w, w[2], 2) - r.ft * xm;
-    xs[(long long)i * s] = x;
+    xs[(long long)i * xq] = x;
     xm = x;
     w[0] = w[1]; w[1] = w[2]; w[2] = w[3]; w[3] = w[4];
     if (i + 3 < n) w[4] = u[(long long)(i + 3) * s];
   }
   // the twist: this side's last eliminated value and the partner's
   const double other = __shfl_xor_sync(mask, xm, 16);
-  const bool need_u = fin.mode == 0;
+  const bool need_u = fin.mode == 0 && fin.sigma != 0.0;  // u enters only through sigma u
   auto uval = [&](long long o) { return need_u ? widen(fin.u[o]) : 0.0; };
   i = cnt - 1;
   const TriRow& rt = R[i];
@@ -712,7 +721,7 @@ __device__ __forceinline__ void solve_line_twist(const TriRow* __restrict__ R, i
   for (int k = 0; k < kTwB; ++k) {
     const bool in = i - k >= 0;
     const long long o = (long long)(i - k) * s;
-    rb[k] = in ? xs[o] : 0.0;
+    rb[k] = in ? xs[(long long)(i - k) * xq] : 0.0;
     rr[k] = in ? fin.rin[o] : 0.0;
     ru[k] = (in && need_u) ? fin.u[o] : 0.f;
   }
@@ -723,7 +732,7 @@ __device__ __forceinline__ void solve_line_twist(const TriRow* __restrict__ R, i
     for (int k = 0; k < kTwB; ++k) {
       const int j = i - kTwB - k;
       const long long o = (long long)j * s;
-      nb[k] = (j >= 0) ? xs[o] : 0.0;
+      nb[k] = (j >= 0) ? xs[(long long)j * xq] : 0.0;
       nr[k] = (j >= 0) ? fin.rin[o] : 0.0;
       nu[k] = (j >= 0 && need_u) ? fin.u[o] : 0.f;
     }
@@ -742,7 +751,7 @@ __device__ __forceinline__ void solve_line_twist(const TriRow* __restrict__ R, i
   }
   for (; i >= 0; --i) {
     const long long o = (long long)i * s;
-    const double yy = xs[o] - R[i].dt * y1;
+    const double yy = xs[(long long)i * xq] - R[i].dt * y1;
     fin.put(i, o, yy, fin.rin[o], uval(o));
     y1 = yy;
   }
@@ -753,9 +762,9 @@ __device__ __forceinline__ void solve_line_twist(const TriRow* __restrict__ R, i
 template <int MODE>
 __global__ void __launch_bounds__(128) k_resid_twist(ResidPass<double> p, const TriRow* __restrict__ Rt,
                                                      const TriRow* __restrict__ Rb, const float* u,
-                                                     const double* rin, double* scratch, double* rout,
-                                                     __nv_bfloat16* hi, __nv_bfloat16* lo, float* x32,
-                                                     float* r32) {
+                                                     const double* rin, double* scratch, long long xq,
+                                                     double* rout, __nv_bfloat16* hi, __nv_bfloat16* lo,
+                                                     float* x32, float* r32) {
   const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
   const bool top = lane < 16;
@@ -782,7 +791,13 @@ __global__ void __launch_bounds__(128) k_resid_twist(ResidPass<double> p, const 
   fin.x32 = x32 ? x32 + pbase : nullptr;
   fin.pstride = top ? p.pstride : -p.pstride;
   fin.r32 = r32 ? r32 + base : nullptr;
-  solve_line_twist(top ? Rt : Rb, p.n, cnt, u + base, scratch + base, s, bcv, fin, mask);
+  // xq != 0: the forward values in a separate array, row i of line t at
+  // i * xq + t (the bottom lane walks it from row n-1 upwards)
+  if (xq)
+    solve_line_twist(top ? Rt : Rb, p.n, cnt, u + base, scratch + t + (top ? 0 : (long long)(p.n - 1) * xq),
+                     s, top ? xq : -xq, bcv, fin, mask);
+  else
+    solve_line_twist(top ? Rt : Rb, p.n, cnt, u + base, scratch + base, s, s, bcv, fin, mask);
 }
 
 // ---- the same residual entirely on the FP32 pipe (double-float sweeps)
@@ -1729,17 +1744,23 @@ static int residual_passes(mf_solver3d* sc, const T* rin, const In* u, double si
                          reinterpret_cast<float2*>(s1), hi, lo, x32, r32, st);
   }
   int axis_of_pass = 0;
+  // xt: a field-sized array free during the pass, for the forward values of
+  // the unit-stride pass (nullptr: they go to scratch, in the field's layout)
   auto launch = [&](const ResidPass<T>& p, int kind, const T* in_r, T* scratch, T* rout,
-                    __nv_bfloat16* h, __nv_bfloat16* l, float* x, float* r32p) -> int {
+                    __nv_bfloat16* h, __nv_bfloat16* l, float* x, float* r32p, T* xt) -> int {
     sc->prof.begin(kind, st);
     if constexpr (sizeof(T) == 8 && sizeof(In) == 4) {
-      // The x pass (unit stride along the line) stays one thread per line:
-      // with two lanes per line its per-lane sector streams outgrow L1
-      // (257^3 on GB300: 0.41 ms two-sided, ~0.33 ms one thread per line,
-      // while the y and z passes drop from 0.25 to 0.19 ms each).
-      if (tri && (sc->resid_mode == MF_RESID_FP64_LINE || p.s == 1)) {
+      // The x pass (unit stride along the line) runs two-sided only with its
+      // forward values stored across lines (xt): in the field's layout the
+      // per-lane sector streams outgrow L1 (257^3 on GB300: 0.41 ms
+      // two-sided, 0.33 ms one thread per line, 0.31 ms two-sided with xt;
+      // the y and z passes drop from 0.25 to 0.19 ms each).  Without xt it
+      // stays one thread per line.
+      const bool across = p.s == 1 && xt;
+      if (tri && (sc->resid_mode == MF_RESID_FP64_LINE || (p.s == 1 && !across))) {
         k_resid_tri<<<blocks_for((long long)p.na * p.nb, 128), 128, 0, st>>>(
-            p, sc->ax[axis_of_pass].tri.template as<TriRow>(), u, in_r, scratch, rout, h, l, x, r32p);
+            p, sc->ax[axis_of_pass].tri.template as<TriRow>(), u, in_r, across ? xt : scratch,
+            across ? (long long)p.na * p.nb : 0LL, rout, h, l, x, r32p);
         sc->prof.end(st);
         MF_CUDA(cudaGetLastError());
         return MF_OK;
@@ -1749,8 +1770,8 @@ static int residual_passes(mf_solver3d* sc, const T* rin, const In* u, double si
         auto kern = p.mode == 0 ? k_resid_twist<0> : p.mode == 1 ? k_resid_twist<1>
                   : p.mode == 2 ? k_resid_twist<2> : k_resid_twist<3>;
         kern<<<blocks_for(2 * (long long)p.na * p.nb, 128), 128, 0, st>>>(
-            p, d.tri.template as<TriRow>(), d.trib.template as<TriRow>(), u, in_r, scratch, rout, h, l, x,
-            r32p);
+            p, d.tri.template as<TriRow>(), d.trib.template as<TriRow>(), u, in_r, across ? xt : scratch,
+            across ? (long long)p.na * p.nb : 0LL, rout, h, l, x, r32p);
         sc->prof.end(st);
         MF_CUDA(cudaGetLastError());
         return MF_OK;
@@ -1766,11 +1787,11 @@ static int residual_passes(mf_solver3d* sc, const T* rin, const In* u, double si
   ResidPass<T> px = pass(0);
   px.mode = 0;
   axis_of_pass = 0;
-  if ((rc = launch(px, prof_kind_x, rin, s0, s0, nullptr, nullptr, nullptr, nullptr))) return rc;
+  if ((rc = launch(px, prof_kind_x, rin, s0, s0, nullptr, nullptr, nullptr, nullptr, s1))) return rc;
   ResidPass<T> py = pass(1);
   py.mode = 1;
   axis_of_pass = 1;
-  if ((rc = launch(py, prof_kind_yz, s0, s1, s1, nullptr, nullptr, nullptr, nullptr))) return rc;
+  if ((rc = launch(py, prof_kind_yz, s0, s1, s1, nullptr, nullptr, nullptr, nullptr, nullptr))) return rc;
   ResidPass<T> pz = pass(2);
   axis_of_pass = 2;
   if (hi || x32) {
@@ -1778,10 +1799,10 @@ static int residual_passes(mf_solver3d* sc, const T* rin, const In* u, double si
     pz.pa = 1;
     pz.pb = sc->P[0];
     pz.pstride = (long long)sc->P[0] * sc->P[1];
-    return launch(pz, prof_kind_yz, s1, s0, nullptr, hi, lo, x32, r32);
+    return launch(pz, prof_kind_yz, s1, s0, nullptr, hi, lo, x32, r32, nullptr);
   }
   pz.mode = 1;
-  return launch(pz, prof_kind_yz, s1, r, r, nullptr, nullptr, nullptr, nullptr);
+  return launch(pz, prof_kind_yz, s1, r, r, nullptr, nullptr, nullptr, nullptr, nullptr);
 }
 
 // Operand buffers and tensor-core plans of one mixed format (split-BF16 or
