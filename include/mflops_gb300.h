@@ -205,15 +205,15 @@ int mf_solve_3d(mf_solver3d_t* sc, const double* rhs, double sigma, double* solf
  * cudaMalloc: applications whose device memory belongs to their own pool
  * allocator, which budgets every byte and forbids other allocations, and
  * latency-bound host loops that cannot afford cudaMalloc's implicit
- * device-wide synchronisation.  Its
- * two work arrays live in a fixed 4 MiB file-scope device array, so the
- * interior n1*n2*n3 is limited to 262144 points (64^3); larger sizes return
- * MF_ERR_UNSUPPORTED.  All pointers must be device memory (MF_ERR_ARG
- * otherwise).  The first call on each device looks up that array's address
- * (no allocation) and should come before any stream capture.  Every call
- * shares the array, so calls that overlap on the GPU (different streams or
- * handles) race; each call overwrites the work arrays before reading them.
- * It calls no cudaMalloc, cudaFree or allocating library routine. */
+ * device-wide synchronisation.  Its two work arrays live in a fixed 4 MiB
+ * file-scope device array, so the interior n1*n2*n3 is limited to 262144
+ * points (64^3); larger sizes return MF_ERR_UNSUPPORTED.  All pointers must
+ * be device memory (MF_ERR_ARG otherwise).  The first call on each device
+ * looks up that array's address with cudaGetSymbolAddress (no allocation).
+ * Every call shares the array, so calls that overlap on the GPU (different
+ * streams or handles) race; each call overwrites the work arrays before
+ * reading them.  It calls no cudaMalloc, cudaFree or allocating library
+ * routine. */
 int mf_solve_3d_noalloc(mf_solver3d_t* sc, const double* rhs, double sigma, double* solf,
                         const double* bcx, const double* bcy, const double* bcz,
                         int n1, int n2, int n3, void* stream);

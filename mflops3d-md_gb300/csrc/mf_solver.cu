@@ -2131,8 +2131,8 @@ constexpr long long kNoAllocMaxPoints = 1LL << 18;  // interior points n1*n2*n3 
 static __device__ __align__(256) double g_noalloc_scratch[2 * kNoAllocMaxPoints];  // 4 MiB
 
 // Device address of g_noalloc_scratch for the current device, looked up
-// once per device (the first call on a device does this; it allocates
-// nothing and should happen before any stream capture).
+// once per device by the first call on it (cudaGetSymbolAddress allocates
+// nothing).
 static int noalloc_scratch(double** out) {
   static std::mutex mu;
   static double* addr[64] = {nullptr};
