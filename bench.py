@@ -220,6 +220,33 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------
+# replicas (N > 1): every rank solves its own copy of the workload; the job's
+# time is the slowest rank's, its rate the units of all ranks over that time
+# ---------------------------------------------------------------------------
+
+def ranks_max(values, dist, device):
+    """Element-wise maximum of a list of floats over the ranks of `dist` (the
+    slowest rank's timings); the values themselves on a single process."""
+    if dist is None:
+        return [float(v) for v in values]
+    import torch
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.tolist()]
+
+
+def replica_rate(world, units, seconds):
+    """Whole-job rate of `world` replicas that each processed `units` units
+    within `seconds` (the slowest rank's time)."""
+    return world * units / seconds
+
+
+def ranks_barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+# ---------------------------------------------------------------------------
 # reference arm: CPU restatement of the reference algorithm
 # ---------------------------------------------------------------------------
 
@@ -409,8 +436,7 @@ def run_gb300(args, rank, world, dist):
     # timed region: K solves eagerly, then K replays of the captured solve
     # (the headline), per-step CUDA events on the launching stream, L2
     # flushed (256 MiB write) between steps outside the event pairs
-    if dist is not None:
-        dist.barrier()
+    ranks_barrier(dist)
     torch.cuda.synchronize()
     clocks.mark_start()
     wall0 = time.perf_counter()
@@ -418,14 +444,9 @@ def run_gb300(args, rank, world, dist):
     step_ms = timed(graph.replay, args.steps)
     wall = time.perf_counter() - wall0
     clocks.mark_end()
-    if dist is not None:
-        dist.barrier()
+    ranks_barrier(dist)
     clk = clocks.stop()
-    total_ms = sum(step_ms)
-    if dist is not None:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = t.item()
+    total_ms, = ranks_max([sum(step_ms)], dist, "cuda")
     final_err = err_vs_plain()
 
     # per-kernel timing of one solve (separate pass, profiling on)
@@ -451,6 +472,7 @@ def run_gb300(args, rank, world, dist):
     for _ in range(2):
         sc.solve_3d(pin_rhs, 0.0, pin_solf, *pin_bc, precision=prec, refine=refine)
     e2e_steps = max(3, min(args.steps, 10))
+    ranks_barrier(dist)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         sc.solve_3d(pin_rhs, 0.0, pin_solf, *pin_bc, precision=prec, refine=refine)
@@ -468,9 +490,11 @@ def run_gb300(args, rank, world, dist):
                          [pin_bc[2]] * e2e_many, precision=prec, refine=refine)
 
     many()
+    ranks_barrier(dist)
     t0 = time.perf_counter()
     many()
     e2e_dt = (time.perf_counter() - t0) / e2e_many
+    e2e_single_dt, e2e_dt = ranks_max([e2e_single_dt, e2e_dt], dist, "cuda")
     # uploads: the right-hand side, the boundary arrays and the 12 edge lines
     # of the solution array (the solve writes every other entry of it)
     h2d = pin_rhs.nbytes + sum(b.nbytes for b in pin_bc) + 8 * 4 * 3 * (n + 2)
@@ -558,7 +582,7 @@ def run_gb300(args, rank, world, dist):
                 "frac": achieved / hbm, "traffic": profile_traffic("k_resid_tri_257cube.md"),
                 "peak_source": src + " copy",
                 "algorithmic_per_launch": algo_bytes}
-    value = world * args.steps / (total_ms * 1e-3)
+    value = replica_rate(world, args.steps, total_ms * 1e-3)
     accuracy = {"rel_l2_vs_cpu_oracle": oracle_err, "fp64_gpu_vs_cpu_oracle": plain_vs_oracle}
     accuracy.update(accuracy_exact)
     accuracy.update({"rel_l2_vs_fp64_gpu": final_err,
@@ -595,11 +619,11 @@ def run_gb300(args, rank, world, dist):
         "kernel_launches_per_solve": {k: v[1] for k, v in prof.items() if v[1]},
         "roofline": roof,
         "cpu_baseline": cpu,
-        "e2e": {"value": world / e2e_dt, "unit": UNIT, "h2d_bytes_per_step": h2d,
+        "e2e": {"value": replica_rate(world, 1, e2e_dt), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h,
                 "api": "mf_solve_3d_mixed_many with pinned host pointers (%d steps per call, uploads and "
                        "downloads overlapping the solves)" % e2e_many,
-                "single_call_value": world / e2e_single_dt,
+                "single_call_value": replica_rate(world, 1, e2e_single_dt),
                 "single_call_api": "mf_solve_3d_mixed with pinned host pointers, one call per step"},
         "rows": rows,
         "gpu_launches": 2 * launches * args.steps,  # K eager solves + K graph replays
