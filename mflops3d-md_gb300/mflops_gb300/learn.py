@@ -311,8 +311,8 @@ class APosteriori:
     run at the same times.  Models: none (les_type 0), Smagorinsky with the
     training's best constant (les_c^2 = c0), and the learned coefficient
     (les_type 4, Smagorinsky with c0 where the features leave the training
-    range).  The plain model is the judge: the network's errors are reported
-    next to it."""
+    range).  The plain model is the yardstick: the network's errors are
+    reported next to it."""
 
     def __init__(self, fine_flow, pairs, mlp, scaling, precision=None, refine=1):
         self.fine = fine_flow
