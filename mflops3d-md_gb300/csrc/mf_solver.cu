@@ -2569,6 +2569,22 @@ int mf_solve_3d_noalloc(mf_solver3d_t* sc, const double* rhs, double sigma, doub
   return MF_OK;
 }
 
+}  // extern "C"
+
+// The staging slots' graphs of mf_solve_3d_mixed_many were captured with the
+// set-up's device pointers and the launch parameters derived from it (the
+// null-mode projection of a closed operator, its rows and columns); new
+// tables can release or change those, so the graphs are captured again.
+static void drop_pipe_graphs(mf_solver3d* sc) {
+  for (auto& G : sc->pipe_graph)
+    if (G.exec) {
+      cudaGraphExecDestroy(G.exec);
+      G.exec = nullptr;
+    }
+}
+
+extern "C" {
+
 int mf_solver3d_set_eigen(mf_solver3d_t* sc, int axis, const double* eigen, const double* vect,
                           const double* inv_vect) {
   if (!sc || !eigen || !vect || !inv_vect || axis < 0 || axis > 2)
@@ -2595,6 +2611,7 @@ int mf_solver3d_set_eigen(mf_solver3d_t* sc, int axis, const double* eigen, cons
       Vi[(size_t)i * n + j] = ic[i + (size_t)n * j];
     }
   MF_CUDA(cudaDeviceSynchronize());
+  drop_pipe_graphs(sc);
   if ((rc = axis_set_eigen(d, e, V, Vi))) return rc;
   MF_CUDA(cudaDeviceSynchronize());  // uploads complete before use on any stream
   return MF_OK;

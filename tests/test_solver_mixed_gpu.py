@@ -227,6 +227,48 @@ def test_many_problems_equal_single_calls(mf, gpu, prec_name, refine):
         assert np.array_equal(one[edge], solf0[b][edge]), b
 
 
+def test_many_after_new_eigen_tables(mf, gpu):
+    """New eigen tables (mf_solver3d_set_eigen) between two
+    mf_solve_3d_mixed_many calls: the staging slots' graphs of the first call
+    are not replayed by the second.  All-Neumann operator at sigma = -10,
+    first with the oracle's tables (closed: one null eigenvalue per axis, so
+    FP64 residual passes), then with axis 0's null eigenvalue moved to 1e-3
+    (no longer closed: the residual passes store the operand directly); the
+    second call's problems must equal single eager calls with those tables."""
+    nall = (26, 22, 18)
+    gx, gy, gz = grids(*nall, kind="tanh")
+    n1, n2, n3 = (v - 2 for v in nall)
+    bct = (2,) * 6
+    sc_ref = S.Solver3D(gx, gy, gz, bct, 6)
+    sc = mf.SolverCoeffs3D(gx, gy, gz, bct, 6)
+    axes = (sc_ref.cx, sc_ref.cy, sc_ref.cz)
+    for a, ax in enumerate(axes):
+        sc.set_eigen(a, ax.eigen, ax.vect, ax.inv_vect)
+    prec, sigma, B = mf.MF_PREC_3XTF32, -10.0, 5
+    rhs = [field((n1, n2, n3), 140 + b) for b in range(B)]
+    bcs = [bc_arrays(n1, n2, n3, 150 + b) for b in range(B)]
+    solf0 = [field(nall, 160 + b) for b in range(B)]
+
+    def many():
+        outs = [np.asfortranarray(x.copy()) for x in solf0]
+        sc.solve_3d_many(rhs, sigma, outs, [b[0] for b in bcs], [b[1] for b in bcs], [b[2] for b in bcs],
+                         precision=prec, refine=1)
+        return outs
+
+    first = many()  # problems 1-3 capture the slots' graphs, 4 replays one
+    e0 = np.array(axes[0].eigen, dtype=np.float64)
+    k = int(np.argmin(np.abs(e0)))
+    assert abs(e0[k]) < 1e-8
+    e0[k] = 1e-3
+    sc.set_eigen(0, e0, axes[0].vect, axes[0].inv_vect)
+    second = many()
+    for b in range(B):
+        one = np.asfortranarray(solf0[b].copy())
+        sc.solve_3d(rhs[b], sigma, one, *bcs[b], precision=prec, refine=1)
+        assert np.array_equal(second[b], one), b
+    assert not np.array_equal(first[0], second[0])
+
+
 @pytest.mark.parametrize("prec_name,refine", [("MF_PREC_3XTF32", 1), ("MF_PREC_3XTF32", 2),
                                               ("MF_PREC_SPLIT_BF16", 2), ("MF_PREC_SPLIT_BF16", 3)])
 @pytest.mark.parametrize("sigma", [0.0, -10.0])
