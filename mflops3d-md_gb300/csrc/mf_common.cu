@@ -113,9 +113,9 @@ int stage_in(DevBuf& buf, const void* host, size_t bytes, cudaStream_t s) {
   return MF_OK;
 }
 
-void StageProfiler::begin(int kind, cudaStream_t st) {
+void StageProfiler::begin(int kind, cudaStream_t st, int count) {
   if (!on) return;
-  Rec r{kind, nullptr, nullptr};
+  Rec r{kind, nullptr, nullptr, count};
   cudaEventCreate(&r.a);
   cudaEventCreate(&r.b);
   cudaEventRecord(r.a, st);
@@ -132,7 +132,7 @@ void StageProfiler::collect() {
     float ms = 0.f;
     if (cudaEventSynchronize(r.b) == cudaSuccess && cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) {
       total_ms[r.kind] += ms;
-      launches[r.kind] += 1;
+      launches[r.kind] += r.count;
     }
     cudaEventDestroy(r.a);
     cudaEventDestroy(r.b);

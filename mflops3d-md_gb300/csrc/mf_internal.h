@@ -96,19 +96,22 @@ int solver_axis_view(const ::mf_solver3d* sc, int axis, SolverAxisView* out);
 int stage_in(DevBuf& buf, const void* host, size_t bytes, cudaStream_t s);
 
 // Optional per-kernel CUDA-event timers of a handle.  When enabled, every
-// launch of the handle is bracketed by an event pair on its stream; read()
-// synchronises on the recorded events and accumulates per-kind totals.
+// launch of the handle (or a short group of launches of one stage, whose
+// count begin() is given) is bracketed by an event pair on its stream;
+// collect() synchronises on the recorded events and accumulates per-kind
+// totals of time and launches.
 struct StageProfiler {
   static constexpr int kKinds = 12;
   bool on = false;
   struct Rec {
     int kind;
     cudaEvent_t a, b;
+    int count;  // kernel launches between a and b
   };
   std::vector<Rec> pending;
   double total_ms[kKinds] = {0};
   long long launches[kKinds] = {0};
-  void begin(int kind, cudaStream_t st);
+  void begin(int kind, cudaStream_t st, int count = 1);
   void end(cudaStream_t st);
   void collect();
   void reset();

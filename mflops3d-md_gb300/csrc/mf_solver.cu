@@ -1941,7 +1941,7 @@ static int fold_split(mf_solver3d* sc, bool tf32, const double* rhs, const doubl
   if ((rc = sc->foldf.ensure(sizeof(float) * 4 * (ps[0] + ps[1] + ps[2])))) return rc;
   float* f = sc->foldf.as<float>();
   float* fa[3] = {f, f + 4 * ps[0], f + 4 * (ps[0] + ps[1])};
-  sc->prof.begin(kProfFold, st);
+  sc->prof.begin(kProfFold, st, 4);  // three face-product launches and the fold
   for (int a = 0; a < 3; ++a) {
     const AxisDev& d = sc->ax[a];
     const long long r = a == 0 ? n2 : nf[a], rp = a == 0 ? bxp : nf[a];
@@ -2006,7 +2006,7 @@ static int null_project(mf_solver3d* sc, const double* r, bool project, __nv_bfl
   const double* coef = nullptr;
   float* r32 = nullptr;
   int rc;
-  sc->prof.begin(kProfNull, st);
+  sc->prof.begin(kProfNull, st, project ? 3 : 1);  // null_coef launches two kernels
   if (project && (rc = null_coef<T>(sc, r, n1, (long long)n1 * n2, &coef, st))) return rc;
   k_null_split<T><<<dim3(blocks_for(n1, 256), n2, std::min(n3, 16)), 256, 0, st>>>(
       r, coef, sc->ax[0].null_col.as<double>(), sc->ax[1].null_col.as<double>(),
@@ -2023,7 +2023,7 @@ static int null_remove(mf_solver3d* sc, double* solf, cudaStream_t st) {
   double* u = solf + 1 + sy + sz;
   const double* coef = nullptr;
   int rc;
-  sc->prof.begin(kProfNull, st);
+  sc->prof.begin(kProfNull, st, 3);
   if ((rc = null_coef<double>(sc, u, sy, sz, &coef, st))) return rc;
   k_null_remove<<<dim3(blocks_for(n1, 256), n2, std::min(n3, 16)), 256, 0, st>>>(
       u, sy, sz, coef, sc->ax[0].null_col.as<double>(), sc->ax[1].null_col.as<double>(),
