@@ -247,8 +247,8 @@ int mf_solve_3d_mixed(mf_solver3d_t* sc, const double* rhs, double sigma, double
  * slots).  In the mixed modes every problem after the first of a call is
  * one replay of its slot's CUDA graph, captured on first use and again
  * when sigma, the precision, the refinement count, the transform plan, the
- * tuner mode or the residual form change (not while the per-kernel timers
- * of mf_solver3d_profile are on).  Each problem's result equals that of a
+ * tuner mode or the residual form change, or after mf_solver3d_set_eigen
+ * (not while the per-kernel timers of mf_solver3d_profile are on).  Each problem's result equals that of a
  * single call; the call returns when every result is in place.  No
  * reference counterpart (the reference solves one right-hand side per
  * call). */
@@ -287,9 +287,10 @@ int mf_solver3d_device_status(mf_solver3d_t* sc);
  * spirit of the reference's cpu_time/MPI_WTIME stage prints,
  * class_solver_3d.f90:106-259, class_field.f90:1317-1386).  profile(sc,1)
  * resets and enables, profile(sc,0) disables.  profile_read syncs and
- * returns the accumulated time and launch count of one kernel kind:
+ * returns the accumulated time and kernel launch count of one stage:
  * 0 tensor-core transform (split store), 1 residual x pass, 2 residual y/z passes,
- * 3 FP64->split-BF16 conversion, 4 boundary fold, 5 boundary faces,
+ * 3 FP64 residual narrowed to the operand (with the null-mode projection
+ * of closed operators), 4 boundary fold (with its face products), 5 boundary faces,
  * 6 FP64 transform, 7 interior copy, 8 tensor-core transform with the
  * eigenvalue divide, 9 tensor-core transform updating the FP64 solution,
  * 10 FP32 correction residual. */
