@@ -2380,83 +2380,95 @@ int mf_solve_3d_mixed_many(mf_solver3d_t* sc, int count, const double* const* rh
     for (int a = 0; a < 3; ++a)
       if ((rc = sc->pipe_bc[q][a].ensure(bb[a]))) return rc;
   }
-  // the copy streams start after the work already queued on the caller's stream
-  MF_CUDA(cudaEventRecord(sc->solved[0], st));
-  MF_CUDA(cudaStreamWaitEvent(sc->cin, sc->solved[0], 0));
-  const double* const* bsrc[3] = {bcx, bcy, bcz};
-  for (int b = 0; b < count; ++b) {
-    const int q = b % kPipeSlots;
-    if (b >= kPipeSlots) {  // slot q is free once problem b - kPipeSlots is solved and downloaded
-      MF_CUDA(cudaStreamWaitEvent(sc->cin, sc->solved[q], 0));
-      MF_CUDA(cudaStreamWaitEvent(sc->cin, sc->out_done[q], 0));
-    }
-    MF_CUDA(cudaMemcpyAsync(sc->pipe_rhs[q].ptr, rhs[b], rb, cudaMemcpyDefault, sc->cin));
-    if (is_device_ptr(solf[b])) {
-      MF_CUDA(cudaMemcpyAsync(sc->pipe_solf[q].ptr, solf[b], sb, cudaMemcpyDefault, sc->cin));
-    } else if ((rc = stage_edges(sc->pipe_solf[q], solf[b], n1 + 2, n2 + 2, n3 + 2, sc->cin))) {
-      return rc;
-    }
-    const double* bcs[3];
-    for (int a = 0; a < 3; ++a) {
-      MF_CUDA(cudaMemcpyAsync(sc->pipe_bc[q][a].ptr, bsrc[a][b], bb[a], cudaMemcpyDefault, sc->cin));
-      bcs[a] = sc->pipe_bc[q][a].as<double>();
-    }
-    MF_CUDA(cudaEventRecord(sc->in_ready[q], sc->cin));
-    MF_CUDA(cudaStreamWaitEvent(st, sc->in_ready[q], 0));
-    double* s = sc->pipe_solf[q].as<double>();
-    if (precision != MF_PREC_FP64 && b > 0 && !sc->prof.on) {
-      // Mixed solves after the first of the call (which has made every
-      // buffer and plan these settings need) replay the slot's graph,
-      // captured on first use or when a setting changed; a capture that
-      // fails leaves the eager launches below to do the work.
-      mf_solver3d::PipeGraph& G = sc->pipe_graph[q];
-      const int plan = tc_get_tf32_plan(), tmode = tune_mode();
-      if (!G.exec || G.sigma != sigma || G.precision != precision || G.refine != refine || G.plan != plan ||
-          G.tune != tmode || G.resid != sc->resid_mode) {
-        if (G.exec) {
-          MF_CUDA(cudaGraphExecDestroy(G.exec));
-          G.exec = nullptr;
-        }
-        if (!sc->gcap) MF_CUDA(cudaStreamCreateWithFlags(&sc->gcap, cudaStreamNonBlocking));
-        if (cudaStreamBeginCapture(sc->gcap, cudaStreamCaptureModeRelaxed) == cudaSuccess) {
-          const int crc = solve_mixed_dev(sc, sc->pipe_rhs[q].as<double>(), sigma, s, bcs, precision, refine,
-                                          sc->gcap);
-          cudaGraph_t graph = nullptr;
-          const cudaError_t e = cudaStreamEndCapture(sc->gcap, &graph);
-          if (crc == MF_OK && e == cudaSuccess && graph &&
-              cudaGraphInstantiate(&G.exec, graph, 0) == cudaSuccess) {
-            G.sigma = sigma;
-            G.precision = precision;
-            G.refine = refine;
-            G.plan = plan;
-            G.tune = tmode;
-            G.resid = sc->resid_mode;
-          } else {
+  // Every copy and solve of the call is queued by `queue`; if it fails part
+  // way, the copies already queued (downloads into the caller's arrays
+  // among them) are waited for before the error is returned.
+  auto queue = [&]() -> int {
+    // the copy streams start after the work already queued on the caller's stream
+    MF_CUDA(cudaEventRecord(sc->solved[0], st));
+    MF_CUDA(cudaStreamWaitEvent(sc->cin, sc->solved[0], 0));
+    const double* const* bsrc[3] = {bcx, bcy, bcz};
+    for (int b = 0; b < count; ++b) {
+      const int q = b % kPipeSlots;
+      if (b >= kPipeSlots) {  // slot q is free once problem b - kPipeSlots is solved and downloaded
+        MF_CUDA(cudaStreamWaitEvent(sc->cin, sc->solved[q], 0));
+        MF_CUDA(cudaStreamWaitEvent(sc->cin, sc->out_done[q], 0));
+      }
+      MF_CUDA(cudaMemcpyAsync(sc->pipe_rhs[q].ptr, rhs[b], rb, cudaMemcpyDefault, sc->cin));
+      if (is_device_ptr(solf[b])) {
+        MF_CUDA(cudaMemcpyAsync(sc->pipe_solf[q].ptr, solf[b], sb, cudaMemcpyDefault, sc->cin));
+      } else if ((rc = stage_edges(sc->pipe_solf[q], solf[b], n1 + 2, n2 + 2, n3 + 2, sc->cin))) {
+        return rc;
+      }
+      const double* bcs[3];
+      for (int a = 0; a < 3; ++a) {
+        MF_CUDA(cudaMemcpyAsync(sc->pipe_bc[q][a].ptr, bsrc[a][b], bb[a], cudaMemcpyDefault, sc->cin));
+        bcs[a] = sc->pipe_bc[q][a].as<double>();
+      }
+      MF_CUDA(cudaEventRecord(sc->in_ready[q], sc->cin));
+      MF_CUDA(cudaStreamWaitEvent(st, sc->in_ready[q], 0));
+      double* s = sc->pipe_solf[q].as<double>();
+      if (precision != MF_PREC_FP64 && b > 0 && !sc->prof.on) {
+        // Mixed solves after the first of the call (which has made every
+        // buffer and plan these settings need) replay the slot's graph,
+        // captured on first use or when a setting changed; a capture that
+        // fails leaves the eager launches below to do the work.
+        mf_solver3d::PipeGraph& G = sc->pipe_graph[q];
+        const int plan = tc_get_tf32_plan(), tmode = tune_mode();
+        if (!G.exec || G.sigma != sigma || G.precision != precision || G.refine != refine || G.plan != plan ||
+            G.tune != tmode || G.resid != sc->resid_mode) {
+          if (G.exec) {
+            MF_CUDA(cudaGraphExecDestroy(G.exec));
             G.exec = nullptr;
           }
-          if (graph) cudaGraphDestroy(graph);
-          (void)cudaGetLastError();
-        } else {
-          (void)cudaGetLastError();
+          if (!sc->gcap) MF_CUDA(cudaStreamCreateWithFlags(&sc->gcap, cudaStreamNonBlocking));
+          if (cudaStreamBeginCapture(sc->gcap, cudaStreamCaptureModeRelaxed) == cudaSuccess) {
+            const int crc = solve_mixed_dev(sc, sc->pipe_rhs[q].as<double>(), sigma, s, bcs, precision, refine,
+                                            sc->gcap);
+            cudaGraph_t graph = nullptr;
+            const cudaError_t e = cudaStreamEndCapture(sc->gcap, &graph);
+            if (crc == MF_OK && e == cudaSuccess && graph &&
+                cudaGraphInstantiate(&G.exec, graph, 0) == cudaSuccess) {
+              G.sigma = sigma;
+              G.precision = precision;
+              G.refine = refine;
+              G.plan = plan;
+              G.tune = tmode;
+              G.resid = sc->resid_mode;
+            } else {
+              G.exec = nullptr;
+            }
+            if (graph) cudaGraphDestroy(graph);
+            (void)cudaGetLastError();
+          } else {
+            (void)cudaGetLastError();
+          }
+        }
+        if (G.exec) {
+          MF_CUDA(cudaGraphLaunch(G.exec, st));
+          MF_CUDA(cudaEventRecord(sc->solved[q], st));
+          MF_CUDA(cudaStreamWaitEvent(sc->cout, sc->solved[q], 0));
+          MF_CUDA(cudaMemcpyAsync(solf[b], s, sb, cudaMemcpyDefault, sc->cout));
+          MF_CUDA(cudaEventRecord(sc->out_done[q], sc->cout));
+          continue;
         }
       }
-      if (G.exec) {
-        MF_CUDA(cudaGraphLaunch(G.exec, st));
-        MF_CUDA(cudaEventRecord(sc->solved[q], st));
-        MF_CUDA(cudaStreamWaitEvent(sc->cout, sc->solved[q], 0));
-        MF_CUDA(cudaMemcpyAsync(solf[b], s, sb, cudaMemcpyDefault, sc->cout));
-        MF_CUDA(cudaEventRecord(sc->out_done[q], sc->cout));
-        continue;
-      }
+      rc = precision == MF_PREC_FP64
+               ? solve_plain_dev(sc, sc->pipe_rhs[q].as<double>(), sigma, s, bcs, st)
+               : solve_mixed_dev(sc, sc->pipe_rhs[q].as<double>(), sigma, s, bcs, precision, refine, st);
+      if (rc) return rc;
+      MF_CUDA(cudaEventRecord(sc->solved[q], st));
+      MF_CUDA(cudaStreamWaitEvent(sc->cout, sc->solved[q], 0));
+      MF_CUDA(cudaMemcpyAsync(solf[b], s, sb, cudaMemcpyDefault, sc->cout));
+      MF_CUDA(cudaEventRecord(sc->out_done[q], sc->cout));
     }
-    rc = precision == MF_PREC_FP64
-             ? solve_plain_dev(sc, sc->pipe_rhs[q].as<double>(), sigma, s, bcs, st)
-             : solve_mixed_dev(sc, sc->pipe_rhs[q].as<double>(), sigma, s, bcs, precision, refine, st);
-    if (rc) return rc;
-    MF_CUDA(cudaEventRecord(sc->solved[q], st));
-    MF_CUDA(cudaStreamWaitEvent(sc->cout, sc->solved[q], 0));
-    MF_CUDA(cudaMemcpyAsync(solf[b], s, sb, cudaMemcpyDefault, sc->cout));
-    MF_CUDA(cudaEventRecord(sc->out_done[q], sc->cout));
+    return MF_OK;
+  };
+  if ((rc = queue())) {
+    cudaStreamSynchronize(sc->cin);
+    cudaStreamSynchronize(sc->cout);
+    cudaStreamSynchronize(st);
+    return rc;
   }
   MF_CUDA(cudaStreamSynchronize(sc->cout));
   MF_CUDA(cudaStreamSynchronize(st));
