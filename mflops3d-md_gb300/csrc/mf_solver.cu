@@ -2271,32 +2271,43 @@ static int solve_front(mf_solver3d_t* sc, const double* rhs, double* solf, const
   const size_t bb[3] = {(size_t)n2 * n3 * 2 * 8, (size_t)n1 * n3 * 2 * 8, (size_t)n1 * n2 * 2 * 8};
   const double* bcs_in[3] = {bcx, bcy, bcz};
   const double* bcs[3];
-  int rc;
   bool any_host = false;
-  for (int a = 0; a < 3; ++a) {
-    if (is_device_ptr(bcs_in[a])) {
-      bcs[a] = bcs_in[a];
-    } else {
-      if ((rc = stage_in(sc->st_bc[a], bcs_in[a], bb[a], st))) return rc;
-      bcs[a] = sc->st_bc[a].as<double>();
-      any_host = true;
+  // Staging, solve and download; on an error part way, the copies already
+  // queued from or to the caller's host arrays are waited for before the
+  // error is returned.
+  auto run = [&]() -> int {
+    int rc;
+    for (int a = 0; a < 3; ++a) {
+      if (is_device_ptr(bcs_in[a])) {
+        bcs[a] = bcs_in[a];
+      } else {
+        any_host = true;
+        if ((rc = stage_in(sc->st_bc[a], bcs_in[a], bb[a], st))) return rc;
+        bcs[a] = sc->st_bc[a].as<double>();
+      }
     }
+    const double* r = rhs;
+    if (!is_device_ptr(rhs)) {
+      any_host = true;
+      if ((rc = stage_in(sc->st_rhs, rhs, rb, st))) return rc;
+      r = sc->st_rhs.as<double>();
+    }
+    double* s = solf;
+    const bool host_solf = !is_device_ptr(solf);
+    if (host_solf) {
+      any_host = true;
+      if ((rc = stage_edges(sc->st_solf, solf, n1 + 2, n2 + 2, n3 + 2, st))) return rc;
+      s = sc->st_solf.as<double>();
+    }
+    if ((rc = body(r, s, bcs, st))) return rc;
+    if (host_solf) MF_CUDA(cudaMemcpyAsync(solf, s, sb, cudaMemcpyDeviceToHost, st));
+    return MF_OK;
+  };
+  const int rc = run();
+  if (rc) {
+    if (any_host) cudaStreamSynchronize(st);
+    return rc;
   }
-  const double* r = rhs;
-  if (!is_device_ptr(rhs)) {
-    if ((rc = stage_in(sc->st_rhs, rhs, rb, st))) return rc;
-    r = sc->st_rhs.as<double>();
-    any_host = true;
-  }
-  double* s = solf;
-  const bool host_solf = !is_device_ptr(solf);
-  if (host_solf) {
-    if ((rc = stage_edges(sc->st_solf, solf, n1 + 2, n2 + 2, n3 + 2, st))) return rc;
-    s = sc->st_solf.as<double>();
-    any_host = true;
-  }
-  if ((rc = body(r, s, bcs, st))) return rc;
-  if (host_solf) MF_CUDA(cudaMemcpyAsync(solf, s, sb, cudaMemcpyDeviceToHost, st));
   if (any_host) {
     MF_CUDA(cudaStreamSynchronize(st));
     if (sc->err.ptr) {
