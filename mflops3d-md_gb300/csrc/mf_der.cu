@@ -418,6 +418,8 @@ int mf_der_apply(const mf_der_t* dc_c, int axis, int order, const double* f, dou
   // host pointers: stage through the handle's buffers
   const double* fin = f;
   int rc;
+  HostCopyWait wait(st);
+  wait.armed = true;
   if (!dev_in) {
     if ((rc = stage_in(dc->stage_in_buf, f, bytes, st))) return rc;
     fin = dc->stage_in_buf.as<double>();
@@ -466,6 +468,8 @@ int mf_der_lines(const mf_der_t* dc_c, int order, int solver_variant, const doub
   const double* fin = x;
   double* dout = dx;
   int rc;
+  HostCopyWait wait(st);
+  wait.armed = !dev_in || !dev_out;
   if (!dev_in) {
     if ((rc = stage_in(dc->stage_in_buf, x, bytes, st))) return rc;
     fin = dc->stage_in_buf.as<double>();

@@ -608,6 +608,8 @@ int mf_filter_apply(const mf_filter_t* fc, int axis, int deriv, const double* in
   const double* din = in;
   double* dout = out;
   int rc;
+  HostCopyWait wait(st);
+  wait.armed = !dev_in || !dev_out;
   if (!dev_in) {
     if ((rc = stage_in(f->st_in, in, in_bytes, st))) return rc;
     din = f->st_in.as<double>();

@@ -95,6 +95,18 @@ int solver_axis_view(const ::mf_solver3d* sc, int axis, SolverAxisView* out);
 // Copies host -> device buffer (growing it) on stream; returns MF_OK or error.
 int stage_in(DevBuf& buf, const void* host, size_t bytes, cudaStream_t s);
 
+// Waits on a stream when it goes out of scope armed: an entry point that
+// has queued copies from or to the caller's host arrays returns, on an
+// error too, only after they are done.
+struct HostCopyWait {
+  cudaStream_t st;
+  bool armed = false;
+  explicit HostCopyWait(cudaStream_t s) : st(s) {}
+  ~HostCopyWait() {
+    if (armed) cudaStreamSynchronize(st);
+  }
+};
+
 // Optional per-kernel CUDA-event timers of a handle.  When enabled, every
 // launch of the handle (or a short group of launches of one stage, whose
 // count begin() is given) is bracketed by an event pair on its stream;
