@@ -298,3 +298,37 @@ def test_mixed_pure_neumann_pressure(mf, gpu, prec_name, refine, sigma):
     err, full = rel_l2(g - g.mean(), r - r.mean()), rel_l2(g, r)
     print("all-Neumann sigma %g %s refine %d: mean-free %.3e whole %.3e" % (sigma, prec_name, refine, err, full))
     assert err < 1e-10 and full < 1e-10
+
+
+def test_error_after_staging_pinned_arrays(mf, gpu):
+    """A solve refused after the caller's (pinned) host arrays were staged
+    -- an unknown precision, checked by the solve itself -- returns its
+    error only after the queued copies are done; the handle then solves
+    normally, single and pipelined, with the same arrays."""
+    import torch
+    nall = (22, 20, 18)
+    gx, gy, gz = grids(*nall, kind="tanh")
+    n1, n2, n3 = (v - 2 for v in nall)
+    sc = mf.SolverCoeffs3D(gx, gy, gz, (1,) * 6, 6)
+
+    def pinned(a):
+        t = torch.empty(a.size, dtype=torch.float64, pin_memory=True).numpy().reshape(a.shape, order="F")
+        t[...] = a
+        return t
+
+    rhs = pinned(field((n1, n2, n3), 170))
+    bcs = [pinned(b) for b in bc_arrays(n1, n2, n3, 171)]
+    solf0 = field(nall, 172)
+    out = pinned(solf0)
+    with pytest.raises(mf.MflopsError) as e:
+        sc.solve_3d(rhs, -2.0, out, *bcs, precision=99, refine=1)
+    assert e.value.code == mf.MF_ERR_UNSUPPORTED
+    with pytest.raises(mf.MflopsError):
+        sc.solve_3d_many([rhs, rhs], -2.0, [out, out], [bcs[0]] * 2, [bcs[1]] * 2, [bcs[2]] * 2,
+                         precision=99, refine=1)
+    assert np.array_equal(out, solf0)  # nothing was written back
+    sc.solve_3d(rhs, -2.0, out, *bcs, precision=mf.MF_PREC_3XTF32, refine=1)
+    ref = np.asfortranarray(solf0.copy())
+    mf.SolverCoeffs3D(gx, gy, gz, (1,) * 6, 6).solve_3d(np.array(rhs), -2.0, ref, *[np.array(b) for b in bcs],
+                                                         precision=mf.MF_PREC_3XTF32, refine=1)
+    assert np.array_equal(out, ref)
